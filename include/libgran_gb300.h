@@ -1,0 +1,247 @@
+/*
+ * libgran_gb300.h -- C ABI of the GB300 (sm_103a) DEM pair-force + integration engine.
+ *
+ * This is the drop-in boundary for libgran's hot path: a granular_system stepped by a rotational
+ * velocity-Verlet integrator over binary pair-force functors (frictional contact, sintered bond,
+ * breaking sintered bond, Hamaker van der Waals) and unary triangular-facet surface functors.
+ * libgran itself is a header-only C++ template library without any FFI; the entry points below are
+ * what its templates bind to when they are re-targeted at the GPU (see the headers in include/libgran_gb300/,
+ * which keep libgran's class names and constructor signatures and call into this ABI).
+ *
+ * Conventions
+ *   - Every function returns an int status: LG_OK (0) on success, a negative LG_E* code otherwise.
+ *     lg_last_error() returns a human readable description of the last failure on this thread.
+ *     No C++ exception crosses this boundary.
+ *   - A handle owns all of its device memory and one CUDA stream. A handle is not thread safe;
+ *     distinct handles are independent. Vectors cross the ABI as AoS double[3*n] host arrays.
+ *   - Host pointers are plain pages or pinned pages; nothing here keeps a host pointer after return.
+ *
+ * Reference citations use paths inside the libgran project (egor-demidov/libgran).
+ */
+#ifndef LIBGRAN_GB300_H
+#define LIBGRAN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------- */
+#define LG_OK 0
+#define LG_E_INVALID (-1)   /* bad argument (null pointer, size out of range, unknown enum) */
+#define LG_E_CUDA (-2)      /* a CUDA runtime call failed */
+#define LG_E_NOMEM (-3)     /* device or host allocation failed, or a budget was exceeded */
+#define LG_E_STATE (-4)     /* call not valid in the handle's current state */
+#define LG_E_DEVICE (-5)    /* a kernel reported an error word (capacity overflow, non-finite) */
+
+/* ---- model selectors ---------------------------------------------------------------------- */
+/* Which binary functor sits in the binary_force_functor_container (binary_force_container.h:14-35).
+ * SINTER and BREAKING_SINTER embed their own copy of a contact_force_functor for non-bonded pairs
+ * (alt_sinter_bridge.h:36,100-101; alt_breaking_sinter_bridge.h:35,86-87). */
+#define LG_BINARY_NONE 0
+#define LG_BINARY_CONTACT 1          /* contact_force_functor, contact_force/contact_force.h:8-157 */
+#define LG_BINARY_SINTER 2           /* alt_sinter_functor, sinter_bridge/alt_sinter_bridge.h:17-180 */
+#define LG_BINARY_BREAKING_SINTER 3  /* alt_breaking_sinter_functor, alt_breaking_sinter_bridge.h:16-166 */
+
+/* Which Hamaker functor (if any) is folded in after the binary functor. */
+#define LG_HAMAKER_NONE 0
+#define LG_HAMAKER_FULL 1        /* hamaker_functor, hamaker_force/hamaker_force.h:18-48 */
+#define LG_HAMAKER_LIMITED 2     /* limited_range_hamaker_functor, limited_range_hamaker_force.h:18-52 */
+#define LG_HAMAKER_SIMPLIFIED 3  /* simplified_hamaker_functor, simplified_hamaker_force.h:8-34 */
+
+/* Neck strength lookup of the breaking sintered bond. The reference stores strengths at particle
+ * indices (alt_breaking_sinter_bridge.h:71-73) and reads them at pair indices (:118), so in the
+ * reference nearly every bond reads strength 0. PER_BOND gives each bond its own strength (the
+ * evident intent); REFERENCE_INDEXING reproduces the reference's lookup bit for bit. */
+#define LG_NECK_PER_BOND 0
+#define LG_NECK_REFERENCE_INDEXING 1
+
+/* Arithmetic of the pair kernel. */
+#define LG_PRECISION_FP64 0   /* every operation in FP64 */
+#define LG_PRECISION_MIXED 1  /* FP64 separation, overlap, springs, sums, integration; FP32 rest */
+
+/* Pair enumeration. */
+#define LG_PAIRS_ALL 0        /* all ordered pairs j != i (granular_system, granular_system.h:25-86) */
+#define LG_PAIRS_VERLET 1     /* Verlet list of radius r_verlet (granular_system_neighbor_list.h:54-64) */
+
+/* ---- functor parameter blocks (same order as the reference constructors) ------------------- */
+
+/* contact_force_functor(n_part, k, gamma_n, k_t, gamma_t, mu_s, phi_d, k_r, gamma_r, mu_r, phi_r,
+ *                       k_o, gamma_o, mu_o, phi_o, r_part, mass, inertia, dt, ...)
+ * contact_force/contact_force.h:10-30; surface_contact_force_functor has the same list,
+ * contact_force/surface_contact_force.h:10-30. */
+typedef struct lg_contact_params {
+    double k, gamma_n;
+    double k_t, gamma_t, mu_s, phi_d;
+    double k_r, gamma_r, mu_r, phi_r;
+    double k_o, gamma_o, mu_o, phi_o;
+    double r_part, mass, inertia, dt;
+} lg_contact_params;
+
+/* alt_sinter_functor(n_part, x0, k, gamma_n, k_t, gamma_t, k_r, gamma_r, k_o, gamma_o,
+ *                    r_part, mass, inertia, dt, ..., critical_separation, contact_force)
+ * sinter_bridge/alt_sinter_bridge.h:19-36 (alt_breaking_sinter_bridge.h:17-35 adds the neck
+ * strength distribution, passed to lg_create as an array). */
+typedef struct lg_sinter_params {
+    double k, gamma_n, k_t, gamma_t, k_r, gamma_r, k_o, gamma_o;
+    double r_part, mass, inertia, dt;
+    double critical_separation;
+} lg_sinter_params;
+
+/* hamaker_functor(A, h0, r_part, mass, ...)                hamaker_force.h:20-26
+ * limited_range_hamaker_functor(A, h0, r_cutoff, r_part, mass, ...) limited_range_hamaker_force.h:20-27
+ * simplified_hamaker_functor(A, h0, r_part, mass, ...)     simplified_hamaker_force.h:10-16
+ * surface_hamaker_functor(A, h0, r_part, mass, ...)        surface_hamaker_force.h:10-15 */
+typedef struct lg_hamaker_params {
+    double A, h0, r_cutoff, r_part, mass;
+} lg_hamaker_params;
+
+/* triangular_facet(v_facet, {v0, v1, v2}, surface functors...), triangular_facet.h:18-19, with an
+ * optional surface_contact_force_functor and an optional surface_hamaker_functor folded in that
+ * order (triangular_facet.h:32-51). */
+typedef struct lg_facet_desc {
+    double v_facet[3];
+    double vertices[9];
+    int32_t has_contact;
+    int32_t has_hamaker;
+    lg_contact_params contact;
+    lg_hamaker_params hamaker;
+} lg_facet_desc;
+
+/* Everything the granular_system constructor and its functor list fix at compile/construct time
+ * (granular_system.h:53-63; granular_system_neighbor_list.h:54-64 adds n_part and r_verlet). */
+typedef struct lg_system_desc {
+    int64_t n_part;
+    int32_t binary_model;    /* LG_BINARY_* */
+    int32_t hamaker_model;   /* LG_HAMAKER_* */
+    lg_contact_params contact;  /* contact functor, or the sintered functor's inner contact copy */
+    lg_sinter_params sinter;    /* used by LG_BINARY_SINTER / LG_BINARY_BREAKING_SINTER */
+    lg_hamaker_params hamaker;  /* used unless hamaker_model == LG_HAMAKER_NONE */
+    int32_t neck_mode;       /* LG_NECK_* */
+    int32_t pairs;           /* LG_PAIRS_* */
+    double r_verlet;         /* list radius (centre distance) for LG_PAIRS_VERLET */
+    int32_t precision;       /* LG_PRECISION_* */
+    int32_t n_facets;        /* number of lg_facet_desc passed to lg_create */
+    int32_t facet_auto_move; /* 1: move every facet by v_facet*dt after each step */
+    int32_t max_neighbors;   /* Verlet list row capacity; 0 picks a default */
+} lg_system_desc;
+
+/* Fields that lg_get / lg_set move. */
+#define LG_FIELD_X 0       /* positions            get_x()     Granular-system.md:84-120 */
+#define LG_FIELD_V 1       /* velocities           get_v() */
+#define LG_FIELD_THETA 2   /* orientations         get_theta() */
+#define LG_FIELD_OMEGA 3   /* angular velocities   get_omega() */
+#define LG_FIELD_A 4       /* translational acceleration buffer of the last force evaluation */
+#define LG_FIELD_ALPHA 5   /* angular acceleration buffer of the last force evaluation */
+
+/* Observables of test/compute_energy.cpp:7-58 and test/mass_distribution.cpp:7-27, plus the
+ * potential energy bookkeeping that the reference lacks (spring and Hamaker potentials). */
+typedef struct lg_observables {
+    double ke_translational, ke_rotational, ke_total;
+    double linear_momentum;   /* |sum m v| */
+    double angular_momentum;  /* |sum I w + x x m v| */
+    double center_of_mass[3];
+    double radius_of_gyration;
+    double potential_energy;  /* normal springs + tangential springs + Hamaker */
+    int64_t n_contacts;       /* ordered pairs with positive overlap (non-bonded) */
+    int64_t n_bonds;          /* ordered bonded pairs still intact */
+    int64_t n_bonds_initial;  /* ordered bonded pairs at construction */
+} lg_observables;
+
+typedef struct lg_system lg_system; /* opaque */
+
+/* Build version string, e.g. "libgran_gb300 0.1 sm_103a". Never fails. */
+const char *lg_version(void);
+
+/* Description of the last error raised on the calling thread ("" if none). */
+const char *lg_last_error(void);
+
+/* Number of CUDA devices visible (0 without a GPU). Returns LG_OK or LG_E_CUDA. */
+int lg_device_count(int *count);
+
+/* Construct a system: granular_system ctor (granular_system.h:53-63) together with the functor
+ * constructors, including the bond detection of alt_sinter_functor (alt_sinter_bridge.h:55-89,
+ * cycle-free) or alt_breaking_sinter_functor (alt_breaking_sinter_bridge.h:37-77).
+ * x0, v0, theta0, omega0: double[3*n]. facets: n_facets descriptors (may be NULL if 0).
+ * neck_strengths: one value per bond in detection order (i ascending, then j > i ascending), as the
+ * reference draws them from its distribution (alt_breaking_sinter_bridge.h:70); only read for
+ * LG_BINARY_BREAKING_SINTER; n_neck_strengths must equal the number of bonds found, or be 0 to
+ * mean "no strength" (+infinity). The initial accelerations are evaluated here, as the integrator's
+ * first half kick needs them. */
+int lg_create(const lg_system_desc *desc, const double *x0, const double *v0, const double *theta0,
+              const double *omega0, const lg_facet_desc *facets, const double *neck_strengths,
+              int64_t n_neck_strengths, int device, lg_system **out);
+
+/* Release every resource of the handle. NULL is accepted. */
+int lg_destroy(lg_system *sys);
+
+/* Advance nsteps steps of size dt: nsteps x do_step(dt) (Granular-system.md:65-80), each a
+ * rotational velocity-Verlet step with one force evaluation. With LG_PAIRS_VERLET and
+ * rebuild_every > 0, the Verlet list is rebuilt before every step whose global step index is a
+ * multiple of rebuild_every (test/hamaker_neighbor.cpp:121-122 uses 20). Asynchronous with respect
+ * to the host; errors from the device surface at the next synchronising call. */
+int lg_step(lg_system *sys, double dt, int64_t nsteps, int64_t rebuild_every);
+
+/* Rebuild the Verlet list now: update_neighbor_list() (test/hamaker_neighbor.cpp:122). Spring
+ * history of pairs present before and after is carried over. */
+int lg_update_neighbor_list(lg_system *sys);
+
+/* Copy a field to/from the host (double[3*n]). lg_get synchronises the handle's stream. */
+int lg_get(lg_system *sys, int field, double *out);
+int lg_set(lg_system *sys, int field, const double *in);
+
+/* reset_acceleration_buffers() (Granular-system.md:228-244): zero a and alpha. */
+int lg_reset_acceleration_buffers(lg_system *sys);
+
+/* Reductions on the device: observables of test/compute_energy.cpp and test/mass_distribution.cpp. */
+int lg_get_observables(lg_system *sys, lg_observables *out);
+
+/* Device error word (bit set of LG_DEVERR_*) accumulated since creation; synchronises. */
+#define LG_DEVERR_LIST_OVERFLOW 1    /* a Verlet list row exceeded its capacity */
+#define LG_DEVERR_NONFINITE 2        /* a non-finite acceleration was produced */
+#define LG_DEVERR_BOND_LOST 4        /* a bonded pair fell out of the Verlet list */
+int lg_get_device_errors(lg_system *sys, int32_t *errors);
+
+/* Bond bookkeeping of the sintered functors.
+ * lg_get_bonds: number of ordered bonded pairs still intact, and optionally (i, j) of each, sorted
+ * (the nonzero entries of bonded_contacts, alt_sinter_bridge.h:163). out_pairs may be NULL;
+ * capacity is the number of int64 pairs it can hold. */
+int lg_get_bonds(lg_system *sys, int64_t *n_bonds, int64_t *out_pairs, int64_t capacity);
+
+/* Spring state of an ordered pair (i, j): 9 doubles (xi_t, xi_r, xi_o), the tuple of
+ * contact_force_functor::contact_springs[i*n+j] (contact_force.h:156) for non-bonded pairs and of
+ * alt_sinter_functor::get_contact_springs()[i*n+j] (alt_sinter_bridge.h:159-161) for bonded pairs.
+ * Pairs not tracked (outside the Verlet list) report zeros. */
+int lg_get_pair_springs(lg_system *sys, int64_t i, int64_t j, double *out9);
+
+/* Facet control: triangular_facet::update_positions(dt) (triangular_facet.h:62-66) and the current
+ * vertices (get_vertices(), triangular_facet.h:57-59). */
+int lg_facet_update_positions(lg_system *sys, int32_t facet, double dt);
+int lg_facet_get_vertices(lg_system *sys, int32_t facet, double *out9);
+
+/* Number of CUDA kernel launches issued by this handle since creation (diagnostics). */
+int lg_get_launch_count(lg_system *sys, int64_t *count);
+
+/* Lanes per row group of the force kernel: 1 walks each row sequentially (the reference's summation
+ * order), 2..32 split a row across lanes and combine the partial sums with a fixed butterfly
+ * (deterministic, different rounding). 0 restores the automatic choice. */
+int lg_set_threads_per_row(lg_system *sys, int32_t threads_per_row);
+
+/* Seeded synthetic aggregate: random sequential attachment of n spheres of radius r (each new sphere
+ * touches a uniformly chosen existing one in a uniformly random direction; a candidate that overlaps
+ * any other sphere by more than 1e-12 r is rejected). x: double[3n]. Host-only, no GPU needed. */
+int lg_generate_rsa_aggregate(uint64_t seed, int64_t n, double r, double *x);
+
+/* Uniform random velocity components in [-vmax, vmax] from a seeded stream. Host-only. */
+int lg_generate_velocities(uint64_t seed, int64_t n, double vmax, double *v);
+
+/* Time `nsteps` steps with CUDA events on the handle's stream (no host copies inside); ms_out
+ * receives the elapsed device time. Same semantics as lg_step. */
+int lg_step_timed(lg_system *sys, double dt, int64_t nsteps, int64_t rebuild_every, float *ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIBGRAN_GB300_H */

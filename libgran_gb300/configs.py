@@ -1,0 +1,102 @@
+"""Parameter presets: the material constants libgran's drivers use and the seeded synthetic
+aggregate workloads (r = 14 nm soot monomers, density 1700 kg/m^3).
+
+Reference: the constants of test/contact.cpp:37-51 (rho, r_part, mass, inertia, k, gamma_n, mu, phi,
+mu_o, gamma_t, gamma_r, gamma_o) and the functor argument order of contact_force.h:10-30.
+"""
+import math
+
+from . import _abi as A
+
+PI = 3.14159265358979323846
+RHO = 1700.0
+R_PART = 1.4e-8
+
+
+def mass_of(r=R_PART, rho=RHO):
+    """4/3 pi r^3 rho, written as test/contact.cpp:40 computes it."""
+    return 4.0 / 3.0 * PI * math.pow(r, 3.0) * rho
+
+
+def inertia_of(m, r=R_PART):
+    """2/5 m r^2 (test/contact.cpp:41)."""
+    return 2.0 / 5.0 * m * math.pow(r, 2.0)
+
+
+def contact_params(k, gamma_n, k_t, gamma_t, mu_s, phi_d, k_r, gamma_r, mu_r, phi_r, k_o, gamma_o, mu_o, phi_o,
+                   r_part, mass, inertia, dt):
+    """Same argument order as contact_force_functor's constructor (contact_force.h:10-30)."""
+    return A.lg_contact_params(k, gamma_n, k_t, gamma_t, mu_s, phi_d, k_r, gamma_r, mu_r, phi_r, k_o, gamma_o,
+                               mu_o, phi_o, r_part, mass, inertia, dt)
+
+
+def sinter_params(k, gamma_n, k_t, gamma_t, k_r, gamma_r, k_o, gamma_o, r_part, mass, inertia, dt,
+                  critical_separation):
+    """Same argument order as alt_sinter_functor's constructor (alt_sinter_bridge.h:19-36)."""
+    return A.lg_sinter_params(k, gamma_n, k_t, gamma_t, k_r, gamma_r, k_o, gamma_o, r_part, mass, inertia, dt,
+                              critical_separation)
+
+
+def hamaker_params(A_, h0, r_part, mass, r_cutoff=0.0):
+    return A.lg_hamaker_params(A_, h0, r_cutoff, r_part, mass)
+
+
+def make_desc(n_part, binary_model=A.LG_BINARY_CONTACT, hamaker_model=A.LG_HAMAKER_NONE, contact=None,
+              sinter=None, hamaker=None, neck_mode=A.LG_NECK_PER_BOND, pairs=A.LG_PAIRS_ALL, r_verlet=0.0,
+              precision=A.LG_PRECISION_FP64, n_facets=0, facet_auto_move=0, max_neighbors=0):
+    d = A.lg_system_desc()
+    d.n_part = int(n_part)
+    d.binary_model = binary_model
+    d.hamaker_model = hamaker_model
+    if contact is not None:
+        d.contact = contact
+    if sinter is not None:
+        d.sinter = sinter
+    if hamaker is not None:
+        d.hamaker = hamaker
+    d.neck_mode = neck_mode
+    d.pairs = pairs
+    d.r_verlet = r_verlet
+    d.precision = precision
+    d.n_facets = n_facets
+    d.facet_auto_move = facet_auto_move
+    d.max_neighbors = max_neighbors
+    return d
+
+
+# --------------------------------------------------------------------------------------------
+# Synthetic aggregate workloads (seeded random-sequential-attachment aggregates)
+# --------------------------------------------------------------------------------------------
+class Material:
+    """Constants of the aggregate workloads: r = 14 nm, rho = 1700 kg/m^3, k_n = 1e4 N/m,
+    tangential/rolling/torsion stiffness 0.5 k_n, damping ratio 0.1 on the reduced mass m/2,
+    friction coefficient 1, Hamaker constant 1e-19 J with saturation distance 0.4 nm, surface-gap
+    cutoff 2r (centre distance 4r), time step 0.01 sqrt(m/k_n)."""
+
+    def __init__(self, r=R_PART, rho=RHO, k_n=1e4, stiff_ratio=0.5, zeta=0.1, mu=1.0, A_h=1e-19, h0=0.4e-9,
+                 d_crit=1.0e-9):
+        self.r = r
+        self.m = mass_of(r, rho)
+        self.I = inertia_of(self.m, r)
+        self.k_n = k_n
+        self.k_s = stiff_ratio * k_n
+        damp = lambda k: 2.0 * zeta * math.sqrt(k * self.m / 2.0)
+        self.g_n = damp(k_n)
+        self.g_s = damp(self.k_s)
+        self.mu = mu
+        self.A = A_h
+        self.h0 = h0
+        self.r_cut = 4.0 * r
+        self.d_crit = d_crit
+        self.dt = 0.01 * math.sqrt(self.m / k_n)
+
+    def contact(self):
+        return contact_params(self.k_n, self.g_n, self.k_s, self.g_s, self.mu, 1.0, self.k_s, self.g_s, self.mu,
+                              1.0, self.k_s, self.g_s, self.mu, 1.0, self.r, self.m, self.I, self.dt)
+
+    def sinter(self):
+        return sinter_params(self.k_n, self.g_n, self.k_s, self.g_s, self.k_s, self.g_s, self.k_s, self.g_s, self.r,
+                             self.m, self.I, self.dt, self.d_crit)
+
+    def hamaker(self):
+        return hamaker_params(self.A, self.h0, self.r, self.m, r_cutoff=self.r_cut)

@@ -1,0 +1,319 @@
+// lg_common.cuh -- device-side data layout and FP64 pair functors of the GB300 engine.
+//
+// The functors restate libgran's force models (paths inside the libgran project):
+//   contact      contact_force/contact_force.h:57-147
+//   bond         sinter_bridge/alt_sinter_bridge.h:103-156, alt_breaking_sinter_bridge.h:89-131
+//   Hamaker      hamaker_force/hamaker_force.h:28-43, limited_range_hamaker_force.h:29-47,
+//                simplified_hamaker_force.h:18-31
+//   surface      contact_force/surface_contact_force.h:57-145, surface_hamaker_force.h:18-30,
+//                surface_force/triangular_facet.h:32-137
+// Every FP64 expression keeps the evaluation order of the reference (Eigen component-wise
+// semantics: norm = sqrt((x*x + y*y) + z*z), normalized = v / norm). Translation units that include
+// this header for the FP64 path are compiled with --fmad=false, so a thread that walks a row in
+// ascending j produces the same bits as a sequential CPU evaluation built with -ffp-contract=off.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/libgran_gb300.h"
+
+namespace lg {
+
+// ------------------------------------------------------------------------------------------------
+// Small FP64 vector with the reference's evaluation order
+// ------------------------------------------------------------------------------------------------
+struct d3 {
+    double x, y, z;
+};
+__host__ __device__ __forceinline__ d3 mk3(double x, double y, double z) { return d3{x, y, z}; }
+__host__ __device__ __forceinline__ d3 add(d3 a, d3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ d3 sub(d3 a, d3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ d3 scl(double s, d3 a) { return mk3(s * a.x, s * a.y, s * a.z); }
+__host__ __device__ __forceinline__ d3 dvs(d3 a, double s) { return mk3(a.x / s, a.y / s, a.z / s); }
+__host__ __device__ __forceinline__ d3 neg(d3 a) { return mk3(-a.x, -a.y, -a.z); }
+__host__ __device__ __forceinline__ double dot(d3 a, d3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__host__ __device__ __forceinline__ double sqn(d3 a) { return (a.x * a.x + a.y * a.y) + a.z * a.z; }
+__host__ __device__ __forceinline__ double nrm(d3 a) { return sqrt(sqn(a)); }
+__host__ __device__ __forceinline__ d3 nrmz(d3 a) {
+    double z = sqn(a);
+    if (z > 0.0) return dvs(a, sqrt(z));
+    return a;
+}
+__host__ __device__ __forceinline__ d3 crs(d3 a, d3 b) {
+    return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__host__ __device__ __forceinline__ d3 zero3() { return mk3(0.0, 0.0, 0.0); }
+
+// State vectors live in 32-byte aligned slots (w unused) so that one particle field is one aligned
+// 32-byte sector, fetched by a single 256-bit load on sm_103a.
+typedef double4_32a dbl4;
+#ifdef __CUDACC__
+__device__ __forceinline__ d3 ld4(const dbl4 *p, int64_t i) {
+    dbl4 q = p[i];
+    return mk3(q.x, q.y, q.z);
+}
+__device__ __forceinline__ void st4(dbl4 *p, int64_t i, d3 a) { p[i] = make_double4_32a(a.x, a.y, a.z, 0.0); }
+#endif
+
+// ------------------------------------------------------------------------------------------------
+// Parameters (one POD block passed by value to every kernel)
+// ------------------------------------------------------------------------------------------------
+constexpr int kMaxFacets = 4;
+
+struct FacetDev {
+    double v[3];
+    double area;
+    double normal[3];
+    int32_t has_contact, has_hamaker;
+    lg_contact_params contact;
+    lg_hamaker_params hamaker;
+};
+
+struct Params {
+    int64_t n;
+    int32_t binary_model, hamaker_model, neck_mode, pairs;
+    lg_contact_params contact;
+    lg_sinter_params sinter;
+    lg_hamaker_params hamaker;
+    double r_verlet;
+    int32_t n_facets;
+    FacetDev facets[kMaxFacets];
+    double contact_skip_d2;  // squared centre distance above which overlap <= 0 is certain
+    double hamaker_skip_d2;  // squared centre distance above which the limited Hamaker is zero
+};
+
+// Entry flags of a pair slot (Verlet list slot or implicit all-pairs slot)
+constexpr uint32_t kXiLive = 1u;      // contact springs may be nonzero
+constexpr uint32_t kBonded = 2u;      // pair is an intact sintered bond; bond slot in bits 8..15
+__host__ __device__ __forceinline__ uint32_t bond_slot_of(uint32_t f) { return (f >> 8) & 0xffu; }
+
+// Device-side views of the pair data. Slot e = k * n + i (column-major "ELL" layout: slot k of
+// every row is contiguous, so the threads of a warp reading slot k of consecutive rows coalesce).
+struct PairView {
+    int32_t *nbr;       // [cap * n] neighbour index (Verlet mode)
+    int32_t *row_len;   // [n] (Verlet mode)
+    uint32_t *flags;    // [cap * n]
+    double *xi;         // [9][cap * n] contact springs, component-major
+    int64_t cap;        // slots per row
+};
+
+struct BondView {
+    int32_t *j;         // [bcap * n] partner of bond slot b of row i (-1 = none)
+    int8_t *intact;     // [bcap * n]
+    double *strength;   // [bcap * n]
+    double *xi;         // [9][bcap * n] bond springs
+    int32_t bcap;       // bond slots per row
+};
+
+struct StateView {
+    dbl4 *x, *v, *th, *w;        // positions, velocities (half step inside a step), orientation, spin
+    dbl4 *a, *al;                // accelerations of the last force evaluation
+    dbl4 *v_out, *w_out;         // full-step velocities written by the force kernel
+    double *sxi;                    // [n_facets][9][n] surface contact springs
+    double *facet_vert;             // [n_facets * 9] vertices read this step
+    double *facet_vert_next;        // [n_facets * 9] vertices after this step's move
+    int32_t *err;                   // device error word
+};
+
+#ifdef __CUDACC__
+// ------------------------------------------------------------------------------------------------
+// FP64 functors
+// ------------------------------------------------------------------------------------------------
+
+// contact_force.h:105-147
+__device__ __forceinline__ d3 shear_coulomb(d3 &xi, d3 n, double stiffness, double damping, double normal_force,
+                                            double mu_static, double phi_dynamic, d3 rel, double dt) {
+    double mu_dynamic = mu_static * phi_dynamic;
+    d3 xi_new = sub(xi, scl(dot(xi, n), n));
+    if (nrm(xi_new) > 0.0) {
+        double z = sqn(xi_new);
+        if (z > 0.0) xi_new = dvs(xi_new, sqrt(z));
+        double old = nrm(xi);
+        xi_new = scl(old, xi_new);
+    }
+    xi = xi_new;
+    d3 f0 = sub(scl(-stiffness, xi), scl(damping, rel));
+    double static_friction = mu_static * normal_force;
+    double dynamic_friction = mu_dynamic * normal_force;
+    double f0n = nrm(f0);
+    d3 t = (f0n > 0.0) ? nrmz(f0) : zero3();
+    double f_selected;
+    if (f0n <= static_friction) {
+        xi = add(xi, scl(dt, rel));
+        f_selected = static_friction;
+    } else {
+        xi = scl(-1.0 / stiffness, add(scl(dynamic_friction, t), scl(damping, rel)));
+        f_selected = dynamic_friction;
+    }
+    double m = (f0n < f_selected) ? f0n : f_selected;
+    return scl(m, t);
+}
+
+// alt_sinter_bridge.h:137-156
+__device__ __forceinline__ d3 shear_bond(d3 &xi, d3 n, double stiffness, double damping, d3 rel, double dt) {
+    d3 xi_new = sub(xi, scl(dot(xi, n), n));
+    if (nrm(xi_new) > 0.0) {
+        double z = sqn(xi_new);
+        if (z > 0.0) xi_new = dvs(xi_new, sqrt(z));
+        double old = nrm(xi);
+        xi_new = scl(old, xi_new);
+    }
+    xi = xi_new;
+    d3 f0 = sub(scl(-stiffness, xi), scl(damping, rel));
+    xi = add(xi, scl(dt, rel));
+    return f0;
+}
+
+// contact_force.h:57-96 -- the in-contact branch (caller has established overlap > 0 with the
+// reference's own arithmetic, n and overlap are passed in).
+__device__ __forceinline__ void contact_touching(const lg_contact_params &p, d3 n, double overlap, d3 vi, d3 vj,
+                                                 d3 wi, d3 wj, d3 *s, d3 &oa, d3 &oal) {
+    double rp = p.r_part - overlap / 2.0;
+    double v_n = -dot(sub(vi, vj), n);
+    double f_n = p.k * overlap + p.gamma_n * v_n;
+    d3 nwi = crs(n, wi), nwj = crs(n, wj);
+    d3 v_ij = add(add(sub(vi, vj), scl(rp, nwi)), scl(rp, nwj));
+    d3 v_t = sub(v_ij, scl(dot(v_ij, n), n));
+    d3 v_r = scl(-rp, sub(nwi, nwj));
+    d3 v_o = scl(p.r_part * (dot(n, wi) - dot(n, wj)), n);
+    d3 f_t = shear_coulomb(s[0], n, p.k_t, p.gamma_t, f_n, p.mu_s, p.phi_d, v_t, p.dt);
+    d3 f_r = shear_coulomb(s[1], n, p.k_r, p.gamma_r, f_n, p.mu_r, p.phi_r, v_r, p.dt);
+    d3 f_o = shear_coulomb(s[2], n, p.k_o, p.gamma_o, f_n, p.mu_o, p.phi_o, v_o, p.dt);
+    d3 tau_t = scl(rp, crs(n, f_t));
+    d3 tau_r = scl(p.r_part, crs(n, f_r));
+    d3 tau_o = scl(p.r_part, f_o);
+    oa = dvs(add(scl(f_n, n), f_t), p.mass);
+    oal = dvs(add(add(neg(tau_t), tau_r), tau_o), p.inertia);
+}
+
+// alt_sinter_bridge.h:103-128 / alt_breaking_sinter_bridge.h:89-121. Returns true when the
+// breaking variant breaks the (i, j) bond (|f_tot| > strength, alt_breaking_sinter_bridge.h:118).
+__device__ __forceinline__ bool bond_force(const lg_sinter_params &p, d3 dx, d3 vi, d3 vj, d3 wi, d3 wj, d3 *s,
+                                           bool breaking, double strength, d3 &oa, d3 &oal) {
+    d3 n = nrmz(dx);
+    double overlap = 2.0 * p.r_part - dot(dx, n);
+    double rp = p.r_part - overlap / 2.0;
+    double v_n = -dot(sub(vi, vj), n);
+    double f_n = p.k * overlap + p.gamma_n * v_n;
+    d3 nwi = crs(n, wi), nwj = crs(n, wj);
+    d3 v_ij = add(add(sub(vi, vj), scl(rp, nwi)), scl(rp, nwj));
+    d3 v_t = sub(v_ij, scl(dot(v_ij, n), n));
+    d3 v_r = scl(-rp, sub(nwi, nwj));
+    d3 v_o = scl(p.r_part * (dot(n, wi) - dot(n, wj)), n);
+    d3 f_t = shear_bond(s[0], n, p.k_t, p.gamma_t, v_t, p.dt);
+    d3 f_r = shear_bond(s[1], n, p.k_r, p.gamma_r, v_r, p.dt);
+    d3 f_o = shear_bond(s[2], n, p.k_o, p.gamma_o, v_o, p.dt);
+    d3 tau_t = scl(rp, crs(n, f_t));
+    d3 tau_r = scl(p.r_part, crs(n, f_r));
+    d3 tau_o = scl(p.r_part, f_o);
+    d3 f_tot = add(scl(f_n, n), f_t);
+    d3 tau_tot = add(add(neg(tau_t), tau_r), tau_o);
+    bool brk = breaking && (nrm(f_tot) > strength);
+    oa = dvs(f_tot, p.mass);
+    oal = dvs(tau_tot, p.inertia);
+    return brk;
+}
+
+__device__ __forceinline__ double sq_(double x) { return x * x; }
+__device__ __forceinline__ double cb_(double x) { return x * x * x; }
+
+// hamaker_force.h:28-43 / limited_range_hamaker_force.h:33-45 / simplified_hamaker_force.h:23-29.
+// r = x_j - x_i. Angular part is zero. The limited variant's cutoff test is done by the caller.
+__device__ __forceinline__ d3 hamaker_accel(int mode, const lg_hamaker_params &p, d3 r) {
+    double h = nrm(r) - 2.0 * p.r_part;
+    if (h < p.h0) h = p.h0;
+    double rp = p.r_part;
+    double s;
+    if (mode == LG_HAMAKER_SIMPLIFIED) {
+        s = 2.0 * p.A * rp / sq_(h);
+    } else {
+        double br = (4.0 * rp + 2.0 * h) / (4.0 * rp + h) / h - 2.0 / (2.0 * rp + h) - 4.0 * sq_(rp) / cb_(2.0 * rp + h) -
+                    2.0 * sq_(rp) * (4.0 * rp + 2.0 * h) / sq_(4.0 * rp + h) / sq_(h);
+        s = -p.A / 6.0 * br;
+    }
+    return dvs(scl(s, nrmz(r)), p.mass);
+}
+
+// triangular_facet.h:73-137
+__device__ __forceinline__ d3 closest_point_on_triangle(const double *vt, double area, d3 N, d3 p) {
+    d3 v0 = mk3(vt[0], vt[1], vt[2]), v1 = mk3(vt[3], vt[4], vt[5]), v2 = mk3(vt[6], vt[7], vt[8]);
+    d3 off = scl(dot(v0, N), N);
+    d3 proj = sub(p, scl(dot(p, N), N));
+    d3 cp = add(proj, off);
+    double s = 0.0;
+    d3 pa = sub(v0, cp), pb = sub(v1, cp), pc = sub(v2, cp);
+    s += 1.0 / 2.0 * nrm(crs(pa, pb));
+    s += 1.0 / 2.0 * nrm(crs(pb, pc));
+    s += 1.0 / 2.0 * nrm(crs(pc, pa));
+    if (!(s > area)) return cp;
+    d3 e[3];
+    d3 vv[3] = {v0, v1, v2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        d3 a = vv[k], b = vv[(k + 1) % 3];
+        d3 L = sub(b, a);
+        d3 uL = nrmz(L);
+        d3 tp = sub(p, a);
+        double len = nrm(L);
+        double pr = dot(tp, uL);
+        if (pr < 0.0)
+            e[k] = a;
+        else if (pr > len)
+            e[k] = b;
+        else
+            e[k] = add(a, scl(pr, uL));
+    }
+    double d1 = sqn(sub(p, e[0])), d2 = sqn(sub(p, e[1])), d3_ = sqn(sub(p, e[2]));
+    if (d1 < d2) {
+        if (d1 < d3_) return e[0];
+    } else {
+        if (d2 < d3_) return e[1];
+    }
+    return e[2];
+}
+
+// surface_contact_force.h:57-96
+__device__ __forceinline__ void surface_contact(const lg_contact_params &p, d3 xf, d3 vf, d3 xi_, d3 vi, d3 wi, d3 *s,
+                                                d3 &oa, d3 &oal) {
+    d3 dx = sub(xi_, xf);
+    d3 n = nrmz(dx);
+    double overlap = p.r_part - dot(dx, n);
+    if (overlap <= 0) {
+        s[0] = s[1] = s[2] = zero3();
+        oa = zero3();
+        oal = zero3();
+        return;
+    }
+    double rp = p.r_part - overlap;
+    double v_n = -dot(sub(vi, vf), n);
+    double f_n = p.k * overlap + p.gamma_n * v_n;
+    d3 nwi = crs(n, wi);
+    d3 v_ij = add(sub(vi, vf), scl(rp, nwi));
+    d3 v_t = sub(v_ij, scl(dot(v_ij, n), n));
+    d3 v_r = scl(-rp, nwi);
+    d3 v_o = scl(p.r_part * dot(n, wi), n);
+    d3 f_t = shear_coulomb(s[0], n, p.k_t, p.gamma_t, f_n, p.mu_s, p.phi_d, v_t, p.dt);
+    d3 f_r = shear_coulomb(s[1], n, p.k_r, p.gamma_r, f_n, p.mu_r, p.phi_r, v_r, p.dt);
+    d3 f_o = shear_coulomb(s[2], n, p.k_o, p.gamma_o, f_n, p.mu_o, p.phi_o, v_o, p.dt);
+    d3 tau_t = scl(rp, crs(n, f_t));
+    d3 tau_r = scl(p.r_part, crs(n, f_r));
+    d3 tau_o = scl(p.r_part, f_o);
+    oa = dvs(add(scl(f_n, n), f_t), p.mass);
+    oal = dvs(add(add(neg(tau_t), tau_r), tau_o), p.inertia);
+}
+
+// surface_hamaker_force.h:18-30
+__device__ __forceinline__ d3 surface_hamaker(const lg_hamaker_params &p, d3 xf, d3 xi_) {
+    d3 r = sub(xf, xi_);
+    double h = nrm(r) - p.r_part;
+    if (h < p.h0) h = p.h0;
+    double s = 2.0 * p.A / 3.0 * (cb_(p.r_part) / sq_(h) / sq_(h + 2.0 * p.r_part));
+    return dvs(scl(s, nrmz(r)), p.mass);
+}
+
+__device__ __forceinline__ void set_error(int32_t *err, int32_t bit) {
+    if (err) atomicOr(err, bit);
+}
+#endif  // __CUDACC__
+
+}  // namespace lg

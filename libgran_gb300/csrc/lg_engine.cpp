@@ -1,0 +1,810 @@
+// lg_engine.cpp -- host side of the C ABI (include/libgran_gb300.h): handle lifetime, bond
+// detection, state transfer, the step loop, Verlet-list management and read-back.
+//
+// Built with -ffp-contract=off: the few host computations that feed the kernels (bond detection,
+// facet area and normal) use the reference's arithmetic exactly.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "lg_engine_internal.h"
+#include "lg_kernels.h"
+
+using namespace lg;
+
+// ------------------------------------------------------------------------------------------------
+// Errors
+// ------------------------------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+int lg_fail(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define LG_CUDA(call)                                                                                     \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) return lg_fail(LG_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                              __FILE__, __LINE__);                                        \
+    } while (0)
+
+extern "C" const char *lg_version(void) { return "libgran_gb300 0.1 sm_103a"; }
+extern "C" const char *lg_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int lg_device_count(int *count) {
+    if (!count) return lg_fail(LG_E_INVALID, "lg_device_count: null pointer");
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    if (e != cudaSuccess) {
+        *count = 0;
+        cudaGetLastError();
+        return LG_OK;
+    }
+    *count = c;
+    return LG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host vector helpers (reference evaluation order)
+// ------------------------------------------------------------------------------------------------
+static inline d3 hld(const double *p, int64_t i) { return mk3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+
+// ------------------------------------------------------------------------------------------------
+// Bond detection: the reference's double loop over i < j (alt_sinter_bridge.h:67-89,
+// alt_breaking_sinter_bridge.h:65-76) tests |(|x_i - x_j| - 2r)| < critical_separation in
+// lexicographic (i, j) order. Candidates are gathered through a cell grid and then processed in
+// that same order; the cycle test "i and j already connected" is answered by a union-find, which
+// gives the same decisions as the reference's subset relabelling.
+// ------------------------------------------------------------------------------------------------
+static int64_t uf_find(std::vector<int64_t> &p, int64_t a) {
+    while (p[a] != a) {
+        p[a] = p[p[a]];
+        a = p[a];
+    }
+    return a;
+}
+
+int lg_detect_bonds(const double *x0, int64_t n, double r, double dc, bool cycle_free,
+                    std::vector<std::pair<int32_t, int32_t>> &bonds) {
+    bonds.clear();
+    if (n < 2) return LG_OK;
+    const double reach = 2.0 * r + dc;
+    std::vector<std::pair<int32_t, int32_t>> cand;
+    if (n <= 2048) {
+        for (int64_t i = 0; i + 1 < n; ++i)
+            for (int64_t j = i + 1; j < n; ++j) {
+                double g = nrm(sub(hld(x0, i), hld(x0, j))) - 2.0 * r;
+                if (std::fabs(g) < dc) cand.emplace_back((int32_t)i, (int32_t)j);
+            }
+    } else {
+        double lo[3] = {1e300, 1e300, 1e300};
+        for (int64_t i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) lo[c] = std::min(lo[c], x0[3 * i + c]);
+        auto key = [&](int64_t a, int64_t b, int64_t c) { return (a * 2097152 + b) * 2097152 + c; };
+        std::unordered_map<int64_t, std::vector<int32_t>> grid;
+        grid.reserve((size_t)n);
+        std::vector<int64_t> cc(3 * (size_t)n);
+        for (int64_t i = 0; i < n; ++i) {
+            for (int c = 0; c < 3; ++c) cc[3 * i + c] = (int64_t)std::floor((x0[3 * i + c] - lo[c]) / reach);
+            grid[key(cc[3 * i], cc[3 * i + 1], cc[3 * i + 2])].push_back((int32_t)i);
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            for (int64_t dz = -1; dz <= 1; ++dz)
+                for (int64_t dy = -1; dy <= 1; ++dy)
+                    for (int64_t dx = -1; dx <= 1; ++dx) {
+                        auto it = grid.find(key(cc[3 * i] + dx, cc[3 * i + 1] + dy, cc[3 * i + 2] + dz));
+                        if (it == grid.end()) continue;
+                        for (int32_t j : it->second) {
+                            if (j <= i) continue;
+                            double g = nrm(sub(hld(x0, i), hld(x0, j))) - 2.0 * r;
+                            if (std::fabs(g) < dc) cand.emplace_back((int32_t)i, j);
+                        }
+                    }
+        }
+        std::sort(cand.begin(), cand.end());
+    }
+    std::vector<int64_t> parent((size_t)n);
+    for (int64_t i = 0; i < n; ++i) parent[i] = i;
+    for (auto &pr : cand) {
+        if (cycle_free) {
+            int64_t a = uf_find(parent, pr.first), b = uf_find(parent, pr.second);
+            if (a == b) continue;  // "preventing neck insertion to avoid a cycle"
+            parent[b] = a;
+        }
+        bonds.push_back(pr);
+    }
+    return LG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Seeded synthetic aggregates (random sequential attachment)
+// ------------------------------------------------------------------------------------------------
+struct SplitMix {
+    uint64_t s;
+    uint64_t next() {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return (double)(next() >> 11) * 0x1.0p-53; }
+    d3 unit() {
+        for (;;) {
+            double a = 2.0 * uniform() - 1.0, b = 2.0 * uniform() - 1.0, c = 2.0 * uniform() - 1.0;
+            double s2 = (a * a + b * b) + c * c;
+            if (s2 > 1e-6 && s2 <= 1.0) {
+                double s = std::sqrt(s2);
+                return mk3(a / s, b / s, c / s);
+            }
+        }
+    }
+};
+
+// Each new sphere touches a uniformly chosen existing sphere in a uniformly random direction and is
+// rejected when it overlaps any other sphere by more than 1e-12 r.
+extern "C" int lg_generate_rsa_aggregate(uint64_t seed, int64_t n, double r, double *x) {
+    if (n < 1 || !x || !(r > 0)) return lg_fail(LG_E_INVALID, "lg_generate_rsa_aggregate: bad arguments");
+    SplitMix rng{seed};
+    const double edge = 2.0 * r;
+    const double lim = 2.0 * r - 1e-12 * r;
+    const double lim2 = lim * lim;
+    auto key = [](int64_t a, int64_t b, int64_t c) {
+        return ((a + 1048576) * 2097152 + (b + 1048576)) * 2097152 + (c + 1048576);
+    };
+    std::unordered_map<int64_t, std::vector<int32_t>> grid;
+    grid.reserve((size_t)n * 2);
+    auto cell = [&](d3 p, int64_t *c) {
+        c[0] = (int64_t)std::floor(p.x / edge);
+        c[1] = (int64_t)std::floor(p.y / edge);
+        c[2] = (int64_t)std::floor(p.z / edge);
+    };
+    x[0] = x[1] = x[2] = 0.0;
+    int64_t c0[3];
+    cell(mk3(0, 0, 0), c0);
+    grid[key(c0[0], c0[1], c0[2])].push_back(0);
+    for (int64_t k = 1; k < n; ++k) {
+        for (int attempt = 0;; ++attempt) {
+            if (attempt > 100000) return lg_fail(LG_E_STATE, "lg_generate_rsa_aggregate: no free site found");
+            int64_t p = (int64_t)(rng.uniform() * (double)k);
+            if (p >= k) p = k - 1;
+            d3 dir = rng.unit();
+            d3 c = add(hld(x, p), scl(2.0 * r, dir));
+            int64_t cc[3];
+            cell(c, cc);
+            bool ok = true;
+            for (int64_t dz = -1; dz <= 1 && ok; ++dz)
+                for (int64_t dy = -1; dy <= 1 && ok; ++dy)
+                    for (int64_t dx = -1; dx <= 1 && ok; ++dx) {
+                        auto it = grid.find(key(cc[0] + dx, cc[1] + dy, cc[2] + dz));
+                        if (it == grid.end()) continue;
+                        for (int32_t q : it->second) {
+                            if (q == p) continue;
+                            if (sqn(sub(c, hld(x, q))) < lim2) {
+                                ok = false;
+                                break;
+                            }
+                        }
+                    }
+            if (!ok) continue;
+            x[3 * k] = c.x;
+            x[3 * k + 1] = c.y;
+            x[3 * k + 2] = c.z;
+            grid[key(cc[0], cc[1], cc[2])].push_back((int32_t)k);
+            break;
+        }
+    }
+    return LG_OK;
+}
+
+// Uniform random velocity components in [-vmax, vmax].
+extern "C" int lg_generate_velocities(uint64_t seed, int64_t n, double vmax, double *v) {
+    if (n < 0 || !v) return lg_fail(LG_E_INVALID, "lg_generate_velocities: bad arguments");
+    SplitMix rng{seed ^ 0x5DEECE66Dull};
+    for (int64_t q = 0; q < 3 * n; ++q) v[q] = (2.0 * rng.uniform() - 1.0) * vmax;
+    return LG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Handle
+// ------------------------------------------------------------------------------------------------
+template <typename T>
+static int dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return lg_fail(LG_E_NOMEM, "cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
+    }
+    return LG_OK;
+}
+
+#define LG_TRY(expr)              \
+    do {                          \
+        int rc_ = (expr);         \
+        if (rc_ != LG_OK) return rc_; \
+    } while (0)
+
+static void to_dev4(const double *aos, int64_t n, std::vector<dbl4> &tmp) {
+    tmp.resize((size_t)n);
+    for (int64_t i = 0; i < n; ++i) tmp[i] = make_double4_32a(aos[3 * i], aos[3 * i + 1], aos[3 * i + 2], 0.0);
+}
+
+static int upload4(dbl4 *dst, const double *aos, int64_t n, cudaStream_t st) {
+    std::vector<dbl4> tmp;
+    to_dev4(aos, n, tmp);
+    LG_CUDA(cudaMemcpyAsync(dst, tmp.data(), sizeof(dbl4) * (size_t)n, cudaMemcpyHostToDevice, st));
+    LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+static int download4(const dbl4 *src, double *aos, int64_t n, cudaStream_t st) {
+    std::vector<dbl4> tmp((size_t)n);
+    LG_CUDA(cudaMemcpyAsync(tmp.data(), src, sizeof(dbl4) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    LG_CUDA(cudaStreamSynchronize(st));
+    for (int64_t i = 0; i < n; ++i) {
+        aos[3 * i] = tmp[i].x;
+        aos[3 * i + 1] = tmp[i].y;
+        aos[3 * i + 2] = tmp[i].z;
+    }
+    return LG_OK;
+}
+
+void lg_system::release() {
+    if (device >= 0) cudaSetDevice(device);
+    for (void *p : allocations) cudaFree(p);
+    allocations.clear();
+    if (stream) cudaStreamDestroy(stream);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    stream = nullptr;
+}
+
+template <typename U>
+int lg_system::alloc(U **p, size_t count) {
+    LG_TRY(dalloc(p, count));
+    allocations.push_back((void *)*p);
+    return LG_OK;
+}
+
+static int choose_threads_per_row(const lg_system *s) {
+    const int64_t n = s->P.n;
+    const int64_t want = 152 * 1024;
+    int T = 1;
+    while (T < 32 && n * T < want) T *= 2;
+    const int64_t len = s->P.pairs == LG_PAIRS_VERLET ? 32 : n - 1;
+    while (T > 1 && T * 2 > len) T /= 2;
+    return T;
+}
+
+static int rebuild_list(lg_system *s) {
+    PairView &oldv = s->pv[s->pcur];
+    PairView &newv = s->pv[1 - s->pcur];
+    PairView o = oldv;
+    if (!s->list_built) o.row_len = nullptr;
+    launch_list_build(s->P.n, s->x, s->P.r_verlet, s->max_cells, s->ls, o, newv, s->bv, s->err, s->stream);
+    s->launches += 7;
+    s->pcur = 1 - s->pcur;
+    s->list_built = true;
+    LG_CUDA(cudaGetLastError());
+    return LG_OK;
+}
+
+static StateView state_view(lg_system *s, bool half_step_inputs) {
+    StateView S{};
+    S.x = s->x;
+    S.th = s->th;
+    S.v = s->v[s->vcur];
+    S.w = s->w[s->vcur];
+    S.a = s->a;
+    S.al = s->al;
+    S.v_out = s->v[1 - s->vcur];
+    S.w_out = s->w[1 - s->vcur];
+    S.sxi = s->sxi;
+    S.facet_vert = s->fv[s->fcur];
+    S.facet_vert_next = s->fv[1 - s->fcur];
+    S.err = s->err;
+    (void)half_step_inputs;
+    return S;
+}
+
+static int launch_forces(lg_system *s, double hdt, double dt, int move_facets) {
+    StateView S = state_view(s, true);
+    if (s->precision == LG_PRECISION_MIXED)
+        launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
+    else
+        launch_forces_fp64(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
+    s->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    return LG_OK;
+}
+
+static int step_once(lg_system *s, double dt, int64_t rebuild_every) {
+    if (s->P.pairs == LG_PAIRS_VERLET && rebuild_every > 0 && (s->step_index % rebuild_every) == 0)
+        LG_TRY(rebuild_list(s));
+    const double hdt = dt / 2.0;
+    launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->stream);
+    s->launches += 1;
+    const int mv = (s->facet_auto_move && s->P.n_facets > 0) ? 1 : 0;
+    LG_TRY(launch_forces(s, hdt, dt, mv));
+    s->vcur = 1 - s->vcur;
+    if (mv) s->fcur = 1 - s->fcur;
+    s->step_index++;
+    return LG_OK;
+}
+
+static int check_args(const lg_system_desc *d) {
+    if (!d) return lg_fail(LG_E_INVALID, "lg_create: null descriptor");
+    if (d->n_part < 1 || d->n_part > (int64_t)1 << 30) return lg_fail(LG_E_INVALID, "lg_create: n_part %lld out of range", (long long)d->n_part);
+    if (d->binary_model < 0 || d->binary_model > 3) return lg_fail(LG_E_INVALID, "lg_create: unknown binary_model %d", d->binary_model);
+    if (d->hamaker_model < 0 || d->hamaker_model > 3) return lg_fail(LG_E_INVALID, "lg_create: unknown hamaker_model %d", d->hamaker_model);
+    if (d->binary_model == LG_BINARY_NONE && d->hamaker_model == LG_HAMAKER_NONE)
+        return lg_fail(LG_E_INVALID, "lg_create: at least one binary force functor must be provided");
+    if (d->pairs != LG_PAIRS_ALL && d->pairs != LG_PAIRS_VERLET) return lg_fail(LG_E_INVALID, "lg_create: unknown pairs mode %d", d->pairs);
+    if (d->pairs == LG_PAIRS_VERLET && !(d->r_verlet > 0)) return lg_fail(LG_E_INVALID, "lg_create: r_verlet must be > 0");
+    if (d->pairs == LG_PAIRS_ALL && d->n_part > 8192)
+        return lg_fail(LG_E_INVALID, "lg_create: all-pairs mode holds n^2 spring slots; n_part %lld > 8192 needs LG_PAIRS_VERLET", (long long)d->n_part);
+    if (d->precision != LG_PRECISION_FP64 && d->precision != LG_PRECISION_MIXED) return lg_fail(LG_E_INVALID, "lg_create: unknown precision %d", d->precision);
+    if (d->precision == LG_PRECISION_MIXED && !lg::mixed_available()) return lg_fail(LG_E_INVALID, "lg_create: mixed precision is not built in this library");
+    if (d->n_facets < 0 || d->n_facets > kMaxFacets) return lg_fail(LG_E_INVALID, "lg_create: n_facets %d out of range [0, %d]", d->n_facets, kMaxFacets);
+    if (d->neck_mode != LG_NECK_PER_BOND && d->neck_mode != LG_NECK_REFERENCE_INDEXING) return lg_fail(LG_E_INVALID, "lg_create: unknown neck_mode %d", d->neck_mode);
+    if (d->max_neighbors < 0) return lg_fail(LG_E_INVALID, "lg_create: max_neighbors < 0");
+    return LG_OK;
+}
+
+static int create_impl(const lg_system_desc *d, const double *x0, const double *v0, const double *th0, const double *om0,
+                       const lg_facet_desc *facets, const double *neck, int64_t n_neck, int device, lg_system *s) {
+    LG_TRY(check_args(d));
+    if (!x0 || !v0 || !th0 || !om0) return lg_fail(LG_E_INVALID, "lg_create: null state pointer");
+    if (d->n_facets > 0 && !facets) return lg_fail(LG_E_INVALID, "lg_create: n_facets > 0 but facets is null");
+    const int64_t n = d->n_part;
+    s->device = device;
+    LG_CUDA(cudaSetDevice(device));
+    LG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    LG_CUDA(cudaEventCreate(&s->ev0));
+    LG_CUDA(cudaEventCreate(&s->ev1));
+    s->desc = *d;
+    s->precision = d->precision;
+    s->facet_auto_move = d->facet_auto_move != 0;
+
+    Params &P = s->P;
+    memset(&P, 0, sizeof(P));
+    P.n = n;
+    P.binary_model = d->binary_model;
+    P.hamaker_model = d->hamaker_model;
+    P.neck_mode = d->neck_mode;
+    P.pairs = d->pairs;
+    P.contact = d->contact;
+    P.sinter = d->sinter;
+    P.hamaker = d->hamaker;
+    P.r_verlet = d->r_verlet;
+    P.n_facets = d->n_facets;
+    const double cr = 2.0 * d->contact.r_part;
+    P.contact_skip_d2 = cr * cr * (1.0 + 1e-9);
+    P.hamaker_skip_d2 = d->hamaker.r_cutoff * d->hamaker.r_cutoff * (1.0 + 1e-9);
+    for (int f = 0; f < d->n_facets; ++f) {
+        const lg_facet_desc &fd = facets[f];
+        FacetDev &o = P.facets[f];
+        for (int c = 0; c < 3; ++c) o.v[c] = fd.v_facet[c];
+        d3 v0_ = mk3(fd.vertices[0], fd.vertices[1], fd.vertices[2]);
+        d3 v1_ = mk3(fd.vertices[3], fd.vertices[4], fd.vertices[5]);
+        d3 v2_ = mk3(fd.vertices[6], fd.vertices[7], fd.vertices[8]);
+        d3 u = sub(v1_, v0_), w = sub(v2_, v0_);
+        o.area = 1.0 / 2.0 * nrm(crs(u, w));  // triangular_facet.h:23-27
+        d3 N = nrmz(crs(u, w));
+        o.normal[0] = N.x;
+        o.normal[1] = N.y;
+        o.normal[2] = N.z;
+        o.has_contact = fd.has_contact;
+        o.has_hamaker = fd.has_hamaker;
+        o.contact = fd.contact;
+        o.hamaker = fd.hamaker;
+    }
+
+    // bonds
+    std::vector<std::pair<int32_t, int32_t>> bonds;
+    const bool sinter = d->binary_model == LG_BINARY_SINTER || d->binary_model == LG_BINARY_BREAKING_SINTER;
+    if (sinter) LG_TRY(lg_detect_bonds(x0, n, d->sinter.r_part, d->sinter.critical_separation,
+                                       d->binary_model == LG_BINARY_SINTER, bonds));
+    if (d->binary_model == LG_BINARY_BREAKING_SINTER && n_neck != 0 && n_neck != (int64_t)bonds.size())
+        return lg_fail(LG_E_INVALID, "lg_create: %lld neck strengths given but %zu bonds were detected", (long long)n_neck,
+                       bonds.size());
+    std::vector<int32_t> deg((size_t)n, 0);
+    for (auto &b : bonds) {
+        deg[b.first]++;
+        deg[b.second]++;
+    }
+    int32_t bcap = 1;
+    for (int64_t i = 0; i < n; ++i) bcap = std::max(bcap, deg[i]);
+    if (bcap > 255) return lg_fail(LG_E_INVALID, "lg_create: a particle has %d bonds (max 255)", bcap);
+    s->bv.bcap = bcap;
+    s->n_bonds_initial = 2 * (int64_t)bonds.size();
+    {
+        const size_t bs = (size_t)bcap * (size_t)n;
+        std::vector<int32_t> bj(bs, -1);
+        std::vector<int8_t> bint(bs, 0);
+        std::vector<double> bstr(bs, 0.0);
+        std::vector<double> pstr((size_t)n, 0.0);  // particle-indexed strengths of the reference
+        std::vector<int32_t> fill((size_t)n, 0);
+        for (size_t b = 0; b < bonds.size(); ++b) {
+            double sv = (neck && n_neck > 0) ? neck[b] : INFINITY;
+            pstr[bonds[b].first] = sv;
+            pstr[bonds[b].second] = sv;
+        }
+        for (size_t b = 0; b < bonds.size(); ++b) {
+            double sv = (neck && n_neck > 0) ? neck[b] : INFINITY;
+            int32_t i = bonds[b].first, j = bonds[b].second;
+            int32_t si = fill[i]++, sj = fill[j]++;
+            size_t ei = (size_t)si * n + i, ej = (size_t)sj * n + j;
+            bj[ei] = j;
+            bj[ej] = i;
+            bint[ei] = bint[ej] = 1;
+            if (d->neck_mode == LG_NECK_REFERENCE_INDEXING) {
+                bstr[ei] = (i == 0) ? pstr[j] : 0.0;  // neck_strengths[i*n + j] is set only where i == 0
+                bstr[ej] = (j == 0) ? pstr[i] : 0.0;
+            } else {
+                bstr[ei] = bstr[ej] = sv;
+            }
+        }
+        LG_TRY(s->alloc(&s->bv.j, bs));
+        LG_TRY(s->alloc(&s->bv.intact, bs));
+        LG_TRY(s->alloc(&s->bv.strength, bs));
+        LG_TRY(s->alloc(&s->bv.xi, 9 * bs));
+        LG_CUDA(cudaMemcpy(s->bv.j, bj.data(), sizeof(int32_t) * bs, cudaMemcpyHostToDevice));
+        LG_CUDA(cudaMemcpy(s->bv.intact, bint.data(), sizeof(int8_t) * bs, cudaMemcpyHostToDevice));
+        LG_CUDA(cudaMemcpy(s->bv.strength, bstr.data(), sizeof(double) * bs, cudaMemcpyHostToDevice));
+        LG_CUDA(cudaMemset(s->bv.xi, 0, sizeof(double) * 9 * bs));
+        s->host_bond_j = std::move(bj);
+    }
+
+    // state
+    LG_TRY(s->alloc(&s->x, n));
+    LG_TRY(s->alloc(&s->th, n));
+    LG_TRY(s->alloc(&s->v[0], n));
+    LG_TRY(s->alloc(&s->v[1], n));
+    LG_TRY(s->alloc(&s->w[0], n));
+    LG_TRY(s->alloc(&s->w[1], n));
+    LG_TRY(s->alloc(&s->a, n));
+    LG_TRY(s->alloc(&s->al, n));
+    LG_TRY(s->alloc(&s->err, 1));
+    LG_CUDA(cudaMemset(s->err, 0, sizeof(int32_t)));
+    LG_CUDA(cudaMemset(s->a, 0, sizeof(dbl4) * n));
+    LG_CUDA(cudaMemset(s->al, 0, sizeof(dbl4) * n));
+    LG_TRY(upload4(s->x, x0, n, s->stream));
+    LG_TRY(upload4(s->v[0], v0, n, s->stream));
+    LG_TRY(upload4(s->th, th0, n, s->stream));
+    LG_TRY(upload4(s->w[0], om0, n, s->stream));
+    s->vcur = 0;
+
+    // facets
+    const int nf = std::max(d->n_facets, 1);
+    LG_TRY(s->alloc(&s->fv[0], 9 * (size_t)nf));
+    LG_TRY(s->alloc(&s->fv[1], 9 * (size_t)nf));
+    LG_TRY(s->alloc(&s->sxi, 9 * (size_t)nf * (size_t)n));
+    LG_CUDA(cudaMemset(s->sxi, 0, sizeof(double) * 9 * (size_t)nf * (size_t)n));
+    if (d->n_facets > 0) {
+        std::vector<double> fvh(9 * (size_t)d->n_facets);
+        for (int f = 0; f < d->n_facets; ++f)
+            for (int q = 0; q < 9; ++q) fvh[9 * f + q] = facets[f].vertices[q];
+        LG_CUDA(cudaMemcpy(s->fv[0], fvh.data(), sizeof(double) * fvh.size(), cudaMemcpyHostToDevice));
+        LG_CUDA(cudaMemcpy(s->fv[1], fvh.data(), sizeof(double) * fvh.size(), cudaMemcpyHostToDevice));
+    }
+    s->fcur = 0;
+
+    // pair slots
+    if (d->pairs == LG_PAIRS_ALL) {
+        const int64_t cap = std::max<int64_t>(n - 1, 1);
+        PairView &pv = s->pv[0];
+        pv.cap = cap;
+        pv.nbr = nullptr;
+        pv.row_len = nullptr;
+        LG_TRY(s->alloc(&pv.flags, (size_t)(cap * n)));
+        LG_TRY(s->alloc(&pv.xi, 9 * (size_t)(cap * n)));
+        LG_CUDA(cudaMemset(pv.xi, 0, sizeof(double) * 9 * (size_t)(cap * n)));
+        std::vector<uint32_t> fl((size_t)(cap * n), 0u);
+        for (int64_t b = 0; b < bcap; ++b)
+            for (int64_t i = 0; i < n; ++i) {
+                int32_t j = s->host_bond_j[(size_t)b * n + i];
+                if (j < 0) continue;
+                int64_t k = j < i ? j : j - 1;
+                fl[(size_t)(k * n + i)] = kBonded | ((uint32_t)b << 8);
+            }
+        LG_CUDA(cudaMemcpy(pv.flags, fl.data(), sizeof(uint32_t) * fl.size(), cudaMemcpyHostToDevice));
+        s->pv[1] = pv;
+        s->pcur = 0;
+    } else {
+        int64_t cap = d->max_neighbors > 0 ? d->max_neighbors : 96;
+        cap = std::min<int64_t>(cap, std::max<int64_t>(n - 1, 1));
+        for (int q = 0; q < 2; ++q) {
+            PairView &pv = s->pv[q];
+            pv.cap = cap;
+            LG_TRY(s->alloc(&pv.nbr, (size_t)(cap * n)));
+            LG_TRY(s->alloc(&pv.row_len, (size_t)n));
+            LG_TRY(s->alloc(&pv.flags, (size_t)(cap * n)));
+            LG_TRY(s->alloc(&pv.xi, 9 * (size_t)(cap * n)));
+            LG_CUDA(cudaMemset(pv.row_len, 0, sizeof(int32_t) * n));
+        }
+        s->pcur = 0;
+        s->max_cells = std::max<int64_t>(64, 4 * n);
+        s->ls.nparts = 256;
+        LG_TRY(s->alloc(&s->ls.part, 6 * 256));
+        LG_TRY(s->alloc(&s->ls.grid, 1));
+        LG_TRY(s->alloc(&s->ls.cell_of, (size_t)n));
+        LG_TRY(s->alloc(&s->ls.count, (size_t)s->max_cells));
+        LG_TRY(s->alloc(&s->ls.start, (size_t)s->max_cells));
+        LG_TRY(s->alloc(&s->ls.fill, (size_t)s->max_cells));
+        LG_TRY(s->alloc(&s->ls.sorted, (size_t)n));
+        LG_TRY(rebuild_list(s));
+    }
+    LG_TRY(s->alloc(&s->obs_scratch, (size_t)obs_scratch_doubles(n)));
+    LG_TRY(s->alloc(&s->obs_out, 32));
+
+    s->T = choose_threads_per_row(s);
+    // initial accelerations (the first half kick needs them); velocities are unchanged (hdt = 0)
+    LG_TRY(launch_forces(s, 0.0, 0.0, 0));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    return LG_OK;
+}
+
+extern "C" int lg_create(const lg_system_desc *desc, const double *x0, const double *v0, const double *theta0,
+                         const double *omega0, const lg_facet_desc *facets, const double *neck_strengths,
+                         int64_t n_neck_strengths, int device, lg_system **out) {
+    if (!out) return lg_fail(LG_E_INVALID, "lg_create: null output handle");
+    *out = nullptr;
+    lg_system *s = new (std::nothrow) lg_system();
+    if (!s) return lg_fail(LG_E_NOMEM, "lg_create: host allocation failed");
+    int rc = create_impl(desc, x0, v0, theta0, omega0, facets, neck_strengths, n_neck_strengths, device, s);
+    if (rc != LG_OK) {
+        std::string keep = g_last_error;
+        s->release();
+        delete s;
+        g_last_error = keep;
+        return rc;
+    }
+    *out = s;
+    return LG_OK;
+}
+
+extern "C" int lg_destroy(lg_system *s) {
+    if (!s) return LG_OK;
+    s->release();
+    delete s;
+    return LG_OK;
+}
+
+#define LG_HANDLE(s)                                                   \
+    do {                                                               \
+        if (!(s)) return lg_fail(LG_E_INVALID, "null system handle"); \
+        LG_CUDA(cudaSetDevice((s)->device));                           \
+    } while (0)
+
+extern "C" int lg_step(lg_system *s, double dt, int64_t nsteps, int64_t rebuild_every) {
+    LG_HANDLE(s);
+    if (nsteps < 0) return lg_fail(LG_E_INVALID, "lg_step: nsteps < 0");
+    if (!std::isfinite(dt)) return lg_fail(LG_E_INVALID, "lg_step: dt is not finite");
+    for (int64_t k = 0; k < nsteps; ++k) LG_TRY(step_once(s, dt, rebuild_every));
+    return LG_OK;
+}
+
+extern "C" int lg_step_timed(lg_system *s, double dt, int64_t nsteps, int64_t rebuild_every, float *ms) {
+    LG_HANDLE(s);
+    if (!ms) return lg_fail(LG_E_INVALID, "lg_step_timed: null output");
+    LG_CUDA(cudaEventRecord(s->ev0, s->stream));
+    LG_TRY(lg_step(s, dt, nsteps, rebuild_every));
+    LG_CUDA(cudaEventRecord(s->ev1, s->stream));
+    LG_CUDA(cudaEventSynchronize(s->ev1));
+    LG_CUDA(cudaEventElapsedTime(ms, s->ev0, s->ev1));
+    return LG_OK;
+}
+
+extern "C" int lg_update_neighbor_list(lg_system *s) {
+    LG_HANDLE(s);
+    if (s->P.pairs != LG_PAIRS_VERLET) return LG_OK;
+    return rebuild_list(s);
+}
+
+static dbl4 *field_ptr(lg_system *s, int field) {
+    switch (field) {
+        case LG_FIELD_X: return s->x;
+        case LG_FIELD_V: return s->v[s->vcur];
+        case LG_FIELD_THETA: return s->th;
+        case LG_FIELD_OMEGA: return s->w[s->vcur];
+        case LG_FIELD_A: return s->a;
+        case LG_FIELD_ALPHA: return s->al;
+        default: return nullptr;
+    }
+}
+
+extern "C" int lg_get(lg_system *s, int field, double *out) {
+    LG_HANDLE(s);
+    dbl4 *p = field_ptr(s, field);
+    if (!p || !out) return lg_fail(LG_E_INVALID, "lg_get: bad field %d or null output", field);
+    return download4(p, out, s->P.n, s->stream);
+}
+
+extern "C" int lg_set(lg_system *s, int field, const double *in) {
+    LG_HANDLE(s);
+    dbl4 *p = field_ptr(s, field);
+    if (!p || !in) return lg_fail(LG_E_INVALID, "lg_set: bad field %d or null input", field);
+    return upload4(p, in, s->P.n, s->stream);
+}
+
+extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
+    LG_HANDLE(s);
+    if (T == 0) {
+        s->T = choose_threads_per_row(s);
+        return LG_OK;
+    }
+    if (T != 1 && T != 2 && T != 4 && T != 8 && T != 16 && T != 32)
+        return lg_fail(LG_E_INVALID, "lg_set_threads_per_row: T must be 0 or a power of two <= 32");
+    s->T = T;
+    return LG_OK;
+}
+
+extern "C" int lg_reset_acceleration_buffers(lg_system *s) {
+    LG_HANDLE(s);
+    LG_CUDA(cudaMemsetAsync(s->a, 0, sizeof(dbl4) * s->P.n, s->stream));
+    LG_CUDA(cudaMemsetAsync(s->al, 0, sizeof(dbl4) * s->P.n, s->stream));
+    return LG_OK;
+}
+
+extern "C" int lg_get_device_errors(lg_system *s, int32_t *errors) {
+    LG_HANDLE(s);
+    if (!errors) return lg_fail(LG_E_INVALID, "lg_get_device_errors: null output");
+    LG_CUDA(cudaMemcpyAsync(errors, s->err, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    return LG_OK;
+}
+
+extern "C" int lg_get_observables(lg_system *s, lg_observables *o) {
+    LG_HANDLE(s);
+    if (!o) return lg_fail(LG_E_INVALID, "lg_get_observables: null output");
+    const Params &P = s->P;
+    double m, I;
+    if (P.binary_model == LG_BINARY_SINTER || P.binary_model == LG_BINARY_BREAKING_SINTER) {
+        m = P.sinter.mass;
+        I = P.sinter.inertia;
+    } else if (P.binary_model == LG_BINARY_CONTACT) {
+        m = P.contact.mass;
+        I = P.contact.inertia;
+    } else {
+        m = P.hamaker.mass;
+        I = P.contact.inertia;
+    }
+    StateView S = state_view(s, false);
+    launch_observables(P, S, s->pv[s->pcur], s->bv, m, I, s->obs_scratch, s->obs_out, s->stream);
+    s->launches += 2;
+    LG_CUDA(cudaGetLastError());
+    double h[32];
+    LG_CUDA(cudaMemcpyAsync(h, s->obs_out, sizeof(double) * 18, cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    const double nn = (double)P.n;
+    double c[3] = {h[12] / nn, h[13] / nn, h[14] / nn};
+    double *dc = s->obs_out + 24;
+    LG_CUDA(cudaMemcpyAsync(dc, c, sizeof(double) * 3, cudaMemcpyHostToDevice, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    launch_observables_rg(P.n, s->x, c, s->obs_scratch, s->obs_out, s->stream);
+    s->launches += 2;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaMemcpyAsync(h + 18, s->obs_out + 18, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    memset(o, 0, sizeof(*o));
+    o->ke_total = h[0];
+    o->ke_translational = h[1] / 2.0;
+    o->ke_rotational = h[2] / 2.0;
+    o->linear_momentum = m * std::sqrt((h[3] * h[3] + h[4] * h[4]) + h[5] * h[5]);
+    double L[3] = {h[6] + h[9], h[7] + h[10], h[8] + h[11]};
+    o->angular_momentum = std::sqrt((L[0] * L[0] + L[1] * L[1]) + L[2] * L[2]);
+    for (int k = 0; k < 3; ++k) o->center_of_mass[k] = c[k];
+    o->radius_of_gyration = std::sqrt(h[18] / nn);
+    o->potential_energy = h[15];
+    o->n_contacts = (int64_t)h[16];
+    o->n_bonds = (int64_t)h[17];
+    o->n_bonds_initial = s->n_bonds_initial;
+    return LG_OK;
+}
+
+extern "C" int lg_get_bonds(lg_system *s, int64_t *n_bonds, int64_t *pairs, int64_t cap) {
+    LG_HANDLE(s);
+    if (!n_bonds) return lg_fail(LG_E_INVALID, "lg_get_bonds: null count");
+    const int64_t n = s->P.n;
+    const size_t bs = (size_t)s->bv.bcap * (size_t)n;
+    std::vector<int8_t> intact(bs);
+    LG_CUDA(cudaMemcpyAsync(intact.data(), s->bv.intact, bs, cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    std::vector<std::pair<int64_t, int64_t>> out;
+    for (size_t b = 0; b < (size_t)s->bv.bcap; ++b)
+        for (int64_t i = 0; i < n; ++i) {
+            size_t e = b * (size_t)n + (size_t)i;
+            if (s->host_bond_j[e] >= 0 && intact[e]) out.emplace_back(i, s->host_bond_j[e]);
+        }
+    std::sort(out.begin(), out.end());
+    *n_bonds = (int64_t)out.size();
+    if (pairs)
+        for (int64_t k = 0; k < (int64_t)out.size() && k < cap; ++k) {
+            pairs[2 * k] = out[k].first;
+            pairs[2 * k + 1] = out[k].second;
+        }
+    return LG_OK;
+}
+
+extern "C" int lg_get_pair_springs(lg_system *s, int64_t i, int64_t j, double *out9) {
+    LG_HANDLE(s);
+    if (!out9) return lg_fail(LG_E_INVALID, "lg_get_pair_springs: null output");
+    const int64_t n = s->P.n;
+    if (i < 0 || j < 0 || i >= n || j >= n || i == j) return lg_fail(LG_E_INVALID, "lg_get_pair_springs: bad pair");
+    for (int q = 0; q < 9; ++q) out9[q] = 0.0;
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    // an intact bond reports its bond springs
+    for (int b = 0; b < s->bv.bcap; ++b) {
+        size_t be = (size_t)b * n + i;
+        if (s->host_bond_j[be] != j) continue;
+        int8_t in = 0;
+        LG_CUDA(cudaMemcpy(&in, s->bv.intact + be, 1, cudaMemcpyDeviceToHost));
+        if (in) {
+            const size_t bs = (size_t)s->bv.bcap * n;
+            for (int q = 0; q < 9; ++q) LG_CUDA(cudaMemcpy(out9 + q, s->bv.xi + q * bs + be, sizeof(double), cudaMemcpyDeviceToHost));
+            return LG_OK;
+        }
+    }
+    const PairView &pv = s->pv[s->pcur];
+    int64_t k = -1;
+    if (s->P.pairs == LG_PAIRS_ALL) {
+        k = j < i ? j : j - 1;
+    } else {
+        int32_t len = 0;
+        LG_CUDA(cudaMemcpy(&len, pv.row_len + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        for (int64_t q = 0; q < len; ++q) {
+            int32_t jj = 0;
+            LG_CUDA(cudaMemcpy(&jj, pv.nbr + q * n + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
+            if (jj == j) {
+                k = q;
+                break;
+            }
+        }
+    }
+    if (k < 0) return LG_OK;
+    const size_t e = (size_t)(k * n + i), xs = (size_t)(pv.cap * n);
+    for (int q = 0; q < 9; ++q) LG_CUDA(cudaMemcpy(out9 + q, pv.xi + q * xs + e, sizeof(double), cudaMemcpyDeviceToHost));
+    return LG_OK;
+}
+
+extern "C" int lg_facet_update_positions(lg_system *s, int32_t facet, double dt) {
+    LG_HANDLE(s);
+    if (facet < 0 || facet >= s->P.n_facets) return lg_fail(LG_E_INVALID, "lg_facet_update_positions: bad facet");
+    double h[9];
+    LG_CUDA(cudaMemcpyAsync(h, s->fv[s->fcur] + 9 * facet, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    for (int q = 0; q < 9; ++q) h[q] = h[q] + s->P.facets[facet].v[q % 3] * dt;
+    LG_CUDA(cudaMemcpyAsync(s->fv[s->fcur] + 9 * facet, h, sizeof(h), cudaMemcpyHostToDevice, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    return LG_OK;
+}
+
+extern "C" int lg_facet_get_vertices(lg_system *s, int32_t facet, double *out9) {
+    LG_HANDLE(s);
+    if (facet < 0 || facet >= s->P.n_facets || !out9) return lg_fail(LG_E_INVALID, "lg_facet_get_vertices: bad facet");
+    LG_CUDA(cudaMemcpyAsync(out9, s->fv[s->fcur] + 9 * facet, sizeof(double) * 9, cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    return LG_OK;
+}
+
+extern "C" int lg_get_launch_count(lg_system *s, int64_t *count) {
+    if (!s || !count) return lg_fail(LG_E_INVALID, "lg_get_launch_count: null argument");
+    *count = s->launches;
+    return LG_OK;
+}

@@ -1,0 +1,475 @@
+// lg_forces_fp64.cu -- FP64 force evaluation, integration and Verlet-list kernels (sm_103a).
+//
+// Compiled with --fmad=false: a thread that walks its row in ascending j evaluates every pair with
+// the same operations, in the same order, as libgran's functors evaluated sequentially on a CPU
+// (see lg_common.cuh). One "row group" of T consecutive lanes (T in {1, 2, 4, 8, 16, 32}) owns one
+// particle i: lane l handles slots k = l, l + T, ... of row i, and the group then combines its T
+// partial sums with a fixed xor-butterfly. T = 1 reproduces the sequential sum bit for bit; larger
+// T spreads short, FP64-heavy rows (all-pairs mode on a few hundred particles) over more of the
+// GPU's FP64 units. No floating-point atomics are used anywhere: every per-particle sum is owned
+// by one row group, so results are deterministic run to run.
+#include "lg_common.cuh"
+#include "lg_kernels.h"
+
+namespace lg {
+
+// ------------------------------------------------------------------------------------------------
+// Kick + drift (first half of the rotational velocity-Verlet step):
+//   v += a*(dt/2); w += al*(dt/2); x += v*dt; th += w*dt
+// ------------------------------------------------------------------------------------------------
+__global__ void kick_drift_fp64(int64_t n, dbl4 *__restrict__ x, dbl4 *__restrict__ v,
+                                dbl4 *__restrict__ th, dbl4 *__restrict__ w, const dbl4 *__restrict__ a,
+                                const dbl4 *__restrict__ al, double dt, double hdt) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));
+    d3 wi = add(ld4(w, i), scl(hdt, ld4(al, i)));
+    st4(v, i, vi);
+    st4(w, i, wi);
+    st4(x, i, add(ld4(x, i), scl(dt, vi)));
+    st4(th, i, add(ld4(th, i), scl(dt, wi)));
+}
+
+// ------------------------------------------------------------------------------------------------
+// Pair force kernel
+// ------------------------------------------------------------------------------------------------
+template <int T>
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int T, bool VERLET>
+__global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairView PV, BondView BV, double hdt,
+                                                   double dt, int move_facets) {
+    const int64_t n = P.n;
+    const int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t i = gid / T;
+    const int lane = (int)(gid % T);
+    const bool active = i < n;
+    const int bm = P.binary_model, hm = P.hamaker_model;
+    const bool breaking = bm == LG_BINARY_BREAKING_SINTER;
+
+    if (move_facets && gid == 0) {
+        for (int f = 0; f < P.n_facets; ++f)
+            for (int q = 0; q < 9; ++q) S.facet_vert_next[9 * f + q] = S.facet_vert[9 * f + q] + P.facets[f].v[q % 3] * dt;
+    }
+
+    d3 acc = zero3(), accw = zero3();
+    d3 xi_ = zero3(), vi = zero3(), wi = zero3();
+    if (active) {
+        xi_ = ld4(S.x, i);
+        vi = ld4(S.v, i);
+        wi = ld4(S.w, i);
+        const int64_t len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
+        const int64_t stride = n;  // slot k of row i lives at k * n + i
+        for (int64_t k = lane; k < len; k += T) {
+            const int64_t e = k * stride + i;
+            const int64_t j = VERLET ? (int64_t)PV.nbr[e] : (k < i ? k : k + 1);
+            const uint32_t fl = PV.flags[e];
+            const d3 xj = ld4(S.x, j);
+            const d3 dx = sub(xi_, xj);
+            d3 pa = zero3(), pal = zero3();
+            bool have = false;
+            if (bm != LG_BINARY_NONE) {
+                have = true;
+                if (fl & kBonded) {
+                    const int b = (int)bond_slot_of(fl);
+                    const int64_t be = (int64_t)b * n + i;
+                    const int64_t bs = (int64_t)BV.bcap * n;
+                    d3 s[3];
+#pragma unroll
+                    for (int q = 0; q < 3; ++q)
+                        s[q] = mk3(BV.xi[(3 * q) * bs + be], BV.xi[(3 * q + 1) * bs + be], BV.xi[(3 * q + 2) * bs + be]);
+                    const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+                    bool brk = bond_force(P.sinter, dx, vi, vj, wi, wj, s, breaking, breaking ? BV.strength[be] : 0.0, pa,
+                                          pal);
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        BV.xi[(3 * q) * bs + be] = s[q].x;
+                        BV.xi[(3 * q + 1) * bs + be] = s[q].y;
+                        BV.xi[(3 * q + 2) * bs + be] = s[q].z;
+                    }
+                    if (brk) {
+                        BV.intact[be] = 0;
+                        PV.flags[e] = fl & ~(kBonded | (0xffu << 8));
+                    }
+                } else {
+                    const int64_t xs = PV.cap * n;
+                    bool touching = false;
+                    d3 nn = zero3();
+                    double overlap = 0.0;
+                    if (!(sqn(dx) > P.contact_skip_d2)) {
+                        nn = nrmz(dx);
+                        overlap = 2.0 * P.contact.r_part - dot(dx, nn);
+                        touching = !(overlap <= 0);
+                    }
+                    if (touching) {
+                        d3 s[3];
+#pragma unroll
+                        for (int q = 0; q < 3; ++q)
+                            s[q] = mk3(PV.xi[(3 * q) * xs + e], PV.xi[(3 * q + 1) * xs + e], PV.xi[(3 * q + 2) * xs + e]);
+                        const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+                        contact_touching(P.contact, nn, overlap, vi, vj, wi, wj, s, pa, pal);
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            PV.xi[(3 * q) * xs + e] = s[q].x;
+                            PV.xi[(3 * q + 1) * xs + e] = s[q].y;
+                            PV.xi[(3 * q + 2) * xs + e] = s[q].z;
+                        }
+                        if (!(fl & kXiLive)) PV.flags[e] = fl | kXiLive;
+                    } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+#pragma unroll
+                        for (int q = 0; q < 9; ++q) PV.xi[q * xs + e] = 0.0;
+                        PV.flags[e] = fl & ~kXiLive;
+                    }
+                }
+            }
+            if (hm != LG_HAMAKER_NONE) {
+                d3 ha = zero3();
+                bool on = true;
+                if (hm == LG_HAMAKER_LIMITED) on = !(sqn(dx) > P.hamaker_skip_d2) && !(nrm(dx) > P.hamaker.r_cutoff);
+                if (on) ha = hamaker_accel(hm, P.hamaker, sub(xj, xi_));
+                if (have) {
+                    pa = add(pa, ha);
+                    pal = add(pal, zero3());
+                } else {
+                    pa = ha;
+                    pal = zero3();
+                }
+            }
+            acc = add(acc, pa);
+            accw = add(accw, pal);
+        }
+    }
+    if (T > 1) {
+        acc.x = group_sum<T>(acc.x);
+        acc.y = group_sum<T>(acc.y);
+        acc.z = group_sum<T>(acc.z);
+        accw.x = group_sum<T>(accw.x);
+        accw.y = group_sum<T>(accw.y);
+        accw.z = group_sum<T>(accw.z);
+    }
+    if (!active || lane != 0) return;
+
+    if (P.n_facets > 0) {
+        d3 ua = zero3(), ual = zero3();
+        for (int f = 0; f < P.n_facets; ++f) {
+            const FacetDev &fd = P.facets[f];
+            d3 N = mk3(fd.normal[0], fd.normal[1], fd.normal[2]);
+            d3 xf = closest_point_on_triangle(S.facet_vert + 9 * f, fd.area, N, xi_);
+            d3 vf = mk3(fd.v[0], fd.v[1], fd.v[2]);
+            d3 fa = zero3(), fal = zero3();
+            bool hv = false;
+            if (fd.has_contact) {
+                double *sx = S.sxi;
+                const int64_t base = (int64_t)f * 9 * n;
+                d3 s[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    s[q] = mk3(sx[base + (3 * q) * n + i], sx[base + (3 * q + 1) * n + i], sx[base + (3 * q + 2) * n + i]);
+                surface_contact(fd.contact, xf, vf, xi_, vi, wi, s, fa, fal);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    sx[base + (3 * q) * n + i] = s[q].x;
+                    sx[base + (3 * q + 1) * n + i] = s[q].y;
+                    sx[base + (3 * q + 2) * n + i] = s[q].z;
+                }
+                hv = true;
+            }
+            if (fd.has_hamaker) {
+                d3 ha = surface_hamaker(fd.hamaker, xf, xi_);
+                if (hv) {
+                    fa = add(fa, ha);
+                    fal = add(fal, zero3());
+                } else {
+                    fa = ha;
+                    fal = zero3();
+                }
+            }
+            if (f == 0) {
+                ua = fa;
+                ual = fal;
+            } else {
+                ua = add(ua, fa);
+                ual = add(ual, fal);
+            }
+        }
+        acc = add(acc, ua);
+        accw = add(accw, ual);
+    }
+    st4(S.a, i, acc);
+    st4(S.al, i, accw);
+    st4(S.v_out, i, add(vi, scl(hdt, acc)));
+    st4(S.w_out, i, add(wi, scl(hdt, accw)));
+    if (!isfinite(acc.x) || !isfinite(acc.y) || !isfinite(acc.z) || !isfinite(accw.x) || !isfinite(accw.y) ||
+        !isfinite(accw.z))
+        set_error(S.err, LG_DEVERR_NONFINITE);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Verlet list: bounding box, cell grid, counting sort, row build with spring carry
+// ------------------------------------------------------------------------------------------------
+__global__ void bbox_partial(int64_t n, const dbl4 *__restrict__ x, double *__restrict__ part) {
+    __shared__ double s[6][256];
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        dbl4 q = x[i];
+        lo[0] = fmin(lo[0], q.x); lo[1] = fmin(lo[1], q.y); lo[2] = fmin(lo[2], q.z);
+        hi[0] = fmax(hi[0], q.x); hi[1] = fmax(hi[1], q.y); hi[2] = fmax(hi[2], q.z);
+    }
+    for (int c = 0; c < 3; ++c) {
+        s[c][threadIdx.x] = lo[c];
+        s[3 + c][threadIdx.x] = hi[c];
+    }
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int c = 0; c < 3; ++c) {
+                s[c][threadIdx.x] = fmin(s[c][threadIdx.x], s[c][threadIdx.x + o]);
+                s[3 + c][threadIdx.x] = fmax(s[3 + c][threadIdx.x], s[3 + c][threadIdx.x + o]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 6; ++c) part[6 * blockIdx.x + c] = s[c][0];
+}
+
+// One thread: combine the block partials and size the grid (cells of edge >= r_verlet; the edge
+// grows by 1.25 until the grid has at most max_cells cells).
+__global__ void grid_setup(int nparts, const double *__restrict__ part, double rv, int64_t max_cells, GridDev *g) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int b = 0; b < nparts; ++b)
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = fmin(lo[c], part[6 * b + c]);
+            hi[c] = fmax(hi[c], part[6 * b + 3 + c]);
+        }
+    double edge = rv;
+    int64_t dim[3];
+    for (int it = 0; it < 4096; ++it) {
+        for (int c = 0; c < 3; ++c) {
+            double m = floor((hi[c] - lo[c]) / edge) + 1.0;
+            dim[c] = m < 1.0 ? 1 : (int64_t)m;
+        }
+        double cells = (double)dim[0] * (double)dim[1] * (double)dim[2];
+        if (cells <= (double)max_cells) break;
+        edge *= 1.25;
+    }
+    double cells = (double)dim[0] * (double)dim[1] * (double)dim[2];
+    if (!(cells <= (double)max_cells) || !(edge < 1e300)) {  // non-finite positions: one cell
+        dim[0] = dim[1] = dim[2] = 1;
+        edge = 1e300;
+    }
+    for (int c = 0; c < 3; ++c) {
+        g->lo[c] = lo[c];
+        g->dim[c] = dim[c];
+    }
+    g->edge = edge;
+    g->ncell = dim[0] * dim[1] * dim[2];
+}
+
+__device__ __forceinline__ int64_t cell_coord(double q, double lo, double edge, int64_t dim) {
+    int64_t k = (int64_t)floor((q - lo) / edge);
+    return k < 0 ? 0 : (k >= dim ? dim - 1 : k);
+}
+
+__global__ void cell_count(int64_t n, const dbl4 *__restrict__ x, const GridDev *__restrict__ g,
+                           int32_t *__restrict__ cell_of, int32_t *__restrict__ count) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dbl4 q = x[i];
+    int64_t cx = cell_coord(q.x, g->lo[0], g->edge, g->dim[0]);
+    int64_t cy = cell_coord(q.y, g->lo[1], g->edge, g->dim[1]);
+    int64_t cz = cell_coord(q.z, g->lo[2], g->edge, g->dim[2]);
+    int32_t c = (int32_t)((cz * g->dim[1] + cy) * g->dim[0] + cx);
+    cell_of[i] = c;
+    atomicAdd(&count[c], 1);
+}
+
+// Exclusive scan of cell counts, single block (cells <= a few million).
+__global__ void scan_cells(const GridDev *__restrict__ g, const int32_t *__restrict__ count, int32_t *__restrict__ start) {
+    __shared__ int32_t part[1024];
+    const int64_t nc = g->ncell;
+    const int t = threadIdx.x, T = blockDim.x;
+    const int64_t per = (nc + T - 1) / T;
+    const int64_t b = (int64_t)t * per, e = b + per < nc ? b + per : nc;
+    int32_t s = 0;
+    for (int64_t c = b; c < e; ++c) s += count[c];
+    part[t] = s;
+    __syncthreads();
+    if (t == 0) {
+        int32_t run = 0;
+        for (int q = 0; q < T; ++q) {
+            int32_t v = part[q];
+            part[q] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    int32_t run = part[t];
+    for (int64_t c = b; c < e; ++c) {
+        start[c] = run;
+        run += count[c];
+    }
+}
+
+__global__ void cell_scatter(int64_t n, const int32_t *__restrict__ cell_of, const int32_t *__restrict__ start,
+                             int32_t *__restrict__ fill, int32_t *__restrict__ sorted) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t c = cell_of[i];
+    int32_t p = atomicAdd(&fill[c], 1);
+    sorted[start[c] + p] = (int32_t)i;
+}
+
+// Build row i: every j != i with squared centre distance < r_verlet^2, ascending j, carrying the
+// springs (and live flag) of pairs that were already listed, and marking intact bonds.
+__global__ void __launch_bounds__(128) build_rows(int64_t n, const dbl4 *__restrict__ x, const GridDev *__restrict__ g,
+                                                  const int32_t *__restrict__ cstart, const int32_t *__restrict__ ccount,
+                                                  const int32_t *__restrict__ sorted, double rv2, PairView oldv,
+                                                  PairView newv, BondView BV, int32_t *err) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t cap = newv.cap;
+    const d3 xi_ = ld4(x, i);
+    int64_t cx = cell_coord(xi_.x, g->lo[0], g->edge, g->dim[0]);
+    int64_t cy = cell_coord(xi_.y, g->lo[1], g->edge, g->dim[1]);
+    int64_t cz = cell_coord(xi_.z, g->lo[2], g->edge, g->dim[2]);
+    int32_t cnt = 0;
+    bool overflow = false;
+    // candidates are written straight into the new row's slots (column-major), then sorted there
+    for (int64_t z = cz - 1; z <= cz + 1; ++z) {
+        if (z < 0 || z >= g->dim[2]) continue;
+        for (int64_t y = cy - 1; y <= cy + 1; ++y) {
+            if (y < 0 || y >= g->dim[1]) continue;
+            for (int64_t xx = cx - 1; xx <= cx + 1; ++xx) {
+                if (xx < 0 || xx >= g->dim[0]) continue;
+                int64_t c = (z * g->dim[1] + y) * g->dim[0] + xx;
+                int32_t b = cstart[c], m = ccount[c];
+                for (int32_t q = 0; q < m; ++q) {
+                    int32_t j = sorted[b + q];
+                    if (j == (int32_t)i) continue;
+                    if (sqn(sub(xi_, ld4(x, j))) < rv2) {
+                        if (cnt < cap)
+                            newv.nbr[(int64_t)cnt * n + i] = j;
+                        else
+                            overflow = true;
+                        ++cnt;
+                    }
+                }
+            }
+        }
+    }
+    if (overflow) {
+        set_error(err, LG_DEVERR_LIST_OVERFLOW);
+        cnt = (int32_t)cap;
+    }
+    // insertion sort of the row (rows hold tens of entries)
+    for (int32_t a = 1; a < cnt; ++a) {
+        int32_t key = newv.nbr[(int64_t)a * n + i];
+        int32_t b = a - 1;
+        while (b >= 0 && newv.nbr[(int64_t)b * n + i] > key) {
+            newv.nbr[(int64_t)(b + 1) * n + i] = newv.nbr[(int64_t)b * n + i];
+            --b;
+        }
+        newv.nbr[(int64_t)(b + 1) * n + i] = key;
+    }
+    newv.row_len[i] = cnt;
+    // carry springs from the old row (sorted) and mark bonds
+    const int32_t olen = oldv.row_len ? oldv.row_len[i] : 0;
+    const int64_t oxs = oldv.cap * n, nxs = newv.cap * n;
+    int32_t found_bonds = 0;
+    int32_t p = 0;
+    for (int32_t k = 0; k < cnt; ++k) {
+        const int64_t e = (int64_t)k * n + i;
+        const int32_t j = newv.nbr[e];
+        uint32_t fl = 0;
+        while (p < olen && oldv.nbr[(int64_t)p * n + i] < j) ++p;
+        if (p < olen && oldv.nbr[(int64_t)p * n + i] == j) {
+            const int64_t oe = (int64_t)p * n + i;
+            const uint32_t ofl = oldv.flags[oe];
+            if (ofl & kXiLive) {
+                for (int q = 0; q < 9; ++q) newv.xi[q * nxs + e] = oldv.xi[q * oxs + oe];
+                fl |= kXiLive;
+            }
+        }
+        if (!(fl & kXiLive))
+            for (int q = 0; q < 9; ++q) newv.xi[q * nxs + e] = 0.0;
+        for (int b = 0; b < BV.bcap; ++b) {
+            const int64_t be = (int64_t)b * n + i;
+            if (BV.j[be] == j && BV.intact[be]) {
+                fl |= kBonded | ((uint32_t)b << 8);
+                ++found_bonds;
+                break;
+            }
+        }
+        newv.flags[e] = fl;
+    }
+    int32_t intact = 0;
+    for (int b = 0; b < BV.bcap; ++b)
+        if (BV.j[(int64_t)b * n + i] >= 0 && BV.intact[(int64_t)b * n + i]) ++intact;
+    if (intact != found_bonds) set_error(err, LG_DEVERR_BOND_LOST);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host-side launchers
+// ------------------------------------------------------------------------------------------------
+template <int T, bool VERLET>
+static void launch_forces_t(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                            double dt, int move_facets, cudaStream_t st) {
+    const int threads = 256;
+    const int64_t total = P.n * T;
+    const int64_t blocks = (total + threads - 1) / threads;
+    forces_fp64<T, VERLET><<<(unsigned)(blocks > 0 ? blocks : 1), threads, 0, st>>>(P, S, PV, BV, hdt, dt, move_facets);
+}
+
+void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                        double dt, int move_facets, cudaStream_t st) {
+    const bool ver = P.pairs == LG_PAIRS_VERLET;
+#define LG_CASE(TT)                                                                \
+    case TT:                                                                       \
+        if (ver)                                                                   \
+            launch_forces_t<TT, true>(P, S, PV, BV, hdt, dt, move_facets, st);     \
+        else                                                                       \
+            launch_forces_t<TT, false>(P, S, PV, BV, hdt, dt, move_facets, st);    \
+        break;
+    switch (T) {
+        LG_CASE(1)
+        LG_CASE(2)
+        LG_CASE(4)
+        LG_CASE(8)
+        LG_CASE(16)
+        LG_CASE(32)
+        default:
+            launch_forces_t<1, false>(P, S, PV, BV, hdt, dt, move_facets, st);
+    }
+#undef LG_CASE
+}
+
+void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
+                            const dbl4 *al, double dt, double hdt, cudaStream_t st) {
+    const int threads = 256;
+    int64_t blocks = (n + threads - 1) / threads;
+    if (blocks == 0) return;
+    kick_drift_fp64<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt);
+}
+
+void launch_list_build(int64_t n, const dbl4 *x, double rv, int64_t max_cells, ListScratch &ls, PairView oldv,
+                       PairView newv, BondView BV, int32_t *err, cudaStream_t st) {
+    const int nparts = ls.nparts;
+    bbox_partial<<<nparts, 256, 0, st>>>(n, x, ls.part);
+    grid_setup<<<1, 32, 0, st>>>(nparts, ls.part, rv, max_cells, ls.grid);
+    cudaMemsetAsync(ls.count, 0, sizeof(int32_t) * (size_t)max_cells, st);
+    cudaMemsetAsync(ls.fill, 0, sizeof(int32_t) * (size_t)max_cells, st);
+    const int threads = 256;
+    unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    cell_count<<<blocks, threads, 0, st>>>(n, x, ls.grid, ls.cell_of, ls.count);
+    scan_cells<<<1, 1024, 0, st>>>(ls.grid, ls.count, ls.start);
+    cell_scatter<<<blocks, threads, 0, st>>>(n, ls.cell_of, ls.start, ls.fill, ls.sorted);
+    unsigned b2 = (unsigned)((n + 127) / 128);
+    build_rows<<<b2, 128, 0, st>>>(n, x, ls.grid, ls.start, ls.count, ls.sorted, rv * rv, oldv, newv, BV, err);
+}
+
+}  // namespace lg

@@ -1,0 +1,48 @@
+// lg_kernels.h -- launchers shared between the engine host code and the kernel translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lg_common.cuh"
+
+namespace lg {
+
+struct GridDev {
+    double lo[3];
+    double edge;
+    int64_t dim[3];
+    int64_t ncell;
+};
+
+struct ListScratch {
+    int nparts;        // blocks of the bounding-box pass
+    double *part;      // [nparts * 6]
+    GridDev *grid;     // device grid description
+    int32_t *cell_of;  // [n]
+    int32_t *count;    // [max_cells]
+    int32_t *start;    // [max_cells]
+    int32_t *fill;     // [max_cells]
+    int32_t *sorted;   // [n]
+};
+
+// FP64 path (lg_forces_fp64.cu, compiled with --fmad=false)
+void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                        double dt, int move_facets, cudaStream_t st);
+void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
+                            const dbl4 *al, double dt, double hdt, cudaStream_t st);
+void launch_list_build(int64_t n, const dbl4 *x, double rv, int64_t max_cells, ListScratch &ls, PairView oldv,
+                       PairView newv, BondView BV, int32_t *err, cudaStream_t st);
+
+// Mixed-precision path (lg_forces_mixed.cu)
+bool mixed_available();
+void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
+                         double hdt, double dt, int move_facets, cudaStream_t st);
+
+// Observables (lg_reduce.cu). scratch: at least obs_scratch_doubles(n) doubles of device memory;
+// out: 20 doubles of device memory (column sums, see lg_reduce.cu).
+int64_t obs_scratch_doubles(int64_t n);
+void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
+                        double inertia, double *scratch, double *out, cudaStream_t st);
+void launch_observables_rg(int64_t n, const dbl4 *x, const double *c, double *scratch, double *out, cudaStream_t st);
+
+}  // namespace lg

@@ -1,0 +1,128 @@
+// lg_reduce.cu -- observables of the system state (test/compute_energy.cpp:7-58 and
+// test/mass_distribution.cpp:7-27 of libgran) plus the potential-energy bookkeeping used for
+// energy-balance checks. Each particle writes its terms to a scratch row; one block then reduces
+// the rows in a fixed order (strided sequential sums followed by a fixed tree), so the result is
+// identical run to run. No floating-point atomics.
+#include "lg_common.cuh"
+#include "lg_kernels.h"
+
+namespace lg {
+
+constexpr int kObs = 20;  // values per particle in the scratch rows
+
+__device__ __forceinline__ double hamaker_energy(double A, double r, double h) {
+    return -A / 6.0 *
+           (2.0 * r * r / ((4.0 * r + h) * h) + 2.0 * r * r / ((2.0 * r + h) * (2.0 * r + h)) +
+            log((4.0 * r + h) * h / ((2.0 * r + h) * (2.0 * r + h))));
+}
+
+// Per-particle terms. Column layout of a scratch row:
+//  0 e_tot  1 m|v|^2  2 I|w|^2  3-5 v  6-8 I w  9-11 x cross m v  12-14 x  15 potential energy
+//  16 contacts  17 intact bonds
+__global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double m, double I, double *__restrict__ out) {
+    const int64_t n = P.n;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const d3 v = ld4(S.v, i), w = ld4(S.w, i), x = ld4(S.x, i);
+    double *o = out + i * kObs;
+    o[0] = m * dot(v, v) / 2.0 + I * dot(w, w) / 2.0;
+    o[1] = m * dot(v, v);
+    o[2] = I * dot(w, w);
+    o[3] = v.x; o[4] = v.y; o[5] = v.z;
+    d3 Iw = scl(I, w);
+    o[6] = Iw.x; o[7] = Iw.y; o[8] = Iw.z;
+    d3 L = crs(x, scl(m, v));
+    o[9] = L.x; o[10] = L.y; o[11] = L.z;
+    o[12] = x.x; o[13] = x.y; o[14] = x.z;
+    double pe = 0.0, ncont = 0.0, nbond = 0.0;
+    const bool ver = P.pairs == LG_PAIRS_VERLET;
+    const int64_t len = ver ? (int64_t)PV.row_len[i] : n - 1;
+    const int64_t xs = PV.cap * n, bs = (int64_t)BV.bcap * n;
+    for (int64_t k = 0; k < len; ++k) {
+        const int64_t e = k * n + i;
+        const int64_t j = ver ? (int64_t)PV.nbr[e] : (k < i ? k : k + 1);
+        const uint32_t fl = PV.flags[e];
+        const double dist = nrm(sub(x, ld4(S.x, j)));
+        double u = 0.0;
+        if (fl & kBonded) {
+            const int64_t be = (int64_t)bond_slot_of(fl) * n + i;
+            double dl = 2.0 * P.sinter.r_part - dist;
+            u += 0.5 * P.sinter.k * dl * dl;
+            d3 s0 = mk3(BV.xi[0 * bs + be], BV.xi[1 * bs + be], BV.xi[2 * bs + be]);
+            d3 s1 = mk3(BV.xi[3 * bs + be], BV.xi[4 * bs + be], BV.xi[5 * bs + be]);
+            d3 s2 = mk3(BV.xi[6 * bs + be], BV.xi[7 * bs + be], BV.xi[8 * bs + be]);
+            u += 0.5 * P.sinter.k_t * sqn(s0) + 0.5 * P.sinter.k_r * sqn(s1) + 0.5 * P.sinter.k_o * sqn(s2);
+            nbond += 1.0;
+        } else if (P.binary_model != LG_BINARY_NONE) {
+            double dl = 2.0 * P.contact.r_part - dist;
+            if (dl > 0) {
+                u += 0.5 * P.contact.k * dl * dl;
+                ncont += 1.0;
+            }
+            if (fl & kXiLive) {
+                d3 s0 = mk3(PV.xi[0 * xs + e], PV.xi[1 * xs + e], PV.xi[2 * xs + e]);
+                d3 s1 = mk3(PV.xi[3 * xs + e], PV.xi[4 * xs + e], PV.xi[5 * xs + e]);
+                d3 s2 = mk3(PV.xi[6 * xs + e], PV.xi[7 * xs + e], PV.xi[8 * xs + e]);
+                u += 0.5 * P.contact.k_t * sqn(s0) + 0.5 * P.contact.k_r * sqn(s1) + 0.5 * P.contact.k_o * sqn(s2);
+            }
+        }
+        if (P.hamaker_model == LG_HAMAKER_FULL ||
+            (P.hamaker_model == LG_HAMAKER_LIMITED && !(dist > P.hamaker.r_cutoff))) {
+            double h = dist - 2.0 * P.hamaker.r_part;
+            if (h < P.hamaker.h0) h = P.hamaker.h0;
+            u += hamaker_energy(P.hamaker.A, P.hamaker.r_part, h);
+        }
+        pe += 0.5 * u;
+    }
+    o[15] = pe;
+    o[16] = ncont;
+    o[17] = nbond;
+    o[18] = 0.0;
+    o[19] = 0.0;
+}
+
+// |x - c|^2 per particle into column 18.
+__global__ void obs_rg(int64_t n, const dbl4 *__restrict__ x, double cx, double cy, double cz, double *__restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d3 q = sub(ld4(x, i), mk3(cx, cy, cz));
+    out[i * kObs + 18] = dot(q, q);
+}
+
+// One block of 1024 threads: thread t sums rows t, t + 1024, ... in order, then a fixed tree.
+__global__ void __launch_bounds__(1024) obs_reduce(int64_t n, const double *__restrict__ rows, int c0, int c1,
+                                                   double *__restrict__ out) {
+    __shared__ double s[1024];
+    for (int c = c0; c < c1; ++c) {
+        double acc = 0.0;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += rows[i * kObs + c];
+        s[threadIdx.x] = acc;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[c] = s[0];
+        __syncthreads();
+    }
+}
+
+int64_t obs_scratch_doubles(int64_t n) { return n * kObs; }
+
+// out16 receives the column sums 0..17 and, in 18, sum |x - c|^2 (c from columns 12..14). The
+// caller synchronises the stream before reading out16 (device memory).
+void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
+                        double inertia, double *scratch, double *out, cudaStream_t st) {
+    const int64_t n = P.n;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    obs_rows<<<blocks, 256, 0, st>>>(P, S, PV, BV, mass, inertia, scratch);
+    obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 0, 18, out);
+}
+
+void launch_observables_rg(int64_t n, const dbl4 *x, const double *c, double *scratch, double *out, cudaStream_t st) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    obs_rg<<<blocks, 256, 0, st>>>(n, x, c[0], c[1], c[2], scratch);
+    obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 18, 19, out);
+}
+
+}  // namespace lg

@@ -1,0 +1,130 @@
+"""Handle-level Python wrapper of the C ABI (one lg_system).
+
+This is plumbing for tests, benchmarks and the libgran-style classes in ``granular.py``; every
+call goes straight to the CUDA engine in ``_lib/liblg_gb300.so``.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _vec(a, n):
+    if a is None:
+        return np.zeros((n, 3))
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(n, 3))
+
+
+class System:
+    """One simulated system resident on a GPU."""
+
+    def __init__(self, desc, x0, v0=None, th0=None, om0=None, facets=None, neck=None, device=0):
+        L = A.lib()
+        self.n = int(desc.n_part)
+        self.desc = desc
+        self._x0 = _vec(x0, self.n)
+        v0, th0, om0 = _vec(v0, self.n), _vec(th0, self.n), _vec(om0, self.n)
+        fp = None
+        if facets:
+            self._facets = (A.lg_facet_desc * len(facets))(*facets)
+            fp = C.cast(self._facets, C.POINTER(A.lg_facet_desc))
+        neck_a = None if neck is None else np.ascontiguousarray(neck, dtype=np.float64)
+        h = C.c_void_p()
+        A.check(L.lg_create(C.byref(desc), _dp(self._x0), _dp(v0), _dp(th0), _dp(om0), fp,
+                            None if neck_a is None else _dp(neck_a), 0 if neck_a is None else len(neck_a),
+                            int(device), C.byref(h)), "lg_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            A.lib().lg_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, dt, nsteps=1, rebuild_every=0):
+        A.check(A.lib().lg_step(self.h, float(dt), int(nsteps), int(rebuild_every)), "lg_step")
+
+    def step_timed(self, dt, nsteps=1, rebuild_every=0):
+        ms = C.c_float()
+        A.check(A.lib().lg_step_timed(self.h, float(dt), int(nsteps), int(rebuild_every), C.byref(ms)),
+                "lg_step_timed")
+        return ms.value
+
+    def update_neighbor_list(self):
+        A.check(A.lib().lg_update_neighbor_list(self.h), "lg_update_neighbor_list")
+
+    def get(self, field):
+        out = np.empty((self.n, 3))
+        A.check(A.lib().lg_get(self.h, int(field), _dp(out)), "lg_get")
+        return out
+
+    def set(self, field, arr):
+        a = _vec(arr, self.n)
+        A.check(A.lib().lg_set(self.h, int(field), _dp(a)), "lg_set")
+
+    def set_threads_per_row(self, T):
+        A.check(A.lib().lg_set_threads_per_row(self.h, int(T)), "lg_set_threads_per_row")
+
+    def reset_acceleration_buffers(self):
+        A.check(A.lib().lg_reset_acceleration_buffers(self.h), "lg_reset_acceleration_buffers")
+
+    def observables(self):
+        o = A.lg_observables()
+        A.check(A.lib().lg_get_observables(self.h, C.byref(o)), "lg_get_observables")
+        return o.as_dict()
+
+    def device_errors(self):
+        e = C.c_int32()
+        A.check(A.lib().lg_get_device_errors(self.h, C.byref(e)), "lg_get_device_errors")
+        return e.value
+
+    def bonds(self):
+        L = A.lib()
+        nb = C.c_int64()
+        A.check(L.lg_get_bonds(self.h, C.byref(nb), None, 0), "lg_get_bonds")
+        arr = np.zeros(2 * max(nb.value, 1), dtype=np.int64)
+        A.check(L.lg_get_bonds(self.h, C.byref(nb), arr.ctypes.data_as(C.POINTER(C.c_int64)), nb.value),
+                "lg_get_bonds")
+        return arr[:2 * nb.value].reshape(nb.value, 2)
+
+    def springs(self, i, j):
+        out = np.zeros(9)
+        A.check(A.lib().lg_get_pair_springs(self.h, int(i), int(j), _dp(out)), "lg_get_pair_springs")
+        return out
+
+    def facet_vertices(self, f):
+        out = np.zeros(9)
+        A.check(A.lib().lg_facet_get_vertices(self.h, int(f), _dp(out)), "lg_facet_get_vertices")
+        return out
+
+    def facet_update_positions(self, f, dt):
+        A.check(A.lib().lg_facet_update_positions(self.h, int(f), float(dt)), "lg_facet_update_positions")
+
+    def launch_count(self):
+        c = C.c_int64()
+        A.check(A.lib().lg_get_launch_count(self.h, C.byref(c)), "lg_get_launch_count")
+        return c.value
+
+
+def generate_aggregate(seed, n, r):
+    """Seeded random-sequential-attachment aggregate of n spheres of radius r (host code)."""
+    x = np.zeros((int(n), 3))
+    A.check(A.lib().lg_generate_rsa_aggregate(C.c_uint64(seed), int(n), float(r), _dp(x)),
+            "lg_generate_rsa_aggregate")
+    return x
+
+
+def generate_velocities(seed, n, vmax):
+    v = np.zeros((int(n), 3))
+    A.check(A.lib().lg_generate_velocities(C.c_uint64(seed), int(n), float(vmax), _dp(v)), "lg_generate_velocities")
+    return v

@@ -1,0 +1,79 @@
+"""The C-ABI library: loads without a GPU, exports every declared entry point, rejects bad input."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from libgran_gb300 import _abi as A
+from libgran_gb300 import configs as K
+from libgran_gb300.system import generate_aggregate, generate_velocities
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names |= set(re.findall(r"\b(lg_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    L = A.lib()
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_version_and_device_count():
+    L = A.lib()
+    assert b"sm_103a" in L.lg_version()
+    c = C.c_int(-1)
+    assert L.lg_device_count(C.byref(c)) == A.LG_OK
+    assert c.value >= 0
+
+
+def _create(desc, n):
+    x = np.zeros((n, 3))
+    h = C.c_void_p()
+    p = x.ctypes.data_as(C.POINTER(C.c_double))
+    return A.lib().lg_create(C.byref(desc), p, p, p, p, None, None, 0, 0, C.byref(h)), h
+
+
+def test_create_rejects_bad_descriptors_before_touching_a_gpu():
+    mat = K.Material()
+    bad = [
+        K.make_desc(0, A.LG_BINARY_CONTACT, contact=mat.contact()),
+        K.make_desc(4, 9, contact=mat.contact()),
+        K.make_desc(4, A.LG_BINARY_NONE, A.LG_HAMAKER_NONE),
+        K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), pairs=A.LG_PAIRS_VERLET, r_verlet=0.0),
+        K.make_desc(10000, A.LG_BINARY_CONTACT, contact=mat.contact(), pairs=A.LG_PAIRS_ALL),
+        K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), n_facets=9),
+    ]
+    for d in bad:
+        rc, h = _create(d, max(int(d.n_part), 1))
+        assert rc == A.LG_E_INVALID
+        assert not h.value
+        assert len(A.lib().lg_last_error()) > 0
+
+
+def test_generator_is_seeded_and_overlap_free():
+    r = 1.4e-8
+    a = generate_aggregate(3, 400, r)
+    b = generate_aggregate(3, 400, r)
+    c = generate_aggregate(4, 400, r)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+    d = np.sqrt(((a[:, None] - a[None]) ** 2).sum(-1))
+    np.fill_diagonal(d, np.inf)
+    assert d.min() > 2 * r * (1 - 1e-9)
+    # every sphere after the first touches at least one earlier sphere
+    for k in range(1, 400):
+        assert np.isclose(d[k, :k].min(), 2 * r, rtol=1e-12)
+    v = generate_velocities(3, 400, 0.1)
+    assert np.abs(v).max() <= 0.1 and v.std() > 0.03
