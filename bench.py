@@ -1,0 +1,360 @@
+"""Benchmark of the DEM pair-force + integration path on GB300.
+
+Workload (default): one seeded random-sequential-attachment aggregate of 32768 monomers
+(r = 14 nm, rho = 1700 kg/m^3), Luding frictional contact plus limited-range Hamaker attraction
+(A = 1e-19 J, h0 = 0.4 nm, surface-gap cutoff 2r = centre distance 4r), no bonds, Verlet list of
+radius 4.5r (cutoff + 0.5r skin) rebuilt every 20 steps with spring history carried across
+rebuilds, velocity-Verlet with dt = 0.01 sqrt(m/k_n), velocities uniform in +-0.1 m/s. One bench
+step = 20 velocity-Verlet steps (one rebuild period) over all 32768 particles; the metric is
+particle-steps/s. The headline value is the mixed-precision path (FP32 pair arithmetic, FP64
+separation/overlap/springs/sums/integration); the plain FP64 path is timed in the same run.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun (N > 1) every rank runs an independent replica (the single aggregate does not
+shard without a halo exchange); value = all ranks' particle-steps / max rank time.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_PART = 32768
+VV_PER_STEP = 20
+SEED = (1 << 32) + 0
+METRIC = "particle-steps/s batched FP32/FP64 vs plain FP64 GPU at <=1e-6 rel err; p99 latency"
+
+
+def workload_desc(precision):
+    from libgran_gb300 import _abi as A
+    from libgran_gb300 import configs as K
+    mat = K.Material()
+    d = K.make_desc(N_PART, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, contact=mat.contact(), hamaker=mat.hamaker(),
+                    pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r, precision=precision, max_neighbors=96)
+    return mat, d
+
+
+def workload_state():
+    from libgran_gb300.system import generate_aggregate, generate_velocities
+    from libgran_gb300 import configs as K
+    mat = K.Material()
+    x0 = generate_aggregate(SEED, N_PART, mat.r)
+    v0 = generate_velocities(SEED, N_PART, 0.1)
+    return x0, v0
+
+
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(parts)
+            except Exception:
+                pass
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        out.update(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows))
+        return out
+
+
+def read_profile_traffic(kernel_tag):
+    """DRAM bytes per launch from the committed ncu summary of this kernel (profiles/*.md)."""
+    import glob
+    for p in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        for line in open(p):
+            if line.startswith("traffic_per_launch_bytes[%s]:" % kernel_tag):
+                try:
+                    return float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+# ------------------------------------------------------------------------------------------------
+def cpu_reference_rate(x0, v0, target_s=12.0, threads=None):
+    """The oracle (CPU restatement of libgran's path, FP64, OpenMP over all host cores) on a bounded
+    sample of the same workload: the same aggregate and parameters, timed over whole
+    20-step rebuild periods."""
+    from libgran_gb300 import _abi as A
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    mat, d = workload_desc(A.LG_PRECISION_FP64)
+    o = O.OracleSystem(d, x0, v0, threads=threads)
+    t = time.perf_counter()
+    o.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+    probe = time.perf_counter() - t
+    periods = max(1, int(target_s / max(probe, 1e-6)))
+    t = time.perf_counter()
+    o.step(mat.dt, VV_PER_STEP * periods, VV_PER_STEP)
+    el = time.perf_counter() - t
+    steps = VV_PER_STEP * periods
+    return {"value": N_PART * steps / el, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d particles x %d velocity-Verlet steps (%d rebuild periods) of the same aggregate, %.1f s"
+                      % (N_PART, steps, periods, el)}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    x0, v0 = workload_state()
+    from libgran_gb300 import _abi as A
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    mat, d = workload_desc(A.LG_PRECISION_FP64)
+    o = O.OracleSystem(d, x0, v0, threads=threads)
+    # a bounded sample per bench step keeps the whole run within a few minutes
+    probe_t = time.perf_counter()
+    o.step(mat.dt, 2, VV_PER_STEP)
+    per_vv = (time.perf_counter() - probe_t) / 2
+    vv_per_sample = max(2, min(VV_PER_STEP, int(4.0 / max(per_vv, 1e-6))))
+    for _ in range(args.warmup):
+        o.step(mat.dt, vv_per_sample, VV_PER_STEP)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        o.step(mat.dt, vv_per_sample, VV_PER_STEP)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = N_PART * vv_per_sample * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "rsa_aggregate_32768_contact_hamaker_verlet", "n_part": N_PART,
+                   "vv_steps_per_sample": vv_per_sample, "precision": "fp64", "threads": threads},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d particles x %d velocity-Verlet steps per bench step (oracle port of libgran's "
+                                   "functors and loop; libgran's own build needs its absent submodules)"
+                                   % (N_PART, vv_per_sample)},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def force_error_mixed_vs_fp64(x0, v0):
+    """Normwise relative error of the mixed-precision accelerations against FP64 at identical
+    states: the aggregate after 200 FP64 steps (contacts developed), evaluated by both paths."""
+    from libgran_gb300 import _abi as A
+    from libgran_gb300.system import System
+    mat, d64 = workload_desc(A.LG_PRECISION_FP64)
+    s = System(d64, x0, v0)
+    s.step(mat.dt, 200, VV_PER_STEP)
+    st = [s.get(f) for f in (A.LG_FIELD_X, A.LG_FIELD_V, A.LG_FIELD_THETA, A.LG_FIELD_OMEGA)]
+    s.close()
+    a = System(d64, *st)
+    _, dm = workload_desc(A.LG_PRECISION_MIXED)
+    b = System(dm, *st)
+    fa, fb = a.get(A.LG_FIELD_A), b.get(A.LG_FIELD_A)
+    ta, tb = a.get(A.LG_FIELD_ALPHA), b.get(A.LG_FIELD_ALPHA)
+    contacts = a.pair_stats()["live_contact_slots"]
+    return {"force_rel_err": float(np.abs(fa - fb).max() / np.abs(fa).max()),
+            "torque_rel_err": float(np.abs(ta - tb).max() / max(np.abs(ta).max(), 1e-300)),
+            "state": "aggregate after 200 FP64 steps, %d live contact slots" % contacts}
+
+
+def time_path(precision, x0, v0, args, l2_flush):
+    """Device-timed K bench steps (each 20 VV steps) with CUDA events on the handle's stream;
+    L2 is flushed before every timed bench step (the flush is outside the timed region)."""
+    import ctypes as C
+    from libgran_gb300 import _abi as A
+    from libgran_gb300.system import System
+    mat, d = workload_desc(precision)
+    s = System(d, x0, v0)
+    for _ in range(args.warmup):
+        s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+    s.enable_kernel_timing(True)
+    s.force_kernel_time()
+    l0 = s.launch_count()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        l2_flush()
+        total_ms += s.step_timed(mat.dt, VV_PER_STEP, VV_PER_STEP)
+    launches = s.launch_count() - l0
+    kms, kcount = s.force_kernel_time()
+    s.enable_kernel_timing(False)
+    stats = s.pair_stats()
+    errs = s.device_errors()
+    return s, mat, {"ms": total_ms, "launches": launches, "kernel_ms": kms, "kernel_launches": kcount,
+                    "pair_stats": stats, "device_errors": errs}
+
+
+def e2e_path(s, mat, args, x0, v0):
+    """Same metric through the public API with host buffers: every bench step uploads the state
+    (x, v, theta, omega) from pinned host memory, runs 20 VV steps and reads back the state and
+    the observables; host<->device copies are inside the timed region."""
+    import torch
+    from libgran_gb300 import _abi as A
+    fields = (A.LG_FIELD_X, A.LG_FIELD_V, A.LG_FIELD_THETA, A.LG_FIELD_OMEGA)
+    host = {f: torch.from_numpy(np.ascontiguousarray(s.get(f))).pin_memory() for f in fields}
+    times = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for f in fields:
+            s.set(f, host[f].numpy())
+        s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+        for f in fields:
+            host[f].numpy()[:] = s.get(f)
+        obs = s.observables()
+        t = time.perf_counter() - t
+        if k >= args.warmup:
+            times.append(t)
+    h2d = 4 * N_PART * 3 * 8
+    d2h = 4 * N_PART * 3 * 8 + 8 * 20
+    return {"value": N_PART * VV_PER_STEP * len(times) / sum(times), "unit": "particle-steps/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}, obs
+
+
+def run_gb300(args, rank, world):
+    import torch
+    from libgran_gb300 import _abi as A
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    x0, v0 = workload_state()
+    flush_buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def l2_flush():
+        flush_buf.fill_(1.0)
+        torch.cuda.synchronize()
+
+    # plain FP64 first (its number is reported beside the headline)
+    s64, mat, t64 = time_path(A.LG_PRECISION_FP64, x0, v0, args, l2_flush)
+    s64.close()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    sm, mat, tm = time_path(A.LG_PRECISION_MIXED, x0, v0, args, l2_flush)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+        t = torch.tensor([tm["ms"], t64["ms"]], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tm["ms"], t64["ms"] = float(t[0]), float(t[1])
+    units = N_PART * VV_PER_STEP * args.steps
+    value = world * units / (tm["ms"] / 1e3)
+    value64 = world * units / (t64["ms"] / 1e3)
+    e2e, obs = e2e_path(sm, mat, args, x0, v0)
+    e2e["value"] *= world
+    sm.close()
+    if rank != 0:
+        return
+    acc = force_error_mixed_vs_fp64(x0, v0)
+    # roofline of the dominant kernel (mixed force kernel)
+    ps = tm["pair_stats"]
+    z_list = ps["mean_row_length"]
+    z_act = (ps["live_contact_slots"] + ps["bonded_slots"]) / N_PART
+    bytes_per_particle = 168.0 + 4.0 * z_list + 144.0 * z_act
+    per_launch_ms = tm["kernel_ms"] / max(tm["kernel_launches"], 1)
+    achieved = bytes_per_particle * N_PART / (per_launch_ms / 1e3) / 1e9
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = read_profile_traffic("forces_mixed_c1")
+    cpu = cpu_reference_rate(x0, v0, target_s=float(os.environ.get("LG_CPU_SAMPLE_S", "12")))
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": tm["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "rsa_aggregate_32768_contact_hamaker_verlet", "n_part": N_PART,
+                   "vv_steps_per_step": VV_PER_STEP, "rebuild_every": VV_PER_STEP, "r_verlet": "4.5r",
+                   "hamaker_cutoff": "centre distance 4r (surface gap 2r)", "precision": "mixed",
+                   "l2": "flushed (512 MiB write) before every timed step", "parallelism": "replicas" if world > 1
+                   else "single GPU"},
+        "plain_fp64": {"value": value64, "unit": "particle-steps/s", "ms_per_step": t64["ms"] / args.steps,
+                       "force_kernel_ms_per_launch": t64["kernel_ms"] / max(t64["kernel_launches"], 1)},
+        "mixed_over_fp64": value / value64,
+        "accuracy": acc,
+        "e2e": e2e,
+        "gpu_launches": tm["launches"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "forces_mixed", "bytes_per_particle": bytes_per_particle,
+                     "per_launch_ms": per_launch_ms, "peak_source": "measured" if peaks else "fallback"},
+        "cpu_baseline": cpu,
+        "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
+        "device_errors": tm["device_errors"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+    run_gb300(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -125,6 +125,8 @@ typedef struct lg_system_desc {
     int32_t n_facets;        /* number of lg_facet_desc passed to lg_create */
     int32_t facet_auto_move; /* 1: move every facet by v_facet*dt after each step */
     int32_t max_neighbors;   /* Verlet list row capacity; 0 picks a default */
+    int32_t threads_per_row; /* lanes per row group of the force kernel (see lg_set_threads_per_row);
+                                0 picks automatically; used from the construction-time evaluation on */
 } lg_system_desc;
 
 /* Fields that lg_get / lg_set move. */
@@ -222,6 +224,22 @@ int lg_facet_get_vertices(lg_system *sys, int32_t facet, double *out9);
 
 /* Number of CUDA kernel launches issued by this handle since creation (diagnostics). */
 int lg_get_launch_count(lg_system *sys, int64_t *count);
+
+/* Pair-slot statistics of the current pair data: mean and maximum row length (all-pairs mode: n-1),
+ * and the number of ordered pairs whose contact springs are live or that are intact bonds. */
+typedef struct lg_pair_stats {
+    double mean_row_length;
+    int64_t max_row_length;
+    int64_t live_contact_slots;
+    int64_t bonded_slots;
+} lg_pair_stats;
+int lg_get_pair_stats(lg_system *sys, lg_pair_stats *out);
+
+/* Kernel timing: while enabled, every force-kernel launch is bracketed by CUDA events on the
+ * handle's stream; lg_get_force_kernel_time returns the summed device time (ms) and the number of
+ * launches timed since the last reset (the call synchronises and resets the counters). */
+int lg_enable_kernel_timing(lg_system *sys, int32_t enable);
+int lg_get_force_kernel_time(lg_system *sys, double *ms_total, int64_t *launches);
 
 /* Lanes per row group of the force kernel: 1 walks each row sequentially (the reference's summation
  * order), 2..32 split a row across lanes and combine the partial sums with a fixed butterfly

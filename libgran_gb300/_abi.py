@@ -41,12 +41,17 @@ class lg_facet_desc(C.Structure):
                 ("contact", lg_contact_params), ("hamaker", lg_hamaker_params)]
 
 
+class lg_pair_stats(C.Structure):
+    _fields_ = [("mean_row_length", C.c_double), ("max_row_length", C.c_int64),
+                ("live_contact_slots", C.c_int64), ("bonded_slots", C.c_int64)]
+
+
 class lg_system_desc(C.Structure):
     _fields_ = [("n_part", C.c_int64), ("binary_model", C.c_int32), ("hamaker_model", C.c_int32),
                 ("contact", lg_contact_params), ("sinter", lg_sinter_params),
                 ("hamaker", lg_hamaker_params), ("neck_mode", C.c_int32), ("pairs", C.c_int32),
                 ("r_verlet", C.c_double), ("precision", C.c_int32), ("n_facets", C.c_int32),
-                ("facet_auto_move", C.c_int32), ("max_neighbors", C.c_int32)]
+                ("facet_auto_move", C.c_int32), ("max_neighbors", C.c_int32), ("threads_per_row", C.c_int32)]
 
 
 class lg_observables(C.Structure):
@@ -110,6 +115,9 @@ def _declare(L):
         "lg_facet_get_vertices": (C.c_int, [vp, i32, P(d)]),
         "lg_get_launch_count": (C.c_int, [vp, P(i64)]),
         "lg_set_threads_per_row": (C.c_int, [vp, i32]),
+        "lg_get_pair_stats": (C.c_int, [vp, P(lg_pair_stats)]),
+        "lg_enable_kernel_timing": (C.c_int, [vp, i32]),
+        "lg_get_force_kernel_time": (C.c_int, [vp, P(d), P(i64)]),
         "lg_generate_rsa_aggregate": (C.c_int, [C.c_uint64, i64, d, P(d)]),
         "lg_generate_velocities": (C.c_int, [C.c_uint64, i64, d, P(d)]),
     }

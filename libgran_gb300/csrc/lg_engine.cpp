@@ -271,6 +271,8 @@ void lg_system::release() {
     if (stream) cudaStreamDestroy(stream);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    for (cudaEvent_t e : tev) cudaEventDestroy(e);
+    tev.clear();
     stream = nullptr;
 }
 
@@ -324,12 +326,26 @@ static StateView state_view(lg_system *s, bool half_step_inputs) {
 
 static int launch_forces(lg_system *s, double hdt, double dt, int move_facets) {
     StateView S = state_view(s, true);
+    cudaEvent_t stop_ev = nullptr;
+    if (s->timing) {
+        if (s->tev_used + 2 > s->tev.size()) {
+            for (int q = 0; q < 64; ++q) {
+                cudaEvent_t e;
+                LG_CUDA(cudaEventCreate(&e));
+                s->tev.push_back(e);
+            }
+        }
+        LG_CUDA(cudaEventRecord(s->tev[s->tev_used], s->stream));
+        stop_ev = s->tev[s->tev_used + 1];
+        s->tev_used += 2;
+    }
     if (s->precision == LG_PRECISION_MIXED)
-        launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
+        launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
     else
         launch_forces_fp64(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
     s->launches += 1;
     LG_CUDA(cudaGetLastError());
+    if (stop_ev) LG_CUDA(cudaEventRecord(stop_ev, s->stream));
     return LG_OK;
 }
 
@@ -337,7 +353,11 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every) {
     if (s->P.pairs == LG_PAIRS_VERLET && rebuild_every > 0 && (s->step_index % rebuild_every) == 0)
         LG_TRY(rebuild_list(s));
     const double hdt = dt / 2.0;
-    launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->stream);
+    if (s->precision == LG_PRECISION_MIXED)
+        launch_kick_drift_mixed(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->origin,
+                                s->x32, s->stream);
+    else
+        launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->stream);
     s->launches += 1;
     const int mv = (s->facet_auto_move && s->P.n_facets > 0) ? 1 : 0;
     LG_TRY(launch_forces(s, hdt, dt, mv));
@@ -363,6 +383,11 @@ static int check_args(const lg_system_desc *d) {
     if (d->n_facets < 0 || d->n_facets > kMaxFacets) return lg_fail(LG_E_INVALID, "lg_create: n_facets %d out of range [0, %d]", d->n_facets, kMaxFacets);
     if (d->neck_mode != LG_NECK_PER_BOND && d->neck_mode != LG_NECK_REFERENCE_INDEXING) return lg_fail(LG_E_INVALID, "lg_create: unknown neck_mode %d", d->neck_mode);
     if (d->max_neighbors < 0) return lg_fail(LG_E_INVALID, "lg_create: max_neighbors < 0");
+    {
+        int T = d->threads_per_row;
+        if (T != 0 && T != 1 && T != 2 && T != 4 && T != 8 && T != 16 && T != 32)
+            return lg_fail(LG_E_INVALID, "lg_create: threads_per_row must be 0 or a power of two <= 32");
+    }
     return LG_OK;
 }
 
@@ -553,7 +578,25 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     LG_TRY(s->alloc(&s->obs_scratch, (size_t)obs_scratch_doubles(n)));
     LG_TRY(s->alloc(&s->obs_out, 32));
 
-    s->T = choose_threads_per_row(s);
+    if (s->precision == LG_PRECISION_MIXED) {
+        for (int c = 0; c < 3; ++c) {
+            double sum = 0.0;
+            for (int64_t i = 0; i < n; ++i) sum += x0[3 * i + c];
+            s->origin[c] = sum / (double)n;
+        }
+        LG_TRY(s->alloc(&s->x32, (size_t)n));
+        launch_positions_to_f32(n, s->x, s->origin, s->x32, s->stream);
+        double near = 0.0;
+        if (d->binary_model != LG_BINARY_NONE) near = std::max(near, 2.0 * d->contact.r_part);
+        if (sinter) near = std::max(near, 2.0 * d->sinter.r_part);
+        if (d->hamaker_model == LG_HAMAKER_LIMITED) near = std::max(near, d->hamaker.r_cutoff);
+        if (d->hamaker_model == LG_HAMAKER_FULL || d->hamaker_model == LG_HAMAKER_SIMPLIFIED)
+            near = std::max(near, 7.0 * d->hamaker.r_part);
+        s->mx.x32 = s->x32;
+        s->mx.near2 = (float)(near * near * 1.004);
+        s->mx.rcut2 = d->hamaker.r_cutoff * d->hamaker.r_cutoff;
+    }
+    s->T = d->threads_per_row > 0 ? d->threads_per_row : choose_threads_per_row(s);
     // initial accelerations (the first half kick needs them); velocities are unchanged (hdt = 0)
     LG_TRY(launch_forces(s, 0.0, 0.0, 0));
     LG_CUDA(cudaStreamSynchronize(s->stream));
@@ -640,7 +683,13 @@ extern "C" int lg_set(lg_system *s, int field, const double *in) {
     LG_HANDLE(s);
     dbl4 *p = field_ptr(s, field);
     if (!p || !in) return lg_fail(LG_E_INVALID, "lg_set: bad field %d or null input", field);
-    return upload4(p, in, s->P.n, s->stream);
+    LG_TRY(upload4(p, in, s->P.n, s->stream));
+    if (field == LG_FIELD_X && s->x32) {
+        launch_positions_to_f32(s->P.n, s->x, s->origin, s->x32, s->stream);
+        s->launches += 1;
+        LG_CUDA(cudaGetLastError());
+    }
+    return LG_OK;
 }
 
 extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
@@ -806,5 +855,58 @@ extern "C" int lg_facet_get_vertices(lg_system *s, int32_t facet, double *out9) 
 extern "C" int lg_get_launch_count(lg_system *s, int64_t *count) {
     if (!s || !count) return lg_fail(LG_E_INVALID, "lg_get_launch_count: null argument");
     *count = s->launches;
+    return LG_OK;
+}
+
+extern "C" int lg_enable_kernel_timing(lg_system *s, int32_t enable) {
+    LG_HANDLE(s);
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    s->timing = enable != 0;
+    s->tev_used = 0;
+    return LG_OK;
+}
+
+extern "C" int lg_get_force_kernel_time(lg_system *s, double *ms_total, int64_t *launches) {
+    LG_HANDLE(s);
+    if (!ms_total || !launches) return lg_fail(LG_E_INVALID, "lg_get_force_kernel_time: null output");
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    double tot = 0.0;
+    for (size_t q = 0; q + 1 < s->tev_used; q += 2) {
+        float ms = 0.f;
+        LG_CUDA(cudaEventElapsedTime(&ms, s->tev[q], s->tev[q + 1]));
+        tot += ms;
+    }
+    *ms_total = tot;
+    *launches = (int64_t)(s->tev_used / 2);
+    s->tev_used = 0;
+    return LG_OK;
+}
+
+extern "C" int lg_get_pair_stats(lg_system *s, lg_pair_stats *out) {
+    LG_HANDLE(s);
+    if (!out) return lg_fail(LG_E_INVALID, "lg_get_pair_stats: null output");
+    const int64_t n = s->P.n;
+    const PairView &pv = s->pv[s->pcur];
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    std::vector<int32_t> len((size_t)n, (int32_t)(n - 1));
+    if (s->P.pairs == LG_PAIRS_VERLET)
+        LG_CUDA(cudaMemcpy(len.data(), pv.row_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> fl((size_t)(pv.cap * n));
+    LG_CUDA(cudaMemcpy(fl.data(), pv.flags, sizeof(uint32_t) * fl.size(), cudaMemcpyDeviceToHost));
+    double sum = 0.0;
+    int64_t mx = 0, live = 0, bonded = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        sum += len[i];
+        mx = std::max<int64_t>(mx, len[i]);
+        for (int64_t k = 0; k < len[i]; ++k) {
+            uint32_t f = fl[(size_t)(k * n + i)];
+            if (f & kBonded) ++bonded;
+            else if (f & kXiLive) ++live;
+        }
+    }
+    out->mean_row_length = sum / (double)n;
+    out->max_row_length = mx;
+    out->live_contact_slots = live;
+    out->bonded_slots = bonded;
     return LG_OK;
 }

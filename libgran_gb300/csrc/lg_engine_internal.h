@@ -39,6 +39,16 @@ struct lg_system {
     double *obs_scratch = nullptr;
     double *obs_out = nullptr;
 
+    // mixed precision: FP32 position copy for culling
+    float4 *x32 = nullptr;
+    double origin[3] = {0.0, 0.0, 0.0};
+    lg::MixedExtra mx{};
+
+    // force-kernel timing (bench instrumentation)
+    bool timing = false;
+    std::vector<cudaEvent_t> tev;  // pairs: start, stop
+    size_t tev_used = 0;
+
     int T = 1;  // lanes per row group of the force kernel
     int64_t step_index = 0;
     int64_t launches = 0;

@@ -34,9 +34,18 @@ void launch_list_build(int64_t n, const dbl4 *x, double rv, int64_t max_cells, L
                        PairView newv, BondView BV, int32_t *err, cudaStream_t st);
 
 // Mixed-precision path (lg_forces_mixed.cu)
+struct MixedExtra {
+    float4 *x32;   // [n] FP32 positions relative to the system origin (culling only)
+    float near2;   // squared culling radius (FP32 positions); beyond it a pair cannot touch and the
+                   // limited Hamaker force is zero
+    double rcut2;  // squared limited-Hamaker cutoff (FP64 separation)
+};
 bool mixed_available();
 void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
-                         double hdt, double dt, int move_facets, cudaStream_t st);
+                         double hdt, double dt, int move_facets, const MixedExtra &MX, cudaStream_t st);
+void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, float4 *x32, cudaStream_t st);
+void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
+                             double hdt, const double *origin, float4 *x32, cudaStream_t st);
 
 // Observables (lg_reduce.cu). scratch: at least obs_scratch_doubles(n) doubles of device memory;
 // out: 20 doubles of device memory (column sums, see lg_reduce.cu).

@@ -110,6 +110,20 @@ class System:
     def facet_update_positions(self, f, dt):
         A.check(A.lib().lg_facet_update_positions(self.h, int(f), float(dt)), "lg_facet_update_positions")
 
+    def pair_stats(self):
+        st = A.lg_pair_stats()
+        A.check(A.lib().lg_get_pair_stats(self.h, C.byref(st)), "lg_get_pair_stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def enable_kernel_timing(self, on=True):
+        A.check(A.lib().lg_enable_kernel_timing(self.h, 1 if on else 0), "lg_enable_kernel_timing")
+
+    def force_kernel_time(self):
+        ms = C.c_double()
+        cnt = C.c_int64()
+        A.check(A.lib().lg_get_force_kernel_time(self.h, C.byref(ms), C.byref(cnt)), "lg_get_force_kernel_time")
+        return ms.value, cnt.value
+
     def launch_count(self):
         c = C.c_int64()
         A.check(A.lib().lg_get_launch_count(self.h, C.byref(c)), "lg_get_launch_count")

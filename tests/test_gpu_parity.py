@@ -27,8 +27,8 @@ POS_TOL = 1e-9
 def test_gpu_reproduces_golden_sequential_rows(path):
     g = np.load(path)
     case = H.golden_case(os.path.basename(path)[:-4])
+    case["desc"].threads_per_row = 1
     s = System(case["desc"], g["x0"], g["v0"], facets=case.get("facets"), neck=case.get("neck"))
-    s.set_threads_per_row(1)
     worst = {}
 
     def check(f, cp, got, want):
@@ -48,8 +48,8 @@ def test_gpu_reproduces_golden_sequential_rows(path):
 def test_gpu_sequential_rows_are_bit_exact_with_oracle(path):
     g = np.load(path)
     case = H.golden_case(os.path.basename(path)[:-4])
+    case["desc"].threads_per_row = 1
     s = System(case["desc"], g["x0"], g["v0"], facets=case.get("facets"), neck=case.get("neck"))
-    s.set_threads_per_row(1)
     o = O.OracleSystem(case["desc"], g["x0"], g["v0"], facets=case.get("facets"), neck=case.get("neck"))
     for nst in (1, 9, 90):
         s.step(case["dt"], nst, case.get("rebuild", 0))
@@ -76,8 +76,8 @@ def test_all_pairs_forces_and_positions(T, bm, hm):
     if bm == A.LG_BINARY_BREAKING_SINTER:
         probe = O.OracleSystem(d, x0, v0)
         nb = np.full(len(probe.bonds()) // 2, 2e-9)
+    d.threads_per_row = T
     s = System(d, x0, v0, neck=nb)
-    s.set_threads_per_row(T)
     o = O.OracleSystem(d, x0, v0, neck=nb, threads=4)
     for step in range(1, 101):
         s.step(mat.dt, 1)
@@ -96,8 +96,8 @@ def test_all_pairs_forces_and_positions(T, bm, hm):
 def test_verlet_list_with_spring_carry(T):
     mat, d, x0, v0 = _aggregate_system(2000, 33, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET,
                                        squeeze=3e7)
+    d.threads_per_row = T
     s = System(d, x0, v0)
-    s.set_threads_per_row(T)
     o = O.OracleSystem(d, x0, v0, threads=8)
     for k in range(5):
         s.step(mat.dt, 20, 20)
@@ -135,8 +135,8 @@ def test_results_are_deterministic():
     mat, d, x0, v0 = _aggregate_system(3000, 4, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET)
     outs = []
     for _ in range(2):
+        d.threads_per_row = 4
         s = System(d, x0, v0)
-        s.set_threads_per_row(4)
         s.step(mat.dt, 60, 20)
         outs.append([s.get(f) for f in H.FIELDS])
     for a, b in zip(*outs):
