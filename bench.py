@@ -341,8 +341,26 @@ def run_gb300(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    """Profiling driver (no timing output): build the workload and run --warmup + --steps bench
+    steps of one path, so that ncu can capture its kernels."""
+    import torch
+    from libgran_gb300 import _abi as A
+    from libgran_gb300.system import System
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    prec = A.LG_PRECISION_MIXED if args.profile == "mixed" else A.LG_PRECISION_FP64
+    x0, v0 = workload_state()
+    mat, d = workload_desc(prec)
+    s = System(d, x0, v0)
+    s.step(mat.dt, VV_PER_STEP * (args.warmup + args.steps), VV_PER_STEP)
+    print(json.dumps({"profile": args.profile, "vv_steps": VV_PER_STEP * (args.warmup + args.steps),
+                      "device_errors": s.device_errors(), "launches": s.launch_count()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--profile", default=None, choices=[None, "mixed", "fp64"],
+                    help="profiling driver: run one path without timing")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -350,6 +368,9 @@ def main():
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    if args.profile:
+        run_profile(args)
+        return
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
         return

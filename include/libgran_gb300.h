@@ -127,7 +127,15 @@ typedef struct lg_system_desc {
     int32_t max_neighbors;   /* Verlet list row capacity; 0 picks a default */
     int32_t threads_per_row; /* lanes per row group of the force kernel (see lg_set_threads_per_row);
                                 0 picks automatically; used from the construction-time evaluation on */
+    int32_t force_kernel;    /* LG_FORCE_KERNEL_*: which force kernel evaluates the pairs */
 } lg_system_desc;
+
+/* Force kernels. Both give deterministic sums; in FP64 both add each row in ascending j, and the
+ * compacted kernel and the row-group kernel with one lane per row are bit-identical to a
+ * sequential evaluation of libgran's functors. */
+#define LG_FORCE_KERNEL_AUTO 0       /* compacted for large systems, row groups for small ones */
+#define LG_FORCE_KERNEL_ROWGROUP 1   /* T lanes per row (threads_per_row), fixed butterfly combine */
+#define LG_FORCE_KERNEL_COMPACT 2    /* one row per lane, warp-compacted pair queues (see csrc) */
 
 /* Fields that lg_get / lg_set move. */
 #define LG_FIELD_X 0       /* positions            get_x()     Granular-system.md:84-120 */
@@ -245,6 +253,9 @@ int lg_get_force_kernel_time(lg_system *sys, double *ms_total, int64_t *launches
  * order), 2..32 split a row across lanes and combine the partial sums with a fixed butterfly
  * (deterministic, different rounding). 0 restores the automatic choice. */
 int lg_set_threads_per_row(lg_system *sys, int32_t threads_per_row);
+
+/* Select the force kernel (LG_FORCE_KERNEL_*) for the following steps. */
+int lg_set_force_kernel(lg_system *sys, int32_t force_kernel);
 
 /* Seeded synthetic aggregate: random sequential attachment of n spheres of radius r (each new sphere
  * touches a uniformly chosen existing one in a uniformly random direction; a candidate that overlaps

@@ -15,6 +15,7 @@ LG_HAMAKER_NONE, LG_HAMAKER_FULL, LG_HAMAKER_LIMITED, LG_HAMAKER_SIMPLIFIED = 0,
 LG_NECK_PER_BOND, LG_NECK_REFERENCE_INDEXING = 0, 1
 LG_PRECISION_FP64, LG_PRECISION_MIXED = 0, 1
 LG_PAIRS_ALL, LG_PAIRS_VERLET = 0, 1
+LG_FORCE_KERNEL_AUTO, LG_FORCE_KERNEL_ROWGROUP, LG_FORCE_KERNEL_COMPACT = 0, 1, 2
 LG_FIELD_X, LG_FIELD_V, LG_FIELD_THETA, LG_FIELD_OMEGA, LG_FIELD_A, LG_FIELD_ALPHA = range(6)
 LG_DEVERR_LIST_OVERFLOW, LG_DEVERR_NONFINITE, LG_DEVERR_BOND_LOST = 1, 2, 4
 
@@ -51,7 +52,8 @@ class lg_system_desc(C.Structure):
                 ("contact", lg_contact_params), ("sinter", lg_sinter_params),
                 ("hamaker", lg_hamaker_params), ("neck_mode", C.c_int32), ("pairs", C.c_int32),
                 ("r_verlet", C.c_double), ("precision", C.c_int32), ("n_facets", C.c_int32),
-                ("facet_auto_move", C.c_int32), ("max_neighbors", C.c_int32), ("threads_per_row", C.c_int32)]
+                ("facet_auto_move", C.c_int32), ("max_neighbors", C.c_int32), ("threads_per_row", C.c_int32),
+                ("force_kernel", C.c_int32)]
 
 
 class lg_observables(C.Structure):
@@ -115,6 +117,7 @@ def _declare(L):
         "lg_facet_get_vertices": (C.c_int, [vp, i32, P(d)]),
         "lg_get_launch_count": (C.c_int, [vp, P(i64)]),
         "lg_set_threads_per_row": (C.c_int, [vp, i32]),
+        "lg_set_force_kernel": (C.c_int, [vp, i32]),
         "lg_get_pair_stats": (C.c_int, [vp, P(lg_pair_stats)]),
         "lg_enable_kernel_timing": (C.c_int, [vp, i32]),
         "lg_get_force_kernel_time": (C.c_int, [vp, P(d), P(i64)]),

@@ -43,7 +43,8 @@ def hamaker_params(A_, h0, r_part, mass, r_cutoff=0.0):
 
 def make_desc(n_part, binary_model=A.LG_BINARY_CONTACT, hamaker_model=A.LG_HAMAKER_NONE, contact=None,
               sinter=None, hamaker=None, neck_mode=A.LG_NECK_PER_BOND, pairs=A.LG_PAIRS_ALL, r_verlet=0.0,
-              precision=A.LG_PRECISION_FP64, n_facets=0, facet_auto_move=0, max_neighbors=0, threads_per_row=0):
+              precision=A.LG_PRECISION_FP64, n_facets=0, facet_auto_move=0, max_neighbors=0, threads_per_row=0,
+              force_kernel=A.LG_FORCE_KERNEL_AUTO):
     d = A.lg_system_desc()
     d.n_part = int(n_part)
     d.binary_model = binary_model
@@ -62,6 +63,7 @@ def make_desc(n_part, binary_model=A.LG_BINARY_CONTACT, hamaker_model=A.LG_HAMAK
     d.facet_auto_move = facet_auto_move
     d.max_neighbors = max_neighbors
     d.threads_per_row = threads_per_row
+    d.force_kernel = force_kernel
     return d
 
 

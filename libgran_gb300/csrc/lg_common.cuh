@@ -234,6 +234,23 @@ __device__ __forceinline__ d3 hamaker_accel(int mode, const lg_hamaker_params &p
     return dvs(scl(s, nrmz(r)), p.mass);
 }
 
+// As hamaker_accel, with rn = nrm(r) already computed (the same value nrm() and nrmz() would compute).
+__device__ __forceinline__ d3 hamaker_accel_n(int mode, const lg_hamaker_params &p, d3 r, double rn) {
+    double h = rn - 2.0 * p.r_part;
+    if (h < p.h0) h = p.h0;
+    double rp = p.r_part;
+    double s;
+    if (mode == LG_HAMAKER_SIMPLIFIED) {
+        s = 2.0 * p.A * rp / sq_(h);
+    } else {
+        double br = (4.0 * rp + 2.0 * h) / (4.0 * rp + h) / h - 2.0 / (2.0 * rp + h) - 4.0 * sq_(rp) / cb_(2.0 * rp + h) -
+                    2.0 * sq_(rp) * (4.0 * rp + 2.0 * h) / sq_(4.0 * rp + h) / sq_(h);
+        s = -p.A / 6.0 * br;
+    }
+    d3 u = (rn > 0.0) ? dvs(r, rn) : r;  // nrmz(r)
+    return dvs(scl(s, u), p.mass);
+}
+
 // triangular_facet.h:73-137
 __device__ __forceinline__ d3 closest_point_on_triangle(const double *vt, double area, d3 N, d3 p) {
     d3 v0 = mk3(vt[0], vt[1], vt[2]), v1 = mk3(vt[3], vt[4], vt[5]), v2 = mk3(vt[6], vt[7], vt[8]);

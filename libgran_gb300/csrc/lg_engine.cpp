@@ -283,6 +283,13 @@ int lg_system::alloc(U **p, size_t count) {
     return LG_OK;
 }
 
+static int choose_kernel(const lg_system *s, int requested) {
+    if (requested == LG_FORCE_KERNEL_ROWGROUP || requested == LG_FORCE_KERNEL_COMPACT) return requested;
+    const int64_t n = s->P.n;
+    if (s->P.pairs == LG_PAIRS_VERLET ? n >= 1024 : n >= 4096) return LG_FORCE_KERNEL_COMPACT;
+    return LG_FORCE_KERNEL_ROWGROUP;
+}
+
 static int choose_threads_per_row(const lg_system *s) {
     const int64_t n = s->P.n;
     const int64_t want = 152 * 1024;
@@ -339,10 +346,18 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets) {
         stop_ev = s->tev[s->tev_used + 1];
         s->tev_used += 2;
     }
-    if (s->precision == LG_PRECISION_MIXED)
-        launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
-    else
-        launch_forces_fp64(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
+    const bool compact = s->kernel == LG_FORCE_KERNEL_COMPACT;
+    if (s->precision == LG_PRECISION_MIXED) {
+        if (compact)
+            launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
+        else
+            launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
+    } else {
+        if (compact)
+            launch_forces_compact_fp64(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
+        else
+            launch_forces_fp64(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
+    }
     s->launches += 1;
     LG_CUDA(cudaGetLastError());
     if (stop_ev) LG_CUDA(cudaEventRecord(stop_ev, s->stream));
@@ -382,7 +397,9 @@ static int check_args(const lg_system_desc *d) {
     if (d->precision == LG_PRECISION_MIXED && !lg::mixed_available()) return lg_fail(LG_E_INVALID, "lg_create: mixed precision is not built in this library");
     if (d->n_facets < 0 || d->n_facets > kMaxFacets) return lg_fail(LG_E_INVALID, "lg_create: n_facets %d out of range [0, %d]", d->n_facets, kMaxFacets);
     if (d->neck_mode != LG_NECK_PER_BOND && d->neck_mode != LG_NECK_REFERENCE_INDEXING) return lg_fail(LG_E_INVALID, "lg_create: unknown neck_mode %d", d->neck_mode);
-    if (d->max_neighbors < 0) return lg_fail(LG_E_INVALID, "lg_create: max_neighbors < 0");
+    if (d->max_neighbors < 0 || d->max_neighbors > 255)
+        return lg_fail(LG_E_INVALID, "lg_create: max_neighbors must be in [0, 255]");
+    if (d->force_kernel < 0 || d->force_kernel > 2) return lg_fail(LG_E_INVALID, "lg_create: unknown force_kernel %d", d->force_kernel);
     {
         int T = d->threads_per_row;
         if (T != 0 && T != 1 && T != 2 && T != 4 && T != 8 && T != 16 && T != 32)
@@ -573,6 +590,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         LG_TRY(s->alloc(&s->ls.start, (size_t)s->max_cells));
         LG_TRY(s->alloc(&s->ls.fill, (size_t)s->max_cells));
         LG_TRY(s->alloc(&s->ls.sorted, (size_t)n));
+        LG_TRY(s->alloc(&s->ls.x32, (size_t)n));
         LG_TRY(rebuild_list(s));
     }
     LG_TRY(s->alloc(&s->obs_scratch, (size_t)obs_scratch_doubles(n)));
@@ -594,9 +612,34 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
             near = std::max(near, 7.0 * d->hamaker.r_part);
         s->mx.x32 = s->x32;
         s->mx.near2 = (float)(near * near * 1.004);
+        double cnear = 0.0;
+        if (d->binary_model != LG_BINARY_NONE) cnear = std::max(cnear, 2.0 * d->contact.r_part);
+        if (sinter) cnear = std::max(cnear, 2.0 * d->sinter.r_part);
+        s->mx.contact2f = (float)(cnear * cnear * 1.004);
+        s->mx.inv_mass_h = d->hamaker.mass > 0 ? (float)(1.0 / d->hamaker.mass) : 0.f;
+        s->mx.inv_mass_c = d->contact.mass > 0 ? 1.0 / d->contact.mass : 0.0;
+        s->mx.inv_inertia_c = d->contact.inertia > 0 ? 1.0 / d->contact.inertia : 0.0;
+        s->mx.inv_mass_b = d->sinter.mass > 0 ? 1.0 / d->sinter.mass : 0.0;
+        s->mx.inv_inertia_b = d->sinter.inertia > 0 ? 1.0 / d->sinter.inertia : 0.0;
+        s->mx.four_rc2 = 4.0 * d->contact.r_part * d->contact.r_part;
+        s->mx.four_rb2 = 4.0 * d->sinter.r_part * d->sinter.r_part;
+        s->mx.four_rh2 = 4.0 * d->hamaker.r_part * d->hamaker.r_part;
+        const lg_contact_params &C = d->contact;
+        const lg_sinter_params &B = d->sinter;
+        MixedExtra &M = s->mx;
+        M.c_k = (float)C.k; M.c_gn = (float)C.gamma_n; M.c_kt = (float)C.k_t; M.c_gt = (float)C.gamma_t;
+        M.c_mus = (float)C.mu_s; M.c_phid = (float)C.phi_d; M.c_kr = (float)C.k_r; M.c_gr = (float)C.gamma_r;
+        M.c_mur = (float)C.mu_r; M.c_phir = (float)C.phi_r; M.c_ko = (float)C.k_o; M.c_go = (float)C.gamma_o;
+        M.c_muo = (float)C.mu_o; M.c_phio = (float)C.phi_o; M.c_r = (float)C.r_part; M.c_dt = (float)C.dt;
+        M.b_k = (float)B.k; M.b_gn = (float)B.gamma_n; M.b_kt = (float)B.k_t; M.b_gt = (float)B.gamma_t;
+        M.b_kr = (float)B.k_r; M.b_gr = (float)B.gamma_r; M.b_ko = (float)B.k_o; M.b_go = (float)B.gamma_o;
+        M.b_r = (float)B.r_part; M.b_dt = (float)B.dt;
+        M.h_A = (float)d->hamaker.A; M.h_h0 = (float)d->hamaker.h0; M.h_r = (float)d->hamaker.r_part;
         s->mx.rcut2 = d->hamaker.r_cutoff * d->hamaker.r_cutoff;
     }
     s->T = d->threads_per_row > 0 ? d->threads_per_row : choose_threads_per_row(s);
+    s->kernel = choose_kernel(s, d->force_kernel);
+    if (d->threads_per_row > 0 && d->force_kernel == LG_FORCE_KERNEL_AUTO) s->kernel = LG_FORCE_KERNEL_ROWGROUP;
     // initial accelerations (the first half kick needs them); velocities are unchanged (hdt = 0)
     LG_TRY(launch_forces(s, 0.0, 0.0, 0));
     LG_CUDA(cudaStreamSynchronize(s->stream));
@@ -701,6 +744,13 @@ extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
     if (T != 1 && T != 2 && T != 4 && T != 8 && T != 16 && T != 32)
         return lg_fail(LG_E_INVALID, "lg_set_threads_per_row: T must be 0 or a power of two <= 32");
     s->T = T;
+    return LG_OK;
+}
+
+extern "C" int lg_set_force_kernel(lg_system *s, int32_t variant) {
+    LG_HANDLE(s);
+    if (variant < 0 || variant > 2) return lg_fail(LG_E_INVALID, "lg_set_force_kernel: unknown variant %d", variant);
+    s->kernel = choose_kernel(s, variant);
     return LG_OK;
 }
 

@@ -50,6 +50,7 @@ struct lg_system {
     size_t tev_used = 0;
 
     int T = 1;  // lanes per row group of the force kernel
+    int kernel = LG_FORCE_KERNEL_ROWGROUP;  // resolved force kernel
     int64_t step_index = 0;
     int64_t launches = 0;
     std::vector<void *> allocations;

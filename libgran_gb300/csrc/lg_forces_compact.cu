@@ -1,0 +1,637 @@
+// lg_forces_compact.cu -- warp-compacted force kernel (sm_103a), FP64 and mixed precision.
+//
+// On GB300 a warp instruction on the FP64 pipe costs the same issue time whether 1 or 32 lanes are
+// active, so a kernel whose lanes each walk their own row and branch on "is this pair in Hamaker
+// range / in contact" wastes most of its FP64 issue slots. This kernel gives each lane one row (one
+// particle i) and processes the rows of a warp in rounds of up to kRound slots:
+//   A. classify  -- every lane tests its slot k (separation against the cutoffs); the warp appends
+//                   contact/bond candidates to a shared-memory queue in a fixed order (slot-major,
+//                   lane-minor, via ballots) and records which slots need a Hamaker evaluation.
+//                   As soon as 32 contact items are pending, all 32 lanes evaluate them, one pair
+//                   per lane (springs read and written in global memory: each slot belongs to
+//                   exactly one item), so the expensive contact code runs with full warps;
+//   B. Hamaker   -- per window of kWin slots, the warp queues that window's Hamaker pairs and all
+//                   32 lanes evaluate them, one pair per lane;
+//      fold      -- each lane adds its row's results in ascending slot order, exactly as the
+//                   reference's loop adds (contact + Hamaker) pair by pair.
+// Per-pair results live only in shared memory, so the per-particle sums come out in a fixed order
+// with no floating-point atomics. In FP64 (this file compiled with --fmad=false) every pair value
+// is computed by the same functions as the sequential kernel and the fold adds in the same order,
+// so the result is bit-identical to the sequential evaluation.
+//
+// Compiled twice: LG_COMPACT_MIXED=0 (FP64) and LG_COMPACT_MIXED=1 (FP32 pair arithmetic with FP64
+// separation, overlap, springs, sums; see lg_forces_mixed.cu for the split).
+#include "lg_common.cuh"
+#include "lg_kernels.h"
+
+#ifndef LG_COMPACT_MIXED
+#define LG_COMPACT_MIXED 0
+#endif
+
+namespace lg {
+
+namespace {
+
+constexpr int kWin = 4;            // Hamaker window (slots)
+constexpr int kHCap = 32 * kWin;   // Hamaker queue capacity per window
+constexpr int kRound = 128;        // slots classified per round
+constexpr int kCCap = 256;         // contact queue capacity per round
+constexpr int kWarps = 2;
+#if LG_COMPACT_MIXED
+typedef float rt;
+#else
+typedef double rt;
+#endif
+
+struct WarpSmem {
+    rt hres[kHCap][3];
+    rt cres[kCCap][6];
+    int32_t hj[kHCap], cj[kCCap];
+    uint16_t hown[kHCap], cown[kCCap];  // (owner lane << 8) | slot offset
+    uint32_t cball[kRound], hballA[kRound];
+    int32_t cbase[kRound];
+    uint32_t hball[kWin];
+    int32_t hbase[kWin];
+    d3 xo[32], vo[32], wo[32];
+};
+
+#if LG_COMPACT_MIXED
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 fm(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 fadd(f3 a, f3 b) { return fm(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 fsub(f3 a, f3 b) { return fm(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 fscl(float s, f3 a) { return fm(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float fdot(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+__device__ __forceinline__ f3 fcrs(f3 a, f3 b) {
+    return fm(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ f3 tof(d3 a) { return fm((float)a.x, (float)a.y, (float)a.z); }
+
+// Shear spring (contact_force.h:105-147, Coulomb-capped; alt_sinter_bridge.h:137-156, bond form)
+// with the spring vector held in FP64. Each evaluation computes, in FP32, the increment of the
+// spring: the rotation onto the tangent plane, -(xi.n) n, the rescale to the old magnitude,
+// (s - 1)(xi - (xi.n) n) with s - 1 evaluated as a series for small tilts, and the stretch rel*dt;
+// the increment is small next to xi and is added to the FP64 spring, so rounding does not
+// accumulate at the spring's own scale. The dynamic (sliding) branch sets the spring outright.
+__device__ __forceinline__ f3 shear_mx(d3 &xi, f3 n, float stiffness, float damping, float normal_force, float mu_s,
+                                       float phi, f3 rel, float dtf, bool coulomb) {
+    f3 xf = tof(xi);
+    f3 drot = fm(0.f, 0.f, 0.f);
+    float xx = fdot(xf, xf);
+    if (xx > 0.0f) {
+        float c = fdot(xf, n);
+        f3 xr = fsub(xf, fscl(c, n));
+        float e = (c * c) / xx;
+        float sm1 = 0.0f;
+        if (e < 1.0f) sm1 = e < 1e-3f ? e * (0.5f + 0.375f * e) : rsqrtf(1.0f - e) - 1.0f;
+        drot = fadd(fscl(-c, n), fscl(sm1, xr));
+    }
+    const f3 xn = fadd(xf, drot);
+    const f3 f0 = fsub(fscl(-stiffness, xn), fscl(damping, rel));
+    if (!coulomb) {
+        const f3 dxi = fadd(drot, fscl(dtf, rel));
+        xi.x += (double)dxi.x;
+        xi.y += (double)dxi.y;
+        xi.z += (double)dxi.z;
+        return f0;
+    }
+    const float fs = mu_s * normal_force;
+    const float fd = mu_s * phi * normal_force;
+    const float f0n = sqrtf(fdot(f0, f0));
+    const f3 t = f0n > 0.0f ? fscl(1.0f / f0n, f0) : fm(0.f, 0.f, 0.f);
+    float sel;
+    if (f0n <= fs) {
+        const f3 dxi = fadd(drot, fscl(dtf, rel));
+        xi.x += (double)dxi.x;
+        xi.y += (double)dxi.y;
+        xi.z += (double)dxi.z;
+        sel = fs;
+    } else {
+        const f3 nx = fscl(-1.0f / stiffness, fadd(fscl(fd, t), fscl(damping, rel)));
+        xi = mk3((double)nx.x, (double)nx.y, (double)nx.z);
+        sel = fd;
+    }
+    return fscl(fminf(sel, f0n), t);
+}
+
+// Hamaker factor of hamaker_force.h:36-40 with two reciprocals:
+// s = -A/6 [ (4r+2h) u - 2 w - 4 r^2 w^3 - 2 r^2 (4r+2h) u^2 ], u = 1/((4r+h) h), w = 1/(2r+h).
+__device__ __forceinline__ float ham_factor(int mode, float A, float r, float h) {
+    if (mode == LG_HAMAKER_SIMPLIFIED) return 2.0f * A * r / (h * h);
+    float u = 1.0f / ((4.0f * r + h) * h);
+    float w = 1.0f / (2.0f * r + h);
+    float a = 4.0f * r + 2.0f * h;
+    float br = a * u - 2.0f * w - 4.0f * r * r * (w * w * w) - 2.0f * r * r * a * (u * u);
+    return -A / 6.0f * br;
+}
+#endif
+
+// One queued contact / bond pair: owner row io (lane own of the warp), slot e, partner j.
+#if LG_COMPACT_MIXED
+__device__ __forceinline__ void contact_item(const Params &P, const StateView &S, const PairView &PV,
+                                             const BondView &BV, const MixedExtra &M, WarpSmem &W, int q, int64_t row0,
+                                             int64_t kstart, int64_t n, int64_t xs, int64_t bs) {
+    const int own = W.cown[q] >> 8;
+    const int64_t io = row0 + own;
+    const int64_t e = (kstart + (W.cown[q] & 0xff)) * n + io;
+    const int32_t j = W.cj[q];
+    const uint32_t fl = PV.flags[e];
+    const bool bonded = (fl & kBonded) != 0;
+    const d3 xo = W.xo[own], vo = W.vo[own], wo = W.wo[own];
+    const d3 xj = ld4(S.x, j);
+    const d3 dx = sub(xo, xj);
+    const double q4 = fma(dx.z, dx.z, fma(dx.y, dx.y, fma(dx.x, dx.x, -(bonded ? M.four_rb2 : M.four_rc2))));
+    const f3 dxf = tof(dx);
+    const float d2f = fdot(dxf, dxf);
+    const float rr = bonded ? M.b_r : M.c_r;
+    const float rsd = rsqrtf(d2f);
+    const float overlap = -(float)q4 / (d2f * rsd + 2.0f * rr);  // 2r - |d|, from |d|^2 - (2r)^2 in FP64
+    f3 force = fm(0.f, 0.f, 0.f), torque = fm(0.f, 0.f, 0.f);
+    if (bonded || overlap > 0.0f) {
+        const f3 n3 = fscl(rsd, dxf);
+        const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+        const f3 vij0 = tof(sub(vo, vj));
+        const f3 wfi = tof(wo), wfj = tof(wj);
+        int64_t base, stride;
+        double *store;
+        if (bonded) {
+            base = (int64_t)bond_slot_of(fl) * n + io;
+            stride = bs;
+            store = BV.xi;
+        } else {
+            base = e;
+            stride = xs;
+            store = PV.xi;
+        }
+        d3 s[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            s[c] = mk3(store[(3 * c) * stride + base], store[(3 * c + 1) * stride + base], store[(3 * c + 2) * stride + base]);
+        const float kn = bonded ? M.b_k : M.c_k, gn = bonded ? M.b_gn : M.c_gn;
+        const float rp = rr - 0.5f * overlap;
+        const float v_n = -fdot(vij0, n3);
+        const float f_n = kn * overlap + gn * v_n;
+        const f3 nwi = fcrs(n3, wfi), nwj = fcrs(n3, wfj);
+        const f3 v_ij = fadd(vij0, fscl(rp, fadd(nwi, nwj)));
+        const f3 v_t = fsub(v_ij, fscl(fdot(v_ij, n3), n3));
+        const f3 v_r = fscl(-rp, fsub(nwi, nwj));
+        const f3 v_o = fscl(rr * (fdot(n3, wfi) - fdot(n3, wfj)), n3);
+        f3 f_t, f_r, f_o;
+        if (bonded) {
+            f_t = shear_mx(s[0], n3, M.b_kt, M.b_gt, f_n, 0.f, 0.f, v_t, M.b_dt, false);
+            f_r = shear_mx(s[1], n3, M.b_kr, M.b_gr, f_n, 0.f, 0.f, v_r, M.b_dt, false);
+            f_o = shear_mx(s[2], n3, M.b_ko, M.b_go, f_n, 0.f, 0.f, v_o, M.b_dt, false);
+        } else {
+            f_t = shear_mx(s[0], n3, M.c_kt, M.c_gt, f_n, M.c_mus, M.c_phid, v_t, M.c_dt, true);
+            f_r = shear_mx(s[1], n3, M.c_kr, M.c_gr, f_n, M.c_mur, M.c_phir, v_r, M.c_dt, true);
+            f_o = shear_mx(s[2], n3, M.c_ko, M.c_go, f_n, M.c_muo, M.c_phio, v_o, M.c_dt, true);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            store[(3 * c) * stride + base] = s[c].x;
+            store[(3 * c + 1) * stride + base] = s[c].y;
+            store[(3 * c + 2) * stride + base] = s[c].z;
+        }
+        force = fadd(fscl(f_n, n3), f_t);
+        torque = fadd(fsub(fscl(rr, fcrs(n3, f_r)), fscl(rp, fcrs(n3, f_t))), fscl(rr, f_o));
+        if (bonded) {
+            if (P.binary_model == LG_BINARY_BREAKING_SINTER) {
+                const double st = BV.strength[base];
+                if ((double)fdot(force, force) > st * st) {
+                    BV.intact[base] = 0;
+                    PV.flags[e] = fl & ~(kBonded | (0xffu << 8));
+                }
+            }
+        } else if (!(fl & kXiLive)) {
+            PV.flags[e] = fl | kXiLive;
+        }
+    } else if (fl & kXiLive) {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+        PV.flags[e] = fl & ~kXiLive;
+    }
+    W.cres[q][0] = force.x;
+    W.cres[q][1] = force.y;
+    W.cres[q][2] = force.z;
+    W.cres[q][3] = torque.x;
+    W.cres[q][4] = torque.y;
+    W.cres[q][5] = torque.z;
+}
+
+__device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S, const MixedExtra &M, WarpSmem &W,
+                                             int q) {
+    const int own = W.hown[q] >> 8;
+    const d3 dx = sub(W.xo[own], ld4(S.x, W.hj[q]));
+    const double q4 = fma(dx.z, dx.z, fma(dx.y, dx.y, fma(dx.x, dx.x, -M.four_rh2)));  // |d|^2 - (2r)^2
+    f3 a = fm(0.f, 0.f, 0.f);
+    if (!(P.hamaker_model == LG_HAMAKER_LIMITED && q4 > M.rcut2 - M.four_rh2)) {
+        const f3 dxf = tof(dx);
+        const float d2f = fdot(dxf, dxf);
+        const float rsd = rsqrtf(d2f);
+        float h = (float)q4 / (d2f * rsd + 2.0f * M.h_r);  // |d| - 2r, exact to FP32
+        h = fmaxf(h, M.h_h0);
+        const float sfac = ham_factor(P.hamaker_model, M.h_A, M.h_r, h) * M.inv_mass_h * rsd;
+        a = fscl(-sfac, dxf);  // along x_j - x_i
+    }
+    W.hres[q][0] = a.x;
+    W.hres[q][1] = a.y;
+    W.hres[q][2] = a.z;
+}
+#else
+__device__ __forceinline__ void contact_item(const Params &P, const StateView &S, const PairView &PV,
+                                             const BondView &BV, WarpSmem &W, int q, int64_t row0, int64_t kstart,
+                                             int64_t n, int64_t xs, int64_t bs) {
+    const int own = W.cown[q] >> 8;
+    const int64_t io = row0 + own;
+    const int64_t e = (kstart + (W.cown[q] & 0xff)) * n + io;
+    const int32_t j = W.cj[q];
+    const uint32_t fl = PV.flags[e];
+    const d3 xo = W.xo[own], vo = W.vo[own], wo = W.wo[own];
+    const d3 dx = sub(xo, ld4(S.x, j));
+    d3 pa = zero3(), pal = zero3();
+    if (fl & kBonded) {
+        const bool breaking = P.binary_model == LG_BINARY_BREAKING_SINTER;
+        const int64_t be = (int64_t)bond_slot_of(fl) * n + io;
+        d3 s[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            s[c] = mk3(BV.xi[(3 * c) * bs + be], BV.xi[(3 * c + 1) * bs + be], BV.xi[(3 * c + 2) * bs + be]);
+        const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+        const bool brk = bond_force(P.sinter, dx, vo, vj, wo, wj, s, breaking, breaking ? BV.strength[be] : 0.0, pa, pal);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            BV.xi[(3 * c) * bs + be] = s[c].x;
+            BV.xi[(3 * c + 1) * bs + be] = s[c].y;
+            BV.xi[(3 * c + 2) * bs + be] = s[c].z;
+        }
+        if (brk) {
+            BV.intact[be] = 0;
+            PV.flags[e] = fl & ~(kBonded | (0xffu << 8));
+        }
+    } else {
+        const d3 nn = nrmz(dx);
+        const double overlap = 2.0 * P.contact.r_part - dot(dx, nn);
+        if (!(overlap <= 0)) {
+            d3 s[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                s[c] = mk3(PV.xi[(3 * c) * xs + e], PV.xi[(3 * c + 1) * xs + e], PV.xi[(3 * c + 2) * xs + e]);
+            const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+            contact_touching(P.contact, nn, overlap, vo, vj, wo, wj, s, pa, pal);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                PV.xi[(3 * c) * xs + e] = s[c].x;
+                PV.xi[(3 * c + 1) * xs + e] = s[c].y;
+                PV.xi[(3 * c + 2) * xs + e] = s[c].z;
+            }
+            if (!(fl & kXiLive)) PV.flags[e] = fl | kXiLive;
+        } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+#pragma unroll
+            for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+            PV.flags[e] = fl & ~kXiLive;
+        }
+    }
+    W.cres[q][0] = pa.x;
+    W.cres[q][1] = pa.y;
+    W.cres[q][2] = pa.z;
+    W.cres[q][3] = pal.x;
+    W.cres[q][4] = pal.y;
+    W.cres[q][5] = pal.z;
+}
+
+__device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S, WarpSmem &W, int q) {
+    const int own = W.hown[q] >> 8;
+    const d3 xo = W.xo[own];
+    const d3 xj = ld4(S.x, W.hj[q]);
+    d3 ha = zero3();
+    // |x_i - x_j| and |x_j - x_i| are the same value (the squares of negated differences are
+    // identical), so one square root serves the cutoff test, h and the unit vector
+    const d3 r = sub(xj, xo);
+    const double rn = nrm(r);
+    bool on = true;
+    if (P.hamaker_model == LG_HAMAKER_LIMITED) on = !(rn > P.hamaker.r_cutoff);
+    if (on) ha = hamaker_accel_n(P.hamaker_model, P.hamaker, r, rn);
+    W.hres[q][0] = ha.x;
+    W.hres[q][1] = ha.y;
+    W.hres[q][2] = ha.z;
+}
+#endif
+
+}  // namespace
+
+template <bool VERLET>
+__global__ void __launch_bounds__(kWarps * 32)
+#if LG_COMPACT_MIXED
+    forces_compact_mixed(Params P, StateView S, PairView PV, BondView BV, double hdt, double dt, int move_facets,
+                         MixedExtra MX)
+#else
+    forces_compact_fp64(Params P, StateView S, PairView PV, BondView BV, double hdt, double dt, int move_facets)
+#endif
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpSmem &W = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
+    const int64_t n = P.n;
+    const int64_t row0 = ((int64_t)blockIdx.x * kWarps + warp) * 32;
+    const int64_t i = row0 + lane;
+    const bool active = i < n;
+    const int bm = P.binary_model, hm = P.hamaker_model;
+    const uint32_t lt = (1u << lane) - 1u;
+
+    if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int f = 0; f < P.n_facets; ++f)
+            for (int q = 0; q < 9; ++q) S.facet_vert_next[9 * f + q] = S.facet_vert[9 * f + q] + P.facets[f].v[q % 3] * dt;
+    }
+
+    d3 xi_ = zero3(), vi = zero3(), wi = zero3();
+    int64_t len = 0;
+    if (active) {
+        xi_ = ld4(S.x, i);
+        vi = ld4(S.v, i);
+        wi = ld4(S.w, i);
+        len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
+    }
+    W.xo[lane] = xi_;
+    W.vo[lane] = vi;
+    W.wo[lane] = wi;
+    const int64_t maxlen = (int64_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
+    const int64_t xs = PV.cap * n;
+    const int64_t bs = (int64_t)BV.bcap * n;
+#if LG_COMPACT_MIXED
+    const float4 q4i = active ? MX.x32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    d3 acc = zero3(), accw = zero3(), acch = zero3();
+#else
+    d3 acc = zero3(), accw = zero3();
+#endif
+    __syncwarp();
+
+    for (int64_t kstart = 0; kstart < maxlen;) {
+        // ---------------- pass A: classify, queue contacts, evaluate them in full warps ----------------
+        int ccount = 0, cdone = 0;
+        int64_t k = kstart;
+        for (; k < maxlen && k - kstart < kRound && ccount + 32 <= kCCap; ++k) {
+            bool hb = false, cb = false;
+            int32_t j = 0;
+            if (k < len) {
+                const int64_t e = k * n + i;
+                j = VERLET ? PV.nbr[e] : (int32_t)(k < i ? k : k + 1);
+                const uint32_t fl = PV.flags[e];
+                const bool bonded = (fl & kBonded) && bm != LG_BINARY_NONE;
+#if LG_COMPACT_MIXED
+                const float4 qj = MX.x32[j];
+                const float dxf = q4i.x - qj.x, dyf = q4i.y - qj.y, dzf = q4i.z - qj.z;
+                const float d2f = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
+                const bool ccand = d2f <= MX.contact2f;
+                if (hm == LG_HAMAKER_LIMITED)
+                    hb = d2f <= MX.near2;
+                else if (hm != LG_HAMAKER_NONE)
+                    hb = true;
+#else
+                const double d2 = sqn(sub(xi_, ld4(S.x, j)));
+                const bool ccand = !(d2 > P.contact_skip_d2);
+                if (hm == LG_HAMAKER_LIMITED)
+                    hb = !(d2 > P.hamaker_skip_d2);
+                else if (hm != LG_HAMAKER_NONE)
+                    hb = true;
+#endif
+                if (bm != LG_BINARY_NONE) {
+                    if (bonded || ccand)
+                        cb = true;
+                    else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+#pragma unroll
+                        for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+                        PV.flags[e] = fl & ~kXiLive;
+                    }
+                }
+            }
+            const uint32_t bc = __ballot_sync(0xffffffffu, cb);
+            const uint32_t bh = __ballot_sync(0xffffffffu, hb);
+            if (cb) {
+                const int q = ccount + __popc(bc & lt);
+                W.cj[q] = j;
+                W.cown[q] = (uint16_t)((lane << 8) | (int)(k - kstart));
+            }
+            if (lane == 0) {
+                W.cball[k - kstart] = bc;
+                W.cbase[k - kstart] = ccount;
+                W.hballA[k - kstart] = bh;
+            }
+            ccount += __popc(bc);
+            __syncwarp();
+            if (ccount - cdone >= 32) {
+#if LG_COMPACT_MIXED
+                contact_item(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, n, xs, bs);
+#else
+                contact_item(P, S, PV, BV, W, cdone + lane, row0, kstart, n, xs, bs);
+#endif
+                cdone += 32;
+                __syncwarp();
+            }
+        }
+        const int64_t kend = k;
+        if (cdone < ccount) {
+            if (cdone + lane < ccount)
+#if LG_COMPACT_MIXED
+                contact_item(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, n, xs, bs);
+#else
+                contact_item(P, S, PV, BV, W, cdone + lane, row0, kstart, n, xs, bs);
+#endif
+            cdone = ccount;
+        }
+        __syncwarp();
+
+        // ---------------- pass B: Hamaker windows and the ordered fold ----------------
+        for (int64_t kw = kstart; kw < kend; kw += kWin) {
+            int hcount = 0;
+#pragma unroll
+            for (int t = 0; t < kWin; ++t) {
+                const int64_t kk = kw + t;
+                const uint32_t bh = kk < kend ? W.hballA[kk - kstart] : 0u;
+                if ((bh >> lane) & 1u) {
+                    const int q = hcount + __popc(bh & lt);
+                    W.hj[q] = VERLET ? PV.nbr[kk * n + i] : (int32_t)(kk < i ? kk : kk + 1);
+                    W.hown[q] = (uint16_t)((lane << 8) | t);
+                }
+                if (lane == 0) {
+                    W.hball[t] = bh;
+                    W.hbase[t] = hcount;
+                }
+                hcount += __popc(bh);
+            }
+            __syncwarp();
+            for (int q = lane; q < hcount; q += 32)
+#if LG_COMPACT_MIXED
+                hamaker_item(P, S, MX, W, q);
+#else
+                hamaker_item(P, S, W, q);
+#endif
+            __syncwarp();
+#pragma unroll
+            for (int t = 0; t < kWin; ++t) {
+                const int64_t kk = kw + t;
+                if (kk < kend && kk < len) {
+                    const uint32_t bh = W.hball[t], bc = W.cball[kk - kstart];
+                    const bool hb = (bh >> lane) & 1u, cb = (bc >> lane) & 1u;
+#if LG_COMPACT_MIXED
+                    if (cb) {
+                        const int q = W.cbase[kk - kstart] + __popc(bc & lt);
+                        acc.x += (double)W.cres[q][0];
+                        acc.y += (double)W.cres[q][1];
+                        acc.z += (double)W.cres[q][2];
+                        accw.x += (double)W.cres[q][3];
+                        accw.y += (double)W.cres[q][4];
+                        accw.z += (double)W.cres[q][5];
+                    }
+                    if (hb) {
+                        const int q = W.hbase[t] + __popc(bh & lt);
+                        acch.x += (double)W.hres[q][0];
+                        acch.y += (double)W.hres[q][1];
+                        acch.z += (double)W.hres[q][2];
+                    }
+#else
+                    // the reference's fold: pa = binary(i, j) [+ hamaker(i, j)]; acc += pa. Pairs with no
+                    // queued item contribute exact zeros, which leave the sums unchanged.
+                    if (cb || hb) {
+                        d3 pa = zero3(), pal = zero3();
+                        bool have = false;
+                        if (bm != LG_BINARY_NONE) {
+                            have = true;
+                            if (cb) {
+                                const int q = W.cbase[kk - kstart] + __popc(bc & lt);
+                                pa = mk3(W.cres[q][0], W.cres[q][1], W.cres[q][2]);
+                                pal = mk3(W.cres[q][3], W.cres[q][4], W.cres[q][5]);
+                            }
+                        }
+                        if (hm != LG_HAMAKER_NONE) {
+                            d3 ha = zero3();
+                            if (hb) {
+                                const int q = W.hbase[t] + __popc(bh & lt);
+                                ha = mk3(W.hres[q][0], W.hres[q][1], W.hres[q][2]);
+                            }
+                            if (have) {
+                                pa = add(pa, ha);
+                                pal = add(pal, zero3());
+                            } else {
+                                pa = ha;
+                                pal = zero3();
+                            }
+                        }
+                        acc = add(acc, pa);
+                        accw = add(accw, pal);
+                    }
+#endif
+                }
+            }
+            __syncwarp();
+        }
+        kstart = kend;
+    }
+    if (!active) return;
+
+#if LG_COMPACT_MIXED
+    const bool sint = bm == LG_BINARY_SINTER || bm == LG_BINARY_BREAKING_SINTER;
+    d3 a_tot = add(scl(sint ? MX.inv_mass_b : MX.inv_mass_c, acc), acch);
+    d3 al_tot = scl(sint ? MX.inv_inertia_b : MX.inv_inertia_c, accw);
+    d3 &accA = a_tot;
+    d3 &accW = al_tot;
+#else
+    d3 &accA = acc;
+    d3 &accW = accw;
+#endif
+    if (P.n_facets > 0) {
+        d3 ua = zero3(), ual = zero3();
+        for (int f = 0; f < P.n_facets; ++f) {
+            const FacetDev &fd = P.facets[f];
+            d3 N = mk3(fd.normal[0], fd.normal[1], fd.normal[2]);
+            d3 xf = closest_point_on_triangle(S.facet_vert + 9 * f, fd.area, N, xi_);
+            d3 vf = mk3(fd.v[0], fd.v[1], fd.v[2]);
+            d3 fa = zero3(), fal = zero3();
+            bool hv = false;
+            if (fd.has_contact) {
+                const int64_t base = (int64_t)f * 9 * n;
+                d3 s[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    s[q] = mk3(S.sxi[base + (3 * q) * n + i], S.sxi[base + (3 * q + 1) * n + i], S.sxi[base + (3 * q + 2) * n + i]);
+                surface_contact(fd.contact, xf, vf, xi_, vi, wi, s, fa, fal);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    S.sxi[base + (3 * q) * n + i] = s[q].x;
+                    S.sxi[base + (3 * q + 1) * n + i] = s[q].y;
+                    S.sxi[base + (3 * q + 2) * n + i] = s[q].z;
+                }
+                hv = true;
+            }
+            if (fd.has_hamaker) {
+                d3 ha = surface_hamaker(fd.hamaker, xf, xi_);
+                if (hv) {
+                    fa = add(fa, ha);
+                    fal = add(fal, zero3());
+                } else {
+                    fa = ha;
+                    fal = zero3();
+                }
+            }
+            if (f == 0) {
+                ua = fa;
+                ual = fal;
+            } else {
+                ua = add(ua, fa);
+                ual = add(ual, fal);
+            }
+        }
+        accA = add(accA, ua);
+        accW = add(accW, ual);
+    }
+    st4(S.a, i, accA);
+    st4(S.al, i, accW);
+    st4(S.v_out, i, add(vi, scl(hdt, accA)));
+    st4(S.w_out, i, add(wi, scl(hdt, accW)));
+    if (!isfinite(accA.x) || !isfinite(accA.y) || !isfinite(accA.z) || !isfinite(accW.x) || !isfinite(accW.y) ||
+        !isfinite(accW.z))
+        set_error(S.err, LG_DEVERR_NONFINITE);
+}
+
+#if LG_COMPACT_MIXED
+void launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                                 double dt, int move_facets, const MixedExtra &MX, cudaStream_t st) {
+    const size_t smem = sizeof(WarpSmem) * kWarps;
+    const int64_t rows_per_block = kWarps * 32;
+    const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
+    static thread_local int attr_device = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (attr_device != dev) {  // the attribute is per device; set it once per thread and device
+        cudaFuncSetAttribute(forces_compact_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(forces_compact_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_device = dev;
+    }
+    if (P.pairs == LG_PAIRS_VERLET)
+        forces_compact_mixed<true><<<blocks, kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets, MX);
+    else
+        forces_compact_mixed<false><<<blocks, kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets, MX);
+}
+#else
+void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                                double dt, int move_facets, cudaStream_t st) {
+    const size_t smem = sizeof(WarpSmem) * kWarps;
+    const int64_t rows_per_block = kWarps * 32;
+    const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
+    static thread_local int attr_device = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (attr_device != dev) {  // the attribute is per device; set it once per thread and device
+        cudaFuncSetAttribute(forces_compact_fp64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(forces_compact_fp64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_device = dev;
+    }
+    if (P.pairs == LG_PAIRS_VERLET)
+        forces_compact_fp64<true><<<blocks, kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets);
+    else
+        forces_compact_fp64<false><<<blocks, kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets);
+}
+#endif
+
+}  // namespace lg

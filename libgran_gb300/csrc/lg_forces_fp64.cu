@@ -236,16 +236,36 @@ __global__ void bbox_partial(int64_t n, const dbl4 *__restrict__ x, double *__re
         for (int c = 0; c < 6; ++c) part[6 * blockIdx.x + c] = s[c][0];
 }
 
-// One thread: combine the block partials and size the grid (cells of edge >= r_verlet; the edge
-// grows by 1.25 until the grid has at most max_cells cells).
-__global__ void grid_setup(int nparts, const double *__restrict__ part, double rv, int64_t max_cells, GridDev *g) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// One block: combine the block partials and size the grid (cells of edge >= r_verlet; the edge
+// grows by 1.25 until the grid has at most max_cells cells). Also fixes the FP32 accept / reject
+// bounds of the squared list radius for positions stored relative to the grid origin.
+__global__ void __launch_bounds__(256) grid_setup(int nparts, const double *__restrict__ part, double rv, int64_t max_cells,
+                                                  GridDev *g) {
+    __shared__ double s[6][256];
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int b = 0; b < nparts; ++b)
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x)
         for (int c = 0; c < 3; ++c) {
             lo[c] = fmin(lo[c], part[6 * b + c]);
             hi[c] = fmax(hi[c], part[6 * b + 3 + c]);
         }
+    for (int c = 0; c < 3; ++c) {
+        s[c][threadIdx.x] = lo[c];
+        s[3 + c][threadIdx.x] = hi[c];
+    }
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int c = 0; c < 3; ++c) {
+                s[c][threadIdx.x] = fmin(s[c][threadIdx.x], s[c][threadIdx.x + o]);
+                s[3 + c][threadIdx.x] = fmax(s[3 + c][threadIdx.x], s[3 + c][threadIdx.x + o]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    for (int c = 0; c < 3; ++c) {
+        lo[c] = s[c][0];
+        hi[c] = s[3 + c][0];
+    }
     double edge = rv;
     int64_t dim[3];
     for (int it = 0; it < 4096; ++it) {
@@ -262,12 +282,20 @@ __global__ void grid_setup(int nparts, const double *__restrict__ part, double r
         dim[0] = dim[1] = dim[2] = 1;
         edge = 1e300;
     }
+    double span = 0.0;
     for (int c = 0; c < 3; ++c) {
         g->lo[c] = lo[c];
         g->dim[c] = dim[c];
+        span = fmax(span, hi[c] - lo[c]);
     }
     g->edge = edge;
     g->ncell = dim[0] * dim[1] * dim[2];
+    // FP32 coordinates relative to lo carry an error below span * 2^-24 each; bound |d| by 2 such
+    // errors per component and the squared radius by a further relative 1e-6
+    const double del = 4.0 * span * 5.9604644775390625e-8 + 1e-300;
+    const double lo_r = rv - 2.0 * del, hi_r = rv + 2.0 * del;
+    g->rv2_lo = lo_r > 0 ? (float)(lo_r * lo_r * (1.0 - 1e-6)) : 0.0f;
+    g->rv2_hi = (float)(hi_r * hi_r * (1.0 + 1e-6));
 }
 
 __device__ __forceinline__ int64_t cell_coord(double q, double lo, double edge, int64_t dim) {
@@ -276,7 +304,7 @@ __device__ __forceinline__ int64_t cell_coord(double q, double lo, double edge, 
 }
 
 __global__ void cell_count(int64_t n, const dbl4 *__restrict__ x, const GridDev *__restrict__ g,
-                           int32_t *__restrict__ cell_of, int32_t *__restrict__ count) {
+                           int32_t *__restrict__ cell_of, int32_t *__restrict__ count, float4 *__restrict__ x32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     dbl4 q = x[i];
@@ -285,6 +313,7 @@ __global__ void cell_count(int64_t n, const dbl4 *__restrict__ x, const GridDev 
     int64_t cz = cell_coord(q.z, g->lo[2], g->edge, g->dim[2]);
     int32_t c = (int32_t)((cz * g->dim[1] + cy) * g->dim[0] + cx);
     cell_of[i] = c;
+    x32[i] = make_float4((float)(q.x - g->lo[0]), (float)(q.y - g->lo[1]), (float)(q.z - g->lo[2]), 0.0f);
     atomicAdd(&count[c], 1);
 }
 
@@ -299,16 +328,14 @@ __global__ void scan_cells(const GridDev *__restrict__ g, const int32_t *__restr
     for (int64_t c = b; c < e; ++c) s += count[c];
     part[t] = s;
     __syncthreads();
-    if (t == 0) {
-        int32_t run = 0;
-        for (int q = 0; q < T; ++q) {
-            int32_t v = part[q];
-            part[q] = run;
-            run += v;
-        }
+    // Hillis-Steele inclusive scan of the per-thread sums
+    for (int o = 1; o < T; o <<= 1) {
+        int32_t v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
     }
-    __syncthreads();
-    int32_t run = part[t];
+    int32_t run = part[t] - s;
     for (int64_t c = b; c < e; ++c) {
         start[c] = run;
         run += count[c];
@@ -324,22 +351,31 @@ __global__ void cell_scatter(int64_t n, const int32_t *__restrict__ cell_of, con
     sorted[start[c] + p] = (int32_t)i;
 }
 
-// Build row i: every j != i with squared centre distance < r_verlet^2, ascending j, carrying the
-// springs (and live flag) of pairs that were already listed, and marking intact bonds.
-__global__ void __launch_bounds__(128) build_rows(int64_t n, const dbl4 *__restrict__ x, const GridDev *__restrict__ g,
-                                                  const int32_t *__restrict__ cstart, const int32_t *__restrict__ ccount,
-                                                  const int32_t *__restrict__ sorted, double rv2, PairView oldv,
-                                                  PairView newv, BondView BV, int32_t *err) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+constexpr int kBuildThreads = 64;
+
+// Build row i: every j != i with squared centre distance < r_verlet^2 (the FP64 test; an FP32
+// filter accepts or rejects the clear cases), ascending j, carrying the springs (and live flag) of
+// pairs that were already listed, and marking intact bonds. Candidates are gathered and sorted in
+// shared memory (slot k of thread t at k * blockDim + t, conflict-free).
+__global__ void __launch_bounds__(kBuildThreads) build_rows(int64_t n, const dbl4 *__restrict__ x, const float4 *__restrict__ x32,
+                                                            const GridDev *__restrict__ g, const int32_t *__restrict__ cstart,
+                                                            const int32_t *__restrict__ ccount, const int32_t *__restrict__ sorted,
+                                                            double rv2, PairView oldv, PairView newv, BondView BV,
+                                                            int32_t *err) {
+    extern __shared__ int32_t js[];
+    const int tid = threadIdx.x;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + tid;
     if (i >= n) return;
     const int64_t cap = newv.cap;
-    const d3 xi_ = ld4(x, i);
+    const float4 fi = x32[i];
+    const float rlo = g->rv2_lo, rhi = g->rv2_hi;
+    const dbl4 xd = x[i];
+    const d3 xi_ = mk3(xd.x, xd.y, xd.z);
     int64_t cx = cell_coord(xi_.x, g->lo[0], g->edge, g->dim[0]);
     int64_t cy = cell_coord(xi_.y, g->lo[1], g->edge, g->dim[1]);
     int64_t cz = cell_coord(xi_.z, g->lo[2], g->edge, g->dim[2]);
     int32_t cnt = 0;
     bool overflow = false;
-    // candidates are written straight into the new row's slots (column-major), then sorted there
     for (int64_t z = cz - 1; z <= cz + 1; ++z) {
         if (z < 0 || z >= g->dim[2]) continue;
         for (int64_t y = cy - 1; y <= cy + 1; ++y) {
@@ -351,9 +387,19 @@ __global__ void __launch_bounds__(128) build_rows(int64_t n, const dbl4 *__restr
                 for (int32_t q = 0; q < m; ++q) {
                     int32_t j = sorted[b + q];
                     if (j == (int32_t)i) continue;
-                    if (sqn(sub(xi_, ld4(x, j))) < rv2) {
+                    const float4 fj = x32[j];
+                    const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
+                    const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                    bool in;
+                    if (d2f < rlo)
+                        in = true;
+                    else if (d2f > rhi)
+                        in = false;
+                    else
+                        in = sqn(sub(xi_, ld4(x, j))) < rv2;
+                    if (in) {
                         if (cnt < cap)
-                            newv.nbr[(int64_t)cnt * n + i] = j;
+                            js[(int64_t)cnt * kBuildThreads + tid] = j;
                         else
                             overflow = true;
                         ++cnt;
@@ -366,15 +412,14 @@ __global__ void __launch_bounds__(128) build_rows(int64_t n, const dbl4 *__restr
         set_error(err, LG_DEVERR_LIST_OVERFLOW);
         cnt = (int32_t)cap;
     }
-    // insertion sort of the row (rows hold tens of entries)
-    for (int32_t a = 1; a < cnt; ++a) {
-        int32_t key = newv.nbr[(int64_t)a * n + i];
+    for (int32_t a = 1; a < cnt; ++a) {  // insertion sort (rows hold tens of entries)
+        int32_t key = js[a * kBuildThreads + tid];
         int32_t b = a - 1;
-        while (b >= 0 && newv.nbr[(int64_t)b * n + i] > key) {
-            newv.nbr[(int64_t)(b + 1) * n + i] = newv.nbr[(int64_t)b * n + i];
+        while (b >= 0 && js[b * kBuildThreads + tid] > key) {
+            js[(b + 1) * kBuildThreads + tid] = js[b * kBuildThreads + tid];
             --b;
         }
-        newv.nbr[(int64_t)(b + 1) * n + i] = key;
+        js[(b + 1) * kBuildThreads + tid] = key;
     }
     newv.row_len[i] = cnt;
     // carry springs from the old row (sorted) and mark bonds
@@ -384,7 +429,8 @@ __global__ void __launch_bounds__(128) build_rows(int64_t n, const dbl4 *__restr
     int32_t p = 0;
     for (int32_t k = 0; k < cnt; ++k) {
         const int64_t e = (int64_t)k * n + i;
-        const int32_t j = newv.nbr[e];
+        const int32_t j = js[k * kBuildThreads + tid];
+        newv.nbr[e] = j;
         uint32_t fl = 0;
         while (p < olen && oldv.nbr[(int64_t)p * n + i] < j) ++p;
         if (p < olen && oldv.nbr[(int64_t)p * n + i] == j) {
@@ -395,8 +441,6 @@ __global__ void __launch_bounds__(128) build_rows(int64_t n, const dbl4 *__restr
                 fl |= kXiLive;
             }
         }
-        if (!(fl & kXiLive))
-            for (int q = 0; q < 9; ++q) newv.xi[q * nxs + e] = 0.0;
         for (int b = 0; b < BV.bcap; ++b) {
             const int64_t be = (int64_t)b * n + i;
             if (BV.j[be] == j && BV.intact[be]) {
@@ -460,16 +504,24 @@ void launch_list_build(int64_t n, const dbl4 *x, double rv, int64_t max_cells, L
                        PairView newv, BondView BV, int32_t *err, cudaStream_t st) {
     const int nparts = ls.nparts;
     bbox_partial<<<nparts, 256, 0, st>>>(n, x, ls.part);
-    grid_setup<<<1, 32, 0, st>>>(nparts, ls.part, rv, max_cells, ls.grid);
+    grid_setup<<<1, 256, 0, st>>>(nparts, ls.part, rv, max_cells, ls.grid);
     cudaMemsetAsync(ls.count, 0, sizeof(int32_t) * (size_t)max_cells, st);
     cudaMemsetAsync(ls.fill, 0, sizeof(int32_t) * (size_t)max_cells, st);
     const int threads = 256;
     unsigned blocks = (unsigned)((n + threads - 1) / threads);
-    cell_count<<<blocks, threads, 0, st>>>(n, x, ls.grid, ls.cell_of, ls.count);
+    cell_count<<<blocks, threads, 0, st>>>(n, x, ls.grid, ls.cell_of, ls.count, ls.x32);
     scan_cells<<<1, 1024, 0, st>>>(ls.grid, ls.count, ls.start);
     cell_scatter<<<blocks, threads, 0, st>>>(n, ls.cell_of, ls.start, ls.fill, ls.sorted);
-    unsigned b2 = (unsigned)((n + 127) / 128);
-    build_rows<<<b2, 128, 0, st>>>(n, x, ls.grid, ls.start, ls.count, ls.sorted, rv * rv, oldv, newv, BV, err);
+    unsigned b2 = (unsigned)((n + kBuildThreads - 1) / kBuildThreads);
+    const size_t smem = sizeof(int32_t) * (size_t)newv.cap * kBuildThreads;
+    static thread_local int attr_device = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (attr_device != dev) {
+        cudaFuncSetAttribute(build_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(int32_t) * 255 * kBuildThreads));
+        attr_device = dev;
+    }
+    build_rows<<<b2, kBuildThreads, smem, st>>>(n, x, ls.x32, ls.grid, ls.start, ls.count, ls.sorted, rv * rv, oldv, newv, BV, err);
 }
 
 }  // namespace lg

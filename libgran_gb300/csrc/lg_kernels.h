@@ -12,6 +12,7 @@ struct GridDev {
     double edge;
     int64_t dim[3];
     int64_t ncell;
+    float rv2_lo, rv2_hi;  // FP32 accept / reject bounds of the squared list radius
 };
 
 struct ListScratch {
@@ -23,6 +24,7 @@ struct ListScratch {
     int32_t *start;    // [max_cells]
     int32_t *fill;     // [max_cells]
     int32_t *sorted;   // [n]
+    float4 *x32;       // [n] positions relative to the grid origin, FP32 (candidate filter)
 };
 
 // FP64 path (lg_forces_fp64.cu, compiled with --fmad=false)
@@ -35,10 +37,19 @@ void launch_list_build(int64_t n, const dbl4 *x, double rv, int64_t max_cells, L
 
 // Mixed-precision path (lg_forces_mixed.cu)
 struct MixedExtra {
-    float4 *x32;   // [n] FP32 positions relative to the system origin (culling only)
-    float near2;   // squared culling radius (FP32 positions); beyond it a pair cannot touch and the
-                   // limited Hamaker force is zero
-    double rcut2;  // squared limited-Hamaker cutoff (FP64 separation)
+    float4 *x32;      // [n] FP32 positions relative to the system origin (culling only)
+    float near2;      // squared culling radius (FP32 positions); beyond it a pair cannot touch and the
+                      // limited Hamaker force is zero
+    float contact2f;  // squared contact-candidate radius (FP32 positions, with margin)
+    double rcut2;     // squared limited-Hamaker cutoff (FP64 separation)
+    float inv_mass_h; // 1 / mass of the Hamaker functor
+    double inv_mass_c, inv_inertia_c;  // 1 / mass, 1 / inertia of the contact functor
+    double inv_mass_b, inv_inertia_b;  // 1 / mass, 1 / inertia of the sintered-bond functor
+    double four_rc2, four_rb2, four_rh2;  // (2r)^2 of the contact, bond and Hamaker functors
+    // FP32 copies of the functor parameters (converted once, not per pair)
+    float c_k, c_gn, c_kt, c_gt, c_mus, c_phid, c_kr, c_gr, c_mur, c_phir, c_ko, c_go, c_muo, c_phio, c_r, c_dt;
+    float b_k, b_gn, b_kt, b_gt, b_kr, b_gr, b_ko, b_go, b_r, b_dt;
+    float h_A, h_h0, h_r;
 };
 bool mixed_available();
 void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
@@ -46,6 +57,12 @@ void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairV
 void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, float4 *x32, cudaStream_t st);
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, float4 *x32, cudaStream_t st);
+
+// Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
+void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                                double dt, int move_facets, cudaStream_t st);
+void launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                                 double dt, int move_facets, const MixedExtra &MX, cudaStream_t st);
 
 // Observables (lg_reduce.cu). scratch: at least obs_scratch_doubles(n) doubles of device memory;
 // out: 20 doubles of device memory (column sums, see lg_reduce.cu).

@@ -75,6 +75,9 @@ class System:
     def set_threads_per_row(self, T):
         A.check(A.lib().lg_set_threads_per_row(self.h, int(T)), "lg_set_threads_per_row")
 
+    def set_force_kernel(self, variant):
+        A.check(A.lib().lg_set_force_kernel(self.h, int(variant)), "lg_set_force_kernel")
+
     def reset_acceleration_buffers(self):
         A.check(A.lib().lg_reset_acceleration_buffers(self.h), "lg_reset_acceleration_buffers")
 

@@ -16,15 +16,17 @@ MIXED_TOL = 1e-6
 STATE_FIELDS = (A.LG_FIELD_X, A.LG_FIELD_V, A.LG_FIELD_THETA, A.LG_FIELD_OMEGA)
 
 
-def _desc(n, bm, hm, pairs, precision, mat):
+def _desc(n, bm, hm, pairs, precision, mat, kernel=A.LG_FORCE_KERNEL_AUTO):
     return K.make_desc(n, bm, hm, contact=mat.contact(), sinter=mat.sinter(), hamaker=mat.hamaker(), pairs=pairs,
-                       r_verlet=4.5 * mat.r if pairs == A.LG_PAIRS_VERLET else 0.0, precision=precision)
+                       r_verlet=4.5 * mat.r if pairs == A.LG_PAIRS_VERLET else 0.0, precision=precision,
+                       force_kernel=kernel)
 
 
+@pytest.mark.parametrize("kernel", [A.LG_FORCE_KERNEL_ROWGROUP, A.LG_FORCE_KERNEL_COMPACT], ids=["rowgroup", "compact"])
 @pytest.mark.parametrize("pairs,n", [(A.LG_PAIRS_ALL, 300), (A.LG_PAIRS_VERLET, 4000)])
 @pytest.mark.parametrize("bm,hm", [(A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED), (A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED),
                                    (A.LG_BINARY_CONTACT, A.LG_HAMAKER_FULL), (A.LG_BINARY_SINTER, A.LG_HAMAKER_NONE)])
-def test_mixed_forces_within_1e6_of_fp64(pairs, n, bm, hm):
+def test_mixed_forces_within_1e6_of_fp64(pairs, n, bm, hm, kernel):
     mat = K.Material()
     x0 = generate_aggregate(77, n, mat.r)
     v0 = generate_velocities(77, n, 0.1) - 2e7 * (x0 - x0.mean(0))
@@ -32,7 +34,7 @@ def test_mixed_forces_within_1e6_of_fp64(pairs, n, bm, hm):
     ref.step(mat.dt, 100, 20)  # develop overlaps, springs and contacts
     state = [ref.get(f) for f in STATE_FIELDS]
     a64 = System(_desc(n, bm, hm, pairs, A.LG_PRECISION_FP64, mat), *state)
-    amx = System(_desc(n, bm, hm, pairs, A.LG_PRECISION_MIXED, mat), *state)
+    amx = System(_desc(n, bm, hm, pairs, A.LG_PRECISION_MIXED, mat, kernel), *state)
     assert H.rel_err(amx.get(A.LG_FIELD_A), a64.get(A.LG_FIELD_A)) <= MIXED_TOL
     assert H.rel_err(amx.get(A.LG_FIELD_ALPHA), a64.get(A.LG_FIELD_ALPHA)) <= MIXED_TOL
     # both continue from the same state; the 1e-7-level per-step differences are amplified by the

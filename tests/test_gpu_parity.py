@@ -44,11 +44,13 @@ def test_gpu_reproduces_golden_sequential_rows(path):
     assert s.device_errors() == 0
 
 
+@pytest.mark.parametrize("kernel", [A.LG_FORCE_KERNEL_ROWGROUP, A.LG_FORCE_KERNEL_COMPACT], ids=["rowgroup1", "compact"])
 @pytest.mark.parametrize("path", H.golden_files(), ids=lambda p: os.path.basename(p)[:-4])
-def test_gpu_sequential_rows_are_bit_exact_with_oracle(path):
+def test_gpu_sequential_rows_are_bit_exact_with_oracle(path, kernel):
     g = np.load(path)
     case = H.golden_case(os.path.basename(path)[:-4])
     case["desc"].threads_per_row = 1
+    case["desc"].force_kernel = kernel
     s = System(case["desc"], g["x0"], g["v0"], facets=case.get("facets"), neck=case.get("neck"))
     o = O.OracleSystem(case["desc"], g["x0"], g["v0"], facets=case.get("facets"), neck=case.get("neck"))
     for nst in (1, 9, 90):
@@ -67,11 +69,14 @@ def _aggregate_system(n, seed, bm, hm, pairs, neck_mode=A.LG_NECK_PER_BOND, vsca
     return mat, d, x0, v0
 
 
-@pytest.mark.parametrize("T", [1, 4, 32])
+@pytest.mark.parametrize("T", [1, 4, 32, 0])
 @pytest.mark.parametrize("bm,hm", [(A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED), (A.LG_BINARY_CONTACT, A.LG_HAMAKER_FULL),
                                    (A.LG_BINARY_BREAKING_SINTER, A.LG_HAMAKER_LIMITED)])
 def test_all_pairs_forces_and_positions(T, bm, hm):
     mat, d, x0, v0 = _aggregate_system(256, 21, bm, hm, A.LG_PAIRS_ALL, squeeze=2e7)
+    if T == 0:
+        d.force_kernel = A.LG_FORCE_KERNEL_COMPACT
+        T = 1
     nb = None
     if bm == A.LG_BINARY_BREAKING_SINTER:
         probe = O.OracleSystem(d, x0, v0)
@@ -92,10 +97,15 @@ def test_all_pairs_forces_and_positions(T, bm, hm):
     assert np.array_equal(s.bonds(), o.bonds())
 
 
-@pytest.mark.parametrize("T", [1, 8])
+@pytest.mark.parametrize("T", [1, 8, 0])
 def test_verlet_list_with_spring_carry(T):
     mat, d, x0, v0 = _aggregate_system(2000, 33, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET,
                                        squeeze=3e7)
+    if T == 0:  # compacted kernel: sequential order per row, bit-exact
+        d.force_kernel = A.LG_FORCE_KERNEL_COMPACT
+        T = 1
+    else:
+        d.force_kernel = A.LG_FORCE_KERNEL_ROWGROUP
     d.threads_per_row = T
     s = System(d, x0, v0)
     o = O.OracleSystem(d, x0, v0, threads=8)
