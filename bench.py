@@ -212,29 +212,93 @@ def force_error_mixed_vs_fp64(x0, v0):
 
 
 def time_path(precision, x0, v0, args, l2_flush):
-    """Device-timed K bench steps (each 20 VV steps) with CUDA events on the handle's stream;
-    L2 is flushed before every timed bench step (the flush is outside the timed region)."""
-    import ctypes as C
+    """Device-timed K bench steps (each 20 VV steps, replayed as one CUDA graph) with CUDA events on
+    the handle's stream; L2 is flushed before every timed bench step (the flush is outside the
+    timed region). The force kernel's own duration is then measured on 2 further bench steps with
+    events around every launch (no graphs), so the roofline uses the kernel time alone."""
     from libgran_gb300 import _abi as A
     from libgran_gb300.system import System
     mat, d = workload_desc(precision)
     s = System(d, x0, v0)
     for _ in range(args.warmup):
         s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
-    s.enable_kernel_timing(True)
-    s.force_kernel_time()
     l0 = s.launch_count()
     total_ms = 0.0
     for _ in range(args.steps):
         l2_flush()
         total_ms += s.step_timed(mat.dt, VV_PER_STEP, VV_PER_STEP)
     launches = s.launch_count() - l0
+    s.enable_kernel_timing(True)
+    s.force_kernel_time()
+    for _ in range(2):
+        l2_flush()
+        s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
     kms, kcount = s.force_kernel_time()
     s.enable_kernel_timing(False)
     stats = s.pair_stats()
     errs = s.device_errors()
     return s, mat, {"ms": total_ms, "launches": launches, "kernel_ms": kms, "kernel_launches": kcount,
                     "pair_stats": stats, "device_errors": errs}
+
+
+def batched_section(args, l2_flush):
+    """Batched workload: 4096 independent aggregates (log-normal sizes, median 256, clipped to
+    32..2048, about 1 % clipped per side), sintered bonds + limited Hamaker + frictional contact for
+    non-bonded pairs, velocity Verlet, one handle, 20-step rebuild periods replayed as CUDA graphs,
+    force kernel chosen by the autotuner. Compared with launching a sample of the same aggregates
+    one by one (one handle each)."""
+    from libgran_gb300 import _abi as A
+    from libgran_gb300 import configs as K
+    from libgran_gb300.system import System
+    mat = K.Material()
+    count = int(os.environ.get("LG_BATCH_COUNT", "4096"))
+    sizes = K.lognormal_sizes(count, 256, 32, 2048, seed=2)
+    t0 = time.perf_counter()
+    x0, v0 = K.seeded_aggregates(sizes, 2, mat.r)
+    out = {"systems": count, "particles": int(sizes.sum()), "median_size": float(np.median(sizes)),
+           "max_size": int(sizes.max())}
+
+    def desc(n, prec):
+        return K.make_desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(), sinter=mat.sinter(),
+                           hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r, precision=prec)
+    res = {}
+    for name, prec in (("mixed", A.LG_PRECISION_MIXED), ("fp64", A.LG_PRECISION_FP64)):
+        s = System(desc(int(sizes.sum()), prec), x0, v0, sizes=sizes)
+        kern, T = s.autotune(mat.dt, probe_steps=VV_PER_STEP, rebuild_every=VV_PER_STEP)
+        for _ in range(args.warmup):
+            s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+        ms = 0.0
+        steps = max(2, args.steps // (1 if name == "mixed" else 2))
+        for _ in range(steps):
+            l2_flush()
+            ms += s.step_timed(mat.dt, VV_PER_STEP, VV_PER_STEP)
+        res[name] = {"value": sizes.sum() * VV_PER_STEP * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                     "force_kernel": "compact" if kern == A.LG_FORCE_KERNEL_COMPACT else "rowgroup%d" % T,
+                     "device_errors": s.device_errors()}
+        s.close()
+    # one by one: a sample of the aggregates, each its own handle, launched in turn
+    sample = min(64, count)
+    handles = [System(desc(int(sizes[a]), A.LG_PRECISION_MIXED),
+                      x0[int(sizes[:a].sum()):int(sizes[:a + 1].sum())],
+                      v0[int(sizes[:a].sum()):int(sizes[:a + 1].sum())]) for a in range(sample)]
+    for h in handles:
+        h.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+    import torch
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(2):
+        for h in handles:
+            h.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+    for h in handles:
+        h.device_errors()  # synchronises each handle's stream
+    el = time.perf_counter() - t
+    res["one_by_one_mixed"] = {"value": sizes[:sample].sum() * VV_PER_STEP * 2 / el, "sample_systems": sample}
+    for h in handles:
+        h.close()
+    out.update(res)
+    out["batched_over_one_by_one"] = res["mixed"]["value"] / res["one_by_one_mixed"]["value"]
+    out["setup_s"] = time.perf_counter() - t0
+    return out
 
 
 def e2e_path(s, mat, args, x0, v0):
@@ -316,6 +380,9 @@ def run_gb300(args, rank, world):
     peak = peaks.get("hbm_gbs", 6800.0)
     traffic = read_profile_traffic("forces_mixed_c1")
     cpu = cpu_reference_rate(x0, v0, target_s=float(os.environ.get("LG_CPU_SAMPLE_S", "12")))
+    batched = None
+    if os.environ.get("LG_BENCH_BATCHED", "1") != "0":
+        batched = batched_section(args, l2_flush)
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tm["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -337,6 +404,7 @@ def run_gb300(args, rank, world):
         "cpu_baseline": cpu,
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
         "device_errors": tm["device_errors"],
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
 

@@ -265,6 +265,38 @@ int lg_generate_rsa_aggregate(uint64_t seed, int64_t n, double r, double *x);
 /* Uniform random velocity components in [-vmax, vmax] from a seeded stream. Host-only. */
 int lg_generate_velocities(uint64_t seed, int64_t n, double vmax, double *v);
 
+/* CUDA graphs: lg_step replays each whole rebuild period (or 16 steps without a Verlet list) as one
+ * captured graph from the second period on (default on). 0 disables and frees the graphs. */
+int lg_set_graphs(lg_system *sys, int32_t enable);
+
+/* ---- batches: many independent aggregates in one handle ------------------------------------
+ * Every system of a batch is simulated exactly as it would be alone (its own bonds, pair rows and
+ * springs; rows never cross systems), with the functor parameters of `desc` shared by all. desc
+ * n_part is the total particle count, sizes[n_systems] the particle count of each system, and the
+ * state arrays hold the systems one after another, each in its own coordinates. Verlet pairs only.
+ * Facets apply to every system in that system's coordinates. Neck strengths: per bond, system by
+ * system. All single-system calls (lg_step, lg_get, ...) act on the whole batch. */
+int lg_batch_create(const lg_system_desc *desc, int64_t n_systems, const int64_t *sizes, const double *x0,
+                    const double *v0, const double *theta0, const double *omega0, const lg_facet_desc *facets,
+                    const double *neck_strengths, int64_t n_neck_strengths, int device, lg_system **out);
+/* Number of systems (0 for a single system) and, if offsets is not NULL, their prefix offsets
+ * (n_systems + 1 values). */
+int lg_batch_info(lg_system *sys, int64_t *n_systems, int64_t *offsets);
+/* Observables of every system: out[n_systems]. */
+int lg_batch_get_observables(lg_system *sys, lg_observables *out);
+
+/* Device-state snapshot of the handle (state, springs, bonds, pair rows, facets) and its restore; one
+ * snapshot slot per handle, allocated on first use (about the handle's own device footprint). */
+int lg_snapshot(lg_system *sys);
+int lg_restore(lg_system *sys);
+
+/* Project autotuner: times the force-kernel variants (compacted; row groups of 1..32 lanes) for
+ * probe_steps steps on the live system between a snapshot and its restore (the state afterwards is
+ * the state before the call) and keeps the fastest; the choice is cached per
+ * (precision, pair mode, functor set, log2 size, batch) when use_cache is 1. */
+int lg_autotune(lg_system *sys, double dt, int64_t probe_steps, int64_t rebuild_every, int32_t *force_kernel,
+                int32_t *threads_per_row, int32_t use_cache);
+
 /* Time `nsteps` steps with CUDA events on the handle's stream (no host copies inside); ms_out
  * receives the elapsed device time. Same semantics as lg_step. */
 int lg_step_timed(lg_system *sys, double dt, int64_t nsteps, int64_t rebuild_every, float *ms_out);

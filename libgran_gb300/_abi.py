@@ -118,6 +118,14 @@ def _declare(L):
         "lg_get_launch_count": (C.c_int, [vp, P(i64)]),
         "lg_set_threads_per_row": (C.c_int, [vp, i32]),
         "lg_set_force_kernel": (C.c_int, [vp, i32]),
+        "lg_set_graphs": (C.c_int, [vp, i32]),
+        "lg_batch_create": (C.c_int, [P(lg_system_desc), i64, P(i64), P(d), P(d), P(d), P(d), P(lg_facet_desc),
+                                      P(d), i64, C.c_int, P(vp)]),
+        "lg_batch_info": (C.c_int, [vp, P(i64), P(i64)]),
+        "lg_batch_get_observables": (C.c_int, [vp, P(lg_observables)]),
+        "lg_autotune": (C.c_int, [vp, d, i64, i64, P(i32), P(i32), i32]),
+        "lg_snapshot": (C.c_int, [vp]),
+        "lg_restore": (C.c_int, [vp]),
         "lg_get_pair_stats": (C.c_int, [vp, P(lg_pair_stats)]),
         "lg_enable_kernel_timing": (C.c_int, [vp, i32]),
         "lg_get_force_kernel_time": (C.c_int, [vp, P(d), P(i64)]),

@@ -103,3 +103,35 @@ class Material:
 
     def hamaker(self):
         return hamaker_params(self.A, self.h0, self.r, self.m, r_cutoff=self.r_cut)
+
+
+def lognormal_sizes(count, median, lo, hi, seed, clip_frac=0.01):
+    """Aggregate sizes: log-normal with the given median, sigma chosen so that about clip_frac of the
+    draws fall outside [lo, hi] on each side of a symmetric range, clipped to [lo, hi]."""
+    import numpy as np
+    from math import log
+    z = 2.326347874040841  # standard-normal quantile of 0.99
+    sigma = log(hi / median) / z
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.normal(log(median), sigma, size=count))
+    return np.clip(np.rint(n), lo, hi).astype(np.int64)
+
+
+def loguniform_sizes(count, lo, hi, seed):
+    """Aggregate sizes log-uniform in [lo, hi]."""
+    import numpy as np
+    from math import log
+    rng = np.random.default_rng(seed)
+    return np.clip(np.rint(np.exp(rng.uniform(log(lo), log(hi), size=count))), lo, hi).astype(np.int64)
+
+
+def seeded_aggregates(sizes, config_id, r, vmax=0.1):
+    """Positions and velocities of a list of aggregates; aggregate a uses seed config_id * 2^32 + a."""
+    import numpy as np
+    from .system import generate_aggregate, generate_velocities
+    xs, vs = [], []
+    for a, n in enumerate(sizes):
+        seed = (int(config_id) << 32) + a
+        xs.append(generate_aggregate(seed, int(n), r))
+        vs.append(generate_velocities(seed, int(n), vmax))
+    return np.concatenate(xs), np.concatenate(vs)

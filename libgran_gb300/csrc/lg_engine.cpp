@@ -264,8 +264,14 @@ static int download4(const dbl4 *src, double *aos, int64_t n, cudaStream_t st) {
     return LG_OK;
 }
 
+void lg_system::drop_graphs() {
+    for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+}
+
 void lg_system::release() {
     if (device >= 0) cudaSetDevice(device);
+    drop_graphs();
     for (void *p : allocations) cudaFree(p);
     allocations.clear();
     if (stream) cudaStreamDestroy(stream);
@@ -305,7 +311,8 @@ static int rebuild_list(lg_system *s) {
     PairView &newv = s->pv[1 - s->pcur];
     PairView o = oldv;
     if (!s->list_built) o.row_len = nullptr;
-    launch_list_build(s->P.n, s->x, s->P.r_verlet, s->max_cells, s->ls, o, newv, s->bv, s->err, s->stream);
+    BatchView B{s->d_agg, s->d_hoff};
+    launch_list_build(s->P.n, s->x, B, s->P.r_verlet, s->max_cells, s->ls, o, newv, s->bv, s->err, s->stream);
     s->launches += 7;
     s->pcur = 1 - s->pcur;
     s->list_built = true;
@@ -370,7 +377,7 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every) {
     const double hdt = dt / 2.0;
     if (s->precision == LG_PRECISION_MIXED)
         launch_kick_drift_mixed(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->origin,
-                                s->x32, s->stream);
+                                s->d_agg, s->d_orig, s->x32, s->stream);
     else
         launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->stream);
     s->launches += 1;
@@ -409,11 +416,25 @@ static int check_args(const lg_system_desc *d) {
 }
 
 static int create_impl(const lg_system_desc *d, const double *x0, const double *v0, const double *th0, const double *om0,
-                       const lg_facet_desc *facets, const double *neck, int64_t n_neck, int device, lg_system *s) {
+                       const lg_facet_desc *facets, const double *neck, int64_t n_neck, int device, lg_system *s,
+                       int64_t n_sys = 0, const int64_t *sizes = nullptr) {
     LG_TRY(check_args(d));
     if (!x0 || !v0 || !th0 || !om0) return lg_fail(LG_E_INVALID, "lg_create: null state pointer");
     if (d->n_facets > 0 && !facets) return lg_fail(LG_E_INVALID, "lg_create: n_facets > 0 but facets is null");
     const int64_t n = d->n_part;
+    if (n_sys > 0) {
+        if (!sizes) return lg_fail(LG_E_INVALID, "lg_batch_create: null sizes");
+        if (d->pairs != LG_PAIRS_VERLET) return lg_fail(LG_E_INVALID, "lg_batch_create: batches need LG_PAIRS_VERLET");
+        s->n_systems = n_sys;
+        s->sys_off.assign((size_t)n_sys + 1, 0);
+        for (int64_t q = 0; q < n_sys; ++q) {
+            if (sizes[q] < 1) return lg_fail(LG_E_INVALID, "lg_batch_create: system %lld has size %lld", (long long)q, (long long)sizes[q]);
+            s->sys_off[q + 1] = s->sys_off[q] + sizes[q];
+        }
+        if (s->sys_off[n_sys] != n)
+            return lg_fail(LG_E_INVALID, "lg_batch_create: sizes add up to %lld, desc.n_part is %lld",
+                           (long long)s->sys_off[n_sys], (long long)n);
+    }
     s->device = device;
     LG_CUDA(cudaSetDevice(device));
     LG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -421,6 +442,9 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     LG_CUDA(cudaEventCreate(&s->ev1));
     s->desc = *d;
     s->precision = d->precision;
+    if (d->n_facets > 0) s->facet_descs.assign(facets, facets + d->n_facets);
+    if (neck && n_neck > 0) s->neck_copy.assign(neck, neck + n_neck);
+    if (n_sys > 0) s->sizes_copy.assign(sizes, sizes + n_sys);
     s->facet_auto_move = d->facet_auto_move != 0;
 
     Params &P = s->P;
@@ -460,8 +484,22 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     // bonds
     std::vector<std::pair<int32_t, int32_t>> bonds;
     const bool sinter = d->binary_model == LG_BINARY_SINTER || d->binary_model == LG_BINARY_BREAKING_SINTER;
-    if (sinter) LG_TRY(lg_detect_bonds(x0, n, d->sinter.r_part, d->sinter.critical_separation,
-                                       d->binary_model == LG_BINARY_SINTER, bonds));
+    if (sinter) {
+        if (s->n_systems == 0) {
+            LG_TRY(lg_detect_bonds(x0, n, d->sinter.r_part, d->sinter.critical_separation,
+                                   d->binary_model == LG_BINARY_SINTER, bonds));
+        } else {  // every system's bonds are found alone, in the order a standalone system finds them
+            s->n_bonds_initial_sys.assign((size_t)s->n_systems, 0);
+            std::vector<std::pair<int32_t, int32_t>> local;
+            for (int64_t q = 0; q < s->n_systems; ++q) {
+                const int64_t b = s->sys_off[q], e = s->sys_off[q + 1];
+                LG_TRY(lg_detect_bonds(x0 + 3 * b, e - b, d->sinter.r_part, d->sinter.critical_separation,
+                                       d->binary_model == LG_BINARY_SINTER, local));
+                for (auto &pr : local) bonds.emplace_back((int32_t)(pr.first + b), (int32_t)(pr.second + b));
+                s->n_bonds_initial_sys[q] = 2 * (int64_t)local.size();
+            }
+        }
+    }
     if (d->binary_model == LG_BINARY_BREAKING_SINTER && n_neck != 0 && n_neck != (int64_t)bonds.size())
         return lg_fail(LG_E_INVALID, "lg_create: %lld neck strengths given but %zu bonds were detected", (long long)n_neck,
                        bonds.size());
@@ -532,6 +570,46 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     LG_TRY(upload4(s->w[0], om0, n, s->stream));
     s->vcur = 0;
 
+    // batch segmentation: system index per particle, hashing offsets that keep systems apart
+    if (s->n_systems > 0) {
+        const int64_t ns = s->n_systems;
+        std::vector<int32_t> agg((size_t)n);
+        std::vector<double> cen(3 * (size_t)ns), rad((size_t)ns, 0.0);
+        double rmax = 0.0;
+        for (int64_t q = 0; q < ns; ++q) {
+            const int64_t b = s->sys_off[q], e = s->sys_off[q + 1];
+            for (int k = 0; k < 3; ++k) {
+                double sum = 0.0;
+                for (int64_t i = b; i < e; ++i) sum += x0[3 * i + k];
+                cen[3 * q + k] = sum / (double)(e - b);
+            }
+            for (int64_t i = b; i < e; ++i) {
+                agg[i] = (int32_t)q;
+                double r2 = 0.0;
+                for (int k = 0; k < 3; ++k) r2 += (x0[3 * i + k] - cen[3 * q + k]) * (x0[3 * i + k] - cen[3 * q + k]);
+                rad[q] = std::max(rad[q], std::sqrt(r2));
+            }
+            rmax = std::max(rmax, rad[q]);
+        }
+        // lattice spacing: two system radii, room for growth, and two list radii
+        const double L = 4.0 * rmax + 2.0 * d->r_verlet + 8.0 * d->contact.r_part + 1e-12;
+        int64_t m = 1;
+        while (m * m * m < ns) ++m;
+        std::vector<dbl4> hoff((size_t)ns);
+        for (int64_t q = 0; q < ns; ++q) {
+            const double gx = (double)(q % m) * L, gy = (double)((q / m) % m) * L, gz = (double)(q / (m * m)) * L;
+            hoff[q] = make_double4_32a(gx - cen[3 * q], gy - cen[3 * q + 1], gz - cen[3 * q + 2], 0.0);
+        }
+        LG_TRY(s->alloc(&s->d_agg, (size_t)n));
+        LG_TRY(s->alloc(&s->d_hoff, (size_t)ns));
+        LG_TRY(s->alloc(&s->d_sys_off, (size_t)ns + 1));
+        LG_TRY(s->alloc(&s->d_centres, 3 * (size_t)ns));
+        LG_TRY(s->alloc(&s->d_sys_obs, 20 * (size_t)ns));
+        LG_CUDA(cudaMemcpy(s->d_agg, agg.data(), sizeof(int32_t) * agg.size(), cudaMemcpyHostToDevice));
+        LG_CUDA(cudaMemcpy(s->d_hoff, hoff.data(), sizeof(dbl4) * hoff.size(), cudaMemcpyHostToDevice));
+        LG_CUDA(cudaMemcpy(s->d_sys_off, s->sys_off.data(), sizeof(int64_t) * s->sys_off.size(), cudaMemcpyHostToDevice));
+    }
+
     // facets
     const int nf = std::max(d->n_facets, 1);
     LG_TRY(s->alloc(&s->fv[0], 9 * (size_t)nf));
@@ -569,19 +647,23 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         s->pv[1] = pv;
         s->pcur = 0;
     } else {
-        int64_t cap = d->max_neighbors > 0 ? d->max_neighbors : 96;
+        int64_t cap = d->max_neighbors > 0 ? d->max_neighbors : 48;
         cap = std::min<int64_t>(cap, std::max<int64_t>(n - 1, 1));
-        for (int q = 0; q < 2; ++q) {
-            PairView &pv = s->pv[q];
-            pv.cap = cap;
-            LG_TRY(s->alloc(&pv.nbr, (size_t)(cap * n)));
-            LG_TRY(s->alloc(&pv.row_len, (size_t)n));
-            LG_TRY(s->alloc(&pv.flags, (size_t)(cap * n)));
-            LG_TRY(s->alloc(&pv.xi, 9 * (size_t)(cap * n)));
-            LG_CUDA(cudaMemset(pv.row_len, 0, sizeof(int32_t) * n));
-        }
+        auto alloc_rows = [&](int64_t c) -> int {
+            for (int q = 0; q < 2; ++q) {
+                PairView &pv = s->pv[q];
+                pv.cap = c;
+                LG_TRY(s->alloc(&pv.nbr, (size_t)(c * n)));
+                LG_TRY(s->alloc(&pv.row_len, (size_t)n));
+                LG_TRY(s->alloc(&pv.flags, (size_t)(c * n)));
+                LG_TRY(s->alloc(&pv.xi, 9 * (size_t)(c * n)));
+                LG_CUDA(cudaMemset(pv.row_len, 0, sizeof(int32_t) * n));
+            }
+            return LG_OK;
+        };
+        LG_TRY(alloc_rows(cap));
         s->pcur = 0;
-        s->max_cells = std::max<int64_t>(64, 4 * n);
+        s->max_cells = std::max<int64_t>(64, (s->n_systems > 0 ? 8 : 4) * n);
         s->ls.nparts = 256;
         LG_TRY(s->alloc(&s->ls.part, 6 * 256));
         LG_TRY(s->alloc(&s->ls.grid, 1));
@@ -591,7 +673,30 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         LG_TRY(s->alloc(&s->ls.fill, (size_t)s->max_cells));
         LG_TRY(s->alloc(&s->ls.sorted, (size_t)n));
         LG_TRY(s->alloc(&s->ls.x32, (size_t)n));
+        LG_TRY(s->alloc(&s->ls.max_row, 1));
+        LG_CUDA(cudaMemset(s->ls.max_row, 0, sizeof(int32_t)));
         LG_TRY(rebuild_list(s));
+        // without an explicit max_neighbors the row capacity follows the initial state: rows get
+        // 1.5x the longest initial row (at most 255)
+        int32_t mr = 0;
+        LG_CUDA(cudaMemcpy(&mr, s->ls.max_row, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        const int64_t want = std::min<int64_t>(255, std::max<int64_t>(8, (int64_t)(1.5 * mr) + 1));
+        if (d->max_neighbors == 0 && want > cap && cap < std::max<int64_t>(n - 1, 1)) {
+            for (int q = 0; q < 2; ++q) {
+                PairView &pv = s->pv[q];
+                void *old_ptrs[4] = {pv.nbr, pv.row_len, pv.flags, pv.xi};
+                for (void *o : old_ptrs) {
+                    cudaFree(o);
+                    s->allocations.erase(std::find(s->allocations.begin(), s->allocations.end(), o));
+                }
+            }
+            cap = std::min<int64_t>(want, std::max<int64_t>(n - 1, 1));
+            LG_TRY(alloc_rows(cap));
+            s->list_built = false;
+            s->pcur = 0;
+            LG_CUDA(cudaMemset(s->err, 0, sizeof(int32_t)));
+            LG_TRY(rebuild_list(s));
+        }
     }
     LG_TRY(s->alloc(&s->obs_scratch, (size_t)obs_scratch_doubles(n)));
     LG_TRY(s->alloc(&s->obs_out, 32));
@@ -603,7 +708,22 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
             s->origin[c] = sum / (double)n;
         }
         LG_TRY(s->alloc(&s->x32, (size_t)n));
-        launch_positions_to_f32(n, s->x, s->origin, s->x32, s->stream);
+        if (s->n_systems > 0) {
+            std::vector<dbl4> org((size_t)s->n_systems);
+            for (int64_t q = 0; q < s->n_systems; ++q) {
+                double c[3];
+                const int64_t b = s->sys_off[q], e = s->sys_off[q + 1];
+                for (int k = 0; k < 3; ++k) {
+                    double sum = 0.0;
+                    for (int64_t i = b; i < e; ++i) sum += x0[3 * i + k];
+                    c[k] = e > b ? sum / (double)(e - b) : 0.0;
+                }
+                org[q] = make_double4_32a(c[0], c[1], c[2], 0.0);
+            }
+            LG_TRY(s->alloc(&s->d_orig, (size_t)s->n_systems));
+            LG_CUDA(cudaMemcpy(s->d_orig, org.data(), sizeof(dbl4) * org.size(), cudaMemcpyHostToDevice));
+        }
+        launch_positions_to_f32(n, s->x, s->origin, s->d_agg, s->d_orig, s->x32, s->stream);
         double near = 0.0;
         if (d->binary_model != LG_BINARY_NONE) near = std::max(near, 2.0 * d->contact.r_part);
         if (sinter) near = std::max(near, 2.0 * d->sinter.r_part);
@@ -678,11 +798,79 @@ extern "C" int lg_destroy(lg_system *s) {
         LG_CUDA(cudaSetDevice((s)->device));                           \
     } while (0)
 
+// Run `period` steps as one CUDA graph (captured on first use for this pointer parity). The host
+// bookkeeping (buffer parities, step index) advances exactly as step_once advances it.
+static int run_period_graph(lg_system *s, double dt, int64_t period, int64_t rebuild_every) {
+    lg_system::GraphKey key{dt, period, s->kernel, s->T, s->vcur, s->pcur, s->fcur};
+    for (auto &g : s->graphs) {
+        if (!(g.key == key)) continue;
+        LG_CUDA(cudaGraphLaunch(g.exec, s->stream));
+        // replay the host-side state transitions of `period` steps
+        for (int64_t k = 0; k < period; ++k) {
+            if (s->P.pairs == LG_PAIRS_VERLET && rebuild_every > 0 && (s->step_index % rebuild_every) == 0) {
+                s->pcur = 1 - s->pcur;
+                s->list_built = true;
+            }
+            s->vcur = 1 - s->vcur;
+            if (s->facet_auto_move && s->P.n_facets > 0) s->fcur = 1 - s->fcur;
+            s->step_index++;
+        }
+        s->launches += g.launches;
+        return LG_OK;
+    }
+    const int64_t l0 = s->launches;
+    LG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = LG_OK;
+    for (int64_t k = 0; k < period && rc == LG_OK; ++k) rc = step_once(s, dt, rebuild_every);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ec = cudaStreamEndCapture(s->stream, &graph);
+    if (rc != LG_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (ec != cudaSuccess) return lg_fail(LG_E_CUDA, "stream capture failed: %s", cudaGetErrorString(ec));
+    cudaGraphExec_t exec = nullptr;
+    ec = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ec != cudaSuccess) return lg_fail(LG_E_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ec));
+    s->graphs.push_back({key, exec, s->launches - l0});
+    LG_CUDA(cudaGraphLaunch(exec, s->stream));
+    return LG_OK;
+}
+
 extern "C" int lg_step(lg_system *s, double dt, int64_t nsteps, int64_t rebuild_every) {
     LG_HANDLE(s);
     if (nsteps < 0) return lg_fail(LG_E_INVALID, "lg_step: nsteps < 0");
     if (!std::isfinite(dt)) return lg_fail(LG_E_INVALID, "lg_step: dt is not finite");
-    for (int64_t k = 0; k < nsteps; ++k) LG_TRY(step_once(s, dt, rebuild_every));
+    const bool verlet = s->P.pairs == LG_PAIRS_VERLET;
+    const int64_t period = (verlet && rebuild_every > 0) ? rebuild_every : 16;
+    int64_t k = 0;
+    while (k < nsteps) {
+        const bool aligned = !(verlet && rebuild_every > 0) || (s->step_index % rebuild_every) == 0;
+        if (s->use_graphs && !s->timing && aligned && nsteps - k >= period && s->periods_run > 0 && period <= 4096) {
+            LG_TRY(run_period_graph(s, dt, period, rebuild_every));
+            k += period;
+            s->periods_run++;
+            continue;
+        }
+        // eager steps: up to the next period boundary
+        int64_t stop = nsteps;
+        if (verlet && rebuild_every > 0) {
+            const int64_t to_boundary = rebuild_every - (s->step_index % rebuild_every);
+            stop = std::min<int64_t>(nsteps, k + to_boundary);
+        } else {
+            stop = std::min<int64_t>(nsteps, k + period);
+        }
+        for (; k < stop; ++k) LG_TRY(step_once(s, dt, rebuild_every));
+        s->periods_run++;
+    }
+    return LG_OK;
+}
+
+extern "C" int lg_set_graphs(lg_system *s, int32_t enable) {
+    LG_HANDLE(s);
+    s->use_graphs = enable != 0;
+    if (!s->use_graphs) s->drop_graphs();
     return LG_OK;
 }
 
@@ -728,7 +916,7 @@ extern "C" int lg_set(lg_system *s, int field, const double *in) {
     if (!p || !in) return lg_fail(LG_E_INVALID, "lg_set: bad field %d or null input", field);
     LG_TRY(upload4(p, in, s->P.n, s->stream));
     if (field == LG_FIELD_X && s->x32) {
-        launch_positions_to_f32(s->P.n, s->x, s->origin, s->x32, s->stream);
+        launch_positions_to_f32(s->P.n, s->x, s->origin, s->d_agg, s->d_orig, s->x32, s->stream);
         s->launches += 1;
         LG_CUDA(cudaGetLastError());
     }
@@ -878,6 +1066,9 @@ extern "C" int lg_get_pair_springs(lg_system *s, int64_t i, int64_t j, double *o
     }
     if (k < 0) return LG_OK;
     const size_t e = (size_t)(k * n + i), xs = (size_t)(pv.cap * n);
+    uint32_t fl = 0;
+    LG_CUDA(cudaMemcpy(&fl, pv.flags + e, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (!(fl & kXiLive)) return LG_OK;  // springs of a slot that is not live are zero
     for (int q = 0; q < 9; ++q) LG_CUDA(cudaMemcpy(out9 + q, pv.xi + q * xs + e, sizeof(double), cudaMemcpyDeviceToHost));
     return LG_OK;
 }
@@ -958,5 +1149,233 @@ extern "C" int lg_get_pair_stats(lg_system *s, lg_pair_stats *out) {
     out->max_row_length = mx;
     out->live_contact_slots = live;
     out->bonded_slots = bonded;
+    return LG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Batches
+// ------------------------------------------------------------------------------------------------
+extern "C" int lg_batch_create(const lg_system_desc *desc, int64_t n_systems, const int64_t *sizes, const double *x0,
+                               const double *v0, const double *theta0, const double *omega0,
+                               const lg_facet_desc *facets, const double *neck_strengths, int64_t n_neck_strengths,
+                               int device, lg_system **out) {
+    if (!out) return lg_fail(LG_E_INVALID, "lg_batch_create: null output handle");
+    *out = nullptr;
+    if (n_systems < 1) return lg_fail(LG_E_INVALID, "lg_batch_create: n_systems < 1");
+    lg_system *s = new (std::nothrow) lg_system();
+    if (!s) return lg_fail(LG_E_NOMEM, "lg_batch_create: host allocation failed");
+    int rc = create_impl(desc, x0, v0, theta0, omega0, facets, neck_strengths, n_neck_strengths, device, s, n_systems,
+                         sizes);
+    if (rc != LG_OK) {
+        std::string keep = g_last_error;
+        s->release();
+        delete s;
+        g_last_error = keep;
+        return rc;
+    }
+    *out = s;
+    return LG_OK;
+}
+
+extern "C" int lg_batch_info(lg_system *s, int64_t *n_systems, int64_t *offsets) {
+    LG_HANDLE(s);
+    if (!n_systems) return lg_fail(LG_E_INVALID, "lg_batch_info: null count");
+    *n_systems = s->n_systems;
+    if (offsets)
+        for (int64_t q = 0; q <= s->n_systems; ++q) offsets[q] = s->sys_off[q];
+    return LG_OK;
+}
+
+// Observables of every system of a batch (out[n_systems]).
+extern "C" int lg_batch_get_observables(lg_system *s, lg_observables *out) {
+    LG_HANDLE(s);
+    if (!out) return lg_fail(LG_E_INVALID, "lg_batch_get_observables: null output");
+    if (s->n_systems == 0) return lg_get_observables(s, out);
+    const Params &P = s->P;
+    const bool sint = P.binary_model == LG_BINARY_SINTER || P.binary_model == LG_BINARY_BREAKING_SINTER;
+    const double m = sint ? P.sinter.mass : (P.binary_model == LG_BINARY_CONTACT ? P.contact.mass : P.hamaker.mass);
+    const double I = sint ? P.sinter.inertia : P.contact.inertia;
+    StateView S = state_view(s, false);
+    // per-particle rows (the single-system reduction is launched too; its result is unused)
+    launch_observables(P, S, s->pv[s->pcur], s->bv, m, I, s->obs_scratch, s->obs_out, s->stream);
+    launch_segmented_sums(s->n_systems, s->d_sys_off, s->obs_scratch, s->d_sys_obs, s->stream);
+    s->launches += 3;
+    LG_CUDA(cudaGetLastError());
+    const int64_t ns = s->n_systems;
+    std::vector<double> h((size_t)(20 * ns));
+    LG_CUDA(cudaMemcpyAsync(h.data(), s->d_sys_obs, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    std::vector<double> c((size_t)(3 * ns));
+    for (int64_t q = 0; q < ns; ++q) {
+        const double nn = (double)(s->sys_off[q + 1] - s->sys_off[q]);
+        for (int k = 0; k < 3; ++k) c[3 * q + k] = h[20 * q + 12 + k] / nn;
+    }
+    LG_CUDA(cudaMemcpyAsync(s->d_centres, c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice, s->stream));
+    launch_segmented_rg(P.n, ns, s->d_sys_off, s->x, s->d_centres, s->obs_scratch, s->d_sys_obs, s->stream);
+    s->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaMemcpyAsync(h.data(), s->d_sys_obs, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    for (int64_t q = 0; q < ns; ++q) {
+        const double *hq = h.data() + 20 * q;
+        const double nn = (double)(s->sys_off[q + 1] - s->sys_off[q]);
+        lg_observables &o = out[q];
+        memset(&o, 0, sizeof(o));
+        o.ke_total = hq[0];
+        o.ke_translational = hq[1] / 2.0;
+        o.ke_rotational = hq[2] / 2.0;
+        o.linear_momentum = m * std::sqrt((hq[3] * hq[3] + hq[4] * hq[4]) + hq[5] * hq[5]);
+        double L[3] = {hq[6] + hq[9], hq[7] + hq[10], hq[8] + hq[11]};
+        o.angular_momentum = std::sqrt((L[0] * L[0] + L[1] * L[1]) + L[2] * L[2]);
+        for (int k = 0; k < 3; ++k) o.center_of_mass[k] = c[3 * q + k];
+        o.radius_of_gyration = std::sqrt(hq[18] / nn);
+        o.potential_energy = hq[15];
+        o.n_contacts = (int64_t)hq[16];
+        o.n_bonds = (int64_t)hq[17];
+        o.n_bonds_initial = s->n_bonds_initial_sys.empty() ? 0 : s->n_bonds_initial_sys[q];
+    }
+    return LG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Autotuner: force kernel and lanes per row, measured on a clone of the system
+// ------------------------------------------------------------------------------------------------
+#include <map>
+#include <mutex>
+#include <tuple>
+
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
+
+static int snapshot_take(lg_system *s) {
+    if (s->snap.empty()) {
+        const int64_t n = s->P.n;
+        auto addb = [&](void *live, size_t bytes) { s->snap.push_back({live, nullptr, bytes}); };
+        addb(s->x, sizeof(dbl4) * n);
+        addb(s->th, sizeof(dbl4) * n);
+        for (int q = 0; q < 2; ++q) {
+            addb(s->v[q], sizeof(dbl4) * n);
+            addb(s->w[q], sizeof(dbl4) * n);
+        }
+        addb(s->a, sizeof(dbl4) * n);
+        addb(s->al, sizeof(dbl4) * n);
+        const int nf = std::max(s->P.n_facets, 1);
+        addb(s->sxi, sizeof(double) * 9 * (size_t)nf * (size_t)n);
+        addb(s->fv[0], sizeof(double) * 9 * (size_t)nf);
+        addb(s->fv[1], sizeof(double) * 9 * (size_t)nf);
+        addb(s->err, sizeof(int32_t));
+        if (s->x32) addb(s->x32, sizeof(float4) * n);
+        const int npv = s->P.pairs == LG_PAIRS_VERLET ? 2 : 1;
+        for (int q = 0; q < npv; ++q) {
+            PairView &pv = s->pv[q];
+            const size_t slots = (size_t)(pv.cap * n);
+            if (pv.nbr) addb(pv.nbr, sizeof(int32_t) * slots);
+            if (pv.row_len) addb(pv.row_len, sizeof(int32_t) * n);
+            addb(pv.flags, sizeof(uint32_t) * slots);
+            addb(pv.xi, sizeof(double) * 9 * slots);
+        }
+        const size_t bs = (size_t)s->bv.bcap * (size_t)n;
+        addb(s->bv.intact, bs);
+        addb(s->bv.xi, sizeof(double) * 9 * bs);
+        for (auto &b : s->snap) {
+            void *p = nullptr;
+            cudaError_t e = cudaMalloc(&p, b.bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                for (auto &c : s->snap)
+                    if (c.copy) cudaFree(c.copy);
+                s->snap.clear();
+                return lg_fail(LG_E_NOMEM, "snapshot: cudaMalloc of %zu bytes failed", b.bytes);
+            }
+            b.copy = p;
+            s->allocations.push_back(p);
+        }
+    }
+    for (auto &b : s->snap) LG_CUDA(cudaMemcpyAsync(b.copy, b.live, b.bytes, cudaMemcpyDeviceToDevice, s->stream));
+    s->snap_vcur = s->vcur;
+    s->snap_pcur = s->pcur;
+    s->snap_fcur = s->fcur;
+    s->snap_step = s->step_index;
+    s->snap_built = s->list_built;
+    return LG_OK;
+}
+
+static int snapshot_restore(lg_system *s) {
+    if (s->snap.empty()) return lg_fail(LG_E_STATE, "snapshot: nothing to restore");
+    for (auto &b : s->snap) LG_CUDA(cudaMemcpyAsync(b.live, b.copy, b.bytes, cudaMemcpyDeviceToDevice, s->stream));
+    s->vcur = s->snap_vcur;
+    s->pcur = s->snap_pcur;
+    s->fcur = s->snap_fcur;
+    s->step_index = s->snap_step;
+    s->list_built = s->snap_built;
+    return LG_OK;
+}
+
+extern "C" int lg_snapshot(lg_system *s) {
+    LG_HANDLE(s);
+    return snapshot_take(s);
+}
+
+extern "C" int lg_restore(lg_system *s) {
+    LG_HANDLE(s);
+    return snapshot_restore(s);
+}
+
+extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t rebuild_every, int32_t *kernel_out,
+                           int32_t *T_out, int32_t use_cache) {
+    LG_HANDLE(s);
+    if (probe_steps < 1) return lg_fail(LG_E_INVALID, "lg_autotune: probe_steps < 1");
+    int lg2 = 0;
+    while (((int64_t)1 << (lg2 + 1)) <= s->P.n) ++lg2;
+    auto key = std::make_tuple(s->precision, s->P.pairs, s->P.binary_model, s->P.hamaker_model, lg2,
+                               s->n_systems > 0 ? 1 : 0);
+    if (use_cache) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            s->kernel = it->second.first;
+            s->T = it->second.second;
+            if (kernel_out) *kernel_out = s->kernel;
+            if (T_out) *T_out = s->T;
+            return LG_OK;
+        }
+    }
+    // candidates run on the live system between a snapshot and its restore
+    LG_TRY(snapshot_take(s));
+    const int keep_kernel = s->kernel, keep_T = s->T;
+    const int64_t keep_launch = s->launches;
+    std::vector<std::pair<int, int>> cands;
+    cands.emplace_back(LG_FORCE_KERNEL_COMPACT, 1);
+    for (int T = 1; T <= 32; T *= 2) cands.emplace_back(LG_FORCE_KERNEL_ROWGROUP, T);
+    double best = 1e300;
+    std::pair<int, int> pick(keep_kernel, keep_T);
+    for (auto &c : cands) {
+        s->kernel = c.first;
+        s->T = c.second;
+        float ms = 0.f;
+        int rc = lg_step(s, dt, probe_steps, rebuild_every);  // warm-up (and graph capture)
+        if (rc == LG_OK) rc = snapshot_restore(s);
+        if (rc == LG_OK) rc = lg_step_timed(s, dt, probe_steps, rebuild_every, &ms);
+        int rc2 = snapshot_restore(s);
+        if (rc != LG_OK || rc2 != LG_OK) {
+            s->kernel = keep_kernel;
+            s->T = keep_T;
+            return rc != LG_OK ? rc : rc2;
+        }
+        if (ms < best) {
+            best = ms;
+            pick = c;
+        }
+    }
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    s->launches = keep_launch;
+    s->kernel = pick.first;
+    s->T = pick.second;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = pick;
+    }
+    if (kernel_out) *kernel_out = s->kernel;
+    if (T_out) *T_out = s->T;
     return LG_OK;
 }

@@ -49,6 +49,52 @@ struct lg_system {
     std::vector<cudaEvent_t> tev;  // pairs: start, stop
     size_t tev_used = 0;
 
+    // batch segmentation (n_systems == 0 for a single system)
+    int64_t n_systems = 0;
+    std::vector<int64_t> sys_off;        // host prefix offsets [n_systems + 1]
+    int64_t *d_sys_off = nullptr;        // device copy
+    int32_t *d_agg = nullptr;            // [n] system of every particle
+    lg::dbl4 *d_hoff = nullptr;          // [n_systems] hashing offsets
+    lg::dbl4 *d_orig = nullptr;          // [n_systems] FP32-copy origins (mixed precision)
+    double *d_centres = nullptr;         // [3 n_systems] scratch for per-system observables
+    double *d_sys_obs = nullptr;         // [20 n_systems]
+    std::vector<int64_t> n_bonds_initial_sys;
+
+    // CUDA graphs of whole rebuild periods, keyed by the state that determines their pointers
+    struct GraphKey {
+        double dt;
+        int64_t period;
+        int kernel, T, vcur, pcur, fcur;
+        bool operator==(const GraphKey &o) const {
+            return dt == o.dt && period == o.period && kernel == o.kernel && T == o.T && vcur == o.vcur &&
+                   pcur == o.pcur && fcur == o.fcur;
+        }
+    };
+    struct GraphEntry {
+        GraphKey key;
+        cudaGraphExec_t exec;
+        int64_t launches;
+    };
+    std::vector<GraphEntry> graphs;
+    bool use_graphs = true;
+    int64_t periods_run = 0;
+
+    // device-state snapshot (autotuner, serving): list of (live buffer, copy, bytes)
+    struct SnapBuf {
+        void *live;
+        void *copy;
+        size_t bytes;
+    };
+    std::vector<SnapBuf> snap;
+    int snap_vcur = 0, snap_pcur = 0, snap_fcur = 0;
+    int64_t snap_step = 0;
+    bool snap_built = false;
+
+    // inputs kept for cloning (autotuner)
+    std::vector<lg_facet_desc> facet_descs;
+    std::vector<double> neck_copy;
+    std::vector<int64_t> sizes_copy;
+
     int T = 1;  // lanes per row group of the force kernel
     int kernel = LG_FORCE_KERNEL_ROWGROUP;  // resolved force kernel
     int64_t step_index = 0;
@@ -58,6 +104,7 @@ struct lg_system {
     template <typename U>
     int alloc(U **p, size_t count);
     void release();
+    void drop_graphs();
 };
 
 int lg_fail(int code, const char *fmt, ...);

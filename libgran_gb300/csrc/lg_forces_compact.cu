@@ -165,10 +165,11 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
             stride = xs;
             store = PV.xi;
         }
-        d3 s[3];
+        d3 s[3] = {zero3(), zero3(), zero3()};  // springs of a slot that is not live are zero
+        if (bonded || (fl & kXiLive))
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            s[c] = mk3(store[(3 * c) * stride + base], store[(3 * c + 1) * stride + base], store[(3 * c + 2) * stride + base]);
+            for (int c = 0; c < 3; ++c)
+                s[c] = mk3(store[(3 * c) * stride + base], store[(3 * c + 1) * stride + base], store[(3 * c + 2) * stride + base]);
         const float kn = bonded ? M.b_k : M.c_k, gn = bonded ? M.b_gn : M.c_gn;
         const float rp = rr - 0.5f * overlap;
         const float v_n = -fdot(vij0, n3);
@@ -274,10 +275,11 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
         const d3 nn = nrmz(dx);
         const double overlap = 2.0 * P.contact.r_part - dot(dx, nn);
         if (!(overlap <= 0)) {
-            d3 s[3];
+            d3 s[3] = {zero3(), zero3(), zero3()};  // springs of a slot that is not live are zero
+            if (fl & kXiLive)
 #pragma unroll
-            for (int c = 0; c < 3; ++c)
-                s[c] = mk3(PV.xi[(3 * c) * xs + e], PV.xi[(3 * c + 1) * xs + e], PV.xi[(3 * c + 2) * xs + e]);
+                for (int c = 0; c < 3; ++c)
+                    s[c] = mk3(PV.xi[(3 * c) * xs + e], PV.xi[(3 * c + 1) * xs + e], PV.xi[(3 * c + 2) * xs + e]);
             const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
             contact_touching(P.contact, nn, overlap, vo, vj, wo, wj, s, pa, pal);
 #pragma unroll

@@ -106,10 +106,11 @@ __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairVi
                         touching = !(overlap <= 0);
                     }
                     if (touching) {
-                        d3 s[3];
+                        d3 s[3] = {zero3(), zero3(), zero3()};  // springs of a slot that is not live are zero
+                        if (fl & kXiLive)
 #pragma unroll
-                        for (int q = 0; q < 3; ++q)
-                            s[q] = mk3(PV.xi[(3 * q) * xs + e], PV.xi[(3 * q + 1) * xs + e], PV.xi[(3 * q + 2) * xs + e]);
+                            for (int q = 0; q < 3; ++q)
+                                s[q] = mk3(PV.xi[(3 * q) * xs + e], PV.xi[(3 * q + 1) * xs + e], PV.xi[(3 * q + 2) * xs + e]);
                         const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
                         contact_touching(P.contact, nn, overlap, vi, vj, wi, wj, s, pa, pal);
 #pragma unroll
@@ -211,11 +212,25 @@ __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairVi
 // ------------------------------------------------------------------------------------------------
 // Verlet list: bounding box, cell grid, counting sort, row build with spring carry
 // ------------------------------------------------------------------------------------------------
-__global__ void bbox_partial(int64_t n, const dbl4 *__restrict__ x, double *__restrict__ part) {
+// Position used for cell hashing: the particle's own coordinates plus, in a batch, the spatial
+// offset of its system (systems of a batch keep their own coordinates; the offsets only keep
+// their cells apart).
+__device__ __forceinline__ dbl4 hash_pos(const dbl4 *__restrict__ x, BatchView B, int64_t i) {
+    dbl4 q = x[i];
+    if (B.agg) {
+        const dbl4 o = B.hoff[B.agg[i]];
+        q.x += o.x;
+        q.y += o.y;
+        q.z += o.z;
+    }
+    return q;
+}
+
+__global__ void bbox_partial(int64_t n, const dbl4 *__restrict__ x, BatchView B, double *__restrict__ part) {
     __shared__ double s[6][256];
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        dbl4 q = x[i];
+        dbl4 q = hash_pos(x, B, i);
         lo[0] = fmin(lo[0], q.x); lo[1] = fmin(lo[1], q.y); lo[2] = fmin(lo[2], q.z);
         hi[0] = fmax(hi[0], q.x); hi[1] = fmax(hi[1], q.y); hi[2] = fmax(hi[2], q.z);
     }
@@ -303,11 +318,11 @@ __device__ __forceinline__ int64_t cell_coord(double q, double lo, double edge, 
     return k < 0 ? 0 : (k >= dim ? dim - 1 : k);
 }
 
-__global__ void cell_count(int64_t n, const dbl4 *__restrict__ x, const GridDev *__restrict__ g,
+__global__ void cell_count(int64_t n, const dbl4 *__restrict__ x, BatchView B, const GridDev *__restrict__ g,
                            int32_t *__restrict__ cell_of, int32_t *__restrict__ count, float4 *__restrict__ x32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    dbl4 q = x[i];
+    dbl4 q = hash_pos(x, B, i);
     int64_t cx = cell_coord(q.x, g->lo[0], g->edge, g->dim[0]);
     int64_t cy = cell_coord(q.y, g->lo[1], g->edge, g->dim[1]);
     int64_t cz = cell_coord(q.z, g->lo[2], g->edge, g->dim[2]);
@@ -357,11 +372,12 @@ constexpr int kBuildThreads = 64;
 // filter accepts or rejects the clear cases), ascending j, carrying the springs (and live flag) of
 // pairs that were already listed, and marking intact bonds. Candidates are gathered and sorted in
 // shared memory (slot k of thread t at k * blockDim + t, conflict-free).
-__global__ void __launch_bounds__(kBuildThreads) build_rows(int64_t n, const dbl4 *__restrict__ x, const float4 *__restrict__ x32,
+__global__ void __launch_bounds__(kBuildThreads) build_rows(int64_t n, const dbl4 *__restrict__ x, BatchView B,
+                                                            const float4 *__restrict__ x32,
                                                             const GridDev *__restrict__ g, const int32_t *__restrict__ cstart,
                                                             const int32_t *__restrict__ ccount, const int32_t *__restrict__ sorted,
                                                             double rv2, PairView oldv, PairView newv, BondView BV,
-                                                            int32_t *err) {
+                                                            int32_t *err, int32_t *max_row) {
     extern __shared__ int32_t js[];
     const int tid = threadIdx.x;
     int64_t i = blockIdx.x * (int64_t)blockDim.x + tid;
@@ -371,9 +387,11 @@ __global__ void __launch_bounds__(kBuildThreads) build_rows(int64_t n, const dbl
     const float rlo = g->rv2_lo, rhi = g->rv2_hi;
     const dbl4 xd = x[i];
     const d3 xi_ = mk3(xd.x, xd.y, xd.z);
-    int64_t cx = cell_coord(xi_.x, g->lo[0], g->edge, g->dim[0]);
-    int64_t cy = cell_coord(xi_.y, g->lo[1], g->edge, g->dim[1]);
-    int64_t cz = cell_coord(xi_.z, g->lo[2], g->edge, g->dim[2]);
+    const dbl4 hp = hash_pos(x, B, i);
+    const int32_t ai = B.agg ? B.agg[i] : 0;
+    int64_t cx = cell_coord(hp.x, g->lo[0], g->edge, g->dim[0]);
+    int64_t cy = cell_coord(hp.y, g->lo[1], g->edge, g->dim[1]);
+    int64_t cz = cell_coord(hp.z, g->lo[2], g->edge, g->dim[2]);
     int32_t cnt = 0;
     bool overflow = false;
     for (int64_t z = cz - 1; z <= cz + 1; ++z) {
@@ -387,6 +405,7 @@ __global__ void __launch_bounds__(kBuildThreads) build_rows(int64_t n, const dbl
                 for (int32_t q = 0; q < m; ++q) {
                     int32_t j = sorted[b + q];
                     if (j == (int32_t)i) continue;
+                    if (B.agg && B.agg[j] != ai) continue;  // pairs never cross systems of a batch
                     const float4 fj = x32[j];
                     const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
                     const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
@@ -408,6 +427,7 @@ __global__ void __launch_bounds__(kBuildThreads) build_rows(int64_t n, const dbl
             }
         }
     }
+    atomicMax(max_row, cnt);
     if (overflow) {
         set_error(err, LG_DEVERR_LIST_OVERFLOW);
         cnt = (int32_t)cap;
@@ -500,16 +520,16 @@ void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, cons
     kick_drift_fp64<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt);
 }
 
-void launch_list_build(int64_t n, const dbl4 *x, double rv, int64_t max_cells, ListScratch &ls, PairView oldv,
+void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, int64_t max_cells, ListScratch &ls, PairView oldv,
                        PairView newv, BondView BV, int32_t *err, cudaStream_t st) {
     const int nparts = ls.nparts;
-    bbox_partial<<<nparts, 256, 0, st>>>(n, x, ls.part);
+    bbox_partial<<<nparts, 256, 0, st>>>(n, x, B, ls.part);
     grid_setup<<<1, 256, 0, st>>>(nparts, ls.part, rv, max_cells, ls.grid);
     cudaMemsetAsync(ls.count, 0, sizeof(int32_t) * (size_t)max_cells, st);
     cudaMemsetAsync(ls.fill, 0, sizeof(int32_t) * (size_t)max_cells, st);
     const int threads = 256;
     unsigned blocks = (unsigned)((n + threads - 1) / threads);
-    cell_count<<<blocks, threads, 0, st>>>(n, x, ls.grid, ls.cell_of, ls.count, ls.x32);
+    cell_count<<<blocks, threads, 0, st>>>(n, x, B, ls.grid, ls.cell_of, ls.count, ls.x32);
     scan_cells<<<1, 1024, 0, st>>>(ls.grid, ls.count, ls.start);
     cell_scatter<<<blocks, threads, 0, st>>>(n, ls.cell_of, ls.start, ls.fill, ls.sorted);
     unsigned b2 = (unsigned)((n + kBuildThreads - 1) / kBuildThreads);
@@ -521,7 +541,7 @@ void launch_list_build(int64_t n, const dbl4 *x, double rv, int64_t max_cells, L
         cudaFuncSetAttribute(build_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(int32_t) * 255 * kBuildThreads));
         attr_device = dev;
     }
-    build_rows<<<b2, kBuildThreads, smem, st>>>(n, x, ls.x32, ls.grid, ls.start, ls.count, ls.sorted, rv * rv, oldv, newv, BV, err);
+    build_rows<<<b2, kBuildThreads, smem, st>>>(n, x, B, ls.x32, ls.grid, ls.start, ls.count, ls.sorted, rv * rv, oldv, newv, BV, err, ls.max_row);
 }
 
 }  // namespace lg

@@ -218,10 +218,14 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
                         stride = xs;
                         store = PV.xi;
                     }
+                    if (bonded || (fl & kXiLive)) {  // springs of a slot that is not live are zero
 #pragma unroll
-                    for (int q3 = 0; q3 < 3; ++q3)
-                        s[q3] = mk3(store[(3 * q3) * stride + base], store[(3 * q3 + 1) * stride + base],
-                                    store[(3 * q3 + 2) * stride + base]);
+                        for (int q3 = 0; q3 < 3; ++q3)
+                            s[q3] = mk3(store[(3 * q3) * stride + base], store[(3 * q3 + 1) * stride + base],
+                                        store[(3 * q3 + 2) * stride + base]);
+                    } else {
+                        s[0] = s[1] = s[2] = zero3();
+                    }
                     f3 force, torque;
                     if (bonded)
                         contact_mixed((float)B.k, (float)B.gamma_n, (float)B.k_t, (float)B.gamma_t, 0.f, 0.f,
@@ -323,19 +327,32 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
         set_error(S.err, LG_DEVERR_NONFINITE);
 }
 
-// FP32 copy of the positions relative to the system origin (for culling).
+__device__ __forceinline__ float4 rel_f32(d3 q, double ox, double oy, double oz, const int32_t *agg,
+                                          const dbl4 *orig, int64_t i) {
+    if (agg) {
+        const dbl4 o = orig[agg[i]];
+        ox = o.x;
+        oy = o.y;
+        oz = o.z;
+    }
+    return make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), 0.0f);
+}
+
+// FP32 copy of the positions relative to the system origin (for culling); in a batch every system
+// has its own origin.
 __global__ void positions_to_f32(int64_t n, const dbl4 *__restrict__ x, double ox, double oy, double oz,
+                                 const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig,
                                  float4 *__restrict__ x32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    dbl4 q = x[i];
-    x32[i] = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), 0.0f);
+    x32[i] = rel_f32(ld4(x, i), ox, oy, oz, agg, orig, i);
 }
 
 // Kick + drift of the mixed path: FP64 integration, then the FP32 position copy.
 __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restrict__ v, dbl4 *__restrict__ th,
                                  dbl4 *__restrict__ w, const dbl4 *__restrict__ a, const dbl4 *__restrict__ al,
-                                 double dt, double hdt, double ox, double oy, double oz, float4 *__restrict__ x32) {
+                                 double dt, double hdt, double ox, double oy, double oz, const int32_t *__restrict__ agg,
+                                 const dbl4 *__restrict__ orig, float4 *__restrict__ x32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));
@@ -345,7 +362,7 @@ __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restri
     d3 xn = add(ld4(x, i), scl(dt, vi));
     st4(x, i, xn);
     st4(th, i, add(ld4(th, i), scl(dt, wi)));
-    x32[i] = make_float4((float)(xn.x - ox), (float)(xn.y - oy), (float)(xn.z - oz), 0.0f);
+    x32[i] = rel_f32(xn, ox, oy, oz, agg, orig, i);
 }
 
 template <int T, bool VERLET>
@@ -381,20 +398,22 @@ void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairV
 #undef LG_CASE
 }
 
-void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, float4 *x32, cudaStream_t st) {
+void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, const int32_t *agg, const dbl4 *orig,
+                             float4 *x32, cudaStream_t st) {
     const int threads = 256;
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
-    positions_to_f32<<<(unsigned)blocks, threads, 0, st>>>(n, x, origin[0], origin[1], origin[2], x32);
+    positions_to_f32<<<(unsigned)blocks, threads, 0, st>>>(n, x, origin[0], origin[1], origin[2], agg, orig, x32);
 }
 
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
-                             double hdt, const double *origin, float4 *x32, cudaStream_t st) {
+                             double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
+                             cudaStream_t st) {
     const int threads = 256;
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
     kick_drift_mixed<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt, origin[0], origin[1],
-                                                           origin[2], x32);
+                                                           origin[2], agg, orig, x32);
 }
 
 }  // namespace lg

@@ -15,6 +15,13 @@ struct GridDev {
     float rv2_lo, rv2_hi;  // FP32 accept / reject bounds of the squared list radius
 };
 
+// Batch segmentation (null pointers for a single system): system index of every particle and the
+// spatial offset of every system used only for cell hashing.
+struct BatchView {
+    const int32_t *agg;  // [n]
+    const dbl4 *hoff;    // [n_systems]
+};
+
 struct ListScratch {
     int nparts;        // blocks of the bounding-box pass
     double *part;      // [nparts * 6]
@@ -25,6 +32,7 @@ struct ListScratch {
     int32_t *fill;     // [max_cells]
     int32_t *sorted;   // [n]
     float4 *x32;       // [n] positions relative to the grid origin, FP32 (candidate filter)
+    int32_t *max_row;  // [1] longest row found by the last build (before truncation)
 };
 
 // FP64 path (lg_forces_fp64.cu, compiled with --fmad=false)
@@ -32,7 +40,7 @@ void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairVi
                         double dt, int move_facets, cudaStream_t st);
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
                             const dbl4 *al, double dt, double hdt, cudaStream_t st);
-void launch_list_build(int64_t n, const dbl4 *x, double rv, int64_t max_cells, ListScratch &ls, PairView oldv,
+void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, int64_t max_cells, ListScratch &ls, PairView oldv,
                        PairView newv, BondView BV, int32_t *err, cudaStream_t st);
 
 // Mixed-precision path (lg_forces_mixed.cu)
@@ -54,9 +62,11 @@ struct MixedExtra {
 bool mixed_available();
 void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
                          double hdt, double dt, int move_facets, const MixedExtra &MX, cudaStream_t st);
-void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, float4 *x32, cudaStream_t st);
+void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, const int32_t *agg, const dbl4 *orig,
+                             float4 *x32, cudaStream_t st);
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
-                             double hdt, const double *origin, float4 *x32, cudaStream_t st);
+                             double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
+                             cudaStream_t st);
 
 // Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
@@ -70,5 +80,12 @@ int64_t obs_scratch_doubles(int64_t n);
 void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
                         double inertia, double *scratch, double *out, cudaStream_t st);
 void launch_observables_rg(int64_t n, const dbl4 *x, const double *c, double *scratch, double *out, cudaStream_t st);
+// Per-system observables of a batch: out[s * 20 + c] = column sums over system s's particles
+// (rows from launch_observables' scratch), then column 18 = sum |x - c_s|^2 with centres from
+// centres[3 s ..].
+void launch_segmented_sums(int64_t n_systems, const int64_t *offsets, const double *scratch, double *out,
+                           cudaStream_t st);
+void launch_segmented_rg(int64_t n, int64_t n_systems, const int64_t *offsets, const dbl4 *x, const double *centres,
+                         double *scratch, double *out, cudaStream_t st);
 
 }  // namespace lg

@@ -125,4 +125,56 @@ void launch_observables_rg(int64_t n, const dbl4 *x, const double *c, double *sc
     obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 18, 19, out);
 }
 
+// One block per system: fixed-order sums of the system's scratch rows (columns 0..17).
+__global__ void __launch_bounds__(256) seg_sums(const int64_t *__restrict__ off, const double *__restrict__ rows,
+                                                double *__restrict__ out) {
+    __shared__ double s[256];
+    const int64_t sys = blockIdx.x;
+    const int64_t b = off[sys], e = off[sys + 1];
+    for (int c = 0; c < 18; ++c) {
+        double acc = 0.0;
+        for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) acc += rows[i * kObs + c];
+        s[threadIdx.x] = acc;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[sys * kObs + c] = s[0];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) seg_rg(const int64_t *__restrict__ off, const dbl4 *__restrict__ x,
+                                              const double *__restrict__ centres, double *__restrict__ out) {
+    __shared__ double s[256];
+    const int64_t sys = blockIdx.x;
+    const int64_t b = off[sys], e = off[sys + 1];
+    const d3 c = mk3(centres[3 * sys], centres[3 * sys + 1], centres[3 * sys + 2]);
+    double acc = 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        d3 q = sub(ld4(x, i), c);
+        acc += dot(q, q);
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[sys * kObs + 18] = s[0];
+}
+
+void launch_segmented_sums(int64_t n_systems, const int64_t *offsets, const double *scratch, double *out,
+                           cudaStream_t st) {
+    if (n_systems > 0) seg_sums<<<(unsigned)n_systems, 256, 0, st>>>(offsets, scratch, out);
+}
+
+void launch_segmented_rg(int64_t n, int64_t n_systems, const int64_t *offsets, const dbl4 *x, const double *centres,
+                         double *scratch, double *out, cudaStream_t st) {
+    (void)n;
+    (void)scratch;
+    if (n_systems > 0) seg_rg<<<(unsigned)n_systems, 256, 0, st>>>(offsets, x, centres, out);
+}
+
 }  // namespace lg

@@ -21,9 +21,9 @@ def _vec(a, n):
 
 
 class System:
-    """One simulated system resident on a GPU."""
+    """One simulated system (or, with ``sizes``, a batch of independent systems) resident on a GPU."""
 
-    def __init__(self, desc, x0, v0=None, th0=None, om0=None, facets=None, neck=None, device=0):
+    def __init__(self, desc, x0, v0=None, th0=None, om0=None, facets=None, neck=None, device=0, sizes=None):
         L = A.lib()
         self.n = int(desc.n_part)
         self.desc = desc
@@ -35,9 +35,18 @@ class System:
             fp = C.cast(self._facets, C.POINTER(A.lg_facet_desc))
         neck_a = None if neck is None else np.ascontiguousarray(neck, dtype=np.float64)
         h = C.c_void_p()
-        A.check(L.lg_create(C.byref(desc), _dp(self._x0), _dp(v0), _dp(th0), _dp(om0), fp,
-                            None if neck_a is None else _dp(neck_a), 0 if neck_a is None else len(neck_a),
-                            int(device), C.byref(h)), "lg_create")
+        if sizes is None:
+            A.check(L.lg_create(C.byref(desc), _dp(self._x0), _dp(v0), _dp(th0), _dp(om0), fp,
+                                None if neck_a is None else _dp(neck_a), 0 if neck_a is None else len(neck_a),
+                                int(device), C.byref(h)), "lg_create")
+            self.sizes = None
+        else:
+            sz = np.ascontiguousarray(sizes, dtype=np.int64)
+            A.check(L.lg_batch_create(C.byref(desc), len(sz), sz.ctypes.data_as(C.POINTER(C.c_int64)), _dp(self._x0),
+                                      _dp(v0), _dp(th0), _dp(om0), fp, None if neck_a is None else _dp(neck_a),
+                                      0 if neck_a is None else len(neck_a), int(device), C.byref(h)),
+                    "lg_batch_create")
+            self.sizes = sz
         self.h = h
 
     def close(self):
@@ -85,6 +94,29 @@ class System:
         o = A.lg_observables()
         A.check(A.lib().lg_get_observables(self.h, C.byref(o)), "lg_get_observables")
         return o.as_dict()
+
+    def batch_observables(self):
+        """Per-system observables of a batch (list of dicts)."""
+        ns = len(self.sizes)
+        arr = (A.lg_observables * ns)()
+        A.check(A.lib().lg_batch_get_observables(self.h, C.cast(arr, C.POINTER(A.lg_observables))),
+                "lg_batch_get_observables")
+        return [arr[q].as_dict() for q in range(ns)]
+
+    def snapshot(self):
+        A.check(A.lib().lg_snapshot(self.h), "lg_snapshot")
+
+    def restore(self):
+        A.check(A.lib().lg_restore(self.h), "lg_restore")
+
+    def set_graphs(self, on):
+        A.check(A.lib().lg_set_graphs(self.h, 1 if on else 0), "lg_set_graphs")
+
+    def autotune(self, dt, probe_steps=20, rebuild_every=20, use_cache=True):
+        k, t = C.c_int32(), C.c_int32()
+        A.check(A.lib().lg_autotune(self.h, float(dt), int(probe_steps), int(rebuild_every), C.byref(k), C.byref(t),
+                                    1 if use_cache else 0), "lg_autotune")
+        return k.value, t.value
 
     def device_errors(self):
         e = C.c_int32()

@@ -1,0 +1,118 @@
+"""Batches of independent aggregates in one handle, CUDA-graph replay and the autotuner.
+
+A system inside a batch must give the same result as the same system alone (its rows, springs and
+bonds never involve other systems): for the compacted kernels this holds bit for bit."""
+import numpy as np
+import pytest
+
+from libgran_gb300 import _abi as A
+from libgran_gb300 import configs as K
+from libgran_gb300.system import System, generate_aggregate, generate_velocities
+from oracle import oracle as O
+
+import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = (A.LG_FIELD_X, A.LG_FIELD_V, A.LG_FIELD_OMEGA, A.LG_FIELD_A, A.LG_FIELD_ALPHA)
+
+
+def _systems(sizes, seed0=1000, squeeze=2e7):
+    mat = K.Material()
+    xs, vs = [], []
+    for q, n in enumerate(sizes):
+        x = generate_aggregate(seed0 + q, n, mat.r)
+        v = generate_velocities(seed0 + q, n, 0.1) - squeeze * (x - x.mean(0))
+        xs.append(x)
+        vs.append(v)
+    return mat, xs, vs
+
+
+def _desc(mat, n, bm, precision, kernel=A.LG_FORCE_KERNEL_COMPACT):
+    return K.make_desc(n, bm, A.LG_HAMAKER_LIMITED, contact=mat.contact(), sinter=mat.sinter(), hamaker=mat.hamaker(),
+                       pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r, precision=precision, force_kernel=kernel,
+                       max_neighbors=160)
+
+
+@pytest.mark.parametrize("precision", [A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("bm", [A.LG_BINARY_SINTER, A.LG_BINARY_CONTACT], ids=["sinter", "contact"])
+def test_batch_matches_systems_alone_bit_for_bit(precision, bm):
+    sizes = [37, 256, 90, 600, 33]
+    mat, xs, vs = _systems(sizes)
+    batch = System(_desc(mat, sum(sizes), bm, precision), np.concatenate(xs), np.concatenate(vs), sizes=sizes)
+    batch.step(mat.dt, 100, 20)
+    bx = batch.get(A.LG_FIELD_X)
+    bobs = batch.batch_observables()
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for q, n in enumerate(sizes):
+        alone = System(_desc(mat, n, bm, precision), xs[q], vs[q])
+        alone.step(mat.dt, 100, 20)
+        for f in FIELDS:
+            assert np.array_equal(alone.get(f), batch.get(f)[off[q]:off[q + 1]]), (q, H.FIELD_NAMES[f])
+        ao = alone.observables()
+        for k in ("ke_total", "radius_of_gyration", "potential_energy", "linear_momentum"):
+            assert abs(ao[k] - bobs[q][k]) <= 1e-12 * max(abs(ao[k]), 1e-300), (q, k)
+        assert ao["n_bonds"] == bobs[q]["n_bonds"]
+    assert batch.device_errors() == 0
+
+
+def test_batch_fp64_matches_oracle():
+    sizes = [64, 200, 48]
+    mat, xs, vs = _systems(sizes, seed0=55)
+    batch = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, A.LG_PRECISION_FP64), np.concatenate(xs),
+                   np.concatenate(vs), sizes=sizes)
+    batch.step(mat.dt, 60, 20)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for q, n in enumerate(sizes):
+        o = O.OracleSystem(_desc(mat, n, A.LG_BINARY_SINTER, A.LG_PRECISION_FP64), xs[q], vs[q])
+        o.step(mat.dt, 60, 20)
+        for f in FIELDS:
+            assert np.array_equal(o.get(f), batch.get(f)[off[q]:off[q + 1]]), (q, H.FIELD_NAMES[f])
+    assert batch.device_errors() == 0
+
+
+@pytest.mark.parametrize("precision", [A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_graph_replay_equals_eager_launches(precision):
+    sizes = [300, 500, 120]
+    mat, xs, vs = _systems(sizes, seed0=7)
+    outs = []
+    for graphs in (False, True):
+        s = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, precision), np.concatenate(xs), np.concatenate(vs),
+                   sizes=sizes)
+        s.set_graphs(graphs)
+        s.step(mat.dt, 100, 20)
+        s.step(mat.dt, 7, 20)   # unaligned tail
+        s.step(mat.dt, 53, 20)  # realigns and replays again
+        outs.append([s.get(f) for f in FIELDS])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+def test_autotuner_picks_a_valid_variant():
+    sizes = [256] * 64
+    mat, xs, vs = _systems(sizes, seed0=99)
+    s = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, A.LG_PRECISION_MIXED, kernel=A.LG_FORCE_KERNEL_AUTO),
+               np.concatenate(xs), np.concatenate(vs), sizes=sizes)
+    before = [s.get(f) for f in FIELDS]
+    k, T = s.autotune(mat.dt, probe_steps=20, rebuild_every=20, use_cache=False)
+    assert k in (A.LG_FORCE_KERNEL_COMPACT, A.LG_FORCE_KERNEL_ROWGROUP)
+    assert T in (1, 2, 4, 8, 16, 32)
+    for f, b in zip(FIELDS, before):  # tuning leaves the state as it was
+        assert np.array_equal(s.get(f), b)
+    s.step(mat.dt, 40, 20)
+    assert s.device_errors() == 0
+
+
+def test_snapshot_restore_replays_identically():
+    sizes = [200, 300]
+    mat, xs, vs = _systems(sizes, seed0=3)
+    s = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, A.LG_PRECISION_FP64), np.concatenate(xs), np.concatenate(vs),
+               sizes=sizes)
+    s.step(mat.dt, 20, 20)
+    s.snapshot()
+    s.step(mat.dt, 60, 20)
+    first = [s.get(f) for f in FIELDS]
+    s.restore()
+    s.step(mat.dt, 60, 20)
+    for a, f in zip(first, FIELDS):
+        assert np.array_equal(a, s.get(f))
