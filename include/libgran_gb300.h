@@ -297,6 +297,26 @@ int lg_restore(lg_system *sys);
 int lg_autotune(lg_system *sys, double dt, int64_t probe_steps, int64_t rebuild_every, int32_t *force_kernel,
                 int32_t *threads_per_row, int32_t use_cache);
 
+/* Observables of a particle state held in device memory that the caller owns, computed without
+ * allocating any device memory. No counterpart in the reference: it serves callers that cannot
+ * allocate when they need these numbers -- a serving loop that admits work against a fixed device
+ * memory budget, a host framework whose own caching allocator holds the device memory, code that
+ * must not stall other streams (cudaMalloc and cudaFree can synchronise the device).
+ *   x, v, omega: device arrays double[3n] (AoS); out: device array of LG_NOALLOC_OBS doubles:
+ *   0 translational KE, 1 rotational KE, 2 total KE, 3 |linear momentum|, 4 |angular momentum|,
+ *   5..7 centre of mass, 8 radius of gyration (test/compute_energy.cpp, test/mass_distribution.cpp
+ *   quantities). stream: a cudaStream_t (NULL = default stream); the call is asynchronous.
+ * Limit: 1 <= n <= LG_NOALLOC_MAX_PARTICLES, else LG_E_INVALID with a message. Partial sums live in
+ * one fixed 512 KiB array in device memory that every GPU loading this library holds until the
+ * process exits; all calls share it, so calls that overlap on the GPU (e.g. on two streams at once)
+ * race and must be serialised by the caller. The first call on each device looks up the array's
+ * device address (set-up, with that device current); make that first call before any stream
+ * capture. Calls no cudaMalloc, cudaFree or allocating library routine. */
+#define LG_NOALLOC_OBS 9
+#define LG_NOALLOC_MAX_PARTICLES 1048320
+int lg_observables_noalloc(const double *x, const double *v, const double *omega, int64_t n, double mass,
+                           double inertia, double *out, void *stream);
+
 /* Time `nsteps` steps with CUDA events on the handle's stream (no host copies inside); ms_out
  * receives the elapsed device time. Same semantics as lg_step. */
 int lg_step_timed(lg_system *sys, double dt, int64_t nsteps, int64_t rebuild_every, float *ms_out);

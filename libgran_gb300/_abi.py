@@ -18,6 +18,7 @@ LG_PAIRS_ALL, LG_PAIRS_VERLET = 0, 1
 LG_FORCE_KERNEL_AUTO, LG_FORCE_KERNEL_ROWGROUP, LG_FORCE_KERNEL_COMPACT = 0, 1, 2
 LG_FIELD_X, LG_FIELD_V, LG_FIELD_THETA, LG_FIELD_OMEGA, LG_FIELD_A, LG_FIELD_ALPHA = range(6)
 LG_DEVERR_LIST_OVERFLOW, LG_DEVERR_NONFINITE, LG_DEVERR_BOND_LOST = 1, 2, 4
+LG_NOALLOC_OBS, LG_NOALLOC_MAX_PARTICLES = 9, 1048320
 
 
 class lg_contact_params(C.Structure):
@@ -125,6 +126,7 @@ def _declare(L):
         "lg_batch_get_observables": (C.c_int, [vp, P(lg_observables)]),
         "lg_autotune": (C.c_int, [vp, d, i64, i64, P(i32), P(i32), i32]),
         "lg_snapshot": (C.c_int, [vp]),
+        "lg_observables_noalloc": (C.c_int, [vp, vp, vp, i64, d, d, vp, vp]),
         "lg_restore": (C.c_int, [vp]),
         "lg_get_pair_stats": (C.c_int, [vp, P(lg_pair_stats)]),
         "lg_enable_kernel_timing": (C.c_int, [vp, i32]),
