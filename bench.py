@@ -355,14 +355,15 @@ def run_gb300(args, rank, world):
     sm, mat, tm = time_path(A.LG_PRECISION_MIXED, x0, v0, args, l2_flush)
     clk = clocks.stop()
     torch.cuda.synchronize()
+    def amax(v):
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t[0])
     if dist:
         dist.barrier()
-        t = torch.tensor([tm["ms"], t64["ms"]], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tm["ms"], t64["ms"] = float(t[0]), float(t[1])
     units = N_PART * VV_PER_STEP * args.steps
-    value = world * units / (tm["ms"] / 1e3)
-    value64 = world * units / (t64["ms"] / 1e3)
+    value, tm["ms"] = combine_ranks(tm["ms"], units, world, amax if dist else None)
+    value64, t64["ms"] = combine_ranks(t64["ms"], units, world, amax if dist else None)
     e2e, obs = e2e_path(sm, mat, args, x0, v0)
     e2e["value"] *= world
     sm.close()
@@ -383,6 +384,11 @@ def run_gb300(args, rank, world):
     batched = None
     if os.environ.get("LG_BENCH_BATCHED", "1") != "0":
         batched = batched_section(args, l2_flush)
+    serving = None
+    if os.environ.get("LG_BENCH_SERVING", "1") != "0":
+        lams = [float(v) for v in os.environ.get("LG_SERVE_LAMBDAS", "4").split(",")]
+        dur = float(os.environ.get("LG_SERVE_SECONDS", "15"))
+        serving = [serving_section(lam, dur) for lam in lams]
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tm["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -405,8 +411,66 @@ def run_gb300(args, rank, world):
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
         "device_errors": tm["device_errors"],
         "batched": batched,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
+
+
+def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):
+    """Serving workload: Poisson arrivals at rate lam (requests/s) for duration_s seconds; each
+    request an aggregate of log-uniform 64..8192 monomers with its own seed and a step budget drawn
+    uniformly from 2e3..2e4 (multiples of 20), mixed precision, sintered bonds + contact + limited
+    Hamaker; a 150 GB device-memory budget. Reports request latency percentiles and the sustained
+    particle-steps/s of the whole run (submission of the first request to retirement of the last)."""
+    from libgran_gb300 import _abi as A
+    from libgran_gb300 import configs as K
+    from libgran_gb300.serving import Server
+    from libgran_gb300.system import generate_aggregate, generate_velocities
+    mat = K.Material()
+    d = K.make_desc(1, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(), sinter=mat.sinter(),
+                    hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r,
+                    precision=A.LG_PRECISION_MIXED, max_neighbors=96)
+    rng = np.random.default_rng(seed)
+    t, arrivals = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / lam)
+        if t > duration_s:
+            break
+        n = int(K.loguniform_sizes(1, 64, 8192, seed=int(rng.integers(1 << 31)))[0])
+        steps = int(rng.integers(100, 1001)) * 20
+        arrivals.append((t, n, steps, len(arrivals)))
+    # inputs are generated before the clock starts (a client would send them)
+    inputs = [(generate_aggregate((4 << 32) + k, n, mat.r), generate_velocities((4 << 32) + k, n, 0.1))
+              for (_, n, _, k) in arrivals]
+    srv = Server(d, budget_bytes=budget_bytes, dt=mat.dt)
+    t0 = time.perf_counter()
+    nxt = 0
+    while True:
+        now = time.perf_counter() - t0
+        while nxt < len(arrivals) and arrivals[nxt][0] <= now:
+            _, n, steps, k = arrivals[nxt]
+            srv.submit(inputs[k][0], inputs[k][1], steps)
+            nxt += 1
+        a, q, _ = srv.tick()
+        if nxt >= len(arrivals) and a == 0 and q == 0:
+            break
+        if a == 0 and q == 0 and nxt < len(arrivals):
+            time.sleep(max(0.0, min(0.01, arrivals[nxt][0] - (time.perf_counter() - t0))))
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    return {"lambda_per_s": lam, "requests": len(arrivals), "completed": st["completed"], "failed": st["failed"],
+            "p50_latency_ms": st["p50_latency_ms"], "p99_latency_ms": st["p99_latency_ms"],
+            "max_latency_ms": st["max_latency_ms"], "particle_steps_per_s": st["particle_steps"] / wall,
+            "wall_s": wall, "peak_bytes": st["peak_bytes"], "budget_bytes": budget_bytes}
+
+
+def combine_ranks(ms, units_per_rank, world, all_reduce_max=None):
+    """Whole-job throughput of `world` replicas: every rank processed units_per_rank units; the job
+    time is the slowest rank's (max over ranks)."""
+    if world > 1 and all_reduce_max is not None:
+        ms = all_reduce_max(ms)
+    return world * units_per_rank / (ms / 1e3), ms
 
 
 def run_profile(args):

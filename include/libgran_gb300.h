@@ -321,6 +321,49 @@ int lg_observables_noalloc(const double *x, const double *v, const double *omega
  * receives the elapsed device time. Same semantics as lg_step. */
 int lg_step_timed(lg_system *sys, double dt, int64_t nsteps, int64_t rebuild_every, float *ms_out);
 
+/* ---- serving: continuous batching of aggregate-mechanics requests ---------------------------
+ * No counterpart in libgran (its drivers run one system per process). A server holds a system
+ * template (functors, pair mode, precision), a device-memory budget and a step size. Requests (an
+ * aggregate state and a step budget) may be submitted at any time; each lg_server_tick admits queued
+ * requests that fit the budget (first come first served, with backfill), advances every resident
+ * request by one rebuild period -- the requests' kernels are enqueued on their own streams before
+ * any wait, so they overlap on the device -- and retires finished requests (observables and
+ * positions copied back, memory returned to the budget). Each request is simulated exactly as it
+ * would be alone. Latency = host time from submission to retirement. */
+#define LG_REQ_QUEUED 0
+#define LG_REQ_RUNNING 1
+#define LG_REQ_DONE 2
+#define LG_REQ_FAILED 3
+#define LG_REQ_CANCELLED 4
+
+typedef struct lg_server lg_server;
+typedef struct lg_server_stats {
+    int64_t budget_bytes, used_bytes, peak_bytes;
+    int64_t active, queued, completed, rejected, failed, cancelled;
+    int64_t particle_steps;
+    double p50_latency_ms, p99_latency_ms, max_latency_ms;
+} lg_server_stats;
+
+/* Device bytes a request of n particles is charged against the budget. */
+int64_t lg_estimate_device_bytes(const lg_system_desc *tmpl, int64_t n);
+int lg_server_create(const lg_system_desc *tmpl, int64_t budget_bytes, int64_t rebuild_every, double dt, int device,
+                     lg_server **out);
+int lg_server_destroy(lg_server *srv);
+/* Queue a request (x0, v0: double[3n]; v0 may be NULL). Malformed requests (n < 1, nsteps < 1,
+ * non-finite state) fail with LG_E_INVALID; a request larger than the whole budget with LG_E_NOMEM. */
+int lg_server_submit(lg_server *srv, int64_t n, const double *x0, const double *v0, int64_t nsteps,
+                     int64_t *request_id);
+int lg_server_cancel(lg_server *srv, int64_t request_id);
+int lg_server_tick(lg_server *srv, int32_t *n_active, int32_t *n_queued, int32_t *n_retired);
+/* State (LG_REQ_*) of a request; when done, its observables and final positions (double[3n], may be
+ * NULL) and its latency. A failed request's reason is in lg_last_error(). */
+int lg_server_poll(lg_server *srv, int64_t request_id, int32_t *state, lg_observables *obs, double *x_out,
+                   double *latency_ms);
+int lg_server_release(lg_server *srv, int64_t request_id);
+int lg_server_get_stats(lg_server *srv, lg_server_stats *out);
+/* Test hook: the next `count` admissions fail as a device allocation failure would (host side). */
+int lg_server_inject_alloc_failures(lg_server *srv, int32_t count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,7 @@ LG_FORCE_KERNEL_AUTO, LG_FORCE_KERNEL_ROWGROUP, LG_FORCE_KERNEL_COMPACT = 0, 1, 
 LG_FIELD_X, LG_FIELD_V, LG_FIELD_THETA, LG_FIELD_OMEGA, LG_FIELD_A, LG_FIELD_ALPHA = range(6)
 LG_DEVERR_LIST_OVERFLOW, LG_DEVERR_NONFINITE, LG_DEVERR_BOND_LOST = 1, 2, 4
 LG_NOALLOC_OBS, LG_NOALLOC_MAX_PARTICLES = 9, 1048320
+LG_REQ_QUEUED, LG_REQ_RUNNING, LG_REQ_DONE, LG_REQ_FAILED, LG_REQ_CANCELLED = 0, 1, 2, 3, 4
 
 
 class lg_contact_params(C.Structure):
@@ -46,6 +47,12 @@ class lg_facet_desc(C.Structure):
 class lg_pair_stats(C.Structure):
     _fields_ = [("mean_row_length", C.c_double), ("max_row_length", C.c_int64),
                 ("live_contact_slots", C.c_int64), ("bonded_slots", C.c_int64)]
+
+
+class lg_server_stats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("budget_bytes", "used_bytes", "peak_bytes", "active", "queued", "completed",
+                                         "rejected", "failed", "cancelled", "particle_steps")] + \
+               [(n, C.c_double) for n in ("p50_latency_ms", "p99_latency_ms", "max_latency_ms")]
 
 
 class lg_system_desc(C.Structure):
@@ -126,6 +133,16 @@ def _declare(L):
         "lg_batch_get_observables": (C.c_int, [vp, P(lg_observables)]),
         "lg_autotune": (C.c_int, [vp, d, i64, i64, P(i32), P(i32), i32]),
         "lg_snapshot": (C.c_int, [vp]),
+        "lg_estimate_device_bytes": (i64, [P(lg_system_desc), i64]),
+        "lg_server_create": (C.c_int, [P(lg_system_desc), i64, i64, d, C.c_int, P(vp)]),
+        "lg_server_destroy": (C.c_int, [vp]),
+        "lg_server_submit": (C.c_int, [vp, i64, P(d), P(d), i64, P(i64)]),
+        "lg_server_cancel": (C.c_int, [vp, i64]),
+        "lg_server_tick": (C.c_int, [vp, P(i32), P(i32), P(i32)]),
+        "lg_server_poll": (C.c_int, [vp, i64, P(i32), P(lg_observables), P(d), P(d)]),
+        "lg_server_release": (C.c_int, [vp, i64]),
+        "lg_server_get_stats": (C.c_int, [vp, P(lg_server_stats)]),
+        "lg_server_inject_alloc_failures": (C.c_int, [vp, i32]),
         "lg_observables_noalloc": (C.c_int, [vp, vp, vp, i64, d, d, vp, vp]),
         "lg_restore": (C.c_int, [vp]),
         "lg_get_pair_stats": (C.c_int, [vp, P(lg_pair_stats)]),
