@@ -384,9 +384,12 @@ def run_gb300(args, rank, world):
     batched = None
     if os.environ.get("LG_BENCH_BATCHED", "1") != "0":
         batched = batched_section(args, l2_flush)
+    restruct = None
+    if os.environ.get("LG_BENCH_RESTRUCT", "1") != "0":
+        restruct = restructuring_section(args, l2_flush)
     serving = None
     if os.environ.get("LG_BENCH_SERVING", "1") != "0":
-        lams = [float(v) for v in os.environ.get("LG_SERVE_LAMBDAS", "4").split(",")]
+        lams = [float(v) for v in os.environ.get("LG_SERVE_LAMBDAS", "4,16").split(",")]
         dur = float(os.environ.get("LG_SERVE_SECONDS", "15"))
         serving = [serving_section(lam, dur) for lam in lams]
     line = {
@@ -411,9 +414,57 @@ def run_gb300(args, rank, world):
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
         "device_errors": tm["device_errors"],
         "batched": batched,
+        "restructuring": restruct,
         "serving": serving,
     }
     print(json.dumps(line), flush=True)
+
+
+def restructuring_section(args, l2_flush, steps=None, count=None):
+    """Batched restructuring: aggregates of log-uniform 128..4096 monomers, sintered bonds that break
+    above 10 nN (each bond its own strength), frictional contact for non-bonded pairs, limited
+    Hamaker, each pushed by a rigid plane wall moving at 1 m/s (surface contact k_n = 1e4 N/m). Runs
+    the batch in mixed precision and in FP64 (the FP64 path is bit-identical to the FP64 oracle)
+    and reports the broken-bond fraction and final radius of gyration of both, their relative
+    difference, and particle-steps/s."""
+    from libgran_gb300 import _abi as A
+    from libgran_gb300 import configs as K
+    from libgran_gb300.system import System
+    mat = K.Material()
+    count = count or int(os.environ.get("LG_RESTRUCT_COUNT", "1024"))
+    steps = steps or int(os.environ.get("LG_RESTRUCT_STEPS", "2000"))
+    sizes = K.loguniform_sizes(count, 128, 4096, seed=3)
+    x0, v0 = K.seeded_aggregates(sizes, 3, mat.r)
+    x0 = K.rest_on_wall(x0, sizes, mat.r)
+    wall = K.wall_facet(mat, extent=50 * mat.r)
+    out = {"systems": count, "particles": int(sizes.sum()), "vv_steps": steps}
+    res = {}
+    for name, prec in (("mixed", A.LG_PRECISION_MIXED), ("fp64", A.LG_PRECISION_FP64)):
+        d = K.make_desc(int(sizes.sum()), A.LG_BINARY_BREAKING_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(),
+                        sinter=mat.sinter(), hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r,
+                        precision=prec, n_facets=1, facet_auto_move=1, force_kernel=A.LG_FORCE_KERNEL_COMPACT)
+        probe = System(d, x0, v0, facets=[wall], sizes=sizes)
+        nb = len(probe.bonds()) // 2
+        probe.close()
+        s = System(d, x0, v0, facets=[wall], neck=np.full(nb, 1e-8), sizes=sizes)
+        b0 = len(s.bonds())
+        l2_flush()
+        ms = s.step_timed(mat.dt, steps, VV_PER_STEP)
+        obs = s.batch_observables()
+        b1 = len(s.bonds())
+        res[name] = {"particle_steps_per_s": sizes.sum() * steps / (ms / 1e3),
+                     "broken_fraction": (b0 - b1) / max(b0, 1),
+                     "rg_mean": float(np.mean([o["radius_of_gyration"] for o in obs])),
+                     "rg": np.array([o["radius_of_gyration"] for o in obs]), "device_errors": s.device_errors()}
+        s.close()
+    rg_rel = float(np.max(np.abs(res["mixed"]["rg"] - res["fp64"]["rg"]) / res["fp64"]["rg"]))
+    for k in res:
+        res[k].pop("rg")
+    out.update(res)
+    out["rg_max_rel_diff_mixed_vs_fp64"] = rg_rel
+    bf = res["fp64"]["broken_fraction"]
+    out["broken_fraction_rel_diff"] = abs(res["mixed"]["broken_fraction"] - bf) / bf if bf > 0 else None
+    return out
 
 
 def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):

@@ -135,3 +135,38 @@ def seeded_aggregates(sizes, config_id, r, vmax=0.1):
         xs.append(generate_aggregate(seed, int(n), r))
         vs.append(generate_velocities(seed, int(n), vmax))
     return np.concatenate(xs), np.concatenate(vs)
+
+
+def wall_facet(mat, extent, v_wall=1.0, k_n=1e4):
+    """A rigid plane wall z = 0 moving along +z at v_wall, as one large triangle (side ~ 20 extent)
+    carrying a surface contact functor with normal stiffness k_n (the aggregate workload's other
+    contact constants) and a surface Hamaker functor."""
+    f = A.lg_facet_desc()
+    L = 20.0 * extent
+    f.v_facet[0], f.v_facet[1], f.v_facet[2] = 0.0, 0.0, v_wall
+    verts = [(-L, -L, 0.0), (-L, 3 * L, 0.0), (3 * L, -L, 0.0)]
+    for k, v in enumerate(verts):
+        for c in range(3):
+            f.vertices[3 * k + c] = v[c]
+    f.has_contact = 1
+    f.has_hamaker = 1
+    c = mat.contact()
+    c.k = k_n
+    f.contact = c
+    f.hamaker = mat.hamaker()
+    return f
+
+
+def rest_on_wall(x, sizes, r):
+    """Translate every aggregate so that its lowest sphere touches the plane z = 0 from above
+    (x, y centred on the aggregate's centroid)."""
+    import numpy as np
+    out = np.array(x, dtype=np.float64, copy=True)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for a in range(len(sizes)):
+        seg = out[off[a]:off[a + 1]]
+        c = seg.mean(0)
+        seg[:, 0] -= c[0]
+        seg[:, 1] -= c[1]
+        seg[:, 2] -= seg[:, 2].min() - r
+    return out

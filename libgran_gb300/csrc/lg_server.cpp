@@ -4,8 +4,9 @@
 //   1. admits queued requests, first come first served with backfill, while their device
 //      footprint fits the memory budget: a request becomes a resident engine handle (its state,
 //      springs and bonds stay in HBM until it finishes) with its own CUDA stream;
-//   2. advances every resident request by one rebuild period (graph replays, enqueued on all
-//      streams before any wait, so the requests' kernels overlap on the device);
+//   2. keeps every resident request two rebuild periods ahead on its own stream (graph replays;
+//      completion is tracked with events, no global synchronisation), so requests of different
+//      sizes progress at their own pace and their kernels overlap on the device;
 //   3. retires requests whose budget is spent: observables and positions are copied back, the
 //      handle is destroyed and its memory returns to the budget.
 // A request's result does not depend on what else is resident (each is its own handle), so a
@@ -44,7 +45,12 @@ struct Request {
     lg_observables obs{};
     std::vector<double> x_final;
     std::string error;
+    int64_t enqueued_steps = 0;
+    std::deque<std::pair<cudaEvent_t, int64_t>> inflight;  // (event after a period, its steps)
+    std::vector<cudaEvent_t> free_events;
 };
+
+constexpr int kPeriodsAhead = 2;
 
 }  // namespace
 
@@ -100,6 +106,11 @@ extern "C" int lg_server_create(const lg_system_desc *tmpl, int64_t budget_bytes
 
 static void release_request(lg_server *s, Request &r) {
     if (r.sys) {
+        cudaStreamSynchronize(r.sys->stream);
+        for (auto &p : r.inflight) cudaEventDestroy(p.first);
+        for (auto e : r.free_events) cudaEventDestroy(e);
+        r.inflight.clear();
+        r.free_events.clear();
         lg_destroy(r.sys);
         r.sys = nullptr;
         s->used -= r.bytes;
@@ -211,25 +222,61 @@ static int admit(lg_server *s) {
     return LG_OK;
 }
 
+static void retire(lg_server *s, Request &r) {
+    r.x_final.resize(3 * r.n);
+    int rc = lg_get_observables(r.sys, &r.obs);  // synchronises the request's stream
+    if (rc == LG_OK) rc = lg_get(r.sys, LG_FIELD_X, r.x_final.data());
+    int32_t errs = 0;
+    if (rc == LG_OK) rc = lg_get_device_errors(r.sys, &errs);
+    std::string why = rc != LG_OK ? std::string(lg_last_error()) : std::string("device error word set");
+    release_request(s, r);
+    r.t_done = now_ms();
+    if (rc != LG_OK || errs != 0) {
+        r.state = LG_REQ_FAILED;
+        r.error = why;
+        s->failed++;
+    } else {
+        r.state = LG_REQ_DONE;
+        s->completed++;
+        s->latencies.push_back(r.t_done - r.t_submit);
+    }
+}
+
 extern "C" int lg_server_tick(lg_server *s, int32_t *n_active, int32_t *n_queued, int32_t *n_retired) {
     if (!s) return lg_fail(LG_E_INVALID, "lg_server_tick: null server");
+    const size_t queued_before = s->queue.size();
     int rc = admit(s);
     if (rc != LG_OK) return rc;
-    // enqueue one rebuild period of every resident request on its own stream, then wait
-    std::vector<int64_t> stepping;
+    bool progress = s->queue.size() != queued_before;
+    const int64_t rb = s->tmpl.pairs == LG_PAIRS_VERLET ? s->rebuild_every : 0;
+    // keep every resident request kPeriodsAhead periods ahead on its stream
     for (int64_t id : s->active) {
         Request &r = s->reqs[id];
-        const int64_t k = std::min(s->rebuild_every, r.nsteps - r.done_steps);
-        rc = lg_step(r.sys, s->dt, k, s->tmpl.pairs == LG_PAIRS_VERLET ? s->rebuild_every : 0);
-        if (rc != LG_OK) {
-            r.state = LG_REQ_FAILED;
-            r.error = lg_last_error();
-            continue;
+        while ((int)r.inflight.size() < kPeriodsAhead && r.enqueued_steps < r.nsteps && r.state == LG_REQ_RUNNING) {
+            const int64_t k = std::min(s->rebuild_every, r.nsteps - r.enqueued_steps);
+            rc = lg_step(r.sys, s->dt, k, rb);
+            cudaEvent_t ev = nullptr;
+            if (rc == LG_OK) {
+                if (!r.free_events.empty()) {
+                    ev = r.free_events.back();
+                    r.free_events.pop_back();
+                } else if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+                    ev = nullptr;
+                    rc = lg_fail(LG_E_CUDA, "cudaEventCreate failed");
+                }
+            }
+            if (rc == LG_OK && cudaEventRecord(ev, r.sys->stream) != cudaSuccess) rc = lg_fail(LG_E_CUDA, "cudaEventRecord failed");
+            if (rc != LG_OK) {
+                r.state = LG_REQ_FAILED;
+                r.error = lg_last_error();
+                if (ev) r.free_events.push_back(ev);
+                break;
+            }
+            r.inflight.emplace_back(ev, k);
+            r.enqueued_steps += k;
         }
-        r.done_steps += k;
-        s->particle_steps += k * r.n;
-        stepping.push_back(id);
     }
+    // collect finished periods; retire finished requests
     int32_t retired = 0;
     std::vector<int64_t> still;
     for (int64_t id : s->active) {
@@ -238,35 +285,30 @@ extern "C" int lg_server_tick(lg_server *s, int32_t *n_active, int32_t *n_queued
             release_request(s, r);
             r.t_done = now_ms();
             s->failed++;
+            ++retired;
+            progress = true;
             continue;
         }
-        if (r.done_steps < r.nsteps) {
-            still.push_back(id);
+        while (!r.inflight.empty() && cudaEventQuery(r.inflight.front().first) == cudaSuccess) {
+            r.done_steps += r.inflight.front().second;
+            s->particle_steps += r.inflight.front().second * r.n;
+            r.free_events.push_back(r.inflight.front().first);
+            r.inflight.pop_front();
+            progress = true;
+        }
+        cudaGetLastError();  // cudaEventQuery reports cudaErrorNotReady for pending events
+        if (r.done_steps >= r.nsteps) {
+            retire(s, r);
+            ++retired;
             continue;
         }
-        r.x_final.resize(3 * r.n);
-        int rc1 = lg_get_observables(r.sys, &r.obs);  // synchronises the request's stream
-        int rc2 = rc1 == LG_OK ? lg_get(r.sys, LG_FIELD_X, r.x_final.data()) : rc1;
-        int32_t errs = 0;
-        if (rc2 == LG_OK) rc2 = lg_get_device_errors(r.sys, &errs);
-        release_request(s, r);
-        r.t_done = now_ms();
-        if (rc2 != LG_OK || errs != 0) {
-            r.state = LG_REQ_FAILED;
-            r.error = rc2 != LG_OK ? std::string(lg_last_error()) : std::string("device error word set");
-            s->failed++;
-        } else {
-            r.state = LG_REQ_DONE;
-            s->completed++;
-            s->latencies.push_back(r.t_done - r.t_submit);
-        }
-        ++retired;
+        still.push_back(id);
     }
     s->active.swap(still);
-    // make sure the period is complete on the device before the next tick's host work
-    for (int64_t id : s->active) {
-        Request &r = s->reqs[id];
-        if (r.sys) cudaStreamSynchronize(r.sys->stream);
+    // nothing moved: wait for the oldest outstanding period instead of spinning
+    if (!progress && !s->active.empty()) {
+        Request &r = s->reqs[s->active.front()];
+        if (!r.inflight.empty()) cudaEventSynchronize(r.inflight.front().first);
     }
     if (n_active) *n_active = (int32_t)s->active.size();
     if (n_queued) *n_queued = (int32_t)s->queue.size();

@@ -1,7 +1,9 @@
 // A libgran driver written against the libgran_gb300 drop-in headers: the set-up of libgran's
 // test/hamaker.cpp and test/hamaker_neighbor.cpp (18-particle plate + projectile, contact + Hamaker)
 // with the same template composition and constructor calls, checked against libgran's 1 % targets.
-// Usage: dropin_hamaker [neighbor] [steps_per_call]
+// Usage: dropin_hamaker [all|neighbor] [steps_per_call] [n_steps]
+// With n_steps given the driver prints its end state (momentum, kinetic energy, radius of gyration)
+// and skips the 1 % check, which applies to the full 3e6-step run.
 #include <libgran/contact_force/contact_force.h>
 #include <libgran/granular_system/granular_system.h>
 #include <libgran/granular_system/granular_system_neighbor_list.h>
@@ -23,7 +25,7 @@ struct vec3 {  // a minimal field_value_t (libgran's drivers use Eigen::Vector3d
 };
 
 template <bool neighbor, typename S>
-int run(S &system, double dt, size_t n_steps, size_t per_call, double mass, double inertia) {
+int run(S &system, double dt, size_t n_steps, size_t per_call, double mass, double inertia, bool check) {
     for (size_t n = 0; n < n_steps;) {
         if constexpr (neighbor) {  // update_neighbor_list() every 20 steps, as test/hamaker_neighbor.cpp:121-122
             system.update_neighbor_list();
@@ -55,7 +57,9 @@ int run(S &system, double dt, size_t n_steps, size_t per_call, double mass, doub
     for (auto const &q : x) rg += ((q[0] - cx) * (q[0] - cx) + (q[1] - cy) * (q[1] - cy)) + (q[2] - cz) * (q[2] - cz);
     rg = std::sqrt(rg / x.size());
     const double tp = 1.96373e-19, tke = 8.33959e-20, trg = 3.56253e-08;
-    std::printf("momentum %.6g (target %.6g) ke %.6g (target %.6g) rg %.6g (target %.6g)\n", p, tp, ke, tke, rg, trg);
+    std::printf("momentum %.17g ke %.17g rg %.17g\n", p, ke, rg);
+    if (!check) return 0;
+    std::printf("targets: momentum %.6g ke %.6g rg %.6g\n", tp, tke, trg);
     if (std::fabs(ke - tke) / tke > 0.01 || std::fabs(p - tp) / tp > 0.01 || std::fabs(rg - trg) / trg > 0.01)
         return EXIT_FAILURE;
     return 0;
@@ -65,7 +69,8 @@ int main(int argc, char **argv) {
     const bool neighbor = argc > 1 && std::strcmp(argv[1], "neighbor") == 0;
     const size_t per_call = argc > 2 ? (size_t)std::atol(argv[2]) : 1000;
     const double dt = 1e-13, t_tot = 3.0e-7;
-    const auto n_steps = size_t(t_tot / dt);
+    const bool full = argc <= 3;
+    const auto n_steps = full ? size_t(t_tot / dt) : (size_t)std::atol(argv[3]);
     const double rho = 1700.0, r_part = 1.4e-8;
     const double mass = 4.0 / 3.0 * M_PI * std::pow(r_part, 3.0) * rho;
     const double inertia = 2.0 / 5.0 * mass * std::pow(r_part, 2.0);
@@ -102,9 +107,9 @@ int main(int argc, char **argv) {
         granular_system_neighbor_list<vec3, double, rotational_velocity_verlet_half, rotational_step_handler, bin_t, un_t>
             system(x0.size(), 5.0 * r_part, x0, v0, theta0, omega0, 0.0, vec3::Zero(), 0.0, step_handler_instance,
                    binary_force_functors, unary_force_functors);
-        return run<true>(system, dt, n_steps, per_call, mass, inertia);
+        return run<true>(system, dt, n_steps, per_call, mass, inertia, full);
     }
     granular_system<vec3, double, rotational_velocity_verlet_half, rotational_step_handler, bin_t, un_t> system(
         x0, v0, theta0, omega0, 0.0, vec3::Zero(), 0.0, step_handler_instance, binary_force_functors, unary_force_functors);
-    return run<false>(system, dt, n_steps, per_call, mass, inertia);
+    return run<false>(system, dt, n_steps, per_call, mass, inertia, full);
 }

@@ -116,3 +116,48 @@ def test_snapshot_restore_replays_identically():
     s.step(mat.dt, 60, 20)
     for a, f in zip(first, FIELDS):
         assert np.array_equal(a, s.get(f))
+
+
+def test_restructuring_batch_with_wall_and_breaking_bonds_matches_oracle():
+    """Batched aggregates pushed by a moving wall, bonds breaking at 10 nN: the FP64 batch is
+    bit-identical to the oracle system by system; mixed precision gives the broken-bond fraction
+    and radius of gyration within 1e-3 relative."""
+    from libgran_gb300 import configs as K2
+    mat = K.Material()
+    sizes = np.array([128, 300, 200, 160])
+    x0, v0 = K2.seeded_aggregates(sizes, 77, mat.r)
+    x0 = K2.rest_on_wall(x0, sizes, mat.r)
+    v0 = v0 * 20.0  # livelier than the workload so that bonds load within a short test
+    wall = K2.wall_facet(mat, extent=50 * mat.r)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    res = {}
+    for prec in (A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED):
+        d = K.make_desc(int(sizes.sum()), A.LG_BINARY_BREAKING_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(),
+                        sinter=mat.sinter(), hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r,
+                        precision=prec, n_facets=1, facet_auto_move=1, force_kernel=A.LG_FORCE_KERNEL_COMPACT,
+                        max_neighbors=128)
+        probe = System(d, x0, v0, facets=[wall], sizes=sizes)
+        nb = len(probe.bonds()) // 2
+        s = System(d, x0, v0, facets=[wall], neck=np.full(nb, 1e-8), sizes=sizes)
+        b0 = len(s.bonds())
+        s.step(mat.dt, 400, 20)
+        res[prec] = (s, b0, len(s.bonds()), np.array([o["radius_of_gyration"] for o in s.batch_observables()]))
+        assert s.device_errors() == 0
+    s64, b0, b1, rg64 = res[A.LG_PRECISION_FP64]
+    assert b1 < b0  # some bonds broke
+    # FP64 batch == oracle, system by system
+    for q in range(len(sizes)):
+        n = int(sizes[q])
+        dq = K.make_desc(n, A.LG_BINARY_BREAKING_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(),
+                         sinter=mat.sinter(), hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r,
+                         n_facets=1, facet_auto_move=1)
+        xq, vq = x0[off[q]:off[q + 1]], v0[off[q]:off[q + 1]]
+        probe = O.OracleSystem(dq, xq, vq, facets=[wall])
+        nbq = len(probe.bonds()) // 2
+        o = O.OracleSystem(dq, xq, vq, facets=[wall], neck=np.full(nbq, 1e-8))
+        o.step(mat.dt, 400, 20)
+        assert np.array_equal(o.get(A.LG_FIELD_X), s64.get(A.LG_FIELD_X)[off[q]:off[q + 1]]), q
+    smx, c0, c1, rgmx = res[A.LG_PRECISION_MIXED]
+    assert c0 == b0
+    assert abs((c0 - c1) - (b0 - b1)) <= max(2, 1e-3 * (b0 - b1))  # 2 ordered pairs = one bond
+    assert np.max(np.abs(rgmx - rg64) / rg64) <= 1e-3
