@@ -33,21 +33,39 @@ namespace lg {
 namespace {
 
 constexpr int kWin = 4;            // Hamaker window (slots)
+constexpr int kGroup = 4;          // slots classified per memory round trip
 constexpr int kHCap = 32 * kWin;   // Hamaker queue capacity per window
-constexpr int kRound = 128;        // slots classified per round
-constexpr int kCCap = 256;         // contact queue capacity per round
-constexpr int kWarps = 2;
+// Slicing: the slots of a 32-row group may be split over SL warps (window w of a row goes to warp
+// w % SL), which gives the GPU SL times as many warps to hide latency with when a launch has few
+// rows; each warp's per-row partial sums are then combined in warp order at the end. The FP64
+// kernel always uses SL = 1, so every row is added in ascending slot order.
+template <int SL>
+struct Shape {
+    static constexpr int kSlices = SL;
+    static constexpr int kRowWarps = SL == 1 ? 2 : 1;
+    static constexpr int kRound = SL == 1 ? 128 : 64;  // slots classified per round (per warp)
+    static constexpr int kCCap = SL == 1 ? 256 : 160;  // contact queue capacity per round
+    static constexpr int kWarps = kSlices * kRowWarps;
+};
 #if LG_COMPACT_MIXED
 typedef float rt;
 #else
 typedef double rt;
 #endif
 
+// Virtual slot v of slice sl (its windows sl, sl + SL, ...) -> slot of the row.
+template <int SL>
+__device__ __forceinline__ int64_t slot_of(int64_t v, int sl) {
+    return ((v / kWin) * SL + sl) * kWin + (v % kWin);
+}
+
+template <int SL>
 struct WarpSmem {
+    static constexpr int kCCap = Shape<SL>::kCCap, kRound = Shape<SL>::kRound;
     rt hres[kHCap][3];
     rt cres[kCCap][6];
     int32_t hj[kHCap], cj[kCCap];
-    uint16_t hown[kHCap], cown[kCCap];  // (owner lane << 8) | slot offset
+    uint16_t hown[kHCap], cown[kCCap];  // (owner lane << 8) | slot offset within the round
     uint32_t cball[kRound], hballA[kRound];
     int32_t cbase[kRound];
     uint32_t hball[kWin];
@@ -130,12 +148,13 @@ __device__ __forceinline__ float ham_factor(int mode, float A, float r, float h)
 
 // One queued contact / bond pair: owner row io (lane own of the warp), slot e, partner j.
 #if LG_COMPACT_MIXED
+template <int SL>
 __device__ __forceinline__ void contact_item(const Params &P, const StateView &S, const PairView &PV,
-                                             const BondView &BV, const MixedExtra &M, WarpSmem &W, int q, int64_t row0,
-                                             int64_t kstart, int64_t n, int64_t xs, int64_t bs) {
+                                             const BondView &BV, const MixedExtra &M, WarpSmem<SL> &W, int q,
+                                             int64_t row0, int64_t kstart, int sl, int64_t n, int64_t xs, int64_t bs) {
     const int own = W.cown[q] >> 8;
     const int64_t io = row0 + own;
-    const int64_t e = (kstart + (W.cown[q] & 0xff)) * n + io;
+    const int64_t e = slot_of<SL>(kstart + (W.cown[q] & 0xff), sl) * n + io;
     const int32_t j = W.cj[q];
     const uint32_t fl = PV.flags[e];
     const bool bonded = (fl & kBonded) != 0;
@@ -221,8 +240,9 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
     W.cres[q][5] = torque.z;
 }
 
-__device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S, const MixedExtra &M, WarpSmem &W,
-                                             int q) {
+template <int SL>
+__device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S, const MixedExtra &M,
+                                             WarpSmem<SL> &W, int q) {
     const int own = W.hown[q] >> 8;
     const d3 dx = sub(W.xo[own], ld4(S.x, W.hj[q]));
     const double q4 = fma(dx.z, dx.z, fma(dx.y, dx.y, fma(dx.x, dx.x, -M.four_rh2)));  // |d|^2 - (2r)^2
@@ -241,12 +261,13 @@ __device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S
     W.hres[q][2] = a.z;
 }
 #else
+template <int SL>
 __device__ __forceinline__ void contact_item(const Params &P, const StateView &S, const PairView &PV,
-                                             const BondView &BV, WarpSmem &W, int q, int64_t row0, int64_t kstart,
-                                             int64_t n, int64_t xs, int64_t bs) {
+                                             const BondView &BV, WarpSmem<SL> &W, int q, int64_t row0, int64_t kstart,
+                                             int sl, int64_t n, int64_t xs, int64_t bs) {
     const int own = W.cown[q] >> 8;
     const int64_t io = row0 + own;
-    const int64_t e = (kstart + (W.cown[q] & 0xff)) * n + io;
+    const int64_t e = slot_of<SL>(kstart + (W.cown[q] & 0xff), sl) * n + io;
     const int32_t j = W.cj[q];
     const uint32_t fl = PV.flags[e];
     const d3 xo = W.xo[own], vo = W.vo[own], wo = W.wo[own];
@@ -303,7 +324,8 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
     W.cres[q][5] = pal.z;
 }
 
-__device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S, WarpSmem &W, int q) {
+template <int SL>
+__device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S, WarpSmem<SL> &W, int q) {
     const int own = W.hown[q] >> 8;
     const d3 xo = W.xo[own];
     const d3 xj = ld4(S.x, W.hj[q]);
@@ -323,8 +345,8 @@ __device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S
 
 }  // namespace
 
-template <bool VERLET>
-__global__ void __launch_bounds__(kWarps * 32)
+template <bool VERLET, int SL>
+__global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
 #if LG_COMPACT_MIXED
     forces_compact_mixed(Params P, StateView S, PairView PV, BondView BV, double hdt, double dt, int move_facets,
                          MixedExtra MX)
@@ -334,9 +356,12 @@ __global__ void __launch_bounds__(kWarps * 32)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    WarpSmem &W = reinterpret_cast<WarpSmem *>(smem_raw)[warp];
+    constexpr int kSlices = Shape<SL>::kSlices, kRowWarps = Shape<SL>::kRowWarps, kWarps = Shape<SL>::kWarps;
+    constexpr int kRound = Shape<SL>::kRound, kCCap = Shape<SL>::kCCap;
+    WarpSmem<SL> &W = reinterpret_cast<WarpSmem<SL> *>(smem_raw)[warp];
+    const int rw = warp / kSlices, sl = warp % kSlices;  // row group of the block, slice of it
     const int64_t n = P.n;
-    const int64_t row0 = ((int64_t)blockIdx.x * kWarps + warp) * 32;
+    const int64_t row0 = ((int64_t)blockIdx.x * kRowWarps + rw) * 32;
     const int64_t i = row0 + lane;
     const bool active = i < n;
     const int bm = P.binary_model, hm = P.hamaker_model;
@@ -359,6 +384,11 @@ __global__ void __launch_bounds__(kWarps * 32)
     W.vo[lane] = vi;
     W.wo[lane] = wi;
     const int64_t maxlen = (int64_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
+    // this warp's slots: windows sl, sl + kSlices, ...; virtual slot v maps to slot_of(v)
+    const int64_t nwin = (maxlen + kWin - 1) / kWin;
+    const int64_t mywin = nwin > sl ? (nwin - sl + kSlices - 1) / kSlices : 0;
+    const int64_t vmax = mywin * kWin;
+    auto slot = [sl](int64_t v) -> int64_t { return slot_of<SL>(v, sl); };
     const int64_t xs = PV.cap * n;
     const int64_t bs = (int64_t)BV.bcap * n;
 #if LG_COMPACT_MIXED
@@ -369,64 +399,92 @@ __global__ void __launch_bounds__(kWarps * 32)
 #endif
     __syncwarp();
 
-    for (int64_t kstart = 0; kstart < maxlen;) {
+    for (int64_t kstart = 0; kstart < vmax;) {
         // ---------------- pass A: classify, queue contacts, evaluate them in full warps ----------------
         int ccount = 0, cdone = 0;
-        int64_t k = kstart;
-        for (; k < maxlen && k - kstart < kRound && ccount + 32 <= kCCap; ++k) {
-            bool hb = false, cb = false;
-            int32_t j = 0;
-            if (k < len) {
-                const int64_t e = k * n + i;
-                j = VERLET ? PV.nbr[e] : (int32_t)(k < i ? k : k + 1);
-                const uint32_t fl = PV.flags[e];
-                const bool bonded = (fl & kBonded) && bm != LG_BINARY_NONE;
-#if LG_COMPACT_MIXED
-                const float4 qj = MX.x32[j];
-                const float dxf = q4i.x - qj.x, dyf = q4i.y - qj.y, dzf = q4i.z - qj.z;
-                const float d2f = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
-                const bool ccand = d2f <= MX.contact2f;
-                if (hm == LG_HAMAKER_LIMITED)
-                    hb = d2f <= MX.near2;
-                else if (hm != LG_HAMAKER_NONE)
-                    hb = true;
-#else
-                const double d2 = sqn(sub(xi_, ld4(S.x, j)));
-                const bool ccand = !(d2 > P.contact_skip_d2);
-                if (hm == LG_HAMAKER_LIMITED)
-                    hb = !(d2 > P.hamaker_skip_d2);
-                else if (hm != LG_HAMAKER_NONE)
-                    hb = true;
-#endif
-                if (bm != LG_BINARY_NONE) {
-                    if (bonded || ccand)
-                        cb = true;
-                    else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+        int64_t k = kstart;  // virtual slot index (the actual slot is slot_of(k))
+        // slots are taken four at a time: their indices and neighbour positions are loaded together
+        // (one memory round trip per group), then classified and queued slot by slot
+        for (; k < vmax && k - kstart + kGroup <= kRound && ccount + 32 * kGroup <= kCCap; k += kGroup) {
+            int32_t jg[kGroup];
+            uint32_t fg[kGroup];
+            const int64_t k0 = slot(k);  // kGroup == kWin: a group is one window of consecutive slots
 #pragma unroll
-                        for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
-                        PV.flags[e] = fl & ~kXiLive;
-                    }
+            for (int u = 0; u < kGroup; ++u) {
+                const int64_t kk = k0 + u;
+                jg[u] = 0;
+                fg[u] = 0;
+                if (kk < len) {
+                    const int64_t e = kk * n + i;
+                    jg[u] = VERLET ? PV.nbr[e] : (int32_t)(kk < i ? kk : kk + 1);
+                    fg[u] = PV.flags[e];
                 }
             }
-            const uint32_t bc = __ballot_sync(0xffffffffu, cb);
-            const uint32_t bh = __ballot_sync(0xffffffffu, hb);
-            if (cb) {
-                const int q = ccount + __popc(bc & lt);
-                W.cj[q] = j;
-                W.cown[q] = (uint16_t)((lane << 8) | (int)(k - kstart));
-            }
-            if (lane == 0) {
-                W.cball[k - kstart] = bc;
-                W.cbase[k - kstart] = ccount;
-                W.hballA[k - kstart] = bh;
-            }
-            ccount += __popc(bc);
-            __syncwarp();
-            if (ccount - cdone >= 32) {
 #if LG_COMPACT_MIXED
-                contact_item(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, n, xs, bs);
+            float4 pg[kGroup];
+#pragma unroll
+            for (int u = 0; u < kGroup; ++u) pg[u] = (k0 + u < len) ? MX.x32[jg[u]] : q4i;
 #else
-                contact_item(P, S, PV, BV, W, cdone + lane, row0, kstart, n, xs, bs);
+            d3 pg[kGroup];
+#pragma unroll
+            for (int u = 0; u < kGroup; ++u) pg[u] = (k0 + u < len) ? ld4(S.x, jg[u]) : xi_;
+#endif
+#pragma unroll
+            for (int u = 0; u < kGroup; ++u) {
+                const int64_t kk = k0 + u;
+                const int64_t vv = k + u;
+                bool hb = false, cb = false;
+                const int32_t j = jg[u];
+                if (kk < len) {
+                    const int64_t e = kk * n + i;
+                    const uint32_t fl = fg[u];
+                    const bool bonded = (fl & kBonded) && bm != LG_BINARY_NONE;
+#if LG_COMPACT_MIXED
+                    const float dxf = q4i.x - pg[u].x, dyf = q4i.y - pg[u].y, dzf = q4i.z - pg[u].z;
+                    const float d2f = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
+                    const bool ccand = d2f <= MX.contact2f;
+                    if (hm == LG_HAMAKER_LIMITED)
+                        hb = d2f <= MX.near2;
+                    else if (hm != LG_HAMAKER_NONE)
+                        hb = true;
+#else
+                    const double d2 = sqn(sub(xi_, pg[u]));
+                    const bool ccand = !(d2 > P.contact_skip_d2);
+                    if (hm == LG_HAMAKER_LIMITED)
+                        hb = !(d2 > P.hamaker_skip_d2);
+                    else if (hm != LG_HAMAKER_NONE)
+                        hb = true;
+#endif
+                    if (bm != LG_BINARY_NONE) {
+                        if (bonded || ccand)
+                            cb = true;
+                        else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+#pragma unroll
+                            for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+                            PV.flags[e] = fl & ~kXiLive;
+                        }
+                    }
+                }
+                const uint32_t bc = __ballot_sync(0xffffffffu, cb);
+                const uint32_t bh = __ballot_sync(0xffffffffu, hb);
+                if (cb) {
+                    const int q = ccount + __popc(bc & lt);
+                    W.cj[q] = j;
+                    W.cown[q] = (uint16_t)((lane << 8) | (int)(vv - kstart));
+                }
+                if (lane == 0) {
+                    W.cball[vv - kstart] = bc;
+                    W.cbase[vv - kstart] = ccount;
+                    W.hballA[vv - kstart] = bh;
+                }
+                ccount += __popc(bc);
+            }
+            __syncwarp();
+            while (ccount - cdone >= 32) {
+#if LG_COMPACT_MIXED
+                contact_item<SL>(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, sl, n, xs, bs);
+#else
+                contact_item<SL>(P, S, PV, BV, W, cdone + lane, row0, kstart, sl, n, xs, bs);
 #endif
                 cdone += 32;
                 __syncwarp();
@@ -436,21 +494,22 @@ __global__ void __launch_bounds__(kWarps * 32)
         if (cdone < ccount) {
             if (cdone + lane < ccount)
 #if LG_COMPACT_MIXED
-                contact_item(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, n, xs, bs);
+                contact_item<SL>(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, sl, n, xs, bs);
 #else
-                contact_item(P, S, PV, BV, W, cdone + lane, row0, kstart, n, xs, bs);
+                contact_item<SL>(P, S, PV, BV, W, cdone + lane, row0, kstart, sl, n, xs, bs);
 #endif
             cdone = ccount;
         }
         __syncwarp();
 
         // ---------------- pass B: Hamaker windows and the ordered fold ----------------
-        for (int64_t kw = kstart; kw < kend; kw += kWin) {
+        for (int64_t vw = kstart; vw < kend; vw += kWin) {
             int hcount = 0;
+            const int64_t kw = slot(vw);  // first slot of the window
 #pragma unroll
             for (int t = 0; t < kWin; ++t) {
                 const int64_t kk = kw + t;
-                const uint32_t bh = kk < kend ? W.hballA[kk - kstart] : 0u;
+                const uint32_t bh = vw + t < kend ? W.hballA[vw + t - kstart] : 0u;
                 if ((bh >> lane) & 1u) {
                     const int q = hcount + __popc(bh & lt);
                     W.hj[q] = VERLET ? PV.nbr[kk * n + i] : (int32_t)(kk < i ? kk : kk + 1);
@@ -465,20 +524,20 @@ __global__ void __launch_bounds__(kWarps * 32)
             __syncwarp();
             for (int q = lane; q < hcount; q += 32)
 #if LG_COMPACT_MIXED
-                hamaker_item(P, S, MX, W, q);
+                hamaker_item<SL>(P, S, MX, W, q);
 #else
-                hamaker_item(P, S, W, q);
+                hamaker_item<SL>(P, S, W, q);
 #endif
             __syncwarp();
 #pragma unroll
             for (int t = 0; t < kWin; ++t) {
                 const int64_t kk = kw + t;
-                if (kk < kend && kk < len) {
-                    const uint32_t bh = W.hball[t], bc = W.cball[kk - kstart];
+                if (vw + t < kend && kk < len) {
+                    const uint32_t bh = W.hball[t], bc = W.cball[vw + t - kstart];
                     const bool hb = (bh >> lane) & 1u, cb = (bc >> lane) & 1u;
 #if LG_COMPACT_MIXED
                     if (cb) {
-                        const int q = W.cbase[kk - kstart] + __popc(bc & lt);
+                        const int q = W.cbase[vw + t - kstart] + __popc(bc & lt);
                         acc.x += (double)W.cres[q][0];
                         acc.y += (double)W.cres[q][1];
                         acc.z += (double)W.cres[q][2];
@@ -501,7 +560,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                         if (bm != LG_BINARY_NONE) {
                             have = true;
                             if (cb) {
-                                const int q = W.cbase[kk - kstart] + __popc(bc & lt);
+                                const int q = W.cbase[vw + t - kstart] + __popc(bc & lt);
                                 pa = mk3(W.cres[q][0], W.cres[q][1], W.cres[q][2]);
                                 pal = mk3(W.cres[q][3], W.cres[q][4], W.cres[q][5]);
                             }
@@ -530,6 +589,25 @@ __global__ void __launch_bounds__(kWarps * 32)
         }
         kstart = kend;
     }
+#if LG_COMPACT_MIXED
+    // combine the slices' partial sums of each row in slice order (fixed, deterministic)
+    if (kSlices > 1) {
+        double *part = reinterpret_cast<double *>(smem_raw + sizeof(WarpSmem<SL>) * kWarps);
+        double *mine = part + ((int64_t)(rw * kSlices + sl) * 32 + lane) * 9;
+        mine[0] = acc.x; mine[1] = acc.y; mine[2] = acc.z;
+        mine[3] = accw.x; mine[4] = accw.y; mine[5] = accw.z;
+        mine[6] = acch.x; mine[7] = acch.y; mine[8] = acch.z;
+        __syncthreads();
+        if (sl != 0) return;
+        acc = accw = acch = zero3();
+        for (int q = 0; q < kSlices; ++q) {
+            const double *o = part + ((int64_t)(rw * kSlices + q) * 32 + lane) * 9;
+            acc = add(acc, mk3(o[0], o[1], o[2]));
+            accw = add(accw, mk3(o[3], o[4], o[5]));
+            acch = add(acch, mk3(o[6], o[7], o[8]));
+        }
+    }
+#endif
     if (!active) return;
 
 #if LG_COMPACT_MIXED
@@ -596,43 +674,51 @@ __global__ void __launch_bounds__(kWarps * 32)
         set_error(S.err, LG_DEVERR_NONFINITE);
 }
 
+template <bool VERLET, int SL>
+static void launch_compact(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                           double dt, int move_facets, const MixedExtra *MX, cudaStream_t st) {
+    using Sh = Shape<SL>;
+    const size_t smem = sizeof(WarpSmem<SL>) * Sh::kWarps + (SL > 1 ? sizeof(double) * 9 * 32 * Sh::kWarps : 0);
+    const int64_t rows_per_block = Sh::kRowWarps * 32;
+    const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
+    static thread_local int attr_device = -1;  // the attribute is per device; set once per thread and device
+    int dev = 0;
+    cudaGetDevice(&dev);
+#if LG_COMPACT_MIXED
+    auto kern = forces_compact_mixed<VERLET, SL>;
+#else
+    auto kern = forces_compact_fp64<VERLET, SL>;
+#endif
+    if (attr_device != dev) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_device = dev;
+    }
+#if LG_COMPACT_MIXED
+    kern<<<blocks, Sh::kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets, *MX);
+#else
+    (void)MX;
+    kern<<<blocks, Sh::kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets);
+#endif
+}
+
 #if LG_COMPACT_MIXED
 void launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                  double dt, int move_facets, const MixedExtra &MX, cudaStream_t st) {
-    const size_t smem = sizeof(WarpSmem) * kWarps;
-    const int64_t rows_per_block = kWarps * 32;
-    const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
-    static thread_local int attr_device = -1;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (attr_device != dev) {  // the attribute is per device; set it once per thread and device
-        cudaFuncSetAttribute(forces_compact_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(forces_compact_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_device = dev;
-    }
-    if (P.pairs == LG_PAIRS_VERLET)
-        forces_compact_mixed<true><<<blocks, kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets, MX);
-    else
-        forces_compact_mixed<false><<<blocks, kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets, MX);
+    // slice rows over four warps when the launch has too few rows to fill the GPU with warps
+    const bool slice = P.n < 152 * 32 * 12;
+    const bool ver = P.pairs == LG_PAIRS_VERLET;
+    if (ver && slice) launch_compact<true, 4>(P, S, PV, BV, hdt, dt, move_facets, &MX, st);
+    else if (ver) launch_compact<true, 1>(P, S, PV, BV, hdt, dt, move_facets, &MX, st);
+    else if (slice) launch_compact<false, 4>(P, S, PV, BV, hdt, dt, move_facets, &MX, st);
+    else launch_compact<false, 1>(P, S, PV, BV, hdt, dt, move_facets, &MX, st);
 }
 #else
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                 double dt, int move_facets, cudaStream_t st) {
-    const size_t smem = sizeof(WarpSmem) * kWarps;
-    const int64_t rows_per_block = kWarps * 32;
-    const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
-    static thread_local int attr_device = -1;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (attr_device != dev) {  // the attribute is per device; set it once per thread and device
-        cudaFuncSetAttribute(forces_compact_fp64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(forces_compact_fp64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_device = dev;
-    }
     if (P.pairs == LG_PAIRS_VERLET)
-        forces_compact_fp64<true><<<blocks, kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets);
+        launch_compact<true, 1>(P, S, PV, BV, hdt, dt, move_facets, nullptr, st);
     else
-        forces_compact_fp64<false><<<blocks, kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets);
+        launch_compact<false, 1>(P, S, PV, BV, hdt, dt, move_facets, nullptr, st);
 }
 #endif
 
