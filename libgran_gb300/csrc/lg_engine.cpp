@@ -707,7 +707,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
             for (int64_t i = 0; i < n; ++i) sum += x0[3 * i + c];
             s->origin[c] = sum / (double)n;
         }
-        LG_TRY(s->alloc(&s->x32, (size_t)n));
+        LG_TRY(s->alloc(&s->x32, 2 * (size_t)n));  // float-float: high parts, then low parts
         if (s->n_systems > 0) {
             std::vector<dbl4> org((size_t)s->n_systems);
             for (int64_t q = 0; q < s->n_systems; ++q) {
@@ -731,6 +731,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         if (d->hamaker_model == LG_HAMAKER_FULL || d->hamaker_model == LG_HAMAKER_SIMPLIFIED)
             near = std::max(near, 7.0 * d->hamaker.r_part);
         s->mx.x32 = s->x32;
+        s->mx.x32lo = s->x32 + n;
         s->mx.near2 = (float)(near * near * 1.004);
         double cnear = 0.0;
         if (d->binary_model != LG_BINARY_NONE) cnear = std::max(cnear, 2.0 * d->contact.r_part);
@@ -756,6 +757,16 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         M.b_r = (float)B.r_part; M.b_dt = (float)B.dt;
         M.h_A = (float)d->hamaker.A; M.h_h0 = (float)d->hamaker.h0; M.h_r = (float)d->hamaker.r_part;
         s->mx.rcut2 = d->hamaker.r_cutoff * d->hamaker.r_cutoff;
+        auto split = [](double v, float &hi, float &lo) {
+            hi = (float)v;
+            lo = (float)(v - (double)hi);
+        };
+        split(s->mx.four_rh2, M.h_fr_hi, M.h_fr_lo);
+        split(s->mx.four_rc2, M.c_fr_hi, M.c_fr_lo);
+        split(s->mx.four_rb2, M.b_fr_hi, M.b_fr_lo);
+        M.h_qcut = (float)(s->mx.rcut2 - s->mx.four_rh2);
+        M.bin_im = (float)(sinter ? s->mx.inv_mass_b : s->mx.inv_mass_c);
+        M.bin_iI = (float)(sinter ? s->mx.inv_inertia_b : s->mx.inv_inertia_c);
     }
     s->T = d->threads_per_row > 0 ? d->threads_per_row : choose_threads_per_row(s);
     s->kernel = choose_kernel(s, d->force_kernel);
@@ -1264,7 +1275,7 @@ static int snapshot_take(lg_system *s) {
         addb(s->fv[0], sizeof(double) * 9 * (size_t)nf);
         addb(s->fv[1], sizeof(double) * 9 * (size_t)nf);
         addb(s->err, sizeof(int32_t));
-        if (s->x32) addb(s->x32, sizeof(float4) * n);
+        if (s->x32) addb(s->x32, sizeof(float4) * 2 * n);
         const int npv = s->P.pairs == LG_PAIRS_VERLET ? 2 : 1;
         for (int q = 0; q < npv; ++q) {
             PairView &pv = s->pv[q];

@@ -19,8 +19,11 @@
 // is computed by the same functions as the sequential kernel and the fold adds in the same order,
 // so the result is bit-identical to the sequential evaluation.
 //
-// Compiled twice: LG_COMPACT_MIXED=0 (FP64) and LG_COMPACT_MIXED=1 (FP32 pair arithmetic with FP64
-// separation, overlap, springs, sums; see lg_forces_mixed.cu for the split).
+// Compiled twice: LG_COMPACT_MIXED=0 (FP64) and LG_COMPACT_MIXED=1. The mixed build keeps the FP64
+// pipe for the contact/bond items only (FP64 separation, overlap and springs, as in
+// lg_forces_mixed.cu): every Hamaker pair takes its separation and |d|^2 - (2r)^2 from float-float
+// positions with error-free FP32 transformations, and the per-row sums are float-float
+// (compensated) FP32 accumulations, converted to FP64 once per row.
 #include "lg_common.cuh"
 #include "lg_kernels.h"
 
@@ -71,6 +74,9 @@ struct WarpSmem {
     uint32_t hball[kWin];
     int32_t hbase[kWin];
     d3 xo[32], vo[32], wo[32];
+#if LG_COMPACT_MIXED
+    float4 xh[32], xl[32];  // own position as float-float (high, low parts)
+#endif
 };
 
 #if LG_COMPACT_MIXED
@@ -144,6 +150,55 @@ __device__ __forceinline__ float ham_factor(int mode, float A, float r, float h)
     float br = a * u - 2.0f * w - 4.0f * r * r * (w * w * w) - 2.0f * r * r * a * (u * u);
     return -A / 6.0f * br;
 }
+
+// Float-float arithmetic (a value is hi + lo with |lo| <= ulp(hi) / 2). The _rn intrinsics keep the
+// compiler from contracting or reordering the error-free steps.
+struct ff {
+    float hi, lo;
+};
+// TwoSum (Knuth): s + e == a + b exactly, whatever the magnitudes of a and b.
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+// Compensated accumulation a += b: the rounding error of every addition is kept in a.lo.
+__device__ __forceinline__ void ff_acc(ff &a, float b) {
+    const ff s = two_sum(a.hi, b);
+    a.hi = s.hi;
+    a.lo = __fadd_rn(a.lo, s.lo);
+}
+__device__ __forceinline__ void ff_acc(ff &a, ff b) {
+    const ff s = two_sum(a.hi, b.hi);
+    a.hi = s.hi;
+    a.lo = __fadd_rn(a.lo, __fadd_rn(s.lo, b.lo));
+}
+__device__ __forceinline__ double ff_to_d(ff a) { return (double)a.hi + (double)a.lo; }
+
+// Separation d = x_i - x_j (FP32) and q = |d|^2 - (2r)^2 from float-float positions. Per component
+// the high parts' difference is split exactly (TwoSum) and its error joins the low parts'
+// difference, so dh + dl equals the separation to about 2^-48 of the coordinates. Then
+// (dh + dl)^2 = dh^2 + dl (2 dh + dl), with dh^2 split exactly by FMA; the three large squares and
+// -(2r)^2 (given as fr_hi + fr_lo) are added with TwoSum, so q comes out with FP32 relative
+// precision however close |d| is to 2r.
+struct SepFF {
+    f3 d;
+    float q;
+};
+__device__ __forceinline__ SepFF separation_ff(float4 hi, float4 lo, float4 hj, float4 lj, float fr_hi, float fr_lo) {
+    const ff tx = two_sum(hi.x, -hj.x), ty = two_sum(hi.y, -hj.y), tz = two_sum(hi.z, -hj.z);
+    const float lx = __fadd_rn(tx.lo, __fsub_rn(lo.x, lj.x));
+    const float ly = __fadd_rn(ty.lo, __fsub_rn(lo.y, lj.y));
+    const float lz = __fadd_rn(tz.lo, __fsub_rn(lo.z, lj.z));
+    const float px = __fmul_rn(tx.hi, tx.hi), py = __fmul_rn(ty.hi, ty.hi), pz = __fmul_rn(tz.hi, tz.hi);
+    const float ex = __fmaf_rn(tx.hi, tx.hi, -px), ey = __fmaf_rn(ty.hi, ty.hi, -py), ez = __fmaf_rn(tz.hi, tz.hi, -pz);
+    const float cx = lx * (2.0f * tx.hi + lx), cy = ly * (2.0f * ty.hi + ly), cz = lz * (2.0f * tz.hi + lz);
+    const ff s1 = two_sum(px, py);
+    const ff s2 = two_sum(s1.hi, pz);
+    const ff s3 = two_sum(s2.hi, -fr_hi);
+    const float rest = ((s1.lo + s2.lo) + s3.lo) + ((ex + ey) + ez) + ((cx + cy) + cz) - fr_lo;
+    return SepFF{fm(tx.hi + lx, ty.hi + ly, tz.hi + lz), s3.hi + rest};
+}
 #endif
 
 // One queued contact / bond pair: owner row io (lane own of the warp), slot e, partner j.
@@ -158,15 +213,14 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
     const int32_t j = W.cj[q];
     const uint32_t fl = PV.flags[e];
     const bool bonded = (fl & kBonded) != 0;
-    const d3 xo = W.xo[own], vo = W.vo[own], wo = W.wo[own];
-    const d3 xj = ld4(S.x, j);
-    const d3 dx = sub(xo, xj);
-    const double q4 = fma(dx.z, dx.z, fma(dx.y, dx.y, fma(dx.x, dx.x, -(bonded ? M.four_rb2 : M.four_rc2))));
-    const f3 dxf = tof(dx);
+    const d3 vo = W.vo[own], wo = W.wo[own];
+    const SepFF sp = separation_ff(W.xh[own], W.xl[own], M.x32[j], M.x32lo[j], bonded ? M.b_fr_hi : M.c_fr_hi,
+                                   bonded ? M.b_fr_lo : M.c_fr_lo);
+    const f3 dxf = sp.d;
     const float d2f = fdot(dxf, dxf);
     const float rr = bonded ? M.b_r : M.c_r;
     const float rsd = rsqrtf(d2f);
-    const float overlap = -(float)q4 / (d2f * rsd + 2.0f * rr);  // 2r - |d|, from |d|^2 - (2r)^2 in FP64
+    const float overlap = -sp.q / (d2f * rsd + 2.0f * rr);  // 2r - |d|, from |d|^2 - (2r)^2
     f3 force = fm(0.f, 0.f, 0.f), torque = fm(0.f, 0.f, 0.f);
     if (bonded || overlap > 0.0f) {
         const f3 n3 = fscl(rsd, dxf);
@@ -232,26 +286,28 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
         for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
         PV.flags[e] = fl & ~kXiLive;
     }
-    W.cres[q][0] = force.x;
-    W.cres[q][1] = force.y;
-    W.cres[q][2] = force.z;
-    W.cres[q][3] = torque.x;
-    W.cres[q][4] = torque.y;
-    W.cres[q][5] = torque.z;
+    // accelerations: the binary functor's force and torque over its mass and moment of inertia
+    W.cres[q][0] = force.x * M.bin_im;
+    W.cres[q][1] = force.y * M.bin_im;
+    W.cres[q][2] = force.z * M.bin_im;
+    W.cres[q][3] = torque.x * M.bin_iI;
+    W.cres[q][4] = torque.y * M.bin_iI;
+    W.cres[q][5] = torque.z * M.bin_iI;
 }
 
 template <int SL>
 __device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S, const MixedExtra &M,
                                              WarpSmem<SL> &W, int q) {
+    (void)S;
     const int own = W.hown[q] >> 8;
-    const d3 dx = sub(W.xo[own], ld4(S.x, W.hj[q]));
-    const double q4 = fma(dx.z, dx.z, fma(dx.y, dx.y, fma(dx.x, dx.x, -M.four_rh2)));  // |d|^2 - (2r)^2
+    const int32_t j = W.hj[q];
+    const SepFF sp = separation_ff(W.xh[own], W.xl[own], M.x32[j], M.x32lo[j], M.h_fr_hi, M.h_fr_lo);
     f3 a = fm(0.f, 0.f, 0.f);
-    if (!(P.hamaker_model == LG_HAMAKER_LIMITED && q4 > M.rcut2 - M.four_rh2)) {
-        const f3 dxf = tof(dx);
+    if (!(P.hamaker_model == LG_HAMAKER_LIMITED && sp.q > M.h_qcut)) {
+        const f3 dxf = sp.d;
         const float d2f = fdot(dxf, dxf);
         const float rsd = rsqrtf(d2f);
-        float h = (float)q4 / (d2f * rsd + 2.0f * M.h_r);  // |d| - 2r, exact to FP32
+        float h = sp.q / (d2f * rsd + 2.0f * M.h_r);  // |d| - 2r to FP32 precision
         h = fmaxf(h, M.h_h0);
         const float sfac = ham_factor(P.hamaker_model, M.h_A, M.h_r, h) * M.inv_mass_h * rsd;
         a = fscl(-sfac, dxf);  // along x_j - x_i
@@ -380,7 +436,13 @@ __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
         wi = ld4(S.w, i);
         len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
     }
+#if LG_COMPACT_MIXED
+    const float4 q4i = active ? MX.x32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    W.xh[lane] = q4i;
+    W.xl[lane] = active ? MX.x32lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+#else
     W.xo[lane] = xi_;
+#endif
     W.vo[lane] = vi;
     W.wo[lane] = wi;
     const int64_t maxlen = (int64_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
@@ -392,8 +454,7 @@ __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
     const int64_t xs = PV.cap * n;
     const int64_t bs = (int64_t)BV.bcap * n;
 #if LG_COMPACT_MIXED
-    const float4 q4i = active ? MX.x32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    d3 acc = zero3(), accw = zero3(), acch = zero3();
+    ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accw[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 #else
     d3 acc = zero3(), accw = zero3();
 #endif
@@ -538,18 +599,16 @@ __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
 #if LG_COMPACT_MIXED
                     if (cb) {
                         const int q = W.cbase[vw + t - kstart] + __popc(bc & lt);
-                        acc.x += (double)W.cres[q][0];
-                        acc.y += (double)W.cres[q][1];
-                        acc.z += (double)W.cres[q][2];
-                        accw.x += (double)W.cres[q][3];
-                        accw.y += (double)W.cres[q][4];
-                        accw.z += (double)W.cres[q][5];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            ff_acc(acc[c], W.cres[q][c]);
+                            ff_acc(accw[c], W.cres[q][3 + c]);
+                        }
                     }
                     if (hb) {
                         const int q = W.hbase[t] + __popc(bh & lt);
-                        acch.x += (double)W.hres[q][0];
-                        acch.y += (double)W.hres[q][1];
-                        acch.z += (double)W.hres[q][2];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) ff_acc(acc[c], W.hres[q][c]);
                     }
 #else
                     // the reference's fold: pa = binary(i, j) [+ hamaker(i, j)]; acc += pa. Pairs with no
@@ -592,28 +651,30 @@ __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
 #if LG_COMPACT_MIXED
     // combine the slices' partial sums of each row in slice order (fixed, deterministic)
     if (kSlices > 1) {
-        double *part = reinterpret_cast<double *>(smem_raw + sizeof(WarpSmem<SL>) * kWarps);
-        double *mine = part + ((int64_t)(rw * kSlices + sl) * 32 + lane) * 9;
-        mine[0] = acc.x; mine[1] = acc.y; mine[2] = acc.z;
-        mine[3] = accw.x; mine[4] = accw.y; mine[5] = accw.z;
-        mine[6] = acch.x; mine[7] = acch.y; mine[8] = acch.z;
+        ff *part = reinterpret_cast<ff *>(smem_raw + sizeof(WarpSmem<SL>) * kWarps);
+        ff *mine = part + ((int64_t)(rw * kSlices + sl) * 32 + lane) * 6;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            mine[c] = acc[c];
+            mine[3 + c] = accw[c];
+        }
         __syncthreads();
         if (sl != 0) return;
-        acc = accw = acch = zero3();
-        for (int q = 0; q < kSlices; ++q) {
-            const double *o = part + ((int64_t)(rw * kSlices + q) * 32 + lane) * 9;
-            acc = add(acc, mk3(o[0], o[1], o[2]));
-            accw = add(accw, mk3(o[3], o[4], o[5]));
-            acch = add(acch, mk3(o[6], o[7], o[8]));
+        for (int q = 1; q < kSlices; ++q) {
+            const ff *o = part + ((int64_t)(rw * kSlices + q) * 32 + lane) * 6;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                ff_acc(acc[c], o[c]);
+                ff_acc(accw[c], o[3 + c]);
+            }
         }
     }
 #endif
     if (!active) return;
 
 #if LG_COMPACT_MIXED
-    const bool sint = bm == LG_BINARY_SINTER || bm == LG_BINARY_BREAKING_SINTER;
-    d3 a_tot = add(scl(sint ? MX.inv_mass_b : MX.inv_mass_c, acc), acch);
-    d3 al_tot = scl(sint ? MX.inv_inertia_b : MX.inv_inertia_c, accw);
+    d3 a_tot = mk3(ff_to_d(acc[0]), ff_to_d(acc[1]), ff_to_d(acc[2]));
+    d3 al_tot = mk3(ff_to_d(accw[0]), ff_to_d(accw[1]), ff_to_d(accw[2]));
     d3 &accA = a_tot;
     d3 &accW = al_tot;
 #else
@@ -678,7 +739,7 @@ template <bool VERLET, int SL>
 static void launch_compact(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                            double dt, int move_facets, const MixedExtra *MX, cudaStream_t st) {
     using Sh = Shape<SL>;
-    const size_t smem = sizeof(WarpSmem<SL>) * Sh::kWarps + (SL > 1 ? sizeof(double) * 9 * 32 * Sh::kWarps : 0);
+    const size_t smem = sizeof(WarpSmem<SL>) * Sh::kWarps + (SL > 1 ? sizeof(float) * 12 * 32 * Sh::kWarps : 0);
     const int64_t rows_per_block = Sh::kRowWarps * 32;
     const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
     static thread_local int attr_device = -1;  // the attribute is per device; set once per thread and device

@@ -327,28 +327,33 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
         set_error(S.err, LG_DEVERR_NONFINITE);
 }
 
-__device__ __forceinline__ float4 rel_f32(d3 q, double ox, double oy, double oz, const int32_t *agg,
-                                          const dbl4 *orig, int64_t i) {
+// Position of particle i relative to its system's origin as a float-float pair: x32[i] receives
+// the FP32 rounding of the FP64 difference, x32[n + i] the FP32 rounding of what that leaves.
+__device__ __forceinline__ void rel_ff(d3 q, double ox, double oy, double oz, const int32_t *agg, const dbl4 *orig,
+                                       int64_t i, int64_t n, float4 *__restrict__ x32) {
     if (agg) {
         const dbl4 o = orig[agg[i]];
         ox = o.x;
         oy = o.y;
         oz = o.z;
     }
-    return make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), 0.0f);
+    const double rx = q.x - ox, ry = q.y - oy, rz = q.z - oz;
+    const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
+    x32[i] = make_float4(hx, hy, hz, 0.0f);
+    x32[n + i] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.0f);
 }
 
-// FP32 copy of the positions relative to the system origin (for culling); in a batch every system
-// has its own origin.
+// Float-float copy of the positions relative to the system origin; in a batch every system has
+// its own origin.
 __global__ void positions_to_f32(int64_t n, const dbl4 *__restrict__ x, double ox, double oy, double oz,
                                  const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig,
                                  float4 *__restrict__ x32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    x32[i] = rel_f32(ld4(x, i), ox, oy, oz, agg, orig, i);
+    rel_ff(ld4(x, i), ox, oy, oz, agg, orig, i, n, x32);
 }
 
-// Kick + drift of the mixed path: FP64 integration, then the FP32 position copy.
+// Kick + drift of the mixed path: FP64 integration, then the float-float position copy.
 __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restrict__ v, dbl4 *__restrict__ th,
                                  dbl4 *__restrict__ w, const dbl4 *__restrict__ a, const dbl4 *__restrict__ al,
                                  double dt, double hdt, double ox, double oy, double oz, const int32_t *__restrict__ agg,
@@ -362,7 +367,7 @@ __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restri
     d3 xn = add(ld4(x, i), scl(dt, vi));
     st4(x, i, xn);
     st4(th, i, add(ld4(th, i), scl(dt, wi)));
-    x32[i] = rel_f32(xn, ox, oy, oz, agg, orig, i);
+    rel_ff(xn, ox, oy, oz, agg, orig, i, n, x32);
 }
 
 template <int T, bool VERLET>

@@ -45,7 +45,11 @@ void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, int64_t
 
 // Mixed-precision path (lg_forces_mixed.cu)
 struct MixedExtra {
-    float4 *x32;      // [n] FP32 positions relative to the system origin (culling only)
+    // [2n] positions relative to the system origin as float-float pairs: x32[i] = FP32 rounding of
+    // x_i - origin (culling, and the high part), x32lo[i] = x32[n + i] = FP32 rounding of the
+    // remainder (x_i - origin) - x32[i]; hi + lo holds the position to about 2^-48 of its magnitude
+    float4 *x32;
+    const float4 *x32lo;
     float near2;      // squared culling radius (FP32 positions); beyond it a pair cannot touch and the
                       // limited Hamaker force is zero
     float contact2f;  // squared contact-candidate radius (FP32 positions, with margin)
@@ -58,10 +62,16 @@ struct MixedExtra {
     float c_k, c_gn, c_kt, c_gt, c_mus, c_phid, c_kr, c_gr, c_mur, c_phir, c_ko, c_go, c_muo, c_phio, c_r, c_dt;
     float b_k, b_gn, b_kt, b_gt, b_kr, b_gr, b_ko, b_go, b_r, b_dt;
     float h_A, h_h0, h_r;
+    // compacted kernel: (2r)^2 of the Hamaker functor as hi + lo, the limited-Hamaker cutoff as a
+    // bound on |d|^2 - (2r)^2, and the reciprocal mass and inertia of the binary functor in use
+    float h_fr_hi, h_fr_lo, h_qcut;
+    float c_fr_hi, c_fr_lo, b_fr_hi, b_fr_lo;
+    float bin_im, bin_iI;
 };
 bool mixed_available();
 void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
                          double hdt, double dt, int move_facets, const MixedExtra &MX, cudaStream_t st);
+// x32 has 2n entries (high parts, then low parts; see MixedExtra)
 void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, const int32_t *agg, const dbl4 *orig,
                              float4 *x32, cudaStream_t st);
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
