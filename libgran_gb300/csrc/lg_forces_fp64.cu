@@ -366,115 +366,171 @@ __global__ void cell_scatter(int64_t n, const int32_t *__restrict__ cell_of, con
     sorted[start[c] + p] = (int32_t)i;
 }
 
-constexpr int kBuildThreads = 64;
+constexpr int kBuildRows = 32;   // rows per block
+constexpr int kBuildWarps = 8;   // warps per block; warp w builds rows w, w + 8, ...
 
-// Build row i: every j != i with squared centre distance < r_verlet^2 (the FP64 test; an FP32
-// filter accepts or rejects the clear cases), ascending j, carrying the springs (and live flag) of
-// pairs that were already listed, and marking intact bonds. Candidates are gathered and sorted in
-// shared memory (slot k of thread t at k * blockDim + t, conflict-free).
-__global__ void __launch_bounds__(kBuildThreads) build_rows(int64_t n, const dbl4 *__restrict__ x, BatchView B,
-                                                            const float4 *__restrict__ x32,
-                                                            const GridDev *__restrict__ g, const int32_t *__restrict__ cstart,
-                                                            const int32_t *__restrict__ ccount, const int32_t *__restrict__ sorted,
-                                                            double rv2, PairView oldv, PairView newv, BondView BV,
-                                                            int32_t *err, int32_t *max_row) {
-    extern __shared__ int32_t js[];
-    const int tid = threadIdx.x;
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + tid;
-    if (i >= n) return;
-    const int64_t cap = newv.cap;
-    const float4 fi = x32[i];
+// Shared-memory layout of build_rows for row capacity cap and bond capacity bcap: three 32-row
+// tiles (partner, flags, old slot) with an odd row stride, then per warp the unsorted candidates,
+// the old row and the row's bond partners.
+__host__ __device__ inline int64_t build_tile_stride(int64_t cap) { return cap | 1; }
+__host__ __device__ inline size_t build_smem_bytes(int64_t cap, int64_t bcap) {
+    return sizeof(int32_t) * (size_t)(3 * kBuildRows * build_tile_stride(cap) + kBuildWarps * (2 * cap + bcap));
+}
+
+// Build rows row0 .. row0 + 31: every j != i with squared centre distance < r_verlet^2 (the FP64
+// test; an FP32 filter accepts or rejects the clear cases), ascending j, carrying the springs (and
+// live flag) of pairs that were already listed, and marking intact bonds.
+// One warp per row: the 27 neighbour cells are 9 runs of consecutive cells (x fastest), i.e. 9
+// contiguous ranges of the cell-sorted particle list; the lanes test 32 candidates at a time and
+// append the accepted ones in scan order (ballot + popc). The row is ordered by a rank sort (j is
+// unique), the old row is searched by bisection for spring carry-over, and the finished rows of the
+// block are written slot-major so that the 32 rows' slot k go out as one coalesced store.
+__global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
+    int64_t n, const dbl4 *__restrict__ x, BatchView B, const float4 *__restrict__ x32, const GridDev *__restrict__ g,
+    const int32_t *__restrict__ cstart, const int32_t *__restrict__ ccount, const int32_t *__restrict__ sorted,
+    double rv2, PairView oldv, PairView newv, BondView BV, int32_t *err, int32_t *max_row) {
+    extern __shared__ int32_t sm[];
+    __shared__ int32_t rlen[kBuildRows];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    const int64_t cap = newv.cap, ts = build_tile_stride(cap);
+    const int bcap = BV.bcap;
+    int32_t *tj = sm;
+    uint32_t *tf = reinterpret_cast<uint32_t *>(tj + kBuildRows * ts);
+    int32_t *tp = reinterpret_cast<int32_t *>(tf + kBuildRows * ts);
+    int32_t *wraw = tp + kBuildRows * ts + (int64_t)warp * (2 * cap + bcap);
+    int32_t *wold = wraw + cap;
+    int32_t *wbond = wold + cap;
+    const int64_t row0 = (int64_t)blockIdx.x * kBuildRows;
     const float rlo = g->rv2_lo, rhi = g->rv2_hi;
-    const dbl4 xd = x[i];
-    const d3 xi_ = mk3(xd.x, xd.y, xd.z);
-    const dbl4 hp = hash_pos(x, B, i);
-    const int32_t ai = B.agg ? B.agg[i] : 0;
-    int64_t cx = cell_coord(hp.x, g->lo[0], g->edge, g->dim[0]);
-    int64_t cy = cell_coord(hp.y, g->lo[1], g->edge, g->dim[1]);
-    int64_t cz = cell_coord(hp.z, g->lo[2], g->edge, g->dim[2]);
-    int32_t cnt = 0;
-    bool overflow = false;
-    for (int64_t z = cz - 1; z <= cz + 1; ++z) {
-        if (z < 0 || z >= g->dim[2]) continue;
-        for (int64_t y = cy - 1; y <= cy + 1; ++y) {
-            if (y < 0 || y >= g->dim[1]) continue;
-            for (int64_t xx = cx - 1; xx <= cx + 1; ++xx) {
-                if (xx < 0 || xx >= g->dim[0]) continue;
-                int64_t c = (z * g->dim[1] + y) * g->dim[0] + xx;
-                int32_t b = cstart[c], m = ccount[c];
-                for (int32_t q = 0; q < m; ++q) {
-                    int32_t j = sorted[b + q];
-                    if (j == (int32_t)i) continue;
-                    if (B.agg && B.agg[j] != ai) continue;  // pairs never cross systems of a batch
-                    const float4 fj = x32[j];
-                    const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
-                    const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                    bool in;
-                    if (d2f < rlo)
-                        in = true;
-                    else if (d2f > rhi)
-                        in = false;
-                    else
-                        in = sqn(sub(xi_, ld4(x, j))) < rv2;
-                    if (in) {
-                        if (cnt < cap)
-                            js[(int64_t)cnt * kBuildThreads + tid] = j;
-                        else
-                            overflow = true;
-                        ++cnt;
+    const int64_t dim0 = g->dim[0], dim1 = g->dim[1], dim2 = g->dim[2];
+
+    for (int r = warp; r < kBuildRows; r += kBuildWarps) {
+        const int64_t i = row0 + r;
+        if (i >= n) {
+            if (lane == 0) rlen[r] = 0;
+            continue;
+        }
+        const float4 fi = x32[i];
+        const dbl4 xd = x[i];
+        const d3 xi_ = mk3(xd.x, xd.y, xd.z);
+        const dbl4 hp = hash_pos(x, B, i);
+        const int32_t ai = B.agg ? B.agg[i] : 0;
+        const int64_t cx = cell_coord(hp.x, g->lo[0], g->edge, dim0);
+        const int64_t cy = cell_coord(hp.y, g->lo[1], g->edge, dim1);
+        const int64_t cz = cell_coord(hp.z, g->lo[2], g->edge, dim2);
+        const int64_t x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < dim0 ? cx + 1 : dim0 - 1;
+        int32_t cnt = 0;
+        for (int64_t z = cz - 1; z <= cz + 1; ++z) {
+            if (z < 0 || z >= dim2) continue;
+            for (int64_t y = cy - 1; y <= cy + 1; ++y) {
+                if (y < 0 || y >= dim1) continue;
+                const int64_t c0 = (z * dim1 + y) * dim0 + x0, c1 = (z * dim1 + y) * dim0 + x1;
+                const int32_t b = cstart[c0], e = cstart[c1] + ccount[c1];
+                for (int32_t q0 = b; q0 < e; q0 += 32) {
+                    const int32_t q = q0 + lane;
+                    int32_t j = -1;
+                    bool in = false;
+                    if (q < e) {
+                        j = sorted[q];
+                        if (j != (int32_t)i && (!B.agg || B.agg[j] == ai)) {  // pairs never cross systems
+                            const float4 fj = x32[j];
+                            const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
+                            const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                            if (d2f < rlo)
+                                in = true;
+                            else if (!(d2f > rhi))
+                                in = sqn(sub(xi_, ld4(x, j))) < rv2;
+                        }
                     }
+                    const uint32_t bal = __ballot_sync(0xffffffffu, in);
+                    if (in) {
+                        const int32_t pos = cnt + __popc(bal & lt);
+                        if (pos < cap) wraw[pos] = j;
+                    }
+                    cnt += __popc(bal);
                 }
             }
         }
-    }
-    atomicMax(max_row, cnt);
-    if (overflow) {
-        set_error(err, LG_DEVERR_LIST_OVERFLOW);
-        cnt = (int32_t)cap;
-    }
-    for (int32_t a = 1; a < cnt; ++a) {  // insertion sort (rows hold tens of entries)
-        int32_t key = js[a * kBuildThreads + tid];
-        int32_t b = a - 1;
-        while (b >= 0 && js[b * kBuildThreads + tid] > key) {
-            js[(b + 1) * kBuildThreads + tid] = js[b * kBuildThreads + tid];
-            --b;
+        if (lane == 0) atomicMax(max_row, cnt);
+        if (cnt > cap) {
+            if (lane == 0) set_error(err, LG_DEVERR_LIST_OVERFLOW);
+            cnt = (int32_t)cap;
         }
-        js[(b + 1) * kBuildThreads + tid] = key;
-    }
-    newv.row_len[i] = cnt;
-    // carry springs from the old row (sorted) and mark bonds
-    const int32_t olen = oldv.row_len ? oldv.row_len[i] : 0;
-    const int64_t oxs = oldv.cap * n, nxs = newv.cap * n;
-    int32_t found_bonds = 0;
-    int32_t p = 0;
-    for (int32_t k = 0; k < cnt; ++k) {
-        const int64_t e = (int64_t)k * n + i;
-        const int32_t j = js[k * kBuildThreads + tid];
-        newv.nbr[e] = j;
-        uint32_t fl = 0;
-        while (p < olen && oldv.nbr[(int64_t)p * n + i] < j) ++p;
-        if (p < olen && oldv.nbr[(int64_t)p * n + i] == j) {
-            const int64_t oe = (int64_t)p * n + i;
-            const uint32_t ofl = oldv.flags[oe];
-            if (ofl & kXiLive) {
-                for (int q = 0; q < 9; ++q) newv.xi[q * nxs + e] = oldv.xi[q * oxs + oe];
-                fl |= kXiLive;
-            }
-        }
-        for (int b = 0; b < BV.bcap; ++b) {
+        int32_t olen = oldv.row_len ? oldv.row_len[i] : 0;
+        if (olen > oldv.cap) olen = (int32_t)oldv.cap;  // both buffers share one capacity
+        for (int32_t p = lane; p < olen; p += 32) wold[p] = oldv.nbr[(int64_t)p * n + i];
+        int32_t intact = 0;
+        for (int b = lane; b < bcap; b += 32) {
             const int64_t be = (int64_t)b * n + i;
-            if (BV.j[be] == j && BV.intact[be]) {
-                fl |= kBonded | ((uint32_t)b << 8);
-                ++found_bonds;
-                break;
-            }
+            const int32_t bj = BV.j[be];
+            const bool ok = bj >= 0 && BV.intact[be];
+            wbond[b] = ok ? bj : -1;
+            intact += ok ? 1 : 0;
         }
-        newv.flags[e] = fl;
+        __syncwarp();
+        // rank sort: the partners are distinct, so each one's rank is its slot
+        for (int32_t a = lane; a < cnt; a += 32) {
+            const int32_t v = wraw[a];
+            int32_t rank = 0;
+            for (int32_t t = 0; t < cnt; ++t) rank += wraw[t] < v ? 1 : 0;
+            tj[r * ts + rank] = v;
+        }
+        __syncwarp();
+        int32_t found = 0;
+        for (int32_t k = lane; k < cnt; k += 32) {
+            const int32_t j = tj[r * ts + k];
+            int32_t lo = 0, hi = olen;
+            while (lo < hi) {
+                const int32_t mid = (lo + hi) >> 1;
+                if (wold[mid] < j)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            uint32_t fl = 0;
+            int32_t po = -1;
+            if (lo < olen && wold[lo] == j && (oldv.flags[(int64_t)lo * n + i] & kXiLive)) {
+                fl |= kXiLive;
+                po = lo;
+            }
+            for (int b = 0; b < bcap; ++b)
+                if (wbond[b] == j) {
+                    fl |= kBonded | ((uint32_t)b << 8);
+                    ++found;
+                    break;
+                }
+            tf[r * ts + k] = fl;
+            tp[r * ts + k] = po;
+        }
+        found = __reduce_add_sync(0xffffffffu, found);
+        intact = __reduce_add_sync(0xffffffffu, intact);
+        if (lane == 0) {
+            if (intact != found) set_error(err, LG_DEVERR_BOND_LOST);
+            rlen[r] = cnt;
+        }
+        __syncwarp();
     }
-    int32_t intact = 0;
-    for (int b = 0; b < BV.bcap; ++b)
-        if (BV.j[(int64_t)b * n + i] >= 0 && BV.intact[(int64_t)b * n + i]) ++intact;
-    if (intact != found_bonds) set_error(err, LG_DEVERR_BOND_LOST);
+    __syncthreads();
+
+    // slot-major write-out: lane l owns row row0 + l, warp w writes slots w, w + 8, ...
+    const int64_t il = row0 + lane;
+    const int32_t len = il < n ? rlen[lane] : 0;
+    if (warp == 0 && il < n) newv.row_len[il] = len;
+    const int32_t kmax = (int32_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
+    const int64_t oxs = oldv.cap * n, nxs = newv.cap * n;
+    for (int32_t k = warp; k < kmax; k += kBuildWarps) {
+        if (k >= len) continue;
+        const int64_t e = (int64_t)k * n + il;
+        newv.nbr[e] = tj[lane * ts + k];
+        newv.flags[e] = tf[lane * ts + k];
+        const int32_t po = tp[lane * ts + k];
+        if (po >= 0) {
+            const int64_t oe = (int64_t)po * n + il;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) newv.xi[q * nxs + e] = oldv.xi[q * oxs + oe];
+        }
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -532,16 +588,17 @@ void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, int64_t
     cell_count<<<blocks, threads, 0, st>>>(n, x, B, ls.grid, ls.cell_of, ls.count, ls.x32);
     scan_cells<<<1, 1024, 0, st>>>(ls.grid, ls.count, ls.start);
     cell_scatter<<<blocks, threads, 0, st>>>(n, ls.cell_of, ls.start, ls.fill, ls.sorted);
-    unsigned b2 = (unsigned)((n + kBuildThreads - 1) / kBuildThreads);
-    const size_t smem = sizeof(int32_t) * (size_t)newv.cap * kBuildThreads;
+    const unsigned b2 = (unsigned)((n + kBuildRows - 1) / kBuildRows);
+    const size_t smem = build_smem_bytes(newv.cap, BV.bcap);
     static thread_local int attr_device = -1;
     int dev = 0;
     cudaGetDevice(&dev);
-    if (attr_device != dev) {
-        cudaFuncSetAttribute(build_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(int32_t) * 255 * kBuildThreads));
+    if (attr_device != dev) {  // room for the largest capacities (rows and bonds of up to 255 slots)
+        cudaFuncSetAttribute(build_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)build_smem_bytes(255, 255));
         attr_device = dev;
     }
-    build_rows<<<b2, kBuildThreads, smem, st>>>(n, x, B, ls.x32, ls.grid, ls.start, ls.count, ls.sorted, rv * rv, oldv, newv, BV, err, ls.max_row);
+    build_rows<<<b2, kBuildRows * kBuildWarps, smem, st>>>(n, x, B, ls.x32, ls.grid, ls.start, ls.count, ls.sorted,
+                                                           rv * rv, oldv, newv, BV, err, ls.max_row);
 }
 
 }  // namespace lg
