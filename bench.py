@@ -317,7 +317,7 @@ def e2e_path(s, mat, args, x0, v0):
             s.set(f, host[f].numpy())
         s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
         for f in fields:
-            host[f].numpy()[:] = s.get(f)
+            s.get(f, out=host[f].numpy())
         obs = s.observables()
         t = time.perf_counter() - t
         if k >= args.warmup:

@@ -1,0 +1,90 @@
+// lg_compact.cuh -- pieces shared by the FP64 (lg_forces_compact.cu) and mixed-precision
+// (lg_forces_compact_mixed.cu) warp-compacted force kernels: the slot windows, the slicing of a
+// row's windows over several warps, and the per-particle tail of a force evaluation (unary facet
+// terms, stores, half kick, finiteness check). Everything here is inline device code, so each
+// translation unit compiles it with its own floating-point flags.
+#pragma once
+#include "lg_common.cuh"
+
+namespace lg {
+namespace compact {
+
+constexpr int kWin = 4;           // slots per window (classified per memory round trip)
+constexpr int kHCap = 32 * kWin;  // Hamaker queue capacity per window
+
+// Slicing: the windows of a 32-row group may be split over SL warps (window w of a row goes to
+// warp w % SL); virtual slot v of slice sl (its windows sl, sl + SL, ...) -> slot of the row.
+template <int SL>
+__device__ __forceinline__ int64_t slot_of(int64_t v, int sl) {
+    return ((v / kWin) * SL + sl) * kWin + (v % kWin);
+}
+
+// Facet auto-move: the vertices one step ahead, written once per launch into the second vertex
+// buffer; the engine swaps the two buffers after the step.
+__device__ __forceinline__ void move_facets(const Params &P, const StateView &S, double dt) {
+    for (int f = 0; f < P.n_facets; ++f)
+        for (int q = 0; q < 9; ++q) S.facet_vert_next[9 * f + q] = S.facet_vert[9 * f + q] + P.facets[f].v[q % 3] * dt;
+}
+
+// Tail of particle i's force evaluation: the unary (facet) terms in facet order, added after the
+// binary sums; stores a and alpha, the half-kicked velocities, and flags non-finite results.
+__device__ __forceinline__ void finish_row(const Params &P, const StateView &S, int64_t i, int64_t n, d3 accA, d3 accW,
+                                           d3 vi, d3 wi, double hdt) {
+    if (P.n_facets > 0) {
+        const d3 xi = ld4(S.x, i);
+        d3 ua = zero3(), ual = zero3();
+        for (int f = 0; f < P.n_facets; ++f) {
+            const FacetDev &fd = P.facets[f];
+            d3 N = mk3(fd.normal[0], fd.normal[1], fd.normal[2]);
+            d3 xf = closest_point_on_triangle(S.facet_vert + 9 * f, fd.area, N, xi);
+            d3 vf = mk3(fd.v[0], fd.v[1], fd.v[2]);
+            d3 fa = zero3(), fal = zero3();
+            bool hv = false;
+            if (fd.has_contact) {
+                const int64_t base = (int64_t)f * 9 * n;
+                d3 s[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    s[q] = mk3(S.sxi[base + (3 * q) * n + i], S.sxi[base + (3 * q + 1) * n + i],
+                               S.sxi[base + (3 * q + 2) * n + i]);
+                surface_contact(fd.contact, xf, vf, xi, vi, wi, s, fa, fal);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    S.sxi[base + (3 * q) * n + i] = s[q].x;
+                    S.sxi[base + (3 * q + 1) * n + i] = s[q].y;
+                    S.sxi[base + (3 * q + 2) * n + i] = s[q].z;
+                }
+                hv = true;
+            }
+            if (fd.has_hamaker) {
+                d3 ha = surface_hamaker(fd.hamaker, xf, xi);
+                if (hv) {
+                    fa = add(fa, ha);
+                    fal = add(fal, zero3());
+                } else {
+                    fa = ha;
+                    fal = zero3();
+                }
+            }
+            if (f == 0) {
+                ua = fa;
+                ual = fal;
+            } else {
+                ua = add(ua, fa);
+                ual = add(ual, fal);
+            }
+        }
+        accA = add(accA, ua);
+        accW = add(accW, ual);
+    }
+    st4(S.a, i, accA);
+    st4(S.al, i, accW);
+    st4(S.v_out, i, add(vi, scl(hdt, accA)));
+    st4(S.w_out, i, add(wi, scl(hdt, accW)));
+    if (!isfinite(accA.x) || !isfinite(accA.y) || !isfinite(accA.z) || !isfinite(accW.x) || !isfinite(accW.y) ||
+        !isfinite(accW.z))
+        set_error(S.err, LG_DEVERR_NONFINITE);
+}
+
+}  // namespace compact
+}  // namespace lg

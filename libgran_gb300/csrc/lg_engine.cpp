@@ -252,15 +252,70 @@ static int upload4(dbl4 *dst, const double *aos, int64_t n, cudaStream_t st) {
     return LG_OK;
 }
 
-static int download4(const dbl4 *src, double *aos, int64_t n, cudaStream_t st) {
-    std::vector<dbl4> tmp((size_t)n);
-    LG_CUDA(cudaMemcpyAsync(tmp.data(), src, sizeof(dbl4) * (size_t)n, cudaMemcpyDeviceToHost, st));
-    LG_CUDA(cudaStreamSynchronize(st));
-    for (int64_t i = 0; i < n; ++i) {
-        aos[3 * i] = tmp[i].x;
-        aos[3 * i + 1] = tmp[i].y;
-        aos[3 * i + 2] = tmp[i].z;
+// Origin of one system's float-float positions (mixed precision): the centroid; out[3] receives
+// the largest coordinate offset from it (at least 8 particle radii), which bounds the FP32
+// rounding of the high parts.
+static void origin_of(const double *x, int64_t b, int64_t e, double r_max, double out[4]) {
+    for (int k = 0; k < 3; ++k) {
+        double sum = 0.0;
+        for (int64_t i = b; i < e; ++i) sum += x[3 * i + k];
+        out[k] = e > b ? sum / (double)(e - b) : 0.0;
     }
+    double ext = 8.0 * r_max;
+    for (int64_t i = b; i < e; ++i)
+        for (int k = 0; k < 3; ++k) ext = std::max(ext, std::fabs(x[3 * i + k] - out[k]));
+    out[3] = ext;
+}
+
+// FP32 culling radii of the mixed kernels: the interaction radii with a relative margin of 2e-3
+// (FP32 rounding of the squared distance) plus the rounding of two high parts (each within
+// 2^-24 of the offset, taken with a fourfold allowance for the system spreading out).
+static void set_cull_radii(lg_system *s) {
+    const double m = 2.0 * 4.0 * s->ext_max * 5.9604644775390625e-8;
+    auto sq = [&](double r) { return (float)((r * 1.002 + m) * (r * 1.002 + m)); };
+    s->mx.near2 = sq(s->cull_near);
+    s->mx.contact2f = sq(s->cull_contact);
+}
+
+static int set_mixed_origins(lg_system *s, const double *x) {
+    origin_of(x, 0, s->P.n, s->r_max, s->origin);
+    s->ext_max = s->origin[3];
+    if (s->n_systems > 0) {
+        std::vector<dbl4> org((size_t)s->n_systems);
+        s->ext_max = 0.0;
+        for (int64_t q = 0; q < s->n_systems; ++q) {
+            double o[4];
+            origin_of(x, s->sys_off[q], s->sys_off[q + 1], s->r_max, o);
+            org[q] = make_double4_32a(o[0], o[1], o[2], o[3]);
+            s->ext_max = std::max(s->ext_max, o[3]);
+        }
+        LG_CUDA(cudaMemcpyAsync(s->d_orig, org.data(), sizeof(dbl4) * org.size(), cudaMemcpyHostToDevice, s->stream));
+        LG_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    return LG_OK;
+}
+
+// lg_get / lg_set: the caller's [n][3] array moves in one copy to device scratch (the observables
+// scratch, n * 20 doubles, ordered with every other use on the handle's stream) and a kernel converts
+// it to or from the padded device layout, so no host-side staging or conversion loop is involved and
+// a pinned caller buffer is copied by DMA directly.
+static int upload_staged(lg_system *s, dbl4 *dst, const double *aos) {
+    const int64_t n = s->P.n;
+    LG_CUDA(cudaMemcpyAsync(s->obs_scratch, aos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    launch_aos_to_dev4(n, s->obs_scratch, dst, s->stream);
+    s->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaStreamSynchronize(s->stream));  // the caller may reuse its buffer on return
+    return LG_OK;
+}
+
+static int download_staged(lg_system *s, const dbl4 *src, double *aos) {
+    const int64_t n = s->P.n;
+    launch_dev4_to_aos(n, src, s->obs_scratch, s->stream);
+    s->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaMemcpyAsync(aos, s->obs_scratch, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
     return LG_OK;
 }
 
@@ -702,27 +757,10 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     LG_TRY(s->alloc(&s->obs_out, 32));
 
     if (s->precision == LG_PRECISION_MIXED) {
-        for (int c = 0; c < 3; ++c) {
-            double sum = 0.0;
-            for (int64_t i = 0; i < n; ++i) sum += x0[3 * i + c];
-            s->origin[c] = sum / (double)n;
-        }
         LG_TRY(s->alloc(&s->x32, 2 * (size_t)n));  // float-float: high parts, then low parts
-        if (s->n_systems > 0) {
-            std::vector<dbl4> org((size_t)s->n_systems);
-            for (int64_t q = 0; q < s->n_systems; ++q) {
-                double c[3];
-                const int64_t b = s->sys_off[q], e = s->sys_off[q + 1];
-                for (int k = 0; k < 3; ++k) {
-                    double sum = 0.0;
-                    for (int64_t i = b; i < e; ++i) sum += x0[3 * i + k];
-                    c[k] = e > b ? sum / (double)(e - b) : 0.0;
-                }
-                org[q] = make_double4_32a(c[0], c[1], c[2], 0.0);
-            }
-            LG_TRY(s->alloc(&s->d_orig, (size_t)s->n_systems));
-            LG_CUDA(cudaMemcpy(s->d_orig, org.data(), sizeof(dbl4) * org.size(), cudaMemcpyHostToDevice));
-        }
+        if (s->n_systems > 0) LG_TRY(s->alloc(&s->d_orig, (size_t)s->n_systems));
+        s->r_max = std::max(d->contact.r_part, std::max(d->sinter.r_part, d->hamaker.r_part));
+        LG_TRY(set_mixed_origins(s, x0));
         launch_positions_to_f32(n, s->x, s->origin, s->d_agg, s->d_orig, s->x32, s->stream);
         double near = 0.0;
         if (d->binary_model != LG_BINARY_NONE) near = std::max(near, 2.0 * d->contact.r_part);
@@ -732,11 +770,12 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
             near = std::max(near, 7.0 * d->hamaker.r_part);
         s->mx.x32 = s->x32;
         s->mx.x32lo = s->x32 + n;
-        s->mx.near2 = (float)(near * near * 1.004);
         double cnear = 0.0;
         if (d->binary_model != LG_BINARY_NONE) cnear = std::max(cnear, 2.0 * d->contact.r_part);
         if (sinter) cnear = std::max(cnear, 2.0 * d->sinter.r_part);
-        s->mx.contact2f = (float)(cnear * cnear * 1.004);
+        s->cull_near = near;
+        s->cull_contact = cnear;
+        set_cull_radii(s);
         s->mx.inv_mass_h = d->hamaker.mass > 0 ? (float)(1.0 / d->hamaker.mass) : 0.f;
         s->mx.inv_mass_c = d->contact.mass > 0 ? 1.0 / d->contact.mass : 0.0;
         s->mx.inv_inertia_c = d->contact.inertia > 0 ? 1.0 / d->contact.inertia : 0.0;
@@ -918,15 +957,18 @@ extern "C" int lg_get(lg_system *s, int field, double *out) {
     LG_HANDLE(s);
     dbl4 *p = field_ptr(s, field);
     if (!p || !out) return lg_fail(LG_E_INVALID, "lg_get: bad field %d or null output", field);
-    return download4(p, out, s->P.n, s->stream);
+    return download_staged(s, p, out);
 }
 
 extern "C" int lg_set(lg_system *s, int field, const double *in) {
     LG_HANDLE(s);
     dbl4 *p = field_ptr(s, field);
     if (!p || !in) return lg_fail(LG_E_INVALID, "lg_set: bad field %d or null input", field);
-    LG_TRY(upload4(p, in, s->P.n, s->stream));
+    LG_TRY(upload_staged(s, p, in));
     if (field == LG_FIELD_X && s->x32) {
+        LG_TRY(set_mixed_origins(s, in));  // new positions: new origins and culling radii
+        set_cull_radii(s);
+        s->drop_graphs();  // captured launches hold the old values
         launch_positions_to_f32(s->P.n, s->x, s->origin, s->d_agg, s->d_orig, s->x32, s->stream);
         s->launches += 1;
         LG_CUDA(cudaGetLastError());

@@ -41,7 +41,10 @@ struct lg_system {
 
     // mixed precision: FP32 position copy for culling
     float4 *x32 = nullptr;
-    double origin[3] = {0.0, 0.0, 0.0};
+    double origin[4] = {0.0, 0.0, 0.0, 0.0};  // mixed: origin of the float-float positions, extent in [3]
+    double r_max = 0.0;                        // mixed: largest particle radius of the functors
+    double ext_max = 0.0;                      // mixed: largest extent of a system about its origin
+    double cull_near = 0.0, cull_contact = 0.0;  // mixed: culling radii before margins
     lg::MixedExtra mx{};
 
     // force-kernel timing (bench instrumentation)
@@ -55,7 +58,7 @@ struct lg_system {
     int64_t *d_sys_off = nullptr;        // device copy
     int32_t *d_agg = nullptr;            // [n] system of every particle
     lg::dbl4 *d_hoff = nullptr;          // [n_systems] hashing offsets
-    lg::dbl4 *d_orig = nullptr;          // [n_systems] FP32-copy origins (mixed precision)
+    lg::dbl4 *d_orig = nullptr;          // [n_systems] float-float origins (x, y, z; w: extent), mixed
     double *d_centres = nullptr;         // [3 n_systems] scratch for per-system observables
     double *d_sys_obs = nullptr;         // [20 n_systems]
     std::vector<int64_t> n_bonds_initial_sys;

@@ -1,0 +1,566 @@
+// lg_forces_compact_mixed.cu -- warp-compacted force kernel, mixed precision (sm_103a).
+//
+// Same row/slot layout and division of work as the FP64 compacted kernel (lg_forces_compact.cu):
+// one lane per row, slots taken in windows of four, contact/bond pairs queued per warp and
+// evaluated 32 at a time. What the precision changes:
+//  * positions come as float-float pairs (MixedExtra::x32 / x32lo, hi + lo = x - origin); a pair's
+//    separation and q = |d|^2 - (2r)^2 are formed with error-free FP32 transformations
+//    (separation_ff), so a Hamaker pair costs no FP64 operation at all and its surface gap keeps
+//    FP32 relative precision however small it is;
+//  * the owner lane gathers both halves of its partners' positions while it classifies a window,
+//    and the window's Hamaker pairs are evaluated right away, one pair per lane, from those
+//    shared-memory copies: one global round trip per window for the partners' data;
+//  * the next window's partner indices and flags are loaded while the current one is evaluated;
+//  * per-row sums are float-float FP32 accumulations (compensated, about 2^-44 relative): one for
+//    the Hamaker pairs, to which each window adds its (up to four) terms summed in FP32 in slot
+//    order as the window completes, and one each for the linear
+//    and angular accelerations of the contact/bond pairs, folded in slot order at the end of each
+//    round; the sums become FP64 once per row. Each sum's order depends only on the row itself, not
+//    on which rows share its warp, so a system gives the same bits alone and inside a batch;
+//  * contact and bond pairs keep their FP64 spring vectors, updated by FP32 increments (shear_mx).
+// For launches with few rows the windows of a row are sliced over SL warps (slot_of), each slice
+// keeping its own partial sums, which are combined in slice order at the end.
+#include <cstddef>
+
+#include "lg_compact.cuh"
+#include "lg_kernels.h"
+
+// Slices per row group: 0 chooses from the launch size (compile-time override for tuning).
+#ifndef LG_MIXED_SLICES
+#define LG_MIXED_SLICES 0
+#endif
+
+namespace lg {
+
+namespace {
+
+using compact::kHCap;
+using compact::kWin;
+using compact::slot_of;
+
+constexpr int kRound = 64;  // virtual slots classified per round (per warp)
+constexpr int kCCap = 160;  // contact queue capacity per round (>= 32 * kWin + 31)
+
+template <int SL>
+struct ShapeM {
+    static constexpr int kSlices = SL;
+    static constexpr int kRowWarps = SL == 1 ? 2 : 1;  // 32-row groups per block
+    static constexpr int kWarps = kSlices * kRowWarps;
+    // blocks per SM that the 128-register budget allows (shared memory allows as many)
+    static constexpr int kMinBlocks = 65536 / (kWarps * 32 * 128);
+};
+
+struct WarpSmemM {
+    float4 hhi[kHCap];     // queued Hamaker partners: high part of the position, w = owner lane
+    float4 hlo[kHCap];     // low part of the position
+    float hres[kHCap][3];  // their accelerations
+    float cres[kCCap][6];  // contact/bond results: linear and angular acceleration
+    int32_t cj[kCCap];
+    uint16_t cown[kCCap];  // (owner lane << 8) | virtual slot offset within the round
+    uint32_t cball[kRound];
+    int32_t cbase[kRound];
+    float4 xh[32], xl[32];  // the rows' own positions (float-float)
+    d3 vo[32], wo[32];      // the rows' own velocities and spins (FP64)
+};
+static_assert(offsetof(WarpSmemM, hlo) == sizeof(WarpSmemM::hhi) &&
+                  sizeof(WarpSmemM::hhi) + sizeof(WarpSmemM::hlo) >= 18 * 32 * sizeof(float),
+              "slice partial sums reuse the Hamaker queue (hhi, hlo)");
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 fm(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 fadd(f3 a, f3 b) { return fm(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 fsub(f3 a, f3 b) { return fm(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 fscl(float s, f3 a) { return fm(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float fdot(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+__device__ __forceinline__ f3 fcrs(f3 a, f3 b) {
+    return fm(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ f3 tof(d3 a) { return fm((float)a.x, (float)a.y, (float)a.z); }
+
+// Shear spring (contact_force.h:105-147, Coulomb-capped; alt_sinter_bridge.h:137-156, bond form)
+// with the spring vector held in FP64. Each evaluation computes, in FP32, the increment of the
+// spring: the rotation onto the tangent plane, -(xi.n) n, the rescale to the old magnitude,
+// (s - 1)(xi - (xi.n) n) with s - 1 evaluated as a series for small tilts, and the stretch rel*dt;
+// the increment is small next to xi and is added to the FP64 spring, so rounding does not
+// accumulate at the spring's own scale. The dynamic (sliding) branch sets the spring outright.
+__device__ __forceinline__ f3 shear_mx(d3 &xi, f3 n, float stiffness, float damping, float normal_force, float mu_s,
+                                       float phi, f3 rel, float dtf, bool coulomb) {
+    f3 xf = tof(xi);
+    f3 drot = fm(0.f, 0.f, 0.f);
+    float xx = fdot(xf, xf);
+    if (xx > 0.0f) {
+        float c = fdot(xf, n);
+        f3 xr = fsub(xf, fscl(c, n));
+        float e = (c * c) / xx;
+        float sm1 = 0.0f;
+        if (e < 1.0f) sm1 = e < 1e-3f ? e * (0.5f + 0.375f * e) : rsqrtf(1.0f - e) - 1.0f;
+        drot = fadd(fscl(-c, n), fscl(sm1, xr));
+    }
+    const f3 xn = fadd(xf, drot);
+    const f3 f0 = fsub(fscl(-stiffness, xn), fscl(damping, rel));
+    if (!coulomb) {
+        const f3 dxi = fadd(drot, fscl(dtf, rel));
+        xi.x += (double)dxi.x;
+        xi.y += (double)dxi.y;
+        xi.z += (double)dxi.z;
+        return f0;
+    }
+    const float fs = mu_s * normal_force;
+    const float fd = mu_s * phi * normal_force;
+    const float f0n = sqrtf(fdot(f0, f0));
+    const f3 t = f0n > 0.0f ? fscl(1.0f / f0n, f0) : fm(0.f, 0.f, 0.f);
+    float sel;
+    if (f0n <= fs) {
+        const f3 dxi = fadd(drot, fscl(dtf, rel));
+        xi.x += (double)dxi.x;
+        xi.y += (double)dxi.y;
+        xi.z += (double)dxi.z;
+        sel = fs;
+    } else {
+        const f3 nx = fscl(-1.0f / stiffness, fadd(fscl(fd, t), fscl(damping, rel)));
+        xi = mk3((double)nx.x, (double)nx.y, (double)nx.z);
+        sel = fd;
+    }
+    return fscl(fminf(sel, f0n), t);
+}
+
+// Hamaker factor of hamaker_force.h:36-40 with two reciprocals:
+// s = -A/6 [ (4r+2h) u - 2 w - 4 r^2 w^3 - 2 r^2 (4r+2h) u^2 ], u = 1/((4r+h) h), w = 1/(2r+h).
+__device__ __forceinline__ float ham_factor(int mode, float A, float r, float h) {
+    if (mode == LG_HAMAKER_SIMPLIFIED) return 2.0f * A * r * __frcp_rn(h * h);
+    float u = __frcp_rn((4.0f * r + h) * h);
+    float w = __frcp_rn(2.0f * r + h);
+    float a = 4.0f * r + 2.0f * h;
+    float br = a * u - 2.0f * w - 4.0f * r * r * (w * w * w) - 2.0f * r * r * a * (u * u);
+    return -A / 6.0f * br;
+}
+
+// Float-float arithmetic (a value is hi + lo with |lo| <= ulp(hi) / 2). The _rn intrinsics keep the
+// compiler from contracting or reordering the error-free steps.
+struct ff {
+    float hi, lo;
+};
+// TwoSum (Knuth): s + e == a + b exactly, whatever the magnitudes of a and b.
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+// Compensated accumulation a += b: the rounding error of every addition is kept in a.lo.
+__device__ __forceinline__ void ff_acc(ff &a, float b) {
+    const ff s = two_sum(a.hi, b);
+    a.hi = s.hi;
+    a.lo = __fadd_rn(a.lo, s.lo);
+}
+__device__ __forceinline__ double ff_to_d(ff a) { return (double)a.hi + (double)a.lo; }
+
+// Separation d = x_i - x_j (FP32) and q = |d|^2 - (2r)^2 from float-float positions. Per component
+// the high parts' difference is split exactly (TwoSum) and its error joins the low parts'
+// difference, so dh + dl equals the separation to about 2^-48 of the coordinates. Then
+// (dh + dl)^2 = dh^2 + dl (2 dh + dl) with dh^2 split exactly by FMA, the three large squares added
+// with TwoSum, and -(2r)^2 (fr_hi + fr_lo) subtracted: that subtraction is exact (Sterbenz) whenever
+// |d| is within a factor sqrt(2) of 2r, and otherwise |q| >= 2 r^2, so q keeps FP32 relative
+// precision however small the surface gap or the overlap is.
+struct SepFF {
+    f3 d;
+    float q;
+};
+__device__ __forceinline__ SepFF separation_ff(float4 hi, float4 lo, float4 hj, float4 lj, float fr_hi, float fr_lo) {
+    const ff tx = two_sum(hi.x, -hj.x), ty = two_sum(hi.y, -hj.y), tz = two_sum(hi.z, -hj.z);
+    const float lx = __fadd_rn(tx.lo, __fsub_rn(lo.x, lj.x));
+    const float ly = __fadd_rn(ty.lo, __fsub_rn(lo.y, lj.y));
+    const float lz = __fadd_rn(tz.lo, __fsub_rn(lo.z, lj.z));
+    const float px = __fmul_rn(tx.hi, tx.hi), py = __fmul_rn(ty.hi, ty.hi), pz = __fmul_rn(tz.hi, tz.hi);
+    const float ex = __fmaf_rn(tx.hi, tx.hi, -px), ey = __fmaf_rn(ty.hi, ty.hi, -py), ez = __fmaf_rn(tz.hi, tz.hi, -pz);
+    const float cx = lx * (2.0f * tx.hi + lx), cy = ly * (2.0f * ty.hi + ly), cz = lz * (2.0f * tz.hi + lz);
+    const ff s1 = two_sum(px, py);
+    const ff s2 = two_sum(s1.hi, pz);
+    const float s3 = __fsub_rn(s2.hi, fr_hi);
+    const float rest = (s1.lo + s2.lo) + ((ex + ey) + ez) + ((cx + cy) + cz) - fr_lo;
+    return SepFF{fm(tx.hi + lx, ty.hi + ly, tz.hi + lz), s3 + rest};
+}
+
+// One queued contact / bond pair: owner row io (lane own of the warp), slot e, partner j. Writes the
+// pair's linear and angular accelerations (force over mass, torque over moment of inertia).
+template <int SL>
+__device__ __forceinline__ void contact_item(const Params &P, const StateView &S, const PairView &PV,
+                                             const BondView &BV, const MixedExtra &M, WarpSmemM &W, int q,
+                                             int64_t row0, int64_t kstart, int sl, int64_t n, int64_t xs, int64_t bs) {
+    const int own = W.cown[q] >> 8;
+    const int64_t io = row0 + own;
+    const int64_t e = slot_of<SL>(kstart + (W.cown[q] & 0xff), sl) * n + io;
+    const int32_t j = W.cj[q];
+    const uint32_t fl = PV.flags[e];
+    const bool bonded = (fl & kBonded) != 0;
+    const d3 vo = W.vo[own], wo = W.wo[own];
+    const SepFF sp = separation_ff(W.xh[own], W.xl[own], M.x32[j], M.x32lo[j], bonded ? M.b_fr_hi : M.c_fr_hi,
+                                   bonded ? M.b_fr_lo : M.c_fr_lo);
+    const f3 dxf = sp.d;
+    const float d2f = fdot(dxf, dxf);
+    const float rr = bonded ? M.b_r : M.c_r;
+    const float rsd = rsqrtf(d2f);
+    const float overlap = -sp.q / (d2f * rsd + 2.0f * rr);  // 2r - |d|, from |d|^2 - (2r)^2
+    f3 force = fm(0.f, 0.f, 0.f), torque = fm(0.f, 0.f, 0.f);
+    if (bonded || overlap > 0.0f) {
+        const f3 n3 = fscl(rsd, dxf);
+        const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+        const f3 vij0 = tof(sub(vo, vj));
+        const f3 wfi = tof(wo), wfj = tof(wj);
+        int64_t base, stride;
+        double *store;
+        if (bonded) {
+            base = (int64_t)bond_slot_of(fl) * n + io;
+            stride = bs;
+            store = BV.xi;
+        } else {
+            base = e;
+            stride = xs;
+            store = PV.xi;
+        }
+        d3 s[3] = {zero3(), zero3(), zero3()};  // springs of a slot that is not live are zero
+        if (bonded || (fl & kXiLive))
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                s[c] = mk3(store[(3 * c) * stride + base], store[(3 * c + 1) * stride + base],
+                           store[(3 * c + 2) * stride + base]);
+        const float kn = bonded ? M.b_k : M.c_k, gn = bonded ? M.b_gn : M.c_gn;
+        const float rp = rr - 0.5f * overlap;
+        const float v_n = -fdot(vij0, n3);
+        const float f_n = kn * overlap + gn * v_n;
+        const f3 nwi = fcrs(n3, wfi), nwj = fcrs(n3, wfj);
+        const f3 v_ij = fadd(vij0, fscl(rp, fadd(nwi, nwj)));
+        const f3 v_t = fsub(v_ij, fscl(fdot(v_ij, n3), n3));
+        const f3 v_r = fscl(-rp, fsub(nwi, nwj));
+        const f3 v_o = fscl(rr * (fdot(n3, wfi) - fdot(n3, wfj)), n3);
+        f3 f_t, f_r, f_o;
+        if (bonded) {
+            f_t = shear_mx(s[0], n3, M.b_kt, M.b_gt, f_n, 0.f, 0.f, v_t, M.b_dt, false);
+            f_r = shear_mx(s[1], n3, M.b_kr, M.b_gr, f_n, 0.f, 0.f, v_r, M.b_dt, false);
+            f_o = shear_mx(s[2], n3, M.b_ko, M.b_go, f_n, 0.f, 0.f, v_o, M.b_dt, false);
+        } else {
+            f_t = shear_mx(s[0], n3, M.c_kt, M.c_gt, f_n, M.c_mus, M.c_phid, v_t, M.c_dt, true);
+            f_r = shear_mx(s[1], n3, M.c_kr, M.c_gr, f_n, M.c_mur, M.c_phir, v_r, M.c_dt, true);
+            f_o = shear_mx(s[2], n3, M.c_ko, M.c_go, f_n, M.c_muo, M.c_phio, v_o, M.c_dt, true);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            store[(3 * c) * stride + base] = s[c].x;
+            store[(3 * c + 1) * stride + base] = s[c].y;
+            store[(3 * c + 2) * stride + base] = s[c].z;
+        }
+        force = fadd(fscl(f_n, n3), f_t);
+        torque = fadd(fsub(fscl(rr, fcrs(n3, f_r)), fscl(rp, fcrs(n3, f_t))), fscl(rr, f_o));
+        if (bonded) {
+            if (P.binary_model == LG_BINARY_BREAKING_SINTER) {
+                const double st = BV.strength[base];
+                if ((double)fdot(force, force) > st * st) {
+                    BV.intact[base] = 0;
+                    PV.flags[e] = fl & ~(kBonded | (0xffu << 8));
+                }
+            }
+        } else if (!(fl & kXiLive)) {
+            PV.flags[e] = fl | kXiLive;
+        }
+    } else if (fl & kXiLive) {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+        PV.flags[e] = fl & ~kXiLive;
+    }
+    W.cres[q][0] = force.x * M.bin_im;
+    W.cres[q][1] = force.y * M.bin_im;
+    W.cres[q][2] = force.z * M.bin_im;
+    W.cres[q][3] = torque.x * M.bin_iI;
+    W.cres[q][4] = torque.y * M.bin_iI;
+    W.cres[q][5] = torque.z * M.bin_iI;
+}
+
+// One queued Hamaker pair (hamaker_force.h:28-44; limited form hamaker_force.h:86-93): partner
+// position from the queue, owner position from the warp's row data.
+__device__ __forceinline__ void hamaker_item(const Params &P, const MixedExtra &M, WarpSmemM &W, int q) {
+    const float4 ph = W.hhi[q];
+    const int own = __float_as_int(ph.w);
+    const SepFF sp = separation_ff(W.xh[own], W.xl[own], ph, W.hlo[q], M.h_fr_hi, M.h_fr_lo);
+    f3 a = fm(0.f, 0.f, 0.f);
+    if (!(P.hamaker_model == LG_HAMAKER_LIMITED && sp.q > M.h_qcut)) {
+        const f3 dxf = sp.d;
+        const float d2f = fdot(dxf, dxf);
+        const float rsd = rsqrtf(d2f);
+        float h = sp.q * __frcp_rn(d2f * rsd + 2.0f * M.h_r);  // |d| - 2r to FP32 precision
+        h = fmaxf(h, M.h_h0);
+        const float sfac = ham_factor(P.hamaker_model, M.h_A, M.h_r, h) * M.inv_mass_h * rsd;
+        a = fscl(-sfac, dxf);  // along x_j - x_i
+    }
+    W.hres[q][0] = a.x;
+    W.hres[q][1] = a.y;
+    W.hres[q][2] = a.z;
+}
+
+}  // namespace
+
+template <bool VERLET, int SL>
+__global__ void __launch_bounds__(ShapeM<SL>::kWarps * 32, ShapeM<SL>::kMinBlocks)
+    forces_compact_mixed(Params P, StateView S, PairView PV, BondView BV, double hdt, double dt, int move_facets,
+                         MixedExtra MX) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int kSlices = ShapeM<SL>::kSlices, kRowWarps = ShapeM<SL>::kRowWarps;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpSmemM *Wall = reinterpret_cast<WarpSmemM *>(smem_raw);
+    WarpSmemM &W = Wall[warp];
+    const int rw = warp / kSlices, sl = warp % kSlices;  // row group of the block, slice of it
+    const int64_t n = P.n;
+    const int64_t row0 = ((int64_t)blockIdx.x * kRowWarps + rw) * 32;
+    const int64_t i = row0 + lane;
+    const bool active = i < n;
+    const int hm = P.hamaker_model;
+    const bool contacts_on = P.binary_model != LG_BINARY_NONE;
+    const uint32_t lt = (1u << lane) - 1u;
+
+    if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
+
+    int64_t len = 0;
+    float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f);
+    {
+        float4 lo_i = hi_i;
+        d3 vi = zero3(), wi = zero3();
+        if (active) {
+            len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
+            hi_i = MX.x32[i];
+            lo_i = MX.x32lo[i];
+            vi = ld4(S.v, i);
+            wi = ld4(S.w, i);
+        }
+        W.xh[lane] = hi_i;
+        W.xl[lane] = lo_i;
+        W.vo[lane] = vi;
+        W.wo[lane] = wi;
+    }
+    const int64_t maxlen = (int64_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
+    // this warp's windows: sl, sl + kSlices, ...; virtual slot v maps to slot_of<SL>(v, sl)
+    const int64_t nwin = (maxlen + kWin - 1) / kWin;
+    const int64_t mywin = nwin > sl ? (nwin - sl + kSlices - 1) / kSlices : 0;
+    const int64_t vmax = mywin * kWin;
+    const int64_t xs = PV.cap * n;
+    const int64_t bs = (int64_t)BV.bcap * n;
+    ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accw[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    ff acch[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    __syncwarp();
+
+    // partner and flags of the lane's row in the window at virtual slot v (-1: past the row's end)
+    int32_t jn[kWin];
+    uint32_t fn[kWin];
+    auto load_window = [&](int64_t v) {
+        const int64_t k0 = slot_of<SL>(v, sl);
+#pragma unroll
+        for (int u = 0; u < kWin; ++u) {
+            const int64_t kk = k0 + u;
+            jn[u] = -1;
+            fn[u] = 0;
+            if (kk < len) {
+                const int64_t e = kk * n + i;
+                jn[u] = VERLET ? PV.nbr[e] : (int32_t)(kk < i ? kk : kk + 1);
+                fn[u] = PV.flags[e];
+            }
+        }
+    };
+    if (vmax > 0) load_window(0);
+
+    for (int64_t kstart = 0; kstart < vmax;) {
+        int ccount = 0, cdone = 0;
+        int64_t k = kstart;
+        for (; k < vmax && k - kstart + kWin <= kRound && ccount + 32 * kWin <= kCCap; k += kWin) {
+            int32_t jg[kWin];
+            uint32_t fg[kWin];
+            float4 ph[kWin], pl[kWin];
+#pragma unroll
+            for (int u = 0; u < kWin; ++u) {
+                jg[u] = jn[u];
+                fg[u] = fn[u];
+            }
+#pragma unroll
+            for (int u = 0; u < kWin; ++u) {
+                ph[u] = hi_i;
+                pl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (jg[u] >= 0) {
+                    ph[u] = MX.x32[jg[u]];
+                    pl[u] = MX.x32lo[jg[u]];
+                }
+            }
+            if (k + kWin < vmax) load_window(k + kWin);  // next window, in flight during this one
+            const int64_t k0 = slot_of<SL>(k, sl);
+            int hcount = 0;
+            uint32_t hbal[kWin];
+            int hbas[kWin];
+#pragma unroll
+            for (int u = 0; u < kWin; ++u) {
+                const int off = (int)(k - kstart) + u;  // virtual slot offset within the round
+                bool hb = false, cb = false;
+                if (jg[u] >= 0) {
+                    const uint32_t fl = fg[u];
+                    const float dxf = hi_i.x - ph[u].x, dyf = hi_i.y - ph[u].y, dzf = hi_i.z - ph[u].z;
+                    const float d2f = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
+                    if (hm == LG_HAMAKER_LIMITED)
+                        hb = d2f <= MX.near2;
+                    else if (hm != LG_HAMAKER_NONE)
+                        hb = true;
+                    if (contacts_on) {
+                        if ((fl & kBonded) || d2f <= MX.contact2f) {
+                            cb = true;
+                        } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+                            const int64_t e = (k0 + u) * n + i;
+#pragma unroll
+                            for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+                            PV.flags[e] = fl & ~kXiLive;
+                        }
+                    }
+                }
+                const uint32_t bc = __ballot_sync(0xffffffffu, cb);
+                const uint32_t bh = __ballot_sync(0xffffffffu, hb);
+                if (cb) {
+                    const int q = ccount + __popc(bc & lt);
+                    W.cj[q] = jg[u];
+                    W.cown[q] = (uint16_t)((lane << 8) | off);
+                }
+                if (hb) {
+                    const int q = hcount + __popc(bh & lt);
+                    W.hhi[q] = make_float4(ph[u].x, ph[u].y, ph[u].z, __int_as_float(lane));
+                    W.hlo[q] = pl[u];
+                }
+                if (lane == 0) {
+                    W.cball[off] = bc;
+                    W.cbase[off] = ccount;
+                }
+                hbal[u] = bh;
+                hbas[u] = hcount;
+                ccount += __popc(bc);
+                hcount += __popc(bh);
+            }
+            __syncwarp();
+            for (int q = lane; q < hcount; q += 32) hamaker_item(P, MX, W, q);
+            __syncwarp();
+            {  // the window's (at most four) Hamaker terms in slot order, then one compensated add
+                float wsum[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int u = 0; u < kWin; ++u)
+                    if ((hbal[u] >> lane) & 1u) {
+                        const int q = hbas[u] + __popc(hbal[u] & lt);
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) wsum[c] += W.hres[q][c];
+                    }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) ff_acc(acch[c], wsum[c]);
+            }
+            while (ccount - cdone >= 32) {
+                contact_item<SL>(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, sl, n, xs, bs);
+                cdone += 32;
+                __syncwarp();
+            }
+            __syncwarp();  // the next window reuses the Hamaker queue
+        }
+        const int64_t kend = k;
+        if (cdone + lane < ccount) contact_item<SL>(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, sl, n, xs, bs);
+        __syncwarp();
+        // the round's contact and bond pairs, in slot order
+        for (int off = 0; off < (int)(kend - kstart); ++off) {
+            const uint32_t bc = W.cball[off];
+            if ((bc >> lane) & 1u) {
+                const int q = W.cbase[off] + __popc(bc & lt);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    ff_acc(acc[c], W.cres[q][c]);
+                    ff_acc(accw[c], W.cres[q][3 + c]);
+                }
+            }
+        }
+        __syncwarp();
+        kstart = kend;
+    }
+
+    if (kSlices > 1) {
+        // combine the slices' partial sums of each row in slice order (fixed, deterministic); each
+        // warp parks its partials in its own Hamaker queue (hhi, hlo), which is no longer in use
+        float *mine = reinterpret_cast<float *>(W.hhi);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            mine[(2 * c) * 32 + lane] = acc[c].hi;
+            mine[(2 * c + 1) * 32 + lane] = acc[c].lo;
+            mine[(6 + 2 * c) * 32 + lane] = accw[c].hi;
+            mine[(7 + 2 * c) * 32 + lane] = accw[c].lo;
+            mine[(12 + 2 * c) * 32 + lane] = acch[c].hi;
+            mine[(13 + 2 * c) * 32 + lane] = acch[c].lo;
+        }
+        __syncthreads();
+        if (sl != 0) return;
+        for (int q = 1; q < kSlices; ++q) {
+            const float *o = reinterpret_cast<const float *>(Wall[rw * kSlices + q].hhi);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                ff_acc(acc[c], o[(2 * c) * 32 + lane]);
+                ff_acc(acc[c], o[(2 * c + 1) * 32 + lane]);
+                ff_acc(accw[c], o[(6 + 2 * c) * 32 + lane]);
+                ff_acc(accw[c], o[(7 + 2 * c) * 32 + lane]);
+                ff_acc(acch[c], o[(12 + 2 * c) * 32 + lane]);
+                ff_acc(acch[c], o[(13 + 2 * c) * 32 + lane]);
+            }
+        }
+    }
+    if (!active) return;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {  // contact/bond sum + Hamaker sum
+        ff_acc(acc[c], acch[c].hi);
+        ff_acc(acc[c], acch[c].lo);
+    }
+    const d3 a_tot = mk3(ff_to_d(acc[0]), ff_to_d(acc[1]), ff_to_d(acc[2]));
+    const d3 al_tot = mk3(ff_to_d(accw[0]), ff_to_d(accw[1]), ff_to_d(accw[2]));
+    compact::finish_row(P, S, i, n, a_tot, al_tot, W.vo[lane], W.wo[lane], hdt);
+}
+
+template <bool VERLET, int SL>
+static void launch_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
+                                 double hdt, double dt, int move_facets, const MixedExtra &MX, cudaStream_t st) {
+    using Sh = ShapeM<SL>;
+    const size_t smem = sizeof(WarpSmemM) * Sh::kWarps;
+    const int64_t rows_per_block = Sh::kRowWarps * 32;
+    const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
+    static thread_local int attr_device = -1;  // the attribute is per device; set once per thread and device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto kern = forces_compact_mixed<VERLET, SL>;
+    if (attr_device != dev) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_device = dev;
+    }
+    kern<<<blocks, Sh::kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets, MX);
+}
+
+// Slices per 32-row group: the most slices that keep the launch within about two waves of
+// resident warps (152 SMs x 16); rows of long launches are not sliced.
+static int mixed_slices(int64_t n) {
+    if (LG_MIXED_SLICES == 1 || LG_MIXED_SLICES == 2 || LG_MIXED_SLICES == 4) return LG_MIXED_SLICES;
+    const int64_t two_waves = 2 * 152 * 16;
+    const int64_t groups = (n + 31) / 32;
+    if (groups * 4 <= two_waves) return 4;
+    if (groups * 2 <= two_waves) return 2;
+    return 1;
+}
+
+void launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                                 double dt, int move_facets, const MixedExtra &MX, cudaStream_t st) {
+    const bool ver = P.pairs == LG_PAIRS_VERLET;
+    switch (mixed_slices(P.n)) {
+        case 4:
+            if (ver) launch_compact_mixed<true, 4>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
+            else launch_compact_mixed<false, 4>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
+            break;
+        case 2:
+            if (ver) launch_compact_mixed<true, 2>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
+            else launch_compact_mixed<false, 2>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
+            break;
+        default:
+            if (ver) launch_compact_mixed<true, 1>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
+            else launch_compact_mixed<false, 1>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
+    }
+}
+
+}  // namespace lg

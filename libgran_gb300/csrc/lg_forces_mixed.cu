@@ -356,8 +356,9 @@ __global__ void positions_to_f32(int64_t n, const dbl4 *__restrict__ x, double o
 // Kick + drift of the mixed path: FP64 integration, then the float-float position copy.
 __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restrict__ v, dbl4 *__restrict__ th,
                                  dbl4 *__restrict__ w, const dbl4 *__restrict__ a, const dbl4 *__restrict__ al,
-                                 double dt, double hdt, double ox, double oy, double oz, const int32_t *__restrict__ agg,
-                                 const dbl4 *__restrict__ orig, float4 *__restrict__ x32) {
+                                 double dt, double hdt, double ox, double oy, double oz,
+                                 const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig,
+                                 float4 *__restrict__ x32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));

@@ -71,7 +71,8 @@ struct MixedExtra {
 bool mixed_available();
 void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
                          double hdt, double dt, int move_facets, const MixedExtra &MX, cudaStream_t st);
-// x32 has 2n entries (high parts, then low parts; see MixedExtra)
+// x32 has 2n entries (high parts, then low parts; see MixedExtra); origin[0..2] is the origin of a
+// single system, orig[] those of each system of a batch
 void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, const int32_t *agg, const dbl4 *orig,
                              float4 *x32, cudaStream_t st);
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
@@ -83,6 +84,11 @@ void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairV
                                 double dt, int move_facets, cudaStream_t st);
 void launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                  double dt, int move_facets, const MixedExtra &MX, cudaStream_t st);
+
+// Layout conversion between a caller's [n][3] doubles (already in device memory) and the padded
+// device layout (lg_reduce.cu).
+void launch_aos_to_dev4(int64_t n, const double *aos, dbl4 *dst, cudaStream_t st);
+void launch_dev4_to_aos(int64_t n, const dbl4 *src, double *aos, cudaStream_t st);
 
 // Observables (lg_reduce.cu). scratch: at least obs_scratch_doubles(n) doubles of device memory;
 // out: 20 doubles of device memory (column sums, see lg_reduce.cu).

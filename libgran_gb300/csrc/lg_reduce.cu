@@ -177,4 +177,27 @@ void launch_segmented_rg(int64_t n, int64_t n_systems, const int64_t *offsets, c
     if (n_systems > 0) seg_rg<<<(unsigned)n_systems, 256, 0, st>>>(offsets, x, centres, out);
 }
 
+__global__ void aos_to_dev4(int64_t n, const double *__restrict__ aos, dbl4 *__restrict__ dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    st4(dst, i, mk3(aos[3 * i], aos[3 * i + 1], aos[3 * i + 2]));
+}
+
+__global__ void dev4_to_aos(int64_t n, const dbl4 *__restrict__ src, double *__restrict__ aos) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const d3 q = ld4(src, i);
+    aos[3 * i] = q.x;
+    aos[3 * i + 1] = q.y;
+    aos[3 * i + 2] = q.z;
+}
+
+void launch_aos_to_dev4(int64_t n, const double *aos, dbl4 *dst, cudaStream_t st) {
+    if (n > 0) aos_to_dev4<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, aos, dst);
+}
+
+void launch_dev4_to_aos(int64_t n, const dbl4 *src, double *aos, cudaStream_t st) {
+    if (n > 0) dev4_to_aos<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, src, aos);
+}
+
 }  // namespace lg

@@ -72,8 +72,13 @@ class System:
     def update_neighbor_list(self):
         A.check(A.lib().lg_update_neighbor_list(self.h), "lg_update_neighbor_list")
 
-    def get(self, field):
-        out = np.empty((self.n, 3))
+    def get(self, field, out=None):
+        """Copy one per-particle field to the host: a new (n, 3) float64 array, or into `out` (a
+        C-contiguous (n, 3) float64 array, e.g. a view of pinned memory)."""
+        if out is None:
+            out = np.empty((self.n, 3))
+        elif out.dtype != np.float64 or out.shape != (self.n, 3) or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous (n, 3) float64 array")
         A.check(A.lib().lg_get(self.h, int(field), _dp(out)), "lg_get")
         return out
 
