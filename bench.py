@@ -304,7 +304,9 @@ def batched_section(args, l2_flush):
 def e2e_path(s, mat, args, x0, v0):
     """Same metric through the public API with host buffers: every bench step uploads the state
     (x, v, theta, omega) from pinned host memory, runs 20 VV steps and reads back the state and
-    the observables; host<->device copies are inside the timed region."""
+    its observables (kinetic energies, momenta, centre of mass, radius of gyration: the quantities
+    libgran's compute_energy / mass_distribution helpers report); host<->device copies are inside
+    the timed region."""
     import torch
     from libgran_gb300 import _abi as A
     fields = (A.LG_FIELD_X, A.LG_FIELD_V, A.LG_FIELD_THETA, A.LG_FIELD_OMEGA)
@@ -318,12 +320,12 @@ def e2e_path(s, mat, args, x0, v0):
         s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
         for f in fields:
             s.get(f, out=host[f].numpy())
-        obs = s.observables()
+        obs = s.observables(A.LG_OBS_STATE)
         t = time.perf_counter() - t
         if k >= args.warmup:
             times.append(t)
     h2d = 4 * N_PART * 3 * 8
-    d2h = 4 * N_PART * 3 * 8 + 8 * 20
+    d2h = 4 * N_PART * 3 * 8 + 8 * 19
     return {"value": N_PART * VV_PER_STEP * len(times) / sum(times), "unit": "particle-steps/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}, obs
 

@@ -207,6 +207,14 @@ int lg_reset_acceleration_buffers(lg_system *sys);
 /* Reductions on the device: observables of test/compute_energy.cpp and test/mass_distribution.cpp. */
 int lg_get_observables(lg_system *sys, lg_observables *out);
 
+/* The same observables, restricted to the parts requested (fields of parts not requested are 0;
+ * n_bonds_initial is always set): LG_OBS_STATE = kinetic energies, momenta, centre of mass,
+ * radius of gyration (per-particle sums, cheap); LG_OBS_PAIRS = potential energy, contacts, bonds
+ * (a pass over every pair slot). lg_get_observables is LG_OBS_STATE | LG_OBS_PAIRS. */
+#define LG_OBS_STATE 1
+#define LG_OBS_PAIRS 2
+int lg_get_observables_select(lg_system *sys, int32_t parts, lg_observables *out);
+
 /* Device error word (bit set of LG_DEVERR_*) accumulated since creation; synchronises. */
 #define LG_DEVERR_LIST_OVERFLOW 1    /* a Verlet list row exceeded its capacity */
 #define LG_DEVERR_NONFINITE 2        /* a non-finite acceleration was produced */

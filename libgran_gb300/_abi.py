@@ -19,6 +19,7 @@ LG_FORCE_KERNEL_AUTO, LG_FORCE_KERNEL_ROWGROUP, LG_FORCE_KERNEL_COMPACT = 0, 1, 
 LG_FIELD_X, LG_FIELD_V, LG_FIELD_THETA, LG_FIELD_OMEGA, LG_FIELD_A, LG_FIELD_ALPHA = range(6)
 LG_DEVERR_LIST_OVERFLOW, LG_DEVERR_NONFINITE, LG_DEVERR_BOND_LOST = 1, 2, 4
 LG_NOALLOC_OBS, LG_NOALLOC_MAX_PARTICLES = 9, 1048320
+LG_OBS_STATE, LG_OBS_PAIRS = 1, 2
 LG_REQ_QUEUED, LG_REQ_RUNNING, LG_REQ_DONE, LG_REQ_FAILED, LG_REQ_CANCELLED = 0, 1, 2, 3, 4
 
 
@@ -118,6 +119,7 @@ def _declare(L):
         "lg_set": (C.c_int, [vp, C.c_int, P(d)]),
         "lg_reset_acceleration_buffers": (C.c_int, [vp]),
         "lg_get_observables": (C.c_int, [vp, P(lg_observables)]),
+        "lg_get_observables_select": (C.c_int, [vp, C.c_int32, P(lg_observables)]),
         "lg_get_device_errors": (C.c_int, [vp, P(i32)]),
         "lg_get_bonds": (C.c_int, [vp, P(i64), P(i64), i64]),
         "lg_get_pair_springs": (C.c_int, [vp, i64, i64, P(d)]),

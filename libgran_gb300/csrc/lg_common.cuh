@@ -48,6 +48,19 @@ __host__ __device__ __forceinline__ d3 zero3() { return mk3(0.0, 0.0, 0.0); }
 // 32-byte sector, fetched by a single 256-bit load on sm_103a.
 typedef double4_32a dbl4;
 #ifdef __CUDACC__
+// A spring component stored as a float-float pair (hi, lo) in an 8-byte slot.
+__device__ __forceinline__ double ffslot_load(const double *p, int64_t idx) {
+    const float2 v = reinterpret_cast<const float2 *>(p)[idx];
+    return (double)v.x + (double)v.y;
+}
+__device__ __forceinline__ void ffslot_store(double *p, int64_t idx, double d) {
+    const float hi = (float)d;
+    reinterpret_cast<float2 *>(p)[idx] = make_float2(hi, (float)(d - (double)hi));
+}
+// A spring component in either storage form.
+__device__ __forceinline__ double spring_load(const double *p, int64_t idx, bool ff) {
+    return ff ? ffslot_load(p, idx) : p[idx];
+}
 __device__ __forceinline__ d3 ld4(const dbl4 *p, int64_t i) {
     dbl4 q = p[i];
     return mk3(q.x, q.y, q.z);
@@ -80,6 +93,7 @@ struct Params {
     FacetDev facets[kMaxFacets];
     double contact_skip_d2;  // squared centre distance above which overlap <= 0 is certain
     double hamaker_skip_d2;  // squared centre distance above which the limited Hamaker is zero
+    int32_t springs_ff;      // pair and bond springs held as float-float pairs (mixed precision)
 };
 
 // Entry flags of a pair slot (Verlet list slot or implicit all-pairs slot)
@@ -93,7 +107,8 @@ struct PairView {
     int32_t *nbr;       // [cap * n] neighbour index (Verlet mode)
     int32_t *row_len;   // [n] (Verlet mode)
     uint32_t *flags;    // [cap * n]
-    double *xi;         // [9][cap * n] contact springs, component-major
+    double *xi;         // [9][cap * n] contact springs, component-major (8-byte slots: FP64 values,
+                        // or float-float pairs when Params::springs_ff is set)
     int64_t cap;        // slots per row
 };
 

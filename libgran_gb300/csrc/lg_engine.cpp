@@ -281,18 +281,41 @@ static int set_mixed_origins(lg_system *s, const double *x) {
     origin_of(x, 0, s->P.n, s->r_max, s->origin);
     s->ext_max = s->origin[3];
     if (s->n_systems > 0) {
-        std::vector<dbl4> org((size_t)s->n_systems);
+        s->h_orig.assign((size_t)s->n_systems, make_double4_32a(0.0, 0.0, 0.0, 0.0));
         s->ext_max = 0.0;
         for (int64_t q = 0; q < s->n_systems; ++q) {
             double o[4];
             origin_of(x, s->sys_off[q], s->sys_off[q + 1], s->r_max, o);
-            org[q] = make_double4_32a(o[0], o[1], o[2], o[3]);
+            s->h_orig[(size_t)q] = make_double4_32a(o[0], o[1], o[2], o[3]);
             s->ext_max = std::max(s->ext_max, o[3]);
         }
-        LG_CUDA(cudaMemcpyAsync(s->d_orig, org.data(), sizeof(dbl4) * org.size(), cudaMemcpyHostToDevice, s->stream));
+        LG_CUDA(cudaMemcpyAsync(s->d_orig, s->h_orig.data(), sizeof(dbl4) * s->h_orig.size(), cudaMemcpyHostToDevice,
+                                s->stream));
         LG_CUDA(cudaStreamSynchronize(s->stream));
     }
     return LG_OK;
+}
+
+// New positions keep the current origins (and the CUDA graphs that hold them) while every offset
+// from its system's origin stays within four times the extent the origin was set up with: the
+// culling margins of set_cull_radii allow for exactly that.
+static bool origins_cover(const lg_system *s, const double *x) {
+    auto within = [&](int64_t b, int64_t e, double ox, double oy, double oz, double ext) {
+        const double lim = 4.0 * ext;
+        for (int64_t i = b; i < e; ++i)
+            if (!(std::fabs(x[3 * i] - ox) <= lim && std::fabs(x[3 * i + 1] - oy) <= lim &&
+                  std::fabs(x[3 * i + 2] - oz) <= lim))
+                return false;
+        return true;
+    };
+    if (s->n_systems > 0) {
+        for (int64_t q = 0; q < s->n_systems; ++q) {
+            const dbl4 &o = s->h_orig[(size_t)q];
+            if (!within(s->sys_off[q], s->sys_off[q + 1], o.x, o.y, o.z, o.w)) return false;
+        }
+        return true;
+    }
+    return within(0, s->P.n, s->origin[0], s->origin[1], s->origin[2], s->origin[3]);
 }
 
 // lg_get / lg_set: the caller's [n][3] array moves in one copy to device scratch (the observables
@@ -432,7 +455,7 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every) {
     const double hdt = dt / 2.0;
     if (s->precision == LG_PRECISION_MIXED)
         launch_kick_drift_mixed(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->origin,
-                                s->d_agg, s->d_orig, s->x32, s->stream);
+                                s->d_agg, s->d_orig, s->x32, s->v32, s->stream);
     else
         launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->stream);
     s->launches += 1;
@@ -517,6 +540,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     const double cr = 2.0 * d->contact.r_part;
     P.contact_skip_d2 = cr * cr * (1.0 + 1e-9);
     P.hamaker_skip_d2 = d->hamaker.r_cutoff * d->hamaker.r_cutoff * (1.0 + 1e-9);
+    P.springs_ff = d->precision == LG_PRECISION_MIXED ? 1 : 0;
     for (int f = 0; f < d->n_facets; ++f) {
         const lg_facet_desc &fd = facets[f];
         FacetDev &o = P.facets[f];
@@ -758,10 +782,12 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
 
     if (s->precision == LG_PRECISION_MIXED) {
         LG_TRY(s->alloc(&s->x32, 2 * (size_t)n));  // float-float: high parts, then low parts
+        LG_TRY(s->alloc(&s->v32, 3 * (size_t)n));  // v high parts, v low parts, spins
         if (s->n_systems > 0) LG_TRY(s->alloc(&s->d_orig, (size_t)s->n_systems));
         s->r_max = std::max(d->contact.r_part, std::max(d->sinter.r_part, d->hamaker.r_part));
         LG_TRY(set_mixed_origins(s, x0));
-        launch_positions_to_f32(n, s->x, s->origin, s->d_agg, s->d_orig, s->x32, s->stream);
+        launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32, s->v32,
+                            s->stream);
         double near = 0.0;
         if (d->binary_model != LG_BINARY_NONE) near = std::max(near, 2.0 * d->contact.r_part);
         if (sinter) near = std::max(near, 2.0 * d->sinter.r_part);
@@ -770,6 +796,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
             near = std::max(near, 7.0 * d->hamaker.r_part);
         s->mx.x32 = s->x32;
         s->mx.x32lo = s->x32 + n;
+        s->mx.v32 = s->v32;
         double cnear = 0.0;
         if (d->binary_model != LG_BINARY_NONE) cnear = std::max(cnear, 2.0 * d->contact.r_part);
         if (sinter) cnear = std::max(cnear, 2.0 * d->sinter.r_part);
@@ -965,11 +992,14 @@ extern "C" int lg_set(lg_system *s, int field, const double *in) {
     dbl4 *p = field_ptr(s, field);
     if (!p || !in) return lg_fail(LG_E_INVALID, "lg_set: bad field %d or null input", field);
     LG_TRY(upload_staged(s, p, in));
-    if (field == LG_FIELD_X && s->x32) {
-        LG_TRY(set_mixed_origins(s, in));  // new positions: new origins and culling radii
-        set_cull_radii(s);
-        s->drop_graphs();  // captured launches hold the old values
-        launch_positions_to_f32(s->P.n, s->x, s->origin, s->d_agg, s->d_orig, s->x32, s->stream);
+    if (s->x32 && (field == LG_FIELD_X || field == LG_FIELD_V || field == LG_FIELD_OMEGA)) {
+        if (field == LG_FIELD_X && !origins_cover(s, in)) {
+            LG_TRY(set_mixed_origins(s, in));  // positions moved far: new origins and culling radii
+            set_cull_radii(s);
+            s->drop_graphs();  // captured launches hold the old values
+        }
+        launch_mixed_copies(s->P.n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32,
+                            s->v32, s->stream);
         s->launches += 1;
         LG_CUDA(cudaGetLastError());
     }
@@ -1010,9 +1040,10 @@ extern "C" int lg_get_device_errors(lg_system *s, int32_t *errors) {
     return LG_OK;
 }
 
-extern "C" int lg_get_observables(lg_system *s, lg_observables *o) {
+extern "C" int lg_get_observables_select(lg_system *s, int32_t parts, lg_observables *o) {
     LG_HANDLE(s);
     if (!o) return lg_fail(LG_E_INVALID, "lg_get_observables: null output");
+    if (parts & ~(LG_OBS_STATE | LG_OBS_PAIRS)) return lg_fail(LG_E_INVALID, "lg_get_observables: unknown parts %d", parts);
     const Params &P = s->P;
     double m, I;
     if (P.binary_model == LG_BINARY_SINTER || P.binary_model == LG_BINARY_BREAKING_SINTER) {
@@ -1025,37 +1056,40 @@ extern "C" int lg_get_observables(lg_system *s, lg_observables *o) {
         m = P.hamaker.mass;
         I = P.contact.inertia;
     }
+    memset(o, 0, sizeof(*o));
+    o->n_bonds_initial = s->n_bonds_initial;
+    if (!parts) return LG_OK;
+    // every pass stays on the device; one copy back at the end
     StateView S = state_view(s, false);
-    launch_observables(P, S, s->pv[s->pcur], s->bv, m, I, s->obs_scratch, s->obs_out, s->stream);
-    s->launches += 2;
+    launch_observables(P, S, s->pv[s->pcur], s->bv, m, I, s->obs_scratch, s->obs_out, s->stream,
+                       (parts & LG_OBS_PAIRS) != 0);
+    launch_observables_rg(P.n, s->x, s->obs_scratch, s->obs_out, s->stream);
+    s->launches += 4;
     LG_CUDA(cudaGetLastError());
-    double h[32];
-    LG_CUDA(cudaMemcpyAsync(h, s->obs_out, sizeof(double) * 18, cudaMemcpyDeviceToHost, s->stream));
+    double h[19];
+    LG_CUDA(cudaMemcpyAsync(h, s->obs_out, sizeof(double) * 19, cudaMemcpyDeviceToHost, s->stream));
     LG_CUDA(cudaStreamSynchronize(s->stream));
     const double nn = (double)P.n;
-    double c[3] = {h[12] / nn, h[13] / nn, h[14] / nn};
-    double *dc = s->obs_out + 24;
-    LG_CUDA(cudaMemcpyAsync(dc, c, sizeof(double) * 3, cudaMemcpyHostToDevice, s->stream));
-    LG_CUDA(cudaStreamSynchronize(s->stream));
-    launch_observables_rg(P.n, s->x, c, s->obs_scratch, s->obs_out, s->stream);
-    s->launches += 2;
-    LG_CUDA(cudaGetLastError());
-    LG_CUDA(cudaMemcpyAsync(h + 18, s->obs_out + 18, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-    LG_CUDA(cudaStreamSynchronize(s->stream));
-    memset(o, 0, sizeof(*o));
-    o->ke_total = h[0];
-    o->ke_translational = h[1] / 2.0;
-    o->ke_rotational = h[2] / 2.0;
-    o->linear_momentum = m * std::sqrt((h[3] * h[3] + h[4] * h[4]) + h[5] * h[5]);
-    double L[3] = {h[6] + h[9], h[7] + h[10], h[8] + h[11]};
-    o->angular_momentum = std::sqrt((L[0] * L[0] + L[1] * L[1]) + L[2] * L[2]);
-    for (int k = 0; k < 3; ++k) o->center_of_mass[k] = c[k];
-    o->radius_of_gyration = std::sqrt(h[18] / nn);
-    o->potential_energy = h[15];
-    o->n_contacts = (int64_t)h[16];
-    o->n_bonds = (int64_t)h[17];
-    o->n_bonds_initial = s->n_bonds_initial;
+    if (parts & LG_OBS_STATE) {
+        o->ke_total = h[0];
+        o->ke_translational = h[1] / 2.0;
+        o->ke_rotational = h[2] / 2.0;
+        o->linear_momentum = m * std::sqrt((h[3] * h[3] + h[4] * h[4]) + h[5] * h[5]);
+        double L[3] = {h[6] + h[9], h[7] + h[10], h[8] + h[11]};
+        o->angular_momentum = std::sqrt((L[0] * L[0] + L[1] * L[1]) + L[2] * L[2]);
+        for (int k = 0; k < 3; ++k) o->center_of_mass[k] = h[12 + k] / nn;
+        o->radius_of_gyration = std::sqrt(h[18] / nn);
+    }
+    if (parts & LG_OBS_PAIRS) {
+        o->potential_energy = h[15];
+        o->n_contacts = (int64_t)h[16];
+        o->n_bonds = (int64_t)h[17];
+    }
     return LG_OK;
+}
+
+extern "C" int lg_get_observables(lg_system *s, lg_observables *o) {
+    return lg_get_observables_select(s, LG_OBS_STATE | LG_OBS_PAIRS, o);
 }
 
 extern "C" int lg_get_bonds(lg_system *s, int64_t *n_bonds, int64_t *pairs, int64_t cap) {
@@ -1082,6 +1116,16 @@ extern "C" int lg_get_bonds(lg_system *s, int64_t *n_bonds, int64_t *pairs, int6
     return LG_OK;
 }
 
+// Raw 8-byte spring slots -> values: mixed-precision handles store float-float pairs (hi, lo).
+static void spring_values(const lg_system *s, double *v9) {
+    if (!s->P.springs_ff) return;
+    for (int q = 0; q < 9; ++q) {
+        float hl[2];
+        std::memcpy(hl, &v9[q], sizeof(hl));
+        v9[q] = (double)hl[0] + (double)hl[1];
+    }
+}
+
 extern "C" int lg_get_pair_springs(lg_system *s, int64_t i, int64_t j, double *out9) {
     LG_HANDLE(s);
     if (!out9) return lg_fail(LG_E_INVALID, "lg_get_pair_springs: null output");
@@ -1098,6 +1142,7 @@ extern "C" int lg_get_pair_springs(lg_system *s, int64_t i, int64_t j, double *o
         if (in) {
             const size_t bs = (size_t)s->bv.bcap * n;
             for (int q = 0; q < 9; ++q) LG_CUDA(cudaMemcpy(out9 + q, s->bv.xi + q * bs + be, sizeof(double), cudaMemcpyDeviceToHost));
+            spring_values(s, out9);
             return LG_OK;
         }
     }
@@ -1123,6 +1168,7 @@ extern "C" int lg_get_pair_springs(lg_system *s, int64_t i, int64_t j, double *o
     LG_CUDA(cudaMemcpy(&fl, pv.flags + e, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     if (!(fl & kXiLive)) return LG_OK;  // springs of a slot that is not live are zero
     for (int q = 0; q < 9; ++q) LG_CUDA(cudaMemcpy(out9 + q, pv.xi + q * xs + e, sizeof(double), cudaMemcpyDeviceToHost));
+    spring_values(s, out9);
     return LG_OK;
 }
 
@@ -1318,6 +1364,7 @@ static int snapshot_take(lg_system *s) {
         addb(s->fv[1], sizeof(double) * 9 * (size_t)nf);
         addb(s->err, sizeof(int32_t));
         if (s->x32) addb(s->x32, sizeof(float4) * 2 * n);
+        if (s->v32) addb(s->v32, sizeof(float4) * 3 * n);
         const int npv = s->P.pairs == LG_PAIRS_VERLET ? 2 : 1;
         for (int q = 0; q < npv; ++q) {
             PairView &pv = s->pv[q];

@@ -40,7 +40,8 @@ struct lg_system {
     double *obs_out = nullptr;
 
     // mixed precision: FP32 position copy for culling
-    float4 *x32 = nullptr;
+    float4 *x32 = nullptr;  // mixed: [2n] float-float positions
+    float4 *v32 = nullptr;  // mixed: [3n] float-float velocities, FP32 spins
     double origin[4] = {0.0, 0.0, 0.0, 0.0};  // mixed: origin of the float-float positions, extent in [3]
     double r_max = 0.0;                        // mixed: largest particle radius of the functors
     double ext_max = 0.0;                      // mixed: largest extent of a system about its origin
@@ -59,6 +60,7 @@ struct lg_system {
     int32_t *d_agg = nullptr;            // [n] system of every particle
     lg::dbl4 *d_hoff = nullptr;          // [n_systems] hashing offsets
     lg::dbl4 *d_orig = nullptr;          // [n_systems] float-float origins (x, y, z; w: extent), mixed
+    std::vector<lg::dbl4> h_orig;        // host copy of d_orig
     double *d_centres = nullptr;         // [3 n_systems] scratch for per-system observables
     double *d_sys_obs = nullptr;         // [20 n_systems]
     std::vector<int64_t> n_bonds_initial_sys;

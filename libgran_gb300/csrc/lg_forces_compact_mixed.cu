@@ -17,7 +17,9 @@
 //    and angular accelerations of the contact/bond pairs, folded in slot order at the end of each
 //    round; the sums become FP64 once per row. Each sum's order depends only on the row itself, not
 //    on which rows share its warp, so a system gives the same bits alone and inside a batch;
-//  * contact and bond pairs keep their FP64 spring vectors, updated by FP32 increments (shear_mx).
+//  * contact and bond pairs read float-float copies of the velocities (MixedExtra::v32) and keep
+//    their spring vectors as float-float pairs in the 8-byte spring slots, updated by FP32
+//    increments (shear_ff): no FP64 operation in any pair.
 // For launches with few rows the windows of a row are sliced over SL warps (slot_of), each slice
 // keeping its own partial sums, which are combined in slice order at the end.
 #include <cstddef>
@@ -60,7 +62,8 @@ struct WarpSmemM {
     uint32_t cball[kRound];
     int32_t cbase[kRound];
     float4 xh[32], xl[32];  // the rows' own positions (float-float)
-    d3 vo[32], wo[32];      // the rows' own velocities and spins (FP64)
+    float4 vh[32], vl[32];  // the rows' own velocities (float-float)
+    float4 wh[32];          // the rows' own spins (FP32)
 };
 static_assert(offsetof(WarpSmemM, hlo) == sizeof(WarpSmemM::hhi) &&
                   sizeof(WarpSmemM::hhi) + sizeof(WarpSmemM::hlo) >= 18 * 32 * sizeof(float),
@@ -76,54 +79,6 @@ __device__ __forceinline__ f3 fscl(float s, f3 a) { return fm(s * a.x, s * a.y, 
 __device__ __forceinline__ float fdot(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
 __device__ __forceinline__ f3 fcrs(f3 a, f3 b) {
     return fm(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ f3 tof(d3 a) { return fm((float)a.x, (float)a.y, (float)a.z); }
-
-// Shear spring (contact_force.h:105-147, Coulomb-capped; alt_sinter_bridge.h:137-156, bond form)
-// with the spring vector held in FP64. Each evaluation computes, in FP32, the increment of the
-// spring: the rotation onto the tangent plane, -(xi.n) n, the rescale to the old magnitude,
-// (s - 1)(xi - (xi.n) n) with s - 1 evaluated as a series for small tilts, and the stretch rel*dt;
-// the increment is small next to xi and is added to the FP64 spring, so rounding does not
-// accumulate at the spring's own scale. The dynamic (sliding) branch sets the spring outright.
-__device__ __forceinline__ f3 shear_mx(d3 &xi, f3 n, float stiffness, float damping, float normal_force, float mu_s,
-                                       float phi, f3 rel, float dtf, bool coulomb) {
-    f3 xf = tof(xi);
-    f3 drot = fm(0.f, 0.f, 0.f);
-    float xx = fdot(xf, xf);
-    if (xx > 0.0f) {
-        float c = fdot(xf, n);
-        f3 xr = fsub(xf, fscl(c, n));
-        float e = (c * c) / xx;
-        float sm1 = 0.0f;
-        if (e < 1.0f) sm1 = e < 1e-3f ? e * (0.5f + 0.375f * e) : rsqrtf(1.0f - e) - 1.0f;
-        drot = fadd(fscl(-c, n), fscl(sm1, xr));
-    }
-    const f3 xn = fadd(xf, drot);
-    const f3 f0 = fsub(fscl(-stiffness, xn), fscl(damping, rel));
-    if (!coulomb) {
-        const f3 dxi = fadd(drot, fscl(dtf, rel));
-        xi.x += (double)dxi.x;
-        xi.y += (double)dxi.y;
-        xi.z += (double)dxi.z;
-        return f0;
-    }
-    const float fs = mu_s * normal_force;
-    const float fd = mu_s * phi * normal_force;
-    const float f0n = sqrtf(fdot(f0, f0));
-    const f3 t = f0n > 0.0f ? fscl(1.0f / f0n, f0) : fm(0.f, 0.f, 0.f);
-    float sel;
-    if (f0n <= fs) {
-        const f3 dxi = fadd(drot, fscl(dtf, rel));
-        xi.x += (double)dxi.x;
-        xi.y += (double)dxi.y;
-        xi.z += (double)dxi.z;
-        sel = fs;
-    } else {
-        const f3 nx = fscl(-1.0f / stiffness, fadd(fscl(fd, t), fscl(damping, rel)));
-        xi = mk3((double)nx.x, (double)nx.y, (double)nx.z);
-        sel = fd;
-    }
-    return fscl(fminf(sel, f0n), t);
 }
 
 // Hamaker factor of hamaker_force.h:36-40 with two reciprocals:
@@ -155,6 +110,63 @@ __device__ __forceinline__ void ff_acc(ff &a, float b) {
     a.lo = __fadd_rn(a.lo, s.lo);
 }
 __device__ __forceinline__ double ff_to_d(ff a) { return (double)a.hi + (double)a.lo; }
+// a += b for a stored spring component, renormalised so that |lo| <= ulp(hi) / 2 again.
+__device__ __forceinline__ void ff_add_norm(ff &a, float b) {
+    const ff s = two_sum(a.hi, b);
+    const float lo = __fadd_rn(a.lo, s.lo);
+    const float hi = __fadd_rn(s.hi, lo);
+    a = ff{hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
+}
+
+// Shear spring (contact_force.h:105-147, Coulomb-capped; alt_sinter_bridge.h:137-156, bond form)
+// with the spring vector held as float-float components. Each evaluation computes, in FP32, the
+// increment of the spring: the rotation onto the tangent plane, -(xi.n) n, the rescale to the old
+// magnitude, (s - 1)(xi - (xi.n) n) with s - 1 evaluated as a series for small tilts, and the
+// stretch rel*dt; the increment is small next to xi and is added to the float-float spring, so
+// rounding does not accumulate at the spring's own scale. The dynamic (sliding) branch sets the
+// spring outright.
+__device__ __forceinline__ f3 shear_ff(ff (&xi)[3], f3 n, float stiffness, float damping, float normal_force,
+                                       float mu_s, float phi, f3 rel, float dtf, bool coulomb) {
+    const f3 xf = fm(xi[0].hi, xi[1].hi, xi[2].hi);  // the FP32 rounding of the spring
+    f3 drot = fm(0.f, 0.f, 0.f);
+    const float xx = fdot(xf, xf);
+    if (xx > 0.0f) {
+        const float c = fdot(xf, n);
+        const f3 xr = fsub(xf, fscl(c, n));
+        const float e = (c * c) / xx;
+        float sm1 = 0.0f;
+        if (e < 1.0f) sm1 = e < 1e-3f ? e * (0.5f + 0.375f * e) : rsqrtf(1.0f - e) - 1.0f;
+        drot = fadd(fscl(-c, n), fscl(sm1, xr));
+    }
+    const f3 xn = fadd(xf, drot);
+    const f3 f0 = fsub(fscl(-stiffness, xn), fscl(damping, rel));
+    if (!coulomb) {
+        const f3 dxi = fadd(drot, fscl(dtf, rel));
+        ff_add_norm(xi[0], dxi.x);
+        ff_add_norm(xi[1], dxi.y);
+        ff_add_norm(xi[2], dxi.z);
+        return f0;
+    }
+    const float fs = mu_s * normal_force;
+    const float fd = mu_s * phi * normal_force;
+    const float f0n = sqrtf(fdot(f0, f0));
+    const f3 t = f0n > 0.0f ? fscl(1.0f / f0n, f0) : fm(0.f, 0.f, 0.f);
+    float sel;
+    if (f0n <= fs) {
+        const f3 dxi = fadd(drot, fscl(dtf, rel));
+        ff_add_norm(xi[0], dxi.x);
+        ff_add_norm(xi[1], dxi.y);
+        ff_add_norm(xi[2], dxi.z);
+        sel = fs;
+    } else {
+        const f3 nx = fscl(-1.0f / stiffness, fadd(fscl(fd, t), fscl(damping, rel)));
+        xi[0] = ff{nx.x, 0.f};
+        xi[1] = ff{nx.y, 0.f};
+        xi[2] = ff{nx.z, 0.f};
+        sel = fd;
+    }
+    return fscl(fminf(sel, f0n), t);
+}
 
 // Separation d = x_i - x_j (FP32) and q = |d|^2 - (2r)^2 from float-float positions. Per component
 // the high parts' difference is split exactly (TwoSum) and its error joins the low parts'
@@ -194,7 +206,6 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
     const int32_t j = W.cj[q];
     const uint32_t fl = PV.flags[e];
     const bool bonded = (fl & kBonded) != 0;
-    const d3 vo = W.vo[own], wo = W.wo[own];
     const SepFF sp = separation_ff(W.xh[own], W.xl[own], M.x32[j], M.x32lo[j], bonded ? M.b_fr_hi : M.c_fr_hi,
                                    bonded ? M.b_fr_lo : M.c_fr_lo);
     const f3 dxf = sp.d;
@@ -205,26 +216,31 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
     f3 force = fm(0.f, 0.f, 0.f), torque = fm(0.f, 0.f, 0.f);
     if (bonded || overlap > 0.0f) {
         const f3 n3 = fscl(rsd, dxf);
-        const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
-        const f3 vij0 = tof(sub(vo, vj));
-        const f3 wfi = tof(wo), wfj = tof(wj);
+        // relative velocity v_i - v_j from the float-float copies (exact high-part difference)
+        const float4 vhi = W.vh[own], vlo = W.vl[own], vhj = M.v32[j], vlj = M.v32[n + j];
+        const ff tx = two_sum(vhi.x, -vhj.x), ty = two_sum(vhi.y, -vhj.y), tz = two_sum(vhi.z, -vhj.z);
+        const f3 vij0 = fm(tx.hi + (tx.lo + (vlo.x - vlj.x)), ty.hi + (ty.lo + (vlo.y - vlj.y)),
+                           tz.hi + (tz.lo + (vlo.z - vlj.z)));
+        const float4 wo4 = W.wh[own], wj4 = M.v32[2 * n + j];
+        const f3 wfi = fm(wo4.x, wo4.y, wo4.z), wfj = fm(wj4.x, wj4.y, wj4.z);
         int64_t base, stride;
-        double *store;
+        float2 *store;
         if (bonded) {
             base = (int64_t)bond_slot_of(fl) * n + io;
             stride = bs;
-            store = BV.xi;
+            store = reinterpret_cast<float2 *>(BV.xi);
         } else {
             base = e;
             stride = xs;
-            store = PV.xi;
+            store = reinterpret_cast<float2 *>(PV.xi);
         }
-        d3 s[3] = {zero3(), zero3(), zero3()};  // springs of a slot that is not live are zero
+        ff s[3][3] = {};  // springs of a slot that is not live are zero
         if (bonded || (fl & kXiLive))
 #pragma unroll
-            for (int c = 0; c < 3; ++c)
-                s[c] = mk3(store[(3 * c) * stride + base], store[(3 * c + 1) * stride + base],
-                           store[(3 * c + 2) * stride + base]);
+            for (int c = 0; c < 9; ++c) {
+                const float2 v = store[c * stride + base];
+                s[c / 3][c % 3] = ff{v.x, v.y};
+            }
         const float kn = bonded ? M.b_k : M.c_k, gn = bonded ? M.b_gn : M.c_gn;
         const float rp = rr - 0.5f * overlap;
         const float v_n = -fdot(vij0, n3);
@@ -236,26 +252,22 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
         const f3 v_o = fscl(rr * (fdot(n3, wfi) - fdot(n3, wfj)), n3);
         f3 f_t, f_r, f_o;
         if (bonded) {
-            f_t = shear_mx(s[0], n3, M.b_kt, M.b_gt, f_n, 0.f, 0.f, v_t, M.b_dt, false);
-            f_r = shear_mx(s[1], n3, M.b_kr, M.b_gr, f_n, 0.f, 0.f, v_r, M.b_dt, false);
-            f_o = shear_mx(s[2], n3, M.b_ko, M.b_go, f_n, 0.f, 0.f, v_o, M.b_dt, false);
+            f_t = shear_ff(s[0], n3, M.b_kt, M.b_gt, f_n, 0.f, 0.f, v_t, M.b_dt, false);
+            f_r = shear_ff(s[1], n3, M.b_kr, M.b_gr, f_n, 0.f, 0.f, v_r, M.b_dt, false);
+            f_o = shear_ff(s[2], n3, M.b_ko, M.b_go, f_n, 0.f, 0.f, v_o, M.b_dt, false);
         } else {
-            f_t = shear_mx(s[0], n3, M.c_kt, M.c_gt, f_n, M.c_mus, M.c_phid, v_t, M.c_dt, true);
-            f_r = shear_mx(s[1], n3, M.c_kr, M.c_gr, f_n, M.c_mur, M.c_phir, v_r, M.c_dt, true);
-            f_o = shear_mx(s[2], n3, M.c_ko, M.c_go, f_n, M.c_muo, M.c_phio, v_o, M.c_dt, true);
+            f_t = shear_ff(s[0], n3, M.c_kt, M.c_gt, f_n, M.c_mus, M.c_phid, v_t, M.c_dt, true);
+            f_r = shear_ff(s[1], n3, M.c_kr, M.c_gr, f_n, M.c_mur, M.c_phir, v_r, M.c_dt, true);
+            f_o = shear_ff(s[2], n3, M.c_ko, M.c_go, f_n, M.c_muo, M.c_phio, v_o, M.c_dt, true);
         }
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            store[(3 * c) * stride + base] = s[c].x;
-            store[(3 * c + 1) * stride + base] = s[c].y;
-            store[(3 * c + 2) * stride + base] = s[c].z;
-        }
+        for (int c = 0; c < 9; ++c) store[c * stride + base] = make_float2(s[c / 3][c % 3].hi, s[c / 3][c % 3].lo);
         force = fadd(fscl(f_n, n3), f_t);
         torque = fadd(fsub(fscl(rr, fcrs(n3, f_r)), fscl(rp, fcrs(n3, f_t))), fscl(rr, f_o));
         if (bonded) {
             if (P.binary_model == LG_BINARY_BREAKING_SINTER) {
-                const double st = BV.strength[base];
-                if ((double)fdot(force, force) > st * st) {
+                const float st = (float)BV.strength[base];
+                if (fdot(force, force) > st * st) {
                     BV.intact[base] = 0;
                     PV.flags[e] = fl & ~(kBonded | (0xffu << 8));
                 }
@@ -322,19 +334,21 @@ __global__ void __launch_bounds__(ShapeM<SL>::kWarps * 32, ShapeM<SL>::kMinBlock
     int64_t len = 0;
     float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f);
     {
-        float4 lo_i = hi_i;
-        d3 vi = zero3(), wi = zero3();
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 lo_i = z4, vh = z4, vl = z4, wh = z4;
         if (active) {
             len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
             hi_i = MX.x32[i];
             lo_i = MX.x32lo[i];
-            vi = ld4(S.v, i);
-            wi = ld4(S.w, i);
+            vh = MX.v32[i];
+            vl = MX.v32[n + i];
+            wh = MX.v32[2 * n + i];
         }
         W.xh[lane] = hi_i;
         W.xl[lane] = lo_i;
-        W.vo[lane] = vi;
-        W.wo[lane] = wi;
+        W.vh[lane] = vh;
+        W.vl[lane] = vl;
+        W.wh[lane] = wh;
     }
     const int64_t maxlen = (int64_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
     // this warp's windows: sl, sl + kSlices, ...; virtual slot v maps to slot_of<SL>(v, sl)
@@ -369,98 +383,104 @@ __global__ void __launch_bounds__(ShapeM<SL>::kWarps * 32, ShapeM<SL>::kMinBlock
     for (int64_t kstart = 0; kstart < vmax;) {
         int ccount = 0, cdone = 0;
         int64_t k = kstart;
-        for (; k < vmax && k - kstart + kWin <= kRound && ccount + 32 * kWin <= kCCap; k += kWin) {
-            int32_t jg[kWin];
-            uint32_t fg[kWin];
-            float4 ph[kWin], pl[kWin];
+        for (;;) {
+            const bool take = k < vmax && k - kstart + kWin <= kRound && ccount + 32 * kWin <= kCCap;
+            if (take) {
+                int32_t jg[kWin];
+                uint32_t fg[kWin];
+                float4 ph[kWin], pl[kWin];
 #pragma unroll
-            for (int u = 0; u < kWin; ++u) {
-                jg[u] = jn[u];
-                fg[u] = fn[u];
-            }
-#pragma unroll
-            for (int u = 0; u < kWin; ++u) {
-                ph[u] = hi_i;
-                pl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (jg[u] >= 0) {
-                    ph[u] = MX.x32[jg[u]];
-                    pl[u] = MX.x32lo[jg[u]];
+                for (int u = 0; u < kWin; ++u) {
+                    jg[u] = jn[u];
+                    fg[u] = fn[u];
                 }
-            }
-            if (k + kWin < vmax) load_window(k + kWin);  // next window, in flight during this one
-            const int64_t k0 = slot_of<SL>(k, sl);
-            int hcount = 0;
-            uint32_t hbal[kWin];
-            int hbas[kWin];
 #pragma unroll
-            for (int u = 0; u < kWin; ++u) {
-                const int off = (int)(k - kstart) + u;  // virtual slot offset within the round
-                bool hb = false, cb = false;
-                if (jg[u] >= 0) {
-                    const uint32_t fl = fg[u];
-                    const float dxf = hi_i.x - ph[u].x, dyf = hi_i.y - ph[u].y, dzf = hi_i.z - ph[u].z;
-                    const float d2f = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
-                    if (hm == LG_HAMAKER_LIMITED)
-                        hb = d2f <= MX.near2;
-                    else if (hm != LG_HAMAKER_NONE)
-                        hb = true;
-                    if (contacts_on) {
-                        if ((fl & kBonded) || d2f <= MX.contact2f) {
-                            cb = true;
-                        } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
-                            const int64_t e = (k0 + u) * n + i;
+                for (int u = 0; u < kWin; ++u) {
+                    ph[u] = hi_i;
+                    pl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (jg[u] >= 0) {
+                        ph[u] = MX.x32[jg[u]];
+                        if (hm != LG_HAMAKER_NONE) pl[u] = MX.x32lo[jg[u]];
+                    }
+                }
+                if (k + kWin < vmax) load_window(k + kWin);  // next window, in flight during this one
+                const int64_t k0 = slot_of<SL>(k, sl);
+                int hcount = 0;
+                uint32_t hbal[kWin];
+                int hbas[kWin];
 #pragma unroll
-                            for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
-                            PV.flags[e] = fl & ~kXiLive;
+                for (int u = 0; u < kWin; ++u) {
+                    const int off = (int)(k - kstart) + u;  // virtual slot offset within the round
+                    bool hb = false, cb = false;
+                    if (jg[u] >= 0) {
+                        const uint32_t fl = fg[u];
+                        const float dxf = hi_i.x - ph[u].x, dyf = hi_i.y - ph[u].y, dzf = hi_i.z - ph[u].z;
+                        const float d2f = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
+                        if (hm == LG_HAMAKER_LIMITED)
+                            hb = d2f <= MX.near2;
+                        else if (hm != LG_HAMAKER_NONE)
+                            hb = true;
+                        if (contacts_on) {
+                            if ((fl & kBonded) || d2f <= MX.contact2f) {
+                                cb = true;
+                            } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+                                const int64_t e = (k0 + u) * n + i;
+#pragma unroll
+                                for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+                                PV.flags[e] = fl & ~kXiLive;
+                            }
                         }
                     }
-                }
-                const uint32_t bc = __ballot_sync(0xffffffffu, cb);
-                const uint32_t bh = __ballot_sync(0xffffffffu, hb);
-                if (cb) {
-                    const int q = ccount + __popc(bc & lt);
-                    W.cj[q] = jg[u];
-                    W.cown[q] = (uint16_t)((lane << 8) | off);
-                }
-                if (hb) {
-                    const int q = hcount + __popc(bh & lt);
-                    W.hhi[q] = make_float4(ph[u].x, ph[u].y, ph[u].z, __int_as_float(lane));
-                    W.hlo[q] = pl[u];
-                }
-                if (lane == 0) {
-                    W.cball[off] = bc;
-                    W.cbase[off] = ccount;
-                }
-                hbal[u] = bh;
-                hbas[u] = hcount;
-                ccount += __popc(bc);
-                hcount += __popc(bh);
-            }
-            __syncwarp();
-            for (int q = lane; q < hcount; q += 32) hamaker_item(P, MX, W, q);
-            __syncwarp();
-            {  // the window's (at most four) Hamaker terms in slot order, then one compensated add
-                float wsum[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-                for (int u = 0; u < kWin; ++u)
-                    if ((hbal[u] >> lane) & 1u) {
-                        const int q = hbas[u] + __popc(hbal[u] & lt);
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) wsum[c] += W.hres[q][c];
+                    const uint32_t bc = __ballot_sync(0xffffffffu, cb);
+                    const uint32_t bh = __ballot_sync(0xffffffffu, hb);
+                    if (cb) {
+                        const int q = ccount + __popc(bc & lt);
+                        W.cj[q] = jg[u];
+                        W.cown[q] = (uint16_t)((lane << 8) | off);
                     }
+                    if (hb) {
+                        const int q = hcount + __popc(bh & lt);
+                        W.hhi[q] = make_float4(ph[u].x, ph[u].y, ph[u].z, __int_as_float(lane));
+                        W.hlo[q] = pl[u];
+                    }
+                    if (lane == 0) {
+                        W.cball[off] = bc;
+                        W.cbase[off] = ccount;
+                    }
+                    hbal[u] = bh;
+                    hbas[u] = hcount;
+                    ccount += __popc(bc);
+                    hcount += __popc(bh);
+                }
+                __syncwarp();
+                for (int q = lane; q < hcount; q += 32) hamaker_item(P, MX, W, q);
+                __syncwarp();
+                {  // the window's (at most four) Hamaker terms in slot order, then one compensated add
+                    float wsum[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-                for (int c = 0; c < 3; ++c) ff_acc(acch[c], wsum[c]);
+                    for (int u = 0; u < kWin; ++u)
+                        if ((hbal[u] >> lane) & 1u) {
+                            const int q = hbas[u] + __popc(hbal[u] & lt);
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) wsum[c] += W.hres[q][c];
+                        }
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) ff_acc(acch[c], wsum[c]);
+                }
+                __syncwarp();  // the next window reuses the Hamaker queue
+                k += kWin;
             }
-            while (ccount - cdone >= 32) {
-                contact_item<SL>(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, sl, n, xs, bs);
+            // contact/bond items: full batches of 32 while the round is open, the rest when it
+            // closes (one call site keeps the kernel's code small)
+            while (ccount - cdone >= 32 || (!take && cdone < ccount)) {
+                if (cdone + lane < ccount)
+                    contact_item<SL>(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, sl, n, xs, bs);
                 cdone += 32;
                 __syncwarp();
             }
-            __syncwarp();  // the next window reuses the Hamaker queue
+            if (!take) break;
         }
         const int64_t kend = k;
-        if (cdone + lane < ccount) contact_item<SL>(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, sl, n, xs, bs);
-        __syncwarp();
         // the round's contact and bond pairs, in slot order
         for (int off = 0; off < (int)(kend - kstart); ++off) {
             const uint32_t bc = W.cball[off];
@@ -513,7 +533,7 @@ __global__ void __launch_bounds__(ShapeM<SL>::kWarps * 32, ShapeM<SL>::kMinBlock
     }
     const d3 a_tot = mk3(ff_to_d(acc[0]), ff_to_d(acc[1]), ff_to_d(acc[2]));
     const d3 al_tot = mk3(ff_to_d(accw[0]), ff_to_d(accw[1]), ff_to_d(accw[2]));
-    compact::finish_row(P, S, i, n, a_tot, al_tot, W.vo[lane], W.wo[lane], hdt);
+    compact::finish_row(P, S, i, n, a_tot, al_tot, ld4(S.v, i), ld4(S.w, i), hdt);
 }
 
 template <bool VERLET, int SL>

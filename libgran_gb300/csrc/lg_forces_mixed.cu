@@ -4,7 +4,8 @@
 // operation here is spent where cancellation or accumulation needs it):
 //   FP64  separation x_i - x_j of every pair that can interact, the squared distance and
 //         q = |d|^2 - (2r)^2 (the overlap is -q / (|d| + 2r): its leading digits cancel at
-//         nanometre overlaps), the stored spring vectors xi and their updates, the per-particle
+//         nanometre overlaps), the spring vectors xi and their updates (stored, like every mixed
+//         kernel's springs, as float-float pairs: ffslot_load / ffslot_store), the per-particle
 //         force/torque sums, and the velocity-Verlet integration.
 //   FP32  everything else in the pair: unit normal, relative velocities, normal force, Coulomb
 //         test, torques, the Hamaker bracket (rewritten with two reciprocals).
@@ -221,8 +222,9 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
                     if (bonded || (fl & kXiLive)) {  // springs of a slot that is not live are zero
 #pragma unroll
                         for (int q3 = 0; q3 < 3; ++q3)
-                            s[q3] = mk3(store[(3 * q3) * stride + base], store[(3 * q3 + 1) * stride + base],
-                                        store[(3 * q3 + 2) * stride + base]);
+                            s[q3] = mk3(ffslot_load(store, (3 * q3) * stride + base),
+                                        ffslot_load(store, (3 * q3 + 1) * stride + base),
+                                        ffslot_load(store, (3 * q3 + 2) * stride + base));
                     } else {
                         s[0] = s[1] = s[2] = zero3();
                     }
@@ -239,9 +241,9 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
                                       nrm_ij, overlap, vij0, wfi, tof(wj), s, force, torque);
 #pragma unroll
                     for (int q3 = 0; q3 < 3; ++q3) {
-                        store[(3 * q3) * stride + base] = s[q3].x;
-                        store[(3 * q3 + 1) * stride + base] = s[q3].y;
-                        store[(3 * q3 + 2) * stride + base] = s[q3].z;
+                        ffslot_store(store, (3 * q3) * stride + base, s[q3].x);
+                        ffslot_store(store, (3 * q3 + 1) * stride + base, s[q3].y);
+                        ffslot_store(store, (3 * q3 + 2) * stride + base, s[q3].z);
                     }
                     if (bonded) {
                         if (breaking && fdot(force, force) > (float)(BV.strength[base] * BV.strength[base])) {
@@ -343,14 +345,25 @@ __device__ __forceinline__ void rel_ff(d3 q, double ox, double oy, double oz, co
     x32[n + i] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.0f);
 }
 
-// Float-float copy of the positions relative to the system origin; in a batch every system has
-// its own origin.
-__global__ void positions_to_f32(int64_t n, const dbl4 *__restrict__ x, double ox, double oy, double oz,
-                                 const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig,
-                                 float4 *__restrict__ x32) {
+// Velocity copies of the mixed compacted kernel: v32[i] / v32[n + i] = high / low FP32 parts of v_i,
+// v32[2n + i] = FP32 rounding of omega_i.
+__device__ __forceinline__ void vel_ff(d3 v, d3 w, int64_t i, int64_t n, float4 *__restrict__ v32) {
+    const float hx = (float)v.x, hy = (float)v.y, hz = (float)v.z;
+    v32[i] = make_float4(hx, hy, hz, 0.0f);
+    v32[n + i] = make_float4((float)(v.x - (double)hx), (float)(v.y - (double)hy), (float)(v.z - (double)hz), 0.0f);
+    v32[2 * n + i] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.0f);
+}
+
+// Float-float copies of the positions (relative to the system origin; in a batch every system has
+// its own origin) and of the velocities.
+__global__ void mixed_copies(int64_t n, const dbl4 *__restrict__ x, const dbl4 *__restrict__ v,
+                             const dbl4 *__restrict__ w, double ox, double oy, double oz,
+                             const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig, float4 *__restrict__ x32,
+                             float4 *__restrict__ v32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     rel_ff(ld4(x, i), ox, oy, oz, agg, orig, i, n, x32);
+    vel_ff(ld4(v, i), ld4(w, i), i, n, v32);
 }
 
 // Kick + drift of the mixed path: FP64 integration, then the float-float position copy.
@@ -358,7 +371,7 @@ __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restri
                                  dbl4 *__restrict__ w, const dbl4 *__restrict__ a, const dbl4 *__restrict__ al,
                                  double dt, double hdt, double ox, double oy, double oz,
                                  const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig,
-                                 float4 *__restrict__ x32) {
+                                 float4 *__restrict__ x32, float4 *__restrict__ v32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));
@@ -369,6 +382,7 @@ __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restri
     st4(x, i, xn);
     st4(th, i, add(ld4(th, i), scl(dt, wi)));
     rel_ff(xn, ox, oy, oz, agg, orig, i, n, x32);
+    vel_ff(vi, wi, i, n, v32);
 }
 
 template <int T, bool VERLET>
@@ -404,22 +418,22 @@ void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairV
 #undef LG_CASE
 }
 
-void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, const int32_t *agg, const dbl4 *orig,
-                             float4 *x32, cudaStream_t st) {
+void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const double *origin,
+                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st) {
     const int threads = 256;
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
-    positions_to_f32<<<(unsigned)blocks, threads, 0, st>>>(n, x, origin[0], origin[1], origin[2], agg, orig, x32);
+    mixed_copies<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, w, origin[0], origin[1], origin[2], agg, orig, x32, v32);
 }
 
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
-                             cudaStream_t st) {
+                             float4 *v32, cudaStream_t st) {
     const int threads = 256;
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
     kick_drift_mixed<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt, origin[0], origin[1],
-                                                           origin[2], agg, orig, x32);
+                                                           origin[2], agg, orig, x32, v32);
 }
 
 }  // namespace lg

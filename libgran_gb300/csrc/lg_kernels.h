@@ -50,6 +50,9 @@ struct MixedExtra {
     // remainder (x_i - origin) - x32[i]; hi + lo holds the position to about 2^-48 of its magnitude
     float4 *x32;
     const float4 *x32lo;
+    // [3n] velocities of the force evaluation: v32[i] / v32[n + i] = high / low FP32 parts of v_i,
+    // v32[2n + i] = FP32 rounding of omega_i (compacted kernel's contact and bond pairs)
+    const float4 *v32;
     float near2;      // squared culling radius (FP32 positions); beyond it a pair cannot touch and the
                       // limited Hamaker force is zero
     float contact2f;  // squared contact-candidate radius (FP32 positions, with margin)
@@ -71,13 +74,15 @@ struct MixedExtra {
 bool mixed_available();
 void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
                          double hdt, double dt, int move_facets, const MixedExtra &MX, cudaStream_t st);
-// x32 has 2n entries (high parts, then low parts; see MixedExtra); origin[0..2] is the origin of a
-// single system, orig[] those of each system of a batch
-void launch_positions_to_f32(int64_t n, const dbl4 *x, const double *origin, const int32_t *agg, const dbl4 *orig,
-                             float4 *x32, cudaStream_t st);
+// Float-float copies for the mixed kernels: x32 (2n entries) from the positions, v32 (3n entries)
+// from the velocities and spins (see MixedExtra); origin[0..2] is the origin of a single system,
+// orig[] those of each system of a batch.
+void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const double *origin,
+                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st);
+// Kick + drift of the mixed path; also refreshes x32 and v32.
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
-                             cudaStream_t st);
+                             float4 *v32, cudaStream_t st);
 
 // Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
@@ -94,8 +99,8 @@ void launch_dev4_to_aos(int64_t n, const dbl4 *src, double *aos, cudaStream_t st
 // out: 20 doubles of device memory (column sums, see lg_reduce.cu).
 int64_t obs_scratch_doubles(int64_t n);
 void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
-                        double inertia, double *scratch, double *out, cudaStream_t st);
-void launch_observables_rg(int64_t n, const dbl4 *x, const double *c, double *scratch, double *out, cudaStream_t st);
+                        double inertia, double *scratch, double *out, cudaStream_t st, bool pairs = true);
+void launch_observables_rg(int64_t n, const dbl4 *x, double *scratch, double *out, cudaStream_t st);
 // Per-system observables of a batch: out[s * 20 + c] = column sums over system s's particles
 // (rows from launch_observables' scratch), then column 18 = sum |x - c_s|^2 with centres from
 // centres[3 s ..].

@@ -19,7 +19,8 @@ __device__ __forceinline__ double hamaker_energy(double A, double r, double h) {
 // Per-particle terms. Column layout of a scratch row:
 //  0 e_tot  1 m|v|^2  2 I|w|^2  3-5 v  6-8 I w  9-11 x cross m v  12-14 x  15 potential energy
 //  16 contacts  17 intact bonds
-__global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double m, double I, double *__restrict__ out) {
+__global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double m, double I, int pairs,
+                         double *__restrict__ out) {
     const int64_t n = P.n;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -36,7 +37,7 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
     o[12] = x.x; o[13] = x.y; o[14] = x.z;
     double pe = 0.0, ncont = 0.0, nbond = 0.0;
     const bool ver = P.pairs == LG_PAIRS_VERLET;
-    const int64_t len = ver ? (int64_t)PV.row_len[i] : n - 1;
+    const int64_t len = !pairs ? 0 : ver ? (int64_t)PV.row_len[i] : n - 1;
     const int64_t xs = PV.cap * n, bs = (int64_t)BV.bcap * n;
     for (int64_t k = 0; k < len; ++k) {
         const int64_t e = k * n + i;
@@ -48,9 +49,10 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
             const int64_t be = (int64_t)bond_slot_of(fl) * n + i;
             double dl = 2.0 * P.sinter.r_part - dist;
             u += 0.5 * P.sinter.k * dl * dl;
-            d3 s0 = mk3(BV.xi[0 * bs + be], BV.xi[1 * bs + be], BV.xi[2 * bs + be]);
-            d3 s1 = mk3(BV.xi[3 * bs + be], BV.xi[4 * bs + be], BV.xi[5 * bs + be]);
-            d3 s2 = mk3(BV.xi[6 * bs + be], BV.xi[7 * bs + be], BV.xi[8 * bs + be]);
+            const bool f = P.springs_ff != 0;
+            d3 s0 = mk3(spring_load(BV.xi, 0 * bs + be, f), spring_load(BV.xi, 1 * bs + be, f), spring_load(BV.xi, 2 * bs + be, f));
+            d3 s1 = mk3(spring_load(BV.xi, 3 * bs + be, f), spring_load(BV.xi, 4 * bs + be, f), spring_load(BV.xi, 5 * bs + be, f));
+            d3 s2 = mk3(spring_load(BV.xi, 6 * bs + be, f), spring_load(BV.xi, 7 * bs + be, f), spring_load(BV.xi, 8 * bs + be, f));
             u += 0.5 * P.sinter.k_t * sqn(s0) + 0.5 * P.sinter.k_r * sqn(s1) + 0.5 * P.sinter.k_o * sqn(s2);
             nbond += 1.0;
         } else if (P.binary_model != LG_BINARY_NONE) {
@@ -60,9 +62,10 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
                 ncont += 1.0;
             }
             if (fl & kXiLive) {
-                d3 s0 = mk3(PV.xi[0 * xs + e], PV.xi[1 * xs + e], PV.xi[2 * xs + e]);
-                d3 s1 = mk3(PV.xi[3 * xs + e], PV.xi[4 * xs + e], PV.xi[5 * xs + e]);
-                d3 s2 = mk3(PV.xi[6 * xs + e], PV.xi[7 * xs + e], PV.xi[8 * xs + e]);
+                const bool f = P.springs_ff != 0;
+                d3 s0 = mk3(spring_load(PV.xi, 0 * xs + e, f), spring_load(PV.xi, 1 * xs + e, f), spring_load(PV.xi, 2 * xs + e, f));
+                d3 s1 = mk3(spring_load(PV.xi, 3 * xs + e, f), spring_load(PV.xi, 4 * xs + e, f), spring_load(PV.xi, 5 * xs + e, f));
+                d3 s2 = mk3(spring_load(PV.xi, 6 * xs + e, f), spring_load(PV.xi, 7 * xs + e, f), spring_load(PV.xi, 8 * xs + e, f));
                 u += 0.5 * P.contact.k_t * sqn(s0) + 0.5 * P.contact.k_r * sqn(s1) + 0.5 * P.contact.k_o * sqn(s2);
             }
         }
@@ -81,11 +84,12 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
     o[19] = 0.0;
 }
 
-// |x - c|^2 per particle into column 18.
-__global__ void obs_rg(int64_t n, const dbl4 *__restrict__ x, double cx, double cy, double cz, double *__restrict__ out) {
+// |x - c|^2 per particle into column 18; c = (column sums 12..14) / n, read from device memory.
+__global__ void obs_rg(int64_t n, const dbl4 *__restrict__ x, const double *__restrict__ sums, double *__restrict__ out) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    d3 q = sub(ld4(x, i), mk3(cx, cy, cz));
+    const double nn = (double)n;
+    d3 q = sub(ld4(x, i), mk3(sums[12] / nn, sums[13] / nn, sums[14] / nn));
     out[i * kObs + 18] = dot(q, q);
 }
 
@@ -109,19 +113,20 @@ __global__ void __launch_bounds__(1024) obs_reduce(int64_t n, const double *__re
 
 int64_t obs_scratch_doubles(int64_t n) { return n * kObs; }
 
-// out16 receives the column sums 0..17 and, in 18, sum |x - c|^2 (c from columns 12..14). The
-// caller synchronises the stream before reading out16 (device memory).
+// out receives the column sums 0..17 (the pair columns 15..17 are zero unless `pairs`). The caller
+// synchronises the stream before reading out (device memory).
 void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
-                        double inertia, double *scratch, double *out, cudaStream_t st) {
+                        double inertia, double *scratch, double *out, cudaStream_t st, bool pairs) {
     const int64_t n = P.n;
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    obs_rows<<<blocks, 256, 0, st>>>(P, S, PV, BV, mass, inertia, scratch);
+    obs_rows<<<blocks, 256, 0, st>>>(P, S, PV, BV, mass, inertia, pairs ? 1 : 0, scratch);
     obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 0, 18, out);
 }
 
-void launch_observables_rg(int64_t n, const dbl4 *x, const double *c, double *scratch, double *out, cudaStream_t st) {
+// out[18] = sum |x - c|^2 with c from out[12..14] / n (after launch_observables, same stream).
+void launch_observables_rg(int64_t n, const dbl4 *x, double *scratch, double *out, cudaStream_t st) {
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    obs_rg<<<blocks, 256, 0, st>>>(n, x, c[0], c[1], c[2], scratch);
+    obs_rg<<<blocks, 256, 0, st>>>(n, x, out, scratch);
     obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 18, 19, out);
 }
 

@@ -71,14 +71,14 @@ struct lg_server {
     int32_t backfill = 1;
 };
 
-// Device bytes of one request: state and its ping-pong copies, float-float position copy, pair slots (two
+// Device bytes of one request: state and its ping-pong copies, float-float copies, pair slots (two
 // buffers), bonds, facet springs, list scratch, observables scratch, plus a fixed overhead.
 extern "C" int64_t lg_estimate_device_bytes(const lg_system_desc *d, int64_t n) {
     if (!d || n < 1) return -1;
     const int64_t cap = d->pairs == LG_PAIRS_VERLET ? (d->max_neighbors > 0 ? d->max_neighbors : 64) : std::max<int64_t>(n - 1, 1);
     const int64_t nbuf = d->pairs == LG_PAIRS_VERLET ? 2 : 1;
     int64_t b = 10 * 32 * n;                                  // x, th, v[2], w[2], a, al (+ slack)
-    b += 32 * n;                                              // float-float positions
+    b += 80 * n;                                              // float-float positions, velocities
     b += nbuf * cap * n * (4 + 4 + 72) + nbuf * 4 * n;       // nbr, flags, springs, row lengths
     b += 8 * n * (1 + 1 + 8 + 72);                            // bonds (up to 8 per particle)
     b += 72 * std::max(d->n_facets, 1) * n;                   // facet springs

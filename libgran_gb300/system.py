@@ -95,9 +95,14 @@ class System:
     def reset_acceleration_buffers(self):
         A.check(A.lib().lg_reset_acceleration_buffers(self.h), "lg_reset_acceleration_buffers")
 
-    def observables(self):
+    def observables(self, parts=None):
+        """Observables of the current state; `parts` (LG_OBS_STATE | LG_OBS_PAIRS bits) restricts
+        them, e.g. LG_OBS_STATE skips the pass over the pair slots (potential energy, contacts)."""
         o = A.lg_observables()
-        A.check(A.lib().lg_get_observables(self.h, C.byref(o)), "lg_get_observables")
+        if parts is None:
+            A.check(A.lib().lg_get_observables(self.h, C.byref(o)), "lg_get_observables")
+        else:
+            A.check(A.lib().lg_get_observables_select(self.h, int(parts), C.byref(o)), "lg_get_observables_select")
         return o.as_dict()
 
     def batch_observables(self):

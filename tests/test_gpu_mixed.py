@@ -82,3 +82,30 @@ def test_mixed_breaking_bonds_match_fp64_count():
         s.step(mat.dt, 300)
         res[prec] = len(s.bonds())
     assert abs(res[A.LG_PRECISION_MIXED] - res[A.LG_PRECISION_FP64]) <= max(2, 0.01 * res[A.LG_PRECISION_FP64])
+
+
+@pytest.mark.parametrize("shift_r", [0.5, 1e4], ids=["nearby", "far"])
+def test_mixed_set_positions_translation(shift_r):
+    """lg_set of translated positions: a small shift keeps the float-float origins (and captured
+    graphs), a large one re-derives them; either way the translated system follows the original
+    (the physics is translation invariant) to FP64 rounding of the shifted coordinates."""
+    mat = K.Material()
+    n = 3000
+    x0 = generate_aggregate(21, n, mat.r)
+    v0 = generate_velocities(21, n, 0.1)
+    d = _desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, A.LG_PRECISION_MIXED, mat,
+              A.LG_FORCE_KERNEL_COMPACT)
+    a = System(d, x0, v0)
+    b = System(d, x0, v0)
+    a.step(mat.dt, 40, 20)
+    b.step(mat.dt, 40, 20)  # graphs captured for both
+    shift = np.array([shift_r, -0.5 * shift_r, 0.25 * shift_r]) * mat.r
+    b.set(A.LG_FIELD_X, b.get(A.LG_FIELD_X) + shift)
+    b.update_neighbor_list()
+    a.update_neighbor_list()
+    a.step(mat.dt, 40, 20)
+    b.step(mat.dt, 40, 20)
+    dx = (b.get(A.LG_FIELD_X) - shift) - a.get(A.LG_FIELD_X)
+    assert np.abs(dx).max() <= 1e-6 * mat.r
+    assert H.rel_err(b.get(A.LG_FIELD_A), a.get(A.LG_FIELD_A)) <= 1e-4
+    assert a.device_errors() == 0 and b.device_errors() == 0

@@ -139,6 +139,15 @@ def test_observables_match_oracle():
         assert abs(a[k] - b[k]) <= 1e-10 * max(abs(b[k]), 1e-300), (k, a[k], b[k])
     assert a["n_bonds"] == b["n_bonds"] and a["n_contacts"] == b["n_contacts"]
     assert np.allclose(a["center_of_mass"], b["center_of_mass"], rtol=1e-12, atol=1e-22)
+    # the selectable parts give the same numbers as the full call, and zeros for what was not asked
+    st, pr = s.observables(A.LG_OBS_STATE), s.observables(A.LG_OBS_PAIRS)
+    for k in ("ke_translational", "ke_rotational", "ke_total", "linear_momentum", "angular_momentum",
+              "radius_of_gyration"):
+        assert st[k] == a[k] and pr[k] == 0.0, k
+    assert list(st["center_of_mass"]) == list(a["center_of_mass"])
+    assert pr["potential_energy"] == a["potential_energy"] and st["potential_energy"] == 0.0
+    assert pr["n_contacts"] == a["n_contacts"] and pr["n_bonds"] == a["n_bonds"] and st["n_bonds"] == 0
+    assert st["n_bonds_initial"] == pr["n_bonds_initial"] == a["n_bonds_initial"]
 
 
 def test_results_are_deterministic():
