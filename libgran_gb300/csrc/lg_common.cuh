@@ -110,6 +110,12 @@ struct PairView {
     double *xi;         // [9][cap * n] contact springs, component-major (8-byte slots: FP64 values,
                         // or float-float pairs when Params::springs_ff is set)
     int64_t cap;        // slots per row
+    // Contact candidates of each row (mixed precision, Verlet mode; null otherwise): the slots whose
+    // pair was within the near radius (contact reach + Verlet skin) at the last build, or bonded,
+    // in ascending slot order: entry m of row i at m * n + i.
+    int32_t *near_j;    // [cap * n] partner
+    uint8_t *near_k;    // [cap * n] slot in the row
+    int32_t *near_len;  // [n]
 };
 
 struct BondView {

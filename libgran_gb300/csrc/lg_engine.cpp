@@ -353,8 +353,13 @@ void lg_system::release() {
     for (void *p : allocations) cudaFree(p);
     allocations.clear();
     if (stream) cudaStreamDestroy(stream);
+    if (side) cudaStreamDestroy(side);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
+    side = nullptr;
+    fork_ev = join_ev = nullptr;
     for (cudaEvent_t e : tev) cudaEventDestroy(e);
     tev.clear();
     stream = nullptr;
@@ -390,7 +395,8 @@ static int rebuild_list(lg_system *s) {
     PairView o = oldv;
     if (!s->list_built) o.row_len = nullptr;
     BatchView B{s->d_agg, s->d_hoff};
-    launch_list_build(s->P.n, s->x, B, s->P.r_verlet, s->max_cells, s->ls, o, newv, s->bv, s->err, s->stream);
+    launch_list_build(s->P.n, s->x, B, s->P.r_verlet, s->r_near, s->max_cells, s->ls, o, newv, s->bv, s->err,
+                      s->stream);
     s->launches += 7;
     s->pcur = 1 - s->pcur;
     s->list_built = true;
@@ -432,9 +438,11 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets) {
         s->tev_used += 2;
     }
     const bool compact = s->kernel == LG_FORCE_KERNEL_COMPACT;
+    int kernels = 1;
     if (s->precision == LG_PRECISION_MIXED) {
         if (compact)
-            launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
+            kernels = launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream,
+                                                  s->side, s->fork_ev, s->join_ev);
         else
             launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
     } else {
@@ -443,7 +451,7 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets) {
         else
             launch_forces_fp64(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
     }
-    s->launches += 1;
+    s->launches += kernels;
     LG_CUDA(cudaGetLastError());
     if (stop_ev) LG_CUDA(cudaEventRecord(stop_ev, s->stream));
     return LG_OK;
@@ -728,6 +736,17 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     } else {
         int64_t cap = d->max_neighbors > 0 ? d->max_neighbors : 48;
         cap = std::min<int64_t>(cap, std::max<int64_t>(n - 1, 1));
+        // mixed precision: contact candidates are listed per row at each build (PairView::near_*),
+        // within the contact reach plus the Verlet skin (the list radius minus the largest
+        // interaction radius); without a Hamaker cutoff the skin is unknown and every slot is near
+        if (s->precision == LG_PRECISION_MIXED && d->binary_model != LG_BINARY_NONE) {
+            const double creach = std::max(d->binary_model == LG_BINARY_CONTACT ? 2.0 * d->contact.r_part : 0.0,
+                                           sinter ? std::max(2.0 * d->sinter.r_part, 2.0 * d->contact.r_part) : 0.0);
+            double reach = creach;
+            if (d->hamaker_model == LG_HAMAKER_LIMITED) reach = std::max(reach, d->hamaker.r_cutoff);
+            const bool capped = d->hamaker_model == LG_HAMAKER_NONE || d->hamaker_model == LG_HAMAKER_LIMITED;
+            s->r_near = capped ? std::min(d->r_verlet, creach + std::max(d->r_verlet - reach, 0.0)) : d->r_verlet;
+        }
         auto alloc_rows = [&](int64_t c) -> int {
             for (int q = 0; q < 2; ++q) {
                 PairView &pv = s->pv[q];
@@ -737,6 +756,12 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
                 LG_TRY(s->alloc(&pv.flags, (size_t)(c * n)));
                 LG_TRY(s->alloc(&pv.xi, 9 * (size_t)(c * n)));
                 LG_CUDA(cudaMemset(pv.row_len, 0, sizeof(int32_t) * n));
+                if (s->r_near > 0) {
+                    LG_TRY(s->alloc(&pv.near_j, (size_t)(c * n)));
+                    LG_TRY(s->alloc(&pv.near_k, (size_t)(c * n)));
+                    LG_TRY(s->alloc(&pv.near_len, (size_t)n));
+                    LG_CUDA(cudaMemset(pv.near_len, 0, sizeof(int32_t) * n));
+                }
             }
             return LG_OK;
         };
@@ -763,8 +788,9 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         if (d->max_neighbors == 0 && want > cap && cap < std::max<int64_t>(n - 1, 1)) {
             for (int q = 0; q < 2; ++q) {
                 PairView &pv = s->pv[q];
-                void *old_ptrs[4] = {pv.nbr, pv.row_len, pv.flags, pv.xi};
+                void *old_ptrs[7] = {pv.nbr, pv.row_len, pv.flags, pv.xi, pv.near_j, pv.near_k, pv.near_len};
                 for (void *o : old_ptrs) {
+                    if (!o) continue;
                     cudaFree(o);
                     s->allocations.erase(std::find(s->allocations.begin(), s->allocations.end(), o));
                 }
@@ -783,6 +809,10 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     if (s->precision == LG_PRECISION_MIXED) {
         LG_TRY(s->alloc(&s->x32, 2 * (size_t)n));  // float-float: high parts, then low parts
         LG_TRY(s->alloc(&s->v32, 3 * (size_t)n));  // v high parts, v low parts, spins
+        LG_TRY(s->alloc(&s->hsum, (size_t)n));
+        LG_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+        LG_CUDA(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
+        LG_CUDA(cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming));
         if (s->n_systems > 0) LG_TRY(s->alloc(&s->d_orig, (size_t)s->n_systems));
         s->r_max = std::max(d->contact.r_part, std::max(d->sinter.r_part, d->hamaker.r_part));
         LG_TRY(set_mixed_origins(s, x0));
@@ -797,6 +827,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         s->mx.x32 = s->x32;
         s->mx.x32lo = s->x32 + n;
         s->mx.v32 = s->v32;
+        s->mx.hsum = s->hsum;
         double cnear = 0.0;
         if (d->binary_model != LG_BINARY_NONE) cnear = std::max(cnear, 2.0 * d->contact.r_part);
         if (sinter) cnear = std::max(cnear, 2.0 * d->sinter.r_part);
@@ -1373,6 +1404,11 @@ static int snapshot_take(lg_system *s) {
             if (pv.row_len) addb(pv.row_len, sizeof(int32_t) * n);
             addb(pv.flags, sizeof(uint32_t) * slots);
             addb(pv.xi, sizeof(double) * 9 * slots);
+            if (pv.near_len) {
+                addb(pv.near_j, sizeof(int32_t) * slots);
+                addb(pv.near_k, slots);
+                addb(pv.near_len, sizeof(int32_t) * n);
+            }
         }
         const size_t bs = (size_t)s->bv.bcap * (size_t)n;
         addb(s->bv.intact, bs);

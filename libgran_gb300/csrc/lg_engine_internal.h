@@ -11,6 +11,10 @@ struct lg_system {
     int device = -1;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // mixed precision: a second stream on which the contact kernel runs beside the Hamaker kernel
+    // (fork / join events on the handle's stream; captured into the step graphs as two branches)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     lg_system_desc desc{};
     lg::Params P{};
     int precision = LG_PRECISION_FP64;
@@ -42,9 +46,11 @@ struct lg_system {
     // mixed precision: FP32 position copy for culling
     float4 *x32 = nullptr;  // mixed: [2n] float-float positions
     float4 *v32 = nullptr;  // mixed: [3n] float-float velocities, FP32 spins
+    lg::dbl4 *hsum = nullptr;  // mixed: [n] Hamaker part of the accelerations
     double origin[4] = {0.0, 0.0, 0.0, 0.0};  // mixed: origin of the float-float positions, extent in [3]
     double r_max = 0.0;                        // mixed: largest particle radius of the functors
     double ext_max = 0.0;                      // mixed: largest extent of a system about its origin
+    double r_near = 0.0;                       // mixed, Verlet: radius of the contact-candidate lists
     double cull_near = 0.0, cull_contact = 0.0;  // mixed: culling radii before margins
     lg::MixedExtra mx{};
 

@@ -1,33 +1,35 @@
-// lg_forces_compact_mixed.cu -- warp-compacted force kernel, mixed precision (sm_103a).
+// lg_forces_compact_mixed.cu -- force evaluation of the mixed-precision path (sm_103a): two
+// warp-compacted kernels, one lane per row (particle i), slot layout and flags shared with the FP64
+// path.
 //
-// Same row/slot layout and division of work as the FP64 compacted kernel (lg_forces_compact.cu):
-// one lane per row, slots taken in windows of four, contact/bond pairs queued per warp and
-// evaluated 32 at a time. What the precision changes:
-//  * positions come as float-float pairs (MixedExtra::x32 / x32lo, hi + lo = x - origin); a pair's
-//    separation and q = |d|^2 - (2r)^2 are formed with error-free FP32 transformations
-//    (separation_ff), so a Hamaker pair costs no FP64 operation at all and its surface gap keeps
-//    FP32 relative precision however small it is;
-//  * the owner lane gathers both halves of its partners' positions while it classifies a window,
-//    and the window's Hamaker pairs are evaluated right away, one pair per lane, from those
-//    shared-memory copies: one global round trip per window for the partners' data;
-//  * the next window's partner indices and flags are loaded while the current one is evaluated;
-//  * per-row sums are float-float FP32 accumulations (compensated, about 2^-44 relative): one for
-//    the Hamaker pairs, to which each window adds its (up to four) terms summed in FP32 in slot
-//    order as the window completes, and one each for the linear
-//    and angular accelerations of the contact/bond pairs, folded in slot order at the end of each
-//    round; the sums become FP64 once per row. Each sum's order depends only on the row itself, not
-//    on which rows share its warp, so a system gives the same bits alone and inside a batch;
-//  * contact and bond pairs read float-float copies of the velocities (MixedExtra::v32) and keep
-//    their spring vectors as float-float pairs in the 8-byte spring slots, updated by FP32
-//    increments (shear_ff): no FP64 operation in any pair.
-// For launches with few rows the windows of a row are sliced over SL warps (slot_of), each slice
-// keeping its own partial sums, which are combined in slice order at the end.
+//   forces_contacts_mixed  contact and bond pairs. Verlet mode walks each row's contact candidates
+//                          (PairView::near_*, listed by the list build: the slots within contact
+//                          reach plus the Verlet skin, and bonded slots); all-pairs mode walks every
+//                          slot. Candidates are queued per warp (ballot order) and evaluated 32 at a
+//                          time; the pair's linear and angular accelerations are folded per row in
+//                          slot order and stored to a / alpha as the contact part of the sums.
+//   forces_hamaker_mixed   Hamaker pairs over all slots, in windows of four slots: the owner lane
+//                          gathers its partners' float-float positions, the window's Hamaker pairs
+//                          are evaluated one per lane from those shared-memory copies, the next
+//                          window's partners are loaded meanwhile. For launches with few rows a
+//                          row's windows are sliced over SL warps, whose partial sums are combined
+//                          in slice order. Runs beside forces_contacts_mixed (two streams).
+//   forces_finish_mixed    per particle: contact part + Hamaker part, facet terms, stores, half kick.
+//
+// Precision: positions come as float-float pairs (MixedExtra::x32 / x32lo, hi + lo = x - origin) and
+// a pair's separation and q = |d|^2 - (2r)^2 are formed with error-free FP32 transformations
+// (separation_ff), so the surface gap and the overlap keep FP32 relative precision however small
+// they are; velocities come as float-float copies (MixedExtra::v32); springs are float-float pairs
+// in the 8-byte spring slots, updated by FP32 increments (shear_ff). No pair costs an FP64
+// operation. Per-row sums are float-float (compensated) FP32 accumulations in an order fixed by
+// the row alone, so a system gives the same bits alone and inside a batch (with the same slicing).
 #include <cstddef>
 
 #include "lg_compact.cuh"
 #include "lg_kernels.h"
 
-// Slices per row group: 0 chooses from the launch size (compile-time override for tuning).
+// Slices per row group of the Hamaker kernel: 0 chooses from the launch size (compile-time
+// override for tuning).
 #ifndef LG_MIXED_SLICES
 #define LG_MIXED_SLICES 0
 #endif
@@ -40,34 +42,42 @@ using compact::kHCap;
 using compact::kWin;
 using compact::slot_of;
 
-constexpr int kRound = 64;  // virtual slots classified per round (per warp)
-constexpr int kCCap = 160;  // contact queue capacity per round (>= 32 * kWin + 31)
-
-template <int SL>
-struct ShapeM {
-    static constexpr int kSlices = SL;
-    static constexpr int kRowWarps = SL == 1 ? 2 : 1;  // 32-row groups per block
-    static constexpr int kWarps = kSlices * kRowWarps;
-    // blocks per SM that the 128-register budget allows (shared memory allows as many)
-    static constexpr int kMinBlocks = 65536 / (kWarps * 32 * 128);
-};
-
-struct WarpSmemM {
-    float4 hhi[kHCap];     // queued Hamaker partners: high part of the position, w = owner lane
-    float4 hlo[kHCap];     // low part of the position
-    float hres[kHCap][3];  // their accelerations
-    float cres[kCCap][6];  // contact/bond results: linear and angular acceleration
-    int32_t cj[kCCap];
-    uint16_t cown[kCCap];  // (owner lane << 8) | virtual slot offset within the round
-    uint32_t cball[kRound];
-    int32_t cbase[kRound];
+// ---- contact / bond kernel ----
+constexpr int kCRound = 32;  // entries per lane classified per round
+constexpr int kCQ = 64;      // contact queue capacity (>= 32 + 31)
+constexpr int kCWarps = 2;   // warps per block
+#ifndef LG_CONTACT_LANES
+#define LG_CONTACT_LANES 4   // lanes per row (compile-time override for tuning)
+#endif
+constexpr int kContactLanes = LG_CONTACT_LANES;
+struct ContactSmem {
+    float cres[kCQ][6];  // results: linear and angular acceleration
+    int32_t cj[kCQ];     // partner
+    int32_t ck[kCQ];     // slot in the owner's row
+    uint8_t cown[kCQ];   // owner lane
+    uint32_t cball[kCRound];
+    int32_t cbase[kCRound];
     float4 xh[32], xl[32];  // the rows' own positions (float-float)
     float4 vh[32], vl[32];  // the rows' own velocities (float-float)
     float4 wh[32];          // the rows' own spins (FP32)
 };
-static_assert(offsetof(WarpSmemM, hlo) == sizeof(WarpSmemM::hhi) &&
-                  sizeof(WarpSmemM::hhi) + sizeof(WarpSmemM::hlo) >= 18 * 32 * sizeof(float),
-              "slice partial sums reuse the Hamaker queue (hhi, hlo)");
+
+// ---- Hamaker kernel ----
+template <int SL>
+struct ShapeH {
+    static constexpr int kSlices = SL;
+    static constexpr int kRowWarps = SL == 1 ? 2 : 1;  // 32-row groups per block
+    static constexpr int kWarps = kSlices * kRowWarps;
+    // blocks per SM that a 96-register budget allows (shared memory allows as many)
+    static constexpr int kMinBlocks = 65536 / (kWarps * 32 * 96);
+};
+struct HamakerSmem {
+    float4 hhi[kHCap];     // queued Hamaker partners: high part of the position, w = owner lane
+    float4 hlo[kHCap];     // low part of the position
+    float hres[kHCap][3];  // their accelerations
+    float4 xh[32], xl[32];  // the rows' own positions (float-float)
+};
+static_assert(sizeof(HamakerSmem::hhi) >= 6 * 32 * sizeof(float), "slice partial sums reuse hhi");
 
 struct f3 {
     float x, y, z;
@@ -194,15 +204,12 @@ __device__ __forceinline__ SepFF separation_ff(float4 hi, float4 lo, float4 hj, 
     return SepFF{fm(tx.hi + lx, ty.hi + ly, tz.hi + lz), s3 + rest};
 }
 
-// One queued contact / bond pair: owner row io (lane own of the warp), slot e, partner j. Writes the
-// pair's linear and angular accelerations (force over mass, torque over moment of inertia).
-template <int SL>
-__device__ __forceinline__ void contact_item(const Params &P, const StateView &S, const PairView &PV,
-                                             const BondView &BV, const MixedExtra &M, WarpSmemM &W, int q,
-                                             int64_t row0, int64_t kstart, int sl, int64_t n, int64_t xs, int64_t bs) {
-    const int own = W.cown[q] >> 8;
+__device__ __forceinline__ void contact_item(const Params &P, const PairView &PV, const BondView &BV,
+                                             const MixedExtra &M, ContactSmem &W, int q, int64_t row0, int64_t n,
+                                             int64_t xs, int64_t bs) {
+    const int own = W.cown[q];
     const int64_t io = row0 + own;
-    const int64_t e = slot_of<SL>(kstart + (W.cown[q] & 0xff), sl) * n + io;
+    const int64_t e = (int64_t)W.ck[q] * n + io;
     const int32_t j = W.cj[q];
     const uint32_t fl = PV.flags[e];
     const bool bonded = (fl & kBonded) != 0;
@@ -290,7 +297,7 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
 
 // One queued Hamaker pair (hamaker_force.h:28-44; limited form hamaker_force.h:86-93): partner
 // position from the queue, owner position from the warp's row data.
-__device__ __forceinline__ void hamaker_item(const Params &P, const MixedExtra &M, WarpSmemM &W, int q) {
+__device__ __forceinline__ void hamaker_item(const Params &P, const MixedExtra &M, HamakerSmem &W, int q) {
     const float4 ph = W.hhi[q];
     const int own = __float_as_int(ph.w);
     const SepFF sp = separation_ff(W.xh[own], W.xl[own], ph, W.hlo[q], M.h_fr_hi, M.h_fr_lo);
@@ -309,180 +316,116 @@ __device__ __forceinline__ void hamaker_item(const Params &P, const MixedExtra &
     W.hres[q][2] = a.z;
 }
 
+
 }  // namespace
 
-template <bool VERLET, int SL>
-__global__ void __launch_bounds__(ShapeM<SL>::kWarps * 32, ShapeM<SL>::kMinBlocks)
-    forces_compact_mixed(Params P, StateView S, PairView PV, BondView BV, double hdt, double dt, int move_facets,
-                         MixedExtra MX) {
+// Contact and bond pairs of rows row0 .. row0 + 32/T - 1: T lanes per row, lane t of a row taking
+// its entries t, t + T, ... (so short candidate lists still fill the warp); each lane folds its
+// pairs in entry order and the row's T partial sums are combined in lane order. a[i], alpha[i]
+// receive the contact part of the row's accelerations.
+template <bool NEAR, int T>
+__global__ void __launch_bounds__(kCWarps * 32, 8)
+    forces_contacts_mixed(Params P, StateView S, PairView PV, BondView BV, MixedExtra MX) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int kSlices = ShapeM<SL>::kSlices, kRowWarps = ShapeM<SL>::kRowWarps;
+    constexpr int kRows = 32 / T;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    WarpSmemM *Wall = reinterpret_cast<WarpSmemM *>(smem_raw);
-    WarpSmemM &W = Wall[warp];
-    const int rw = warp / kSlices, sl = warp % kSlices;  // row group of the block, slice of it
+    const int r = lane / T, sub = lane % T;  // local row and sub-lane
+    ContactSmem &W = reinterpret_cast<ContactSmem *>(smem_raw)[warp];
     const int64_t n = P.n;
-    const int64_t row0 = ((int64_t)blockIdx.x * kRowWarps + rw) * 32;
-    const int64_t i = row0 + lane;
+    const int64_t row0 = ((int64_t)blockIdx.x * kCWarps + warp) * kRows;
+    const int64_t i = row0 + r;
     const bool active = i < n;
-    const int hm = P.hamaker_model;
-    const bool contacts_on = P.binary_model != LG_BINARY_NONE;
     const uint32_t lt = (1u << lane) - 1u;
-
-    if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
-
     int64_t len = 0;
     float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f);
-    {
-        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 lo_i = z4, vh = z4, vl = z4, wh = z4;
-        if (active) {
-            len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
-            hi_i = MX.x32[i];
-            lo_i = MX.x32lo[i];
-            vh = MX.v32[i];
-            vl = MX.v32[n + i];
-            wh = MX.v32[2 * n + i];
-        }
-        W.xh[lane] = hi_i;
-        W.xl[lane] = lo_i;
-        W.vh[lane] = vh;
-        W.vl[lane] = vl;
-        W.wh[lane] = wh;
+    if (active) {
+        len = NEAR ? (int64_t)PV.near_len[i] : n - 1;
+        hi_i = MX.x32[i];
     }
-    const int64_t maxlen = (int64_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
-    // this warp's windows: sl, sl + kSlices, ...; virtual slot v maps to slot_of<SL>(v, sl)
-    const int64_t nwin = (maxlen + kWin - 1) / kWin;
-    const int64_t mywin = nwin > sl ? (nwin - sl + kSlices - 1) / kSlices : 0;
-    const int64_t vmax = mywin * kWin;
+    if (sub == 0) {
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        W.xh[r] = hi_i;
+        W.xl[r] = active ? MX.x32lo[i] : z4;
+        W.vh[r] = active ? MX.v32[i] : z4;
+        W.vl[r] = active ? MX.v32[n + i] : z4;
+        W.wh[r] = active ? MX.v32[2 * n + i] : z4;
+    }
+    // iterations: the lane's entries sub, sub + T, ... below len
+    const int64_t my_it = len > sub ? (len - sub + T - 1) / T : 0;
+    const int64_t itmax = (int64_t)__reduce_max_sync(0xffffffffu, (unsigned)my_it);
     const int64_t xs = PV.cap * n;
     const int64_t bs = (int64_t)BV.bcap * n;
     ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accw[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    ff acch[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     __syncwarp();
 
-    // partner and flags of the lane's row in the window at virtual slot v (-1: past the row's end)
-    int32_t jn[kWin];
-    uint32_t fn[kWin];
-    auto load_window = [&](int64_t v) {
-        const int64_t k0 = slot_of<SL>(v, sl);
-#pragma unroll
-        for (int u = 0; u < kWin; ++u) {
-            const int64_t kk = k0 + u;
-            jn[u] = -1;
-            fn[u] = 0;
-            if (kk < len) {
-                const int64_t e = kk * n + i;
-                jn[u] = VERLET ? PV.nbr[e] : (int32_t)(kk < i ? kk : kk + 1);
-                fn[u] = PV.flags[e];
+    // entry of iteration it: partner and slot (-1: none); the next one is loaded while the
+    // current one is classified
+    int32_t jn = -1, kn = 0;
+    auto load_entry = [&](int64_t it) {
+        const int64_t m = it * T + sub;
+        jn = -1;
+        if (m < len) {
+            if (NEAR) {
+                jn = PV.near_j[m * n + i];
+                kn = PV.near_k[m * n + i];
+            } else {
+                kn = (int32_t)m;
+                jn = (int32_t)(m < i ? m : m + 1);
             }
         }
     };
-    if (vmax > 0) load_window(0);
-
-    for (int64_t kstart = 0; kstart < vmax;) {
+    if (itmax > 0) load_entry(0);
+    for (int64_t it0 = 0; it0 < itmax;) {
         int ccount = 0, cdone = 0;
-        int64_t k = kstart;
+        int64_t it = it0;
         for (;;) {
-            const bool take = k < vmax && k - kstart + kWin <= kRound && ccount + 32 * kWin <= kCCap;
+            const bool take = it < itmax && it - it0 < kCRound && ccount + 32 <= kCQ;
             if (take) {
-                int32_t jg[kWin];
-                uint32_t fg[kWin];
-                float4 ph[kWin], pl[kWin];
-#pragma unroll
-                for (int u = 0; u < kWin; ++u) {
-                    jg[u] = jn[u];
-                    fg[u] = fn[u];
+                const int32_t j = jn, k = kn;
+                uint32_t fl = 0;
+                float4 pj = hi_i;
+                if (j >= 0) {
+                    fl = PV.flags[(int64_t)k * n + i];
+                    pj = MX.x32[j];
                 }
+                if (it + 1 < itmax) load_entry(it + 1);
+                bool cb = false;
+                if (j >= 0) {
+                    const float dx = hi_i.x - pj.x, dy = hi_i.y - pj.y, dz = hi_i.z - pj.z;
+                    if ((fl & kBonded) || fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= MX.contact2f) {
+                        cb = true;
+                    } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+                        const int64_t e = (int64_t)k * n + i;
 #pragma unroll
-                for (int u = 0; u < kWin; ++u) {
-                    ph[u] = hi_i;
-                    pl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (jg[u] >= 0) {
-                        ph[u] = MX.x32[jg[u]];
-                        if (hm != LG_HAMAKER_NONE) pl[u] = MX.x32lo[jg[u]];
+                        for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+                        PV.flags[e] = fl & ~kXiLive;
                     }
                 }
-                if (k + kWin < vmax) load_window(k + kWin);  // next window, in flight during this one
-                const int64_t k0 = slot_of<SL>(k, sl);
-                int hcount = 0;
-                uint32_t hbal[kWin];
-                int hbas[kWin];
-#pragma unroll
-                for (int u = 0; u < kWin; ++u) {
-                    const int off = (int)(k - kstart) + u;  // virtual slot offset within the round
-                    bool hb = false, cb = false;
-                    if (jg[u] >= 0) {
-                        const uint32_t fl = fg[u];
-                        const float dxf = hi_i.x - ph[u].x, dyf = hi_i.y - ph[u].y, dzf = hi_i.z - ph[u].z;
-                        const float d2f = fmaf(dzf, dzf, fmaf(dyf, dyf, dxf * dxf));
-                        if (hm == LG_HAMAKER_LIMITED)
-                            hb = d2f <= MX.near2;
-                        else if (hm != LG_HAMAKER_NONE)
-                            hb = true;
-                        if (contacts_on) {
-                            if ((fl & kBonded) || d2f <= MX.contact2f) {
-                                cb = true;
-                            } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
-                                const int64_t e = (k0 + u) * n + i;
-#pragma unroll
-                                for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
-                                PV.flags[e] = fl & ~kXiLive;
-                            }
-                        }
-                    }
-                    const uint32_t bc = __ballot_sync(0xffffffffu, cb);
-                    const uint32_t bh = __ballot_sync(0xffffffffu, hb);
-                    if (cb) {
-                        const int q = ccount + __popc(bc & lt);
-                        W.cj[q] = jg[u];
-                        W.cown[q] = (uint16_t)((lane << 8) | off);
-                    }
-                    if (hb) {
-                        const int q = hcount + __popc(bh & lt);
-                        W.hhi[q] = make_float4(ph[u].x, ph[u].y, ph[u].z, __int_as_float(lane));
-                        W.hlo[q] = pl[u];
-                    }
-                    if (lane == 0) {
-                        W.cball[off] = bc;
-                        W.cbase[off] = ccount;
-                    }
-                    hbal[u] = bh;
-                    hbas[u] = hcount;
-                    ccount += __popc(bc);
-                    hcount += __popc(bh);
+                const uint32_t bc = __ballot_sync(0xffffffffu, cb);
+                if (cb) {
+                    const int q = ccount + __popc(bc & lt);
+                    W.cj[q] = j;
+                    W.ck[q] = k;
+                    W.cown[q] = (uint8_t)r;
                 }
-                __syncwarp();
-                for (int q = lane; q < hcount; q += 32) hamaker_item(P, MX, W, q);
-                __syncwarp();
-                {  // the window's (at most four) Hamaker terms in slot order, then one compensated add
-                    float wsum[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-                    for (int u = 0; u < kWin; ++u)
-                        if ((hbal[u] >> lane) & 1u) {
-                            const int q = hbas[u] + __popc(hbal[u] & lt);
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) wsum[c] += W.hres[q][c];
-                        }
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) ff_acc(acch[c], wsum[c]);
+                if (lane == 0) {
+                    W.cball[it - it0] = bc;
+                    W.cbase[it - it0] = ccount;
                 }
-                __syncwarp();  // the next window reuses the Hamaker queue
-                k += kWin;
+                ccount += __popc(bc);
+                ++it;
             }
-            // contact/bond items: full batches of 32 while the round is open, the rest when it
-            // closes (one call site keeps the kernel's code small)
+            __syncwarp();
+            // full batches of 32 while the round is open, the rest when it closes
             while (ccount - cdone >= 32 || (!take && cdone < ccount)) {
-                if (cdone + lane < ccount)
-                    contact_item<SL>(P, S, PV, BV, MX, W, cdone + lane, row0, kstart, sl, n, xs, bs);
+                if (cdone + lane < ccount) contact_item(P, PV, BV, MX, W, cdone + lane, row0, n, xs, bs);
                 cdone += 32;
                 __syncwarp();
             }
             if (!take) break;
         }
-        const int64_t kend = k;
-        // the round's contact and bond pairs, in slot order
-        for (int off = 0; off < (int)(kend - kstart); ++off) {
+        // the round's pairs, in entry order
+        for (int off = 0; off < (int)(it - it0); ++off) {
             const uint32_t bc = W.cball[off];
             if ((bc >> lane) & 1u) {
                 const int q = W.cbase[off] + __popc(bc & lt);
@@ -494,21 +437,148 @@ __global__ void __launch_bounds__(ShapeM<SL>::kWarps * 32, ShapeM<SL>::kMinBlock
             }
         }
         __syncwarp();
-        kstart = kend;
+        it0 = it;
+    }
+    if (T > 1) {  // the row's partial sums, in lane order, onto its first lane
+        const int base = lane - sub;
+#pragma unroll
+        for (int t = 1; t < T; ++t) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float ah = __shfl_sync(0xffffffffu, acc[c].hi, base + t);
+                const float al = __shfl_sync(0xffffffffu, acc[c].lo, base + t);
+                const float wh = __shfl_sync(0xffffffffu, accw[c].hi, base + t);
+                const float wl = __shfl_sync(0xffffffffu, accw[c].lo, base + t);
+                if (sub == 0) {
+                    ff_acc(acc[c], ah);
+                    ff_acc(acc[c], al);
+                    ff_acc(accw[c], wh);
+                    ff_acc(accw[c], wl);
+                }
+            }
+        }
+    }
+    if (!active || sub != 0) return;
+    st4(S.a, i, mk3(ff_to_d(acc[0]), ff_to_d(acc[1]), ff_to_d(acc[2])));
+    st4(S.al, i, mk3(ff_to_d(accw[0]), ff_to_d(accw[1]), ff_to_d(accw[2])));
+}
+
+// Hamaker pairs of rows row0 .. row0 + 31; hsum[i] receives the Hamaker part of the row's
+// acceleration.
+template <bool VERLET, int SL>
+__global__ void __launch_bounds__(ShapeH<SL>::kWarps * 32, ShapeH<SL>::kMinBlocks)
+    forces_hamaker_mixed(Params P, PairView PV, MixedExtra MX) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int kSlices = ShapeH<SL>::kSlices, kRowWarps = ShapeH<SL>::kRowWarps;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    HamakerSmem *Wall = reinterpret_cast<HamakerSmem *>(smem_raw);
+    HamakerSmem &W = Wall[warp];
+    const int rw = warp / kSlices, sl = warp % kSlices;  // row group of the block, slice of it
+    const int64_t n = P.n;
+    const int64_t row0 = ((int64_t)blockIdx.x * kRowWarps + rw) * 32;
+    const int64_t i = row0 + lane;
+    const bool active = i < n;
+    const int hm = P.hamaker_model;
+    const uint32_t lt = (1u << lane) - 1u;
+
+    int64_t len = 0;
+    float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f);
+    {
+        float4 lo_i = hi_i;
+        if (active) {
+            len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
+            hi_i = MX.x32[i];
+            lo_i = MX.x32lo[i];
+        }
+        W.xh[lane] = hi_i;
+        W.xl[lane] = lo_i;
+    }
+    const int64_t maxlen = (int64_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
+    // this warp's windows: sl, sl + kSlices, ...; virtual slot v maps to slot_of<SL>(v, sl)
+    const int64_t nwin = (maxlen + kWin - 1) / kWin;
+    const int64_t mywin = nwin > sl ? (nwin - sl + kSlices - 1) / kSlices : 0;
+    const int64_t vmax = mywin * kWin;
+    ff acch[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    __syncwarp();
+
+    // partners of the lane's row in the window at virtual slot v (-1: past the row's end)
+    int32_t jn[kWin];
+    auto load_window = [&](int64_t v) {
+        const int64_t k0 = slot_of<SL>(v, sl);
+#pragma unroll
+        for (int u = 0; u < kWin; ++u) {
+            const int64_t kk = k0 + u;
+            jn[u] = -1;
+            if (kk < len) jn[u] = VERLET ? PV.nbr[kk * n + i] : (int32_t)(kk < i ? kk : kk + 1);
+        }
+    };
+    if (vmax > 0) load_window(0);
+
+    for (int64_t k = 0; k < vmax; k += kWin) {
+        int32_t jg[kWin];
+        float4 ph[kWin], pl[kWin];
+#pragma unroll
+        for (int u = 0; u < kWin; ++u) jg[u] = jn[u];
+#pragma unroll
+        for (int u = 0; u < kWin; ++u) {
+            ph[u] = hi_i;
+            pl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (jg[u] >= 0) {
+                ph[u] = MX.x32[jg[u]];
+                pl[u] = MX.x32lo[jg[u]];
+            }
+        }
+        if (k + kWin < vmax) load_window(k + kWin);  // next window, in flight during this one
+        int hcount = 0;
+        uint32_t hbal[kWin];
+        int hbas[kWin];
+#pragma unroll
+        for (int u = 0; u < kWin; ++u) {
+            bool hb = false;
+            if (jg[u] >= 0) {
+                if (hm == LG_HAMAKER_LIMITED) {
+                    const float dx = hi_i.x - ph[u].x, dy = hi_i.y - ph[u].y, dz = hi_i.z - ph[u].z;
+                    hb = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= MX.near2;
+                } else {
+                    hb = true;
+                }
+            }
+            const uint32_t bh = __ballot_sync(0xffffffffu, hb);
+            if (hb) {
+                const int q = hcount + __popc(bh & lt);
+                W.hhi[q] = make_float4(ph[u].x, ph[u].y, ph[u].z, __int_as_float(lane));
+                W.hlo[q] = pl[u];
+            }
+            hbal[u] = bh;
+            hbas[u] = hcount;
+            hcount += __popc(bh);
+        }
+        __syncwarp();
+        for (int q = lane; q < hcount; q += 32) hamaker_item(P, MX, W, q);
+        __syncwarp();
+        {  // the window's (at most four) terms in slot order, then one compensated add
+            float wsum[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int u = 0; u < kWin; ++u)
+                if ((hbal[u] >> lane) & 1u) {
+                    const int q = hbas[u] + __popc(hbal[u] & lt);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) wsum[c] += W.hres[q][c];
+                }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ff_acc(acch[c], wsum[c]);
+        }
+        __syncwarp();  // the next window reuses the queue
     }
 
     if (kSlices > 1) {
         // combine the slices' partial sums of each row in slice order (fixed, deterministic); each
-        // warp parks its partials in its own Hamaker queue (hhi, hlo), which is no longer in use
+        // warp parks its partials in its own queue, which is no longer in use
         float *mine = reinterpret_cast<float *>(W.hhi);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            mine[(2 * c) * 32 + lane] = acc[c].hi;
-            mine[(2 * c + 1) * 32 + lane] = acc[c].lo;
-            mine[(6 + 2 * c) * 32 + lane] = accw[c].hi;
-            mine[(7 + 2 * c) * 32 + lane] = accw[c].lo;
-            mine[(12 + 2 * c) * 32 + lane] = acch[c].hi;
-            mine[(13 + 2 * c) * 32 + lane] = acch[c].lo;
+            mine[(2 * c) * 32 + lane] = acch[c].hi;
+            mine[(2 * c + 1) * 32 + lane] = acch[c].lo;
         }
         __syncthreads();
         if (sl != 0) return;
@@ -516,71 +586,105 @@ __global__ void __launch_bounds__(ShapeM<SL>::kWarps * 32, ShapeM<SL>::kMinBlock
             const float *o = reinterpret_cast<const float *>(Wall[rw * kSlices + q].hhi);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                ff_acc(acc[c], o[(2 * c) * 32 + lane]);
-                ff_acc(acc[c], o[(2 * c + 1) * 32 + lane]);
-                ff_acc(accw[c], o[(6 + 2 * c) * 32 + lane]);
-                ff_acc(accw[c], o[(7 + 2 * c) * 32 + lane]);
-                ff_acc(acch[c], o[(12 + 2 * c) * 32 + lane]);
-                ff_acc(acch[c], o[(13 + 2 * c) * 32 + lane]);
+                ff_acc(acch[c], o[(2 * c) * 32 + lane]);
+                ff_acc(acch[c], o[(2 * c + 1) * 32 + lane]);
             }
         }
     }
     if (!active) return;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {  // contact/bond sum + Hamaker sum
-        ff_acc(acc[c], acch[c].hi);
-        ff_acc(acc[c], acch[c].lo);
+    st4(MX.hsum, i, mk3(ff_to_d(acch[0]), ff_to_d(acch[1]), ff_to_d(acch[2])));
+}
+
+// Completion of every row: contact part (a, alpha from forces_contacts_mixed when `contacts`)
+// plus the Hamaker part (hsum when `hamaker`), facet terms, stores and half kick.
+__global__ void __launch_bounds__(128) forces_finish_mixed(Params P, StateView S, double hdt, double dt,
+                                                           int move_facets, int contacts, int hamaker,
+                                                           const dbl4 *__restrict__ hsum) {
+    if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    d3 a_tot = zero3(), al_tot = zero3();
+    if (contacts) {
+        a_tot = ld4(S.a, i);
+        al_tot = ld4(S.al, i);
     }
-    const d3 a_tot = mk3(ff_to_d(acc[0]), ff_to_d(acc[1]), ff_to_d(acc[2]));
-    const d3 al_tot = mk3(ff_to_d(accw[0]), ff_to_d(accw[1]), ff_to_d(accw[2]));
-    compact::finish_row(P, S, i, n, a_tot, al_tot, ld4(S.v, i), ld4(S.w, i), hdt);
+    if (hamaker) a_tot = contacts ? add(a_tot, ld4(hsum, i)) : ld4(hsum, i);
+    compact::finish_row(P, S, i, P.n, a_tot, al_tot, ld4(S.v, i), ld4(S.w, i), hdt);
+}
+
+namespace {
+
+template <bool NEAR>
+void launch_contacts(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, const MixedExtra &MX,
+                     cudaStream_t st) {
+    constexpr int T = kContactLanes;
+    const size_t smem = sizeof(ContactSmem) * kCWarps;
+    const int64_t rows_per_block = (32 / T) * kCWarps;
+    const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
+    forces_contacts_mixed<NEAR, T><<<blocks, kCWarps * 32, smem, st>>>(P, S, PV, BV, MX);
 }
 
 template <bool VERLET, int SL>
-static void launch_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
-                                 double hdt, double dt, int move_facets, const MixedExtra &MX, cudaStream_t st) {
-    using Sh = ShapeM<SL>;
-    const size_t smem = sizeof(WarpSmemM) * Sh::kWarps;
+void launch_hamaker(const Params &P, const PairView &PV, const MixedExtra &MX, cudaStream_t st) {
+    using Sh = ShapeH<SL>;
+    const size_t smem = sizeof(HamakerSmem) * Sh::kWarps;
     const int64_t rows_per_block = Sh::kRowWarps * 32;
     const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
-    static thread_local int attr_device = -1;  // the attribute is per device; set once per thread and device
-    int dev = 0;
-    cudaGetDevice(&dev);
-    auto kern = forces_compact_mixed<VERLET, SL>;
-    if (attr_device != dev) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_device = dev;
-    }
-    kern<<<blocks, Sh::kWarps * 32, smem, st>>>(P, S, PV, BV, hdt, dt, move_facets, MX);
+    forces_hamaker_mixed<VERLET, SL><<<blocks, Sh::kWarps * 32, smem, st>>>(P, PV, MX);
 }
 
-// Slices per 32-row group: the most slices that keep the launch within about two waves of
-// resident warps (152 SMs x 16); rows of long launches are not sliced.
-static int mixed_slices(int64_t n) {
+// Slices per 32-row group of the Hamaker kernel: the most slices that keep the launch within about
+// two waves of resident warps (152 SMs x 20); rows of long launches are not sliced.
+int hamaker_slices(int64_t n) {
     if (LG_MIXED_SLICES == 1 || LG_MIXED_SLICES == 2 || LG_MIXED_SLICES == 4) return LG_MIXED_SLICES;
-    const int64_t two_waves = 2 * 152 * 16;
+    const int64_t two_waves = 2 * 152 * 20;
     const int64_t groups = (n + 31) / 32;
     if (groups * 4 <= two_waves) return 4;
     if (groups * 2 <= two_waves) return 2;
     return 1;
 }
 
-void launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
-                                 double dt, int move_facets, const MixedExtra &MX, cudaStream_t st) {
+}  // namespace
+
+int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                                double dt, int move_facets, const MixedExtra &MX, cudaStream_t st, cudaStream_t side,
+                                cudaEvent_t fork, cudaEvent_t join) {
     const bool ver = P.pairs == LG_PAIRS_VERLET;
-    switch (mixed_slices(P.n)) {
-        case 4:
-            if (ver) launch_compact_mixed<true, 4>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
-            else launch_compact_mixed<false, 4>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
-            break;
-        case 2:
-            if (ver) launch_compact_mixed<true, 2>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
-            else launch_compact_mixed<false, 2>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
-            break;
-        default:
-            if (ver) launch_compact_mixed<true, 1>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
-            else launch_compact_mixed<false, 1>(P, S, PV, BV, hdt, dt, move_facets, MX, st);
+    const int contacts = P.binary_model != LG_BINARY_NONE ? 1 : 0;
+    const int hamaker = P.hamaker_model != LG_HAMAKER_NONE ? 1 : 0;
+    int kernels = 1;
+    if (contacts) {  // the contact branch runs beside the Hamaker kernel
+        cudaEventRecord(fork, st);
+        cudaStreamWaitEvent(side, fork, 0);
+        if (ver && PV.near_len)
+            launch_contacts<true>(P, S, PV, BV, MX, side);
+        else
+            launch_contacts<false>(P, S, PV, BV, MX, side);
+        ++kernels;
     }
+    if (hamaker) {
+        switch (hamaker_slices(P.n)) {
+            case 4:
+                if (ver) launch_hamaker<true, 4>(P, PV, MX, st);
+                else launch_hamaker<false, 4>(P, PV, MX, st);
+                break;
+            case 2:
+                if (ver) launch_hamaker<true, 2>(P, PV, MX, st);
+                else launch_hamaker<false, 2>(P, PV, MX, st);
+                break;
+            default:
+                if (ver) launch_hamaker<true, 1>(P, PV, MX, st);
+                else launch_hamaker<false, 1>(P, PV, MX, st);
+        }
+        ++kernels;
+    }
+    if (contacts) {
+        cudaEventRecord(join, side);
+        cudaStreamWaitEvent(st, join, 0);
+    }
+    const unsigned blocks = (unsigned)((P.n + 127) / 128);
+    forces_finish_mixed<<<blocks, 128, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, MX.hsum);
+    return kernels;
 }
 
 }  // namespace lg

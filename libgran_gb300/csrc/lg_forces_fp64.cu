@@ -254,8 +254,8 @@ __global__ void bbox_partial(int64_t n, const dbl4 *__restrict__ x, BatchView B,
 // One block: combine the block partials and size the grid (cells of edge >= r_verlet; the edge
 // grows by 1.25 until the grid has at most max_cells cells). Also fixes the FP32 accept / reject
 // bounds of the squared list radius for positions stored relative to the grid origin.
-__global__ void __launch_bounds__(256) grid_setup(int nparts, const double *__restrict__ part, double rv, int64_t max_cells,
-                                                  GridDev *g) {
+__global__ void __launch_bounds__(256) grid_setup(int nparts, const double *__restrict__ part, double rv, double rnear,
+                                                  int64_t max_cells, GridDev *g) {
     __shared__ double s[6][256];
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int b = threadIdx.x; b < nparts; b += blockDim.x)
@@ -311,6 +311,7 @@ __global__ void __launch_bounds__(256) grid_setup(int nparts, const double *__re
     const double lo_r = rv - 2.0 * del, hi_r = rv + 2.0 * del;
     g->rv2_lo = lo_r > 0 ? (float)(lo_r * lo_r * (1.0 - 1e-6)) : 0.0f;
     g->rv2_hi = (float)(hi_r * hi_r * (1.0 + 1e-6));
+    g->rn2_hi = rnear > 0 ? (float)((rnear + 2.0 * del) * (rnear + 2.0 * del) * (1.0 + 1e-6)) : -1.0f;
 }
 
 __device__ __forceinline__ int64_t cell_coord(double q, double lo, double edge, int64_t dim) {
@@ -369,12 +370,13 @@ __global__ void cell_scatter(int64_t n, const int32_t *__restrict__ cell_of, con
 constexpr int kBuildRows = 32;   // rows per block
 constexpr int kBuildWarps = 8;   // warps per block; warp w builds rows w, w + 8, ...
 
-// Shared-memory layout of build_rows for row capacity cap and bond capacity bcap: three 32-row
-// tiles (partner, flags, old slot) with an odd row stride, then per warp the unsorted candidates,
-// the old row and the row's bond partners.
+// Shared-memory layout of build_rows for row capacity cap and bond capacity bcap: four 32-row
+// tiles (partner, flags, old slot, near partner) with an odd row stride, then per warp the unsorted
+// candidates, the old row and the row's bond partners, then the near-slot tile (bytes).
 __host__ __device__ inline int64_t build_tile_stride(int64_t cap) { return cap | 1; }
 __host__ __device__ inline size_t build_smem_bytes(int64_t cap, int64_t bcap) {
-    return sizeof(int32_t) * (size_t)(3 * kBuildRows * build_tile_stride(cap) + kBuildWarps * (2 * cap + bcap));
+    return sizeof(int32_t) * (size_t)(4 * kBuildRows * build_tile_stride(cap) + kBuildWarps * (2 * cap + bcap)) +
+           (size_t)(kBuildRows * build_tile_stride(cap));
 }
 
 // Build rows row0 .. row0 + 31: every j != i with squared centre distance < r_verlet^2 (the FP64
@@ -398,9 +400,14 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
     int32_t *tj = sm;
     uint32_t *tf = reinterpret_cast<uint32_t *>(tj + kBuildRows * ts);
     int32_t *tp = reinterpret_cast<int32_t *>(tf + kBuildRows * ts);
-    int32_t *wraw = tp + kBuildRows * ts + (int64_t)warp * (2 * cap + bcap);
+    int32_t *tnj = tp + kBuildRows * ts;
+    int32_t *wraw = tnj + kBuildRows * ts + (int64_t)warp * (2 * cap + bcap);
     int32_t *wold = wraw + cap;
     int32_t *wbond = wold + cap;
+    uint8_t *tnk = reinterpret_cast<uint8_t *>(tnj + kBuildRows * ts + kBuildWarps * (2 * cap + bcap));
+    __shared__ int32_t rnear[kBuildRows];
+    const bool near_lists = newv.near_len != nullptr;
+    const float rn2 = g->rn2_hi;
     const int64_t row0 = (int64_t)blockIdx.x * kBuildRows;
     const float rlo = g->rv2_lo, rhi = g->rv2_hi;
     const int64_t dim0 = g->dim[0], dim1 = g->dim[1], dim2 = g->dim[2];
@@ -408,7 +415,7 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
     for (int r = warp; r < kBuildRows; r += kBuildWarps) {
         const int64_t i = row0 + r;
         if (i >= n) {
-            if (lane == 0) rlen[r] = 0;
+            if (lane == 0) rlen[r] = rnear[r] = 0;
             continue;
         }
         const float4 fi = x32[i];
@@ -477,9 +484,11 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
             tj[r * ts + rank] = v;
         }
         __syncwarp();
-        int32_t found = 0;
-        for (int32_t k = lane; k < cnt; k += 32) {
-            const int32_t j = tj[r * ts + k];
+        int32_t found = 0, nnear = 0;
+        for (int32_t kb = 0; kb < cnt; kb += 32) {  // warp-uniform trip count (ballots inside)
+            const int32_t k = kb + lane;
+            const bool slot_ok = k < cnt;
+            const int32_t j = slot_ok ? tj[r * ts + k] : 0;
             int32_t lo = 0, hi = olen;
             while (lo < hi) {
                 const int32_t mid = (lo + hi) >> 1;
@@ -490,24 +499,47 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
             }
             uint32_t fl = 0;
             int32_t po = -1;
-            if (lo < olen && wold[lo] == j && (oldv.flags[(int64_t)lo * n + i] & kXiLive)) {
+            if (slot_ok && lo < olen && wold[lo] == j && (oldv.flags[(int64_t)lo * n + i] & kXiLive)) {
                 fl |= kXiLive;
                 po = lo;
             }
-            for (int b = 0; b < bcap; ++b)
-                if (wbond[b] == j) {
-                    fl |= kBonded | ((uint32_t)b << 8);
-                    ++found;
-                    break;
+            if (slot_ok)
+                for (int b = 0; b < bcap; ++b)
+                    if (wbond[b] == j) {
+                        fl |= kBonded | ((uint32_t)b << 8);
+                        ++found;
+                        break;
+                    }
+            bool is_near = false;
+            if (near_lists && slot_ok) {
+                const float4 fj = x32[j];
+                const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
+                is_near = (fl & kBonded) || fmaf(ez, ez, fmaf(ey, ey, ex * ex)) <= rn2;
+                if (!is_near) {  // apart: its springs reset, so they are not carried
+                    fl &= ~kXiLive;
+                    po = -1;
                 }
-            tf[r * ts + k] = fl;
-            tp[r * ts + k] = po;
+            }
+            if (near_lists) {
+                const uint32_t bal = __ballot_sync(0xffffffffu, is_near);
+                if (is_near) {
+                    const int32_t m = nnear + __popc(bal & lt);
+                    tnj[r * ts + m] = j;
+                    tnk[r * ts + m] = (uint8_t)k;
+                }
+                nnear += __popc(bal);
+            }
+            if (slot_ok) {
+                tf[r * ts + k] = fl;
+                tp[r * ts + k] = po;
+            }
         }
         found = __reduce_add_sync(0xffffffffu, found);
         intact = __reduce_add_sync(0xffffffffu, intact);
         if (lane == 0) {
             if (intact != found) set_error(err, LG_DEVERR_BOND_LOST);
             rlen[r] = cnt;
+            rnear[r] = nnear;
         }
         __syncwarp();
     }
@@ -519,6 +551,16 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
     if (warp == 0 && il < n) newv.row_len[il] = len;
     const int32_t kmax = (int32_t)__reduce_max_sync(0xffffffffu, (unsigned)len);
     const int64_t oxs = oldv.cap * n, nxs = newv.cap * n;
+    if (near_lists) {
+        const int32_t nl = il < n ? rnear[lane] : 0;
+        if (warp == 0 && il < n) newv.near_len[il] = nl;
+        const int32_t mmax = (int32_t)__reduce_max_sync(0xffffffffu, (unsigned)nl);
+        for (int32_t m = warp; m < mmax; m += kBuildWarps) {
+            if (m >= nl) continue;
+            newv.near_j[(int64_t)m * n + il] = tnj[lane * ts + m];
+            newv.near_k[(int64_t)m * n + il] = tnk[lane * ts + m];
+        }
+    }
     for (int32_t k = warp; k < kmax; k += kBuildWarps) {
         if (k >= len) continue;
         const int64_t e = (int64_t)k * n + il;
@@ -576,11 +618,11 @@ void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, cons
     kick_drift_fp64<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt);
 }
 
-void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, int64_t max_cells, ListScratch &ls, PairView oldv,
-                       PairView newv, BondView BV, int32_t *err, cudaStream_t st) {
+void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, double r_near, int64_t max_cells,
+                       ListScratch &ls, PairView oldv, PairView newv, BondView BV, int32_t *err, cudaStream_t st) {
     const int nparts = ls.nparts;
     bbox_partial<<<nparts, 256, 0, st>>>(n, x, B, ls.part);
-    grid_setup<<<1, 256, 0, st>>>(nparts, ls.part, rv, max_cells, ls.grid);
+    grid_setup<<<1, 256, 0, st>>>(nparts, ls.part, rv, newv.near_len ? r_near : 0.0, max_cells, ls.grid);
     cudaMemsetAsync(ls.count, 0, sizeof(int32_t) * (size_t)max_cells, st);
     cudaMemsetAsync(ls.fill, 0, sizeof(int32_t) * (size_t)max_cells, st);
     const int threads = 256;

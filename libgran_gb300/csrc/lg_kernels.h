@@ -13,6 +13,7 @@ struct GridDev {
     int64_t dim[3];
     int64_t ncell;
     float rv2_lo, rv2_hi;  // FP32 accept / reject bounds of the squared list radius
+    float rn2_hi;          // FP32 bound of the squared near radius (contact candidates), < 0: none
 };
 
 // Batch segmentation (null pointers for a single system): system index of every particle and the
@@ -40,8 +41,11 @@ void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairVi
                         double dt, int move_facets, cudaStream_t st);
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
                             const dbl4 *al, double dt, double hdt, cudaStream_t st);
-void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, int64_t max_cells, ListScratch &ls, PairView oldv,
-                       PairView newv, BondView BV, int32_t *err, cudaStream_t st);
+// Rebuilds the Verlet rows into newv (springs carried from oldv). With r_near > 0 it also lists each
+// row's contact candidates (newv.near_*): slots within r_near or bonded; springs of the other slots
+// are not carried (those pairs are apart, so their springs reset).
+void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, double r_near, int64_t max_cells,
+                       ListScratch &ls, PairView oldv, PairView newv, BondView BV, int32_t *err, cudaStream_t st);
 
 // Mixed-precision path (lg_forces_mixed.cu)
 struct MixedExtra {
@@ -53,6 +57,7 @@ struct MixedExtra {
     // [3n] velocities of the force evaluation: v32[i] / v32[n + i] = high / low FP32 parts of v_i,
     // v32[2n + i] = FP32 rounding of omega_i (compacted kernel's contact and bond pairs)
     const float4 *v32;
+    dbl4 *hsum;  // [n] Hamaker part of the accelerations (compacted kernels' scratch)
     float near2;      // squared culling radius (FP32 positions); beyond it a pair cannot touch and the
                       // limited Hamaker force is zero
     float contact2f;  // squared contact-candidate radius (FP32 positions, with margin)
@@ -87,8 +92,12 @@ void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, con
 // Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                 double dt, int move_facets, cudaStream_t st);
-void launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
-                                 double dt, int move_facets, const MixedExtra &MX, cudaStream_t st);
+// Mixed precision: the contact/bond kernel (if the system has a binary model) on `side`, beside the
+// Hamaker kernel on `st` (fork / join through the two events), then the completion kernel on `st`;
+// returns the number of kernels launched.
+int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
+                                double dt, int move_facets, const MixedExtra &MX, cudaStream_t st, cudaStream_t side,
+                                cudaEvent_t fork, cudaEvent_t join);
 
 // Layout conversion between a caller's [n][3] doubles (already in device memory) and the padded
 // device layout (lg_reduce.cu).

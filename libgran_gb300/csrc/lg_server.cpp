@@ -79,7 +79,7 @@ extern "C" int64_t lg_estimate_device_bytes(const lg_system_desc *d, int64_t n) 
     const int64_t nbuf = d->pairs == LG_PAIRS_VERLET ? 2 : 1;
     int64_t b = 10 * 32 * n;                                  // x, th, v[2], w[2], a, al (+ slack)
     b += 80 * n;                                              // float-float positions, velocities
-    b += nbuf * cap * n * (4 + 4 + 72) + nbuf * 4 * n;       // nbr, flags, springs, row lengths
+    b += nbuf * cap * n * (4 + 4 + 72 + 5) + nbuf * 8 * n;   // nbr, flags, springs, near lists, row lengths
     b += 8 * n * (1 + 1 + 8 + 72);                            // bonds (up to 8 per particle)
     b += 72 * std::max(d->n_facets, 1) * n;                   // facet springs
     b += 4 * 8 * n + 4 * 4 * n;                               // list scratch
