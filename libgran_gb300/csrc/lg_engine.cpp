@@ -809,7 +809,8 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     if (s->precision == LG_PRECISION_MIXED) {
         LG_TRY(s->alloc(&s->x32, 2 * (size_t)n));  // float-float: high parts, then low parts
         LG_TRY(s->alloc(&s->v32, 3 * (size_t)n));  // v high parts, v low parts, spins
-        LG_TRY(s->alloc(&s->hsum, (size_t)n));
+        LG_TRY(s->alloc(&s->csum, 3 * (size_t)n));
+        LG_TRY(s->alloc(&s->hsum, 2 * (size_t)n));
         LG_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
         LG_CUDA(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
         LG_CUDA(cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming));
@@ -827,6 +828,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         s->mx.x32 = s->x32;
         s->mx.x32lo = s->x32 + n;
         s->mx.v32 = s->v32;
+        s->mx.csum = s->csum;
         s->mx.hsum = s->hsum;
         double cnear = 0.0;
         if (d->binary_model != LG_BINARY_NONE) cnear = std::max(cnear, 2.0 * d->contact.r_part);

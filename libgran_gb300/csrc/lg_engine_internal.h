@@ -46,7 +46,8 @@ struct lg_system {
     // mixed precision: FP32 position copy for culling
     float4 *x32 = nullptr;  // mixed: [2n] float-float positions
     float4 *v32 = nullptr;  // mixed: [3n] float-float velocities, FP32 spins
-    lg::dbl4 *hsum = nullptr;  // mixed: [n] Hamaker part of the accelerations
+    float4 *csum = nullptr;    // mixed: [3n] contact sums (float-float)
+    float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
     double origin[4] = {0.0, 0.0, 0.0, 0.0};  // mixed: origin of the float-float positions, extent in [3]
     double r_max = 0.0;                        // mixed: largest particle radius of the functors
     double ext_max = 0.0;                      // mixed: largest extent of a system about its origin

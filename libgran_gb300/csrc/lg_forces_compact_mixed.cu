@@ -7,7 +7,7 @@
 //                          reach plus the Verlet skin, and bonded slots); all-pairs mode walks every
 //                          slot. Candidates are queued per warp (ballot order) and evaluated 32 at a
 //                          time; the pair's linear and angular accelerations are folded per row in
-//                          slot order and stored to a / alpha as the contact part of the sums.
+//                          slot order into float-float sums (MixedExtra::csum).
 //   forces_hamaker_mixed   Hamaker pairs over all slots, in windows of four slots: the owner lane
 //                          gathers its partners' float-float positions, the window's Hamaker pairs
 //                          are evaluated one per lane from those shared-memory copies, the next
@@ -47,7 +47,7 @@ constexpr int kCRound = 32;  // entries per lane classified per round
 constexpr int kCQ = 64;      // contact queue capacity (>= 32 + 31)
 constexpr int kCWarps = 2;   // warps per block
 #ifndef LG_CONTACT_LANES
-#define LG_CONTACT_LANES 4   // lanes per row (compile-time override for tuning)
+#define LG_CONTACT_LANES 2   // lanes per row (compile-time override for tuning)
 #endif
 constexpr int kContactLanes = LG_CONTACT_LANES;
 struct ContactSmem {
@@ -94,9 +94,9 @@ __device__ __forceinline__ f3 fcrs(f3 a, f3 b) {
 // Hamaker factor of hamaker_force.h:36-40 with two reciprocals:
 // s = -A/6 [ (4r+2h) u - 2 w - 4 r^2 w^3 - 2 r^2 (4r+2h) u^2 ], u = 1/((4r+h) h), w = 1/(2r+h).
 __device__ __forceinline__ float ham_factor(int mode, float A, float r, float h) {
-    if (mode == LG_HAMAKER_SIMPLIFIED) return 2.0f * A * r * __frcp_rn(h * h);
-    float u = __frcp_rn((4.0f * r + h) * h);
-    float w = __frcp_rn(2.0f * r + h);
+    if (mode == LG_HAMAKER_SIMPLIFIED) return 2.0f * A * r / (h * h);
+    float u = 1.0f / ((4.0f * r + h) * h);
+    float w = 1.0f / (2.0f * r + h);
     float a = 4.0f * r + 2.0f * h;
     float br = a * u - 2.0f * w - 4.0f * r * r * (w * w * w) - 2.0f * r * r * a * (u * u);
     return -A / 6.0f * br;
@@ -119,7 +119,6 @@ __device__ __forceinline__ void ff_acc(ff &a, float b) {
     a.hi = s.hi;
     a.lo = __fadd_rn(a.lo, s.lo);
 }
-__device__ __forceinline__ double ff_to_d(ff a) { return (double)a.hi + (double)a.lo; }
 // a += b for a stored spring component, renormalised so that |lo| <= ulp(hi) / 2 again.
 __device__ __forceinline__ void ff_add_norm(ff &a, float b) {
     const ff s = two_sum(a.hi, b);
@@ -306,7 +305,7 @@ __device__ __forceinline__ void hamaker_item(const Params &P, const MixedExtra &
         const f3 dxf = sp.d;
         const float d2f = fdot(dxf, dxf);
         const float rsd = rsqrtf(d2f);
-        float h = sp.q * __frcp_rn(d2f * rsd + 2.0f * M.h_r);  // |d| - 2r to FP32 precision
+        float h = sp.q / (d2f * rsd + 2.0f * M.h_r);  // |d| - 2r to FP32 precision
         h = fmaxf(h, M.h_h0);
         const float sfac = ham_factor(P.hamaker_model, M.h_A, M.h_r, h) * M.inv_mass_h * rsd;
         a = fscl(-sfac, dxf);  // along x_j - x_i
@@ -321,8 +320,8 @@ __device__ __forceinline__ void hamaker_item(const Params &P, const MixedExtra &
 
 // Contact and bond pairs of rows row0 .. row0 + 32/T - 1: T lanes per row, lane t of a row taking
 // its entries t, t + T, ... (so short candidate lists still fill the warp); each lane folds its
-// pairs in entry order and the row's T partial sums are combined in lane order. a[i], alpha[i]
-// receive the contact part of the row's accelerations.
+// pairs in entry order and the row's T partial sums are combined in lane order. csum receives the
+// contact part of the row's accelerations as float-float pairs.
 template <bool NEAR, int T>
 __global__ void __launch_bounds__(kCWarps * 32, 8)
     forces_contacts_mixed(Params P, StateView S, PairView PV, BondView BV, MixedExtra MX) {
@@ -459,12 +458,13 @@ __global__ void __launch_bounds__(kCWarps * 32, 8)
         }
     }
     if (!active || sub != 0) return;
-    st4(S.a, i, mk3(ff_to_d(acc[0]), ff_to_d(acc[1]), ff_to_d(acc[2])));
-    st4(S.al, i, mk3(ff_to_d(accw[0]), ff_to_d(accw[1]), ff_to_d(accw[2])));
+    MX.csum[3 * i] = make_float4(acc[0].hi, acc[0].lo, acc[1].hi, acc[1].lo);
+    MX.csum[3 * i + 1] = make_float4(acc[2].hi, acc[2].lo, accw[0].hi, accw[0].lo);
+    MX.csum[3 * i + 2] = make_float4(accw[1].hi, accw[1].lo, accw[2].hi, accw[2].lo);
 }
 
-// Hamaker pairs of rows row0 .. row0 + 31; hsum[i] receives the Hamaker part of the row's
-// acceleration.
+// Hamaker pairs of rows row0 .. row0 + 31; hsum receives the Hamaker part of the row's acceleration
+// as float-float pairs.
 template <bool VERLET, int SL>
 __global__ void __launch_bounds__(ShapeH<SL>::kWarps * 32, ShapeH<SL>::kMinBlocks)
     forces_hamaker_mixed(Params P, PairView PV, MixedExtra MX) {
@@ -592,23 +592,29 @@ __global__ void __launch_bounds__(ShapeH<SL>::kWarps * 32, ShapeH<SL>::kMinBlock
         }
     }
     if (!active) return;
-    st4(MX.hsum, i, mk3(ff_to_d(acch[0]), ff_to_d(acch[1]), ff_to_d(acch[2])));
+    MX.hsum[2 * i] = make_float4(acch[0].hi, acch[0].lo, acch[1].hi, acch[1].lo);
+    MX.hsum[2 * i + 1] = make_float4(acch[2].hi, acch[2].lo, 0.f, 0.f);
 }
 
-// Completion of every row: contact part (a, alpha from forces_contacts_mixed when `contacts`)
-// plus the Hamaker part (hsum when `hamaker`), facet terms, stores and half kick.
+// Completion of every row: contact part (csum when `contacts`) plus the Hamaker part (hsum when
+// `hamaker`), both converted to FP64 here, then facet terms, stores and half kick.
 __global__ void __launch_bounds__(128) forces_finish_mixed(Params P, StateView S, double hdt, double dt,
                                                            int move_facets, int contacts, int hamaker,
-                                                           const dbl4 *__restrict__ hsum) {
+                                                           MixedExtra MX) {
     if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     d3 a_tot = zero3(), al_tot = zero3();
-    if (contacts) {
-        a_tot = ld4(S.a, i);
-        al_tot = ld4(S.al, i);
+    if (contacts) {  // float-float pairs (hi, lo) of the contact sums
+        const float4 c0 = MX.csum[3 * i], c1 = MX.csum[3 * i + 1], c2 = MX.csum[3 * i + 2];
+        a_tot = mk3((double)c0.x + (double)c0.y, (double)c0.z + (double)c0.w, (double)c1.x + (double)c1.y);
+        al_tot = mk3((double)c1.z + (double)c1.w, (double)c2.x + (double)c2.y, (double)c2.z + (double)c2.w);
     }
-    if (hamaker) a_tot = contacts ? add(a_tot, ld4(hsum, i)) : ld4(hsum, i);
+    if (hamaker) {  // then the Hamaker sums
+        const float4 h0 = MX.hsum[2 * i], h1 = MX.hsum[2 * i + 1];
+        const d3 ah = mk3((double)h0.x + (double)h0.y, (double)h0.z + (double)h0.w, (double)h1.x + (double)h1.y);
+        a_tot = contacts ? add(a_tot, ah) : ah;
+    }
     compact::finish_row(P, S, i, P.n, a_tot, al_tot, ld4(S.v, i), ld4(S.w, i), hdt);
 }
 
@@ -683,7 +689,7 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         cudaStreamWaitEvent(st, join, 0);
     }
     const unsigned blocks = (unsigned)((P.n + 127) / 128);
-    forces_finish_mixed<<<blocks, 128, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, MX.hsum);
+    forces_finish_mixed<<<blocks, 128, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, MX);
     return kernels;
 }
 

@@ -57,7 +57,10 @@ struct MixedExtra {
     // [3n] velocities of the force evaluation: v32[i] / v32[n + i] = high / low FP32 parts of v_i,
     // v32[2n + i] = FP32 rounding of omega_i (compacted kernel's contact and bond pairs)
     const float4 *v32;
-    dbl4 *hsum;  // [n] Hamaker part of the accelerations (compacted kernels' scratch)
+    // compacted kernels' scratch: per particle the float-float (hi, lo) pairs of the contact sums
+    // (csum, [3n]: a.x a.y / a.z alpha.x / alpha.y alpha.z) and of the Hamaker sum (hsum, [2n])
+    float4 *csum;
+    float4 *hsum;
     float near2;      // squared culling radius (FP32 positions); beyond it a pair cannot touch and the
                       // limited Hamaker force is zero
     float contact2f;  // squared contact-candidate radius (FP32 positions, with margin)
