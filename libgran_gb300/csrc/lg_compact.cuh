@@ -27,9 +27,10 @@ __device__ __forceinline__ void move_facets(const Params &P, const StateView &S,
 }
 
 // Tail of particle i's force evaluation: the unary (facet) terms in facet order, added after the
-// binary sums; stores a and alpha, the half-kicked velocities, and flags non-finite results.
-__device__ __forceinline__ void finish_row(const Params &P, const StateView &S, int64_t i, int64_t n, d3 accA, d3 accW,
-                                           d3 vi, d3 wi, double hdt) {
+// binary sums (accA, accW return the totals); stores a and alpha, the half-kicked velocities, and
+// flags non-finite results.
+__device__ __forceinline__ void finish_row(const Params &P, const StateView &S, int64_t i, int64_t n, d3 &accA,
+                                           d3 &accW, d3 vi, d3 wi, double hdt) {
     if (P.n_facets > 0) {
         const d3 xi = ld4(S.x, i);
         d3 ua = zero3(), ual = zero3();

@@ -279,6 +279,11 @@ static void set_cull_radii(lg_system *s) {
 
 static int set_mixed_origins(lg_system *s, const double *x) {
     origin_of(x, 0, s->P.n, s->r_max, s->origin);
+    s->mx.ox = s->origin[0];
+    s->mx.oy = s->origin[1];
+    s->mx.oz = s->origin[2];
+    s->mx.agg = s->d_agg;
+    s->mx.orig = s->d_orig;
     s->ext_max = s->origin[3];
     if (s->n_systems > 0) {
         s->h_orig.assign((size_t)s->n_systems, make_double4_32a(0.0, 0.0, 0.0, 0.0));
@@ -422,7 +427,7 @@ static StateView state_view(lg_system *s, bool half_step_inputs) {
     return S;
 }
 
-static int launch_forces(lg_system *s, double hdt, double dt, int move_facets) {
+static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, bool fuse_kick = false) {
     StateView S = state_view(s, true);
     cudaEvent_t stop_ev = nullptr;
     if (s->timing) {
@@ -441,8 +446,8 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets) {
     int kernels = 1;
     if (s->precision == LG_PRECISION_MIXED) {
         if (compact)
-            kernels = launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream,
-                                                  s->side, s->fork_ev, s->join_ev);
+            kernels = launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, fuse_kick,
+                                                  s->mx, s->stream, s->side, s->fork_ev, s->join_ev);
         else
             launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
     } else {
@@ -457,18 +462,26 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets) {
     return LG_OK;
 }
 
-static int step_once(lg_system *s, double dt, int64_t rebuild_every) {
+// One velocity-Verlet step. `fuse_next`: the caller runs another step right after this one with no
+// list rebuild in between; the mixed compacted path then folds that step's opening half kick and
+// drift into this step's completion kernel (same operations, one pass over the state less).
+static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_next) {
     if (s->P.pairs == LG_PAIRS_VERLET && rebuild_every > 0 && (s->step_index % rebuild_every) == 0)
         LG_TRY(rebuild_list(s));
     const double hdt = dt / 2.0;
-    if (s->precision == LG_PRECISION_MIXED)
-        launch_kick_drift_mixed(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->origin,
-                                s->d_agg, s->d_orig, s->x32, s->v32, s->stream);
-    else
-        launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->stream);
-    s->launches += 1;
+    if (!s->kick_done) {
+        if (s->precision == LG_PRECISION_MIXED)
+            launch_kick_drift_mixed(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt,
+                                    s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->stream);
+        else
+            launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt,
+                                   s->stream);
+        s->launches += 1;
+    }
     const int mv = (s->facet_auto_move && s->P.n_facets > 0) ? 1 : 0;
-    LG_TRY(launch_forces(s, hdt, dt, mv));
+    const bool fuse = fuse_next && s->precision == LG_PRECISION_MIXED && s->kernel == LG_FORCE_KERNEL_COMPACT;
+    LG_TRY(launch_forces(s, hdt, dt, mv, fuse));
+    s->kick_done = fuse;
     s->vcur = 1 - s->vcur;
     if (mv) s->fcur = 1 - s->fcur;
     s->step_index++;
@@ -931,7 +944,7 @@ static int run_period_graph(lg_system *s, double dt, int64_t period, int64_t reb
     const int64_t l0 = s->launches;
     LG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     int rc = LG_OK;
-    for (int64_t k = 0; k < period && rc == LG_OK; ++k) rc = step_once(s, dt, rebuild_every);
+    for (int64_t k = 0; k < period && rc == LG_OK; ++k) rc = step_once(s, dt, rebuild_every, k + 1 < period);
     cudaGraph_t graph = nullptr;
     cudaError_t ec = cudaStreamEndCapture(s->stream, &graph);
     if (rc != LG_OK) {
@@ -971,7 +984,7 @@ extern "C" int lg_step(lg_system *s, double dt, int64_t nsteps, int64_t rebuild_
         } else {
             stop = std::min<int64_t>(nsteps, k + period);
         }
-        for (; k < stop; ++k) LG_TRY(step_once(s, dt, rebuild_every));
+        for (; k < stop; ++k) LG_TRY(step_once(s, dt, rebuild_every, k + 1 < stop));
         s->periods_run++;
     }
     return LG_OK;

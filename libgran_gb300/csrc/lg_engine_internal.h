@@ -52,6 +52,7 @@ struct lg_system {
     double r_max = 0.0;                        // mixed: largest particle radius of the functors
     double ext_max = 0.0;                      // mixed: largest extent of a system about its origin
     double r_near = 0.0;                       // mixed, Verlet: radius of the contact-candidate lists
+    bool kick_done = false;                    // the last step already ran the next one's half kick and drift
     double cull_near = 0.0, cull_contact = 0.0;  // mixed: culling radii before margins
     lg::MixedExtra mx{};
 

@@ -14,7 +14,8 @@
 //                          window's partners are loaded meanwhile. For launches with few rows a
 //                          row's windows are sliced over SL warps, whose partial sums are combined
 //                          in slice order. Runs beside forces_contacts_mixed (two streams).
-//   forces_finish_mixed    per particle: contact part + Hamaker part, facet terms, stores, half kick.
+//   forces_finish_mixed    per particle: contact part + Hamaker part, facet terms, stores, half kick;
+//                          within a run of steps also the next step's half kick and drift.
 //
 // Precision: positions come as float-float pairs (MixedExtra::x32 / x32lo, hi + lo = x - origin) and
 // a pair's separation and q = |d|^2 - (2r)^2 are formed with error-free FP32 transformations
@@ -599,7 +600,7 @@ __global__ void __launch_bounds__(ShapeH<SL>::kWarps * 32, ShapeH<SL>::kMinBlock
 // Completion of every row: contact part (csum when `contacts`) plus the Hamaker part (hsum when
 // `hamaker`), both converted to FP64 here, then facet terms, stores and half kick.
 __global__ void __launch_bounds__(128) forces_finish_mixed(Params P, StateView S, double hdt, double dt,
-                                                           int move_facets, int contacts, int hamaker,
+                                                           int move_facets, int contacts, int hamaker, int kick,
                                                            MixedExtra MX) {
     if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -615,7 +616,19 @@ __global__ void __launch_bounds__(128) forces_finish_mixed(Params P, StateView S
         const d3 ah = mk3((double)h0.x + (double)h0.y, (double)h0.z + (double)h0.w, (double)h1.x + (double)h1.y);
         a_tot = contacts ? add(a_tot, ah) : ah;
     }
-    compact::finish_row(P, S, i, P.n, a_tot, al_tot, ld4(S.v, i), ld4(S.w, i), hdt);
+    const d3 vi = ld4(S.v, i), wi = ld4(S.w, i);
+    compact::finish_row(P, S, i, P.n, a_tot, al_tot, vi, wi, hdt);
+    if (kick) {  // the next step's opening half kick and drift (the end-of-step velocities are not kept)
+        const d3 ve = add(vi, scl(hdt, a_tot)), we = add(wi, scl(hdt, al_tot));
+        const d3 vh = add(ve, scl(hdt, a_tot)), wh = add(we, scl(hdt, al_tot));
+        st4(S.v_out, i, vh);
+        st4(S.w_out, i, wh);
+        const d3 xn = add(ld4(S.x, i), scl(dt, vh));
+        st4(S.x, i, xn);
+        st4(S.th, i, add(ld4(S.th, i), scl(dt, wh)));
+        rel_ff(xn, MX.ox, MX.oy, MX.oz, MX.agg, MX.orig, i, P.n, MX.x32);
+        vel_ff(vh, wh, i, P.n, MX.v32);
+    }
 }
 
 namespace {
@@ -653,8 +666,8 @@ int hamaker_slices(int64_t n) {
 }  // namespace
 
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
-                                double dt, int move_facets, const MixedExtra &MX, cudaStream_t st, cudaStream_t side,
-                                cudaEvent_t fork, cudaEvent_t join) {
+                                double dt, int move_facets, bool kick, const MixedExtra &MX, cudaStream_t st,
+                                cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
     const bool ver = P.pairs == LG_PAIRS_VERLET;
     const int contacts = P.binary_model != LG_BINARY_NONE ? 1 : 0;
     const int hamaker = P.hamaker_model != LG_HAMAKER_NONE ? 1 : 0;
@@ -689,7 +702,7 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         cudaStreamWaitEvent(st, join, 0);
     }
     const unsigned blocks = (unsigned)((P.n + 127) / 128);
-    forces_finish_mixed<<<blocks, 128, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, MX);
+    forces_finish_mixed<<<blocks, 128, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, kick ? 1 : 0, MX);
     return kernels;
 }
 

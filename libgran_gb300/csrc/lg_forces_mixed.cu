@@ -329,31 +329,6 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
         set_error(S.err, LG_DEVERR_NONFINITE);
 }
 
-// Position of particle i relative to its system's origin as a float-float pair: x32[i] receives
-// the FP32 rounding of the FP64 difference, x32[n + i] the FP32 rounding of what that leaves.
-__device__ __forceinline__ void rel_ff(d3 q, double ox, double oy, double oz, const int32_t *agg, const dbl4 *orig,
-                                       int64_t i, int64_t n, float4 *__restrict__ x32) {
-    if (agg) {
-        const dbl4 o = orig[agg[i]];
-        ox = o.x;
-        oy = o.y;
-        oz = o.z;
-    }
-    const double rx = q.x - ox, ry = q.y - oy, rz = q.z - oz;
-    const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
-    x32[i] = make_float4(hx, hy, hz, 0.0f);
-    x32[n + i] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.0f);
-}
-
-// Velocity copies of the mixed compacted kernel: v32[i] / v32[n + i] = high / low FP32 parts of v_i,
-// v32[2n + i] = FP32 rounding of omega_i.
-__device__ __forceinline__ void vel_ff(d3 v, d3 w, int64_t i, int64_t n, float4 *__restrict__ v32) {
-    const float hx = (float)v.x, hy = (float)v.y, hz = (float)v.z;
-    v32[i] = make_float4(hx, hy, hz, 0.0f);
-    v32[n + i] = make_float4((float)(v.x - (double)hx), (float)(v.y - (double)hy), (float)(v.z - (double)hz), 0.0f);
-    v32[2 * n + i] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.0f);
-}
-
 // Float-float copies of the positions (relative to the system origin; in a batch every system has
 // its own origin) and of the velocities.
 __global__ void mixed_copies(int64_t n, const dbl4 *__restrict__ x, const dbl4 *__restrict__ v,

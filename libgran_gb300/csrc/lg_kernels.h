@@ -56,11 +56,15 @@ struct MixedExtra {
     const float4 *x32lo;
     // [3n] velocities of the force evaluation: v32[i] / v32[n + i] = high / low FP32 parts of v_i,
     // v32[2n + i] = FP32 rounding of omega_i (compacted kernel's contact and bond pairs)
-    const float4 *v32;
+    float4 *v32;
     // compacted kernels' scratch: per particle the float-float (hi, lo) pairs of the contact sums
     // (csum, [3n]: a.x a.y / a.z alpha.x / alpha.y alpha.z) and of the Hamaker sum (hsum, [2n])
     float4 *csum;
     float4 *hsum;
+    // origins of the float-float positions (for the completion kernel's fused kick and drift)
+    const int32_t *agg;  // [n] system of each particle (batch), or null
+    const dbl4 *orig;    // [n_systems] origins of the systems of a batch
+    double ox, oy, oz;   // origin of a single system
     float near2;      // squared culling radius (FP32 positions); beyond it a pair cannot touch and the
                       // limited Hamaker force is zero
     float contact2f;  // squared contact-candidate radius (FP32 positions, with margin)
@@ -98,9 +102,11 @@ void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairV
 // Mixed precision: the contact/bond kernel (if the system has a binary model) on `side`, beside the
 // Hamaker kernel on `st` (fork / join through the two events), then the completion kernel on `st`;
 // returns the number of kernels launched.
+// With `kick`, the completion kernel goes on to the next step's opening half kick and drift (and the
+// float-float copies), exactly as launch_kick_drift_mixed would.
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
-                                double dt, int move_facets, const MixedExtra &MX, cudaStream_t st, cudaStream_t side,
-                                cudaEvent_t fork, cudaEvent_t join);
+                                double dt, int move_facets, bool kick, const MixedExtra &MX, cudaStream_t st,
+                                cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 
 // Layout conversion between a caller's [n][3] doubles (already in device memory) and the padded
 // device layout (lg_reduce.cu).
