@@ -315,11 +315,9 @@ def e2e_path(s, mat, args, x0, v0):
     for k in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        for f in fields:
-            s.set(f, host[f].numpy())
+        s.set_state(*(host[f].numpy() for f in fields))
         s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
-        for f in fields:
-            s.get(f, out=host[f].numpy())
+        s.get_state(out=tuple(host[f].numpy() for f in fields))
         obs = s.observables(A.LG_OBS_STATE)
         t = time.perf_counter() - t
         if k >= args.warmup:

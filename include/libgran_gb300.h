@@ -201,6 +201,12 @@ int lg_update_neighbor_list(lg_system *sys);
 int lg_get(lg_system *sys, int field, double *out);
 int lg_set(lg_system *sys, int field, const double *in);
 
+/* The whole kinematic state in one call (x, v, theta, omega; double[3*n] each, any may be NULL to
+ * skip it): one copy per array, one conversion pass, one synchronisation, instead of four of each.
+ * Same meaning as the lg_get / lg_set calls of the fields given. */
+int lg_get_state(lg_system *sys, double *x, double *v, double *theta, double *omega);
+int lg_set_state(lg_system *sys, const double *x, const double *v, const double *theta, const double *omega);
+
 /* reset_acceleration_buffers() (Granular-system.md:228-244): zero a and alpha. */
 int lg_reset_acceleration_buffers(lg_system *sys);
 

@@ -120,6 +120,8 @@ def _declare(L):
         "lg_reset_acceleration_buffers": (C.c_int, [vp]),
         "lg_get_observables": (C.c_int, [vp, P(lg_observables)]),
         "lg_get_observables_select": (C.c_int, [vp, C.c_int32, P(lg_observables)]),
+        "lg_get_state": (C.c_int, [vp, P(d), P(d), P(d), P(d)]),
+        "lg_set_state": (C.c_int, [vp, P(d), P(d), P(d), P(d)]),
         "lg_get_device_errors": (C.c_int, [vp, P(i32)]),
         "lg_get_bonds": (C.c_int, [vp, P(i64), P(i64), i64]),
         "lg_get_pair_springs": (C.c_int, [vp, i64, i64, P(d)]),

@@ -26,55 +26,66 @@ __device__ __forceinline__ void move_facets(const Params &P, const StateView &S,
         for (int q = 0; q < 9; ++q) S.facet_vert_next[9 * f + q] = S.facet_vert[9 * f + q] + P.facets[f].v[q % 3] * dt;
 }
 
-// Tail of particle i's force evaluation: the unary (facet) terms in facet order, added after the
-// binary sums (accA, accW return the totals); stores a and alpha, the half-kicked velocities, and
-// flags non-finite results.
-__device__ __forceinline__ void finish_row(const Params &P, const StateView &S, int64_t i, int64_t n, d3 &accA,
-                                           d3 &accW, d3 vi, d3 wi, double hdt) {
-    if (P.n_facets > 0) {
-        const d3 xi = ld4(S.x, i);
-        d3 ua = zero3(), ual = zero3();
-        for (int f = 0; f < P.n_facets; ++f) {
-            const FacetDev &fd = P.facets[f];
-            d3 N = mk3(fd.normal[0], fd.normal[1], fd.normal[2]);
-            d3 xf = closest_point_on_triangle(S.facet_vert + 9 * f, fd.area, N, xi);
-            d3 vf = mk3(fd.v[0], fd.v[1], fd.v[2]);
-            d3 fa = zero3(), fal = zero3();
-            bool hv = false;
-            if (fd.has_contact) {
-                const int64_t base = (int64_t)f * 9 * n;
-                d3 s[3];
+// Unary (facet) terms of particle i in facet order (kept out of line: the common no-facet path then
+// needs few registers; static: each translation unit keeps its own copy, compiled with its own
+// floating-point flags).
+static __device__ __noinline__ void facet_terms(const Params &P, const StateView &S, int64_t i, int64_t n, d3 vi, d3 wi,
+                                         d3 &ua, d3 &ual) {
+    const d3 xi = ld4(S.x, i);
+    ua = zero3();
+    ual = zero3();
+    for (int f = 0; f < P.n_facets; ++f) {
+        const FacetDev &fd = P.facets[f];
+        d3 N = mk3(fd.normal[0], fd.normal[1], fd.normal[2]);
+        d3 xf = closest_point_on_triangle(S.facet_vert + 9 * f, fd.area, N, xi);
+        d3 vf = mk3(fd.v[0], fd.v[1], fd.v[2]);
+        d3 fa = zero3(), fal = zero3();
+        bool hv = false;
+        if (fd.has_contact) {
+            const int64_t base = (int64_t)f * 9 * n;
+            d3 s[3];
 #pragma unroll
-                for (int q = 0; q < 3; ++q)
-                    s[q] = mk3(S.sxi[base + (3 * q) * n + i], S.sxi[base + (3 * q + 1) * n + i],
-                               S.sxi[base + (3 * q + 2) * n + i]);
-                surface_contact(fd.contact, xf, vf, xi, vi, wi, s, fa, fal);
+            for (int q = 0; q < 3; ++q)
+                s[q] = mk3(S.sxi[base + (3 * q) * n + i], S.sxi[base + (3 * q + 1) * n + i],
+                           S.sxi[base + (3 * q + 2) * n + i]);
+            surface_contact(fd.contact, xf, vf, xi, vi, wi, s, fa, fal);
 #pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    S.sxi[base + (3 * q) * n + i] = s[q].x;
-                    S.sxi[base + (3 * q + 1) * n + i] = s[q].y;
-                    S.sxi[base + (3 * q + 2) * n + i] = s[q].z;
-                }
-                hv = true;
+            for (int q = 0; q < 3; ++q) {
+                S.sxi[base + (3 * q) * n + i] = s[q].x;
+                S.sxi[base + (3 * q + 1) * n + i] = s[q].y;
+                S.sxi[base + (3 * q + 2) * n + i] = s[q].z;
             }
-            if (fd.has_hamaker) {
-                d3 ha = surface_hamaker(fd.hamaker, xf, xi);
-                if (hv) {
-                    fa = add(fa, ha);
-                    fal = add(fal, zero3());
-                } else {
-                    fa = ha;
-                    fal = zero3();
-                }
-            }
-            if (f == 0) {
-                ua = fa;
-                ual = fal;
+            hv = true;
+        }
+        if (fd.has_hamaker) {
+            d3 ha = surface_hamaker(fd.hamaker, xf, xi);
+            if (hv) {
+                fa = add(fa, ha);
+                fal = add(fal, zero3());
             } else {
-                ua = add(ua, fa);
-                ual = add(ual, fal);
+                fa = ha;
+                fal = zero3();
             }
         }
+        if (f == 0) {
+            ua = fa;
+            ual = fal;
+        } else {
+            ua = add(ua, fa);
+            ual = add(ual, fal);
+        }
+    }
+}
+
+// Tail of particle i's force evaluation: the unary (facet) terms in facet order, added after the
+// binary sums (accA, accW return the totals); stores a and alpha, the half-kicked velocities, and
+// flags non-finite results. FACETS = false: the caller knows there are no facets.
+template <bool FACETS = true>
+__device__ __forceinline__ void finish_row(const Params &P, const StateView &S, int64_t i, int64_t n, d3 &accA,
+                                           d3 &accW, d3 vi, d3 wi, double hdt) {
+    if (FACETS && P.n_facets > 0) {
+        d3 ua, ual;
+        facet_terms(P, S, i, n, vi, wi, ua, ual);
         accA = add(accA, ua);
         accW = add(accW, ual);
     }

@@ -1052,6 +1052,51 @@ extern "C" int lg_set(lg_system *s, int field, const double *in) {
     return LG_OK;
 }
 
+extern "C" int lg_get_state(lg_system *s, double *x, double *v, double *th, double *w) {
+    LG_HANDLE(s);
+    const int64_t n = s->P.n;
+    const size_t bytes = sizeof(double) * 3 * (size_t)n;
+    double *host[4] = {x, v, th, w};
+    const dbl4 *dev[4] = {s->x, s->v[s->vcur], s->th, s->w[s->vcur]};
+    for (int f = 0; f < 4; ++f) {  // staged in the observables scratch (20 n doubles >= 4 x 3 n)
+        if (!host[f]) continue;
+        launch_dev4_to_aos(n, dev[f], s->obs_scratch + 3 * n * f, s->stream);
+        s->launches += 1;
+        LG_CUDA(cudaMemcpyAsync(host[f], s->obs_scratch + 3 * n * f, bytes, cudaMemcpyDeviceToHost, s->stream));
+    }
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    return LG_OK;
+}
+
+extern "C" int lg_set_state(lg_system *s, const double *x, const double *v, const double *th, const double *w) {
+    LG_HANDLE(s);
+    const int64_t n = s->P.n;
+    const size_t bytes = sizeof(double) * 3 * (size_t)n;
+    const double *host[4] = {x, v, th, w};
+    dbl4 *dev[4] = {s->x, s->v[s->vcur], s->th, s->w[s->vcur]};
+    for (int f = 0; f < 4; ++f) {
+        if (!host[f]) continue;
+        LG_CUDA(cudaMemcpyAsync(s->obs_scratch + 3 * n * f, host[f], bytes, cudaMemcpyHostToDevice, s->stream));
+        launch_aos_to_dev4(n, s->obs_scratch + 3 * n * f, dev[f], s->stream);
+        s->launches += 1;
+    }
+    LG_CUDA(cudaGetLastError());
+    if (s->x32 && (x || v || w)) {
+        if (x && !origins_cover(s, x)) {
+            LG_TRY(set_mixed_origins(s, x));  // positions moved far: new origins and culling radii
+            set_cull_radii(s);
+            s->drop_graphs();
+        }
+        launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32, s->v32,
+                            s->stream);
+        s->launches += 1;
+        LG_CUDA(cudaGetLastError());
+    }
+    LG_CUDA(cudaStreamSynchronize(s->stream));  // the caller may reuse its buffers on return
+    return LG_OK;
+}
+
 extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
     LG_HANDLE(s);
     if (T == 0) {

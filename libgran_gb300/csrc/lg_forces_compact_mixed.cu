@@ -599,33 +599,40 @@ __global__ void __launch_bounds__(ShapeH<SL>::kWarps * 32, ShapeH<SL>::kMinBlock
 
 // Completion of every row: contact part (csum when `contacts`) plus the Hamaker part (hsum when
 // `hamaker`), both converted to FP64 here, then facet terms, stores and half kick.
-__global__ void __launch_bounds__(128) forces_finish_mixed(Params P, StateView S, double hdt, double dt,
-                                                           int move_facets, int contacts, int hamaker, int kick,
-                                                           MixedExtra MX) {
+template <bool FACETS>
+__global__ void __launch_bounds__(64) forces_finish_mixed(Params P, StateView S, double hdt, double dt,
+                                                          int move_facets, int contacts, int hamaker, int kick,
+                                                          MixedExtra MX) {
     if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    d3 a_tot = zero3(), al_tot = zero3();
-    if (contacts) {  // float-float pairs (hi, lo) of the contact sums
-        const float4 c0 = MX.csum[3 * i], c1 = MX.csum[3 * i + 1], c2 = MX.csum[3 * i + 2];
-        a_tot = mk3((double)c0.x + (double)c0.y, (double)c0.z + (double)c0.w, (double)c1.x + (double)c1.y);
-        al_tot = mk3((double)c1.z + (double)c1.w, (double)c2.x + (double)c2.y, (double)c2.z + (double)c2.w);
+    // every input is loaded before anything is stored (the buffers are distinct)
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 c0 = contacts ? MX.csum[3 * i] : z4, c1 = contacts ? MX.csum[3 * i + 1] : z4,
+                 c2 = contacts ? MX.csum[3 * i + 2] : z4;
+    const float4 h0 = hamaker ? MX.hsum[2 * i] : z4, h1 = hamaker ? MX.hsum[2 * i + 1] : z4;
+    const d3 vi = ld4(S.v, i), wi = ld4(S.w, i);
+    d3 xo = zero3(), tho = zero3();
+    if (kick) {
+        xo = ld4(S.x, i);
+        tho = ld4(S.th, i);
     }
-    if (hamaker) {  // then the Hamaker sums
-        const float4 h0 = MX.hsum[2 * i], h1 = MX.hsum[2 * i + 1];
+    // contact part (float-float pairs hi, lo), then the Hamaker part
+    d3 a_tot = mk3((double)c0.x + (double)c0.y, (double)c0.z + (double)c0.w, (double)c1.x + (double)c1.y);
+    d3 al_tot = mk3((double)c1.z + (double)c1.w, (double)c2.x + (double)c2.y, (double)c2.z + (double)c2.w);
+    if (hamaker) {
         const d3 ah = mk3((double)h0.x + (double)h0.y, (double)h0.z + (double)h0.w, (double)h1.x + (double)h1.y);
         a_tot = contacts ? add(a_tot, ah) : ah;
     }
-    const d3 vi = ld4(S.v, i), wi = ld4(S.w, i);
-    compact::finish_row(P, S, i, P.n, a_tot, al_tot, vi, wi, hdt);
+    compact::finish_row<FACETS>(P, S, i, P.n, a_tot, al_tot, vi, wi, hdt);
     if (kick) {  // the next step's opening half kick and drift (the end-of-step velocities are not kept)
         const d3 ve = add(vi, scl(hdt, a_tot)), we = add(wi, scl(hdt, al_tot));
         const d3 vh = add(ve, scl(hdt, a_tot)), wh = add(we, scl(hdt, al_tot));
         st4(S.v_out, i, vh);
         st4(S.w_out, i, wh);
-        const d3 xn = add(ld4(S.x, i), scl(dt, vh));
+        const d3 xn = add(xo, scl(dt, vh));
         st4(S.x, i, xn);
-        st4(S.th, i, add(ld4(S.th, i), scl(dt, wh)));
+        st4(S.th, i, add(tho, scl(dt, wh)));
         rel_ff(xn, MX.ox, MX.oy, MX.oz, MX.agg, MX.orig, i, P.n, MX.x32);
         vel_ff(vh, wh, i, P.n, MX.v32);
     }
@@ -701,8 +708,11 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         cudaEventRecord(join, side);
         cudaStreamWaitEvent(st, join, 0);
     }
-    const unsigned blocks = (unsigned)((P.n + 127) / 128);
-    forces_finish_mixed<<<blocks, 128, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, kick ? 1 : 0, MX);
+    const unsigned blocks = (unsigned)((P.n + 63) / 64);
+    if (P.n_facets > 0)
+        forces_finish_mixed<true><<<blocks, 64, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, kick ? 1 : 0, MX);
+    else
+        forces_finish_mixed<false><<<blocks, 64, 0, st>>>(P, S, hdt, dt, 0, contacts, hamaker, kick ? 1 : 0, MX);
     return kernels;
 }
 

@@ -383,8 +383,8 @@ __host__ __device__ inline size_t build_smem_bytes(int64_t cap, int64_t bcap) {
 // test; an FP32 filter accepts or rejects the clear cases), ascending j, carrying the springs (and
 // live flag) of pairs that were already listed, and marking intact bonds.
 // One warp per row: the 27 neighbour cells are 9 runs of consecutive cells (x fastest), i.e. 9
-// contiguous ranges of the cell-sorted particle list; the lanes test 32 candidates at a time and
-// append the accepted ones in scan order (ballot + popc). The row is ordered by a rank sort (j is
+// contiguous ranges of the cell-sorted particle list, walked as one list; the lanes test 32
+// candidates at a time and append the accepted ones in scan order (ballot + popc). The row is ordered by a rank sort (j is
 // unique), the old row is searched by bisection for spring carry-over, and the finished rows of the
 // block are written slot-major so that the 32 rows' slot k go out as one coalesced store.
 __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
@@ -427,37 +427,59 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
         const int64_t cy = cell_coord(hp.y, g->lo[1], g->edge, dim1);
         const int64_t cz = cell_coord(hp.z, g->lo[2], g->edge, dim2);
         const int64_t x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < dim0 ? cx + 1 : dim0 - 1;
-        int32_t cnt = 0;
-        for (int64_t z = cz - 1; z <= cz + 1; ++z) {
-            if (z < 0 || z >= dim2) continue;
-            for (int64_t y = cy - 1; y <= cy + 1; ++y) {
-                if (y < 0 || y >= dim1) continue;
+        // the 9 runs of cells (z, y fixed; x0..x1) are 9 contiguous ranges of the sorted list; lane
+        // r < 9 looks up range r, and the ranges are walked as one virtual list of `total`
+        // candidates, 32 per iteration, with the next iteration's indices loaded ahead
+        int32_t rb = 0, rl = 0;
+        if (lane < 9) {
+            const int64_t z = cz - 1 + lane / 3, y = cy - 1 + lane % 3;
+            if (z >= 0 && z < dim2 && y >= 0 && y < dim1) {
                 const int64_t c0 = (z * dim1 + y) * dim0 + x0, c1 = (z * dim1 + y) * dim0 + x1;
-                const int32_t b = cstart[c0], e = cstart[c1] + ccount[c1];
-                for (int32_t q0 = b; q0 < e; q0 += 32) {
-                    const int32_t q = q0 + lane;
-                    int32_t j = -1;
-                    bool in = false;
-                    if (q < e) {
-                        j = sorted[q];
-                        if (j != (int32_t)i && (!B.agg || B.agg[j] == ai)) {  // pairs never cross systems
-                            const float4 fj = x32[j];
-                            const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
-                            const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                            if (d2f < rlo)
-                                in = true;
-                            else if (!(d2f > rhi))
-                                in = sqn(sub(xi_, ld4(x, j))) < rv2;
-                        }
-                    }
-                    const uint32_t bal = __ballot_sync(0xffffffffu, in);
-                    if (in) {
-                        const int32_t pos = cnt + __popc(bal & lt);
-                        if (pos < cap) wraw[pos] = j;
-                    }
-                    cnt += __popc(bal);
-                }
+                rb = cstart[c0];
+                rl = cstart[c1] + ccount[c1] - rb;
             }
+        }
+        int32_t incl = rl;  // inclusive prefix sum of the range lengths over lanes 0..8
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+            const int32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int32_t total = __shfl_sync(0xffffffffu, incl, 8);
+        int32_t rbeg[9], rx[9];  // range begin in the sorted list, exclusive prefix (virtual begin)
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            rbeg[q] = __shfl_sync(0xffffffffu, rb, q);
+            rx[q] = __shfl_sync(0xffffffffu, incl - rl, q);
+        }
+        auto fetch = [&](int32_t t) -> int32_t {  // candidate at virtual index t (t < total)
+            int32_t q = 0;
+#pragma unroll
+            for (int r = 0; r < 9; ++r)
+                if (t >= rx[r]) q = rbeg[r] + (t - rx[r]);
+            return sorted[q];
+        };
+        int32_t cnt = 0;
+        int32_t jnext = lane < total ? fetch(lane) : -1;
+        for (int32_t t0 = 0; t0 < total; t0 += 32) {
+            const int32_t j = jnext;
+            jnext = t0 + 32 + lane < total ? fetch(t0 + 32 + lane) : -1;
+            bool in = false;
+            if (j >= 0 && j != (int32_t)i && (!B.agg || B.agg[j] == ai)) {  // pairs never cross systems
+                const float4 fj = x32[j];
+                const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
+                const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                if (d2f < rlo)
+                    in = true;
+                else if (!(d2f > rhi))
+                    in = sqn(sub(xi_, ld4(x, j))) < rv2;
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, in);
+            if (in) {
+                const int32_t pos = cnt + __popc(bal & lt);
+                if (pos < cap) wraw[pos] = j;
+            }
+            cnt += __popc(bal);
         }
         if (lane == 0) atomicMax(max_row, cnt);
         if (cnt > cap) {
@@ -612,7 +634,7 @@ void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairVi
 
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
                             const dbl4 *al, double dt, double hdt, cudaStream_t st) {
-    const int threads = 256;
+    const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
     kick_drift_fp64<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt);

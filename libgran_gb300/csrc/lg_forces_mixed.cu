@@ -395,7 +395,7 @@ void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairV
 
 void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const double *origin,
                          const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st) {
-    const int threads = 256;
+    const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
     mixed_copies<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, w, origin[0], origin[1], origin[2], agg, orig, x32, v32);
@@ -404,7 +404,7 @@ void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w,
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
                              float4 *v32, cudaStream_t st) {
-    const int threads = 256;
+    const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
     kick_drift_mixed<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt, origin[0], origin[1],

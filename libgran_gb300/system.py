@@ -86,6 +86,23 @@ class System:
         a = _vec(arr, self.n)
         A.check(A.lib().lg_set(self.h, int(field), _dp(a)), "lg_set")
 
+    def get_state(self, out=None):
+        """(x, v, theta, omega) in one call: new (n, 3) arrays, or into the four C-contiguous (n, 3)
+        float64 arrays of `out` (e.g. views of pinned memory)."""
+        if out is None:
+            out = tuple(np.empty((self.n, 3)) for _ in range(4))
+        for a in out:
+            if a.dtype != np.float64 or a.shape != (self.n, 3) or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("state arrays must be C-contiguous (n, 3) float64")
+        A.check(A.lib().lg_get_state(self.h, *[_dp(a) for a in out]), "lg_get_state")
+        return out
+
+    def set_state(self, x=None, v=None, theta=None, omega=None):
+        """Upload any of (x, v, theta, omega) in one call (None leaves a field unchanged)."""
+        arrs = [None if a is None else _vec(a, self.n) for a in (x, v, theta, omega)]
+        ptrs = [None if a is None else _dp(a) for a in arrs]
+        A.check(A.lib().lg_set_state(self.h, *ptrs), "lg_set_state")
+
     def set_threads_per_row(self, T):
         A.check(A.lib().lg_set_threads_per_row(self.h, int(T)), "lg_set_threads_per_row")
 

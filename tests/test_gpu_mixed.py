@@ -128,3 +128,35 @@ def test_mixed_fused_kick_matches_step_by_step():
     for f in STATE_FIELDS + (A.LG_FIELD_A, A.LG_FIELD_ALPHA):
         assert np.array_equal(a.get(f), b.get(f)), f
     assert a.device_errors() == 0
+
+
+@pytest.mark.parametrize("precision", [A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_state_calls_match_field_calls(precision):
+    """lg_set_state / lg_get_state move the same numbers as four lg_set / lg_get calls, skip the
+    fields given as NULL, and leave the system stepping as after the per-field calls."""
+    mat = K.Material()
+    n = 1500
+    x0 = generate_aggregate(41, n, mat.r)
+    v0 = generate_velocities(41, n, 0.1)
+    d = _desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, precision, mat)
+    a = System(d, x0, v0)
+    b = System(d, x0, v0)
+    a.step(mat.dt, 30, 20)
+    st = a.get_state()
+    for f, arr in zip(STATE_FIELDS, st):
+        assert np.array_equal(arr, a.get(f))
+    rng = np.random.default_rng(3)
+    th = rng.normal(size=(n, 3))
+    b.set_state(st[0], st[1], th, st[3])
+    b.set_state(theta=st[2])  # only theta; the others stay
+    for f, arr in zip(STATE_FIELDS, b.get_state()):
+        assert np.array_equal(arr, a.get(f))
+    c = System(d, x0, v0)
+    for f, arr in zip(STATE_FIELDS, st):
+        c.set(f, arr)
+    b.update_neighbor_list()
+    c.update_neighbor_list()
+    b.step(mat.dt, 20, 20)
+    c.step(mat.dt, 20, 20)
+    for f in STATE_FIELDS:
+        assert np.array_equal(b.get(f), c.get(f)), f
