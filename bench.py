@@ -379,7 +379,7 @@ def run_gb300(args, rank, world):
     achieved = bytes_per_particle * N_PART / (per_launch_ms / 1e3) / 1e9
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = read_profile_traffic("forces_compact_mixed_c1")
+    traffic = read_profile_traffic("forces_mixed_c1")
     cpu = cpu_reference_rate(x0, v0, target_s=float(os.environ.get("LG_CPU_SAMPLE_S", "12")))
     batched = None
     if os.environ.get("LG_BENCH_BATCHED", "1") != "0":
@@ -408,7 +408,7 @@ def run_gb300(args, rank, world):
         "e2e": e2e,
         "gpu_launches": tm["launches"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "forces_compact_mixed", "bytes_per_particle": bytes_per_particle,
+                     "traffic": traffic, "kernel": "forces_mixed (contacts || hamaker -> finish)", "bytes_per_particle": bytes_per_particle,
                      "per_launch_ms": per_launch_ms, "peak_source": "measured" if peaks else "fallback"},
         "cpu_baseline": cpu,
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
