@@ -656,13 +656,23 @@ void launch_hamaker(const Params &P, const PairView &PV, const MixedExtra &MX, c
     const size_t smem = sizeof(HamakerSmem) * Sh::kWarps;
     const int64_t rows_per_block = Sh::kRowWarps * 32;
     const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
+    if (smem > 48 * 1024) {  // above the default dynamic shared-memory limit: opt in, once per device
+        static thread_local int attr_device = -1;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (attr_device != dev) {
+            cudaFuncSetAttribute(forces_hamaker_mixed<VERLET, SL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            attr_device = dev;
+        }
+    }
     forces_hamaker_mixed<VERLET, SL><<<blocks, Sh::kWarps * 32, smem, st>>>(P, PV, MX);
 }
 
 // Slices per 32-row group of the Hamaker kernel: the most slices that keep the launch within about
 // two waves of resident warps (152 SMs x 20); rows of long launches are not sliced.
 int hamaker_slices(int64_t n) {
-    if (LG_MIXED_SLICES == 1 || LG_MIXED_SLICES == 2 || LG_MIXED_SLICES == 4) return LG_MIXED_SLICES;
+    if (LG_MIXED_SLICES == 1 || LG_MIXED_SLICES == 2 || LG_MIXED_SLICES == 4 || LG_MIXED_SLICES == 8)
+        return LG_MIXED_SLICES;
     const int64_t two_waves = 2 * 152 * 20;
     const int64_t groups = (n + 31) / 32;
     if (groups * 4 <= two_waves) return 4;
@@ -690,6 +700,10 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
     }
     if (hamaker) {
         switch (hamaker_slices(P.n)) {
+            case 8:
+                if (ver) launch_hamaker<true, 8>(P, PV, MX, st);
+                else launch_hamaker<false, 8>(P, PV, MX, st);
+                break;
             case 4:
                 if (ver) launch_hamaker<true, 4>(P, PV, MX, st);
                 else launch_hamaker<false, 4>(P, PV, MX, st);
