@@ -1152,10 +1152,14 @@ extern "C" int lg_get_observables_select(lg_system *s, int32_t parts, lg_observa
     if (!parts) return LG_OK;
     // every pass stays on the device; one copy back at the end
     StateView S = state_view(s, false);
-    launch_observables(P, S, s->pv[s->pcur], s->bv, m, I, s->obs_scratch, s->obs_out, s->stream,
-                       (parts & LG_OBS_PAIRS) != 0);
-    launch_observables_rg(P.n, s->x, s->obs_scratch, s->obs_out, s->stream);
-    s->launches += 4;
+    if (parts & LG_OBS_STATE) {
+        launch_observables_state(P.n, s->x, s->v[s->vcur], s->w[s->vcur], m, I, s->obs_scratch, s->obs_out, s->stream);
+        s->launches += 4;
+    }
+    if (parts & LG_OBS_PAIRS) {
+        launch_observables_pairs(P, S, s->pv[s->pcur], s->bv, m, I, s->obs_scratch, s->obs_out, s->stream);
+        s->launches += 2;
+    }
     LG_CUDA(cudaGetLastError());
     double h[19];
     LG_CUDA(cudaMemcpyAsync(h, s->obs_out, sizeof(double) * 19, cudaMemcpyDeviceToHost, s->stream));

@@ -53,8 +53,10 @@ constexpr int kCWarps = 2;   // warps per block
 constexpr int kContactLanes = LG_CONTACT_LANES;
 struct ContactSmem {
     float cres[kCQ][6];  // results: linear and angular acceleration
+    float4 chj[kCQ];     // partner's position, high part (read while classifying)
     int32_t cj[kCQ];     // partner
     int32_t ck[kCQ];     // slot in the owner's row
+    uint32_t cfl[kCQ];   // the slot's flags (read while classifying)
     uint8_t cown[kCQ];   // owner lane
     uint32_t cball[kCRound];
     int32_t cbase[kCRound];
@@ -211,9 +213,30 @@ __device__ __forceinline__ void contact_item(const Params &P, const PairView &PV
     const int64_t io = row0 + own;
     const int64_t e = (int64_t)W.ck[q] * n + io;
     const int32_t j = W.cj[q];
-    const uint32_t fl = PV.flags[e];
+    const uint32_t fl = W.cfl[q];
     const bool bonded = (fl & kBonded) != 0;
-    const SepFF sp = separation_ff(W.xh[own], W.xl[own], M.x32[j], M.x32lo[j], bonded ? M.b_fr_hi : M.c_fr_hi,
+    int64_t base, stride;
+    float2 *store;
+    if (bonded) {
+        base = (int64_t)bond_slot_of(fl) * n + io;
+        stride = bs;
+        store = reinterpret_cast<float2 *>(BV.xi);
+    } else {
+        base = e;
+        stride = xs;
+        store = reinterpret_cast<float2 *>(PV.xi);
+    }
+    // every load the pair may need is issued before any arithmetic (one memory round trip): the
+    // partner's low position part, velocities and spin, and the springs of a live slot or bond
+    const float4 lj = M.x32lo[j], vhj = M.v32[j], vlj = M.v32[n + j], wj4 = M.v32[2 * n + j];
+    ff s[3][3] = {};  // springs of a slot that is not live are zero
+    if (bonded || (fl & kXiLive))
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+            const float2 v = store[c * stride + base];
+            s[c / 3][c % 3] = ff{v.x, v.y};
+        }
+    const SepFF sp = separation_ff(W.xh[own], W.xl[own], W.chj[q], lj, bonded ? M.b_fr_hi : M.c_fr_hi,
                                    bonded ? M.b_fr_lo : M.c_fr_lo);
     const f3 dxf = sp.d;
     const float d2f = fdot(dxf, dxf);
@@ -224,30 +247,12 @@ __device__ __forceinline__ void contact_item(const Params &P, const PairView &PV
     if (bonded || overlap > 0.0f) {
         const f3 n3 = fscl(rsd, dxf);
         // relative velocity v_i - v_j from the float-float copies (exact high-part difference)
-        const float4 vhi = W.vh[own], vlo = W.vl[own], vhj = M.v32[j], vlj = M.v32[n + j];
+        const float4 vhi = W.vh[own], vlo = W.vl[own];
         const ff tx = two_sum(vhi.x, -vhj.x), ty = two_sum(vhi.y, -vhj.y), tz = two_sum(vhi.z, -vhj.z);
         const f3 vij0 = fm(tx.hi + (tx.lo + (vlo.x - vlj.x)), ty.hi + (ty.lo + (vlo.y - vlj.y)),
                            tz.hi + (tz.lo + (vlo.z - vlj.z)));
-        const float4 wo4 = W.wh[own], wj4 = M.v32[2 * n + j];
+        const float4 wo4 = W.wh[own];
         const f3 wfi = fm(wo4.x, wo4.y, wo4.z), wfj = fm(wj4.x, wj4.y, wj4.z);
-        int64_t base, stride;
-        float2 *store;
-        if (bonded) {
-            base = (int64_t)bond_slot_of(fl) * n + io;
-            stride = bs;
-            store = reinterpret_cast<float2 *>(BV.xi);
-        } else {
-            base = e;
-            stride = xs;
-            store = reinterpret_cast<float2 *>(PV.xi);
-        }
-        ff s[3][3] = {};  // springs of a slot that is not live are zero
-        if (bonded || (fl & kXiLive))
-#pragma unroll
-            for (int c = 0; c < 9; ++c) {
-                const float2 v = store[c * stride + base];
-                s[c / 3][c % 3] = ff{v.x, v.y};
-            }
         const float kn = bonded ? M.b_k : M.c_k, gn = bonded ? M.b_gn : M.c_gn;
         const float rp = rr - 0.5f * overlap;
         const float v_n = -fdot(vij0, n3);
@@ -358,8 +363,8 @@ __global__ void __launch_bounds__(kCWarps * 32, 8)
     ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, accw[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     __syncwarp();
 
-    // entry of iteration it: partner and slot (-1: none); the next one is loaded while the
-    // current one is classified
+    // entry of iteration it: partner and slot (-1: none); loaded two iterations ahead, and its flags
+    // and partner position one iteration ahead of its classification
     int32_t jn = -1, kn = 0;
     auto load_entry = [&](int64_t it) {
         const int64_t m = it * T + sub;
@@ -374,21 +379,37 @@ __global__ void __launch_bounds__(kCWarps * 32, 8)
             }
         }
     };
-    if (itmax > 0) load_entry(0);
+    int32_t jc = -1, kc = 0;  // the entry being classified, with its flags and partner position
+    uint32_t flc = 0;
+    float4 pjc = hi_i;
+    auto take_entry = [&]() {  // the loaded entry becomes the current one; its data is requested
+        jc = jn;
+        kc = kn;
+        flc = 0;
+        pjc = hi_i;
+        if (jc >= 0) {
+            flc = PV.flags[(int64_t)kc * n + i];
+            pjc = MX.x32[jc];
+        }
+    };
+    if (itmax > 0) {
+        load_entry(0);
+        take_entry();
+        if (itmax > 1) load_entry(1);
+    }
     for (int64_t it0 = 0; it0 < itmax;) {
         int ccount = 0, cdone = 0;
         int64_t it = it0;
         for (;;) {
             const bool take = it < itmax && it - it0 < kCRound && ccount + 32 <= kCQ;
             if (take) {
-                const int32_t j = jn, k = kn;
-                uint32_t fl = 0;
-                float4 pj = hi_i;
-                if (j >= 0) {
-                    fl = PV.flags[(int64_t)k * n + i];
-                    pj = MX.x32[j];
+                const int32_t j = jc, k = kc;
+                const uint32_t fl = flc;
+                const float4 pj = pjc;
+                if (it + 1 < itmax) {
+                    take_entry();
+                    if (it + 2 < itmax) load_entry(it + 2);
                 }
-                if (it + 1 < itmax) load_entry(it + 1);
                 bool cb = false;
                 if (j >= 0) {
                     const float dx = hi_i.x - pj.x, dy = hi_i.y - pj.y, dz = hi_i.z - pj.z;
@@ -406,6 +427,8 @@ __global__ void __launch_bounds__(kCWarps * 32, 8)
                     const int q = ccount + __popc(bc & lt);
                     W.cj[q] = j;
                     W.ck[q] = k;
+                    W.cfl[q] = fl;
+                    W.chj[q] = pj;
                     W.cown[q] = (uint8_t)r;
                 }
                 if (lane == 0) {

@@ -119,6 +119,12 @@ int64_t obs_scratch_doubles(int64_t n);
 void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
                         double inertia, double *scratch, double *out, cudaStream_t st, bool pairs = true);
 void launch_observables_rg(int64_t n, const dbl4 *x, double *scratch, double *out, cudaStream_t st);
+// Handle observables: out[0..14] and out[18] from the particles (launch_observables_state), out[15..17]
+// from the pair slots (launch_observables_pairs); scratch as above.
+void launch_observables_state(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, double mass, double inertia,
+                              double *scratch, double *out, cudaStream_t st);
+void launch_observables_pairs(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
+                              double inertia, double *scratch, double *out, cudaStream_t st);
 // Per-system observables of a batch: out[s * 20 + c] = column sums over system s's particles
 // (rows from launch_observables' scratch), then column 18 = sum |x - c_s|^2 with centres from
 // centres[3 s ..].

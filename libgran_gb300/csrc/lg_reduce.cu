@@ -113,6 +113,95 @@ __global__ void __launch_bounds__(1024) obs_reduce(int64_t n, const double *__re
 
 int64_t obs_scratch_doubles(int64_t n) { return n * kObs; }
 
+// Per-particle observables (columns 0..14 of the row layout above, and 18) by a two-level
+// fixed-order reduction: every block of 256 particles reduces its terms with a shared-memory tree
+// into one row of partial sums, then one block sums the rows in order. Columns 12..14 (sum of x)
+// give the centre of mass on the device, which the radius-of-gyration pass reads back.
+constexpr int kObsBlock = 256;
+constexpr int kObsCols = 16;  // 15 terms + |x - c|^2
+
+__device__ __forceinline__ double obs_block_sum(double v, double *sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = kObsBlock / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kObsBlock) obs_state_terms(int64_t n, const dbl4 *__restrict__ x,
+                                                             const dbl4 *__restrict__ v, const dbl4 *__restrict__ w,
+                                                             double m, double I, double *__restrict__ part) {
+    __shared__ double sh[kObsBlock];
+    const int64_t i = blockIdx.x * (int64_t)kObsBlock + threadIdx.x;
+    double t[15];
+#pragma unroll
+    for (int c = 0; c < 15; ++c) t[c] = 0.0;
+    if (i < n) {
+        const d3 vi = ld4(v, i), wi = ld4(w, i), xi = ld4(x, i);
+        t[0] = m * dot(vi, vi) / 2.0 + I * dot(wi, wi) / 2.0;
+        t[1] = m * dot(vi, vi);
+        t[2] = I * dot(wi, wi);
+        t[3] = vi.x; t[4] = vi.y; t[5] = vi.z;
+        const d3 Iw = scl(I, wi);
+        t[6] = Iw.x; t[7] = Iw.y; t[8] = Iw.z;
+        const d3 L = crs(xi, scl(m, vi));
+        t[9] = L.x; t[10] = L.y; t[11] = L.z;
+        t[12] = xi.x; t[13] = xi.y; t[14] = xi.z;
+    }
+    for (int c = 0; c < 15; ++c) {
+        const double r = obs_block_sum(t[c], sh);
+        if (threadIdx.x == 0) part[blockIdx.x * kObsCols + c] = r;
+    }
+}
+
+// One block: out[c0..c1) = sums over the nb rows of part (threads take rows t, t + 256, ... in
+// order, then the block tree).
+__global__ void __launch_bounds__(kObsBlock) obs_state_combine(int nb, const double *__restrict__ part, int c0, int c1,
+                                                               int out0, double *__restrict__ out) {
+    __shared__ double sh[kObsBlock];
+    for (int c = c0; c < c1; ++c) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < nb; b += kObsBlock) acc += part[(int64_t)b * kObsCols + c];
+        const double r = obs_block_sum(acc, sh);
+        if (threadIdx.x == 0) out[out0 + c - c0] = r;
+    }
+}
+
+__global__ void __launch_bounds__(kObsBlock) obs_state_rg(int64_t n, const dbl4 *__restrict__ x,
+                                                          const double *__restrict__ sums, double *__restrict__ part) {
+    __shared__ double sh[kObsBlock];
+    const int64_t i = blockIdx.x * (int64_t)kObsBlock + threadIdx.x;
+    double t = 0.0;
+    if (i < n) {
+        const double nn = (double)n;
+        const d3 q = sub(ld4(x, i), mk3(sums[12] / nn, sums[13] / nn, sums[14] / nn));
+        t = dot(q, q);
+    }
+    const double r = obs_block_sum(t, sh);
+    if (threadIdx.x == 0) part[blockIdx.x * kObsCols + 15] = r;
+}
+
+void launch_observables_state(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, double mass, double inertia,
+                              double *scratch, double *out, cudaStream_t st) {
+    const int nb = (int)((n + kObsBlock - 1) / kObsBlock);
+    obs_state_terms<<<nb, kObsBlock, 0, st>>>(n, x, v, w, mass, inertia, scratch);
+    obs_state_combine<<<1, kObsBlock, 0, st>>>(nb, scratch, 0, 15, 0, out);
+    obs_state_rg<<<nb, kObsBlock, 0, st>>>(n, x, out, scratch);
+    obs_state_combine<<<1, kObsBlock, 0, st>>>(nb, scratch, 15, 16, 18, out);
+}
+
+void launch_observables_pairs(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
+                              double inertia, double *scratch, double *out, cudaStream_t st) {
+    const int64_t n = P.n;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    obs_rows<<<blocks, 256, 0, st>>>(P, S, PV, BV, mass, inertia, 1, scratch);
+    obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 15, 18, out);
+}
+
 // out receives the column sums 0..17 (the pair columns 15..17 are zero unless `pairs`). The caller
 // synchronises the stream before reading out (device memory).
 void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
