@@ -301,26 +301,32 @@ static int set_mixed_origins(lg_system *s, const double *x) {
     return LG_OK;
 }
 
-// New positions keep the current origins (and the CUDA graphs that hold them) while every offset
-// from its system's origin stays within four times the extent the origin was set up with: the
-// culling margins of set_cull_radii allow for exactly that.
-static bool origins_cover(const lg_system *s, const double *x) {
-    auto within = [&](int64_t b, int64_t e, double ox, double oy, double oz, double ext) {
-        const double lim = 4.0 * ext;
-        for (int64_t i = b; i < e; ++i)
-            if (!(std::fabs(x[3 * i] - ox) <= lim && std::fabs(x[3 * i + 1] - oy) <= lim &&
-                  std::fabs(x[3 * i + 2] - oz) <= lim))
-                return false;
-        return true;
-    };
-    if (s->n_systems > 0) {
-        for (int64_t q = 0; q < s->n_systems; ++q) {
-            const dbl4 &o = s->h_orig[(size_t)q];
-            if (!within(s->sys_off[q], s->sys_off[q + 1], o.x, o.y, o.z, o.w)) return false;
-        }
-        return true;
-    }
-    return within(0, s->P.n, s->origin[0], s->origin[1], s->origin[2], s->origin[3]);
+// After new positions (x: the caller's host array) or velocities: refresh the float-float copies. The
+// origins (and the CUDA graphs that hold them) are kept while every offset from its system's origin
+// stays within four times the extent the origin was set up with (the culling margins of
+// set_cull_radii allow for exactly that); the copy kernel checks this on the device, and only when
+// it fails are the origins set up again from x and the copies redone.
+static int refresh_mixed_copies(lg_system *s, const double *x) {
+    const int64_t n = s->P.n;
+    int32_t *flag = x ? s->d_flag : nullptr;
+    if (flag) LG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int32_t), s->stream));
+    launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32, s->v32,
+                        s->stream, flag);
+    s->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    if (!flag) return LG_OK;
+    int32_t h = 0;
+    LG_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    if (!h) return LG_OK;
+    LG_TRY(set_mixed_origins(s, x));  // positions moved far: new origins and culling radii
+    set_cull_radii(s);
+    s->drop_graphs();
+    launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32, s->v32,
+                        s->stream);
+    s->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    return LG_OK;
 }
 
 // lg_get / lg_set: the caller's [n][3] array moves in one copy to device scratch (the observables
@@ -823,6 +829,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         LG_TRY(s->alloc(&s->x32, 2 * (size_t)n));  // float-float: high parts, then low parts
         LG_TRY(s->alloc(&s->v32, 3 * (size_t)n));  // v high parts, v low parts, spins
         LG_TRY(s->alloc(&s->csum, 3 * (size_t)n));
+        LG_TRY(s->alloc(&s->d_flag, 1));
         LG_TRY(s->alloc(&s->hsum, 2 * (size_t)n));
         LG_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
         LG_CUDA(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
@@ -1038,17 +1045,8 @@ extern "C" int lg_set(lg_system *s, int field, const double *in) {
     dbl4 *p = field_ptr(s, field);
     if (!p || !in) return lg_fail(LG_E_INVALID, "lg_set: bad field %d or null input", field);
     LG_TRY(upload_staged(s, p, in));
-    if (s->x32 && (field == LG_FIELD_X || field == LG_FIELD_V || field == LG_FIELD_OMEGA)) {
-        if (field == LG_FIELD_X && !origins_cover(s, in)) {
-            LG_TRY(set_mixed_origins(s, in));  // positions moved far: new origins and culling radii
-            set_cull_radii(s);
-            s->drop_graphs();  // captured launches hold the old values
-        }
-        launch_mixed_copies(s->P.n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32,
-                            s->v32, s->stream);
-        s->launches += 1;
-        LG_CUDA(cudaGetLastError());
-    }
+    if (s->x32 && (field == LG_FIELD_X || field == LG_FIELD_V || field == LG_FIELD_OMEGA))
+        LG_TRY(refresh_mixed_copies(s, field == LG_FIELD_X ? in : nullptr));
     return LG_OK;
 }
 
@@ -1082,17 +1080,7 @@ extern "C" int lg_set_state(lg_system *s, const double *x, const double *v, cons
         s->launches += 1;
     }
     LG_CUDA(cudaGetLastError());
-    if (s->x32 && (x || v || w)) {
-        if (x && !origins_cover(s, x)) {
-            LG_TRY(set_mixed_origins(s, x));  // positions moved far: new origins and culling radii
-            set_cull_radii(s);
-            s->drop_graphs();
-        }
-        launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32, s->v32,
-                            s->stream);
-        s->launches += 1;
-        LG_CUDA(cudaGetLastError());
-    }
+    if (s->x32 && (x || v || w)) LG_TRY(refresh_mixed_copies(s, x));
     LG_CUDA(cudaStreamSynchronize(s->stream));  // the caller may reuse its buffers on return
     return LG_OK;
 }

@@ -48,6 +48,7 @@ struct lg_system {
     float4 *v32 = nullptr;  // mixed: [3n] float-float velocities, FP32 spins
     float4 *csum = nullptr;    // mixed: [3n] contact sums (float-float)
     float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
+    int32_t *d_flag = nullptr;  // mixed: device flag of the float-float copy check
     double origin[4] = {0.0, 0.0, 0.0, 0.0};  // mixed: origin of the float-float positions, extent in [3]
     double r_max = 0.0;                        // mixed: largest particle radius of the functors
     double ext_max = 0.0;                      // mixed: largest extent of a system about its origin

@@ -331,14 +331,28 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
 
 // Float-float copies of the positions (relative to the system origin; in a batch every system has
 // its own origin) and of the velocities.
+// With `uncovered` set, also flags (*uncovered = 1) any position further than four times its system's
+// extent (orig.w, or `oext` for a single system) from the origin in some coordinate.
 __global__ void mixed_copies(int64_t n, const dbl4 *__restrict__ x, const dbl4 *__restrict__ v,
-                             const dbl4 *__restrict__ w, double ox, double oy, double oz,
+                             const dbl4 *__restrict__ w, double ox, double oy, double oz, double oext,
                              const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig, float4 *__restrict__ x32,
-                             float4 *__restrict__ v32) {
+                             float4 *__restrict__ v32, int32_t *uncovered) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    rel_ff(ld4(x, i), ox, oy, oz, agg, orig, i, n, x32);
+    const d3 xi = ld4(x, i);
+    rel_ff(xi, ox, oy, oz, agg, orig, i, n, x32);
     vel_ff(ld4(v, i), ld4(w, i), i, n, v32);
+    if (uncovered) {
+        if (agg) {
+            const dbl4 o = orig[agg[i]];
+            ox = o.x;
+            oy = o.y;
+            oz = o.z;
+            oext = o.w;
+        }
+        const double lim = 4.0 * oext;
+        if (!(fabs(xi.x - ox) <= lim && fabs(xi.y - oy) <= lim && fabs(xi.z - oz) <= lim)) atomicOr(uncovered, 1);
+    }
 }
 
 // Kick + drift of the mixed path: FP64 integration, then the float-float position copy.
@@ -394,11 +408,13 @@ void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairV
 }
 
 void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const double *origin,
-                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st) {
+                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st,
+                         int32_t *uncovered) {
     const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
-    mixed_copies<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, w, origin[0], origin[1], origin[2], agg, orig, x32, v32);
+    mixed_copies<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, w, origin[0], origin[1], origin[2], origin[3], agg, orig,
+                                                       x32, v32, uncovered);
 }
 
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,

@@ -89,8 +89,11 @@ void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairV
 // Float-float copies for the mixed kernels: x32 (2n entries) from the positions, v32 (3n entries)
 // from the velocities and spins (see MixedExtra); origin[0..2] is the origin of a single system,
 // orig[] those of each system of a batch.
+// With `uncovered`, also sets *uncovered when a position lies beyond four times its system's extent
+// (origin[3], orig[].w) from the origin: the origins must then be set up again.
 void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const double *origin,
-                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st);
+                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st,
+                         int32_t *uncovered = nullptr);
 // Kick + drift of the mixed path; also refreshes x32 and v32.
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
