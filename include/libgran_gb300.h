@@ -43,6 +43,9 @@ extern "C" {
 #define LG_BINARY_CONTACT 1          /* contact_force_functor, contact_force/contact_force.h:8-157 */
 #define LG_BINARY_SINTER 2           /* alt_sinter_functor, sinter_bridge/alt_sinter_bridge.h:17-180 */
 #define LG_BINARY_BREAKING_SINTER 3  /* alt_breaking_sinter_functor, alt_breaking_sinter_bridge.h:16-166 */
+#define LG_BINARY_SINTER_CONNECTORS 4  /* sinter_functor + sinter_step_handler, sinter_bridge.h:14-272:
+                                          five connector springs per bond, moved with the particles by
+                                          the integrator's increments; FP64 precision only */
 
 /* Which Hamaker functor (if any) is folded in after the binary functor. */
 #define LG_HAMAKER_NONE 0
@@ -89,6 +92,14 @@ typedef struct lg_sinter_params {
     double critical_separation;
 } lg_sinter_params;
 
+/* sinter_functor(n_part, k_d, gamma_d, <contact parameters>, ..., random_unit_vector_generator,
+ * critical_separation), sinter_bridge.h:100-136: the connector springs' stiffness and damping and
+ * the bonding distance; the contact parameters are lg_system_desc::contact. */
+typedef struct lg_connector_params {
+    double k_d, gamma_d;
+    double critical_separation;
+} lg_connector_params;
+
 /* hamaker_functor(A, h0, r_part, mass, ...)                hamaker_force.h:20-26
  * limited_range_hamaker_functor(A, h0, r_cutoff, r_part, mass, ...) limited_range_hamaker_force.h:20-27
  * simplified_hamaker_functor(A, h0, r_part, mass, ...)     simplified_hamaker_force.h:10-16
@@ -128,6 +139,13 @@ typedef struct lg_system_desc {
     int32_t threads_per_row; /* lanes per row group of the force kernel (see lg_set_threads_per_row);
                                 0 picks automatically; used from the construction-time evaluation on */
     int32_t force_kernel;    /* LG_FORCE_KERNEL_*: which force kernel evaluates the pairs */
+    /* LG_BINARY_SINTER_CONNECTORS: */
+    lg_connector_params connector;
+    const double *connector_axes; /* per bond in detection order (i ascending, then j > i), the unit
+                                     vector that sinter_bridge.h:169-175 draws from the caller's
+                                     generator for it (3 doubles); it must not be parallel to the
+                                     bond axis */
+    int64_t n_connector_axes;     /* must equal the number of bonds found */
 } lg_system_desc;
 
 /* Force kernels. Both give deterministic sums; in FP64 both add each row in ascending j, and the

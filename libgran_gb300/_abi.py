@@ -11,6 +11,7 @@ LG_OK = 0
 LG_E_INVALID, LG_E_CUDA, LG_E_NOMEM, LG_E_STATE, LG_E_DEVICE = -1, -2, -3, -4, -5
 
 LG_BINARY_NONE, LG_BINARY_CONTACT, LG_BINARY_SINTER, LG_BINARY_BREAKING_SINTER = 0, 1, 2, 3
+LG_BINARY_SINTER_CONNECTORS = 4
 LG_HAMAKER_NONE, LG_HAMAKER_FULL, LG_HAMAKER_LIMITED, LG_HAMAKER_SIMPLIFIED = 0, 1, 2, 3
 LG_NECK_PER_BOND, LG_NECK_REFERENCE_INDEXING = 0, 1
 LG_PRECISION_FP64, LG_PRECISION_MIXED = 0, 1
@@ -33,6 +34,10 @@ class lg_sinter_params(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "k", "gamma_n", "k_t", "gamma_t", "k_r", "gamma_r", "k_o", "gamma_o",
         "r_part", "mass", "inertia", "dt", "critical_separation")]
+
+
+class lg_connector_params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("k_d", "gamma_d", "critical_separation")]
 
 
 class lg_hamaker_params(C.Structure):
@@ -62,7 +67,8 @@ class lg_system_desc(C.Structure):
                 ("hamaker", lg_hamaker_params), ("neck_mode", C.c_int32), ("pairs", C.c_int32),
                 ("r_verlet", C.c_double), ("precision", C.c_int32), ("n_facets", C.c_int32),
                 ("facet_auto_move", C.c_int32), ("max_neighbors", C.c_int32), ("threads_per_row", C.c_int32),
-                ("force_kernel", C.c_int32)]
+                ("force_kernel", C.c_int32), ("connector", lg_connector_params),
+                ("connector_axes", C.POINTER(C.c_double)), ("n_connector_axes", C.c_int64)]
 
 
 class lg_observables(C.Structure):

@@ -4,7 +4,10 @@ aggregate workloads (r = 14 nm soot monomers, density 1700 kg/m^3).
 Reference: the constants of test/contact.cpp:37-51 (rho, r_part, mass, inertia, k, gamma_n, mu, phi,
 mu_o, gamma_t, gamma_r, gamma_o) and the functor argument order of contact_force.h:10-30.
 """
+import ctypes as C
 import math
+
+import numpy as np
 
 from . import _abi as A
 
@@ -70,6 +73,41 @@ def make_desc(n_part, binary_model=A.LG_BINARY_CONTACT, hamaker_model=A.LG_HAMAK
 # --------------------------------------------------------------------------------------------
 # Synthetic aggregate workloads (seeded random-sequential-attachment aggregates)
 # --------------------------------------------------------------------------------------------
+def connector_bonds(x0, r_part, critical_separation):
+    """Bonds of the 5-connector sinter model in its detection order (sinter_bridge.h:146-160): every
+    pair i < j with |(|x_j - x_i| - 2 r)| <= critical_separation, i ascending, then j ascending.
+    Returns an (nb, 2) int64 array."""
+    x0 = np.asarray(x0, dtype=np.float64)
+    n = len(x0)
+    out = []
+    for i in range(n - 1):
+        d = x0[i + 1:] - x0[i]
+        g = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]) - 2.0 * r_part
+        for k in np.nonzero(~(np.abs(g) > critical_separation))[0]:
+            out.append((i, i + 1 + int(k)))
+    return np.array(out, dtype=np.int64).reshape(-1, 2)
+
+
+def set_connectors(desc, k_d, gamma_d, critical_separation, axes):
+    """Configure a descriptor for LG_BINARY_SINTER_CONNECTORS: connector stiffness/damping, bonding
+    distance and one unit axis per bond (the vectors the reference draws from its generator). The
+    axes array is kept alive on the descriptor."""
+    axes = np.ascontiguousarray(np.asarray(axes, dtype=np.float64).reshape(-1, 3))
+    desc.binary_model = A.LG_BINARY_SINTER_CONNECTORS
+    desc.connector = A.lg_connector_params(k_d, gamma_d, critical_separation)
+    desc.connector_axes = axes.ctypes.data_as(C.POINTER(C.c_double))
+    desc.n_connector_axes = len(axes)
+    desc._axes_keepalive = axes
+    return desc
+
+
+def random_unit_axes(count, seed):
+    """Seeded unit vectors (uniform in the cube, normalised), one per bond."""
+    rng = np.random.default_rng(seed)
+    v = rng.uniform(-1.0, 1.0, size=(count, 3))
+    return v / np.linalg.norm(v, axis=1)[:, None]
+
+
 class Material:
     """Constants of the aggregate workloads: r = 14 nm, rho = 1700 kg/m^3, k_n = 1e4 N/m,
     tangential/rolling/torsion stiffness 0.5 k_n, damping ratio 0.1 on the reduced mass m/2,

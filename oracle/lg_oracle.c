@@ -10,6 +10,8 @@
  *   contact_force_functor::compute_shear_contribution contact_force/contact_force.h:105-147
  *   alt_sinter_functor (ctor bond detection, bonded branch)  sinter_bridge/alt_sinter_bridge.h:19-156
  *   alt_breaking_sinter_functor                   sinter_bridge/alt_breaking_sinter_bridge.h:17-131
+ *   sinter_functor (ctor connectors, bonded branch) sinter_bridge/sinter_bridge.h:100-268
+ *   sinter_step_handler (connector increments)     sinter_bridge/sinter_bridge.h:14-94
  *   hamaker_functor                               hamaker_force/hamaker_force.h:28-43
  *   limited_range_hamaker_functor                 hamaker_force/limited_range_hamaker_force.h:29-47
  *   simplified_hamaker_functor                    hamaker_force/simplified_hamaker_force.h:18-31
@@ -27,7 +29,11 @@
  *
  *   construction:  (a, alpha) = F(x0, v0, theta0, omega0)          one force evaluation
  *   do_step(dt):   v += a*(dt/2);  omega += alpha*(dt/2)            half kick
- *                  x += v*dt;      theta += omega*dt                drift
+ *                  x += v*dt;      theta += omega*dt                drift (per particle: x, then
+ *                                                                   theta; with the 5-connector
+ *                                                                   sinter model these are the step
+ *                                                                   handler's increment_x and
+ *                                                                   increment_theta)
  *                  (a, alpha) = F(x, v, theta, omega)               one force evaluation
  *                  v += a*(dt/2);  omega += alpha*(dt/2)            half kick
  *   F: for each i, acc = 0; for each j != i in ascending order (or in i's Verlet row, ascending):
@@ -87,6 +93,8 @@ typedef struct {
     int32_t intact;  /* bonded_contacts[i*n+j] */
     double strength; /* neck strength read for (i, j) */
     v3 xi[3];        /* alt_sinter contact_springs[i*n+j] (bond springs) */
+    v3 cn[5];        /* sinter_functor spring_connectors[i*n+j]: the five connectors on particle i */
+    int32_t rev;     /* index of the bond (j, i) in row j (5-connector model) */
 } bond;
 
 typedef struct {
@@ -225,6 +233,27 @@ static int bond_functor(const lg_sinter_params *p, v3 xi_, v3 xj_, v3 vi, v3 vj,
     *oa = dvs(f_tot, p->mass);
     *oal = dvs(tau_tot, p->inertia);
     return brk;
+}
+
+/* sinter_functor::bonded_contact_accelerations, sinter_bridge.h:238-266: five connector springs
+ * between the connectors of i (ci) and of j (cj); rest lengths 2 r for the four side springs and 0
+ * for the centre spring (sinter_bridge.h:201-206). */
+static void connector_functor(const lg_connector_params *cp, double r, double mass, double inertia, v3 xi_, v3 xj_,
+                              v3 vi, v3 vj, v3 wi, v3 wj, const v3 *ci, const v3 *cj, v3 *pa, v3 *pal) {
+    v3 force = ZERO, torque = ZERO;
+    for (int k = 0; k < 5; ++k) {
+        v3 spring = sub(cj[k], ci[k]);
+        double len = nrm(spring);
+        double eq = k < 4 ? 2.0 * r : 0.0;
+        v3 cvi = add(vi, crs(wi, sub(ci[k], xi_)));
+        v3 cvj = add(vj, crs(wj, sub(cj[k], xj_)));
+        v3 rel = sub(cvj, cvi);
+        v3 df = add(scl(-(eq - len) * cp->k_d, nrmz(spring)), scl(cp->gamma_d, rel));
+        force = add(force, df);
+        torque = add(torque, crs(sub(ci[k], xi_), df));
+    }
+    *pa = dvs(force, mass);
+    *pal = dvs(torque, inertia);
 }
 
 static inline double square_(double x) { return x * x; }
@@ -397,6 +426,27 @@ static int64_t detect_bonds(const lg_system_desc *d, const double *x0, int64_t n
     return nb;
 }
 
+/* sinter_functor ctor bond test, sinter_bridge.h:146-160: every pair i < j (i ascending, then j)
+ * with |(|x_j - x_i| - 2 r)| <= critical_separation; no cycle check. */
+static int64_t detect_bonds_connectors(const lg_system_desc *d, const double *x0, int64_t n, ipair **out) {
+    const double r = d->contact.r_part, dc = d->connector.critical_separation;
+    int64_t cap = 16, nb = 0;
+    ipair *pr = (ipair *)malloc(sizeof(ipair) * cap);
+    for (int64_t i = 0; i + 1 < n; ++i) {
+        v3 xi_ = ld(x0, i);
+        for (int64_t j = i + 1; j < n; ++j) {
+            double g = nrm(sub(ld(x0, j), xi_)) - 2.0 * r;
+            if (fabs(g) > dc) continue;
+            if (nb == cap) { cap *= 2; pr = (ipair *)realloc(pr, sizeof(ipair) * cap); }
+            pr[nb].i = (int32_t)i;
+            pr[nb].j = (int32_t)j;
+            ++nb;
+        }
+    }
+    *out = pr;
+    return nb;
+}
+
 static int cmp_bond(const void *a, const void *b) {
     int32_t x = ((const bond *)a)->j, y = ((const bond *)b)->j;
     return (x > y) - (x < y);
@@ -524,8 +574,13 @@ static void eval_forces(lgo_system *s) {
             v3 pa = ZERO, pal = ZERO;
             int have = 0;
             if (bm != LG_BINARY_NONE) {
-                bond *b = (bm == LG_BINARY_SINTER || bm == LG_BINARY_BREAKING_SINTER) ? find_bond(r, (int32_t)j) : NULL;
-                if (b && b->intact) {
+                bond *b = (bm == LG_BINARY_SINTER || bm == LG_BINARY_BREAKING_SINTER || bm == LG_BINARY_SINTER_CONNECTORS)
+                              ? find_bond(r, (int32_t)j) : NULL;
+                if (b && b->intact && bm == LG_BINARY_SINTER_CONNECTORS) {
+                    const bond *bj = &s->rows[j].b[b->rev];
+                    connector_functor(&d->connector, d->contact.r_part, d->contact.mass, d->contact.inertia, xi_, xj_,
+                                      vi, vj, wi, wj, b->cn, bj->cn, &pa, &pal);
+                } else if (b && b->intact) {
                     int brk = bond_functor(&d->sinter, xi_, xj_, vi, vj, wi, wj, b->xi, breaking, b->strength, &pa, &pal);
                     if (brk) b->intact = 0;
                 } else {
@@ -648,6 +703,58 @@ lgo_system *lgo_create(const lg_system_desc *d, const double *x0, const double *
         free(pstr);
         free(pr);
     }
+    if (d->binary_model == LG_BINARY_SINTER_CONNECTORS) {
+        ipair *pr = NULL;
+        int64_t nb = detect_bonds_connectors(d, x0, s->n, &pr);
+        if (!d->connector_axes || d->n_connector_axes != nb) {
+            free(pr);
+            lgo_destroy(s);
+            return NULL;
+        }
+        s->n_bonds_initial = 2 * nb;
+        int32_t *cnt = (int32_t *)calloc((size_t)(s->n > 0 ? s->n : 1), sizeof(int32_t));
+        for (int64_t b = 0; b < nb; ++b) { cnt[pr[b].i]++; cnt[pr[b].j]++; }
+        for (int64_t i = 0; i < s->n; ++i) {
+            s->rows[i].b = (bond *)calloc((size_t)(cnt[i] > 0 ? cnt[i] : 1), sizeof(bond));
+            s->rows[i].nb = 0;
+        }
+        const double r = d->contact.r_part;
+        for (int64_t b = 0; b < nb; ++b) {  /* connectors, sinter_bridge.h:163-197 */
+            const int32_t i = pr[b].i, j = pr[b].j;
+            v3 pi = ld(x0, i), pj = ld(x0, j);
+            v3 ni = nrmz(sub(pj, pi)), nj = neg(ni);
+            v3 v = ld(d->connector_axes, b);
+            v3 db = crs(v, nj);
+            if (nrm(db) == 0.0) {  /* the reference draws again; the caller's axis must not be parallel */
+                free(pr);
+                free(cnt);
+                lgo_destroy(s);
+                return NULL;
+            }
+            v3 ds = sub(v, scl(dot(v, ni), ni));
+            db = nrmz(db);
+            ds = nrmz(ds);
+            bond *bi = &s->rows[i].b[s->rows[i].nb++];
+            bond *bj = &s->rows[j].b[s->rows[j].nb++];
+            bi->j = j; bi->intact = 1; bi->strength = INFINITY;
+            bj->j = i; bj->intact = 1; bj->strength = INFINITY;
+            bi->cn[0] = add(pi, scl(r, ds)); bi->cn[1] = sub(pi, scl(r, ds));
+            bi->cn[2] = add(pi, scl(r, db)); bi->cn[3] = sub(pi, scl(r, db));
+            bi->cn[4] = add(pi, scl(r, ni));
+            bj->cn[0] = add(pj, scl(r, ds)); bj->cn[1] = sub(pj, scl(r, ds));
+            bj->cn[2] = add(pj, scl(r, db)); bj->cn[3] = sub(pj, scl(r, db));
+            bj->cn[4] = add(pj, scl(r, nj));
+        }
+        for (int64_t i = 0; i < s->n; ++i)
+            if (s->rows[i].nb > 1) qsort(s->rows[i].b, (size_t)s->rows[i].nb, sizeof(bond), cmp_bond);
+        for (int64_t i = 0; i < s->n; ++i)
+            for (int32_t q = 0; q < s->rows[i].nb; ++q) {
+                bond *bq = &s->rows[i].b[q];
+                bq->rev = (int32_t)(find_bond(&s->rows[bq->j], (int32_t)i) - s->rows[bq->j].b);
+            }
+        free(cnt);
+        free(pr);
+    }
     build_rows(s, 0);
     eval_forces(s);
     return s;
@@ -684,9 +791,27 @@ int lgo_step(lgo_system *s, double dt, int64_t nsteps, int64_t rebuild_every) {
             s->v[q] += s->a[q] * hdt;
             s->om[q] += s->al[q] * hdt;
         }
-        for (int64_t q = 0; q < 3 * n; ++q) {
-            s->x[q] += s->v[q] * dt;
-            s->th[q] += s->om[q] * dt;
+        if (s->d.binary_model == LG_BINARY_SINTER_CONNECTORS) {
+            /* sinter_step_handler: increment_x moves the particle and its connectors by dx,
+             * increment_theta turns the connectors by dtheta about the (moved) centre
+             * (sinter_bridge.h:24-42, 55-75) */
+            for (int64_t i = 0; i < n; ++i) {
+                v3 dx = mk(s->v[3 * i] * dt, s->v[3 * i + 1] * dt, s->v[3 * i + 2] * dt);
+                v3 xn = add(ld(s->x, i), dx);
+                stv(s->x, i, xn);
+                row *r = &s->rows[i];
+                for (int32_t q = 0; q < r->nb; ++q)
+                    for (int k = 0; k < 5; ++k) r->b[q].cn[k] = add(r->b[q].cn[k], dx);
+                v3 dth = mk(s->om[3 * i] * dt, s->om[3 * i + 1] * dt, s->om[3 * i + 2] * dt);
+                stv(s->th, i, add(ld(s->th, i), dth));
+                for (int32_t q = 0; q < r->nb; ++q)
+                    for (int k = 0; k < 5; ++k) r->b[q].cn[k] = add(r->b[q].cn[k], crs(dth, sub(r->b[q].cn[k], xn)));
+            }
+        } else {
+            for (int64_t q = 0; q < 3 * n; ++q) {
+                s->x[q] += s->v[q] * dt;
+                s->th[q] += s->om[q] * dt;
+            }
         }
         eval_forces(s);
         for (int64_t q = 0; q < 3 * n; ++q) {
@@ -796,7 +921,7 @@ int lgo_observables(lgo_system *s, lg_observables *o) {
     double m, I;
     if (d->binary_model == LG_BINARY_SINTER || d->binary_model == LG_BINARY_BREAKING_SINTER) {
         m = d->sinter.mass; I = d->sinter.inertia;
-    } else if (d->binary_model == LG_BINARY_CONTACT) {
+    } else if (d->binary_model == LG_BINARY_CONTACT || d->binary_model == LG_BINARY_SINTER_CONNECTORS) {
         m = d->contact.mass; I = d->contact.inertia;
     } else {
         m = d->hamaker.mass; I = d->contact.inertia;
@@ -837,7 +962,14 @@ int lgo_observables(lgo_system *s, lg_observables *o) {
             double dist = nrm(sub(xi_, xj_));
             bond *b = r->b ? find_bond(r, e->j) : NULL;
             double u = 0.0;
-            if (b && b->intact) {
+            if (b && b->intact && d->binary_model == LG_BINARY_SINTER_CONNECTORS) {
+                const bond *bj = &s->rows[e->j].b[b->rev];
+                for (int k = 0; k < 5; ++k) {
+                    double dl = (k < 4 ? 2.0 * d->contact.r_part : 0.0) - nrm(sub(bj->cn[k], b->cn[k]));
+                    u += 0.5 * d->connector.k_d * dl * dl;
+                }
+                nbond++;
+            } else if (b && b->intact) {
                 double dl = 2.0 * d->sinter.r_part - dist;
                 u += 0.5 * d->sinter.k * dl * dl;
                 u += 0.5 * d->sinter.k_t * sqn(b->xi[0]) + 0.5 * d->sinter.k_r * sqn(b->xi[1]) + 0.5 * d->sinter.k_o * sqn(b->xi[2]);

@@ -7,6 +7,9 @@ void *lgref_create(const lg_system_desc *d, const double *x0, const double *v0, 
                    const lg_facet_desc *facets, const double *neck, int64_t n_neck) {
     bool brk = d->binary_model == LG_BINARY_BREAKING_SINTER;
     bool lim = d->hamaker_model == LG_HAMAKER_LIMITED;
+    if (d->binary_model == LG_BINARY_SINTER_CONNECTORS)
+        return lim ? lgref_make_conn_limited(d, x0, v0, th0, om0, facets, neck, n_neck)
+                   : lgref_make_conn_full(d, x0, v0, th0, om0, facets, neck, n_neck);
     if (brk && lim) return lgref_make_brk_limited(d, x0, v0, th0, om0, facets, neck, n_neck);
     if (brk) return lgref_make_brk_full(d, x0, v0, th0, om0, facets, neck, n_neck);
     if (lim) return lgref_make_alt_limited(d, x0, v0, th0, om0, facets, neck, n_neck);

@@ -1,8 +1,9 @@
 // harness_tu.cpp -- compiles libgran's own functor headers (from the libgran source tree, unmodified)
 // on lgref_vec3 and wires them into the harness system loop. TEST INFRASTRUCTURE ONLY.
-// Compiled four times: LGREF_BREAKING selects alt_breaking_sinter_bridge.h instead of
-// alt_sinter_bridge.h, LGREF_LIMITED selects limited_range_hamaker_force.h instead of
-// hamaker_force.h + simplified_hamaker_force.h.
+// Compiled six times: LGREF_BREAKING selects alt_breaking_sinter_bridge.h and LGREF_CONNECTORS
+// sinter_bridge.h (the 5-connector model with its step handler) instead of alt_sinter_bridge.h;
+// LGREF_LIMITED selects limited_range_hamaker_force.h instead of hamaker_force.h +
+// simplified_hamaker_force.h.
 #include <cmath>
 #include <math.h>      // ::abs(double), as in an Eigen build (alt_sinter_bridge.h:69 calls abs unqualified)
 #include <iostream>    // alt_sinter_bridge.h:71 uses std::cout without including it
@@ -28,7 +29,9 @@
 #include <libgran/contact_force/surface_contact_force.h>
 #include <libgran/hamaker_force/surface_hamaker_force.h>
 #include <libgran/surface_force/triangular_facet.h>
-#if LGREF_BREAKING
+#if LGREF_CONNECTORS
+#include <libgran/sinter_bridge/sinter_bridge.h>
+#elif LGREF_BREAKING
 #include <libgran/sinter_bridge/alt_breaking_sinter_bridge.h>
 #else
 #include <libgran/sinter_bridge/alt_sinter_bridge.h>
@@ -47,7 +50,9 @@ struct seq_strength {  // neck strength "distribution": hands out the given valu
     size_t k = 0;
     double operator()() { return k < vals->size() ? (*vals)[k++] : std::numeric_limits<double>::infinity(); }
 };
-#if LGREF_BREAKING
+#if LGREF_CONNECTORS
+using SinterT = sinter_functor<V, double>;
+#elif LGREF_BREAKING
 using SinterT = alt_breaking_sinter_functor<V, double, seq_strength>;
 #else
 using SinterT = alt_sinter_functor<V, double>;
@@ -82,7 +87,11 @@ void fill9(double *out, std::tuple<V, V, V> const &t) {
 
 }  // namespace
 
-#if LGREF_BREAKING && LGREF_LIMITED
+#if LGREF_CONNECTORS && LGREF_LIMITED
+#define FACTORY lgref_make_conn_limited
+#elif LGREF_CONNECTORS
+#define FACTORY lgref_make_conn_full
+#elif LGREF_BREAKING && LGREF_LIMITED
 #define FACTORY lgref_make_brk_limited
 #elif LGREF_BREAKING
 #define FACTORY lgref_make_brk_full
@@ -105,6 +114,31 @@ RefSys *FACTORY(const lg_system_desc *d, const double *x0, const double *v0, con
 
     auto contact = make_contact(d->contact, n);
     std::shared_ptr<SinterT> sinter;
+#if LGREF_CONNECTORS
+    (void)neck; (void)n_neck;
+    if (d->binary_model == LG_BINARY_SINTER_CONNECTORS) {
+        const lg_contact_params &p = d->contact;
+        // the caller's axes stand in for the reference's random unit vector generator, in order
+        auto axes = std::make_shared<std::vector<V>>();
+        for (int64_t b = 0; b < d->n_connector_axes; ++b)
+            axes->push_back(V(d->connector_axes[3 * b], d->connector_axes[3 * b + 1], d->connector_axes[3 * b + 2]));
+        auto next = std::make_shared<size_t>(0);
+        std::function<V()> gen = [axes, next]() { return (*next < axes->size()) ? (*axes)[(*next)++] : V(1.0, 0.0, 0.0); };
+        sinter = std::make_shared<SinterT>(n, d->connector.k_d, d->connector.gamma_d, p.k, p.gamma_n, p.k_t, p.gamma_t,
+                                           p.mu_s, p.phi_d, p.k_r, p.gamma_r, p.mu_r, p.phi_r, p.k_o, p.gamma_o, p.mu_o,
+                                           p.phi_o, p.r_part, p.mass, p.inertia, p.dt, V::Zero(), 0.0, s->x.begin(),
+                                           gen, d->connector.critical_separation);
+        auto handler = std::make_shared<sinter_step_handler<Field, V, double>>(sinter->get_step_handler<Field>());
+        s->keep.push_back(handler);
+        s->inc_x = [s, handler](size_t i, V const &dx) {
+            handler->increment_x(i, dx, s->x.begin(), s->v.begin(), s->a.begin(), s->th.begin(), s->om.begin(), s->al.begin());
+        };
+        s->inc_theta = [s, handler](size_t i, V const &dth) {
+            handler->increment_theta(i, dth, s->x.begin(), s->v.begin(), s->a.begin(), s->th.begin(), s->om.begin(),
+                                     s->al.begin());
+        };
+    }
+#else
     if (d->binary_model == LG_BINARY_SINTER || d->binary_model == LG_BINARY_BREAKING_SINTER) {
         const lg_sinter_params &p = d->sinter;
 #if LGREF_BREAKING
@@ -119,6 +153,7 @@ RefSys *FACTORY(const lg_system_desc *d, const double *x0, const double *v0, con
                                            p.critical_separation, *contact);
 #endif
     }
+#endif
     const lg_hamaker_params &hp = d->hamaker;
 #if LGREF_LIMITED
     std::shared_ptr<HamT> ham;
@@ -148,7 +183,14 @@ RefSys *FACTORY(const lg_system_desc *d, const double *x0, const double *v0, con
 
     // spring and bond read-back
     s->springs = [contact, sinter, n, bm = d->binary_model](size_t i, size_t j, double *out) {
+#if LGREF_CONNECTORS
+        if (sinter && sinter->bonded_contacts[i * n + j]) {  // the five connectors of i for the bond
+            for (int k = 0; k < 9; ++k) out[k] = 0.0;
+            return;
+        }
+#else
         if (sinter && sinter->bonded_contacts[i * n + j]) { fill9(out, sinter->contact_springs[i * n + j]); return; }
+#endif
         if (sinter) { fill9(out, sinter->contact_force.contact_springs[i * n + j]); return; }
         if (bm == LG_BINARY_CONTACT) { fill9(out, contact->contact_springs[i * n + j]); return; }
         for (int k = 0; k < 9; ++k) out[k] = 0.0;

@@ -31,6 +31,9 @@ struct RefSys {
     std::vector<std::function<void(double)>> facet_move;
     std::vector<std::function<void(double *)>> facet_vertices;
     bool facet_auto_move = false;
+    // step handler increments of the drift (sinter_step_handler of the 5-connector model); empty:
+    // plain x += v*dt, theta += omega*dt
+    std::function<void(size_t, V const &)> inc_x, inc_theta;
     int64_t step_index = 0;
     double t = 0.0;
 
@@ -67,7 +70,11 @@ struct RefSys {
         for (int64_t s = 0; s < nsteps; ++s) {
             if (verlet && rebuild_every > 0 && step_index % rebuild_every == 0) build_rows();
             for (size_t i = 0; i < n; ++i) { v[i] += a[i] * hdt; om[i] += al[i] * hdt; }
-            for (size_t i = 0; i < n; ++i) { x[i] += v[i] * dt; th[i] += om[i] * dt; }
+            if (inc_x) {
+                for (size_t i = 0; i < n; ++i) { inc_x(i, v[i] * dt); inc_theta(i, om[i] * dt); }
+            } else {
+                for (size_t i = 0; i < n; ++i) { x[i] += v[i] * dt; th[i] += om[i] * dt; }
+            }
             forces();
             for (size_t i = 0; i < n; ++i) { v[i] += a[i] * hdt; om[i] += al[i] * hdt; }
             if (facet_auto_move)
@@ -94,3 +101,7 @@ RefSys *lgref_make_brk_full(const lg_system_desc *, const double *, const double
                             const lg_facet_desc *, const double *, int64_t);
 RefSys *lgref_make_brk_limited(const lg_system_desc *, const double *, const double *, const double *, const double *,
                                const lg_facet_desc *, const double *, int64_t);
+RefSys *lgref_make_conn_full(const lg_system_desc *, const double *, const double *, const double *, const double *,
+                             const lg_facet_desc *, const double *, int64_t);
+RefSys *lgref_make_conn_limited(const lg_system_desc *, const double *, const double *, const double *, const double *,
+                                const lg_facet_desc *, const double *, int64_t);

@@ -71,4 +71,18 @@ def cases():
                     facet_auto_move=1)
     out.append(dict(name="facet_moving", desc=d, x0=c["x0"], v0=c["v0"] * 0.0 + np.array([0.3, 0.1, -0.5]),
                     dt=c["dt"], checkpoints=[0, 10, 2000, 6000], facets=[f]))
+    # 8. 5-connector sintered cube (test/sintered.cpp set-up), short run
+    c = KA.sintered_case()
+    out.append(dict(name="cube_connectors", desc=c["desc"], x0=c["x0"], v0=c["v0"], dt=c["dt"],
+                    checkpoints=[0, 1, 10, 500]))
+    # 9. RSA aggregate, 5-connector bonds + limited Hamaker, inward motion (contacts between
+    #    non-bonded monomers)
+    x0 = generate_aggregate(13, 40, mat.r)
+    v0 = -1.5e7 * (x0 - x0.mean(0)) + generate_velocities(13, 40, 0.2)
+    d = K.make_desc(40, A.LG_BINARY_SINTER_CONNECTORS, A.LG_HAMAKER_LIMITED, contact=mat.contact(),
+                    hamaker=mat.hamaker())
+    nb = len(K.connector_bonds(x0, mat.r, mat.d_crit))
+    K.set_connectors(d, 0.5 * mat.k_n, 0.5 * mat.g_n, mat.d_crit, K.random_unit_axes(nb, 13))
+    out.append(dict(name="rsa40_connectors_limited", desc=d, x0=x0, v0=v0, dt=mat.dt, checkpoints=[0, 1, 10, 300],
+                    spring_pairs=[(0, 1), (1, 0), (0, 2)]))
     return out

@@ -7,9 +7,10 @@ step count and the end-state targets it checks at 1 %):
   hamaker_nbr     test/hamaker_neighbor.cpp (same set-up, Verlet list r=5r rebuilt every 20 steps,
                   :115,121-122,129-144)
   alt_sintered    test/alt_sintered.cpp:37-96,141-149
+  sintered        test/sintered.cpp:54-106,137-150 (5-connector sinter_functor with its
+                  sinter_step_handler; connector axes drawn from a seeded generator, as the test draws
+                  them from its own, test/sintered.cpp:30-39)
   surface         test/surface.cpp:48-90,117-123
-The 5-connector sintered_test (test/sintered.cpp) needs the sinter_step_handler side channel and
-is not part of this engine's path.
 """
 import math
 
@@ -88,6 +89,29 @@ def alt_sintered_case():
                 targets={"radius_of_gyration": 3.9598e-08, "center_displacement": 2.35702e-07})
 
 
+def sintered_case():
+    dt = 1e-13
+    x0, v0 = [], []
+    for i in range(3):
+        y = -1.0 * R + float(i) * 2.0 * R
+        for j in range(3):
+            x = -1.0 * R + float(j) * 2.0 * R
+            x0 += [(x, y, 0.0), (x, y, -2.0 * R), (x, y, -4.0 * R)]
+            vel = (0.0, 0.0, 5.0) if j == 0 else ((0.0, 5.0, 0.0) if j == 2 else (0.0, 0.0, 0.0))
+            v0 += [vel] * 3
+    x0, v0 = np.array(x0), np.array(v0)
+    k, gamma_n, mu, phi, mu_o = 10000.0, 5.0e-9, 1.0, 1.0, 0.1
+    # the driver's sinter_functor arguments (test/sintered.cpp:106): k_d = k, gamma_d = 0, then the
+    # contact pattern (k, gamma_n, k, gamma_t, mu, phi, k, gamma_r, mu_o, phi, k, gamma_o, mu_o, phi)
+    cp = K.contact_params(k, gamma_n, k, 0.2 * gamma_n, mu, phi, k, 0.05 * gamma_n, mu_o, phi, k, 0.05 * gamma_n,
+                          mu_o, phi, R, MASS, INERTIA, dt)
+    desc = K.make_desc(len(x0), A.LG_BINARY_SINTER_CONNECTORS, A.LG_HAMAKER_NONE, contact=cp)
+    nb = len(K.connector_bonds(x0, R, 1.0e-9))
+    K.set_connectors(desc, k, 0.0, 1.0e-9, K.random_unit_axes(nb, 0))
+    return dict(name="sintered", desc=desc, x0=x0, v0=v0, dt=dt, nsteps=int(1.0e-7 / dt), rebuild=0,
+                targets={"radius_of_gyration": 3.95981e-08, "center_displacement": 2.35702e-07})
+
+
 def surface_facet(dt, A_h=0.0, h0=1.0e-9, mu=0.5):
     a = 50.0 * R
     f = A.lg_facet_desc()
@@ -114,7 +138,8 @@ def surface_case():
 
 
 def all_cases():
-    return [contact_case(), hamaker_case(False), hamaker_case(True), alt_sintered_case(), surface_case()]
+    return [contact_case(), hamaker_case(False), hamaker_case(True), alt_sintered_case(), sintered_case(),
+            surface_case()]
 
 
 def measured(case, obs0, obs1):

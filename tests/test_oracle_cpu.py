@@ -65,6 +65,41 @@ def test_oracle_matches_reference_harness(bm, hm):
     assert np.array_equal(orc.bonds(), ref.bonds())
 
 
+@pytest.mark.parametrize("hm", [A.LG_HAMAKER_NONE, A.LG_HAMAKER_LIMITED, A.LG_HAMAKER_FULL])
+@pytest.mark.parametrize("verlet", [False, True], ids=["all", "verlet"])
+def test_oracle_matches_reference_harness_connectors(hm, verlet):
+    """5-connector sinter model (sinter_bridge.h): bonded pairs through the connector springs moved by
+    the step handler, non-bonded pairs through the inner contact functor."""
+    _harness_or_skip()
+    mat = K.Material()
+    n = 36
+    x0 = generate_aggregate(300 + hm, n, mat.r)
+    v0 = generate_velocities(300 + hm, n, 0.5) - 1.5e7 * (x0 - x0.mean(0))
+    d = K.make_desc(n, A.LG_BINARY_SINTER_CONNECTORS, hm, contact=mat.contact(), hamaker=mat.hamaker(),
+                    pairs=A.LG_PAIRS_VERLET if verlet else A.LG_PAIRS_ALL, r_verlet=4.5 * mat.r if verlet else 0.0)
+    nb = len(K.connector_bonds(x0, mat.r, mat.d_crit))
+    assert nb > 0
+    K.set_connectors(d, 0.5 * mat.k_n, 0.3 * mat.g_n, mat.d_crit, K.random_unit_axes(nb, 7))
+    ref = O.RefHarnessSystem(d, x0, v0)
+    orc = O.OracleSystem(d, x0, v0)
+    for _ in range(3):
+        ref.step(mat.dt, 40, 20)
+        orc.step(mat.dt, 40, 20)
+        for f in H.FIELDS:
+            assert np.array_equal(orc.get(f), ref.get(f)), H.FIELD_NAMES[f]
+    assert np.array_equal(orc.bonds(), ref.bonds())
+
+
+def test_connector_axes_are_required_and_checked():
+    mat = K.Material()
+    x0 = generate_aggregate(3, 20, mat.r)
+    d = K.make_desc(20, A.LG_BINARY_SINTER_CONNECTORS, A.LG_HAMAKER_NONE, contact=mat.contact())
+    nb = len(K.connector_bonds(x0, mat.r, mat.d_crit))
+    K.set_connectors(d, mat.k_n, 0.0, mat.d_crit, K.random_unit_axes(nb - 1, 1))  # one short
+    with pytest.raises(Exception):
+        O.OracleSystem(d, x0)
+
+
 def test_oracle_verlet_rows_match_brute_force():
     mat = K.Material()
     n = 300
