@@ -19,6 +19,7 @@ template <typename field_container_t, typename field_value_t>
 struct rotational_step_handler {};
 
 template <typename, typename> struct alt_sinter_functor;
+template <typename, typename> struct sinter_functor;
 template <typename, typename, typename> struct alt_breaking_sinter_functor;
 template <typename, typename> struct hamaker_functor;
 template <typename, typename> struct limited_range_hamaker_functor;
@@ -32,6 +33,8 @@ template <typename V, typename R> struct is_contact<contact_force_functor<V, R>>
 template <typename T> struct is_sinter : std::false_type {};
 template <typename V, typename R> struct is_sinter<alt_sinter_functor<V, R>> : std::true_type {};
 template <typename V, typename R, typename D> struct is_sinter<alt_breaking_sinter_functor<V, R, D>> : std::true_type {};
+template <typename T> struct is_connector_sinter : std::false_type {};
+template <typename V, typename R> struct is_connector_sinter<sinter_functor<V, R>> : std::true_type {};
 template <typename T> struct is_hamaker : std::false_type {};
 template <typename V, typename R> struct is_hamaker<hamaker_functor<V, R>> : std::true_type {};
 template <typename V, typename R> struct is_hamaker<limited_range_hamaker_functor<V, R>> : std::true_type {};
@@ -60,6 +63,15 @@ struct desc_builder {
             d.sinter = f.params;
             d.contact = f.contact;
             neck = f.neck_strengths_drawn;
+            sinter_bindings.push_back(&f.bound);
+        } else if constexpr (is_connector_sinter<T>::value) {
+            if (has_binary) throw std::invalid_argument("one contact or sintered functor per container");
+            has_binary = true;
+            d.binary_model = T::model;
+            d.contact = f.contact;
+            d.connector = f.connector;
+            d.connector_axes = f.axes.data();
+            d.n_connector_axes = (int64_t)(f.axes.size() / 3);
             sinter_bindings.push_back(&f.bound);
         } else if constexpr (is_hamaker<T>::value) {
             if (has_hamaker) throw std::invalid_argument("one Hamaker functor per container");
@@ -129,6 +141,7 @@ protected:
         b.d.pairs = pairs;
         b.d.r_verlet = r_verlet;
         b.d.precision = libgran_gb300::default_precision();
+        if (b.d.binary_model == LG_BINARY_SINTER_CONNECTORS) b.d.precision = LG_PRECISION_FP64;  // FP64 only
         b.d.n_facets = (int32_t)b.facets.size();
         auto xa = libgran_gb300::to_aos(x0), va = libgran_gb300::to_aos(v0), ta = libgran_gb300::to_aos(theta0),
              wa = libgran_gb300::to_aos(omega0);

@@ -119,6 +119,7 @@ struct Params {
     double contact_skip_d2;  // squared centre distance above which overlap <= 0 is certain
     double hamaker_skip_d2;  // squared centre distance above which the limited Hamaker is zero
     int32_t springs_ff;      // pair and bond springs held as float-float pairs (mixed precision)
+    lg_connector_params connector;  // 5-connector sinter model
 };
 
 // Entry flags of a pair slot (Verlet list slot or implicit all-pairs slot)
@@ -149,6 +150,11 @@ struct BondView {
     double *strength;   // [bcap * n]
     double *xi;         // [9][bcap * n] bond springs
     int32_t bcap;       // bond slots per row
+    // 5-connector model (null otherwise): the five connectors that particle i carries for its bond
+    // slot b, component-major (connector k, component c at (3k + c) * bcap * n + b * n + i), and the
+    // slot of i in the partner's bond list
+    double *cn;         // [15][bcap * n]
+    int32_t *rev;       // [bcap * n]
 };
 
 struct StateView {
@@ -258,6 +264,31 @@ __device__ __forceinline__ bool bond_force(const lg_sinter_params &p, d3 dx, d3 
     oa = dvs(f_tot, p.mass);
     oal = dvs(tau_tot, p.inertia);
     return brk;
+}
+
+// sinter_functor::bonded_contact_accelerations (sinter_bridge.h:238-266): five connector springs
+// between the connectors of i (bond slot ei) and those of j (its slot ej for i); rest lengths 2 r
+// for the four side springs, 0 for the centre spring (sinter_bridge.h:201-206).
+__device__ __forceinline__ void connector_force(const lg_connector_params &cp, double r, double mass, double inertia,
+                                                d3 xi, d3 xj, d3 vi, d3 vj, d3 wi, d3 wj, const double *cn,
+                                                int64_t bs, int64_t ei, int64_t ej, d3 &oa, d3 &oal) {
+    d3 force = zero3(), torque = zero3();
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const d3 ci = mk3(cn[(3 * k) * bs + ei], cn[(3 * k + 1) * bs + ei], cn[(3 * k + 2) * bs + ei]);
+        const d3 cj = mk3(cn[(3 * k) * bs + ej], cn[(3 * k + 1) * bs + ej], cn[(3 * k + 2) * bs + ej]);
+        const d3 spring = sub(cj, ci);
+        const double len = nrm(spring);
+        const double eq = k < 4 ? 2.0 * r : 0.0;
+        const d3 cvi = add(vi, crs(wi, sub(ci, xi)));
+        const d3 cvj = add(vj, crs(wj, sub(cj, xj)));
+        const d3 rel = sub(cvj, cvi);
+        const d3 df = add(scl(-(eq - len) * cp.k_d, nrmz(spring)), scl(cp.gamma_d, rel));
+        force = add(force, df);
+        torque = add(torque, crs(sub(ci, xi), df));
+    }
+    oa = dvs(force, mass);
+    oal = dvs(torque, inertia);
 }
 
 __device__ __forceinline__ double sq_(double x) { return x * x; }

@@ -79,7 +79,9 @@ static int64_t uf_find(std::vector<int64_t> &p, int64_t a) {
 }
 
 int lg_detect_bonds(const double *x0, int64_t n, double r, double dc, bool cycle_free,
-                    std::vector<std::pair<int32_t, int32_t>> &bonds) {
+                    std::vector<std::pair<int32_t, int32_t>> &bonds, bool inclusive = false) {
+    // the 5-connector model bonds at |g| <= dc (sinter_bridge.h:156), the alt models at |g| < dc
+    auto bonded = [dc, inclusive](double g) { return inclusive ? !(std::fabs(g) > dc) : std::fabs(g) < dc; };
     bonds.clear();
     if (n < 2) return LG_OK;
     const double reach = 2.0 * r + dc;
@@ -88,7 +90,7 @@ int lg_detect_bonds(const double *x0, int64_t n, double r, double dc, bool cycle
         for (int64_t i = 0; i + 1 < n; ++i)
             for (int64_t j = i + 1; j < n; ++j) {
                 double g = nrm(sub(hld(x0, i), hld(x0, j))) - 2.0 * r;
-                if (std::fabs(g) < dc) cand.emplace_back((int32_t)i, (int32_t)j);
+                if (bonded(g)) cand.emplace_back((int32_t)i, (int32_t)j);
             }
     } else {
         double lo[3] = {1e300, 1e300, 1e300};
@@ -111,7 +113,7 @@ int lg_detect_bonds(const double *x0, int64_t n, double r, double dc, bool cycle
                         for (int32_t j : it->second) {
                             if (j <= i) continue;
                             double g = nrm(sub(hld(x0, i), hld(x0, j))) - 2.0 * r;
-                            if (std::fabs(g) < dc) cand.emplace_back((int32_t)i, j);
+                            if (bonded(g)) cand.emplace_back((int32_t)i, j);
                         }
                     }
         }
@@ -480,7 +482,7 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_n
             launch_kick_drift_mixed(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt,
                                     s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->stream);
         else
-            launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt,
+            launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->bv,
                                    s->stream);
         s->launches += 1;
     }
@@ -497,7 +499,9 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_n
 static int check_args(const lg_system_desc *d) {
     if (!d) return lg_fail(LG_E_INVALID, "lg_create: null descriptor");
     if (d->n_part < 1 || d->n_part > (int64_t)1 << 30) return lg_fail(LG_E_INVALID, "lg_create: n_part %lld out of range", (long long)d->n_part);
-    if (d->binary_model < 0 || d->binary_model > 3) return lg_fail(LG_E_INVALID, "lg_create: unknown binary_model %d", d->binary_model);
+    if (d->binary_model < 0 || d->binary_model > 4) return lg_fail(LG_E_INVALID, "lg_create: unknown binary_model %d", d->binary_model);
+    if (d->binary_model == LG_BINARY_SINTER_CONNECTORS && d->precision != LG_PRECISION_FP64)
+        return lg_fail(LG_E_INVALID, "lg_create: the 5-connector sinter model runs in FP64 precision only");
     if (d->hamaker_model < 0 || d->hamaker_model > 3) return lg_fail(LG_E_INVALID, "lg_create: unknown hamaker_model %d", d->hamaker_model);
     if (d->binary_model == LG_BINARY_NONE && d->hamaker_model == LG_HAMAKER_NONE)
         return lg_fail(LG_E_INVALID, "lg_create: at least one binary force functor must be provided");
@@ -568,6 +572,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     P.contact_skip_d2 = cr * cr * (1.0 + 1e-9);
     P.hamaker_skip_d2 = d->hamaker.r_cutoff * d->hamaker.r_cutoff * (1.0 + 1e-9);
     P.springs_ff = d->precision == LG_PRECISION_MIXED ? 1 : 0;
+    P.connector = d->connector;
     for (int f = 0; f < d->n_facets; ++f) {
         const lg_facet_desc &fd = facets[f];
         FacetDev &o = P.facets[f];
@@ -605,6 +610,25 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
                 s->n_bonds_initial_sys[q] = 2 * (int64_t)local.size();
             }
         }
+    }
+    const bool connectors = d->binary_model == LG_BINARY_SINTER_CONNECTORS;
+    if (connectors) {  // sinter_functor ctor, sinter_bridge.h:146-160: no cycle check, |g| <= dc
+        const double r = d->contact.r_part, dc = d->connector.critical_separation;
+        if (s->n_systems == 0) {
+            LG_TRY(lg_detect_bonds(x0, n, r, dc, false, bonds, true));
+        } else {
+            s->n_bonds_initial_sys.assign((size_t)s->n_systems, 0);
+            std::vector<std::pair<int32_t, int32_t>> local;
+            for (int64_t q = 0; q < s->n_systems; ++q) {
+                const int64_t b = s->sys_off[q], e = s->sys_off[q + 1];
+                LG_TRY(lg_detect_bonds(x0 + 3 * b, e - b, r, dc, false, local, true));
+                for (auto &pr : local) bonds.emplace_back((int32_t)(pr.first + b), (int32_t)(pr.second + b));
+                s->n_bonds_initial_sys[q] = 2 * (int64_t)local.size();
+            }
+        }
+        if (!d->connector_axes || d->n_connector_axes != (int64_t)bonds.size())
+            return lg_fail(LG_E_INVALID, "lg_create: %lld connector axes given but %zu bonds were detected",
+                           (long long)d->n_connector_axes, bonds.size());
     }
     if (d->binary_model == LG_BINARY_BREAKING_SINTER && n_neck != 0 && n_neck != (int64_t)bonds.size())
         return lg_fail(LG_E_INVALID, "lg_create: %lld neck strengths given but %zu bonds were detected", (long long)n_neck,
@@ -654,6 +678,42 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         LG_CUDA(cudaMemcpy(s->bv.intact, bint.data(), sizeof(int8_t) * bs, cudaMemcpyHostToDevice));
         LG_CUDA(cudaMemcpy(s->bv.strength, bstr.data(), sizeof(double) * bs, cudaMemcpyHostToDevice));
         LG_CUDA(cudaMemset(s->bv.xi, 0, sizeof(double) * 9 * bs));
+        if (connectors) {
+            // the connectors of each bond, sinter_bridge.h:163-197 (evaluated in the reference's
+            // order; this file is compiled without contraction)
+            std::vector<double> cn(15 * bs, 0.0);
+            std::vector<int32_t> rev(bs, -1);
+            std::vector<int32_t> slot((size_t)n, 0);
+            const double r = d->contact.r_part;
+            for (size_t b = 0; b < bonds.size(); ++b) {
+                const int32_t i = bonds[b].first, j = bonds[b].second;
+                const d3 pi = hld(x0, i), pj = hld(x0, j);
+                const d3 ni = nrmz(sub(pj, pi)), nj = neg(ni);
+                const d3 v = hld(d->connector_axes, (int64_t)b);
+                d3 db = crs(v, nj);
+                if (nrm(db) == 0.0)
+                    return lg_fail(LG_E_INVALID, "lg_create: connector axis %zu is parallel to its bond", b);
+                d3 ds = sub(v, scl(dot(v, ni), ni));
+                db = nrmz(db);
+                ds = nrmz(ds);
+                const d3 ci[5] = {add(pi, scl(r, ds)), sub(pi, scl(r, ds)), add(pi, scl(r, db)), sub(pi, scl(r, db)),
+                                  add(pi, scl(r, ni))};
+                const d3 cj[5] = {add(pj, scl(r, ds)), sub(pj, scl(r, ds)), add(pj, scl(r, db)), sub(pj, scl(r, db)),
+                                  add(pj, scl(r, nj))};
+                const int32_t si = slot[i]++, sj = slot[j]++;
+                const size_t ei = (size_t)si * n + i, ej = (size_t)sj * n + j;
+                for (int k = 0; k < 5; ++k) {
+                    cn[(3 * k) * bs + ei] = ci[k].x; cn[(3 * k + 1) * bs + ei] = ci[k].y; cn[(3 * k + 2) * bs + ei] = ci[k].z;
+                    cn[(3 * k) * bs + ej] = cj[k].x; cn[(3 * k + 1) * bs + ej] = cj[k].y; cn[(3 * k + 2) * bs + ej] = cj[k].z;
+                }
+                rev[ei] = sj;
+                rev[ej] = si;
+            }
+            LG_TRY(s->alloc(&s->bv.cn, 15 * bs));
+            LG_TRY(s->alloc(&s->bv.rev, bs));
+            LG_CUDA(cudaMemcpy(s->bv.cn, cn.data(), sizeof(double) * cn.size(), cudaMemcpyHostToDevice));
+            LG_CUDA(cudaMemcpy(s->bv.rev, rev.data(), sizeof(int32_t) * rev.size(), cudaMemcpyHostToDevice));
+        }
         s->host_bond_j = std::move(bj);
     }
 
@@ -1128,7 +1188,7 @@ extern "C" int lg_get_observables_select(lg_system *s, int32_t parts, lg_observa
     if (P.binary_model == LG_BINARY_SINTER || P.binary_model == LG_BINARY_BREAKING_SINTER) {
         m = P.sinter.mass;
         I = P.sinter.inertia;
-    } else if (P.binary_model == LG_BINARY_CONTACT) {
+    } else if (P.binary_model == LG_BINARY_CONTACT || P.binary_model == LG_BINARY_SINTER_CONNECTORS) {
         m = P.contact.mass;
         I = P.contact.inertia;
     } else {
@@ -1375,7 +1435,8 @@ extern "C" int lg_batch_get_observables(lg_system *s, lg_observables *out) {
     if (s->n_systems == 0) return lg_get_observables(s, out);
     const Params &P = s->P;
     const bool sint = P.binary_model == LG_BINARY_SINTER || P.binary_model == LG_BINARY_BREAKING_SINTER;
-    const double m = sint ? P.sinter.mass : (P.binary_model == LG_BINARY_CONTACT ? P.contact.mass : P.hamaker.mass);
+    const bool cmass = P.binary_model == LG_BINARY_CONTACT || P.binary_model == LG_BINARY_SINTER_CONNECTORS;
+    const double m = sint ? P.sinter.mass : (cmass ? P.contact.mass : P.hamaker.mass);
     const double I = sint ? P.sinter.inertia : P.contact.inertia;
     StateView S = state_view(s, false);
     // per-particle rows (the single-system reduction is launched too; its result is unused)
@@ -1465,6 +1526,7 @@ static int snapshot_take(lg_system *s) {
         const size_t bs = (size_t)s->bv.bcap * (size_t)n;
         addb(s->bv.intact, bs);
         addb(s->bv.xi, sizeof(double) * 9 * bs);
+        if (s->bv.cn) addb(s->bv.cn, sizeof(double) * 15 * bs);
         for (auto &b : s->snap) {
             void *p = nullptr;
             cudaError_t e = cudaMalloc(&p, b.bytes);

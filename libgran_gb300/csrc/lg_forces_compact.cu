@@ -67,7 +67,12 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
     const d3 xo = W.xo[own], vo = W.vo[own], wo = W.wo[own];
     const d3 dx = sub(xo, ld4(S.x, j));
     d3 pa = zero3(), pal = zero3();
-    if (fl & kBonded) {
+    if ((fl & kBonded) && BV.cn) {  // 5-connector model
+        const int64_t be = (int64_t)bond_slot_of(fl) * n + io;
+        const d3 xj = ld4(S.x, j), vj = ld4(S.v, j), wj = ld4(S.w, j);
+        connector_force(P.connector, P.contact.r_part, P.contact.mass, P.contact.inertia, xo, xj, vo, vj, wo, wj, BV.cn,
+                        bs, be, (int64_t)BV.rev[be] * n + j, pa, pal);
+    } else if (fl & kBonded) {
         const bool breaking = P.binary_model == LG_BINARY_BREAKING_SINTER;
         const int64_t be = (int64_t)bond_slot_of(fl) * n + io;
         d3 s[3];

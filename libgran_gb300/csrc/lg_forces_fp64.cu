@@ -17,17 +17,39 @@ namespace lg {
 // Kick + drift (first half of the rotational velocity-Verlet step):
 //   v += a*(dt/2); w += al*(dt/2); x += v*dt; th += w*dt
 // ------------------------------------------------------------------------------------------------
+// With connectors (BV.cn): the drift is sinter_step_handler's increment_x then increment_theta
+// (sinter_bridge.h:24-42, 55-75): the particle's connectors move with it by dx, then turn by
+// dtheta about its moved centre.
 __global__ void kick_drift_fp64(int64_t n, dbl4 *__restrict__ x, dbl4 *__restrict__ v,
                                 dbl4 *__restrict__ th, dbl4 *__restrict__ w, const dbl4 *__restrict__ a,
-                                const dbl4 *__restrict__ al, double dt, double hdt) {
+                                const dbl4 *__restrict__ al, double dt, double hdt, BondView BV) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));
     d3 wi = add(ld4(w, i), scl(hdt, ld4(al, i)));
     st4(v, i, vi);
     st4(w, i, wi);
-    st4(x, i, add(ld4(x, i), scl(dt, vi)));
-    st4(th, i, add(ld4(th, i), scl(dt, wi)));
+    const d3 dx = scl(dt, vi);
+    const d3 xn = add(ld4(x, i), dx);
+    st4(x, i, xn);
+    const d3 dth = scl(dt, wi);
+    st4(th, i, add(ld4(th, i), dth));
+    if (BV.cn) {
+        const int64_t bs = (int64_t)BV.bcap * n;
+        for (int b = 0; b < BV.bcap; ++b) {
+            const int64_t e = (int64_t)b * n + i;
+            if (BV.j[e] < 0) continue;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                double *cx = BV.cn + (3 * k) * bs + e, *cy = BV.cn + (3 * k + 1) * bs + e, *cz = BV.cn + (3 * k + 2) * bs + e;
+                d3 c = add(mk3(*cx, *cy, *cz), dx);
+                c = add(c, crs(dth, sub(c, xn)));
+                *cx = c.x;
+                *cy = c.y;
+                *cz = c.z;
+            }
+        }
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -74,7 +96,12 @@ __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairVi
             bool have = false;
             if (bm != LG_BINARY_NONE) {
                 have = true;
-                if (fl & kBonded) {
+                if ((fl & kBonded) && BV.cn) {  // 5-connector model
+                    const int64_t be = (int64_t)bond_slot_of(fl) * n + i;
+                    const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+                    connector_force(P.connector, P.contact.r_part, P.contact.mass, P.contact.inertia, xi_, xj, vi, vj,
+                                    wi, wj, BV.cn, (int64_t)BV.bcap * n, be, (int64_t)BV.rev[be] * n + j, pa, pal);
+                } else if (fl & kBonded) {
                     const int b = (int)bond_slot_of(fl);
                     const int64_t be = (int64_t)b * n + i;
                     const int64_t bs = (int64_t)BV.bcap * n;
@@ -633,11 +660,11 @@ void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairVi
 }
 
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
-                            const dbl4 *al, double dt, double hdt, cudaStream_t st) {
+                            const dbl4 *al, double dt, double hdt, const BondView &BV, cudaStream_t st) {
     const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
-    kick_drift_fp64<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt);
+    kick_drift_fp64<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt, BV);
 }
 
 void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, double r_near, int64_t max_cells,

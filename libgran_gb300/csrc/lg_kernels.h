@@ -39,8 +39,9 @@ struct ListScratch {
 // FP64 path (lg_forces_fp64.cu, compiled with --fmad=false)
 void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                         double dt, int move_facets, cudaStream_t st);
+// With connectors (BV.cn non-null) the drift also carries the 5-connector model's connectors.
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
-                            const dbl4 *al, double dt, double hdt, cudaStream_t st);
+                            const dbl4 *al, double dt, double hdt, const BondView &BV, cudaStream_t st);
 // Rebuilds the Verlet rows into newv (springs carried from oldv). With r_near > 0 it also lists each
 // row's contact candidates (newv.near_*): slots within r_near or bonded; springs of the other slots
 // are not carried (those pairs are apart, so their springs reset).

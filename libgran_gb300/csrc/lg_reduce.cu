@@ -45,7 +45,16 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
         const uint32_t fl = PV.flags[e];
         const double dist = nrm(sub(x, ld4(S.x, j)));
         double u = 0.0;
-        if (fl & kBonded) {
+        if ((fl & kBonded) && BV.cn) {  // 5-connector model: the connector springs
+            const int64_t be = (int64_t)bond_slot_of(fl) * n + i, ej = (int64_t)BV.rev[be] * n + j;
+            for (int k = 0; k < 5; ++k) {
+                const d3 ci = mk3(BV.cn[(3 * k) * bs + be], BV.cn[(3 * k + 1) * bs + be], BV.cn[(3 * k + 2) * bs + be]);
+                const d3 cj = mk3(BV.cn[(3 * k) * bs + ej], BV.cn[(3 * k + 1) * bs + ej], BV.cn[(3 * k + 2) * bs + ej]);
+                const double dl = (k < 4 ? 2.0 * P.contact.r_part : 0.0) - nrm(sub(cj, ci));
+                u += 0.5 * P.connector.k_d * dl * dl;
+            }
+            nbond += 1.0;
+        } else if (fl & kBonded) {
             const int64_t be = (int64_t)bond_slot_of(fl) * n + i;
             double dl = 2.0 * P.sinter.r_part - dist;
             u += 0.5 * P.sinter.k * dl * dl;

@@ -48,3 +48,25 @@ def test_dropin_driver_matches_oracle(driver, mode):
 def test_dropin_driver_hits_libgran_targets(driver, mode):
     r = subprocess.run([driver, mode, "1000"], capture_output=True, text=True, timeout=1200)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+@pytest.fixture(scope="module")
+def sintered_driver(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("dropin") / "dropin_sintered")
+    lib = os.path.join(ROOT, "libgran_gb300", "_lib")
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include", "libgran_gb300"),
+           "-I/usr/local/cuda/include", "-o", out, os.path.join(ROOT, "tests", "cpp", "dropin_sintered.cpp"),
+           "-L" + lib, "-llg_gb300", "-Wl,-rpath," + lib]
+    subprocess.check_call(cmd)
+    return out
+
+
+def test_dropin_sintered_driver_hits_libgran_targets(sintered_driver):
+    """libgran's test/sintered.cpp composition (sinter_functor, sinter_step_handler alias, the
+    reference's own generator of connector axes) on the drop-in headers, full 1e6-step run."""
+    r = subprocess.run([sintered_driver], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout + r.stderr
+    vals = dict(zip(("rg", "cd"), [float(t) for t in r.stdout.split()[1::2]]))
+    c = KA.sintered_case()
+    assert abs(vals["rg"] - c["targets"]["radius_of_gyration"]) / c["targets"]["radius_of_gyration"] < 0.01
+    assert abs(vals["cd"] - c["targets"]["center_displacement"]) / c["targets"]["center_displacement"] < 0.01
