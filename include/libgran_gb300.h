@@ -154,6 +154,8 @@ typedef struct lg_system_desc {
 #define LG_FORCE_KERNEL_AUTO 0       /* compacted for large systems, row groups for small ones */
 #define LG_FORCE_KERNEL_ROWGROUP 1   /* T lanes per row (threads_per_row), fixed butterfly combine */
 #define LG_FORCE_KERNEL_COMPACT 2    /* one row per lane, warp-compacted pair queues (see csrc) */
+#define LG_FORCE_KERNEL_PAIRS 3      /* FP64, small systems: one thread per pair slot spread over all SMs,
+                                       then an ordered per-row fold (the reference's summation order) */
 
 /* Fields that lg_get / lg_set move. */
 #define LG_FIELD_X 0       /* positions            get_x()     Granular-system.md:84-120 */

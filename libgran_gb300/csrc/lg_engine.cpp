@@ -385,9 +385,19 @@ int lg_system::alloc(U **p, size_t count) {
     return LG_OK;
 }
 
+// Pair slots up to which an FP64 system keeps the pair-parallel kernel's scratch (48 bytes a slot),
+// and up to which the automatic choice takes that kernel. Measured on GB300 (sinter + limited
+// Hamaker, FP64, graph-replayed steps): it leads the row-group and compacted kernels from 19
+// particles (37 vs 96 us a step) up to 8000 particles in Verlet mode (295 vs 313 us); the compacted
+// kernel keeps the large systems, where full warps and no divergence decide.
+constexpr int64_t kPairsMaxSlots = (int64_t)1 << 21;
+constexpr int64_t kPairsAutoSlots = (int64_t)1 << 19;
+
 static int choose_kernel(const lg_system *s, int requested) {
     if (requested == LG_FORCE_KERNEL_ROWGROUP || requested == LG_FORCE_KERNEL_COMPACT) return requested;
+    if (requested == LG_FORCE_KERNEL_PAIRS) return s->pres ? requested : -1;
     const int64_t n = s->P.n;
+    if (s->pres && (int64_t)s->pv[0].cap * n <= kPairsAutoSlots) return LG_FORCE_KERNEL_PAIRS;
     if (s->P.pairs == LG_PAIRS_VERLET ? n >= 1024 : n >= 4096) return LG_FORCE_KERNEL_COMPACT;
     return LG_FORCE_KERNEL_ROWGROUP;
 }
@@ -459,7 +469,10 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
         else
             launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
     } else {
-        if (compact)
+        if (s->kernel == LG_FORCE_KERNEL_PAIRS)
+            kernels = launch_forces_pairs_fp64(s->P, S, s->pv[s->pcur], s->bv, s->pres, hdt, dt, move_facets,
+                                               fuse_kick, s->stream);
+        else if (compact)
             launch_forces_compact_fp64(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
         else
             launch_forces_fp64(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
@@ -487,7 +500,8 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_n
         s->launches += 1;
     }
     const int mv = (s->facet_auto_move && s->P.n_facets > 0) ? 1 : 0;
-    const bool fuse = fuse_next && s->precision == LG_PRECISION_MIXED && s->kernel == LG_FORCE_KERNEL_COMPACT;
+    const bool fuse = fuse_next && ((s->precision == LG_PRECISION_MIXED && s->kernel == LG_FORCE_KERNEL_COMPACT) ||
+                                    (s->precision == LG_PRECISION_FP64 && s->kernel == LG_FORCE_KERNEL_PAIRS));
     LG_TRY(launch_forces(s, hdt, dt, mv, fuse));
     s->kick_done = fuse;
     s->vcur = 1 - s->vcur;
@@ -515,7 +529,9 @@ static int check_args(const lg_system_desc *d) {
     if (d->neck_mode != LG_NECK_PER_BOND && d->neck_mode != LG_NECK_REFERENCE_INDEXING) return lg_fail(LG_E_INVALID, "lg_create: unknown neck_mode %d", d->neck_mode);
     if (d->max_neighbors < 0 || d->max_neighbors > 255)
         return lg_fail(LG_E_INVALID, "lg_create: max_neighbors must be in [0, 255]");
-    if (d->force_kernel < 0 || d->force_kernel > 2) return lg_fail(LG_E_INVALID, "lg_create: unknown force_kernel %d", d->force_kernel);
+    if (d->force_kernel < 0 || d->force_kernel > 3) return lg_fail(LG_E_INVALID, "lg_create: unknown force_kernel %d", d->force_kernel);
+    if (d->force_kernel == LG_FORCE_KERNEL_PAIRS && d->precision != LG_PRECISION_FP64)
+        return lg_fail(LG_E_INVALID, "lg_create: the pair-parallel force kernel is FP64 only");
     {
         int T = d->threads_per_row;
         if (T != 0 && T != 1 && T != 2 && T != 4 && T != 8 && T != 16 && T != 32)
@@ -882,6 +898,8 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
             LG_TRY(rebuild_list(s));
         }
     }
+    if (s->precision == LG_PRECISION_FP64 && (int64_t)s->pv[0].cap * n <= kPairsMaxSlots)
+        LG_TRY(s->alloc(&s->pres, 6 * (size_t)(s->pv[0].cap * n)));
     LG_TRY(s->alloc(&s->obs_scratch, (size_t)obs_scratch_doubles(n)));
     LG_TRY(s->alloc(&s->obs_out, 32));
 
@@ -949,6 +967,9 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     }
     s->T = d->threads_per_row > 0 ? d->threads_per_row : choose_threads_per_row(s);
     s->kernel = choose_kernel(s, d->force_kernel);
+    if (s->kernel < 0)
+        return lg_fail(LG_E_INVALID, "lg_create: the pair-parallel force kernel takes at most %lld pair slots",
+                       (long long)kPairsMaxSlots);
     if (d->threads_per_row > 0 && d->force_kernel == LG_FORCE_KERNEL_AUTO) s->kernel = LG_FORCE_KERNEL_ROWGROUP;
     // initial accelerations (the first half kick needs them); velocities are unchanged (hdt = 0)
     LG_TRY(launch_forces(s, 0.0, 0.0, 0));
@@ -1159,8 +1180,12 @@ extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
 
 extern "C" int lg_set_force_kernel(lg_system *s, int32_t variant) {
     LG_HANDLE(s);
-    if (variant < 0 || variant > 2) return lg_fail(LG_E_INVALID, "lg_set_force_kernel: unknown variant %d", variant);
-    s->kernel = choose_kernel(s, variant);
+    if (variant < 0 || variant > 3) return lg_fail(LG_E_INVALID, "lg_set_force_kernel: unknown variant %d", variant);
+    const int k = choose_kernel(s, variant);
+    if (k < 0)
+        return lg_fail(LG_E_INVALID, "lg_set_force_kernel: the pair-parallel kernel is FP64 only and takes at most "
+                       "%lld pair slots", (long long)kPairsMaxSlots);
+    s->kernel = k;
     return LG_OK;
 }
 
@@ -1596,6 +1621,7 @@ extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t
     const int64_t keep_launch = s->launches;
     std::vector<std::pair<int, int>> cands;
     cands.emplace_back(LG_FORCE_KERNEL_COMPACT, 1);
+    if (s->pres) cands.emplace_back(LG_FORCE_KERNEL_PAIRS, 1);
     for (int T = 1; T <= 32; T *= 2) cands.emplace_back(LG_FORCE_KERNEL_ROWGROUP, T);
     double best = 1e300;
     std::pair<int, int> pick(keep_kernel, keep_T);

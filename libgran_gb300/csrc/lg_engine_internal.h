@@ -49,6 +49,7 @@ struct lg_system {
     float4 *csum = nullptr;    // mixed: [3n] contact sums (float-float)
     float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
     int32_t *d_flag = nullptr;  // mixed: device flag of the float-float copy check
+    double *pres = nullptr;     // FP64 pair-parallel kernel: per-slot pair values [6][cap * n]
     double origin[4] = {0.0, 0.0, 0.0, 0.0};  // mixed: origin of the float-float positions, extent in [3]
     double r_max = 0.0;                        // mixed: largest particle radius of the functors
     double ext_max = 0.0;                      // mixed: largest extent of a system about its origin

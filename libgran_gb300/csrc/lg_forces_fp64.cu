@@ -8,7 +8,7 @@
 // T spreads short, FP64-heavy rows (all-pairs mode on a few hundred particles) over more of the
 // GPU's FP64 units. No floating-point atomics are used anywhere: every per-particle sum is owned
 // by one row group, so results are deterministic run to run.
-#include "lg_common.cuh"
+#include "lg_compact.cuh"
 #include "lg_kernels.h"
 
 namespace lg {
@@ -20,15 +20,9 @@ namespace lg {
 // With connectors (BV.cn): the drift is sinter_step_handler's increment_x then increment_theta
 // (sinter_bridge.h:24-42, 55-75): the particle's connectors move with it by dx, then turn by
 // dtheta about its moved centre.
-__global__ void kick_drift_fp64(int64_t n, dbl4 *__restrict__ x, dbl4 *__restrict__ v,
-                                dbl4 *__restrict__ th, dbl4 *__restrict__ w, const dbl4 *__restrict__ a,
-                                const dbl4 *__restrict__ al, double dt, double hdt, BondView BV) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));
-    d3 wi = add(ld4(w, i), scl(hdt, ld4(al, i)));
-    st4(v, i, vi);
-    st4(w, i, wi);
+// Drift of particle i with kicked velocities vi, wi (stored by the caller).
+__device__ __forceinline__ void drift_one(int64_t n, int64_t i, dbl4 *__restrict__ x, dbl4 *__restrict__ th, d3 vi,
+                                          d3 wi, double dt, const BondView &BV) {
     const d3 dx = scl(dt, vi);
     const d3 xn = add(ld4(x, i), dx);
     st4(x, i, xn);
@@ -52,6 +46,18 @@ __global__ void kick_drift_fp64(int64_t n, dbl4 *__restrict__ x, dbl4 *__restric
     }
 }
 
+__global__ void kick_drift_fp64(int64_t n, dbl4 *__restrict__ x, dbl4 *__restrict__ v,
+                                dbl4 *__restrict__ th, dbl4 *__restrict__ w, const dbl4 *__restrict__ a,
+                                const dbl4 *__restrict__ al, double dt, double hdt, BondView BV) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));
+    d3 wi = add(ld4(w, i), scl(hdt, ld4(al, i)));
+    st4(v, i, vi);
+    st4(w, i, wi);
+    drift_one(n, i, x, th, vi, wi, dt, BV);
+}
+
 // ------------------------------------------------------------------------------------------------
 // Pair force kernel
 // ------------------------------------------------------------------------------------------------
@@ -62,6 +68,96 @@ __device__ __forceinline__ double group_sum(double v) {
     return v;
 }
 
+// One slot of row i: the binary functor's pair value plus the Hamaker term, in that order (the
+// reference's container returns binary + hamaker for each pair, operator_overloads.h:16-20); pair
+// state (springs, bond state, flags) of slot e is read and written here and nowhere else.
+__device__ __forceinline__ void slot_pair_fp64(const Params &P, const StateView &S, const PairView &PV,
+                                               const BondView &BV, int64_t n, int64_t i, int64_t e, int64_t j,
+                                               const d3 xi_, const d3 vi, const d3 wi, d3 &pa_out, d3 &pal_out) {
+    const int bm = P.binary_model, hm = P.hamaker_model;
+    const bool breaking = bm == LG_BINARY_BREAKING_SINTER;
+    const uint32_t fl = PV.flags[e];
+    const d3 xj = ld4(S.x, j);
+    const d3 dx = sub(xi_, xj);
+    d3 pa = zero3(), pal = zero3();
+    bool have = false;
+    if (bm != LG_BINARY_NONE) {
+        have = true;
+        if ((fl & kBonded) && BV.cn) {  // 5-connector model
+            const int64_t be = (int64_t)bond_slot_of(fl) * n + i;
+            const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+            connector_force(P.connector, P.contact.r_part, P.contact.mass, P.contact.inertia, xi_, xj, vi, vj,
+                            wi, wj, BV.cn, (int64_t)BV.bcap * n, be, (int64_t)BV.rev[be] * n + j, pa, pal);
+        } else if (fl & kBonded) {
+            const int b = (int)bond_slot_of(fl);
+            const int64_t be = (int64_t)b * n + i;
+            const int64_t bs = (int64_t)BV.bcap * n;
+            d3 s[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                s[q] = mk3(BV.xi[(3 * q) * bs + be], BV.xi[(3 * q + 1) * bs + be], BV.xi[(3 * q + 2) * bs + be]);
+            const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+            bool brk = bond_force(P.sinter, dx, vi, vj, wi, wj, s, breaking, breaking ? BV.strength[be] : 0.0, pa,
+                                  pal);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                BV.xi[(3 * q) * bs + be] = s[q].x;
+                BV.xi[(3 * q + 1) * bs + be] = s[q].y;
+                BV.xi[(3 * q + 2) * bs + be] = s[q].z;
+            }
+            if (brk) {
+                BV.intact[be] = 0;
+                PV.flags[e] = fl & ~(kBonded | (0xffu << 8));
+            }
+        } else {
+            const int64_t xs = PV.cap * n;
+            bool touching = false;
+            d3 nn = zero3();
+            double overlap = 0.0;
+            if (!(sqn(dx) > P.contact_skip_d2)) {
+                nn = nrmz(dx);
+                overlap = 2.0 * P.contact.r_part - dot(dx, nn);
+                touching = !(overlap <= 0);
+            }
+            if (touching) {
+                d3 s[3] = {zero3(), zero3(), zero3()};  // springs of a slot that is not live are zero
+                if (fl & kXiLive)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q)
+                        s[q] = mk3(PV.xi[(3 * q) * xs + e], PV.xi[(3 * q + 1) * xs + e], PV.xi[(3 * q + 2) * xs + e]);
+                const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
+                contact_touching(P.contact, nn, overlap, vi, vj, wi, wj, s, pa, pal);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    PV.xi[(3 * q) * xs + e] = s[q].x;
+                    PV.xi[(3 * q + 1) * xs + e] = s[q].y;
+                    PV.xi[(3 * q + 2) * xs + e] = s[q].z;
+                }
+                if (!(fl & kXiLive)) PV.flags[e] = fl | kXiLive;
+            } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
+#pragma unroll
+                for (int q = 0; q < 9; ++q) PV.xi[q * xs + e] = 0.0;
+                PV.flags[e] = fl & ~kXiLive;
+            }
+        }
+    }
+    if (hm != LG_HAMAKER_NONE) {
+        d3 ha = zero3();
+        bool on = true;
+        if (hm == LG_HAMAKER_LIMITED) on = !(sqn(dx) > P.hamaker_skip_d2) && !(nrm(dx) > P.hamaker.r_cutoff);
+        if (on) ha = hamaker_accel(hm, P.hamaker, sub(xj, xi_));
+        if (have) {
+            pa = add(pa, ha);
+            pal = add(pal, zero3());
+        } else {
+            pa = ha;
+            pal = zero3();
+        }
+    }
+    pa_out = pa;
+    pal_out = pal;
+}
+
 template <int T, bool VERLET>
 __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairView PV, BondView BV, double hdt,
                                                    double dt, int move_facets) {
@@ -70,8 +166,6 @@ __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairVi
     const int64_t i = gid / T;
     const int lane = (int)(gid % T);
     const bool active = i < n;
-    const int bm = P.binary_model, hm = P.hamaker_model;
-    const bool breaking = bm == LG_BINARY_BREAKING_SINTER;
 
     if (move_facets && gid == 0) {
         for (int f = 0; f < P.n_facets; ++f)
@@ -89,84 +183,8 @@ __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairVi
         for (int64_t k = lane; k < len; k += T) {
             const int64_t e = k * stride + i;
             const int64_t j = VERLET ? (int64_t)PV.nbr[e] : (k < i ? k : k + 1);
-            const uint32_t fl = PV.flags[e];
-            const d3 xj = ld4(S.x, j);
-            const d3 dx = sub(xi_, xj);
-            d3 pa = zero3(), pal = zero3();
-            bool have = false;
-            if (bm != LG_BINARY_NONE) {
-                have = true;
-                if ((fl & kBonded) && BV.cn) {  // 5-connector model
-                    const int64_t be = (int64_t)bond_slot_of(fl) * n + i;
-                    const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
-                    connector_force(P.connector, P.contact.r_part, P.contact.mass, P.contact.inertia, xi_, xj, vi, vj,
-                                    wi, wj, BV.cn, (int64_t)BV.bcap * n, be, (int64_t)BV.rev[be] * n + j, pa, pal);
-                } else if (fl & kBonded) {
-                    const int b = (int)bond_slot_of(fl);
-                    const int64_t be = (int64_t)b * n + i;
-                    const int64_t bs = (int64_t)BV.bcap * n;
-                    d3 s[3];
-#pragma unroll
-                    for (int q = 0; q < 3; ++q)
-                        s[q] = mk3(BV.xi[(3 * q) * bs + be], BV.xi[(3 * q + 1) * bs + be], BV.xi[(3 * q + 2) * bs + be]);
-                    const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
-                    bool brk = bond_force(P.sinter, dx, vi, vj, wi, wj, s, breaking, breaking ? BV.strength[be] : 0.0, pa,
-                                          pal);
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        BV.xi[(3 * q) * bs + be] = s[q].x;
-                        BV.xi[(3 * q + 1) * bs + be] = s[q].y;
-                        BV.xi[(3 * q + 2) * bs + be] = s[q].z;
-                    }
-                    if (brk) {
-                        BV.intact[be] = 0;
-                        PV.flags[e] = fl & ~(kBonded | (0xffu << 8));
-                    }
-                } else {
-                    const int64_t xs = PV.cap * n;
-                    bool touching = false;
-                    d3 nn = zero3();
-                    double overlap = 0.0;
-                    if (!(sqn(dx) > P.contact_skip_d2)) {
-                        nn = nrmz(dx);
-                        overlap = 2.0 * P.contact.r_part - dot(dx, nn);
-                        touching = !(overlap <= 0);
-                    }
-                    if (touching) {
-                        d3 s[3] = {zero3(), zero3(), zero3()};  // springs of a slot that is not live are zero
-                        if (fl & kXiLive)
-#pragma unroll
-                            for (int q = 0; q < 3; ++q)
-                                s[q] = mk3(PV.xi[(3 * q) * xs + e], PV.xi[(3 * q + 1) * xs + e], PV.xi[(3 * q + 2) * xs + e]);
-                        const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
-                        contact_touching(P.contact, nn, overlap, vi, vj, wi, wj, s, pa, pal);
-#pragma unroll
-                        for (int q = 0; q < 3; ++q) {
-                            PV.xi[(3 * q) * xs + e] = s[q].x;
-                            PV.xi[(3 * q + 1) * xs + e] = s[q].y;
-                            PV.xi[(3 * q + 2) * xs + e] = s[q].z;
-                        }
-                        if (!(fl & kXiLive)) PV.flags[e] = fl | kXiLive;
-                    } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
-#pragma unroll
-                        for (int q = 0; q < 9; ++q) PV.xi[q * xs + e] = 0.0;
-                        PV.flags[e] = fl & ~kXiLive;
-                    }
-                }
-            }
-            if (hm != LG_HAMAKER_NONE) {
-                d3 ha = zero3();
-                bool on = true;
-                if (hm == LG_HAMAKER_LIMITED) on = !(sqn(dx) > P.hamaker_skip_d2) && !(nrm(dx) > P.hamaker.r_cutoff);
-                if (on) ha = hamaker_accel(hm, P.hamaker, sub(xj, xi_));
-                if (have) {
-                    pa = add(pa, ha);
-                    pal = add(pal, zero3());
-                } else {
-                    pa = ha;
-                    pal = zero3();
-                }
-            }
+            d3 pa, pal;
+            slot_pair_fp64(P, S, PV, BV, n, i, e, j, xi_, vi, wi, pa, pal);
             acc = add(acc, pa);
             accw = add(accw, pal);
         }
@@ -234,6 +252,64 @@ __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairVi
     if (!isfinite(acc.x) || !isfinite(acc.y) || !isfinite(acc.z) || !isfinite(accw.x) || !isfinite(accw.y) ||
         !isfinite(accw.z))
         set_error(S.err, LG_DEVERR_NONFINITE);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Pair-parallel evaluation for small systems (latency path)
+// ------------------------------------------------------------------------------------------------
+// A GB300 SM retires few FP64 instructions per clock, so a small system whose rows all sit on one
+// or two SMs spends its step waiting on those SMs' FP64 pipes while the rest of the GPU idles. Here
+// every slot (i, k) gets its own thread, in one-warp blocks that the block scheduler spreads over
+// all SMs; each thread writes its pair value (a, alpha: 6 doubles) to a slot-major scratch array.
+// A second kernel then adds each row's values in ascending slot order, exactly as the sequential
+// row loop adds them (so results match the T = 1 row kernel bit for bit), runs the facet terms
+// and the closing half kick and, when another step follows, the next step's kick and drift.
+constexpr int kPairBlock = 32;
+constexpr int kFoldBlock = 32;
+
+template <bool VERLET>
+__global__ void __launch_bounds__(kPairBlock) forces_pairs_fp64(Params P, StateView S, PairView PV, BondView BV,
+                                                                double *__restrict__ pres, int64_t ps, int64_t total) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int64_t n = P.n;
+    const int64_t k = t / n, i = t - k * n;  // slot t = k * n + i
+    if (VERLET && k >= (int64_t)PV.row_len[i]) return;
+    const int64_t j = VERLET ? (int64_t)PV.nbr[t] : (k < i ? k : k + 1);
+    d3 pa, pal;
+    slot_pair_fp64(P, S, PV, BV, n, i, t, j, ld4(S.x, i), ld4(S.v, i), ld4(S.w, i), pa, pal);
+    pres[t] = pa.x;
+    pres[ps + t] = pa.y;
+    pres[2 * ps + t] = pa.z;
+    pres[3 * ps + t] = pal.x;
+    pres[4 * ps + t] = pal.y;
+    pres[5 * ps + t] = pal.z;
+}
+
+template <bool VERLET, bool FACETS>
+__global__ void __launch_bounds__(kFoldBlock) fold_pairs_fp64(Params P, StateView S, PairView PV, BondView BV,
+                                                              const double *__restrict__ pres, int64_t ps, double hdt,
+                                                              double dt, int move_facets, int kick) {
+    const int64_t n = P.n;
+    if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
+    d3 acc = zero3(), accw = zero3();
+    for (int64_t k = 0; k < len; ++k) {
+        const int64_t e = k * n + i;
+        acc = add(acc, mk3(pres[e], pres[ps + e], pres[2 * ps + e]));
+        accw = add(accw, mk3(pres[3 * ps + e], pres[4 * ps + e], pres[5 * ps + e]));
+    }
+    const d3 vi = ld4(S.v, i), wi = ld4(S.w, i);
+    compact::finish_row<FACETS>(P, S, i, n, acc, accw, vi, wi, hdt);
+    if (kick) {  // the next step's opening half kick and drift, as kick_drift_fp64
+        const d3 v2 = add(add(vi, scl(hdt, acc)), scl(hdt, acc));
+        const d3 w2 = add(add(wi, scl(hdt, accw)), scl(hdt, accw));
+        st4(S.v_out, i, v2);
+        st4(S.w_out, i, w2);
+        drift_one(n, i, S.x, S.th, v2, w2, dt, BV);
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -657,6 +733,35 @@ void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairVi
             launch_forces_t<1, false>(P, S, PV, BV, hdt, dt, move_facets, st);
     }
 #undef LG_CASE
+}
+
+int launch_forces_pairs_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
+                             double *pres, double hdt, double dt, int move_facets, bool kick, cudaStream_t st) {
+    const int64_t n = P.n;
+    const bool verlet = P.pairs == LG_PAIRS_VERLET;
+    const int64_t ps = (int64_t)PV.cap * n;
+    const int64_t total = (verlet ? (int64_t)PV.cap : n - 1) * n;
+    if (total > 0) {
+        const int64_t blocks = (total + kPairBlock - 1) / kPairBlock;
+        if (verlet)
+            forces_pairs_fp64<true><<<(unsigned)blocks, kPairBlock, 0, st>>>(P, S, PV, BV, pres, ps, total);
+        else
+            forces_pairs_fp64<false><<<(unsigned)blocks, kPairBlock, 0, st>>>(P, S, PV, BV, pres, ps, total);
+    }
+    const unsigned fb = (unsigned)((n + kFoldBlock - 1) / kFoldBlock);
+    const int kk = kick ? 1 : 0;
+    if (verlet) {
+        if (P.n_facets > 0)
+            fold_pairs_fp64<true, true><<<fb, kFoldBlock, 0, st>>>(P, S, PV, BV, pres, ps, hdt, dt, move_facets, kk);
+        else
+            fold_pairs_fp64<true, false><<<fb, kFoldBlock, 0, st>>>(P, S, PV, BV, pres, ps, hdt, dt, move_facets, kk);
+    } else {
+        if (P.n_facets > 0)
+            fold_pairs_fp64<false, true><<<fb, kFoldBlock, 0, st>>>(P, S, PV, BV, pres, ps, hdt, dt, move_facets, kk);
+        else
+            fold_pairs_fp64<false, false><<<fb, kFoldBlock, 0, st>>>(P, S, PV, BV, pres, ps, hdt, dt, move_facets, kk);
+    }
+    return total > 0 ? 2 : 1;
 }
 
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,

@@ -39,6 +39,11 @@ struct ListScratch {
 // FP64 path (lg_forces_fp64.cu, compiled with --fmad=false)
 void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                         double dt, int move_facets, cudaStream_t st);
+// Pair-parallel FP64 evaluation for small systems: per-slot pair values into pres [6][PV.cap * n],
+// then an ordered per-row fold; kick: also runs the next step's half kick and drift. Returns the
+// number of kernels launched.
+int launch_forces_pairs_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
+                             double *pres, double hdt, double dt, int move_facets, bool kick, cudaStream_t st);
 // With connectors (BV.cn non-null) the drift also carries the 5-connector model's connectors.
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
                             const dbl4 *al, double dt, double hdt, const BondView &BV, cudaStream_t st);

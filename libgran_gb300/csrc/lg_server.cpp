@@ -84,6 +84,8 @@ extern "C" int64_t lg_estimate_device_bytes(const lg_system_desc *d, int64_t n) 
     b += 72 * std::max(d->n_facets, 1) * n;                   // facet springs
     b += 4 * 8 * n + 4 * 4 * n;                               // list scratch
     b += 20 * 8 * n;                                          // observables scratch
+    if (d->precision == LG_PRECISION_FP64 && cap * n <= ((int64_t)1 << 21))
+        b += 48 * cap * n;                                    // pair-parallel kernel scratch
     return b + (4 << 20);                                     // fixed overhead
 }
 

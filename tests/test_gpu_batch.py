@@ -56,10 +56,11 @@ def test_batch_matches_systems_alone_bit_for_bit(precision, bm):
     assert batch.device_errors() == 0
 
 
-def test_batch_fp64_matches_oracle():
+@pytest.mark.parametrize("kernel", [A.LG_FORCE_KERNEL_COMPACT, A.LG_FORCE_KERNEL_PAIRS], ids=["compact", "pairs"])
+def test_batch_fp64_matches_oracle(kernel):
     sizes = [64, 200, 48]
     mat, xs, vs = _systems(sizes, seed0=55)
-    batch = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, A.LG_PRECISION_FP64), np.concatenate(xs),
+    batch = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, A.LG_PRECISION_FP64, kernel), np.concatenate(xs),
                    np.concatenate(vs), sizes=sizes)
     batch.step(mat.dt, 60, 20)
     off = np.concatenate([[0], np.cumsum(sizes)])
@@ -71,14 +72,17 @@ def test_batch_fp64_matches_oracle():
     assert batch.device_errors() == 0
 
 
-@pytest.mark.parametrize("precision", [A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED], ids=["fp64", "mixed"])
-def test_graph_replay_equals_eager_launches(precision):
+@pytest.mark.parametrize("precision,kernel", [(A.LG_PRECISION_FP64, A.LG_FORCE_KERNEL_COMPACT),
+                                              (A.LG_PRECISION_MIXED, A.LG_FORCE_KERNEL_COMPACT),
+                                              (A.LG_PRECISION_FP64, A.LG_FORCE_KERNEL_PAIRS)],
+                         ids=["fp64", "mixed", "fp64-pairs"])
+def test_graph_replay_equals_eager_launches(precision, kernel):
     sizes = [300, 500, 120]
     mat, xs, vs = _systems(sizes, seed0=7)
     outs = []
     for graphs in (False, True):
-        s = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, precision), np.concatenate(xs), np.concatenate(vs),
-                   sizes=sizes)
+        s = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, precision, kernel), np.concatenate(xs),
+                   np.concatenate(vs), sizes=sizes)
         s.set_graphs(graphs)
         s.step(mat.dt, 100, 20)
         s.step(mat.dt, 7, 20)   # unaligned tail
@@ -95,7 +99,7 @@ def test_autotuner_picks_a_valid_variant():
                np.concatenate(xs), np.concatenate(vs), sizes=sizes)
     before = [s.get(f) for f in FIELDS]
     k, T = s.autotune(mat.dt, probe_steps=20, rebuild_every=20, use_cache=False)
-    assert k in (A.LG_FORCE_KERNEL_COMPACT, A.LG_FORCE_KERNEL_ROWGROUP)
+    assert k in (A.LG_FORCE_KERNEL_COMPACT, A.LG_FORCE_KERNEL_ROWGROUP)  # the pair-parallel kernel is FP64 only
     assert T in (1, 2, 4, 8, 16, 32)
     for f, b in zip(FIELDS, before):  # tuning leaves the state as it was
         assert np.array_equal(s.get(f), b)
@@ -161,3 +165,16 @@ def test_restructuring_batch_with_wall_and_breaking_bonds_matches_oracle():
     assert c0 == b0
     assert abs((c0 - c1) - (b0 - b1)) <= max(2, 1e-3 * (b0 - b1))  # 2 ordered pairs = one bond
     assert np.max(np.abs(rgmx - rg64) / rg64) <= 1e-3
+
+
+def test_pair_parallel_kernel_limits():
+    """The pair-parallel kernel is FP64 only and refuses systems beyond its scratch limit."""
+    sizes = [64, 80]
+    mat, xs, vs = _systems(sizes, seed0=3)
+    with pytest.raises(RuntimeError, match="FP64 only"):
+        System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, A.LG_PRECISION_MIXED, A.LG_FORCE_KERNEL_PAIRS),
+               np.concatenate(xs), np.concatenate(vs), sizes=sizes)
+    s = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, A.LG_PRECISION_MIXED), np.concatenate(xs),
+               np.concatenate(vs), sizes=sizes)
+    with pytest.raises(RuntimeError, match="FP64 only"):
+        s.set_force_kernel(A.LG_FORCE_KERNEL_PAIRS)

@@ -24,7 +24,8 @@ def _connector_desc(mat, x0, pairs, hm, seed, kernel=A.LG_FORCE_KERNEL_AUTO, pre
     return d
 
 
-@pytest.mark.parametrize("kernel", [A.LG_FORCE_KERNEL_ROWGROUP, A.LG_FORCE_KERNEL_COMPACT], ids=["rowgroup1", "compact"])
+@pytest.mark.parametrize("kernel", [A.LG_FORCE_KERNEL_ROWGROUP, A.LG_FORCE_KERNEL_COMPACT, A.LG_FORCE_KERNEL_PAIRS],
+                         ids=["rowgroup1", "compact", "pairs"])
 @pytest.mark.parametrize("pairs,n", [(A.LG_PAIRS_ALL, 200), (A.LG_PAIRS_VERLET, 3000)], ids=["all", "verlet"])
 def test_connectors_bit_exact_with_oracle(pairs, n, kernel):
     mat = K.Material()

@@ -44,7 +44,8 @@ def test_gpu_reproduces_golden_sequential_rows(path):
     assert s.device_errors() == 0
 
 
-@pytest.mark.parametrize("kernel", [A.LG_FORCE_KERNEL_ROWGROUP, A.LG_FORCE_KERNEL_COMPACT], ids=["rowgroup1", "compact"])
+@pytest.mark.parametrize("kernel", [A.LG_FORCE_KERNEL_ROWGROUP, A.LG_FORCE_KERNEL_COMPACT, A.LG_FORCE_KERNEL_PAIRS],
+                         ids=["rowgroup1", "compact", "pairs"])
 @pytest.mark.parametrize("path", H.golden_files(), ids=lambda p: os.path.basename(p)[:-4])
 def test_gpu_sequential_rows_are_bit_exact_with_oracle(path, kernel):
     g = np.load(path)
@@ -69,13 +70,13 @@ def _aggregate_system(n, seed, bm, hm, pairs, neck_mode=A.LG_NECK_PER_BOND, vsca
     return mat, d, x0, v0
 
 
-@pytest.mark.parametrize("T", [1, 4, 32, 0])
+@pytest.mark.parametrize("T", [1, 4, 32, 0, -1])  # 0: compacted kernel, -1: pair-parallel kernel
 @pytest.mark.parametrize("bm,hm", [(A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED), (A.LG_BINARY_CONTACT, A.LG_HAMAKER_FULL),
                                    (A.LG_BINARY_BREAKING_SINTER, A.LG_HAMAKER_LIMITED)])
 def test_all_pairs_forces_and_positions(T, bm, hm):
     mat, d, x0, v0 = _aggregate_system(256, 21, bm, hm, A.LG_PAIRS_ALL, squeeze=2e7)
-    if T == 0:
-        d.force_kernel = A.LG_FORCE_KERNEL_COMPACT
+    if T <= 0:
+        d.force_kernel = A.LG_FORCE_KERNEL_COMPACT if T == 0 else A.LG_FORCE_KERNEL_PAIRS
         T = 1
     nb = None
     if bm == A.LG_BINARY_BREAKING_SINTER:
@@ -97,12 +98,12 @@ def test_all_pairs_forces_and_positions(T, bm, hm):
     assert np.array_equal(s.bonds(), o.bonds())
 
 
-@pytest.mark.parametrize("T", [1, 8, 0])
+@pytest.mark.parametrize("T", [1, 8, 0, -1])
 def test_verlet_list_with_spring_carry(T):
     mat, d, x0, v0 = _aggregate_system(2000, 33, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET,
                                        squeeze=3e7)
-    if T == 0:  # compacted kernel: sequential order per row, bit-exact
-        d.force_kernel = A.LG_FORCE_KERNEL_COMPACT
+    if T <= 0:  # compacted / pair-parallel kernel: sequential order per row, bit-exact
+        d.force_kernel = A.LG_FORCE_KERNEL_COMPACT if T == 0 else A.LG_FORCE_KERNEL_PAIRS
         T = 1
     else:
         d.force_kernel = A.LG_FORCE_KERNEL_ROWGROUP
