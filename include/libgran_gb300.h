@@ -122,6 +122,48 @@ typedef struct lg_facet_desc {
 
 /* Everything the granular_system constructor and its functor list fix at compile/construct time
  * (granular_system.h:53-63; granular_system_neighbor_list.h:54-64 adds n_part and r_verlet). */
+/* ---- step-handler hooks and body forces (types) ------------------------------------------- */
+
+/* Held increments (a custom step handler that holds particles, Custom-step-handler.md:82-97, whose
+ * fixed_particle_step_handler skips increment_v of one particle): mask[i] is a bit set of the
+ * increments the integrator skips for particle i, in both half kicks and in the drift. With
+ * connectors (LG_BINARY_SINTER_CONNECTORS) a held x or theta also keeps the particle's connectors
+ * (the skipped call is sinter_step_handler's, sinter_bridge.h:24-42, 55-75). */
+#define LG_HOLD_X 1
+#define LG_HOLD_V 2
+#define LG_HOLD_THETA 4
+#define LG_HOLD_OMEGA 8
+
+/* Unary body force appended to the unary functor container after the facets (the container folds
+ * its functors as f0 + (f1 + (... + body)), unary_force_container.h:27-29).
+ *   LG_BODY_CENTRAL: central_attraction_functor of Custom-unary-force-model.md:66-120,
+ *     a = k_a / mass * (centre - x_i), alpha = 0; the centre is set with lg_set_body_centre (the
+ *     tutorial's update_center_of_mass), one centre per system of a batch. */
+#define LG_BODY_NONE 0
+#define LG_BODY_CENTRAL 1
+typedef struct lg_body_force {
+    int32_t model;     /* LG_BODY_* */
+    double k_a;        /* N/m */
+    double mass;       /* kg */
+    double centre[3];  /* initial centre of every system */
+} lg_body_force;
+
+/* User-defined unary functor on the device (in place of a body force): called on the host once per
+ * force evaluation, or once per captured graph (replays relaunch what it launched), it launches
+ * work on `stream` that writes every particle's unary terms into a_out and alpha_out. Device
+ * arrays hold 4 doubles per particle (x, y, z, unused). The terms join the fold like a body force.
+ * Return 0, or nonzero to fail the step. include/libgran_gb300/libgran/body_force/device_unary.cuh
+ * builds such a hook from a __device__ functor. */
+typedef struct lg_unary_hook_args {
+    int64_t n;
+    const double *x, *v, *theta, *omega; /* the evaluation's positions and half-step velocities */
+    double *a_out, *alpha_out;
+    const int32_t *system_of;            /* batch: system index per particle; NULL otherwise */
+    double dt;
+    void *stream;                        /* cudaStream_t */
+} lg_unary_hook_args;
+typedef int (*lg_unary_hook)(const lg_unary_hook_args *args, void *user);
+
 typedef struct lg_system_desc {
     int64_t n_part;
     int32_t binary_model;    /* LG_BINARY_* */
@@ -146,6 +188,12 @@ typedef struct lg_system_desc {
                                      generator for it (3 doubles); it must not be parallel to the
                                      bond axis */
     int64_t n_connector_axes;     /* must equal the number of bonds found */
+    /* step-handler hook and unary terms in force from construction on (the construction-time force
+     * evaluation includes them, as the reference's containers do): */
+    const uint8_t *hold_mask;     /* n bytes of LG_HOLD_* bits, or NULL */
+    lg_body_force body;           /* model LG_BODY_NONE (zero-initialised): none */
+    lg_unary_hook unary_hook;     /* or NULL; excludes a body force */
+    void *unary_hook_user;
 } lg_system_desc;
 
 /* Force kernels. Both give deterministic sums; in FP64 both add each row in ascending j, and the
@@ -263,6 +311,18 @@ int lg_get_pair_springs(lg_system *sys, int64_t i, int64_t j, double *out9);
  * vertices (get_vertices(), triangular_facet.h:57-59). */
 int lg_facet_update_positions(lg_system *sys, int32_t facet, double dt);
 int lg_facet_get_vertices(lg_system *sys, int32_t facet, double *out9);
+
+/* ---- step-handler hooks and body forces -------------------------------------------------- */
+
+/* Replace the hold mask (n bytes of LG_HOLD_* bits; NULL holds nothing), from the next step on. */
+int lg_set_hold_mask(lg_system *sys, const uint8_t *mask);
+/* Replace the body force (NULL removes it), from the next force evaluation on. */
+int lg_set_body_force(lg_system *sys, const lg_body_force *force);
+/* centres: 3 doubles per system (one system unless the handle is a batch); queued on the handle's
+ * stream, takes effect from the next force evaluation. */
+int lg_set_body_centre(lg_system *sys, const double *centres);
+/* Replace the unary hook (hook NULL removes it), from the next force evaluation on. */
+int lg_set_unary_hook(lg_system *sys, lg_unary_hook hook, void *user);
 
 /* Number of CUDA kernel launches issued by this handle since creation (diagnostics). */
 int lg_get_launch_count(lg_system *sys, int64_t *count);

@@ -5,6 +5,7 @@
 // get_x/get_v/get_theta/get_omega read the state back (Granular-system.md:65-226).
 #ifndef LIBGRAN_GRANULAR_SYSTEM_H
 #define LIBGRAN_GRANULAR_SYSTEM_H
+#include <functional>
 #include "../contact_force/contact_force.h"
 #include "../utility/operator_overloads.h"
 #include "binary_force_container.h"
@@ -25,6 +26,10 @@ template <typename, typename> struct hamaker_functor;
 template <typename, typename> struct limited_range_hamaker_functor;
 template <typename, typename> struct simplified_hamaker_functor;
 template <typename, typename, typename...> struct triangular_facet;
+template <typename, typename> struct central_attraction_functor;
+namespace libgran_gb300 {
+template <typename> struct device_unary;
+}
 
 namespace libgran_gb300 {
 
@@ -39,6 +44,16 @@ template <typename T> struct is_hamaker : std::false_type {};
 template <typename V, typename R> struct is_hamaker<hamaker_functor<V, R>> : std::true_type {};
 template <typename V, typename R> struct is_hamaker<limited_range_hamaker_functor<V, R>> : std::true_type {};
 template <typename V, typename R> struct is_hamaker<simplified_hamaker_functor<V, R>> : std::true_type {};
+template <typename T> struct is_facet : std::false_type {};
+template <typename V, typename R, typename... F> struct is_facet<triangular_facet<V, R, F...>> : std::true_type {};
+template <typename T> struct is_central : std::false_type {};
+template <typename V, typename R> struct is_central<central_attraction_functor<V, R>> : std::true_type {};
+template <typename T> struct is_device_unary : std::false_type {};
+template <typename F> struct is_device_unary<device_unary<F>> : std::true_type {};
+// step handlers that hold increments expose hold_mask(n)
+template <typename H, typename = void> struct has_hold_mask : std::false_type {};
+template <typename H>
+struct has_hold_mask<H, std::void_t<decltype(std::declval<H const &>().hold_mask(size_t{}))>> : std::true_type {};
 
 struct desc_builder {
     lg_system_desc d{};
@@ -46,7 +61,9 @@ struct desc_builder {
     std::vector<double> neck;
     std::vector<binding *> sinter_bindings;
     std::vector<binding *> facet_bindings;
-    bool has_binary = false, has_hamaker = false;
+    std::vector<binding *> body_bindings;
+    std::vector<uint8_t> hold;
+    bool has_binary = false, has_hamaker = false, has_body = false;
 
     template <typename F>
     void binary(F &f) {
@@ -82,12 +99,40 @@ struct desc_builder {
             static_assert(sizeof(T) == 0, "binary functor has no GPU implementation in libgran_gb300");
         }
     }
+    // Unary functors: the facets, then at most one body force (the container's right fold puts the
+    // engine's body term last, so it must be the last functor).
     template <typename F>
     void unary(F &f) {
-        facets.push_back(f.desc);
-        facet_bindings.push_back(&f.bound);
+        using T = std::decay_t<F>;
+        if constexpr (is_facet<T>::value) {
+            if (has_body) throw std::invalid_argument("the body-force functor must follow the facets in the container");
+            facets.push_back(f.desc);
+            facet_bindings.push_back(&f.bound);
+        } else if constexpr (is_central<T>::value) {
+            if (has_body) throw std::invalid_argument("one body-force functor per container");
+            has_body = true;
+            d.body = f.body;
+            body_bindings.push_back(&f.bound);
+        } else if constexpr (is_device_unary<T>::value) {
+            if (has_body) throw std::invalid_argument("one body-force functor per container");
+            has_body = true;
+            d.unary_hook = &T::launch;
+            d.unary_hook_user = (void *)&f;
+        } else {
+            static_assert(sizeof(T) == 0, "unary functor has no GPU implementation in libgran_gb300");
+        }
     }
 };
+
+// The hold mask of a step handler that holds increments (fixed_particle_step_handler,
+// held_particles_step_handler); empty for the others.
+template <typename H>
+std::vector<uint8_t> hold_of(H const &h, size_t n) {
+    if constexpr (has_hold_mask<H>::value)
+        return h.hold_mask(n);
+    else
+        return {};
+}
 
 }  // namespace libgran_gb300
 
@@ -110,7 +155,8 @@ public:
                     binary_force_functor_container_t binary_force_functors,
                     unary_force_functor_container_t unary_force_functors)
         : granular_system(LG_PAIRS_ALL, 0.0, std::move(x0), std::move(v0), std::move(theta0), std::move(omega0),
-                          binary_force_functors, unary_force_functors) {}
+                          binary_force_functors, unary_force_functors,
+                          [&step_handler](size_t n_part) { return libgran_gb300::hold_of(step_handler, n_part); }) {}
 
     ~granular_system() { lg_destroy(sys); }
 
@@ -132,7 +178,8 @@ public:
 protected:
     granular_system(int pairs, double r_verlet, field_container_t x0, field_container_t v0, field_container_t theta0,
                     field_container_t omega0, binary_force_functor_container_t &binary,
-                    unary_force_functor_container_t &unary) {
+                    unary_force_functor_container_t &unary,
+                    std::function<std::vector<uint8_t>(size_t)> hold_mask_of = nullptr) {
         libgran_gb300::desc_builder b;
         std::apply([&b](auto &...f) { (b.binary(f), ...); }, binary.binary_force_functors);
         std::apply([&b](auto &...f) { (b.unary(f), ...); }, unary.unary_force_functors);
@@ -143,6 +190,9 @@ protected:
         b.d.precision = libgran_gb300::default_precision();
         if (b.d.binary_model == LG_BINARY_SINTER_CONNECTORS) b.d.precision = LG_PRECISION_FP64;  // FP64 only
         b.d.n_facets = (int32_t)b.facets.size();
+        std::vector<uint8_t> hold;
+        if (hold_mask_of) hold = hold_mask_of(x0.size());
+        if (!hold.empty()) b.d.hold_mask = hold.data();
         auto xa = libgran_gb300::to_aos(x0), va = libgran_gb300::to_aos(v0), ta = libgran_gb300::to_aos(theta0),
              wa = libgran_gb300::to_aos(omega0);
         libgran_gb300::check(lg_create(&b.d, xa.data(), va.data(), ta.data(), wa.data(),
@@ -150,6 +200,7 @@ protected:
                                        b.neck.empty() ? nullptr : b.neck.data(), (int64_t)b.neck.size(), 0, &sys),
                              "granular_system");
         for (auto *p : b.sinter_bindings) p->sys = sys;
+        for (auto *p : b.body_bindings) p->sys = sys;
         for (size_t f = 0; f < b.facet_bindings.size(); ++f) {
             b.facet_bindings[f]->sys = sys;
             b.facet_bindings[f]->facet = (int32_t)f;

@@ -25,11 +25,12 @@ public:
                                   field_container_t v0, field_container_t theta0, field_container_t omega0,
                                   real_t t0 [[maybe_unused]], field_value_t field_zero [[maybe_unused]],
                                   real_t real_zero [[maybe_unused]],
-                                  step_handler_t<field_container_t, field_value_t> &step_handler [[maybe_unused]],
+                                  step_handler_t<field_container_t, field_value_t> &step_handler,
                                   binary_force_functor_container_t binary_force_functors,
                                   unary_force_functor_container_t unary_force_functors)
         : base(LG_PAIRS_VERLET, (double)r_verlet, std::move(x0), std::move(v0), std::move(theta0), std::move(omega0),
-               binary_force_functors, unary_force_functors) {}
+               binary_force_functors, unary_force_functors,
+               [&step_handler](size_t n) { return libgran_gb300::hold_of(step_handler, n); }) {}
 
     void update_neighbor_list() { libgran_gb300::check(lg_update_neighbor_list(this->sys), "update_neighbor_list"); }
 };

@@ -22,6 +22,8 @@ LG_DEVERR_LIST_OVERFLOW, LG_DEVERR_NONFINITE, LG_DEVERR_BOND_LOST = 1, 2, 4
 LG_NOALLOC_OBS, LG_NOALLOC_MAX_PARTICLES = 9, 1048320
 LG_OBS_STATE, LG_OBS_PAIRS = 1, 2
 LG_REQ_QUEUED, LG_REQ_RUNNING, LG_REQ_DONE, LG_REQ_FAILED, LG_REQ_CANCELLED = 0, 1, 2, 3, 4
+LG_HOLD_X, LG_HOLD_V, LG_HOLD_THETA, LG_HOLD_OMEGA = 1, 2, 4, 8
+LG_BODY_NONE, LG_BODY_CENTRAL = 0, 1
 
 
 class lg_contact_params(C.Structure):
@@ -61,6 +63,19 @@ class lg_server_stats(C.Structure):
                [(n, C.c_double) for n in ("p50_latency_ms", "p99_latency_ms", "max_latency_ms")]
 
 
+class lg_body_force(C.Structure):
+    _fields_ = [("model", C.c_int32), ("k_a", C.c_double), ("mass", C.c_double), ("centre", C.c_double * 3)]
+
+
+class lg_unary_hook_args(C.Structure):
+    _fields_ = [("n", C.c_int64), ("x", C.c_void_p), ("v", C.c_void_p), ("theta", C.c_void_p),
+                ("omega", C.c_void_p), ("a_out", C.c_void_p), ("alpha_out", C.c_void_p),
+                ("system_of", C.c_void_p), ("dt", C.c_double), ("stream", C.c_void_p)]
+
+
+lg_unary_hook = C.CFUNCTYPE(C.c_int, C.POINTER(lg_unary_hook_args), C.c_void_p)
+
+
 class lg_system_desc(C.Structure):
     _fields_ = [("n_part", C.c_int64), ("binary_model", C.c_int32), ("hamaker_model", C.c_int32),
                 ("contact", lg_contact_params), ("sinter", lg_sinter_params),
@@ -68,7 +83,9 @@ class lg_system_desc(C.Structure):
                 ("r_verlet", C.c_double), ("precision", C.c_int32), ("n_facets", C.c_int32),
                 ("facet_auto_move", C.c_int32), ("max_neighbors", C.c_int32), ("threads_per_row", C.c_int32),
                 ("force_kernel", C.c_int32), ("connector", lg_connector_params),
-                ("connector_axes", C.POINTER(C.c_double)), ("n_connector_axes", C.c_int64)]
+                ("connector_axes", C.POINTER(C.c_double)), ("n_connector_axes", C.c_int64),
+                ("hold_mask", C.POINTER(C.c_uint8)), ("body", lg_body_force), ("unary_hook", lg_unary_hook),
+                ("unary_hook_user", C.c_void_p)]
 
 
 class lg_observables(C.Structure):
@@ -160,6 +177,10 @@ def _declare(L):
         "lg_get_force_kernel_time": (C.c_int, [vp, P(d), P(i64)]),
         "lg_generate_rsa_aggregate": (C.c_int, [C.c_uint64, i64, d, P(d)]),
         "lg_generate_velocities": (C.c_int, [C.c_uint64, i64, d, P(d)]),
+        "lg_set_hold_mask": (C.c_int, [vp, P(C.c_uint8)]),
+        "lg_set_body_force": (C.c_int, [vp, P(lg_body_force)]),
+        "lg_set_body_centre": (C.c_int, [vp, P(d)]),
+        "lg_set_unary_hook": (C.c_int, [vp, lg_unary_hook, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

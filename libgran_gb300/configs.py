@@ -101,6 +101,19 @@ def set_connectors(desc, k_d, gamma_d, critical_separation, axes):
     return desc
 
 
+def set_hold(desc, mask):
+    """Hold mask from construction on: LG_HOLD_* bits per particle (kept alive on the descriptor)."""
+    m = np.ascontiguousarray(np.asarray(mask, dtype=np.uint8).reshape(-1))
+    desc.hold_mask = m.ctypes.data_as(C.POINTER(C.c_uint8))
+    desc._hold_keepalive = m
+    return desc
+
+
+def central_body(k_a, mass, centre):
+    """lg_body_force of the central attraction a = k_a / mass * (centre - x_i)."""
+    return A.lg_body_force(A.LG_BODY_CENTRAL, float(k_a), float(mass), (C.c_double * 3)(*[float(c) for c in centre]))
+
+
 def random_unit_axes(count, seed):
     """Seeded unit vectors (uniform in the cube, normalised), one per bond."""
     rng = np.random.default_rng(seed)

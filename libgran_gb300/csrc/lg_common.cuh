@@ -120,7 +120,14 @@ struct Params {
     double hamaker_skip_d2;  // squared centre distance above which the limited Hamaker is zero
     int32_t springs_ff;      // pair and bond springs held as float-float pairs (mixed precision)
     lg_connector_params connector;  // 5-connector sinter model
+    const uint8_t *hold;     // [n] LG_HOLD_* bits of the increments the integrator skips; null: none
+    const dbl4 *ext_a;       // [n] unary body-force terms (a, alpha) folded after the facets; null: none
+    const dbl4 *ext_al;
 };
+
+// Kick of one half step, v + h * a, unless a step handler holds that increment.
+__device__ __forceinline__ d3 kick_unless(d3 v, double h, d3 a, bool held) { return held ? v : add(v, scl(h, a)); }
+__device__ __forceinline__ uint32_t hold_of(const uint8_t *hold, int64_t i) { return hold ? (uint32_t)hold[i] : 0u; }
 
 // Entry flags of a pair slot (Verlet list slot or implicit all-pairs slot)
 constexpr uint32_t kXiLive = 1u;      // contact springs may be nonzero

@@ -26,15 +26,22 @@ __device__ __forceinline__ void move_facets(const Params &P, const StateView &S,
         for (int q = 0; q < 9; ++q) S.facet_vert_next[9 * f + q] = S.facet_vert[9 * f + q] + P.facets[f].v[q % 3] * dt;
 }
 
-// Unary (facet) terms of particle i in facet order (kept out of line: the common no-facet path then
-// needs few registers; static: each translation unit keeps its own copy, compiled with its own
-// floating-point flags).
-static __device__ __noinline__ void facet_terms(const Params &P, const StateView &S, int64_t i, int64_t n, d3 vi, d3 wi,
-                                         d3 &ua, d3 &ual) {
+// Unary terms of particle i: the facets in order, then the body-force term (P.ext_a / P.ext_al),
+// folded as the reference's unary container folds its functors, f0 + (f1 + (... + body))
+// (unary_force_container.h:27-29): the last term first, each earlier one added in front. Returns
+// false when there is no unary term. Kept out of line: the common no-facet path then needs few
+// registers; static: each translation unit keeps its own copy, compiled with its own
+// floating-point flags.
+static __device__ __noinline__ bool unary_terms(const Params &P, const StateView &S, int64_t i, int64_t n, d3 vi,
+                                                d3 wi, d3 &ua, d3 &ual) {
     const d3 xi = ld4(S.x, i);
-    ua = zero3();
-    ual = zero3();
-    for (int f = 0; f < P.n_facets; ++f) {
+    bool have = false;
+    if (P.ext_a) {
+        ua = ld4(P.ext_a, i);
+        ual = ld4(P.ext_al, i);
+        have = true;
+    }
+    for (int f = P.n_facets - 1; f >= 0; --f) {
         const FacetDev &fd = P.facets[f];
         d3 N = mk3(fd.normal[0], fd.normal[1], fd.normal[2]);
         d3 xf = closest_point_on_triangle(S.facet_vert + 9 * f, fd.area, N, xi);
@@ -67,32 +74,37 @@ static __device__ __noinline__ void facet_terms(const Params &P, const StateView
                 fal = zero3();
             }
         }
-        if (f == 0) {
+        if (have) {
+            ua = add(fa, ua);
+            ual = add(fal, ual);
+        } else {
             ua = fa;
             ual = fal;
-        } else {
-            ua = add(ua, fa);
-            ual = add(ual, fal);
+            have = true;
         }
     }
+    return have;
 }
 
-// Tail of particle i's force evaluation: the unary (facet) terms in facet order, added after the
-// binary sums (accA, accW return the totals); stores a and alpha, the half-kicked velocities, and
-// flags non-finite results. FACETS = false: the caller knows there are no facets.
+// Tail of particle i's force evaluation: the unary terms (facets, body force), added after the
+// binary sums (accA, accW return the totals); stores a and alpha, the half-kicked velocities (a held
+// increment keeps the velocity), and flags non-finite results. FACETS = false: the caller knows
+// there is no unary term.
 template <bool FACETS = true>
 __device__ __forceinline__ void finish_row(const Params &P, const StateView &S, int64_t i, int64_t n, d3 &accA,
                                            d3 &accW, d3 vi, d3 wi, double hdt) {
-    if (FACETS && P.n_facets > 0) {
+    if (FACETS && (P.n_facets > 0 || P.ext_a)) {
         d3 ua, ual;
-        facet_terms(P, S, i, n, vi, wi, ua, ual);
-        accA = add(accA, ua);
-        accW = add(accW, ual);
+        if (unary_terms(P, S, i, n, vi, wi, ua, ual)) {
+            accA = add(accA, ua);
+            accW = add(accW, ual);
+        }
     }
+    const uint32_t h = hold_of(P.hold, i);
     st4(S.a, i, accA);
     st4(S.al, i, accW);
-    st4(S.v_out, i, add(vi, scl(hdt, accA)));
-    st4(S.w_out, i, add(wi, scl(hdt, accW)));
+    st4(S.v_out, i, kick_unless(vi, hdt, accA, h & LG_HOLD_V));
+    st4(S.w_out, i, kick_unless(wi, hdt, accW, h & LG_HOLD_OMEGA));
     if (!isfinite(accA.x) || !isfinite(accA.y) || !isfinite(accA.z) || !isfinite(accW.x) || !isfinite(accW.y) ||
         !isfinite(accW.z))
         set_error(S.err, LG_DEVERR_NONFINITE);

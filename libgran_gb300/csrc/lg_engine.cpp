@@ -462,6 +462,25 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
     }
     const bool compact = s->kernel == LG_FORCE_KERNEL_COMPACT;
     int kernels = 1;
+    if (s->body.model == LG_BODY_CENTRAL) {
+        launch_body_central(s->P.n, s->x, s->n_systems > 0 ? s->d_agg : nullptr, s->d_centre, s->body.k_a / s->body.mass,
+                            s->ext_a, s->ext_al, s->stream);
+        s->launches += 1;
+    } else if (s->hook) {
+        lg_unary_hook_args ha{};
+        ha.n = s->P.n;
+        ha.x = (const double *)s->x;
+        ha.v = (const double *)S.v;
+        ha.theta = (const double *)s->th;
+        ha.omega = (const double *)S.w;
+        ha.a_out = (double *)s->ext_a;
+        ha.alpha_out = (double *)s->ext_al;
+        ha.system_of = s->n_systems > 0 ? s->d_agg : nullptr;
+        ha.dt = dt;
+        ha.stream = (void *)s->stream;
+        const int hr = s->hook(&ha, s->hook_user);
+        if (hr != 0) return lg_fail(LG_E_STATE, "unary hook returned %d", hr);
+    }
     if (s->precision == LG_PRECISION_MIXED) {
         if (compact)
             kernels = launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, fuse_kick,
@@ -493,9 +512,9 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_n
     if (!s->kick_done) {
         if (s->precision == LG_PRECISION_MIXED)
             launch_kick_drift_mixed(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt,
-                                    s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->stream);
+                                    s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->P.hold, s->stream);
         else
-            launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->bv,
+            launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->bv, s->P.hold,
                                    s->stream);
         s->launches += 1;
     }
@@ -537,6 +556,61 @@ static int check_args(const lg_system_desc *d) {
         if (T != 0 && T != 1 && T != 2 && T != 4 && T != 8 && T != 16 && T != 32)
             return lg_fail(LG_E_INVALID, "lg_create: threads_per_row must be 0 or a power of two <= 32");
     }
+    return LG_OK;
+}
+
+// Hold mask (LG_HOLD_* bits per particle); null clears it. Params are captured by value in the
+// CUDA graphs, so the graphs are dropped.
+static int apply_hold(lg_system *s, const uint8_t *mask) {
+    s->drop_graphs();
+    if (!mask) {
+        s->P.hold = nullptr;
+        return LG_OK;
+    }
+    for (int64_t i = 0; i < s->P.n; ++i)
+        if (mask[i] & ~(LG_HOLD_X | LG_HOLD_V | LG_HOLD_THETA | LG_HOLD_OMEGA))
+            return lg_fail(LG_E_INVALID, "hold mask: particle %lld has unknown bits 0x%x", (long long)i, mask[i]);
+    if (!s->d_hold) LG_TRY(s->alloc(&s->d_hold, (size_t)s->P.n));
+    LG_CUDA(cudaMemcpyAsync(s->d_hold, mask, (size_t)s->P.n, cudaMemcpyHostToDevice, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    s->P.hold = s->d_hold;
+    return LG_OK;
+}
+
+// Body force or unary hook (at most one); both write the per-particle unary terms that the force
+// kernels fold after the facets.
+static int apply_unary(lg_system *s, const lg_body_force *body, lg_unary_hook hook, void *user) {
+    const int model = body ? body->model : LG_BODY_NONE;
+    if (model != LG_BODY_NONE && model != LG_BODY_CENTRAL)
+        return lg_fail(LG_E_INVALID, "body force: unknown model %d", model);
+    if (model != LG_BODY_NONE && hook) return lg_fail(LG_E_INVALID, "a body force and a unary hook exclude each other");
+    if (model == LG_BODY_CENTRAL) {
+        if (!(body->mass > 0) || !std::isfinite(body->mass) || !std::isfinite(body->k_a))
+            return lg_fail(LG_E_INVALID, "body force: mass must be positive and k_a finite");
+        for (int c = 0; c < 3; ++c)
+            if (!std::isfinite(body->centre[c])) return lg_fail(LG_E_INVALID, "body force: centre is not finite");
+    }
+    s->drop_graphs();
+    const bool on = model != LG_BODY_NONE || hook;
+    if (on && !s->ext_a) {
+        LG_TRY(s->alloc(&s->ext_a, (size_t)s->P.n));
+        LG_TRY(s->alloc(&s->ext_al, (size_t)s->P.n));
+    }
+    if (model == LG_BODY_CENTRAL) {
+        const int64_t nsys = std::max<int64_t>(1, s->n_systems);
+        if (!s->d_centre) LG_TRY(s->alloc(&s->d_centre, 3 * (size_t)nsys));
+        std::vector<double> c(3 * (size_t)nsys);
+        for (int64_t q = 0; q < nsys; ++q)
+            for (int k = 0; k < 3; ++k) c[3 * q + k] = body->centre[k];
+        LG_CUDA(cudaMemcpyAsync(s->d_centre, c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice, s->stream));
+        LG_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    s->body = lg_body_force{};
+    if (model != LG_BODY_NONE) s->body = *body;
+    s->hook = hook;
+    s->hook_user = hook ? user : nullptr;
+    s->P.ext_a = on ? s->ext_a : nullptr;
+    s->P.ext_al = on ? s->ext_al : nullptr;
     return LG_OK;
 }
 
@@ -971,6 +1045,8 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         return lg_fail(LG_E_INVALID, "lg_create: the pair-parallel force kernel takes at most %lld pair slots",
                        (long long)kPairsMaxSlots);
     if (d->threads_per_row > 0 && d->force_kernel == LG_FORCE_KERNEL_AUTO) s->kernel = LG_FORCE_KERNEL_ROWGROUP;
+    LG_TRY(apply_hold(s, d->hold_mask));
+    LG_TRY(apply_unary(s, &d->body, d->unary_hook, d->unary_hook_user));
     // initial accelerations (the first half kick needs them); velocities are unchanged (hdt = 0)
     LG_TRY(launch_forces(s, 0.0, 0.0, 0));
     LG_CUDA(cudaStreamSynchronize(s->stream));
@@ -1187,6 +1263,33 @@ extern "C" int lg_set_force_kernel(lg_system *s, int32_t variant) {
                        "%lld pair slots", (long long)kPairsMaxSlots);
     s->kernel = k;
     return LG_OK;
+}
+
+extern "C" int lg_set_hold_mask(lg_system *s, const uint8_t *mask) {
+    LG_HANDLE(s);
+    return apply_hold(s, mask);
+}
+
+extern "C" int lg_set_body_force(lg_system *s, const lg_body_force *force) {
+    LG_HANDLE(s);
+    return apply_unary(s, force, nullptr, nullptr);
+}
+
+extern "C" int lg_set_body_centre(lg_system *s, const double *centres) {
+    LG_HANDLE(s);
+    if (!centres) return lg_fail(LG_E_INVALID, "lg_set_body_centre: null centres");
+    if (s->body.model != LG_BODY_CENTRAL) return lg_fail(LG_E_STATE, "lg_set_body_centre: no central body force is set");
+    const int64_t nsys = std::max<int64_t>(1, s->n_systems);
+    for (int64_t q = 0; q < 3 * nsys; ++q)
+        if (!std::isfinite(centres[q])) return lg_fail(LG_E_INVALID, "lg_set_body_centre: centre %lld is not finite", (long long)(q / 3));
+    LG_CUDA(cudaMemcpyAsync(s->d_centre, centres, sizeof(double) * 3 * (size_t)nsys, cudaMemcpyHostToDevice, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
+    return LG_OK;
+}
+
+extern "C" int lg_set_unary_hook(lg_system *s, lg_unary_hook hook, void *user) {
+    LG_HANDLE(s);
+    return apply_unary(s, nullptr, hook, user);
 }
 
 extern "C" int lg_reset_acceleration_buffers(lg_system *s) {

@@ -50,6 +50,12 @@ struct lg_system {
     float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
     int32_t *d_flag = nullptr;  // mixed: device flag of the float-float copy check
     double *pres = nullptr;     // FP64 pair-parallel kernel: per-slot pair values [6][cap * n]
+    uint8_t *d_hold = nullptr;  // [n] LG_HOLD_* bits (allocated on first use)
+    lg::dbl4 *ext_a = nullptr, *ext_al = nullptr;  // [n] unary body-force terms (allocated on first use)
+    double *d_centre = nullptr; // [3 * systems] centres of the central body force
+    lg_body_force body{};       // model LG_BODY_NONE: no body force
+    lg_unary_hook hook = nullptr;
+    void *hook_user = nullptr;
     double origin[4] = {0.0, 0.0, 0.0, 0.0};  // mixed: origin of the float-float positions, extent in [3]
     double r_max = 0.0;                        // mixed: largest particle radius of the functors
     double ext_max = 0.0;                      // mixed: largest extent of a system about its origin

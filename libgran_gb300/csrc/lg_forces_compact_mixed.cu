@@ -649,13 +649,15 @@ __global__ void __launch_bounds__(64) forces_finish_mixed(Params P, StateView S,
     }
     compact::finish_row<FACETS>(P, S, i, P.n, a_tot, al_tot, vi, wi, hdt);
     if (kick) {  // the next step's opening half kick and drift (the end-of-step velocities are not kept)
-        const d3 ve = add(vi, scl(hdt, a_tot)), we = add(wi, scl(hdt, al_tot));
-        const d3 vh = add(ve, scl(hdt, a_tot)), wh = add(we, scl(hdt, al_tot));
+        const uint32_t h = hold_of(P.hold, i);
+        const bool hv = h & LG_HOLD_V, hw = h & LG_HOLD_OMEGA;
+        const d3 vh = kick_unless(kick_unless(vi, hdt, a_tot, hv), hdt, a_tot, hv);
+        const d3 wh = kick_unless(kick_unless(wi, hdt, al_tot, hw), hdt, al_tot, hw);
         st4(S.v_out, i, vh);
         st4(S.w_out, i, wh);
-        const d3 xn = add(xo, scl(dt, vh));
-        st4(S.x, i, xn);
-        st4(S.th, i, add(tho, scl(dt, wh)));
+        const d3 xn = (h & LG_HOLD_X) ? xo : add(xo, scl(dt, vh));
+        if (!(h & LG_HOLD_X)) st4(S.x, i, xn);
+        if (!(h & LG_HOLD_THETA)) st4(S.th, i, add(tho, scl(dt, wh)));
         rel_ff(xn, MX.ox, MX.oy, MX.oz, MX.agg, MX.orig, i, P.n, MX.x32);
         vel_ff(vh, wh, i, P.n, MX.v32);
     }
@@ -746,7 +748,7 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         cudaStreamWaitEvent(st, join, 0);
     }
     const unsigned blocks = (unsigned)((P.n + 63) / 64);
-    if (P.n_facets > 0)
+    if (P.n_facets > 0 || P.ext_a)
         forces_finish_mixed<true><<<blocks, 64, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, kick ? 1 : 0, MX);
     else
         forces_finish_mixed<false><<<blocks, 64, 0, st>>>(P, S, hdt, dt, 0, contacts, hamaker, kick ? 1 : 0, MX);

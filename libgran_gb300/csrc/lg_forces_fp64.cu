@@ -21,14 +21,16 @@ namespace lg {
 // (sinter_bridge.h:24-42, 55-75): the particle's connectors move with it by dx, then turn by
 // dtheta about its moved centre.
 // Drift of particle i with kicked velocities vi, wi (stored by the caller).
+// A held increment (LG_HOLD_X, LG_HOLD_THETA in `h`) is skipped together with its connector update.
 __device__ __forceinline__ void drift_one(int64_t n, int64_t i, dbl4 *__restrict__ x, dbl4 *__restrict__ th, d3 vi,
-                                          d3 wi, double dt, const BondView &BV) {
+                                          d3 wi, double dt, const BondView &BV, uint32_t h) {
+    const bool hx = h & LG_HOLD_X, hth = h & LG_HOLD_THETA;
     const d3 dx = scl(dt, vi);
-    const d3 xn = add(ld4(x, i), dx);
-    st4(x, i, xn);
+    const d3 xn = hx ? ld4(x, i) : add(ld4(x, i), dx);
+    if (!hx) st4(x, i, xn);
     const d3 dth = scl(dt, wi);
-    st4(th, i, add(ld4(th, i), dth));
-    if (BV.cn) {
+    if (!hth) st4(th, i, add(ld4(th, i), dth));
+    if (BV.cn && !(hx && hth)) {
         const int64_t bs = (int64_t)BV.bcap * n;
         for (int b = 0; b < BV.bcap; ++b) {
             const int64_t e = (int64_t)b * n + i;
@@ -36,8 +38,9 @@ __device__ __forceinline__ void drift_one(int64_t n, int64_t i, dbl4 *__restrict
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
                 double *cx = BV.cn + (3 * k) * bs + e, *cy = BV.cn + (3 * k + 1) * bs + e, *cz = BV.cn + (3 * k + 2) * bs + e;
-                d3 c = add(mk3(*cx, *cy, *cz), dx);
-                c = add(c, crs(dth, sub(c, xn)));
+                d3 c = mk3(*cx, *cy, *cz);
+                if (!hx) c = add(c, dx);
+                if (!hth) c = add(c, crs(dth, sub(c, xn)));
                 *cx = c.x;
                 *cy = c.y;
                 *cz = c.z;
@@ -48,14 +51,30 @@ __device__ __forceinline__ void drift_one(int64_t n, int64_t i, dbl4 *__restrict
 
 __global__ void kick_drift_fp64(int64_t n, dbl4 *__restrict__ x, dbl4 *__restrict__ v,
                                 dbl4 *__restrict__ th, dbl4 *__restrict__ w, const dbl4 *__restrict__ a,
-                                const dbl4 *__restrict__ al, double dt, double hdt, BondView BV) {
+                                const dbl4 *__restrict__ al, double dt, double hdt, BondView BV,
+                                const uint8_t *__restrict__ hold) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));
-    d3 wi = add(ld4(w, i), scl(hdt, ld4(al, i)));
+    const uint32_t h = hold_of(hold, i);
+    d3 vi = kick_unless(ld4(v, i), hdt, ld4(a, i), h & LG_HOLD_V);
+    d3 wi = kick_unless(ld4(w, i), hdt, ld4(al, i), h & LG_HOLD_OMEGA);
     st4(v, i, vi);
     st4(w, i, wi);
-    drift_one(n, i, x, th, vi, wi, dt, BV);
+    drift_one(n, i, x, th, vi, wi, dt, BV, h);
+}
+
+// Body force LG_BODY_CENTRAL (central_attraction_functor, Custom-unary-force-model.md:108-118):
+// a = k_a / mass * (centre - x_i), alpha = 0; kam = k_a / mass (formed on the host, as the
+// functor forms it); one centre per system.
+__global__ void body_central(int64_t n, const dbl4 *__restrict__ x, const int32_t *__restrict__ agg,
+                             const double *__restrict__ centre, double kam, dbl4 *__restrict__ ea,
+                             dbl4 *__restrict__ eal) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t q = agg ? (int64_t)agg[i] : 0;
+    const d3 c = mk3(centre[3 * q], centre[3 * q + 1], centre[3 * q + 2]);
+    st4(ea, i, scl(kam, sub(c, ld4(x, i))));
+    st4(eal, i, zero3());
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -198,60 +217,7 @@ __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairVi
         accw.z = group_sum<T>(accw.z);
     }
     if (!active || lane != 0) return;
-
-    if (P.n_facets > 0) {
-        d3 ua = zero3(), ual = zero3();
-        for (int f = 0; f < P.n_facets; ++f) {
-            const FacetDev &fd = P.facets[f];
-            d3 N = mk3(fd.normal[0], fd.normal[1], fd.normal[2]);
-            d3 xf = closest_point_on_triangle(S.facet_vert + 9 * f, fd.area, N, xi_);
-            d3 vf = mk3(fd.v[0], fd.v[1], fd.v[2]);
-            d3 fa = zero3(), fal = zero3();
-            bool hv = false;
-            if (fd.has_contact) {
-                double *sx = S.sxi;
-                const int64_t base = (int64_t)f * 9 * n;
-                d3 s[3];
-#pragma unroll
-                for (int q = 0; q < 3; ++q)
-                    s[q] = mk3(sx[base + (3 * q) * n + i], sx[base + (3 * q + 1) * n + i], sx[base + (3 * q + 2) * n + i]);
-                surface_contact(fd.contact, xf, vf, xi_, vi, wi, s, fa, fal);
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    sx[base + (3 * q) * n + i] = s[q].x;
-                    sx[base + (3 * q + 1) * n + i] = s[q].y;
-                    sx[base + (3 * q + 2) * n + i] = s[q].z;
-                }
-                hv = true;
-            }
-            if (fd.has_hamaker) {
-                d3 ha = surface_hamaker(fd.hamaker, xf, xi_);
-                if (hv) {
-                    fa = add(fa, ha);
-                    fal = add(fal, zero3());
-                } else {
-                    fa = ha;
-                    fal = zero3();
-                }
-            }
-            if (f == 0) {
-                ua = fa;
-                ual = fal;
-            } else {
-                ua = add(ua, fa);
-                ual = add(ual, fal);
-            }
-        }
-        acc = add(acc, ua);
-        accw = add(accw, ual);
-    }
-    st4(S.a, i, acc);
-    st4(S.al, i, accw);
-    st4(S.v_out, i, add(vi, scl(hdt, acc)));
-    st4(S.w_out, i, add(wi, scl(hdt, accw)));
-    if (!isfinite(acc.x) || !isfinite(acc.y) || !isfinite(acc.z) || !isfinite(accw.x) || !isfinite(accw.y) ||
-        !isfinite(accw.z))
-        set_error(S.err, LG_DEVERR_NONFINITE);
+    compact::finish_row(P, S, i, n, acc, accw, vi, wi, hdt);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -304,11 +270,12 @@ __global__ void __launch_bounds__(kFoldBlock) fold_pairs_fp64(Params P, StateVie
     const d3 vi = ld4(S.v, i), wi = ld4(S.w, i);
     compact::finish_row<FACETS>(P, S, i, n, acc, accw, vi, wi, hdt);
     if (kick) {  // the next step's opening half kick and drift, as kick_drift_fp64
-        const d3 v2 = add(add(vi, scl(hdt, acc)), scl(hdt, acc));
-        const d3 w2 = add(add(wi, scl(hdt, accw)), scl(hdt, accw));
+        const uint32_t h = hold_of(P.hold, i);
+        const d3 v2 = kick_unless(kick_unless(vi, hdt, acc, h & LG_HOLD_V), hdt, acc, h & LG_HOLD_V);
+        const d3 w2 = kick_unless(kick_unless(wi, hdt, accw, h & LG_HOLD_OMEGA), hdt, accw, h & LG_HOLD_OMEGA);
         st4(S.v_out, i, v2);
         st4(S.w_out, i, w2);
-        drift_one(n, i, S.x, S.th, v2, w2, dt, BV);
+        drift_one(n, i, S.x, S.th, v2, w2, dt, BV, h);
     }
 }
 
@@ -750,13 +717,14 @@ int launch_forces_pairs_fp64(const Params &P, const StateView &S, const PairView
     }
     const unsigned fb = (unsigned)((n + kFoldBlock - 1) / kFoldBlock);
     const int kk = kick ? 1 : 0;
+    const bool unary = P.n_facets > 0 || P.ext_a;
     if (verlet) {
-        if (P.n_facets > 0)
+        if (unary)
             fold_pairs_fp64<true, true><<<fb, kFoldBlock, 0, st>>>(P, S, PV, BV, pres, ps, hdt, dt, move_facets, kk);
         else
             fold_pairs_fp64<true, false><<<fb, kFoldBlock, 0, st>>>(P, S, PV, BV, pres, ps, hdt, dt, move_facets, kk);
     } else {
-        if (P.n_facets > 0)
+        if (unary)
             fold_pairs_fp64<false, true><<<fb, kFoldBlock, 0, st>>>(P, S, PV, BV, pres, ps, hdt, dt, move_facets, kk);
         else
             fold_pairs_fp64<false, false><<<fb, kFoldBlock, 0, st>>>(P, S, PV, BV, pres, ps, hdt, dt, move_facets, kk);
@@ -764,12 +732,21 @@ int launch_forces_pairs_fp64(const Params &P, const StateView &S, const PairView
     return total > 0 ? 2 : 1;
 }
 
+void launch_body_central(int64_t n, const dbl4 *x, const int32_t *agg, const double *centre, double kam, dbl4 *ea,
+                         dbl4 *eal, cudaStream_t st) {
+    const int threads = 64;
+    const int64_t blocks = (n + threads - 1) / threads;
+    if (blocks == 0) return;
+    body_central<<<(unsigned)blocks, threads, 0, st>>>(n, x, agg, centre, kam, ea, eal);
+}
+
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
-                            const dbl4 *al, double dt, double hdt, const BondView &BV, cudaStream_t st) {
+                            const dbl4 *al, double dt, double hdt, const BondView &BV, const uint8_t *hold,
+                            cudaStream_t st) {
     const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
-    kick_drift_fp64<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt, BV);
+    kick_drift_fp64<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt, BV, hold);
 }
 
 void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, double r_near, int64_t max_cells,

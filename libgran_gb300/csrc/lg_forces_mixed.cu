@@ -13,7 +13,7 @@
 // radius with a 1e-3 margin, so pairs that cannot touch and lie beyond the Hamaker cutoff cost no
 // FP64 work. Row groups, slot layout, flags and springs are shared with the FP64 path
 // (lg_common.cuh), so a system can switch precision between steps.
-#include "lg_common.cuh"
+#include "lg_compact.cuh"
 #include "lg_kernels.h"
 
 namespace lg {
@@ -291,42 +291,7 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
     const double I_c = (bm == LG_BINARY_SINTER || bm == LG_BINARY_BREAKING_SINTER) ? B.inertia : C.inertia;
     d3 a_tot = add(dvs(acc, m_c), acch);
     d3 al_tot = dvs(accw, I_c);
-    if (P.n_facets > 0) {
-        d3 ua = zero3(), ual = zero3();
-        for (int f = 0; f < P.n_facets; ++f) {
-            const FacetDev &fd = P.facets[f];
-            d3 N = mk3(fd.normal[0], fd.normal[1], fd.normal[2]);
-            d3 xf = closest_point_on_triangle(S.facet_vert + 9 * f, fd.area, N, xi_);
-            d3 vf = mk3(fd.v[0], fd.v[1], fd.v[2]);
-            d3 fa = zero3(), fal = zero3();
-            if (fd.has_contact) {
-                const int64_t base = (int64_t)f * 9 * n;
-                d3 s[3];
-#pragma unroll
-                for (int q = 0; q < 3; ++q)
-                    s[q] = mk3(S.sxi[base + (3 * q) * n + i], S.sxi[base + (3 * q + 1) * n + i], S.sxi[base + (3 * q + 2) * n + i]);
-                surface_contact(fd.contact, xf, vf, xi_, vi, wi, s, fa, fal);
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    S.sxi[base + (3 * q) * n + i] = s[q].x;
-                    S.sxi[base + (3 * q + 1) * n + i] = s[q].y;
-                    S.sxi[base + (3 * q + 2) * n + i] = s[q].z;
-                }
-            }
-            if (fd.has_hamaker) fa = add(fa, surface_hamaker(fd.hamaker, xf, xi_));
-            ua = add(ua, fa);
-            ual = add(ual, fal);
-        }
-        a_tot = add(a_tot, ua);
-        al_tot = add(al_tot, ual);
-    }
-    st4(S.a, i, a_tot);
-    st4(S.al, i, al_tot);
-    st4(S.v_out, i, add(vi, scl(hdt, a_tot)));
-    st4(S.w_out, i, add(wi, scl(hdt, al_tot)));
-    if (!isfinite(a_tot.x) || !isfinite(a_tot.y) || !isfinite(a_tot.z) || !isfinite(al_tot.x) ||
-        !isfinite(al_tot.y) || !isfinite(al_tot.z))
-        set_error(S.err, LG_DEVERR_NONFINITE);
+    compact::finish_row(P, S, i, n, a_tot, al_tot, vi, wi, hdt);
 }
 
 // Float-float copies of the positions (relative to the system origin; in a batch every system has
@@ -360,16 +325,20 @@ __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restri
                                  dbl4 *__restrict__ w, const dbl4 *__restrict__ a, const dbl4 *__restrict__ al,
                                  double dt, double hdt, double ox, double oy, double oz,
                                  const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig,
-                                 float4 *__restrict__ x32, float4 *__restrict__ v32) {
+                                 float4 *__restrict__ x32, float4 *__restrict__ v32, const uint8_t *__restrict__ hold) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    d3 vi = add(ld4(v, i), scl(hdt, ld4(a, i)));
-    d3 wi = add(ld4(w, i), scl(hdt, ld4(al, i)));
+    const uint32_t h = hold_of(hold, i);
+    d3 vi = kick_unless(ld4(v, i), hdt, ld4(a, i), h & LG_HOLD_V);
+    d3 wi = kick_unless(ld4(w, i), hdt, ld4(al, i), h & LG_HOLD_OMEGA);
     st4(v, i, vi);
     st4(w, i, wi);
-    d3 xn = add(ld4(x, i), scl(dt, vi));
-    st4(x, i, xn);
-    st4(th, i, add(ld4(th, i), scl(dt, wi)));
+    d3 xn = ld4(x, i);
+    if (!(h & LG_HOLD_X)) {
+        xn = add(xn, scl(dt, vi));
+        st4(x, i, xn);
+    }
+    if (!(h & LG_HOLD_THETA)) st4(th, i, add(ld4(th, i), scl(dt, wi)));
     rel_ff(xn, ox, oy, oz, agg, orig, i, n, x32);
     vel_ff(vi, wi, i, n, v32);
 }
@@ -419,12 +388,12 @@ void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w,
 
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
-                             float4 *v32, cudaStream_t st) {
+                             float4 *v32, const uint8_t *hold, cudaStream_t st) {
     const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
     kick_drift_mixed<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt, origin[0], origin[1],
-                                                           origin[2], agg, orig, x32, v32);
+                                                           origin[2], agg, orig, x32, v32, hold);
 }
 
 }  // namespace lg

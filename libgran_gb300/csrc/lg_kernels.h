@@ -45,8 +45,14 @@ void launch_forces_fp64(int T, const Params &P, const StateView &S, const PairVi
 int launch_forces_pairs_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
                              double *pres, double hdt, double dt, int move_facets, bool kick, cudaStream_t st);
 // With connectors (BV.cn non-null) the drift also carries the 5-connector model's connectors.
+// hold: per-particle LG_HOLD_* bits (null: none).
 void launch_kick_drift_fp64(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a,
-                            const dbl4 *al, double dt, double hdt, const BondView &BV, cudaStream_t st);
+                            const dbl4 *al, double dt, double hdt, const BondView &BV, const uint8_t *hold,
+                            cudaStream_t st);
+// Central body force (LG_BODY_CENTRAL) into ea / eal; centre: 3 doubles per system (agg: system of
+// each particle, null for one system); kam = k_a / mass.
+void launch_body_central(int64_t n, const dbl4 *x, const int32_t *agg, const double *centre, double kam, dbl4 *ea,
+                         dbl4 *eal, cudaStream_t st);
 // Rebuilds the Verlet rows into newv (springs carried from oldv). With r_near > 0 it also lists each
 // row's contact candidates (newv.near_*): slots within r_near or bonded; springs of the other slots
 // are not carried (those pairs are apart, so their springs reset).
@@ -103,7 +109,7 @@ void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w,
 // Kick + drift of the mixed path; also refreshes x32 and v32.
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
-                             float4 *v32, cudaStream_t st);
+                             float4 *v32, const uint8_t *hold, cudaStream_t st);
 
 // Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,

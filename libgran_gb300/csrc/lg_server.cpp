@@ -94,6 +94,8 @@ extern "C" int lg_server_create(const lg_system_desc *tmpl, int64_t budget_bytes
     if (!tmpl || !out) return lg_fail(LG_E_INVALID, "lg_server_create: null argument");
     if (budget_bytes <= 0) return lg_fail(LG_E_INVALID, "lg_server_create: budget must be positive");
     if (rebuild_every < 1) return lg_fail(LG_E_INVALID, "lg_server_create: rebuild_every must be >= 1");
+    if (tmpl->hold_mask || tmpl->unary_hook)
+        return lg_fail(LG_E_INVALID, "lg_server_create: a request template holds no per-particle mask or unary hook");
     if (!(dt > 0) || !std::isfinite(dt)) return lg_fail(LG_E_INVALID, "lg_server_create: dt must be positive");
     lg_server *s = new (std::nothrow) lg_server();
     if (!s) return lg_fail(LG_E_NOMEM, "lg_server_create: host allocation failed");

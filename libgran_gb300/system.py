@@ -109,6 +109,25 @@ class System:
     def set_force_kernel(self, variant):
         A.check(A.lib().lg_set_force_kernel(self.h, int(variant)), "lg_set_force_kernel")
 
+    def set_hold_mask(self, mask):
+        """Per-particle LG_HOLD_* bits of the increments the integrator skips (None: hold nothing)."""
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        if m is not None and m.shape != (self.n,):
+            raise ValueError("hold mask needs one byte per particle")
+        A.check(A.lib().lg_set_hold_mask(self.h, None if m is None else m.ctypes.data_as(C.POINTER(C.c_uint8))),
+                "lg_set_hold_mask")
+
+    def set_body_force(self, body):
+        """An lg_body_force (None removes it)."""
+        A.check(A.lib().lg_set_body_force(self.h, None if body is None else C.byref(body)), "lg_set_body_force")
+
+    def set_body_centre(self, centres):
+        """Centre of the central body force: 3 values, or 3 per system of a batch."""
+        c = np.ascontiguousarray(centres, dtype=np.float64).reshape(-1)
+        if c.size != 3 * (1 if self.sizes is None else len(self.sizes)):
+            raise ValueError("one centre (3 values) per system")
+        A.check(A.lib().lg_set_body_centre(self.h, _dp(c)), "lg_set_body_centre")
+
     def reset_acceleration_buffers(self):
         A.check(A.lib().lg_reset_acceleration_buffers(self.h), "lg_reset_acceleration_buffers")
 

@@ -20,6 +20,9 @@
  *   triangular_facet (closest point, fold, move)  surface_force/triangular_facet.h:18-137
  *   binary/unary functor container folds          granular_system/binary_force_container.h:20-32,
  *                                                 granular_system/unary_force_container.h:20-32
+ *                                                 (a right fold: f0 + (f1 + (... + fN)))
+ *   central_attraction_functor (body force)       Custom-unary-force-model.md:108-118
+ *   fixed_particle_step_handler (held increments) Custom-step-handler.md:82-97
  *   observables                                   test/compute_energy.cpp:7-58,
  *                                                 test/mass_distribution.cpp:7-27
  * The system loop and the rotational velocity-Verlet integrator live in libtimestep, which the
@@ -116,6 +119,8 @@ struct lgo_system {
     int64_t step_index;
     int64_t n_bonds_initial;
     int threads;
+    uint8_t *hold;        /* [n] LG_HOLD_* bits, or NULL */
+    double centre[3];     /* LG_BODY_CENTRAL centre */
 };
 
 /* ---------------------------------------------------------------------------------------------
@@ -601,9 +606,19 @@ static void eval_forces(lgo_system *s) {
             acc = add(acc, pa);
             accw = add(accw, pal);
         }
-        if (d->n_facets > 0) {
+        /* unary functors: the facets, then the body force, folded as the container folds them,
+         * f0 + (f1 + (... + body)) (unary_force_container.h:27-29) */
+        {
             v3 ua = ZERO, ual = ZERO;
-            for (int32_t f = 0; f < d->n_facets; ++f) {
+            int have = 0;
+            if (d->body.model == LG_BODY_CENTRAL) {
+                /* central_attraction_functor (Custom-unary-force-model.md:108-118) */
+                const double kam = d->body.k_a / d->body.mass;
+                ua = scl(kam, sub(mk(s->centre[0], s->centre[1], s->centre[2]), xi_));
+                ual = ZERO;
+                have = 1;
+            }
+            for (int32_t f = d->n_facets - 1; f >= 0; --f) {
                 const lg_facet_desc *fd = &s->facets[f];
                 v3 N = ld(s->facet_normal, f);
                 v3 xf = closest_point_on_triangle(fd->vertices, s->facet_area[f], N, xi_);
@@ -618,10 +633,12 @@ static void eval_forces(lgo_system *s) {
                     v3 ha = surface_hamaker(&fd->hamaker, xf, xi_);
                     if (hv) { fa = add(fa, ha); fal = add(fal, ZERO); } else { fa = ha; fal = ZERO; }
                 }
-                if (f == 0) { ua = fa; ual = fal; } else { ua = add(ua, fa); ual = add(ual, fal); }
+                if (have) { ua = add(fa, ua); ual = add(fal, ual); } else { ua = fa; ual = fal; have = 1; }
             }
-            acc = add(acc, ua);
-            accw = add(accw, ual);
+            if (have) {
+                acc = add(acc, ua);
+                accw = add(accw, ual);
+            }
         }
         stv(s->a, i, acc);
         stv(s->al, i, accw);
@@ -649,6 +666,13 @@ lgo_system *lgo_create(const lg_system_desc *d, const double *x0, const double *
     s->d = *d;
     s->n = d->n_part;
     s->threads = threads > 0 ? threads : 1;
+    s->d.hold_mask = NULL;
+    if (d->hold_mask) {
+        s->hold = (uint8_t *)malloc((size_t)(s->n > 0 ? s->n : 1));
+        memcpy(s->hold, d->hold_mask, (size_t)s->n);
+    }
+    if (d->body.model == LG_BODY_CENTRAL)
+        for (int c = 0; c < 3; ++c) s->centre[c] = d->body.centre[c];
     size_t bytes = sizeof(double) * 3 * (size_t)(s->n > 0 ? s->n : 1);
     s->x = (double *)malloc(bytes); s->v = (double *)malloc(bytes);
     s->th = (double *)malloc(bytes); s->om = (double *)malloc(bytes);
@@ -765,7 +789,7 @@ void lgo_destroy(lgo_system *s) {
     for (int64_t i = 0; i < s->n; ++i) { free(s->rows[i].e); free(s->rows[i].b); }
     free(s->rows);
     free(s->x); free(s->v); free(s->th); free(s->om); free(s->a); free(s->al);
-    free(s->facets); free(s->facet_area); free(s->facet_normal); free(s->surf_xi);
+    free(s->facets); free(s->facet_area); free(s->facet_normal); free(s->surf_xi); free(s->hold);
     free(s);
 }
 
@@ -787,41 +811,81 @@ int lgo_step(lgo_system *s, double dt, int64_t nsteps, int64_t rebuild_every) {
     for (int64_t st = 0; st < nsteps; ++st) {
         if (s->d.pairs == LG_PAIRS_VERLET && rebuild_every > 0 && (s->step_index % rebuild_every) == 0)
             build_rows(s, 1);
-        for (int64_t q = 0; q < 3 * n; ++q) {
-            s->v[q] += s->a[q] * hdt;
-            s->om[q] += s->al[q] * hdt;
+        /* half kick; a step handler's held increments are skipped (Custom-step-handler.md:82-97) */
+        for (int64_t i = 0; i < n; ++i) {
+            const unsigned h = s->hold ? s->hold[i] : 0u;
+            for (int c = 0; c < 3; ++c) {
+                if (!(h & LG_HOLD_V)) s->v[3 * i + c] += s->a[3 * i + c] * hdt;
+                if (!(h & LG_HOLD_OMEGA)) s->om[3 * i + c] += s->al[3 * i + c] * hdt;
+            }
         }
         if (s->d.binary_model == LG_BINARY_SINTER_CONNECTORS) {
             /* sinter_step_handler: increment_x moves the particle and its connectors by dx,
              * increment_theta turns the connectors by dtheta about the (moved) centre
-             * (sinter_bridge.h:24-42, 55-75) */
+             * (sinter_bridge.h:24-42, 55-75); a held increment skips the whole call */
             for (int64_t i = 0; i < n; ++i) {
-                v3 dx = mk(s->v[3 * i] * dt, s->v[3 * i + 1] * dt, s->v[3 * i + 2] * dt);
-                v3 xn = add(ld(s->x, i), dx);
-                stv(s->x, i, xn);
+                const unsigned h = s->hold ? s->hold[i] : 0u;
                 row *r = &s->rows[i];
-                for (int32_t q = 0; q < r->nb; ++q)
-                    for (int k = 0; k < 5; ++k) r->b[q].cn[k] = add(r->b[q].cn[k], dx);
-                v3 dth = mk(s->om[3 * i] * dt, s->om[3 * i + 1] * dt, s->om[3 * i + 2] * dt);
-                stv(s->th, i, add(ld(s->th, i), dth));
-                for (int32_t q = 0; q < r->nb; ++q)
-                    for (int k = 0; k < 5; ++k) r->b[q].cn[k] = add(r->b[q].cn[k], crs(dth, sub(r->b[q].cn[k], xn)));
+                v3 xn = ld(s->x, i);
+                if (!(h & LG_HOLD_X)) {
+                    v3 dx = mk(s->v[3 * i] * dt, s->v[3 * i + 1] * dt, s->v[3 * i + 2] * dt);
+                    xn = add(xn, dx);
+                    stv(s->x, i, xn);
+                    for (int32_t q = 0; q < r->nb; ++q)
+                        for (int k = 0; k < 5; ++k) r->b[q].cn[k] = add(r->b[q].cn[k], dx);
+                }
+                if (!(h & LG_HOLD_THETA)) {
+                    v3 dth = mk(s->om[3 * i] * dt, s->om[3 * i + 1] * dt, s->om[3 * i + 2] * dt);
+                    stv(s->th, i, add(ld(s->th, i), dth));
+                    for (int32_t q = 0; q < r->nb; ++q)
+                        for (int k = 0; k < 5; ++k) r->b[q].cn[k] = add(r->b[q].cn[k], crs(dth, sub(r->b[q].cn[k], xn)));
+                }
             }
         } else {
-            for (int64_t q = 0; q < 3 * n; ++q) {
-                s->x[q] += s->v[q] * dt;
-                s->th[q] += s->om[q] * dt;
+            for (int64_t i = 0; i < n; ++i) {
+                const unsigned h = s->hold ? s->hold[i] : 0u;
+                for (int c = 0; c < 3; ++c) {
+                    if (!(h & LG_HOLD_X)) s->x[3 * i + c] += s->v[3 * i + c] * dt;
+                    if (!(h & LG_HOLD_THETA)) s->th[3 * i + c] += s->om[3 * i + c] * dt;
+                }
             }
         }
         eval_forces(s);
-        for (int64_t q = 0; q < 3 * n; ++q) {
-            s->v[q] += s->a[q] * hdt;
-            s->om[q] += s->al[q] * hdt;
+        for (int64_t i = 0; i < n; ++i) {
+            const unsigned h = s->hold ? s->hold[i] : 0u;
+            for (int c = 0; c < 3; ++c) {
+                if (!(h & LG_HOLD_V)) s->v[3 * i + c] += s->a[3 * i + c] * hdt;
+                if (!(h & LG_HOLD_OMEGA)) s->om[3 * i + c] += s->al[3 * i + c] * hdt;
+            }
         }
         if (s->d.facet_auto_move)
             for (int32_t f = 0; f < s->d.n_facets; ++f) facet_move(s, f, dt);
         s->step_index++;
     }
+    return 0;
+}
+
+int lgo_set_hold_mask(lgo_system *s, const uint8_t *mask) {
+    free(s->hold);
+    s->hold = NULL;
+    if (mask) {
+        s->hold = (uint8_t *)malloc((size_t)(s->n > 0 ? s->n : 1));
+        memcpy(s->hold, mask, (size_t)s->n);
+    }
+    return 0;
+}
+
+int lgo_set_body_force(lgo_system *s, const lg_body_force *f) {
+    lg_body_force none;
+    memset(&none, 0, sizeof(none));
+    s->d.body = f ? *f : none;
+    if (f && f->model == LG_BODY_CENTRAL)
+        for (int c = 0; c < 3; ++c) s->centre[c] = f->centre[c];
+    return 0;
+}
+
+int lgo_set_body_centre(lgo_system *s, const double *c) {
+    for (int k = 0; k < 3; ++k) s->centre[k] = c[k];
     return 0;
 }
 

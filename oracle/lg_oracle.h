@@ -34,6 +34,10 @@ int lgo_observables(lgo_system *s, lg_observables *o);
 int lgo_facet_update_positions(lgo_system *s, int32_t facet, double dt);
 int lgo_facet_get_vertices(lgo_system *s, int32_t facet, double *out9);
 int64_t lgo_step_index(lgo_system *s);
+/* Step-handler hold mask (n bytes of LG_HOLD_* bits; NULL: none), body force, body-force centre. */
+int lgo_set_hold_mask(lgo_system *s, const uint8_t *mask);
+int lgo_set_body_force(lgo_system *s, const lg_body_force *f);
+int lgo_set_body_centre(lgo_system *s, const double *centre);
 int lgo_run_many(lgo_system **systems, const double *dts, const int64_t *nsteps, const int64_t *rebuild,
                  int count);
 

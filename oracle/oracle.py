@@ -75,6 +75,9 @@ def olib():
         L.lgo_step_index.restype = i64
         L.lgo_step_index.argtypes = [vp]
         L.lgo_run_many.argtypes = [P(vp), P(d), P(i64), P(i64), C.c_int]
+        L.lgo_set_hold_mask.argtypes = [vp, P(C.c_uint8)]
+        L.lgo_set_body_force.argtypes = [vp, P(A.lg_body_force)]
+        L.lgo_set_body_centre.argtypes = [vp, P(d)]
         _olib = L
     return _olib
 
@@ -100,6 +103,7 @@ def rlib():
         L.lgref_bonds.argtypes = [vp, P(i64), i64]
         L.lgref_facet_get_vertices.argtypes = [vp, C.c_int32, P(d)]
         L.lgref_facet_update_positions.argtypes = [vp, C.c_int32, d]
+        L.lgref_set_body_centre.argtypes = [vp, P(d)]
         _rlib = L
     return _rlib
 
@@ -185,6 +189,16 @@ class OracleSystem:
     def facet_update_positions(self, f, dt):
         olib().lgo_facet_update_positions(self.h, f, dt)
 
+    def set_hold_mask(self, mask):
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        olib().lgo_set_hold_mask(self.h, None if m is None else m.ctypes.data_as(C.POINTER(C.c_uint8)))
+
+    def set_body_force(self, body):
+        olib().lgo_set_body_force(self.h, None if body is None else C.byref(body))
+
+    def set_body_centre(self, c):
+        olib().lgo_set_body_centre(self.h, _dp(np.ascontiguousarray(c, dtype=np.float64)))
+
 
 def run_many(systems, dts, nsteps, rebuild):
     """Step several oracle systems concurrently (one thread each)."""
@@ -245,3 +259,7 @@ class RefHarnessSystem:
         out = np.zeros(9)
         rlib().lgref_facet_get_vertices(self.h, f, _dp(out))
         return out
+
+    def set_body_centre(self, c):
+        if rlib().lgref_set_body_centre(self.h, _dp(np.ascontiguousarray(c, dtype=np.float64))) != 0:
+            raise RuntimeError("no central body force in this harness system")

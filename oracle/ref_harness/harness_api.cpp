@@ -46,6 +46,13 @@ int lgref_get(void *h, int field, double *out) {
     return 0;
 }
 
+int lgref_set_body_centre(void *h, const double *c) {
+    RefSys *s = (RefSys *)h;
+    if (!s->set_centre) return -1;
+    s->set_centre(c);
+    return 0;
+}
+
 int lgref_pair_springs(void *h, int64_t i, int64_t j, double *out9) {
     ((RefSys *)h)->springs((size_t)i, (size_t)j, out9);
     return 0;

@@ -80,6 +80,44 @@ BinFn bin_of(RefSys *s, std::shared_ptr<F>... f) {
     };
 }
 
+// The tutorial's central_attraction_functor (Custom-unary-force-model.md:108-118): a user-defined
+// unary functor, restated here because it exists only as documentation; the container folds it
+// after the facets.
+struct central_attraction {
+    double k_a, mass;
+    V x0;
+    std::pair<V, V> operator()(size_t i, Field const &x, Field const &, Field const &, Field const &, double) const {
+        V a = k_a / mass * (x0 - x[i]);
+        return std::make_pair(a, V::Zero());
+    }
+};
+
+template <size_t> using FacetAt = FacetT;
+
+// libgran's unary container over the facets (in order) and, when `body` is set, the central
+// functor after them.
+template <size_t... I>
+UnFn unary_of(RefSys *s, std::vector<std::shared_ptr<FacetT>> &fs, std::shared_ptr<central_attraction> body,
+              std::index_sequence<I...>) {
+    if (body) {
+        auto c = std::make_shared<unary_force_functor_container<V, double, FacetAt<I>..., central_attraction>>(*fs[I]...,
+                                                                                                             *body);
+        s->keep.push_back(c);
+        return [c](size_t i, Field const &x, Field const &v, Field const &th, Field const &om, double t) {
+            return (*c)(i, x, v, th, om, t);
+        };
+    }
+    if constexpr (sizeof...(I) == 0) {
+        return UnFn();
+    } else {
+        auto c = std::make_shared<unary_force_functor_container<V, double, FacetAt<I>...>>(*fs[I]...);
+        s->keep.push_back(c);
+        return [c](size_t i, Field const &x, Field const &v, Field const &th, Field const &om, double t) {
+            return (*c)(i, x, v, th, om, t);
+        };
+    }
+}
+
 void fill9(double *out, std::tuple<V, V, V> const &t) {
     V a = std::get<0>(t), b = std::get<1>(t), c = std::get<2>(t);
     for (int k = 0; k < 3; ++k) { out[k] = a[k]; out[3 + k] = b[k]; out[6 + k] = c[k]; }
@@ -230,18 +268,24 @@ RefSys *FACTORY(const lg_system_desc *d, const double *x0, const double *v0, con
             for (int k = 0; k < 3; ++k) { out[k] = a[k]; out[3 + k] = b[k]; out[6 + k] = c[k]; }
         });
     }
-    if (fs.size() == 1) {
-        auto c = std::make_shared<unary_force_functor_container<V, double, FacetT>>(*fs[0]);
-        s->keep.push_back(c);
-        s->un = [c](size_t i, Field const &x, Field const &v, Field const &th, Field const &om, double t) { return (*c)(i, x, v, th, om, t); };
-    } else if (fs.size() == 2) {
-        auto c = std::make_shared<unary_force_functor_container<V, double, FacetT, FacetT>>(*fs[0], *fs[1]);
-        s->keep.push_back(c);
-        s->un = [c](size_t i, Field const &x, Field const &v, Field const &th, Field const &om, double t) { return (*c)(i, x, v, th, om, t); };
-    } else if (fs.size() > 2) {
-        delete s;
-        return nullptr;
+    std::shared_ptr<central_attraction> body;
+    if (d->body.model == LG_BODY_CENTRAL) {
+        body = std::make_shared<central_attraction>();
+        body->k_a = d->body.k_a;
+        body->mass = d->body.mass;
+        body->x0 = V(d->body.centre[0], d->body.centre[1], d->body.centre[2]);
+        s->keep.push_back(body);
+        s->set_centre = [body](const double *c) { body->x0 = V(c[0], c[1], c[2]); };
     }
+    switch (fs.size()) {
+        case 0: s->un = unary_of(s, fs, body, std::make_index_sequence<0>()); break;
+        case 1: s->un = unary_of(s, fs, body, std::make_index_sequence<1>()); break;
+        case 2: s->un = unary_of(s, fs, body, std::make_index_sequence<2>()); break;
+        case 3: s->un = unary_of(s, fs, body, std::make_index_sequence<3>()); break;
+        case 4: s->un = unary_of(s, fs, body, std::make_index_sequence<4>()); break;
+        default: delete s; return nullptr;
+    }
+    if (d->hold_mask) s->hold.assign(d->hold_mask, d->hold_mask + n);
     s->build_rows();
     s->forces();
     return s;

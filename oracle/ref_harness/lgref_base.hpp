@@ -34,6 +34,10 @@ struct RefSys {
     // step handler increments of the drift (sinter_step_handler of the 5-connector model); empty:
     // plain x += v*dt, theta += omega*dt
     std::function<void(size_t, V const &)> inc_x, inc_theta;
+    // a custom step handler that holds increments (Custom-step-handler.md:82-97): LG_HOLD_* bits per
+    // particle; a held increment is not passed on to the base handler
+    std::vector<uint8_t> hold;
+    std::function<void(const double *)> set_centre;  // central body force: the tutorial's update
     int64_t step_index = 0;
     double t = 0.0;
 
@@ -64,19 +68,30 @@ struct RefSys {
             al[i] = acc.second;
         }
     }
+    unsigned held(size_t i) const { return hold.empty() ? 0u : hold[i]; }
+    void kick(double hdt) {
+        for (size_t i = 0; i < x.size(); ++i) {
+            if (!(held(i) & LG_HOLD_V)) v[i] += a[i] * hdt;
+            if (!(held(i) & LG_HOLD_OMEGA)) om[i] += al[i] * hdt;
+        }
+    }
     void step(double dt, int64_t nsteps, int64_t rebuild_every) {
         size_t n = x.size();
         double hdt = dt / 2.0;
         for (int64_t s = 0; s < nsteps; ++s) {
             if (verlet && rebuild_every > 0 && step_index % rebuild_every == 0) build_rows();
-            for (size_t i = 0; i < n; ++i) { v[i] += a[i] * hdt; om[i] += al[i] * hdt; }
-            if (inc_x) {
-                for (size_t i = 0; i < n; ++i) { inc_x(i, v[i] * dt); inc_theta(i, om[i] * dt); }
-            } else {
-                for (size_t i = 0; i < n; ++i) { x[i] += v[i] * dt; th[i] += om[i] * dt; }
+            kick(hdt);
+            for (size_t i = 0; i < n; ++i) {
+                const unsigned h = held(i);
+                if (!(h & LG_HOLD_X)) {
+                    if (inc_x) inc_x(i, v[i] * dt); else x[i] += v[i] * dt;
+                }
+                if (!(h & LG_HOLD_THETA)) {
+                    if (inc_theta) inc_theta(i, om[i] * dt); else th[i] += om[i] * dt;
+                }
             }
             forces();
-            for (size_t i = 0; i < n; ++i) { v[i] += a[i] * hdt; om[i] += al[i] * hdt; }
+            kick(hdt);
             if (facet_auto_move)
                 for (auto &mv : facet_move) mv(dt);
             ++step_index;

@@ -27,6 +27,14 @@ def _bond_count(desc, x0):
     return int((np.abs(d[iu] - 2.0 * r) < dc).sum())
 
 
+def centroid_seq(x):
+    """Centroid as the tutorial's update_center_of_mass forms it: sum in index order, then / count."""
+    c = np.zeros(3)
+    for p in x:
+        c = c + p
+    return c / float(len(x))
+
+
 def cases():
     out = []
     # 1. plate + projectile, contact + full Hamaker (test/hamaker.cpp set-up), short run
@@ -85,4 +93,42 @@ def cases():
     K.set_connectors(d, 0.5 * mat.k_n, 0.5 * mat.g_n, mat.d_crit, K.random_unit_axes(nb, 13))
     out.append(dict(name="rsa40_connectors_limited", desc=d, x0=x0, v0=v0, dt=mat.dt, checkpoints=[0, 1, 10, 300],
                     spring_pairs=[(0, 1), (1, 0), (0, 2)]))
+    # 10. the custom step-handler tutorial set-up (Custom-step-handler.md: contact + Hamaker with
+    #     A = 1e-19, the central attraction body force k_a = 8e-6 towards the initial centroid, the
+    #     velocity of particle 10 held) on a seeded RSA aggregate of 60 monomers
+    c = KA.contact_case()
+    x0 = generate_aggregate(14, 60, KA.R)
+    d = K.make_desc(60, A.LG_BINARY_CONTACT, A.LG_HAMAKER_FULL, contact=c["desc"].contact,
+                    hamaker=K.hamaker_params(1.0e-19, 1.0e-9, KA.R, KA.MASS))
+    d.body = K.central_body(8.0e-6, KA.MASS, centroid_seq(x0))
+    hold = np.zeros(60, dtype=np.uint8)
+    hold[10] = A.LG_HOLD_V
+    K.set_hold(d, hold)
+    out.append(dict(name="tutorial_central_fixed", desc=d, x0=x0, v0=generate_velocities(14, 60, 0.05), dt=c["dt"],
+                    checkpoints=[0, 1, 10, 400], spring_pairs=[(0, 1), (10, 11)]))
+    # 11. three facets (a floor of two triangles and a tilted wall), a central body force after them,
+    #     and held increments (x of one particle, theta of another, v and omega of a third): the unary container's
+    #     right fold f0 + (f1 + (f2 + body))
+    x0 = generate_aggregate(15, 24, KA.R) + np.array([0.0, 0.0, 9.0 * KA.R])
+    x0[:, 2] -= x0[:, 2].min() - 0.995 * KA.R  # the lowest monomer starts touching the floor
+    v0 = generate_velocities(15, 24, 0.2) + np.array([0.3, -0.2, -1.0])
+    fl = []
+    a_ = 40.0 * KA.R
+    for verts in ([(-a_, -a_, 0.0), (a_, -a_, 0.0), (-a_, a_, 0.0)], [(a_, a_, 0.0), (-a_, a_, 0.0), (a_, -a_, 0.0)],
+                  [(6.0 * KA.R, -a_, -a_), (6.0 * KA.R, a_, -a_), (4.0 * KA.R, -a_, a_)]):
+        f = KA.surface_facet(c["dt"], A_h=2.0e-20, h0=1.0e-9, mu=0.5)
+        for k, v in enumerate(verts):
+            for q in range(3):
+                f.vertices[3 * k + q] = v[q]
+        fl.append(f)
+    d = K.make_desc(24, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, contact=c["desc"].contact,
+                    hamaker=K.hamaker_params(1.0e-20, 1.0e-9, KA.R, KA.MASS, r_cutoff=4.0 * KA.R), n_facets=3)
+    d.body = K.central_body(2.0e-6, KA.MASS, x0.mean(0) + np.array([0.0, 0.0, 3.0 * KA.R]))
+    hold = np.zeros(24, dtype=np.uint8)
+    hold[3] = A.LG_HOLD_X
+    hold[7] = A.LG_HOLD_THETA
+    hold[12] = A.LG_HOLD_OMEGA | A.LG_HOLD_V
+    K.set_hold(d, hold)
+    out.append(dict(name="three_facets_body_hold", desc=d, x0=x0, v0=v0, dt=c["dt"], checkpoints=[0, 1, 10, 600],
+                    facets=fl, spring_pairs=[(0, 1)]))
     return out

@@ -90,6 +90,52 @@ def test_oracle_matches_reference_harness_connectors(hm, verlet):
     assert np.array_equal(orc.bonds(), ref.bonds())
 
 
+@pytest.mark.parametrize("hold_bits", [A.LG_HOLD_V, A.LG_HOLD_X, A.LG_HOLD_THETA | A.LG_HOLD_OMEGA,
+                                       A.LG_HOLD_X | A.LG_HOLD_THETA])
+def test_oracle_matches_reference_harness_with_held_connectors(hold_bits):
+    """Held increments with the 5-connector model: a held x or theta also leaves the particle's
+    connectors where they are (the skipped call is sinter_step_handler's)."""
+    _harness_or_skip()
+    mat = K.Material()
+    n = 30
+    x0 = generate_aggregate(77, n, mat.r)
+    v0 = generate_velocities(77, n, 0.5) - 1.5e7 * (x0 - x0.mean(0))
+    d = K.make_desc(n, A.LG_BINARY_SINTER_CONNECTORS, A.LG_HAMAKER_LIMITED, contact=mat.contact(),
+                    hamaker=mat.hamaker())
+    K.set_connectors(d, 0.5 * mat.k_n, 0.3 * mat.g_n, mat.d_crit,
+                     K.random_unit_axes(len(K.connector_bonds(x0, mat.r, mat.d_crit)), 8))
+    hold = np.zeros(n, dtype=np.uint8)
+    hold[[0, 5, 17]] = hold_bits
+    K.set_hold(d, hold)
+    ref = O.RefHarnessSystem(d, x0, v0)
+    orc = O.OracleSystem(d, x0, v0)
+    ref.step(mat.dt, 120)
+    orc.step(mat.dt, 120)
+    for f in H.FIELDS:
+        assert np.array_equal(orc.get(f), ref.get(f)), H.FIELD_NAMES[f]
+    if hold_bits & A.LG_HOLD_X:
+        assert np.array_equal(orc.get(A.LG_FIELD_X)[[0, 5, 17]], x0[[0, 5, 17]])
+    if hold_bits & A.LG_HOLD_V:
+        assert np.array_equal(orc.get(A.LG_FIELD_V)[[0, 5, 17]], v0[[0, 5, 17]])
+
+
+def test_body_centre_update_matches_reference_harness():
+    """The tutorial's update_center_of_mass between steps: the central body force follows the
+    centre it is given (here the current centroid, recomputed every 10 steps)."""
+    _harness_or_skip()
+    c = [c for c in __import__("golden_cases").cases() if c["name"] == "tutorial_central_fixed"][0]
+    ref = O.RefHarnessSystem(c["desc"], c["x0"], c["v0"])
+    orc = O.OracleSystem(c["desc"], c["x0"], c["v0"])
+    for _ in range(6):
+        ref.step(c["dt"], 10)
+        orc.step(c["dt"], 10)
+        centre = np.sum(orc.get(A.LG_FIELD_X), axis=0) / c["desc"].n_part
+        ref.set_body_centre(centre)
+        orc.set_body_centre(centre)
+    for f in H.FIELDS:
+        assert np.array_equal(orc.get(f), ref.get(f)), H.FIELD_NAMES[f]
+
+
 def test_connector_axes_are_required_and_checked():
     mat = K.Material()
     x0 = generate_aggregate(3, 20, mat.r)
