@@ -324,6 +324,34 @@ int lg_set_body_centre(lg_system *sys, const double *centres);
 /* Replace the unary hook (hook NULL removes it), from the next force evaluation on. */
 int lg_set_unary_hook(lg_system *sys, lg_unary_hook hook, void *user);
 
+/* ---- state dumps (libgran's writer.cpp formats) ------------------------------------------- */
+
+/* ASCII VTK files as libgran's writer writes them (writer.cpp:13-170): coordinates divided by
+ * r_part, numbers as std::ostream prints doubles by default ("%.6g"), the same headers and
+ * separators. lg_write_* take the handle's current state; lg_format_* take host arrays and need no
+ * GPU. Output goes to `path` (libgran's writer numbers files in a directory itself; the drop-in
+ * writer.h keeps that naming).
+ *   particles:  write_particles (writer.cpp:51-118): points, and the fields thetax/thetay/thetaz
+ *               (the rotated unit axes of AngleAxis(theta_x, X) AngleAxis(theta_y, Y)
+ *               AngleAxis(theta_z, Z)); theta: 3n doubles
+ *   necks:      write_necks (writer.cpp:120-170): midpoint and unit normal (x_i - x_j) of every
+ *               intact bond i < j in (i, j) order; pairs: n_pairs (i, j) int64 pairs
+ *   connectors: write_spring_connectors (writer.cpp:13-49): the 5 connector points of every bond
+ *               end, particle i ascending, then partner j ascending (5-connector model)
+ *   csv:        the tutorials' dump_particle_positions: "x, y, z" then one line per particle. */
+int lg_write_vtk_particles(lg_system *sys, const char *path, double r_part);
+int lg_write_vtk_necks(lg_system *sys, const char *path, double r_part);
+int lg_write_vtk_connectors(lg_system *sys, const char *path, double r_part);
+int lg_write_csv_positions(lg_system *sys, const char *path, double r_part);
+int lg_format_vtk_particles(const double *x, const double *theta, int64_t n, double r_part, const char *path);
+int lg_format_vtk_necks(const double *x, int64_t n, const int64_t *pairs, int64_t n_pairs, double r_part,
+                        const char *path);
+int lg_format_vtk_connectors(const double *points, int64_t n_points, double r_part, const char *path);
+int lg_format_csv_positions(const double *x, int64_t n, double r_part, const char *path);
+/* Connector points of the 5-connector model in the order of lg_write_vtk_connectors (3 doubles
+ * each, 5 per bond end); n_points is set to the total; out may be NULL. */
+int lg_get_connectors(lg_system *sys, int64_t *n_points, double *out, int64_t capacity);
+
 /* Number of CUDA kernel launches issued by this handle since creation (diagnostics). */
 int lg_get_launch_count(lg_system *sys, int64_t *count);
 

@@ -181,6 +181,15 @@ def _declare(L):
         "lg_set_body_force": (C.c_int, [vp, P(lg_body_force)]),
         "lg_set_body_centre": (C.c_int, [vp, P(d)]),
         "lg_set_unary_hook": (C.c_int, [vp, lg_unary_hook, vp]),
+        "lg_write_vtk_particles": (C.c_int, [vp, C.c_char_p, d]),
+        "lg_write_vtk_necks": (C.c_int, [vp, C.c_char_p, d]),
+        "lg_write_vtk_connectors": (C.c_int, [vp, C.c_char_p, d]),
+        "lg_write_csv_positions": (C.c_int, [vp, C.c_char_p, d]),
+        "lg_format_vtk_particles": (C.c_int, [P(d), P(d), i64, d, C.c_char_p]),
+        "lg_format_vtk_necks": (C.c_int, [P(d), i64, P(i64), i64, d, C.c_char_p]),
+        "lg_format_vtk_connectors": (C.c_int, [P(d), i64, d, C.c_char_p]),
+        "lg_format_csv_positions": (C.c_int, [P(d), i64, d, C.c_char_p]),
+        "lg_get_connectors": (C.c_int, [vp, P(i64), P(d), i64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

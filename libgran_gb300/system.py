@@ -128,6 +128,21 @@ class System:
             raise ValueError("one centre (3 values) per system")
         A.check(A.lib().lg_set_body_centre(self.h, _dp(c)), "lg_set_body_centre")
 
+    def write_vtk(self, kind, path, r_part):
+        """Dump the current state in libgran's writer format: kind "particles", "necks",
+        "connectors", or "csv" (the tutorials' position dump)."""
+        fn = {"particles": "lg_write_vtk_particles", "necks": "lg_write_vtk_necks",
+              "connectors": "lg_write_vtk_connectors", "csv": "lg_write_csv_positions"}[kind]
+        A.check(getattr(A.lib(), fn)(self.h, str(path).encode(), float(r_part)), fn)
+
+    def connectors(self):
+        """Connector points of the 5-connector model (bond ends by particle, then partner; 5 each)."""
+        k = C.c_int64()
+        A.check(A.lib().lg_get_connectors(self.h, C.byref(k), None, 0), "lg_get_connectors")
+        out = np.zeros((max(k.value, 1), 3))
+        A.check(A.lib().lg_get_connectors(self.h, C.byref(k), _dp(out), k.value), "lg_get_connectors")
+        return out[:k.value]
+
     def reset_acceleration_buffers(self):
         A.check(A.lib().lg_reset_acceleration_buffers(self.h), "lg_reset_acceleration_buffers")
 

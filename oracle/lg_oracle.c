@@ -865,6 +865,31 @@ int lgo_step(lgo_system *s, double dt, int64_t nsteps, int64_t rebuild_every) {
     return 0;
 }
 
+/* Connector points of every bond end: particle i ascending, partner j ascending, 5 points each
+ * (spring_connectors[i * n + j] of sinter_bridge.h:139). Returns the number of points. */
+int64_t lgo_get_connectors(lgo_system *s, double *out, int64_t cap) {
+    int64_t k = 0;
+    if (s->d.binary_model != LG_BINARY_SINTER_CONNECTORS) return 0;
+    for (int64_t i = 0; i < s->n; ++i) {
+        row *r = &s->rows[i];
+        int32_t order[256];
+        int32_t m = r->nb < 256 ? r->nb : 256;
+        for (int32_t q = 0; q < m; ++q) order[q] = q;
+        for (int32_t a = 1; a < m; ++a) /* insertion sort by partner */
+            for (int32_t b = a; b > 0 && r->b[order[b]].j < r->b[order[b - 1]].j; --b) {
+                int32_t t = order[b]; order[b] = order[b - 1]; order[b - 1] = t;
+            }
+        for (int32_t q = 0; q < m; ++q)
+            for (int c = 0; c < 5; ++c, ++k)
+                if (out && k < cap) {
+                    out[3 * k] = r->b[order[q]].cn[c].x;
+                    out[3 * k + 1] = r->b[order[q]].cn[c].y;
+                    out[3 * k + 2] = r->b[order[q]].cn[c].z;
+                }
+    }
+    return k;
+}
+
 int lgo_set_hold_mask(lgo_system *s, const uint8_t *mask) {
     free(s->hold);
     s->hold = NULL;

@@ -38,6 +38,7 @@ int64_t lgo_step_index(lgo_system *s);
 int lgo_set_hold_mask(lgo_system *s, const uint8_t *mask);
 int lgo_set_body_force(lgo_system *s, const lg_body_force *f);
 int lgo_set_body_centre(lgo_system *s, const double *centre);
+int64_t lgo_get_connectors(lgo_system *s, double *out, int64_t cap);
 int lgo_run_many(lgo_system **systems, const double *dts, const int64_t *nsteps, const int64_t *rebuild,
                  int count);
 

@@ -78,6 +78,8 @@ def olib():
         L.lgo_set_hold_mask.argtypes = [vp, P(C.c_uint8)]
         L.lgo_set_body_force.argtypes = [vp, P(A.lg_body_force)]
         L.lgo_set_body_centre.argtypes = [vp, P(d)]
+        L.lgo_get_connectors.restype = i64
+        L.lgo_get_connectors.argtypes = [vp, P(d), i64]
         _olib = L
     return _olib
 
@@ -198,6 +200,13 @@ class OracleSystem:
 
     def set_body_centre(self, c):
         olib().lgo_set_body_centre(self.h, _dp(np.ascontiguousarray(c, dtype=np.float64)))
+
+    def connectors(self):
+        L = olib()
+        k = L.lgo_get_connectors(self.h, None, 0)
+        out = np.zeros((max(k, 1), 3))
+        L.lgo_get_connectors(self.h, _dp(out), k)
+        return out[:k]
 
 
 def run_many(systems, dts, nsteps, rebuild):
