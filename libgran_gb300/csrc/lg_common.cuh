@@ -82,6 +82,18 @@ __device__ __forceinline__ void vel_ff(d3 v, d3 w, int64_t i, int64_t n, float4 
     v32[2 * n + i] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.0f);
 }
 
+// The float-float state of particle i after an FP64 update: vel_ff's copies plus, in s32, the low
+// FP32 parts of omega_i, and zero for the displacement and rotation accumulated since (s32[n..5n)).
+__device__ __forceinline__ void state_ff(d3 v, d3 w, int64_t i, int64_t n, float4 *__restrict__ v32,
+                                         float4 *__restrict__ s32) {
+    vel_ff(v, w, i, n, v32);
+    if (!s32) return;
+    s32[i] = make_float4((float)(w.x - (double)(float)w.x), (float)(w.y - (double)(float)w.y),
+                         (float)(w.z - (double)(float)w.z), 0.0f);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int q = 1; q < 5; ++q) s32[q * n + i] = z;
+}
+
 // A spring component in either storage form.
 __device__ __forceinline__ double spring_load(const double *p, int64_t idx, bool ff) {
     return ff ? ffslot_load(p, idx) : p[idx];

@@ -312,7 +312,7 @@ static int refresh_mixed_copies(lg_system *s, const double *x) {
     const int64_t n = s->P.n;
     int32_t *flag = x ? s->d_flag : nullptr;
     if (flag) LG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int32_t), s->stream));
-    launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32, s->v32,
+    launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->th, s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->s32,
                         s->stream, flag);
     s->launches += 1;
     LG_CUDA(cudaGetLastError());
@@ -324,7 +324,7 @@ static int refresh_mixed_copies(lg_system *s, const double *x) {
     LG_TRY(set_mixed_origins(s, x));  // positions moved far: new origins and culling radii
     set_cull_radii(s);
     s->drop_graphs();
-    launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32, s->v32,
+    launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->th, s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->s32,
                         s->stream);
     s->launches += 1;
     LG_CUDA(cudaGetLastError());
@@ -445,7 +445,8 @@ static StateView state_view(lg_system *s, bool half_step_inputs) {
     return S;
 }
 
-static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, bool fuse_kick = false) {
+static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, bool fuse_kick = false,
+                         bool prev_fused = false) {
     StateView S = state_view(s, true);
     cudaEvent_t stop_ev = nullptr;
     if (s->timing) {
@@ -484,7 +485,7 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
     if (s->precision == LG_PRECISION_MIXED) {
         if (compact)
             kernels = launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, fuse_kick,
-                                                  s->mx, s->stream, s->side, s->fork_ev, s->join_ev);
+                                                  prev_fused, s->mx, s->stream, s->side, s->fork_ev, s->join_ev);
         else
             launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
     } else {
@@ -509,10 +510,11 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_n
     if (s->P.pairs == LG_PAIRS_VERLET && rebuild_every > 0 && (s->step_index % rebuild_every) == 0)
         LG_TRY(rebuild_list(s));
     const double hdt = dt / 2.0;
+    const bool prev_fused = s->kick_done;
     if (!s->kick_done) {
         if (s->precision == LG_PRECISION_MIXED)
             launch_kick_drift_mixed(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt,
-                                    s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->P.hold, s->stream);
+                                    s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->s32, s->P.hold, s->stream);
         else
             launch_kick_drift_fp64(s->P.n, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->a, s->al, dt, hdt, s->bv, s->P.hold,
                                    s->stream);
@@ -521,7 +523,7 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_n
     const int mv = (s->facet_auto_move && s->P.n_facets > 0) ? 1 : 0;
     const bool fuse = fuse_next && ((s->precision == LG_PRECISION_MIXED && s->kernel == LG_FORCE_KERNEL_COMPACT) ||
                                     (s->precision == LG_PRECISION_FP64 && s->kernel == LG_FORCE_KERNEL_PAIRS));
-    LG_TRY(launch_forces(s, hdt, dt, mv, fuse));
+    LG_TRY(launch_forces(s, hdt, dt, mv, fuse, prev_fused));
     s->kick_done = fuse;
     s->vcur = 1 - s->vcur;
     if (mv) s->fcur = 1 - s->fcur;
@@ -980,6 +982,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     if (s->precision == LG_PRECISION_MIXED) {
         LG_TRY(s->alloc(&s->x32, 2 * (size_t)n));  // float-float: high parts, then low parts
         LG_TRY(s->alloc(&s->v32, 3 * (size_t)n));  // v high parts, v low parts, spins
+        LG_TRY(s->alloc(&s->s32, 5 * (size_t)n));  // spin low parts, displacement and rotation of a run
         LG_TRY(s->alloc(&s->csum, 3 * (size_t)n));
         LG_TRY(s->alloc(&s->d_flag, 1));
         LG_TRY(s->alloc(&s->hsum, 2 * (size_t)n));
@@ -989,7 +992,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         if (s->n_systems > 0) LG_TRY(s->alloc(&s->d_orig, (size_t)s->n_systems));
         s->r_max = std::max(d->contact.r_part, std::max(d->sinter.r_part, d->hamaker.r_part));
         LG_TRY(set_mixed_origins(s, x0));
-        launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->origin, s->d_agg, s->d_orig, s->x32, s->v32,
+        launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->th, s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->s32,
                             s->stream);
         double near = 0.0;
         if (d->binary_model != LG_BINARY_NONE) near = std::max(near, 2.0 * d->contact.r_part);
@@ -1000,6 +1003,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         s->mx.x32 = s->x32;
         s->mx.x32lo = s->x32 + n;
         s->mx.v32 = s->v32;
+        s->mx.s32 = s->s32;
         s->mx.csum = s->csum;
         s->mx.hsum = s->hsum;
         double cnear = 0.0;
@@ -1637,6 +1641,7 @@ static int snapshot_take(lg_system *s) {
         addb(s->err, sizeof(int32_t));
         if (s->x32) addb(s->x32, sizeof(float4) * 2 * n);
         if (s->v32) addb(s->v32, sizeof(float4) * 3 * n);
+        if (s->s32) addb(s->s32, sizeof(float4) * 5 * n);
         const int npv = s->P.pairs == LG_PAIRS_VERLET ? 2 : 1;
         for (int q = 0; q < npv; ++q) {
             PairView &pv = s->pv[q];

@@ -46,6 +46,7 @@ struct lg_system {
     // mixed precision: FP32 position copy for culling
     float4 *x32 = nullptr;  // mixed: [2n] float-float positions
     float4 *v32 = nullptr;  // mixed: [3n] float-float velocities, FP32 spins
+    float4 *s32 = nullptr;  // mixed: [5n] spin low parts, a run's displacement and rotation (float-float)
     float4 *csum = nullptr;    // mixed: [3n] contact sums (float-float)
     float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
     int32_t *d_flag = nullptr;  // mixed: device flag of the float-float copy check

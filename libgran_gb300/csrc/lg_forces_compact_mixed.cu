@@ -620,15 +620,12 @@ __global__ void __launch_bounds__(ShapeH<SL>::kWarps * 32, ShapeH<SL>::kMinBlock
     MX.hsum[2 * i + 1] = make_float4(acch[2].hi, acch[2].lo, 0.f, 0.f);
 }
 
-// Completion of every row: contact part (csum when `contacts`) plus the Hamaker part (hsum when
-// `hamaker`), both converted to FP64 here, then facet terms, stores and half kick.
+// Completion of row i in FP64: contact part (csum when `contacts`) plus the Hamaker part (hsum when
+// `hamaker`), both converted to FP64, then the unary terms, stores and half kick; with `kick` also
+// the next step's opening half kick and drift, and the float-float copies of the new state.
 template <bool FACETS>
-__global__ void __launch_bounds__(64) forces_finish_mixed(Params P, StateView S, double hdt, double dt,
-                                                          int move_facets, int contacts, int hamaker, int kick,
-                                                          MixedExtra MX) {
-    if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+__device__ __forceinline__ void finish_fp64_row(const Params &P, const StateView &S, int64_t i, double hdt, double dt,
+                                                int contacts, int hamaker, int kick, const MixedExtra &MX) {
     // every input is loaded before anything is stored (the buffers are distinct)
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 c0 = contacts ? MX.csum[3 * i] : z4, c1 = contacts ? MX.csum[3 * i + 1] : z4,
@@ -656,11 +653,119 @@ __global__ void __launch_bounds__(64) forces_finish_mixed(Params P, StateView S,
         st4(S.v_out, i, vh);
         st4(S.w_out, i, wh);
         const d3 xn = (h & LG_HOLD_X) ? xo : add(xo, scl(dt, vh));
+        const d3 thn = (h & LG_HOLD_THETA) ? tho : add(tho, scl(dt, wh));
         if (!(h & LG_HOLD_X)) st4(S.x, i, xn);
-        if (!(h & LG_HOLD_THETA)) st4(S.th, i, add(tho, scl(dt, wh)));
+        if (!(h & LG_HOLD_THETA)) st4(S.th, i, thn);
         rel_ff(xn, MX.ox, MX.oy, MX.oz, MX.agg, MX.orig, i, P.n, MX.x32);
-        vel_ff(vh, wh, i, P.n, MX.v32);
+        state_ff(vh, wh, i, P.n, MX.v32, MX.s32);
     }
+}
+
+template <bool FACETS>
+__global__ void __launch_bounds__(64) forces_finish_mixed(Params P, StateView S, double hdt, double dt,
+                                                          int move_facets, int contacts, int hamaker, int kick,
+                                                          MixedExtra MX) {
+    if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    finish_fp64_row<FACETS>(P, S, i, hdt, dt, contacts, hamaker, kick, MX);
+}
+
+// Float-float sum and product (the product's rounding error from an FMA; results renormalised).
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const ff s = two_sum(a.hi, b.hi);
+    return two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);
+    return two_sum(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ double ff_to_d(ff a) { return (double)a.hi + (double)a.lo; }
+
+// Completion of a step of a run (no facets, no body term), integrating in float-float on the FP32
+// pipes: between the first and the last step of a run the state lives in x32 / v32 / s32 (the FP64
+// x and theta keep the values of the run's first step, v and omega are left behind) and the last
+// step writes the FP64 state. Velocities and spins are float-float values (about 2^-46 of their
+// magnitude). Positions are carried twice: x32 (relative to the system origin) advances for the
+// force kernels, and the displacement since the run's first step accumulates from zero in s32, so
+// that the last step's FP64 position x_first + displacement is not limited by the float-float
+// resolution of x32 (a step moves a particle by about 1e-9 of its distance from the origin); the
+// rotation theta accumulates the same way.
+//   LAST = false: the end-of-step half kick, the next step's opening half kick and drift;
+//   LAST = true:  the end-of-step half kick, then a, alpha, v, omega, x and theta in FP64.
+// s32: [i] low parts of omega; [n + i] / [2n + i] displacement hi / lo; [3n + i] / [4n + i]
+// rotation hi / lo.
+template <bool LAST>
+__global__ void __launch_bounds__(64) forces_finish_ff(Params P, StateView S, int contacts, int hamaker, ff hdt, ff dt,
+                                                       double hdt_d, double dt_d, MixedExtra MX) {
+    const int64_t n = P.n;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t h = hold_of(P.hold, i);
+    if (h) {  // a held particle keeps its FP64 state current (a held value stays exactly as it was)
+        finish_fp64_row<false>(P, S, i, hdt_d, dt_d, contacts, hamaker, LAST ? 0 : 1, MX);
+        return;
+    }
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 c0 = contacts ? MX.csum[3 * i] : z4, c1 = contacts ? MX.csum[3 * i + 1] : z4,
+                 c2 = contacts ? MX.csum[3 * i + 2] : z4;
+    const float4 h0 = hamaker ? MX.hsum[2 * i] : z4, h1 = hamaker ? MX.hsum[2 * i + 1] : z4;
+    const float4 vh = MX.v32[i], vl = MX.v32[n + i], wh = MX.v32[2 * n + i], wl = MX.s32[i];
+    const float4 dh = MX.s32[n + i], dl = MX.s32[2 * n + i], rh = MX.s32[3 * n + i], rl = MX.s32[4 * n + i];
+    ff a[3] = {{c0.x, c0.y}, {c0.z, c0.w}, {c1.x, c1.y}};
+    const ff al[3] = {{c1.z, c1.w}, {c2.x, c2.y}, {c2.z, c2.w}};
+    if (hamaker) {
+        const ff ah[3] = {{h0.x, h0.y}, {h0.z, h0.w}, {h1.x, h1.y}};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a[c] = contacts ? ff_add(a[c], ah[c]) : ah[c];
+    }
+    bool finite = true;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) finite = finite && isfinite(a[c].hi) && isfinite(al[c].hi);
+    if (!finite) set_error(S.err, LG_DEVERR_NONFINITE);
+    ff v[3] = {{vh.x, vl.x}, {vh.y, vl.y}, {vh.z, vl.z}};
+    ff w[3] = {{wh.x, wl.x}, {wh.y, wl.y}, {wh.z, wl.z}};
+    ff dx[3] = {{dh.x, dl.x}, {dh.y, dl.y}, {dh.z, dl.z}};
+    ff dr[3] = {{rh.x, rl.x}, {rh.y, rl.y}, {rh.z, rl.z}};
+    // end-of-step half kick
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        v[c] = ff_add(v[c], ff_mul(hdt, a[c]));
+        w[c] = ff_add(w[c], ff_mul(hdt, al[c]));
+    }
+    if (LAST) {
+        const d3 x0 = ld4(S.x, i), t0 = ld4(S.th, i);
+        st4(S.a, i, mk3(ff_to_d(a[0]), ff_to_d(a[1]), ff_to_d(a[2])));
+        st4(S.al, i, mk3(ff_to_d(al[0]), ff_to_d(al[1]), ff_to_d(al[2])));
+        st4(S.v_out, i, mk3(ff_to_d(v[0]), ff_to_d(v[1]), ff_to_d(v[2])));
+        st4(S.w_out, i, mk3(ff_to_d(w[0]), ff_to_d(w[1]), ff_to_d(w[2])));
+        st4(S.x, i, mk3(x0.x + ff_to_d(dx[0]), x0.y + ff_to_d(dx[1]), x0.z + ff_to_d(dx[2])));
+        st4(S.th, i, mk3(t0.x + ff_to_d(dr[0]), t0.y + ff_to_d(dr[1]), t0.z + ff_to_d(dr[2])));
+        return;
+    }
+    // the next step's opening half kick and drift
+    const float4 xh = MX.x32[i], xl = MX.x32[n + i];
+    ff x[3] = {{xh.x, xl.x}, {xh.y, xl.y}, {xh.z, xl.z}};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        v[c] = ff_add(v[c], ff_mul(hdt, a[c]));
+        w[c] = ff_add(w[c], ff_mul(hdt, al[c]));
+        const ff step = ff_mul(dt, v[c]);
+        x[c] = ff_add(x[c], step);
+        dx[c] = ff_add(dx[c], step);
+        dr[c] = ff_add(dr[c], ff_mul(dt, w[c]));
+    }
+    MX.x32[i] = make_float4(x[0].hi, x[1].hi, x[2].hi, 0.f);
+    MX.x32[n + i] = make_float4(x[0].lo, x[1].lo, x[2].lo, 0.f);
+    MX.v32[i] = make_float4(v[0].hi, v[1].hi, v[2].hi, 0.f);
+    MX.v32[n + i] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
+    MX.v32[2 * n + i] = make_float4(w[0].hi, w[1].hi, w[2].hi, 0.f);
+    MX.s32[i] = make_float4(w[0].lo, w[1].lo, w[2].lo, 0.f);
+    MX.s32[n + i] = make_float4(dx[0].hi, dx[1].hi, dx[2].hi, 0.f);
+    MX.s32[2 * n + i] = make_float4(dx[0].lo, dx[1].lo, dx[2].lo, 0.f);
+    MX.s32[3 * n + i] = make_float4(dr[0].hi, dr[1].hi, dr[2].hi, 0.f);
+    MX.s32[4 * n + i] = make_float4(dr[0].lo, dr[1].lo, dr[2].lo, 0.f);
 }
 
 namespace {
@@ -708,8 +813,8 @@ int hamaker_slices(int64_t n) {
 }  // namespace
 
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
-                                double dt, int move_facets, bool kick, const MixedExtra &MX, cudaStream_t st,
-                                cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+                                double dt, int move_facets, bool kick, bool prev_fused, const MixedExtra &MX,
+                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
     const bool ver = P.pairs == LG_PAIRS_VERLET;
     const int contacts = P.binary_model != LG_BINARY_NONE ? 1 : 0;
     const int hamaker = P.hamaker_model != LG_HAMAKER_NONE ? 1 : 0;
@@ -748,6 +853,18 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         cudaStreamWaitEvent(st, join, 0);
     }
     const unsigned blocks = (unsigned)((P.n + 63) / 64);
+    // without facets or a body term the completion of a run's steps integrates in float-float; the
+    // FP64 completion serves the rest (and a run's last step when the step before was not fused)
+    const bool plain = P.n_facets == 0 && !P.ext_a && MX.s32;
+    auto split = [](double d) { const float hi = (float)d; return ff{hi, (float)(d - (double)hi)}; };
+    if (plain && kick) {
+        forces_finish_ff<false><<<blocks, 64, 0, st>>>(P, S, contacts, hamaker, split(hdt), split(dt), hdt, dt, MX);
+        return kernels;
+    }
+    if (plain && prev_fused) {
+        forces_finish_ff<true><<<blocks, 64, 0, st>>>(P, S, contacts, hamaker, split(hdt), split(dt), hdt, dt, MX);
+        return kernels;
+    }
     if (P.n_facets > 0 || P.ext_a)
         forces_finish_mixed<true><<<blocks, 64, 0, st>>>(P, S, hdt, dt, move_facets, contacts, hamaker, kick ? 1 : 0, MX);
     else

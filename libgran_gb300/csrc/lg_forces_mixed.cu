@@ -299,14 +299,15 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
 // With `uncovered` set, also flags (*uncovered = 1) any position further than four times its system's
 // extent (orig.w, or `oext` for a single system) from the origin in some coordinate.
 __global__ void mixed_copies(int64_t n, const dbl4 *__restrict__ x, const dbl4 *__restrict__ v,
-                             const dbl4 *__restrict__ w, double ox, double oy, double oz, double oext,
-                             const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig, float4 *__restrict__ x32,
-                             float4 *__restrict__ v32, int32_t *uncovered) {
+                             const dbl4 *__restrict__ w, const dbl4 *__restrict__ th, double ox, double oy, double oz,
+                             double oext, const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig,
+                             float4 *__restrict__ x32, float4 *__restrict__ v32, float4 *__restrict__ s32,
+                             int32_t *uncovered) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const d3 xi = ld4(x, i);
     rel_ff(xi, ox, oy, oz, agg, orig, i, n, x32);
-    vel_ff(ld4(v, i), ld4(w, i), i, n, v32);
+    state_ff(ld4(v, i), ld4(w, i), i, n, v32, s32);
     if (uncovered) {
         if (agg) {
             const dbl4 o = orig[agg[i]];
@@ -325,7 +326,8 @@ __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restri
                                  dbl4 *__restrict__ w, const dbl4 *__restrict__ a, const dbl4 *__restrict__ al,
                                  double dt, double hdt, double ox, double oy, double oz,
                                  const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig,
-                                 float4 *__restrict__ x32, float4 *__restrict__ v32, const uint8_t *__restrict__ hold) {
+                                 float4 *__restrict__ x32, float4 *__restrict__ v32, float4 *__restrict__ s32,
+                                 const uint8_t *__restrict__ hold) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t h = hold_of(hold, i);
@@ -340,7 +342,7 @@ __global__ void kick_drift_mixed(int64_t n, dbl4 *__restrict__ x, dbl4 *__restri
     }
     if (!(h & LG_HOLD_THETA)) st4(th, i, add(ld4(th, i), scl(dt, wi)));
     rel_ff(xn, ox, oy, oz, agg, orig, i, n, x32);
-    vel_ff(vi, wi, i, n, v32);
+    state_ff(vi, wi, i, n, v32, s32);
 }
 
 template <int T, bool VERLET>
@@ -376,24 +378,24 @@ void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairV
 #undef LG_CASE
 }
 
-void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const double *origin,
-                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st,
+void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const dbl4 *th, const double *origin,
+                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, float4 *s32, cudaStream_t st,
                          int32_t *uncovered) {
     const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
-    mixed_copies<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, w, origin[0], origin[1], origin[2], origin[3], agg, orig,
-                                                       x32, v32, uncovered);
+    mixed_copies<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, w, th, origin[0], origin[1], origin[2], origin[3], agg,
+                                                       orig, x32, v32, s32, uncovered);
 }
 
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
-                             float4 *v32, const uint8_t *hold, cudaStream_t st) {
+                             float4 *v32, float4 *s32, const uint8_t *hold, cudaStream_t st) {
     const int threads = 64;  // small blocks: all SMs get work at moderate n
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return;
     kick_drift_mixed<<<(unsigned)blocks, threads, 0, st>>>(n, x, v, th, w, a, al, dt, hdt, origin[0], origin[1],
-                                                           origin[2], agg, orig, x32, v32, hold);
+                                                           origin[2], agg, orig, x32, v32, s32, hold);
 }
 
 }  // namespace lg

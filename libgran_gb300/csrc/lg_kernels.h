@@ -69,6 +69,11 @@ struct MixedExtra {
     // [3n] velocities of the force evaluation: v32[i] / v32[n + i] = high / low FP32 parts of v_i,
     // v32[2n + i] = FP32 rounding of omega_i (compacted kernel's contact and bond pairs)
     float4 *v32;
+    // [5n] the rest of the float-float state that runs of fused steps carry (the completion kernel
+    // integrates in float-float between a run's first and last steps): s32[i] = low FP32 parts of
+    // omega_i; s32[n + i], s32[2n + i] = displacement since the run's first step (hi, lo);
+    // s32[3n + i], s32[4n + i] = rotation since then (hi, lo)
+    float4 *s32;
     // compacted kernels' scratch: per particle the float-float (hi, lo) pairs of the contact sums
     // (csum, [3n]: a.x a.y / a.z alpha.x / alpha.y alpha.z) and of the Hamaker sum (hsum, [2n])
     float4 *csum;
@@ -103,13 +108,13 @@ void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairV
 // orig[] those of each system of a batch.
 // With `uncovered`, also sets *uncovered when a position lies beyond four times its system's extent
 // (origin[3], orig[].w) from the origin: the origins must then be set up again.
-void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const double *origin,
-                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, cudaStream_t st,
+void launch_mixed_copies(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, const dbl4 *th, const double *origin,
+                         const int32_t *agg, const dbl4 *orig, float4 *x32, float4 *v32, float4 *s32, cudaStream_t st,
                          int32_t *uncovered = nullptr);
-// Kick + drift of the mixed path; also refreshes x32 and v32.
+// Kick + drift of the mixed path; also refreshes x32, v32 and s32.
 void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, const dbl4 *a, const dbl4 *al, double dt,
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
-                             float4 *v32, const uint8_t *hold, cudaStream_t st);
+                             float4 *v32, float4 *s32, const uint8_t *hold, cudaStream_t st);
 
 // Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
@@ -119,9 +124,11 @@ void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairV
 // returns the number of kernels launched.
 // With `kick`, the completion kernel goes on to the next step's opening half kick and drift (and the
 // float-float copies), exactly as launch_kick_drift_mixed would.
+// kick: another step follows (the completion also runs its opening half kick and drift);
+// prev_fused: the step before was such a step (its state may be float-float only).
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
-                                double dt, int move_facets, bool kick, const MixedExtra &MX, cudaStream_t st,
-                                cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+                                double dt, int move_facets, bool kick, bool prev_fused, const MixedExtra &MX,
+                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 
 // Layout conversion between a caller's [n][3] doubles (already in device memory) and the padded
 // device layout (lg_reduce.cu).

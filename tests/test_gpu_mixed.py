@@ -111,23 +111,81 @@ def test_mixed_set_positions_translation(shift_r):
     assert a.device_errors() == 0 and b.device_errors() == 0
 
 
-def test_mixed_fused_kick_matches_step_by_step():
-    """Within a run of steps the mixed completion kernel also performs the next step's opening half
-    kick and drift; stepping one step per call (no fusion) gives the same bits."""
+def test_mixed_runs_of_steps_track_single_steps():
+    """Inside a run of steps the mixed completion kernel integrates in float-float (the FP64 state is
+    brought up to date by the run's last step); one step per call keeps the FP64 integration. The
+    pair terms are FP32 arithmetic on the high parts of the state, so states that differ by rounding
+    can give pair terms that differ by an FP32 rounding (1e-7 of a term): after two steps the two
+    agree to that; over 20 steps of a bonded aggregate the difference grows with the dynamics'
+    sensitivity (about tenfold every ten steps), as any perturbation does. The integrator itself is
+    checked exactly in free flight (next test)."""
     mat = K.Material()
     n = 2500
     x0 = generate_aggregate(31, n, mat.r)
     v0 = generate_velocities(31, n, 0.1)
     d = _desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, A.LG_PRECISION_MIXED, mat,
               A.LG_FORCE_KERNEL_COMPACT)
-    a = System(d, x0, v0)
-    b = System(d, x0, v0)
-    a.step(mat.dt, 60, 20)
-    for _ in range(60):
-        b.step(mat.dt, 1, 20)
-    for f in STATE_FIELDS + (A.LG_FIELD_A, A.LG_FIELD_ALPHA):
-        assert np.array_equal(a.get(f), b.get(f)), f
-    assert a.device_errors() == 0
+    for nst, tol_x, tol_v, tol_a in ((2, 1e-10, 1e-8, 1e-6), (20, 1e-8, 1e-5, 1e-4)):
+        a, b, c = System(d, x0, v0), System(d, x0, v0), System(d, x0, v0)
+        a.step(mat.dt, nst, 20)
+        for _ in range(nst):
+            b.step(mat.dt, 1, 20)
+            c.step(mat.dt, 1, 20)
+        for f in STATE_FIELDS + (A.LG_FIELD_A, A.LG_FIELD_ALPHA):  # single steps are deterministic
+            assert np.array_equal(b.get(f), c.get(f)), f
+        assert H.rel_err(a.get(A.LG_FIELD_X) - x0, b.get(A.LG_FIELD_X) - x0) <= tol_x
+        for f in (A.LG_FIELD_V, A.LG_FIELD_OMEGA, A.LG_FIELD_THETA):
+            assert H.rel_err(a.get(f), b.get(f)) <= tol_v, (nst, f)
+        for f in (A.LG_FIELD_A, A.LG_FIELD_ALPHA):
+            assert H.rel_err(a.get(f), b.get(f)) <= tol_a, (nst, f)
+        assert a.device_errors() == 0
+
+
+def test_mixed_run_free_flight_is_exact():
+    """Free flight (no contacts, no Hamaker force) through a run of float-float steps: positions
+    follow x0 + v0 t and rotations omega0 t to better than the FP64 step-by-step integration (the
+    run's displacement accumulates from zero and joins the FP64 position once)."""
+    mat = K.Material()
+    n = 2000
+    x0 = generate_aggregate(31, n, mat.r) * 3.0
+    v0 = generate_velocities(31, n, 0.1)
+    om0 = generate_velocities(32, n, 1e8)
+    d = _desc(n, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, A.LG_PRECISION_MIXED, mat,
+              A.LG_FORCE_KERNEL_COMPACT)
+    d.hamaker.A = 0.0
+    s = System(d, x0, v0, om0=om0)
+    s.step(mat.dt, 60, 20)
+    t = 60 * mat.dt
+    assert H.rel_err(s.get(A.LG_FIELD_X) - x0, v0 * t) <= 2e-8
+    assert H.rel_err(s.get(A.LG_FIELD_V), v0) <= 4e-15  # the float-float round trip: 2^-49
+    assert H.rel_err(s.get(A.LG_FIELD_THETA), om0 * t) <= 1e-13
+    assert H.rel_err(s.get(A.LG_FIELD_OMEGA), om0) <= 4e-15
+
+
+def test_mixed_runs_with_held_particles():
+    """Held increments inside runs of float-float steps: held particles keep the FP64 path, so a
+    held velocity or position stays exactly as it was."""
+    mat = K.Material()
+    n = 2000
+    x0 = generate_aggregate(32, n, mat.r)
+    v0 = generate_velocities(32, n, 0.3)
+    hold = np.zeros(n, dtype=np.uint8)
+    hold[::7] = A.LG_HOLD_V
+    hold[3::7] = A.LG_HOLD_X | A.LG_HOLD_THETA
+    descs = []
+    for prec in (A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED):
+        d = _desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, prec, mat, A.LG_FORCE_KERNEL_COMPACT)
+        K.set_hold(d, hold)
+        descs.append(d)
+    s64, smx = System(descs[0], x0, v0), System(descs[1], x0, v0)
+    s64.step(mat.dt, 80, 20)
+    smx.step(mat.dt, 80, 20)
+    hv, hx = hold == A.LG_HOLD_V, (hold & A.LG_HOLD_X) > 0
+    assert np.array_equal(smx.get(A.LG_FIELD_V)[hv], v0[hv])
+    assert np.array_equal(smx.get(A.LG_FIELD_X)[hx], x0[hx])
+    assert np.array_equal(smx.get(A.LG_FIELD_THETA)[hx], np.zeros((hx.sum(), 3)))
+    assert H.rel_err(smx.get(A.LG_FIELD_X) - x0, s64.get(A.LG_FIELD_X) - x0) <= 1e-4
+    assert smx.device_errors() == 0
 
 
 @pytest.mark.parametrize("precision", [A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED], ids=["fp64", "mixed"])
