@@ -460,7 +460,8 @@ __host__ __device__ inline size_t build_smem_bytes(int64_t cap, int64_t bcap) {
 __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
     int64_t n, const dbl4 *__restrict__ x, BatchView B, const float4 *__restrict__ x32, const GridDev *__restrict__ g,
     const int32_t *__restrict__ cstart, const int32_t *__restrict__ ccount, const int32_t *__restrict__ sorted,
-    double rv2, PairView oldv, PairView newv, BondView BV, int32_t *err, int32_t *max_row) {
+    const int32_t *__restrict__ cell_of, double rv2, PairView oldv, PairView newv, BondView BV, int32_t *err,
+    int32_t *max_row) {
     extern __shared__ int32_t sm[];
     __shared__ int32_t rlen[kBuildRows];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -491,11 +492,12 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
         const float4 fi = x32[i];
         const dbl4 xd = x[i];
         const d3 xi_ = mk3(xd.x, xd.y, xd.z);
-        const dbl4 hp = hash_pos(x, B, i);
         const int32_t ai = B.agg ? B.agg[i] : 0;
-        const int64_t cx = cell_coord(hp.x, g->lo[0], g->edge, dim0);
-        const int64_t cy = cell_coord(hp.y, g->lo[1], g->edge, dim1);
-        const int64_t cz = cell_coord(hp.z, g->lo[2], g->edge, dim2);
+        // the row's cell as cell_count placed it (integer decode: an FP64 division here would be a
+        // full-warp FP64 instruction per row)
+        const int32_t ci = cell_of[i];
+        const int32_t d0 = (int32_t)dim0, d1 = (int32_t)dim1;
+        const int64_t cx = ci % d0, cy = (ci / d0) % d1, cz = ci / (d0 * d1);
         const int64_t x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < dim0 ? cx + 1 : dim0 - 1;
         // the 9 runs of cells (z, y fixed; x0..x1) are 9 contiguous ranges of the sorted list; lane
         // r < 9 looks up range r, and the ranges are walked as one virtual list of `total`
@@ -770,7 +772,7 @@ void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, double 
         cudaFuncSetAttribute(build_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)build_smem_bytes(255, 255));
         attr_device = dev;
     }
-    build_rows<<<b2, kBuildRows * kBuildWarps, smem, st>>>(n, x, B, ls.x32, ls.grid, ls.start, ls.count, ls.sorted,
+    build_rows<<<b2, kBuildRows * kBuildWarps, smem, st>>>(n, x, B, ls.x32, ls.grid, ls.start, ls.count, ls.sorted, ls.cell_of,
                                                            rv * rv, oldv, newv, BV, err, ls.max_row);
 }
 
