@@ -303,38 +303,10 @@ static int set_mixed_origins(lg_system *s, const double *x) {
     return LG_OK;
 }
 
-// After new positions (x: the caller's host array) or velocities: refresh the float-float copies. The
-// origins (and the CUDA graphs that hold them) are kept while every offset from its system's origin
-// stays within four times the extent the origin was set up with (the culling margins of
-// set_cull_radii allow for exactly that); the copy kernel checks this on the device, and only when
-// it fails are the origins set up again from x and the copies redone.
-static int refresh_mixed_copies(lg_system *s, const double *x) {
-    const int64_t n = s->P.n;
-    int32_t *flag = x ? s->d_flag : nullptr;
-    if (flag) LG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int32_t), s->stream));
-    launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->th, s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->s32,
-                        s->stream, flag);
-    s->launches += 1;
-    LG_CUDA(cudaGetLastError());
-    if (!flag) return LG_OK;
-    int32_t h = 0;
-    LG_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
-    LG_CUDA(cudaStreamSynchronize(s->stream));
-    if (!h) return LG_OK;
-    LG_TRY(set_mixed_origins(s, x));  // positions moved far: new origins and culling radii
-    set_cull_radii(s);
-    s->drop_graphs();
-    launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->th, s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->s32,
-                        s->stream);
-    s->launches += 1;
-    LG_CUDA(cudaGetLastError());
-    return LG_OK;
-}
-
-// lg_get / lg_set: the caller's [n][3] array moves in one copy to device scratch (the observables
-// scratch, n * 20 doubles, ordered with every other use on the handle's stream) and a kernel converts
-// it to or from the padded device layout, so no host-side staging or conversion loop is involved and
-// a pinned caller buffer is copied by DMA directly.
+// lg_get / lg_set of the accelerations: the caller's [n][3] array moves in one copy to device scratch
+// (the observables scratch, n * 20 doubles, ordered with every other use on the handle's stream) and
+// a kernel converts it to or from the padded device layout. (The state fields go through
+// state_upload / state_download.)
 static int upload_staged(lg_system *s, dbl4 *dst, const double *aos) {
     const int64_t n = s->P.n;
     LG_CUDA(cudaMemcpyAsync(s->obs_scratch, aos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
@@ -363,6 +335,8 @@ void lg_system::drop_graphs() {
 void lg_system::release() {
     if (device >= 0) cudaSetDevice(device);
     drop_graphs();
+    if (h_pin) cudaFreeHost(h_pin);
+    h_pin = nullptr;
     for (void *p : allocations) cudaFree(p);
     allocations.clear();
     if (stream) cudaStreamDestroy(stream);
@@ -977,6 +951,9 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     if (s->precision == LG_PRECISION_FP64 && (int64_t)s->pv[0].cap * n <= kPairsMaxSlots)
         LG_TRY(s->alloc(&s->pres, 6 * (size_t)(s->pv[0].cap * n)));
     LG_TRY(s->alloc(&s->obs_scratch, (size_t)obs_scratch_doubles(n)));
+    LG_TRY(s->alloc(&s->d_ticket, 1));
+    LG_CUDA(cudaMemset(s->d_ticket, 0, sizeof(unsigned)));
+    LG_CUDA(cudaMallocHost(&s->h_pin, 64 * sizeof(double)));
     LG_TRY(s->alloc(&s->obs_out, 32));
 
     if (s->precision == LG_PRECISION_MIXED) {
@@ -1194,56 +1171,126 @@ static dbl4 *field_ptr(lg_system *s, int field) {
     }
 }
 
+static int state_slot(int field) {
+    switch (field) {
+        case LG_FIELD_X: return 0;
+        case LG_FIELD_V: return 1;
+        case LG_FIELD_THETA: return 2;
+        case LG_FIELD_OMEGA: return 3;
+        default: return -1;
+    }
+}
+
+static int state_upload(lg_system *s, const double *const host[4]);
+static int state_download(lg_system *s, double *const host[4]);
+
 extern "C" int lg_get(lg_system *s, int field, double *out) {
     LG_HANDLE(s);
     dbl4 *p = field_ptr(s, field);
     if (!p || !out) return lg_fail(LG_E_INVALID, "lg_get: bad field %d or null output", field);
-    return download_staged(s, p, out);
+    const int q = state_slot(field);
+    if (q < 0) return download_staged(s, p, out);
+    double *host[4] = {nullptr, nullptr, nullptr, nullptr};
+    host[q] = out;
+    return state_download(s, host);
 }
 
 extern "C" int lg_set(lg_system *s, int field, const double *in) {
     LG_HANDLE(s);
     dbl4 *p = field_ptr(s, field);
     if (!p || !in) return lg_fail(LG_E_INVALID, "lg_set: bad field %d or null input", field);
-    LG_TRY(upload_staged(s, p, in));
-    if (s->x32 && (field == LG_FIELD_X || field == LG_FIELD_V || field == LG_FIELD_OMEGA))
-        LG_TRY(refresh_mixed_copies(s, field == LG_FIELD_X ? in : nullptr));
+    const int q = state_slot(field);
+    if (q < 0) return upload_staged(s, p, in);
+    const double *host[4] = {nullptr, nullptr, nullptr, nullptr};
+    host[q] = in;
+    return state_upload(s, host);
+}
+
+// Device address of a caller's host buffer when it is pinned (the GPU then reads or writes it
+// directly over the host link), or null for pageable memory (staged through device scratch).
+static const void *mapped_host(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// State upload of any of x, v, theta, omega (host [n][3] arrays, null: unchanged) in one kernel,
+// which also refreshes the mixed path's float-float copies. The origins (and the CUDA graphs that
+// hold them) are kept while every position stays within four times its system's extent from its
+// origin; the kernel checks that, and only when it fails are the origins set up again from x.
+static int state_upload(lg_system *s, const double *const host[4]) {
+    if (!host[0] && !host[1] && !host[2] && !host[3]) return LG_OK;
+    const int64_t n = s->P.n;
+    const size_t bytes = sizeof(double) * 3 * (size_t)n;
+    StateIO io{};
+    for (int f = 0; f < 4; ++f) {
+        if (!host[f]) continue;
+        const void *m = mapped_host(host[f]);
+        if (m) {
+            io.in[f] = (const double *)m;
+        } else {  // staged in the observables scratch (20 n doubles >= 4 x 3 n)
+            LG_CUDA(cudaMemcpyAsync(s->obs_scratch + 3 * n * f, host[f], bytes, cudaMemcpyHostToDevice, s->stream));
+            io.in[f] = s->obs_scratch + 3 * n * f;
+        }
+    }
+    const bool refresh = s->x32 && (host[0] || host[1] || host[3]);
+    int32_t *flag = refresh && host[0] ? s->d_flag : nullptr;
+    if (flag) LG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int32_t), s->stream));
+    launch_state_in(n, io, s->x, s->v[s->vcur], s->th, s->w[s->vcur], refresh ? s->x32 : nullptr, s->v32, s->s32,
+                    s->origin, s->d_agg, s->d_orig, flag, s->stream);
+    s->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    if (flag) LG_CUDA(cudaMemcpyAsync(s->h_pin, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));  // the caller may reuse its buffers on return
+    if (flag && *reinterpret_cast<int32_t *>(s->h_pin)) {
+        LG_TRY(set_mixed_origins(s, host[0]));  // positions moved far: new origins and culling radii
+        set_cull_radii(s);
+        s->drop_graphs();
+        launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->th, s->origin, s->d_agg, s->d_orig, s->x32,
+                            s->v32, s->s32, s->stream);
+        s->launches += 1;
+        LG_CUDA(cudaGetLastError());
+        LG_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    return LG_OK;
+}
+
+// State download into host [n][3] arrays (null: skipped), one kernel.
+static int state_download(lg_system *s, double *const host[4]) {
+    if (!host[0] && !host[1] && !host[2] && !host[3]) return LG_OK;
+    const int64_t n = s->P.n;
+    const size_t bytes = sizeof(double) * 3 * (size_t)n;
+    StateIO io{};
+    bool staged[4] = {false, false, false, false};
+    for (int f = 0; f < 4; ++f) {
+        if (!host[f]) continue;
+        void *m = const_cast<void *>(mapped_host(host[f]));
+        staged[f] = m == nullptr;
+        io.out[f] = staged[f] ? s->obs_scratch + 3 * n * f : (double *)m;
+    }
+    launch_state_out(n, io, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->stream);
+    s->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    for (int f = 0; f < 4; ++f)
+        if (staged[f])
+            LG_CUDA(cudaMemcpyAsync(host[f], s->obs_scratch + 3 * n * f, bytes, cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaStreamSynchronize(s->stream));
     return LG_OK;
 }
 
 extern "C" int lg_get_state(lg_system *s, double *x, double *v, double *th, double *w) {
     LG_HANDLE(s);
-    const int64_t n = s->P.n;
-    const size_t bytes = sizeof(double) * 3 * (size_t)n;
-    double *host[4] = {x, v, th, w};
-    const dbl4 *dev[4] = {s->x, s->v[s->vcur], s->th, s->w[s->vcur]};
-    for (int f = 0; f < 4; ++f) {  // staged in the observables scratch (20 n doubles >= 4 x 3 n)
-        if (!host[f]) continue;
-        launch_dev4_to_aos(n, dev[f], s->obs_scratch + 3 * n * f, s->stream);
-        s->launches += 1;
-        LG_CUDA(cudaMemcpyAsync(host[f], s->obs_scratch + 3 * n * f, bytes, cudaMemcpyDeviceToHost, s->stream));
-    }
-    LG_CUDA(cudaGetLastError());
-    LG_CUDA(cudaStreamSynchronize(s->stream));
-    return LG_OK;
+    double *const host[4] = {x, v, th, w};
+    return state_download(s, host);
 }
 
 extern "C" int lg_set_state(lg_system *s, const double *x, const double *v, const double *th, const double *w) {
     LG_HANDLE(s);
-    const int64_t n = s->P.n;
-    const size_t bytes = sizeof(double) * 3 * (size_t)n;
-    const double *host[4] = {x, v, th, w};
-    dbl4 *dev[4] = {s->x, s->v[s->vcur], s->th, s->w[s->vcur]};
-    for (int f = 0; f < 4; ++f) {
-        if (!host[f]) continue;
-        LG_CUDA(cudaMemcpyAsync(s->obs_scratch + 3 * n * f, host[f], bytes, cudaMemcpyHostToDevice, s->stream));
-        launch_aos_to_dev4(n, s->obs_scratch + 3 * n * f, dev[f], s->stream);
-        s->launches += 1;
-    }
-    LG_CUDA(cudaGetLastError());
-    if (s->x32 && (x || v || w)) LG_TRY(refresh_mixed_copies(s, x));
-    LG_CUDA(cudaStreamSynchronize(s->stream));  // the caller may reuse its buffers on return
-    return LG_OK;
+    const double *const host[4] = {x, v, th, w};
+    return state_upload(s, host);
 }
 
 extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
@@ -1333,17 +1380,19 @@ extern "C" int lg_get_observables_select(lg_system *s, int32_t parts, lg_observa
     // every pass stays on the device; one copy back at the end
     StateView S = state_view(s, false);
     if (parts & LG_OBS_STATE) {
-        launch_observables_state(P.n, s->x, s->v[s->vcur], s->w[s->vcur], m, I, s->obs_scratch, s->obs_out, s->stream);
-        s->launches += 4;
+        launch_observables_state(P.n, s->x, s->v[s->vcur], s->w[s->vcur], m, I, s->obs_scratch, s->obs_out, s->d_ticket,
+                                 s->stream);
+        s->launches += 2;
     }
     if (parts & LG_OBS_PAIRS) {
         launch_observables_pairs(P, S, s->pv[s->pcur], s->bv, m, I, s->obs_scratch, s->obs_out, s->stream);
         s->launches += 2;
     }
     LG_CUDA(cudaGetLastError());
-    double h[19];
-    LG_CUDA(cudaMemcpyAsync(h, s->obs_out, sizeof(double) * 19, cudaMemcpyDeviceToHost, s->stream));
+    LG_CUDA(cudaMemcpyAsync(s->h_pin, s->obs_out, sizeof(double) * 19, cudaMemcpyDeviceToHost, s->stream));
     LG_CUDA(cudaStreamSynchronize(s->stream));
+    double h[19];
+    std::memcpy(h, s->h_pin, sizeof(h));
     const double nn = (double)P.n;
     if (parts & LG_OBS_STATE) {
         o->ke_total = h[0];

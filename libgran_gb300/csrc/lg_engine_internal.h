@@ -51,6 +51,8 @@ struct lg_system {
     float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
     int32_t *d_flag = nullptr;  // mixed: device flag of the float-float copy check
     double *pres = nullptr;     // FP64 pair-parallel kernel: per-slot pair values [6][cap * n]
+    unsigned *d_ticket = nullptr;  // zeroed counter of the reductions' last-block combine
+    double *h_pin = nullptr;       // pinned host buffer (64 doubles) for small results read back
     uint8_t *d_hold = nullptr;  // [n] LG_HOLD_* bits (allocated on first use)
     lg::dbl4 *ext_a = nullptr, *ext_al = nullptr;  // [n] unary body-force terms (allocated on first use)
     double *d_centre = nullptr; // [3 * systems] centres of the central body force

@@ -132,6 +132,16 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
 
 // Layout conversion between a caller's [n][3] doubles (already in device memory) and the padded
 // device layout (lg_reduce.cu).
+// State transfers: up to four [n][3] fields (x, v, theta, omega) per launch, device or pinned host.
+struct StateIO {
+    const double *in[4];
+    double *out[4];
+};
+void launch_state_in(int64_t n, const StateIO &io, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, float4 *x32, float4 *v32,
+                     float4 *s32, const double *origin, const int32_t *agg, const dbl4 *orig, int32_t *uncovered,
+                     cudaStream_t st);
+void launch_state_out(int64_t n, const StateIO &io, const dbl4 *x, const dbl4 *v, const dbl4 *th, const dbl4 *w,
+                      cudaStream_t st);
 void launch_aos_to_dev4(int64_t n, const double *aos, dbl4 *dst, cudaStream_t st);
 void launch_dev4_to_aos(int64_t n, const dbl4 *src, double *aos, cudaStream_t st);
 
@@ -144,7 +154,7 @@ void launch_observables_rg(int64_t n, const dbl4 *x, double *scratch, double *ou
 // Handle observables: out[0..14] and out[18] from the particles (launch_observables_state), out[15..17]
 // from the pair slots (launch_observables_pairs); scratch as above.
 void launch_observables_state(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, double mass, double inertia,
-                              double *scratch, double *out, cudaStream_t st);
+                              double *scratch, double *out, unsigned *ticket, cudaStream_t st);
 void launch_observables_pairs(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
                               double inertia, double *scratch, double *out, cudaStream_t st);
 // Per-system observables of a batch: out[s * 20 + c] = column sums over system s's particles

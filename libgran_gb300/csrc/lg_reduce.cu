@@ -141,10 +141,64 @@ __device__ __forceinline__ double obs_block_sum(double v, double *sh) {
     return r;
 }
 
+// Block sums of C columns in a fixed order: a butterfly over the warp's lanes, then the kObsBlock /
+// 32 warp sums in warp order by thread c < C; the result row goes to part[blockIdx.x].
+template <int C>
+__device__ __forceinline__ void obs_block_row(double (&t)[C], double *__restrict__ part) {
+    __shared__ double ws[kObsBlock / 32][C];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        double v = t[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) ws[warp][c] = v;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < C) {
+        double r = 0.0;
+#pragma unroll
+        for (int q = 0; q < kObsBlock / 32; ++q) r += ws[q][threadIdx.x];
+        part[(int64_t)blockIdx.x * kObsCols + threadIdx.x] = r;
+    }
+}
+
+// The last block of a grid to finish (counted in *ticket, which it resets) sums the nb rows of
+// columns c0 .. c0 + C into out[out0 ..]: 16 threads per column take the rows b = g, g + 16, ...
+// (g = thread / C), and their 16 partial sums are added in order (short dependent chains: a
+// dependent FP64 add takes tens of cycles on this GPU). Returns without waiting on any block.
+template <int C>
+__device__ __forceinline__ void obs_last_block_combine(int nb, const double *__restrict__ part, int c0, int out0,
+                                                       double *__restrict__ out, unsigned *ticket) {
+    static_assert(16 * C <= kObsBlock, "one thread per (column, group)");
+    __shared__ bool last;
+    __shared__ double pg[16][C];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == (unsigned)nb - 1u;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int c = threadIdx.x % C, g = threadIdx.x / C;
+    if (g < 16) {
+        double acc = 0.0;
+        for (int b = g; b < nb; b += 16) acc += ((volatile const double *)part)[(int64_t)b * kObsCols + c0 + c];
+        pg[g][c] = acc;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < C) {
+        double acc = 0.0;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc += pg[q][threadIdx.x];
+        out[out0 + threadIdx.x] = acc;
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+}
+
 __global__ void __launch_bounds__(kObsBlock) obs_state_terms(int64_t n, const dbl4 *__restrict__ x,
                                                              const dbl4 *__restrict__ v, const dbl4 *__restrict__ w,
-                                                             double m, double I, double *__restrict__ part) {
-    __shared__ double sh[kObsBlock];
+                                                             double m, double I, double *__restrict__ part,
+                                                             double *__restrict__ out, unsigned *ticket) {
     const int64_t i = blockIdx.x * (int64_t)kObsBlock + threadIdx.x;
     double t[15];
 #pragma unroll
@@ -161,46 +215,31 @@ __global__ void __launch_bounds__(kObsBlock) obs_state_terms(int64_t n, const db
         t[9] = L.x; t[10] = L.y; t[11] = L.z;
         t[12] = xi.x; t[13] = xi.y; t[14] = xi.z;
     }
-    for (int c = 0; c < 15; ++c) {
-        const double r = obs_block_sum(t[c], sh);
-        if (threadIdx.x == 0) part[blockIdx.x * kObsCols + c] = r;
-    }
-}
-
-// One block: out[c0..c1) = sums over the nb rows of part (threads take rows t, t + 256, ... in
-// order, then the block tree).
-__global__ void __launch_bounds__(kObsBlock) obs_state_combine(int nb, const double *__restrict__ part, int c0, int c1,
-                                                               int out0, double *__restrict__ out) {
-    __shared__ double sh[kObsBlock];
-    for (int c = c0; c < c1; ++c) {
-        double acc = 0.0;
-        for (int b = threadIdx.x; b < nb; b += kObsBlock) acc += part[(int64_t)b * kObsCols + c];
-        const double r = obs_block_sum(acc, sh);
-        if (threadIdx.x == 0) out[out0 + c - c0] = r;
-    }
+    obs_block_row<15>(t, part);
+    obs_last_block_combine<15>((int)gridDim.x, part, 0, 0, out, ticket);
 }
 
 __global__ void __launch_bounds__(kObsBlock) obs_state_rg(int64_t n, const dbl4 *__restrict__ x,
-                                                          const double *__restrict__ sums, double *__restrict__ part) {
-    __shared__ double sh[kObsBlock];
+                                                          const double *__restrict__ sums, double *__restrict__ part,
+                                                          double *__restrict__ out, unsigned *ticket) {
     const int64_t i = blockIdx.x * (int64_t)kObsBlock + threadIdx.x;
-    double t = 0.0;
+    double t[1] = {0.0};
     if (i < n) {
         const double nn = (double)n;
         const d3 q = sub(ld4(x, i), mk3(sums[12] / nn, sums[13] / nn, sums[14] / nn));
-        t = dot(q, q);
+        t[0] = dot(q, q);
     }
-    const double r = obs_block_sum(t, sh);
-    if (threadIdx.x == 0) part[blockIdx.x * kObsCols + 15] = r;
+    obs_block_row<1>(t, part);
+    obs_last_block_combine<1>((int)gridDim.x, part, 0, 18, out, ticket);
 }
 
+// Two kernels: the terms (with their sums, by the last block to finish), then |x - c|^2 about the
+// centre those sums give (out[18]). ticket: a zeroed device counter owned by the caller.
 void launch_observables_state(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, double mass, double inertia,
-                              double *scratch, double *out, cudaStream_t st) {
+                              double *scratch, double *out, unsigned *ticket, cudaStream_t st) {
     const int nb = (int)((n + kObsBlock - 1) / kObsBlock);
-    obs_state_terms<<<nb, kObsBlock, 0, st>>>(n, x, v, w, mass, inertia, scratch);
-    obs_state_combine<<<1, kObsBlock, 0, st>>>(nb, scratch, 0, 15, 0, out);
-    obs_state_rg<<<nb, kObsBlock, 0, st>>>(n, x, out, scratch);
-    obs_state_combine<<<1, kObsBlock, 0, st>>>(nb, scratch, 15, 16, 18, out);
+    obs_state_terms<<<nb, kObsBlock, 0, st>>>(n, x, v, w, mass, inertia, scratch, out, ticket);
+    obs_state_rg<<<nb, kObsBlock, 0, st>>>(n, x, out, scratch, out, ticket);
 }
 
 void launch_observables_pairs(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
@@ -293,6 +332,74 @@ __global__ void dev4_to_aos(int64_t n, const dbl4 *__restrict__ src, double *__r
     aos[3 * i] = q.x;
     aos[3 * i + 1] = q.y;
     aos[3 * i + 2] = q.z;
+}
+
+// The four state fields in one pass. in[f] / out[f]: [n][3] doubles in device memory or in pinned
+// host memory the GPU reads and writes directly (x, v, theta, omega; null: field not moved).
+// state_in also refreshes the mixed path's float-float copies (x32 non-null) from the new values,
+// and with `uncovered` flags a position further than four times its system's extent from its origin.
+__global__ void state_in(int64_t n, StateIO io, dbl4 *__restrict__ x, dbl4 *__restrict__ v, dbl4 *__restrict__ th,
+                         dbl4 *__restrict__ w, float4 *__restrict__ x32, float4 *__restrict__ v32,
+                         float4 *__restrict__ s32, double ox, double oy, double oz, double oext,
+                         const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig, int32_t *uncovered) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dbl4 *dst[4] = {x, v, th, w};
+    d3 val[4];
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        if (io.in[f]) {
+            const double *p = io.in[f] + 3 * i;
+            val[f] = mk3(p[0], p[1], p[2]);
+            st4(dst[f], i, val[f]);
+        } else {
+            val[f] = ld4(dst[f], i);
+        }
+    }
+    if (!x32 || !(io.in[0] || io.in[1] || io.in[3])) return;
+    rel_ff(val[0], ox, oy, oz, agg, orig, i, n, x32);
+    state_ff(val[1], val[3], i, n, v32, s32);
+    if (uncovered) {
+        if (agg) {
+            const dbl4 o = orig[agg[i]];
+            ox = o.x;
+            oy = o.y;
+            oz = o.z;
+            oext = o.w;
+        }
+        const double lim = 4.0 * oext;
+        const d3 q = val[0];
+        if (!(fabs(q.x - ox) <= lim && fabs(q.y - oy) <= lim && fabs(q.z - oz) <= lim)) atomicOr(uncovered, 1);
+    }
+}
+
+__global__ void state_out(int64_t n, StateIO io, const dbl4 *__restrict__ x, const dbl4 *__restrict__ v,
+                          const dbl4 *__restrict__ th, const dbl4 *__restrict__ w) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const dbl4 *src[4] = {x, v, th, w};
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+        if (io.out[f]) {
+            const d3 q = ld4(src[f], i);
+            double *p = io.out[f] + 3 * i;
+            p[0] = q.x;
+            p[1] = q.y;
+            p[2] = q.z;
+        }
+}
+
+void launch_state_in(int64_t n, const StateIO &io, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, float4 *x32, float4 *v32,
+                     float4 *s32, const double *origin, const int32_t *agg, const dbl4 *orig, int32_t *uncovered,
+                     cudaStream_t st) {
+    if (n > 0)
+        state_in<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, io, x, v, th, w, x32, v32, s32, origin[0], origin[1],
+                                                             origin[2], origin[3], agg, orig, uncovered);
+}
+
+void launch_state_out(int64_t n, const StateIO &io, const dbl4 *x, const dbl4 *v, const dbl4 *th, const dbl4 *w,
+                      cudaStream_t st) {
+    if (n > 0) state_out<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, io, x, v, th, w);
 }
 
 void launch_aos_to_dev4(int64_t n, const double *aos, dbl4 *dst, cudaStream_t st) {

@@ -218,3 +218,36 @@ def test_state_calls_match_field_calls(precision):
     c.step(mat.dt, 20, 20)
     for f in STATE_FIELDS:
         assert np.array_equal(b.get(f), c.get(f)), f
+
+
+@pytest.mark.parametrize("precision", [A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED], ids=["fp64", "mixed"])
+def test_state_calls_pinned_and_pageable_agree(precision):
+    """Pinned host buffers are read and written by the GPU directly, pageable ones are staged; both
+    move the same numbers, and a system set from either steps identically."""
+    import torch
+    mat = K.Material()
+    n = 3000
+    x0 = generate_aggregate(41, n, mat.r)
+    v0 = generate_velocities(41, n, 0.2)
+    d = _desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, precision, mat,
+              A.LG_FORCE_KERNEL_COMPACT)
+    a, b = System(d, x0, v0), System(d, x0, v0)
+    a.step(mat.dt, 30, 20)
+    b.step(mat.dt, 30, 20)
+    pinned = [torch.empty((n, 3), dtype=torch.float64).pin_memory() for _ in range(4)]
+    a.get_state(out=tuple(p.numpy() for p in pinned))
+    pageable = a.get_state()
+    for p, q in zip(pinned, pageable):
+        assert np.array_equal(p.numpy(), q)
+    shifted = [p.numpy() + 0.0 for p in pinned]
+    shifted[0] += 3.0 * mat.r
+    for p, q in zip(pinned, shifted):
+        p.numpy()[:] = q
+    a.set_state(*(p.numpy() for p in pinned))
+    b.set_state(*shifted)
+    for f, q in zip(STATE_FIELDS, shifted):
+        assert np.array_equal(a.get(f), q) and np.array_equal(b.get(f), q)
+    a.step(mat.dt, 25, 20)
+    b.step(mat.dt, 25, 20)
+    for f in STATE_FIELDS + (A.LG_FIELD_A, A.LG_FIELD_ALPHA):
+        assert np.array_equal(a.get(f), b.get(f)), f
