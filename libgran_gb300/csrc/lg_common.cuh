@@ -141,6 +141,15 @@ struct Params {
 __device__ __forceinline__ d3 kick_unless(d3 v, double h, d3 a, bool held) { return held ? v : add(v, scl(h, a)); }
 __device__ __forceinline__ uint32_t hold_of(const uint8_t *hold, int64_t i) { return hold ? (uint32_t)hold[i] : 0u; }
 
+// Spring component c (0..8: xi_t, xi_r, xi_o) of slot e in a spring array of `stride` slots:
+// component-major (c * stride + e, the FP64 kernels' layout: a warp reading slot k of consecutive
+// rows coalesces) or, with `aos` (mixed precision, whose kernels reach slots through compacted
+// queues in no row order), one record of 9 consecutive 8-byte components per slot (a pair touches 3
+// sectors instead of 9).
+__host__ __device__ __forceinline__ int64_t spring_at(int32_t aos, int c, int64_t e, int64_t stride) {
+    return aos ? e * 9 + c : (int64_t)c * stride + e;
+}
+
 // Entry flags of a pair slot (Verlet list slot or implicit all-pairs slot)
 constexpr uint32_t kXiLive = 1u;      // contact springs may be nonzero
 constexpr uint32_t kBonded = 2u;      // pair is an intact sintered bond; bond slot in bits 8..15
@@ -161,6 +170,7 @@ struct PairView {
     int32_t *near_j;    // [cap * n] partner
     uint8_t *near_k;    // [cap * n] slot in the row
     int32_t *near_len;  // [n]
+    int32_t aos;        // springs as one 9-component record per slot (spring_at)
 };
 
 struct BondView {
@@ -174,6 +184,7 @@ struct BondView {
     // slot of i in the partner's bond list
     double *cn;         // [15][bcap * n]
     int32_t *rev;       // [bcap * n]
+    int32_t aos;        // bond springs as one 9-component record per bond slot (spring_at)
 };
 
 struct StateView {

@@ -708,6 +708,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     for (int64_t i = 0; i < n; ++i) bcap = std::max(bcap, deg[i]);
     if (bcap > 255) return lg_fail(LG_E_INVALID, "lg_create: a particle has %d bonds (max 255)", bcap);
     s->bv.bcap = bcap;
+    s->bv.aos = s->precision == LG_PRECISION_MIXED ? 1 : 0;
     s->n_bonds_initial = 2 * (int64_t)bonds.size();
     {
         const size_t bs = (size_t)bcap * (size_t)n;
@@ -862,6 +863,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         const int64_t cap = std::max<int64_t>(n - 1, 1);
         PairView &pv = s->pv[0];
         pv.cap = cap;
+        pv.aos = s->precision == LG_PRECISION_MIXED ? 1 : 0;
         pv.nbr = nullptr;
         pv.row_len = nullptr;
         LG_TRY(s->alloc(&pv.flags, (size_t)(cap * n)));
@@ -896,6 +898,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
             for (int q = 0; q < 2; ++q) {
                 PairView &pv = s->pv[q];
                 pv.cap = c;
+                pv.aos = s->precision == LG_PRECISION_MIXED ? 1 : 0;
                 LG_TRY(s->alloc(&pv.nbr, (size_t)(c * n)));
                 LG_TRY(s->alloc(&pv.row_len, (size_t)n));
                 LG_TRY(s->alloc(&pv.flags, (size_t)(c * n)));
@@ -1465,7 +1468,8 @@ extern "C" int lg_get_pair_springs(lg_system *s, int64_t i, int64_t j, double *o
         LG_CUDA(cudaMemcpy(&in, s->bv.intact + be, 1, cudaMemcpyDeviceToHost));
         if (in) {
             const size_t bs = (size_t)s->bv.bcap * n;
-            for (int q = 0; q < 9; ++q) LG_CUDA(cudaMemcpy(out9 + q, s->bv.xi + q * bs + be, sizeof(double), cudaMemcpyDeviceToHost));
+            for (int q = 0; q < 9; ++q)
+                LG_CUDA(cudaMemcpy(out9 + q, s->bv.xi + spring_at(s->bv.aos, q, be, bs), sizeof(double), cudaMemcpyDeviceToHost));
             spring_values(s, out9);
             return LG_OK;
         }
@@ -1491,7 +1495,8 @@ extern "C" int lg_get_pair_springs(lg_system *s, int64_t i, int64_t j, double *o
     uint32_t fl = 0;
     LG_CUDA(cudaMemcpy(&fl, pv.flags + e, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     if (!(fl & kXiLive)) return LG_OK;  // springs of a slot that is not live are zero
-    for (int q = 0; q < 9; ++q) LG_CUDA(cudaMemcpy(out9 + q, pv.xi + q * xs + e, sizeof(double), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < 9; ++q)
+        LG_CUDA(cudaMemcpy(out9 + q, pv.xi + spring_at(pv.aos, q, e, xs), sizeof(double), cudaMemcpyDeviceToHost));
     spring_values(s, out9);
     return LG_OK;
 }

@@ -217,14 +217,17 @@ __device__ __forceinline__ void contact_item(const Params &P, const PairView &PV
     const bool bonded = (fl & kBonded) != 0;
     int64_t base, stride;
     float2 *store;
+    int32_t aos;
     if (bonded) {
         base = (int64_t)bond_slot_of(fl) * n + io;
         stride = bs;
         store = reinterpret_cast<float2 *>(BV.xi);
+        aos = BV.aos;
     } else {
         base = e;
         stride = xs;
         store = reinterpret_cast<float2 *>(PV.xi);
+        aos = PV.aos;
     }
     // every load the pair may need is issued before any arithmetic (one memory round trip): the
     // partner's low position part, velocities and spin, and the springs of a live slot or bond
@@ -233,7 +236,7 @@ __device__ __forceinline__ void contact_item(const Params &P, const PairView &PV
     if (bonded || (fl & kXiLive))
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
-            const float2 v = store[c * stride + base];
+            const float2 v = store[spring_at(aos, c, base, stride)];
             s[c / 3][c % 3] = ff{v.x, v.y};
         }
     const SepFF sp = separation_ff(W.xh[own], W.xl[own], W.chj[q], lj, bonded ? M.b_fr_hi : M.c_fr_hi,
@@ -273,7 +276,8 @@ __device__ __forceinline__ void contact_item(const Params &P, const PairView &PV
             f_o = shear_ff(s[2], n3, M.c_ko, M.c_go, f_n, M.c_muo, M.c_phio, v_o, M.c_dt, true);
         }
 #pragma unroll
-        for (int c = 0; c < 9; ++c) store[c * stride + base] = make_float2(s[c / 3][c % 3].hi, s[c / 3][c % 3].lo);
+        for (int c = 0; c < 9; ++c)
+            store[spring_at(aos, c, base, stride)] = make_float2(s[c / 3][c % 3].hi, s[c / 3][c % 3].lo);
         force = fadd(fscl(f_n, n3), f_t);
         torque = fadd(fsub(fscl(rr, fcrs(n3, f_r)), fscl(rp, fcrs(n3, f_t))), fscl(rr, f_o));
         if (bonded) {
@@ -289,7 +293,7 @@ __device__ __forceinline__ void contact_item(const Params &P, const PairView &PV
         }
     } else if (fl & kXiLive) {
 #pragma unroll
-        for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+        for (int c = 0; c < 9; ++c) PV.xi[spring_at(PV.aos, c, e, xs)] = 0.0;
         PV.flags[e] = fl & ~kXiLive;
     }
     W.cres[q][0] = force.x * M.bin_im;
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(kCWarps * 32, 8)
                     } else if (fl & kXiLive) {  // reset_springs (contact_force.h:69,99-101)
                         const int64_t e = (int64_t)k * n + i;
 #pragma unroll
-                        for (int c = 0; c < 9; ++c) PV.xi[c * xs + e] = 0.0;
+                        for (int c = 0; c < 9; ++c) PV.xi[spring_at(PV.aos, c, e, xs)] = 0.0;
                         PV.flags[e] = fl & ~kXiLive;
                     }
                 }

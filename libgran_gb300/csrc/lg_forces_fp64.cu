@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
         if (po >= 0) {
             const int64_t oe = (int64_t)po * n + il;
 #pragma unroll
-            for (int q = 0; q < 9; ++q) newv.xi[q * nxs + e] = oldv.xi[q * oxs + oe];
+            for (int q = 0; q < 9; ++q) newv.xi[spring_at(newv.aos, q, e, nxs)] = oldv.xi[spring_at(oldv.aos, q, oe, oxs)];
         }
     }
 }

@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
                 // cannot touch, beyond the limited Hamaker cutoff
                 if (fl & kXiLive) {
 #pragma unroll
-                    for (int q2 = 0; q2 < 9; ++q2) PV.xi[q2 * xs + e] = 0.0;
+                    for (int q2 = 0; q2 < 9; ++q2) PV.xi[spring_at(PV.aos, q2, e, xs)] = 0.0;
                     PV.flags[e] = fl & ~kXiLive;
                 }
                 if (hm == LG_HAMAKER_FULL || hm == LG_HAMAKER_SIMPLIFIED) {
@@ -210,21 +210,24 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
                     d3 s[3];
                     int64_t base, stride;
                     double *store;
+                    int32_t aos;
                     if (bonded) {
                         base = (int64_t)bond_slot_of(fl) * n + i;
                         stride = (int64_t)BV.bcap * n;
                         store = BV.xi;
+                        aos = BV.aos;
                     } else {
                         base = e;
                         stride = xs;
                         store = PV.xi;
+                        aos = PV.aos;
                     }
                     if (bonded || (fl & kXiLive)) {  // springs of a slot that is not live are zero
 #pragma unroll
                         for (int q3 = 0; q3 < 3; ++q3)
-                            s[q3] = mk3(ffslot_load(store, (3 * q3) * stride + base),
-                                        ffslot_load(store, (3 * q3 + 1) * stride + base),
-                                        ffslot_load(store, (3 * q3 + 2) * stride + base));
+                            s[q3] = mk3(ffslot_load(store, spring_at(aos, 3 * q3, base, stride)),
+                                        ffslot_load(store, spring_at(aos, 3 * q3 + 1, base, stride)),
+                                        ffslot_load(store, spring_at(aos, 3 * q3 + 2, base, stride)));
                     } else {
                         s[0] = s[1] = s[2] = zero3();
                     }
@@ -241,9 +244,9 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
                                       nrm_ij, overlap, vij0, wfi, tof(wj), s, force, torque);
 #pragma unroll
                     for (int q3 = 0; q3 < 3; ++q3) {
-                        ffslot_store(store, (3 * q3) * stride + base, s[q3].x);
-                        ffslot_store(store, (3 * q3 + 1) * stride + base, s[q3].y);
-                        ffslot_store(store, (3 * q3 + 2) * stride + base, s[q3].z);
+                        ffslot_store(store, spring_at(aos, 3 * q3, base, stride), s[q3].x);
+                        ffslot_store(store, spring_at(aos, 3 * q3 + 1, base, stride), s[q3].y);
+                        ffslot_store(store, spring_at(aos, 3 * q3 + 2, base, stride), s[q3].z);
                     }
                     if (bonded) {
                         if (breaking && fdot(force, force) > (float)(BV.strength[base] * BV.strength[base])) {
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
                     accum(accw, torque);
                 } else if (fl & kXiLive) {
 #pragma unroll
-                    for (int q2 = 0; q2 < 9; ++q2) PV.xi[q2 * xs + e] = 0.0;
+                    for (int q2 = 0; q2 < 9; ++q2) PV.xi[spring_at(PV.aos, q2, e, xs)] = 0.0;
                     PV.flags[e] = fl & ~kXiLive;
                 }
             }

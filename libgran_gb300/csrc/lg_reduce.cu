@@ -59,9 +59,9 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
             double dl = 2.0 * P.sinter.r_part - dist;
             u += 0.5 * P.sinter.k * dl * dl;
             const bool f = P.springs_ff != 0;
-            d3 s0 = mk3(spring_load(BV.xi, 0 * bs + be, f), spring_load(BV.xi, 1 * bs + be, f), spring_load(BV.xi, 2 * bs + be, f));
-            d3 s1 = mk3(spring_load(BV.xi, 3 * bs + be, f), spring_load(BV.xi, 4 * bs + be, f), spring_load(BV.xi, 5 * bs + be, f));
-            d3 s2 = mk3(spring_load(BV.xi, 6 * bs + be, f), spring_load(BV.xi, 7 * bs + be, f), spring_load(BV.xi, 8 * bs + be, f));
+            d3 s0 = mk3(spring_load(BV.xi, spring_at(BV.aos, 0, be, bs), f), spring_load(BV.xi, spring_at(BV.aos, 1, be, bs), f), spring_load(BV.xi, spring_at(BV.aos, 2, be, bs), f));
+            d3 s1 = mk3(spring_load(BV.xi, spring_at(BV.aos, 3, be, bs), f), spring_load(BV.xi, spring_at(BV.aos, 4, be, bs), f), spring_load(BV.xi, spring_at(BV.aos, 5, be, bs), f));
+            d3 s2 = mk3(spring_load(BV.xi, spring_at(BV.aos, 6, be, bs), f), spring_load(BV.xi, spring_at(BV.aos, 7, be, bs), f), spring_load(BV.xi, spring_at(BV.aos, 8, be, bs), f));
             u += 0.5 * P.sinter.k_t * sqn(s0) + 0.5 * P.sinter.k_r * sqn(s1) + 0.5 * P.sinter.k_o * sqn(s2);
             nbond += 1.0;
         } else if (P.binary_model != LG_BINARY_NONE) {
@@ -72,9 +72,9 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
             }
             if (fl & kXiLive) {
                 const bool f = P.springs_ff != 0;
-                d3 s0 = mk3(spring_load(PV.xi, 0 * xs + e, f), spring_load(PV.xi, 1 * xs + e, f), spring_load(PV.xi, 2 * xs + e, f));
-                d3 s1 = mk3(spring_load(PV.xi, 3 * xs + e, f), spring_load(PV.xi, 4 * xs + e, f), spring_load(PV.xi, 5 * xs + e, f));
-                d3 s2 = mk3(spring_load(PV.xi, 6 * xs + e, f), spring_load(PV.xi, 7 * xs + e, f), spring_load(PV.xi, 8 * xs + e, f));
+                d3 s0 = mk3(spring_load(PV.xi, spring_at(PV.aos, 0, e, xs), f), spring_load(PV.xi, spring_at(PV.aos, 1, e, xs), f), spring_load(PV.xi, spring_at(PV.aos, 2, e, xs), f));
+                d3 s1 = mk3(spring_load(PV.xi, spring_at(PV.aos, 3, e, xs), f), spring_load(PV.xi, spring_at(PV.aos, 4, e, xs), f), spring_load(PV.xi, spring_at(PV.aos, 5, e, xs), f));
+                d3 s2 = mk3(spring_load(PV.xi, spring_at(PV.aos, 6, e, xs), f), spring_load(PV.xi, spring_at(PV.aos, 7, e, xs), f), spring_load(PV.xi, spring_at(PV.aos, 8, e, xs), f));
                 u += 0.5 * P.contact.k_t * sqn(s0) + 0.5 * P.contact.k_r * sqn(s1) + 0.5 * P.contact.k_o * sqn(s2);
             }
         }
