@@ -57,8 +57,9 @@ __device__ __forceinline__ void ffslot_store(double *p, int64_t idx, double d) {
     const float hi = (float)d;
     reinterpret_cast<float2 *>(p)[idx] = make_float2(hi, (float)(d - (double)hi));
 }
-// Position of particle i relative to its system's origin as a float-float pair: x32[i] receives
-// the FP32 rounding of the FP64 difference, x32[n + i] the FP32 rounding of what that leaves.
+// Position of particle i relative to its system's origin as a float-float pair, interleaved (one
+// 32-byte sector per particle): x32[2i] receives the FP32 rounding of the FP64 difference,
+// x32[2i + 1] the FP32 rounding of what that leaves.
 __device__ __forceinline__ void rel_ff(d3 q, double ox, double oy, double oz, const int32_t *agg, const dbl4 *orig,
                                        int64_t i, int64_t n, float4 *__restrict__ x32) {
     if (agg) {
@@ -69,8 +70,9 @@ __device__ __forceinline__ void rel_ff(d3 q, double ox, double oy, double oz, co
     }
     const double rx = q.x - ox, ry = q.y - oy, rz = q.z - oz;
     const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
-    x32[i] = make_float4(hx, hy, hz, 0.0f);
-    x32[n + i] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.0f);
+    (void)n;
+    x32[2 * i] = make_float4(hx, hy, hz, 0.0f);
+    x32[2 * i + 1] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.0f);
 }
 
 // Velocity copies of the mixed compacted kernel: v32[i] / v32[n + i] = high / low FP32 parts of v_i,

@@ -981,7 +981,6 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         if (d->hamaker_model == LG_HAMAKER_FULL || d->hamaker_model == LG_HAMAKER_SIMPLIFIED)
             near = std::max(near, 7.0 * d->hamaker.r_part);
         s->mx.x32 = s->x32;
-        s->mx.x32lo = s->x32 + n;
         s->mx.v32 = s->v32;
         s->mx.s32 = s->s32;
         s->mx.csum = s->csum;

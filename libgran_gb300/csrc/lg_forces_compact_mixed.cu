@@ -17,7 +17,7 @@
 //   forces_finish_mixed    per particle: contact part + Hamaker part, facet terms, stores, half kick;
 //                          within a run of steps also the next step's half kick and drift.
 //
-// Precision: positions come as float-float pairs (MixedExtra::x32 / x32lo, hi + lo = x - origin) and
+// Precision: positions come as float-float pairs (MixedExtra::x32, hi + lo = x - origin) and
 // a pair's separation and q = |d|^2 - (2r)^2 are formed with error-free FP32 transformations
 // (separation_ff), so the surface gap and the overlap keep FP32 relative precision however small
 // they are; velocities come as float-float copies (MixedExtra::v32); springs are float-float pairs
@@ -47,6 +47,9 @@ using compact::slot_of;
 constexpr int kCRound = 32;  // entries per lane classified per round
 constexpr int kCQ = 64;      // contact queue capacity (>= 32 + 31)
 constexpr int kCWarps = 2;   // warps per block
+#ifndef LG_HAMAKER_REGS
+#define LG_HAMAKER_REGS 80  // register budget of the Hamaker kernel (compile-time override for tuning)
+#endif
 #ifndef LG_CONTACT_LANES
 #define LG_CONTACT_LANES 2   // lanes per row (compile-time override for tuning)
 #endif
@@ -71,8 +74,8 @@ struct ShapeH {
     static constexpr int kSlices = SL;
     static constexpr int kRowWarps = SL == 1 ? 2 : 1;  // 32-row groups per block
     static constexpr int kWarps = kSlices * kRowWarps;
-    // blocks per SM that a 96-register budget allows (shared memory allows as many)
-    static constexpr int kMinBlocks = 65536 / (kWarps * 32 * 96);
+    // blocks per SM that the register budget allows (shared memory allows as many)
+    static constexpr int kMinBlocks = 65536 / (kWarps * 32 * LG_HAMAKER_REGS);
 };
 struct HamakerSmem {
     float4 hhi[kHCap];     // queued Hamaker partners: high part of the position, w = owner lane
@@ -231,7 +234,7 @@ __device__ __forceinline__ void contact_item(const Params &P, const PairView &PV
     }
     // every load the pair may need is issued before any arithmetic (one memory round trip): the
     // partner's low position part, velocities and spin, and the springs of a live slot or bond
-    const float4 lj = M.x32lo[j], vhj = M.v32[j], vlj = M.v32[n + j], wj4 = M.v32[2 * n + j];
+    const float4 lj = M.x32[2 * j + 1], vhj = M.v32[j], vlj = M.v32[n + j], wj4 = M.v32[2 * n + j];
     ff s[3][3] = {};  // springs of a slot that is not live are zero
     if (bonded || (fl & kXiLive))
 #pragma unroll
@@ -349,12 +352,12 @@ __global__ void __launch_bounds__(kCWarps * 32, 8)
     float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
         len = NEAR ? (int64_t)PV.near_len[i] : n - 1;
-        hi_i = MX.x32[i];
+        hi_i = MX.x32[2 * i];
     }
     if (sub == 0) {
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         W.xh[r] = hi_i;
-        W.xl[r] = active ? MX.x32lo[i] : z4;
+        W.xl[r] = active ? MX.x32[2 * i + 1] : z4;
         W.vh[r] = active ? MX.v32[i] : z4;
         W.vl[r] = active ? MX.v32[n + i] : z4;
         W.wh[r] = active ? MX.v32[2 * n + i] : z4;
@@ -393,7 +396,7 @@ __global__ void __launch_bounds__(kCWarps * 32, 8)
         pjc = hi_i;
         if (jc >= 0) {
             flc = PV.flags[(int64_t)kc * n + i];
-            pjc = MX.x32[jc];
+            pjc = MX.x32[2 * jc];
         }
     };
     if (itmax > 0) {
@@ -515,8 +518,8 @@ __global__ void __launch_bounds__(ShapeH<SL>::kWarps * 32, ShapeH<SL>::kMinBlock
         float4 lo_i = hi_i;
         if (active) {
             len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
-            hi_i = MX.x32[i];
-            lo_i = MX.x32lo[i];
+            hi_i = MX.x32[2 * i];
+            lo_i = MX.x32[2 * i + 1];
         }
         W.xh[lane] = hi_i;
         W.xl[lane] = lo_i;
@@ -552,8 +555,8 @@ __global__ void __launch_bounds__(ShapeH<SL>::kWarps * 32, ShapeH<SL>::kMinBlock
             ph[u] = hi_i;
             pl[u] = make_float4(0.f, 0.f, 0.f, 0.f);
             if (jg[u] >= 0) {
-                ph[u] = MX.x32[jg[u]];
-                pl[u] = MX.x32lo[jg[u]];
+                ph[u] = MX.x32[2 * jg[u]];
+                pl[u] = MX.x32[2 * jg[u] + 1];
             }
         }
         if (k + kWin < vmax) load_window(k + kWin);  // next window, in flight during this one
@@ -749,7 +752,7 @@ __global__ void __launch_bounds__(64) forces_finish_ff(Params P, StateView S, in
         return;
     }
     // the next step's opening half kick and drift
-    const float4 xh = MX.x32[i], xl = MX.x32[n + i];
+    const float4 xh = MX.x32[2 * i], xl = MX.x32[2 * i + 1];
     ff x[3] = {{xh.x, xl.x}, {xh.y, xl.y}, {xh.z, xl.z}};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -760,8 +763,8 @@ __global__ void __launch_bounds__(64) forces_finish_ff(Params P, StateView S, in
         dx[c] = ff_add(dx[c], step);
         dr[c] = ff_add(dr[c], ff_mul(dt, w[c]));
     }
-    MX.x32[i] = make_float4(x[0].hi, x[1].hi, x[2].hi, 0.f);
-    MX.x32[n + i] = make_float4(x[0].lo, x[1].lo, x[2].lo, 0.f);
+    MX.x32[2 * i] = make_float4(x[0].hi, x[1].hi, x[2].hi, 0.f);
+    MX.x32[2 * i + 1] = make_float4(x[0].lo, x[1].lo, x[2].lo, 0.f);
     MX.v32[i] = make_float4(v[0].hi, v[1].hi, v[2].hi, 0.f);
     MX.v32[n + i] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
     MX.v32[2 * n + i] = make_float4(w[0].hi, w[1].hi, w[2].hi, 0.f);

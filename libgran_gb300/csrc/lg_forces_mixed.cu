@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
         wi = ld4(S.w, i);
         vfi = tof(vi);
         wfi = tof(wi);
-        float4 q = MX.x32[i];
+        float4 q = MX.x32[2 * i];
         xfi = fm(q.x, q.y, q.z);
         const int64_t len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
         const int64_t xs = PV.cap * n;
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
             const int64_t e = k * n + i;
             const int64_t j = VERLET ? (int64_t)PV.nbr[e] : (k < i ? k : k + 1);
             const uint32_t fl = PV.flags[e];
-            const float4 qj = MX.x32[j];
+            const float4 qj = MX.x32[2 * j];
             const f3 d32 = fm(xfi.x - qj.x, xfi.y - qj.y, xfi.z - qj.z);
             const float d2f = fdot(d32, d32);
             const bool bonded = (fl & kBonded) && bm != LG_BINARY_NONE;

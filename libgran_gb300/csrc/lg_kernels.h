@@ -61,11 +61,11 @@ void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, double 
 
 // Mixed-precision path (lg_forces_mixed.cu)
 struct MixedExtra {
-    // [2n] positions relative to the system origin as float-float pairs: x32[i] = FP32 rounding of
-    // x_i - origin (culling, and the high part), x32lo[i] = x32[n + i] = FP32 rounding of the
-    // remainder (x_i - origin) - x32[i]; hi + lo holds the position to about 2^-48 of its magnitude
+    // [2n] positions relative to the system origin as interleaved float-float pairs: x32[2i] = FP32
+    // rounding of x_i - origin (culling, and the high part), x32[2i + 1] = FP32 rounding of the
+    // remainder; hi + lo holds the position to about 2^-48 of its magnitude, and a partner's pair
+    // is one 32-byte sector
     float4 *x32;
-    const float4 *x32lo;
     // [3n] velocities of the force evaluation: v32[i] / v32[n + i] = high / low FP32 parts of v_i,
     // v32[2n + i] = FP32 rounding of omega_i (compacted kernel's contact and bond pairs)
     float4 *v32;
