@@ -48,7 +48,18 @@ constexpr int kCRound = 32;  // entries per lane classified per round
 constexpr int kCQ = 64;      // contact queue capacity (>= 32 + 31)
 constexpr int kCWarps = 2;   // warps per block
 #ifndef LG_HAMAKER_REGS
-#define LG_HAMAKER_REGS 80  // register budget of the Hamaker kernel (compile-time override for tuning)
+#define LG_HAMAKER_REGS 96  // register budget of the Hamaker kernel (compile-time override for tuning)
+#endif
+// Resident blocks per SM the contact kernel is compiled for (its register budget): beside the Hamaker
+// kernel (two streams) a tighter budget lets more of both kernels' warps share an SM; alone, the
+// looser one avoids spills. Measured on the 32768-particle workload (graph-replayed steps): 12 blocks
+// beside the Hamaker kernel, 9.3e8 against 8.2e8 particle-steps/s with 8; contacts alone, 8 blocks,
+// 30 against 36 us per step with 12.
+#ifndef LG_CONTACT_MIN_BLOCKS
+#define LG_CONTACT_MIN_BLOCKS 12
+#endif
+#ifndef LG_CONTACT_MIN_BLOCKS_ALONE
+#define LG_CONTACT_MIN_BLOCKS_ALONE 8
 #endif
 #ifndef LG_CONTACT_LANES
 #define LG_CONTACT_LANES 2   // lanes per row (compile-time override for tuning)
@@ -335,8 +346,8 @@ __device__ __forceinline__ void hamaker_item(const Params &P, const MixedExtra &
 // its entries t, t + T, ... (so short candidate lists still fill the warp); each lane folds its
 // pairs in entry order and the row's T partial sums are combined in lane order. csum receives the
 // contact part of the row's accelerations as float-float pairs.
-template <bool NEAR, int T>
-__global__ void __launch_bounds__(kCWarps * 32, 8)
+template <bool NEAR, int T, int MINB>
+__global__ void __launch_bounds__(kCWarps * 32, MINB)
     forces_contacts_mixed(Params P, StateView S, PairView PV, BondView BV, MixedExtra MX) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int kRows = 32 / T;
@@ -779,12 +790,15 @@ namespace {
 
 template <bool NEAR>
 void launch_contacts(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, const MixedExtra &MX,
-                     cudaStream_t st) {
+                     cudaStream_t st, bool beside_hamaker) {
     constexpr int T = kContactLanes;
     const size_t smem = sizeof(ContactSmem) * kCWarps;
     const int64_t rows_per_block = (32 / T) * kCWarps;
     const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
-    forces_contacts_mixed<NEAR, T><<<blocks, kCWarps * 32, smem, st>>>(P, S, PV, BV, MX);
+    if (beside_hamaker)
+        forces_contacts_mixed<NEAR, T, LG_CONTACT_MIN_BLOCKS><<<blocks, kCWarps * 32, smem, st>>>(P, S, PV, BV, MX);
+    else
+        forces_contacts_mixed<NEAR, T, LG_CONTACT_MIN_BLOCKS_ALONE><<<blocks, kCWarps * 32, smem, st>>>(P, S, PV, BV, MX);
 }
 
 template <bool VERLET, int SL>
@@ -830,9 +844,9 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         cudaEventRecord(fork, st);
         cudaStreamWaitEvent(side, fork, 0);
         if (ver && PV.near_len)
-            launch_contacts<true>(P, S, PV, BV, MX, side);
+            launch_contacts<true>(P, S, PV, BV, MX, side, hamaker != 0);
         else
-            launch_contacts<false>(P, S, PV, BV, MX, side);
+            launch_contacts<false>(P, S, PV, BV, MX, side, hamaker != 0);
         ++kernels;
     }
     if (hamaker) {
