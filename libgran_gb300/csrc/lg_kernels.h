@@ -150,7 +150,6 @@ void launch_dev4_to_aos(int64_t n, const dbl4 *src, double *aos, cudaStream_t st
 int64_t obs_scratch_doubles(int64_t n);
 void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
                         double inertia, double *scratch, double *out, cudaStream_t st, bool pairs = true);
-void launch_observables_rg(int64_t n, const dbl4 *x, double *scratch, double *out, cudaStream_t st);
 // Handle observables: out[0..14] and out[18] from the particles (launch_observables_state), out[15..17]
 // from the pair slots (launch_observables_pairs); scratch as above.
 void launch_observables_state(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, double mass, double inertia,

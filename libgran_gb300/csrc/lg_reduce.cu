@@ -94,14 +94,6 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
 }
 
 // |x - c|^2 per particle into column 18; c = (column sums 12..14) / n, read from device memory.
-__global__ void obs_rg(int64_t n, const dbl4 *__restrict__ x, const double *__restrict__ sums, double *__restrict__ out) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double nn = (double)n;
-    d3 q = sub(ld4(x, i), mk3(sums[12] / nn, sums[13] / nn, sums[14] / nn));
-    out[i * kObs + 18] = dot(q, q);
-}
-
 // One block of 1024 threads: thread t sums rows t, t + 1024, ... in order, then a fixed tree.
 __global__ void __launch_bounds__(1024) obs_reduce(int64_t n, const double *__restrict__ rows, int c0, int c1,
                                                    double *__restrict__ out) {
@@ -128,18 +120,6 @@ int64_t obs_scratch_doubles(int64_t n) { return n * kObs; }
 // give the centre of mass on the device, which the radius-of-gyration pass reads back.
 constexpr int kObsBlock = 256;
 constexpr int kObsCols = 16;  // 15 terms + |x - c|^2
-
-__device__ __forceinline__ double obs_block_sum(double v, double *sh) {
-    sh[threadIdx.x] = v;
-    __syncthreads();
-    for (int o = kObsBlock / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    const double r = sh[0];
-    __syncthreads();
-    return r;
-}
 
 // Block sums of C columns in a fixed order: a butterfly over the warp's lanes, then the kObsBlock /
 // 32 warp sums in warp order by thread c < C; the result row goes to part[blockIdx.x].
@@ -260,12 +240,6 @@ void launch_observables(const Params &P, const StateView &S, const PairView &PV,
     obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 0, 18, out);
 }
 
-// out[18] = sum |x - c|^2 with c from out[12..14] / n (after launch_observables, same stream).
-void launch_observables_rg(int64_t n, const dbl4 *x, double *scratch, double *out, cudaStream_t st) {
-    const unsigned blocks = (unsigned)((n + 255) / 256);
-    obs_rg<<<blocks, 256, 0, st>>>(n, x, out, scratch);
-    obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 18, 19, out);
-}
 
 // One block per system: fixed-order sums of the system's scratch rows (columns 0..17).
 __global__ void __launch_bounds__(256) seg_sums(const int64_t *__restrict__ off, const double *__restrict__ rows,
