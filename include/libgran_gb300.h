@@ -199,7 +199,8 @@ typedef struct lg_system_desc {
 /* Force kernels. Both give deterministic sums; in FP64 both add each row in ascending j, and the
  * compacted kernel and the row-group kernel with one lane per row are bit-identical to a
  * sequential evaluation of libgran's functors. */
-#define LG_FORCE_KERNEL_AUTO 0       /* compacted for large systems, row groups for small ones */
+#define LG_FORCE_KERNEL_AUTO 0       /* mixed: compacted; FP64: pair-parallel for small systems, compacted
+                                       for large ones */
 #define LG_FORCE_KERNEL_ROWGROUP 1   /* T lanes per row (threads_per_row), fixed butterfly combine */
 #define LG_FORCE_KERNEL_COMPACT 2    /* one row per lane, warp-compacted pair queues (see csrc) */
 #define LG_FORCE_KERNEL_PAIRS 3      /* FP64, small systems: one thread per pair slot spread over all SMs,

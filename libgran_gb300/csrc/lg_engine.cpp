@@ -371,6 +371,10 @@ static int choose_kernel(const lg_system *s, int requested) {
     if (requested == LG_FORCE_KERNEL_ROWGROUP || requested == LG_FORCE_KERNEL_COMPACT) return requested;
     if (requested == LG_FORCE_KERNEL_PAIRS) return s->pres ? requested : -1;
     const int64_t n = s->P.n;
+    // mixed precision: the compacted kernels at every size (their float-float completion and fused
+    // runs of steps also make small systems fastest: 19 particles 13.7 against 36.9 us a step, 1000
+    // particles 15.4 against 47.7 us, on GB300 with the row-group kernel)
+    if (s->precision == LG_PRECISION_MIXED) return LG_FORCE_KERNEL_COMPACT;
     if (s->pres && (int64_t)s->pv[0].cap * n <= kPairsAutoSlots) return LG_FORCE_KERNEL_PAIRS;
     if (s->P.pairs == LG_PAIRS_VERLET ? n >= 1024 : n >= 4096) return LG_FORCE_KERNEL_COMPACT;
     return LG_FORCE_KERNEL_ROWGROUP;
