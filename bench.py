@@ -281,8 +281,9 @@ def batched_section(args, l2_flush):
     handles = [System(desc(int(sizes[a]), A.LG_PRECISION_MIXED),
                       x0[int(sizes[:a].sum()):int(sizes[:a + 1].sum())],
                       v0[int(sizes[:a].sum()):int(sizes[:a + 1].sum())]) for a in range(sample)]
-    for h in handles:
-        h.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+    for _ in range(3):  # both list parities replayed once, so the graphs are captured before timing
+        for h in handles:
+            h.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
     import torch
     torch.cuda.synchronize()
     t = time.perf_counter()
