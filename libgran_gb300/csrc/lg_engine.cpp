@@ -509,6 +509,30 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_n
     return LG_OK;
 }
 
+// Hold mask of n particles: only LG_HOLD_* bits.
+static int validate_hold(const uint8_t *mask, int64_t n) {
+    if (!mask) return LG_OK;
+    for (int64_t i = 0; i < n; ++i)
+        if (mask[i] & ~(LG_HOLD_X | LG_HOLD_V | LG_HOLD_THETA | LG_HOLD_OMEGA))
+            return lg_fail(LG_E_INVALID, "hold mask: particle %lld has unknown bits 0x%x", (long long)i, mask[i]);
+    return LG_OK;
+}
+
+// Body force (null: none) and unary hook (null: none): a known model, finite parameters, not both.
+static int validate_unary(const lg_body_force *body, lg_unary_hook hook) {
+    const int model = body ? body->model : LG_BODY_NONE;
+    if (model != LG_BODY_NONE && model != LG_BODY_CENTRAL)
+        return lg_fail(LG_E_INVALID, "body force: unknown model %d", model);
+    if (model != LG_BODY_NONE && hook) return lg_fail(LG_E_INVALID, "a body force and a unary hook exclude each other");
+    if (model == LG_BODY_CENTRAL) {
+        if (!(body->mass > 0) || !std::isfinite(body->mass) || !std::isfinite(body->k_a))
+            return lg_fail(LG_E_INVALID, "body force: mass must be positive and k_a finite");
+        for (int c = 0; c < 3; ++c)
+            if (!std::isfinite(body->centre[c])) return lg_fail(LG_E_INVALID, "body force: centre is not finite");
+    }
+    return LG_OK;
+}
+
 static int check_args(const lg_system_desc *d) {
     if (!d) return lg_fail(LG_E_INVALID, "lg_create: null descriptor");
     if (d->n_part < 1 || d->n_part > (int64_t)1 << 30) return lg_fail(LG_E_INVALID, "lg_create: n_part %lld out of range", (long long)d->n_part);
@@ -529,6 +553,8 @@ static int check_args(const lg_system_desc *d) {
     if (d->max_neighbors < 0 || d->max_neighbors > 255)
         return lg_fail(LG_E_INVALID, "lg_create: max_neighbors must be in [0, 255]");
     if (d->force_kernel < 0 || d->force_kernel > 3) return lg_fail(LG_E_INVALID, "lg_create: unknown force_kernel %d", d->force_kernel);
+    LG_TRY(validate_hold(d->hold_mask, d->n_part));
+    LG_TRY(validate_unary(&d->body, d->unary_hook));
     if (d->force_kernel == LG_FORCE_KERNEL_PAIRS && d->precision != LG_PRECISION_FP64)
         return lg_fail(LG_E_INVALID, "lg_create: the pair-parallel force kernel is FP64 only");
     {
@@ -542,14 +568,12 @@ static int check_args(const lg_system_desc *d) {
 // Hold mask (LG_HOLD_* bits per particle); null clears it. Params are captured by value in the
 // CUDA graphs, so the graphs are dropped.
 static int apply_hold(lg_system *s, const uint8_t *mask) {
+    LG_TRY(validate_hold(mask, s->P.n));
     s->drop_graphs();
     if (!mask) {
         s->P.hold = nullptr;
         return LG_OK;
     }
-    for (int64_t i = 0; i < s->P.n; ++i)
-        if (mask[i] & ~(LG_HOLD_X | LG_HOLD_V | LG_HOLD_THETA | LG_HOLD_OMEGA))
-            return lg_fail(LG_E_INVALID, "hold mask: particle %lld has unknown bits 0x%x", (long long)i, mask[i]);
     if (!s->d_hold) LG_TRY(s->alloc(&s->d_hold, (size_t)s->P.n));
     LG_CUDA(cudaMemcpyAsync(s->d_hold, mask, (size_t)s->P.n, cudaMemcpyHostToDevice, s->stream));
     LG_CUDA(cudaStreamSynchronize(s->stream));
@@ -560,16 +584,8 @@ static int apply_hold(lg_system *s, const uint8_t *mask) {
 // Body force or unary hook (at most one); both write the per-particle unary terms that the force
 // kernels fold after the facets.
 static int apply_unary(lg_system *s, const lg_body_force *body, lg_unary_hook hook, void *user) {
+    LG_TRY(validate_unary(body, hook));
     const int model = body ? body->model : LG_BODY_NONE;
-    if (model != LG_BODY_NONE && model != LG_BODY_CENTRAL)
-        return lg_fail(LG_E_INVALID, "body force: unknown model %d", model);
-    if (model != LG_BODY_NONE && hook) return lg_fail(LG_E_INVALID, "a body force and a unary hook exclude each other");
-    if (model == LG_BODY_CENTRAL) {
-        if (!(body->mass > 0) || !std::isfinite(body->mass) || !std::isfinite(body->k_a))
-            return lg_fail(LG_E_INVALID, "body force: mass must be positive and k_a finite");
-        for (int c = 0; c < 3; ++c)
-            if (!std::isfinite(body->centre[c])) return lg_fail(LG_E_INVALID, "body force: centre is not finite");
-    }
     s->drop_graphs();
     const bool on = model != LG_BODY_NONE || hook;
     if (on && !s->ext_a) {

@@ -54,7 +54,22 @@ def test_create_rejects_bad_descriptors_before_touching_a_gpu():
         K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), pairs=A.LG_PAIRS_VERLET, r_verlet=0.0),
         K.make_desc(10000, A.LG_BINARY_CONTACT, contact=mat.contact(), pairs=A.LG_PAIRS_ALL),
         K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), n_facets=9),
+        K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), precision=A.LG_PRECISION_MIXED,
+                    force_kernel=A.LG_FORCE_KERNEL_PAIRS),
     ]
+    d = K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact())
+    K.set_hold(d, np.array([0, 16, 0, 0], dtype=np.uint8))  # unknown bit
+    bad.append(d)
+    for body in (K.central_body(1e-6, 0.0, (0.0, 0.0, 0.0)), K.central_body(1e-6, 1e-20, (np.inf, 0.0, 0.0)),
+                 A.lg_body_force(7, 1e-6, 1e-20, (C.c_double * 3)())):
+        d = K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact())
+        d.body = body
+        bad.append(d)
+    hook = A.lg_unary_hook(lambda args, user: 0)
+    d = K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact())
+    d.body = K.central_body(1e-6, 1e-20, (0.0, 0.0, 0.0))
+    d.unary_hook = hook
+    bad.append(d)
     for d in bad:
         rc, h = _create(d, max(int(d.n_part), 1))
         assert rc == A.LG_E_INVALID
