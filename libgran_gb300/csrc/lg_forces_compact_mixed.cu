@@ -14,15 +14,19 @@
 //                          window's partners are loaded meanwhile. For launches with few rows a
 //                          row's windows are sliced over SL warps, whose partial sums are combined
 //                          in slice order. Runs beside forces_contacts_mixed (two streams).
-//   forces_finish_mixed    per particle: contact part + Hamaker part, facet terms, stores, half kick;
-//                          within a run of steps also the next step's half kick and drift.
+//   forces_finish_ff       completion inside a run of steps (no facets, no body term): the sums, the
+//                          end-of-step half kick, the next step's half kick and drift, all in
+//                          float-float on the FP32 pipes; the run's last step writes the FP64 state.
+//   forces_finish_mixed    the FP64 completion (facets, body terms, single steps): contact part +
+//                          Hamaker part to FP64, unary terms, stores, half kick (+ next kick and
+//                          drift).
 //
-// Precision: positions come as float-float pairs (MixedExtra::x32, hi + lo = x - origin) and
-// a pair's separation and q = |d|^2 - (2r)^2 are formed with error-free FP32 transformations
-// (separation_ff), so the surface gap and the overlap keep FP32 relative precision however small
-// they are; velocities come as float-float copies (MixedExtra::v32); springs are float-float pairs
-// in the 8-byte spring slots, updated by FP32 increments (shear_ff). No pair costs an FP64
-// operation. Per-row sums are float-float (compensated) FP32 accumulations in an order fixed by
+// Precision: positions come as interleaved float-float pairs (MixedExtra::x32, hi + lo = x -
+// origin) and a pair's separation and q = |d|^2 - (2r)^2 are formed with error-free FP32
+// transformations (separation_ff), so the surface gap and the overlap keep FP32 relative precision
+// however small they are; velocities come as float-float copies (MixedExtra::v32); springs are
+// float-float pairs in 8-byte slots, one 9-component record per slot or bond (spring_at), updated
+// by FP32 increments (shear_ff). No pair costs an FP64 operation. Per-row sums are float-float (compensated) FP32 accumulations in an order fixed by
 // the row alone, so a system gives the same bits alone and inside a batch (with the same slicing).
 #include <cstddef>
 

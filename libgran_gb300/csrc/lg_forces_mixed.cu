@@ -1,4 +1,6 @@
-// lg_forces_mixed.cu -- mixed-precision force kernel (sm_103a).
+// lg_forces_mixed.cu -- mixed-precision row-group force kernel (sm_103a; on request or by the
+// autotuner: the compacted kernels of lg_forces_compact_mixed.cu are the automatic choice), the
+// mixed drift and the float-float copies.
 //
 // Which steps keep FP64 and why (GB300 issues FP64 at about 1/58 of its FP32 rate, so every FP64
 // operation here is spent where cancellation or accumulation needs it):
@@ -9,10 +11,10 @@
 //         force/torque sums, and the velocity-Verlet integration.
 //   FP32  everything else in the pair: unit normal, relative velocities, normal force, Coulomb
 //         test, torques, the Hamaker bracket (rewritten with two reciprocals).
-// Pairs are culled with an FP32 copy of the positions (relative to a per-system origin) against a
-// radius with a 1e-3 margin, so pairs that cannot touch and lie beyond the Hamaker cutoff cost no
-// FP64 work. Row groups, slot layout, flags and springs are shared with the FP64 path
-// (lg_common.cuh), so a system can switch precision between steps.
+// Pairs are culled with the high parts of the float-float positions (relative to a per-system
+// origin) against a radius with a 1e-3 margin, so pairs that cannot touch and lie beyond the
+// Hamaker cutoff cost no FP64 work. Row groups, slot layout and flags are shared with the FP64 path
+// (lg_common.cuh); springs use the mixed path's float-float records (spring_at).
 #include "lg_compact.cuh"
 #include "lg_kernels.h"
 
