@@ -1,5 +1,7 @@
-// lg_engine.cpp -- host side of the C ABI (include/libgran_gb300.h): handle lifetime, bond
-// detection, state transfer, the step loop, Verlet-list management and read-back.
+// lg_engine.cpp -- host side of the C ABI (include/libgran_gb300.h): handle lifetime, bond and
+// connector set-up, state transfer, the step loop (CUDA graphs per rebuild period, the choice of
+// force kernel and the autotuner), Verlet-list management, body forces, hooks and hold masks,
+// snapshots and read-back.
 //
 // Built with -ffp-contract=off: the few host computations that feed the kernels (bond detection,
 // facet area and normal) use the reference's arithmetic exactly.

@@ -1,8 +1,9 @@
 // lg_reduce.cu -- observables of the system state (test/compute_energy.cpp:7-58 and
 // test/mass_distribution.cpp:7-27 of libgran) plus the potential-energy bookkeeping used for
-// energy-balance checks. Each particle writes its terms to a scratch row; one block then reduces
-// the rows in a fixed order (strided sequential sums followed by a fixed tree), so the result is
-// identical run to run. No floating-point atomics.
+// energy-balance checks, and the state transfers between the caller's [n][3] arrays and the
+// device layout. Every sum is taken in a fixed order (per-particle rows reduced by one block, or
+// block rows combined by the last block to finish), so results are identical run to run. No
+// floating-point atomics.
 #include "lg_common.cuh"
 #include "lg_kernels.h"
 
