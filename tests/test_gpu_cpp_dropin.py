@@ -1,8 +1,8 @@
 """The C++ drop-in headers (include/libgran_gb300/libgran/...): a libgran-style driver with the
 template composition of libgran's test/hamaker.cpp and test/hamaker_neighbor.cpp, compiled against
 the drop-in headers and the engine library. A 20000-step run must match the oracle's end state; the
-full 3e6-step run (libgran's own 1 % targets; about 5 minutes per mode on a GB300, where FP64 on a
-19-particle system is latency-bound) runs when LG_LONG_TESTS=1."""
+full 3e6-step run (libgran's own 1 % targets; about 2 minutes per mode on a GB300, where FP64 on a
+19-particle system is latency-bound at about 37 us a step) runs when LG_LONG_TESTS=1."""
 import os
 import subprocess
 
