@@ -198,3 +198,25 @@ def test_known_answers_of_libgran():
         m = KA.measured(c, o0, s.observables())
         for k, tv in c["targets"].items():
             assert abs(m[k] - tv) / tv < 0.01, (c["name"], k, m[k], tv)
+
+
+def test_c0_configuration_matches_reference_harness():
+    """The reference's CPU-runnable configuration: 256 monomers, alt_sinter bonds with the inner
+    contact functor and the full Hamaker functor, all pairs; 40 steps of the oracle equal libgran's
+    own functors on the same loop, bit for bit."""
+    _harness_or_skip()
+    mat = K.Material()
+    n = 256
+    x0 = generate_aggregate(0, n, mat.r)
+    v0 = generate_velocities(0, n, 0.1)
+    d = K.make_desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_FULL, contact=mat.contact(), sinter=mat.sinter(),
+                    hamaker=mat.hamaker())
+    ref = O.RefHarnessSystem(d, x0, v0)
+    orc = O.OracleSystem(d, x0, v0, threads=4)
+    for _ in range(2):
+        ref.step(mat.dt, 20)
+        orc.step(mat.dt, 20)
+        for f in H.FIELDS:
+            assert np.array_equal(orc.get(f), ref.get(f)), H.FIELD_NAMES[f]
+    assert np.array_equal(orc.bonds(), ref.bonds())
+    assert len(orc.bonds()) > 0
