@@ -15,13 +15,11 @@ shard without a halo exchange); value = all ranks' particle-steps / max rank tim
 """
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np

@@ -6,7 +6,6 @@ full 3e6-step run (libgran's own 1 % targets; about 2 minutes per mode on a GB30
 import os
 import subprocess
 
-import numpy as np
 import pytest
 
 import known_answer as KA

@@ -5,7 +5,6 @@ code that must not stall other streams). It is checked against the handle's own
 lg_get_observables on the same state, within the tolerance of the other observable tests, on two
 calls in a row (its fixed scratch keeps the previous call's contents). This file sorts last so that
 a run stopping at the first failure has run every other test before it."""
-import ctypes as C
 
 import numpy as np
 import pytest
