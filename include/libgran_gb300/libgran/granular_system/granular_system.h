@@ -172,6 +172,9 @@ public:
     field_container_t const &get_v() { return fetch(LG_FIELD_V, v); }
     field_container_t const &get_theta() { return fetch(LG_FIELD_THETA, theta); }
     field_container_t const &get_omega() { return fetch(LG_FIELD_OMEGA, omega); }
+    // Extension: the accelerations of the last force evaluation (libgran's a / alpha buffers).
+    field_container_t const &get_a() { return fetch(LG_FIELD_A, a); }
+    field_container_t const &get_alpha() { return fetch(LG_FIELD_ALPHA, alpha); }
     void reset_acceleration_buffers() { libgran_gb300::check(lg_reset_acceleration_buffers(sys), "reset"); }
     lg_system *handle() { return sys; }
 
@@ -217,7 +220,7 @@ private:
         return cache;
     }
     size_t n = 0;
-    field_container_t x, v, theta, omega;
+    field_container_t x, v, theta, omega, a, alpha;
 };
 
 #endif

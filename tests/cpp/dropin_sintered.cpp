@@ -99,6 +99,7 @@ int main(int argc, char **argv) {
     double rg0, rg;
     centre_and_rg(system.get_x(), c0, rg0);
     system.do_steps(dt, (int64_t)n_steps, 0);
+    if (system.get_a().size() != x0.size() || system.get_alpha().size() != x0.size()) return 3;
     centre_and_rg(system.get_x(), c1, rg);
     const double cd = (c1 - c0).norm();
     std::printf("rg %.9e centre_displacement %.9e\n", rg, cd);
