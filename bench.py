@@ -42,13 +42,30 @@ def workload_desc(precision):
     return mat, d
 
 
-def workload_state():
-    from libgran_gb300.system import generate_aggregate, generate_velocities
+def workload_state(generator=None):
+    """The seeded aggregate and velocities; `generator` is a module with generate_aggregate and
+    generate_velocities (the engine's by default; the reference arm passes the oracle's, which gives
+    the same bits without loading the engine library)."""
     from libgran_gb300 import configs as K
+    if generator is None:
+        from libgran_gb300 import system as generator
     mat = K.Material()
-    x0 = generate_aggregate(SEED, N_PART, mat.r)
-    v0 = generate_velocities(SEED, N_PART, 0.1)
+    x0 = generator.generate_aggregate(SEED, N_PART, mat.r)
+    v0 = generator.generate_velocities(SEED, N_PART, 0.1)
     return x0, v0
+
+
+def repo_native_libraries():
+    """Shared libraries of this repository mapped into the process (from /proc/self/maps)."""
+    libs = set()
+    try:
+        for line in open("/proc/self/maps"):
+            path = line.split()[-1] if len(line.split()) >= 6 else ""
+            if path.endswith(".so") and path.startswith(ROOT + os.sep):
+                libs.add(os.path.relpath(path, ROOT))
+    except OSError:
+        return None
+    return sorted(libs)
 
 
 # ------------------------------------------------------------------------------------------------
@@ -151,11 +168,14 @@ def cpu_reference_rate(x0, v0, target_s=12.0, threads=None):
 
 
 def run_reference_arm(args, rank, world):
+    """The reference's CPU path: the oracle (libgran's functors and loop restated in C, OpenMP over
+    all host cores) on the same workload. Inputs come from the oracle's own generator, so this arm
+    loads no library of the engine."""
     if rank != 0:
         return
-    x0, v0 = workload_state()
     from libgran_gb300 import _abi as A
     from oracle import oracle as O
+    x0, v0 = workload_state(O)
     threads = os.cpu_count() or 1
     mat, d = workload_desc(A.LG_PRECISION_FP64)
     o = O.OracleSystem(d, x0, v0, threads=threads)
@@ -184,6 +204,7 @@ def run_reference_arm(args, rank, world):
                                    "functors and loop; libgran's own build needs its absent submodules)"
                                    % (N_PART, vv_per_sample)},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "native_libraries": repo_native_libraries(),
     }
     print(json.dumps(line), flush=True)
 

@@ -427,14 +427,16 @@ int lg_autotune(lg_system *sys, double dt, int64_t probe_steps, int64_t rebuild_
  * must not stall other streams (cudaMalloc and cudaFree can synchronise the device).
  *   x, v, omega: device arrays double[3n] (AoS); out: device array of LG_NOALLOC_OBS doubles:
  *   0 translational KE, 1 rotational KE, 2 total KE, 3 |linear momentum|, 4 |angular momentum|,
- *   5..7 centre of mass, 8 radius of gyration (test/compute_energy.cpp, test/mass_distribution.cpp
- *   quantities). stream: a cudaStream_t (NULL = default stream); the call is asynchronous.
+ *   5..7 centre of mass, 8 radius of gyration. stream: a cudaStream_t (NULL = default stream); the
+ *   call is asynchronous.
  * Limit: 1 <= n <= LG_NOALLOC_MAX_PARTICLES, else LG_E_INVALID with a message. Partial sums live in
  * one fixed 512 KiB array in device memory that every GPU loading this library holds until the
  * process exits; all calls share it, so calls that overlap on the GPU (e.g. on two streams at once)
  * race and must be serialised by the caller. The first call on each device looks up the array's
  * device address (set-up, with that device current); make that first call before any stream
- * capture. Calls no cudaMalloc, cudaFree or allocating library routine. */
+ * capture. Later calls outside a capture look the address up again (a cudaDeviceReset reloads the
+ * module and can move the array); a call during a capture uses the address of the last call made
+ * outside one. Calls no cudaMalloc, cudaFree or allocating library routine. */
 #define LG_NOALLOC_OBS 9
 #define LG_NOALLOC_MAX_PARTICLES 1048320
 int lg_observables_noalloc(const double *x, const double *v, const double *omega, int64_t n, double mass,

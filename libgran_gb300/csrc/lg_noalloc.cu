@@ -30,7 +30,8 @@ constexpr int kNaMaxDevices = 64;
 // that a call reads is written earlier in the same call, so nothing has to be cleared between calls.
 __device__ __align__(256) double g_noalloc_partials[kNaMaxBlocks * kNaCols];
 
-// Host-side handle to the array: its device address, looked up once per device.
+// Host-side handle to the array: its device address per device (refreshed by every call made
+// outside a stream capture).
 std::mutex g_na_mu;
 double *g_na_ptr[kNaMaxDevices] = {nullptr};
 
@@ -142,11 +143,24 @@ extern "C" int lg_observables_noalloc(const double *x, const double *v, const do
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return lg_fail(LG_E_CUDA, "lg_observables_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kNaMaxDevices) return lg_fail(LG_E_INVALID, "lg_observables_noalloc: device %d not supported", dev);
+    cudaStream_t st = (cudaStream_t)stream;
     double *part = nullptr;
     {
-        // set-up, once per device with that device current: the device address of the array
+        // set-up with the device current: the device address of the array. The first call on a
+        // device looks it up; later calls look it up again unless the stream is being captured, so
+        // that an address cached before a cudaDeviceReset (after which the module is loaded anew
+        // and the array can move) is not used; a captured call uses the address cached by an
+        // earlier call outside the capture.
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+            cudaGetLastError();
+            cs = cudaStreamCaptureStatusActive;  // cannot tell: treat as captured, look nothing up
+        }
         std::lock_guard<std::mutex> lk(g_na_mu);
-        if (!g_na_ptr[dev]) {
+        if (cs == cudaStreamCaptureStatusNone || !g_na_ptr[dev]) {
+            if (cs != cudaStreamCaptureStatusNone)
+                return lg_fail(LG_E_STATE, "lg_observables_noalloc: the first call on device %d must come before any "
+                                           "stream capture (it looks up the address of its scratch array)", dev);
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_partials);
             if (e != cudaSuccess)
@@ -156,7 +170,6 @@ extern "C" int lg_observables_noalloc(const double *x, const double *v, const do
         part = g_na_ptr[dev];
     }
     const int nblocks = (int)((n + kNaThreads - 1) / kNaThreads);  // <= kNaMaxBlocks - 1: row nblocks is free
-    cudaStream_t st = (cudaStream_t)stream;
     na_terms<<<nblocks, kNaThreads, 0, st>>>(n, x, v, omega, mass, inertia, part);
     na_combine<<<1, kNaThreads, 0, st>>>(n, nblocks, part, out);
     na_gyration<<<nblocks, kNaThreads, 0, st>>>(n, x, out, part);

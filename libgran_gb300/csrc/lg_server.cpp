@@ -293,14 +293,29 @@ extern "C" int lg_server_tick(lg_server *s, int32_t *n_active, int32_t *n_queued
             progress = true;
             continue;
         }
-        while (!r.inflight.empty() && cudaEventQuery(r.inflight.front().first) == cudaSuccess) {
+        cudaError_t qe = cudaSuccess;
+        while (!r.inflight.empty() && (qe = cudaEventQuery(r.inflight.front().first)) == cudaSuccess) {
             r.done_steps += r.inflight.front().second;
             s->particle_steps += r.inflight.front().second * r.n;
             r.free_events.push_back(r.inflight.front().first);
             r.inflight.pop_front();
             progress = true;
         }
-        cudaGetLastError();  // cudaEventQuery reports cudaErrorNotReady for pending events
+        if (qe == cudaErrorNotReady) {
+            cudaGetLastError();  // a pending event is not an error
+        } else if (qe != cudaSuccess) {
+            // the period failed on the device (or the context is lost): the request fails with the
+            // error instead of staying active with an event that never completes
+            cudaGetLastError();
+            r.state = LG_REQ_FAILED;
+            r.error = std::string("device error while running the request: ") + cudaGetErrorString(qe);
+            release_request(s, r);
+            r.t_done = now_ms();
+            s->failed++;
+            ++retired;
+            progress = true;
+            continue;
+        }
         if (r.done_steps >= r.nsteps) {
             retire(s, r);
             ++retired;

@@ -1096,3 +1096,131 @@ int lgo_run_many(lgo_system **systems, const double *dts, const int64_t *nsteps,
     for (int k = 0; k < count; ++k) lgo_step(systems[k], dts[k], nsteps[k], rebuild[k]);
     return 0;
 }
+
+/* ---------------------------------------------------------------------------------------------
+ * Seeded workload generator (project-defined; libgran has none). Same algorithm and arithmetic as
+ * the engine's lg_generate_rsa_aggregate / lg_generate_velocities, restated here so that the timed
+ * CPU baseline builds its inputs without the engine library: SplitMix64 draws, a parent chosen
+ * uniformly among the spheres placed so far, a direction uniform on the unit sphere (rejection
+ * from the cube), the candidate at distance 2r from the parent, rejected when any other sphere is
+ * closer than 2r - 1e-12 r. Whether a candidate is accepted does not depend on the order in which
+ * the neighbouring spheres are visited, so the spatial hash below gives the engine's bits.
+ */
+typedef struct {
+    uint64_t s;
+} lgo_splitmix;
+
+static uint64_t sm_next(lgo_splitmix *g) {
+    uint64_t z = (g->s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double sm_uniform(lgo_splitmix *g) { return (double)(sm_next(g) >> 11) * 0x1.0p-53; }
+static v3 sm_unit(lgo_splitmix *g) {
+    for (;;) {
+        double a = 2.0 * sm_uniform(g) - 1.0, b = 2.0 * sm_uniform(g) - 1.0, c = 2.0 * sm_uniform(g) - 1.0;
+        double s2 = (a * a + b * b) + c * c;
+        if (s2 > 1e-6 && s2 <= 1.0) {
+            double s = sqrt(s2);
+            return mk(a / s, b / s, c / s);
+        }
+    }
+}
+
+/* open-addressing table: cell key -> head of a singly linked list of sphere indices */
+typedef struct {
+    int64_t *key;
+    int32_t *head;
+    uint64_t mask;
+} lgo_cellmap;
+
+static uint64_t cell_hash(int64_t k) {
+    uint64_t z = (uint64_t)k * 0x9E3779B97F4A7C15ull;
+    return z ^ (z >> 29);
+}
+static int32_t *cell_slot(lgo_cellmap *m, int64_t k, int insert) {
+    uint64_t h = cell_hash(k) & m->mask;
+    for (;;) {
+        if (m->head[h] == -2) {
+            if (!insert) return NULL;
+            m->key[h] = k;
+            m->head[h] = -1;
+            return &m->head[h];
+        }
+        if (m->key[h] == k) return &m->head[h];
+        h = (h + 1) & m->mask;
+    }
+}
+
+int lgo_generate_rsa_aggregate(uint64_t seed, int64_t n, double r, double *x) {
+    if (n < 1 || !x || !(r > 0)) return -1;
+    lgo_splitmix rng = {seed};
+    const double edge = 2.0 * r;
+    const double lim = 2.0 * r - 1e-12 * r;
+    const double lim2 = lim * lim;
+    uint64_t cap = 16;
+    while (cap < 4 * (uint64_t)n) cap <<= 1;
+    lgo_cellmap m = {(int64_t *)malloc(sizeof(int64_t) * cap), (int32_t *)malloc(sizeof(int32_t) * cap), cap - 1};
+    int32_t *next = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    if (!m.key || !m.head || !next) {
+        free(m.key);
+        free(m.head);
+        free(next);
+        return -1;
+    }
+    for (uint64_t q = 0; q < cap; ++q) m.head[q] = -2;
+#define LGO_KEY(a, b, c) ((((a) + 1048576) * 2097152 + ((b) + 1048576)) * 2097152 + ((c) + 1048576))
+    x[0] = x[1] = x[2] = 0.0;
+    {
+        int32_t *h = cell_slot(&m, LGO_KEY((int64_t)floor(0.0 / edge), (int64_t)floor(0.0 / edge),
+                                          (int64_t)floor(0.0 / edge)), 1);
+        next[0] = *h;
+        *h = 0;
+    }
+    int rc = 0;
+    for (int64_t k = 1; k < n && rc == 0; ++k) {
+        for (int attempt = 0;; ++attempt) {
+            if (attempt > 100000) {
+                rc = -1;
+                break;
+            }
+            int64_t p = (int64_t)(sm_uniform(&rng) * (double)k);
+            if (p >= k) p = k - 1;
+            v3 dir = sm_unit(&rng);
+            v3 c = add(ld(x, p), scl(2.0 * r, dir));
+            int64_t cc[3] = {(int64_t)floor(c.x / edge), (int64_t)floor(c.y / edge), (int64_t)floor(c.z / edge)};
+            int ok = 1;
+            for (int64_t dz = -1; dz <= 1 && ok; ++dz)
+                for (int64_t dy = -1; dy <= 1 && ok; ++dy)
+                    for (int64_t dx = -1; dx <= 1 && ok; ++dx) {
+                        int32_t *h = cell_slot(&m, LGO_KEY(cc[0] + dx, cc[1] + dy, cc[2] + dz), 0);
+                        for (int32_t q = h ? *h : -1; q >= 0; q = next[q]) {
+                            if (q == p) continue;
+                            if (sqn(sub(c, ld(x, q))) < lim2) {
+                                ok = 0;
+                                break;
+                            }
+                        }
+                    }
+            if (!ok) continue;
+            stv(x, k, c);
+            int32_t *h = cell_slot(&m, LGO_KEY(cc[0], cc[1], cc[2]), 1);
+            next[k] = *h;
+            *h = (int32_t)k;
+            break;
+        }
+    }
+#undef LGO_KEY
+    free(m.key);
+    free(m.head);
+    free(next);
+    return rc;
+}
+
+int lgo_generate_velocities(uint64_t seed, int64_t n, double vmax, double *v) {
+    if (n < 0 || !v) return -1;
+    lgo_splitmix rng = {seed ^ 0x5DEECE66Dull};
+    for (int64_t q = 0; q < 3 * n; ++q) v[q] = (2.0 * sm_uniform(&rng) - 1.0) * vmax;
+    return 0;
+}

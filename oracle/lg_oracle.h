@@ -41,6 +41,10 @@ int lgo_set_body_centre(lgo_system *s, const double *centre);
 int64_t lgo_get_connectors(lgo_system *s, double *out, int64_t cap);
 int lgo_run_many(lgo_system **systems, const double *dts, const int64_t *nsteps, const int64_t *rebuild,
                  int count);
+/* Seeded inputs of the benchmark workloads, bit-identical to lg_generate_rsa_aggregate and
+ * lg_generate_velocities of the engine (0 = ok). */
+int lgo_generate_rsa_aggregate(uint64_t seed, int64_t n, double r, double *x);
+int lgo_generate_velocities(uint64_t seed, int64_t n, double vmax, double *v);
 
 #ifdef __cplusplus
 }

@@ -15,6 +15,15 @@ from libgran_gb300 import _abi as A
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liblg_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "liblgref.so")
+# where the harness recipe looks for the libgran source tree unless LIBGRAN_ROOT names another
+DEFAULT_LIBGRAN_ROOT = "/root/reference"
+
+
+def libgran_root():
+    """The libgran source tree the reference harness compiles from: $LIBGRAN_ROOT, else the
+    default location; None when neither holds libgran's include tree (the GPU machine)."""
+    root = os.environ.get("LIBGRAN_ROOT") or DEFAULT_LIBGRAN_ROOT
+    return root if os.path.isdir(os.path.join(root, "include", "libgran")) else None
 
 
 def build_oracle(force=False):
@@ -29,10 +38,10 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
-def build_ref(libgran_root=None):
+def build_ref(root=None):
     """Compile the reference harness from the libgran source tree when it is present."""
-    root = libgran_root or "/root/reference"
-    if not os.path.isdir(os.path.join(root, "include", "libgran")):
+    root = root or libgran_root()
+    if not root or not os.path.isdir(os.path.join(root, "include", "libgran")):
         return None
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref_harness"), "LIBGRAN=" + root,
                            "-j4"])
@@ -80,6 +89,8 @@ def olib():
         L.lgo_set_body_centre.argtypes = [vp, P(d)]
         L.lgo_get_connectors.restype = i64
         L.lgo_get_connectors.argtypes = [vp, P(d), i64]
+        L.lgo_generate_rsa_aggregate.argtypes = [C.c_uint64, i64, d, P(d)]
+        L.lgo_generate_velocities.argtypes = [C.c_uint64, i64, d, P(d)]
         _olib = L
     return _olib
 
@@ -108,6 +119,23 @@ def rlib():
         L.lgref_set_body_centre.argtypes = [vp, P(d)]
         _rlib = L
     return _rlib
+
+
+def generate_aggregate(seed, n, r):
+    """Seeded random-sequential-attachment aggregate of n spheres of radius r ([n, 3] positions),
+    bit-identical to the engine's lg_generate_rsa_aggregate."""
+    x = np.zeros((int(n), 3))
+    if olib().lgo_generate_rsa_aggregate(C.c_uint64(seed), int(n), float(r), _dp(x)) != 0:
+        raise RuntimeError("lgo_generate_rsa_aggregate failed")
+    return x
+
+
+def generate_velocities(seed, n, vmax):
+    """Seeded velocity components uniform in [-vmax, vmax], bit-identical to lg_generate_velocities."""
+    v = np.zeros((int(n), 3))
+    if olib().lgo_generate_velocities(C.c_uint64(seed), int(n), float(vmax), _dp(v)) != 0:
+        raise RuntimeError("lgo_generate_velocities failed")
+    return v
 
 
 def _facet_array(facets):

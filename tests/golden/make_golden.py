@@ -4,7 +4,8 @@ The harness compiles libgran's own functor headers (unmodified, from the libgran
 the system loop of the oracle; running it needs that tree and is done on the development machine.
 The fixtures (initial state, states after a few step counts, springs and bonds) travel with the
 repository so that the GPU test machine can check the engine against values produced by
-libgran's code. Usage: python tests/golden/make_golden.py [libgran_root]
+libgran's code. Usage: python tests/golden/make_golden.py [libgran_root] (default: $LIBGRAN_ROOT,
+else the tree oracle.libgran_root() finds)
 """
 import os
 import sys
@@ -44,8 +45,9 @@ def run_case(c):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    O.build_ref(root)
+    root = sys.argv[1] if len(sys.argv) > 1 else O.libgran_root()
+    if not root or O.build_ref(root) is None:
+        sys.exit("make_golden: no libgran source tree (pass its path or set LIBGRAN_ROOT)")
     for c in golden_cases.cases():
         out = run_case(c)
         path = os.path.join(HERE, c["name"] + ".npz")

@@ -92,3 +92,26 @@ def test_generator_is_seeded_and_overlap_free():
         assert np.isclose(d[k, :k].min(), 2 * r, rtol=1e-12)
     v = generate_velocities(3, 400, 0.1)
     assert np.abs(v).max() <= 0.1 and v.std() > 0.03
+
+
+def test_oracle_generator_gives_the_engine_generators_bits():
+    """The reference arm of bench.py builds its inputs with the oracle's generator (so that it loads
+    no engine library); it must produce the engine's aggregate and velocities bit for bit."""
+    from oracle import oracle as O
+    r = 1.4e-8
+    for seed, n in ((1 << 32, 32768), (7, 64), ((2 << 32) + 5, 2048), (3, 1)):
+        assert np.array_equal(O.generate_aggregate(seed, n, r), generate_aggregate(seed, n, r)), (seed, n)
+        assert np.array_equal(O.generate_velocities(seed, n, 0.1), generate_velocities(seed, n, 0.1)), (seed, n)
+
+
+def test_noalloc_refuses_bad_arguments_before_any_cuda_call():
+    """lg_observables_noalloc checks its arguments before it touches a device: sizes beyond its
+    fixed scratch, n = 0 and null pointers are refused with LG_E_INVALID and a message."""
+    L = A.lib()
+    rc = L.lg_observables_noalloc(1, 1, 1, A.LG_NOALLOC_MAX_PARTICLES + 1, 1.0, 1.0, 1, None)
+    assert rc == A.LG_E_INVALID
+    assert b"outside" in L.lg_last_error()
+    assert L.lg_observables_noalloc(1, 1, 1, 0, 1.0, 1.0, 1, None) == A.LG_E_INVALID
+    assert L.lg_observables_noalloc(None, 1, 1, 10, 1.0, 1.0, 1, None) == A.LG_E_INVALID
+    assert L.lg_observables_noalloc(1, 1, 1, 10, 1.0, 1.0, None, None) == A.LG_E_INVALID
+    assert b"null" in L.lg_last_error()

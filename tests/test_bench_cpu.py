@@ -26,3 +26,14 @@ def test_profile_summaries_give_their_commands():
         assert "ncu " in text and "--clock-control none" in text, f
         for cmd in re.findall(r"^\s+ncu .*$", text, flags=re.M):
             assert "--clock-control none" in cmd, (f, cmd)
+
+
+def test_reference_arm_inputs_load_no_engine_library():
+    """The reference arm's inputs come from the oracle alone: in a fresh process, building them maps
+    the oracle's library and no library of the engine."""
+    import subprocess
+    code = ("import sys; sys.path.insert(0, %r); import bench; bench.N_PART = 512; "
+            "from oracle import oracle as O; bench.workload_state(O); print(bench.repo_native_libraries())" % ROOT)
+    out = subprocess.check_output([sys.executable, "-c", code], cwd=ROOT, text=True).strip().splitlines()[-1]
+    libs = eval(out)
+    assert libs == ["oracle/liblg_oracle.so"], libs

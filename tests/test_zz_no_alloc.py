@@ -56,11 +56,3 @@ def test_noalloc_observables_match_handle_observables_twice(n):
         s.step(mat.dt, 20, 20)
         x, v, w = s.get(A.LG_FIELD_X), s.get(A.LG_FIELD_V), s.get(A.LG_FIELD_OMEGA)
         _check(_noalloc(x, v, w, mat.m, mat.I), s.observables())
-
-
-def test_noalloc_rejects_sizes_beyond_its_scratch():
-    L = A.lib()
-    rc = L.lg_observables_noalloc(1, 1, 1, A.LG_NOALLOC_MAX_PARTICLES + 1, 1.0, 1.0, 1, None)
-    assert rc == A.LG_E_INVALID
-    assert b"outside" in L.lg_last_error()
-    assert L.lg_observables_noalloc(1, 1, 1, 0, 1.0, 1.0, 1, None) == A.LG_E_INVALID
