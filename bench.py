@@ -209,25 +209,81 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def force_error_mixed_vs_fp64(x0, v0):
-    """Normwise relative error of the mixed-precision accelerations against FP64 at identical
-    states: the aggregate after 200 FP64 steps (contacts developed), evaluated by both paths."""
+def accuracy_run(x0, v0, total=None, every=1000):
+    """Config 1's accuracy run: total (10^4) velocity-Verlet steps of the 32768 aggregate in FP64
+    and in mixed precision, side by side. Every `every` steps:
+      * forces and torques of both paths at an identical state: fresh FP64 and mixed handles are
+        built from the FP64 run's state (positions, velocities, orientations, spins; springs start
+        from zero in both), and their construction force evaluations are compared (normwise
+        relative error over the system);
+      * one rebuild period (20 steps) of both fresh handles from that state: normwise relative
+        difference of the displacements (float-float integration inside a run of steps, springs);
+      * energy (kinetic + spring + Hamaker potential) of both long runs.
+    Energy drift is reported relative to the initial total energy and to the initial kinetic
+    energy (the Hamaker potential of the contacts is three orders of magnitude larger than the
+    kinetic energy)."""
     from libgran_gb300 import _abi as A
     from libgran_gb300.system import System
+    total = total or int(os.environ.get("LG_ACCURACY_STEPS", "10000"))
     mat, d64 = workload_desc(A.LG_PRECISION_FP64)
-    s = System(d64, x0, v0)
-    s.step(mat.dt, 200, VV_PER_STEP)
-    st = [s.get(f) for f in (A.LG_FIELD_X, A.LG_FIELD_V, A.LG_FIELD_THETA, A.LG_FIELD_OMEGA)]
-    s.close()
-    a = System(d64, *st)
-    _, dm = workload_desc(A.LG_PRECISION_MIXED)
-    b = System(dm, *st)
-    fa, fb = a.get(A.LG_FIELD_A), b.get(A.LG_FIELD_A)
-    ta, tb = a.get(A.LG_FIELD_ALPHA), b.get(A.LG_FIELD_ALPHA)
-    contacts = a.pair_stats()["live_contact_slots"]
-    return {"force_rel_err": float(np.abs(fa - fb).max() / np.abs(fa).max()),
-            "torque_rel_err": float(np.abs(ta - tb).max() / max(np.abs(ta).max(), 1e-300)),
-            "state": "aggregate after 200 FP64 steps, %d live contact slots" % contacts}
+    _, dmx = workload_desc(A.LG_PRECISION_MIXED)
+    run = {"fp64": System(d64, x0, v0), "mixed": System(dmx, x0, v0)}
+    energy = {k: [] for k in run}
+    ke0 = None
+    checkpoints = []
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        for k, s in run.items():
+            o = s.observables()
+            energy[k].append(o["ke_total"] + o["potential_energy"])
+            if ke0 is None:
+                ke0 = o["ke_total"]
+        st = run["fp64"].get_state()
+        a = System(d64, *st)
+        b = System(dmx, *st)
+        fa, fb = a.get(A.LG_FIELD_A), b.get(A.LG_FIELD_A)
+        ta, tb = a.get(A.LG_FIELD_ALPHA), b.get(A.LG_FIELD_ALPHA)
+        cp = {"step": done, "force_rel_err": float(np.abs(fa - fb).max() / np.abs(fa).max()),
+              "torque_rel_err": float(np.abs(ta - tb).max() / max(np.abs(ta).max(), 1e-300)),
+              "live_contact_slots": int(a.pair_stats()["live_contact_slots"])}
+        a.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+        b.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
+        da, db = a.get(A.LG_FIELD_X) - st[0], b.get(A.LG_FIELD_X) - st[0]
+        cp["period_displacement_rel_diff"] = float(np.abs(da - db).max() / np.abs(da).max())
+        a.close()
+        b.close()
+        checkpoints.append(cp)
+        if done >= total:
+            break
+        for s in run.values():
+            s.step(mat.dt, every, VV_PER_STEP)
+        done += every
+    xa, xb = run["fp64"].get(A.LG_FIELD_X), run["mixed"].get(A.LG_FIELD_X)
+    disp = np.abs(xa - x0).max()
+    errs = {k: s.device_errors() for k, s in run.items()}
+    for s in run.values():
+        s.close()
+    e = {k: np.array(v) for k, v in energy.items()}
+    out = {
+        "vv_steps": total, "checkpoint_every": every,
+        "force_rel_err_max": max(c["force_rel_err"] for c in checkpoints),
+        "torque_rel_err_max": max(c["torque_rel_err"] for c in checkpoints),
+        "period_displacement_rel_diff_max": max(c["period_displacement_rel_diff"] for c in checkpoints),
+        "energy_drift_rel_fp64": float(np.abs(e["fp64"] - e["fp64"][0]).max() / abs(e["fp64"][0])),
+        "energy_drift_rel_mixed": float(np.abs(e["mixed"] - e["mixed"][0]).max() / abs(e["mixed"][0])),
+        "energy_drift_over_ke0_fp64": float(np.abs(e["fp64"] - e["fp64"][0]).max() / ke0),
+        "energy_drift_over_ke0_mixed": float(np.abs(e["mixed"] - e["mixed"][0]).max() / ke0),
+        "energy_mixed_minus_fp64_over_ke0_max": float(np.abs(e["mixed"] - e["fp64"]).max() / ke0),
+        "final_position_diff_over_max_displacement": float(np.abs(xa - xb).max() / disp),
+        "device_errors": errs,
+        "checkpoints": checkpoints,
+        "energy_fp64": e["fp64"].tolist(), "energy_mixed": e["mixed"].tolist(), "ke0": ke0,
+        "wall_s": time.perf_counter() - t0,
+        "basis": "identical states: fresh FP64 and mixed handles built from the FP64 run's state every %d steps "
+                 "(springs from zero in both); energies from the two independent %d-step runs" % (every, total),
+    }
+    return out
 
 
 def time_path(precision, x0, v0, args, l2_flush):
@@ -389,7 +445,7 @@ def run_gb300(args, rank, world):
     sm.close()
     if rank != 0:
         return
-    acc = force_error_mixed_vs_fp64(x0, v0)
+    acc = accuracy_run(x0, v0) if os.environ.get("LG_BENCH_ACCURACY", "1") != "0" else None
     # roofline of the dominant kernel (mixed force kernel)
     ps = tm["pair_stats"]
     z_list = ps["mean_row_length"]

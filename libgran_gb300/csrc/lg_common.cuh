@@ -248,6 +248,19 @@ __device__ __forceinline__ d3 shear_bond(d3 &xi, d3 n, double stiffness, double 
     return f0;
 }
 
+// FP64 overlap of a contact pair exactly as the FP64 path computes it (contact_force.h:65-66:
+// n = dx / |dx|, overlap = 2r - dx.n with dx = x_i - x_j), every operation rounded on its own.
+__device__ __forceinline__ double overlap_fp64(const dbl4 *x, int64_t i, int64_t j, double r) {
+    const dbl4 a = x[i], b = x[j];
+    const double dx = __dsub_rn(a.x, b.x), dy = __dsub_rn(a.y, b.y), dz = __dsub_rn(a.z, b.z);
+    const double z = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (z == 0.0) return __dmul_rn(2.0, r);
+    const double s = __dsqrt_rn(z);
+    const double nx = __ddiv_rn(dx, s), ny = __ddiv_rn(dy, s), nz = __ddiv_rn(dz, s);
+    const double d = __dadd_rn(__dadd_rn(__dmul_rn(dx, nx), __dmul_rn(dy, ny)), __dmul_rn(dz, nz));
+    return __dsub_rn(__dmul_rn(2.0, r), d);
+}
+
 // contact_force.h:57-96 -- the in-contact branch (caller has established overlap > 0 with the
 // reference's own arithmetic, n and overlap are passed in).
 __device__ __forceinline__ void contact_touching(const lg_contact_params &p, d3 n, double overlap, d3 vi, d3 vj,

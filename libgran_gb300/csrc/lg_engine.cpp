@@ -1043,6 +1043,10 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         M.h_qcut = (float)(s->mx.rcut2 - s->mx.four_rh2);
         M.bin_im = (float)(sinter ? s->mx.inv_mass_b : s->mx.inv_mass_c);
         M.bin_iI = (float)(sinter ? s->mx.inv_inertia_b : s->mx.inv_inertia_c);
+        // contact threshold band: |q| <= 1e-10 (2r)^2, i.e. |overlap| <~ 5e-11 r, far above the
+        // float-float error of q and far below the overlaps of loaded contacts
+        M.q_marg = (float)(1e-10 * s->mx.four_rc2);
+        M.x64 = nullptr;
     }
     s->T = d->threads_per_row > 0 ? d->threads_per_row : choose_threads_per_row(s);
     s->kernel = choose_kernel(s, d->force_kernel);

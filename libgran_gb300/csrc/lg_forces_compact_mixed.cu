@@ -264,8 +264,12 @@ __device__ __forceinline__ void contact_item(const Params &P, const PairView &PV
     const float rr = bonded ? M.b_r : M.c_r;
     const float rsd = rsqrtf(d2f);
     const float overlap = -sp.q / (d2f * rsd + 2.0f * rr);  // 2r - |d|, from |d|^2 - (2r)^2
+    bool touching = bonded || overlap > 0.0f;
+    // spheres at the contact distance to within rounding (a seeded aggregate places touching
+    // monomers there): the FP64 path's overlap decides whether they touch
+    if (!bonded && M.x64 && fabsf(sp.q) <= M.q_marg) touching = overlap_fp64(M.x64, io, j, (double)P.contact.r_part) > 0.0;
     f3 force = fm(0.f, 0.f, 0.f), torque = fm(0.f, 0.f, 0.f);
-    if (bonded || overlap > 0.0f) {
+    if (touching) {
         const f3 n3 = fscl(rsd, dxf);
         // relative velocity v_i - v_j from the float-float copies (exact high-part difference)
         const float4 vhi = W.vh[own], vlo = W.vl[own];
@@ -847,10 +851,13 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
     if (contacts) {  // the contact branch runs beside the Hamaker kernel
         cudaEventRecord(fork, st);
         cudaStreamWaitEvent(side, fork, 0);
+        // the FP64 positions are current unless the step before integrated in float-float
+        MixedExtra MC = MX;
+        MC.x64 = prev_fused ? nullptr : S.x;
         if (ver && PV.near_len)
-            launch_contacts<true>(P, S, PV, BV, MX, side, hamaker != 0);
+            launch_contacts<true>(P, S, PV, BV, MC, side, hamaker != 0);
         else
-            launch_contacts<false>(P, S, PV, BV, MX, side, hamaker != 0);
+            launch_contacts<false>(P, S, PV, BV, MC, side, hamaker != 0);
         ++kernels;
     }
     if (hamaker) {

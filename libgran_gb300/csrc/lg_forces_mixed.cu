@@ -206,7 +206,11 @@ __global__ void __launch_bounds__(256) forces_mixed(Params P, StateView S, PairV
                 const double q4 = bonded ? four_rb2 : four_r2;
                 const float rr = bonded ? (float)B.r_part : rc;
                 const float overlap = (float)(q4 - d2) / (dist + 2.0f * rr);  // 2r - |d|
-                if (bonded || overlap > 0.0f) {
+                bool touching = bonded || overlap > 0.0f;
+                // at the contact distance to within rounding, the FP64 path's overlap decides
+                if (!bonded && fabs(q4 - d2) <= (double)MX.q_marg)
+                    touching = overlap_fp64(S.x, i, j, C.r_part) > 0.0;
+                if (touching) {
                     const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
                     const f3 vij0 = tof(sub(vi, vj));
                     d3 s[3];

@@ -99,6 +99,12 @@ struct MixedExtra {
     float h_fr_hi, h_fr_lo, h_qcut;
     float c_fr_hi, c_fr_lo, b_fr_hi, b_fr_lo;
     float bin_im, bin_iI;
+    // contact decisions at the threshold: a non-bonded pair whose float-float q lies within q_marg
+    // of zero is in contact when the FP64 overlap of the FP64 path, 2r - dx.(dx/|dx|) from x64, is
+    // positive; x64 is set only for evaluations whose FP64 positions are current (null inside a run
+    // of steps integrated in float-float)
+    const dbl4 *x64;
+    float q_marg;
 };
 bool mixed_available();
 void launch_forces_mixed(int T, const Params &P, const StateView &S, const PairView &PV, const BondView &BV,

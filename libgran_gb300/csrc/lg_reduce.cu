@@ -11,10 +11,34 @@ namespace lg {
 
 constexpr int kObs = 20;  // values per particle in the scratch rows
 
-__device__ __forceinline__ double hamaker_energy(double A, double r, double h) {
+// Pair potential of the Hamaker functors: the exact integral of the force they apply. Full form
+// U(h) = -A/6 [2r^2/((4r+h)h) + 2r^2/(2r+h)^2 + ln((4r+h)h/(2r+h)^2)] (its derivative is the
+// bracket of hamaker_force.h:36-40), simplified form U(h) = -2Ar/h (force 2Ar/h^2,
+// simplified_hamaker_force.h:18-31); linear below the saturation distance h0 (the force stays at
+// its value there), and for the limited form shifted to vanish at the cutoff distance.
+__device__ __forceinline__ double hamaker_u0(int mode, double A, double r, double h) {
+    if (mode == LG_HAMAKER_SIMPLIFIED) return -2.0 * A * r / h;
     return -A / 6.0 *
            (2.0 * r * r / ((4.0 * r + h) * h) + 2.0 * r * r / ((2.0 * r + h) * (2.0 * r + h)) +
             log((4.0 * r + h) * h / ((2.0 * r + h) * (2.0 * r + h))));
+}
+__device__ __forceinline__ double hamaker_slope(int mode, double A, double r, double h) {
+    if (mode == LG_HAMAKER_SIMPLIFIED) return 2.0 * A * r / (h * h);
+    const double br = (4.0 * r + 2.0 * h) / (4.0 * r + h) / h - 2.0 / (2.0 * r + h) -
+                      4.0 * r * r / ((2.0 * r + h) * (2.0 * r + h) * (2.0 * r + h)) -
+                      2.0 * r * r * (4.0 * r + 2.0 * h) / ((4.0 * r + h) * (4.0 * r + h)) / (h * h);
+    return -A / 6.0 * br;
+}
+__device__ __forceinline__ double hamaker_energy(int mode, const lg_hamaker_params &p, double dist) {
+    const double r = p.r_part, h = dist - 2.0 * r;
+    double u = h < p.h0 ? hamaker_u0(mode, p.A, r, p.h0) + hamaker_slope(mode, p.A, r, p.h0) * (h - p.h0)
+                        : hamaker_u0(mode, p.A, r, h);
+    if (mode == LG_HAMAKER_LIMITED) {
+        const double hc = p.r_cutoff - 2.0 * r;
+        u -= hc < p.h0 ? hamaker_u0(mode, p.A, r, p.h0) + hamaker_slope(mode, p.A, r, p.h0) * (hc - p.h0)
+                       : hamaker_u0(mode, p.A, r, hc);
+    }
+    return u;
 }
 
 // Per-particle terms. Column layout of a scratch row:
@@ -79,12 +103,9 @@ __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double
                 u += 0.5 * P.contact.k_t * sqn(s0) + 0.5 * P.contact.k_r * sqn(s1) + 0.5 * P.contact.k_o * sqn(s2);
             }
         }
-        if (P.hamaker_model == LG_HAMAKER_FULL ||
-            (P.hamaker_model == LG_HAMAKER_LIMITED && !(dist > P.hamaker.r_cutoff))) {
-            double h = dist - 2.0 * P.hamaker.r_part;
-            if (h < P.hamaker.h0) h = P.hamaker.h0;
-            u += hamaker_energy(P.hamaker.A, P.hamaker.r_part, h);
-        }
+        if (P.hamaker_model == LG_HAMAKER_FULL || P.hamaker_model == LG_HAMAKER_SIMPLIFIED ||
+            (P.hamaker_model == LG_HAMAKER_LIMITED && !(dist > P.hamaker.r_cutoff)))
+            u += hamaker_energy(P.hamaker_model, P.hamaker, dist);
         pe += 0.5 * u;
     }
     o[15] = pe;

@@ -997,9 +997,34 @@ int64_t lgo_row(lgo_system *s, int64_t i, int32_t *out, int64_t cap) {
 
 /* Hamaker interaction energy between two equal spheres at surface separation h (the potential of
  * the force in hamaker_force.h:36-40; libgran's README states it), evaluated at max(h, h0). */
-static double hamaker_energy(double A, double r, double h) {
+/* Pair potential of the Hamaker functors, the exact integral of the force they apply (the
+ * reference has no energy bookkeeping; this definition is the project's). The full form is
+ *   U(h) = -A/6 [2r^2/((4r+h)h) + 2r^2/(2r+h)^2 + ln((4r+h)h/(2r+h)^2)],
+ * whose derivative is the bracket of hamaker_force.h:36-40; the simplified form (force 2Ar/h^2,
+ * simplified_hamaker_force.h:18-31) has U(h) = -2Ar/h. Below the saturation distance h0 the force
+ * stays at its value at h0, so U continues linearly with that slope; the limited form cuts the
+ * force at the centre distance r_cutoff, so its U is shifted to vanish there. */
+static double hamaker_u0(int mode, double A, double r, double h) {
+    if (mode == LG_HAMAKER_SIMPLIFIED) return -2.0 * A * r / h;
     return -A / 6.0 * (2.0 * r * r / ((4.0 * r + h) * h) + 2.0 * r * r / ((2.0 * r + h) * (2.0 * r + h))
                        + log((4.0 * r + h) * h / ((2.0 * r + h) * (2.0 * r + h))));
+}
+static double hamaker_slope(int mode, double A, double r, double h) {
+    if (mode == LG_HAMAKER_SIMPLIFIED) return 2.0 * A * r / (h * h);
+    double br = (4.0 * r + 2.0 * h) / (4.0 * r + h) / h - 2.0 / (2.0 * r + h) - 4.0 * r * r / ((2.0 * r + h) * (2.0 * r + h) * (2.0 * r + h))
+                - 2.0 * r * r * (4.0 * r + 2.0 * h) / ((4.0 * r + h) * (4.0 * r + h)) / (h * h);
+    return -A / 6.0 * br;
+}
+static double hamaker_energy(int mode, const lg_hamaker_params *p, double dist) {
+    const double r = p->r_part, h = dist - 2.0 * r;
+    double u = h < p->h0 ? hamaker_u0(mode, p->A, r, p->h0) + hamaker_slope(mode, p->A, r, p->h0) * (h - p->h0)
+                         : hamaker_u0(mode, p->A, r, h);
+    if (mode == LG_HAMAKER_LIMITED) {
+        const double hc = p->r_cutoff - 2.0 * r;
+        u -= hc < p->h0 ? hamaker_u0(mode, p->A, r, p->h0) + hamaker_slope(mode, p->A, r, p->h0) * (hc - p->h0)
+                        : hamaker_u0(mode, p->A, r, hc);
+    }
+    return u;
 }
 
 /* test/compute_energy.cpp:7-58, test/mass_distribution.cpp:7-27, plus potential energy. */
@@ -1071,11 +1096,9 @@ int lgo_observables(lgo_system *s, lg_observables *o) {
                 }
                 u += 0.5 * d->contact.k_t * sqn(e->xi[0]) + 0.5 * d->contact.k_r * sqn(e->xi[1]) + 0.5 * d->contact.k_o * sqn(e->xi[2]);
             }
-            if (d->hamaker_model == LG_HAMAKER_FULL || (d->hamaker_model == LG_HAMAKER_LIMITED && !(dist > d->hamaker.r_cutoff))) {
-                double h = dist - 2.0 * d->hamaker.r_part;
-                if (h < d->hamaker.h0) h = d->hamaker.h0;
-                u += hamaker_energy(d->hamaker.A, d->hamaker.r_part, h);
-            }
+            if (d->hamaker_model == LG_HAMAKER_FULL || d->hamaker_model == LG_HAMAKER_SIMPLIFIED ||
+                (d->hamaker_model == LG_HAMAKER_LIMITED && !(dist > d->hamaker.r_cutoff)))
+                u += hamaker_energy(d->hamaker_model, &d->hamaker, dist);
             pe += 0.5 * u;
         }
     }

@@ -47,6 +47,25 @@ def test_mixed_forces_within_1e6_of_fp64(pairs, n, bm, hm, kernel):
     assert amx.device_errors() == 0
 
 
+@pytest.mark.parametrize("kernel", [A.LG_FORCE_KERNEL_ROWGROUP, A.LG_FORCE_KERNEL_COMPACT], ids=["rowgroup", "compact"])
+@pytest.mark.parametrize("bm", [A.LG_BINARY_CONTACT, A.LG_BINARY_SINTER], ids=["contact", "sinter"])
+def test_mixed_forces_at_the_contact_threshold(bm, kernel):
+    """A freshly generated aggregate holds thousands of monomer pairs at the contact distance to
+    within rounding (unbonded for the contact model, beside the bonds for the sinter model): whether
+    such a pair touches, and so feels damping and friction, is decided by the last bits of its
+    separation. The mixed path lets the FP64 overlap decide those pairs, so its forces stay within
+    1e-6 of the FP64 path's at the generated state (32768 monomers, velocities +-0.1 m/s)."""
+    mat = K.Material()
+    n = 32768
+    x0 = generate_aggregate(1 << 32, n, mat.r)
+    v0 = generate_velocities(1 << 32, n, 0.1)
+    a64 = System(_desc(n, bm, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, A.LG_PRECISION_FP64, mat), x0, v0)
+    amx = System(_desc(n, bm, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, A.LG_PRECISION_MIXED, mat, kernel), x0, v0)
+    assert H.rel_err(amx.get(A.LG_FIELD_A), a64.get(A.LG_FIELD_A)) <= MIXED_TOL
+    assert H.rel_err(amx.get(A.LG_FIELD_ALPHA), a64.get(A.LG_FIELD_ALPHA)) <= MIXED_TOL
+    assert a64.observables()["n_contacts"] == amx.observables()["n_contacts"]
+
+
 def test_mixed_energy_drift_tracks_fp64():
     """Energy balance over 2000 steps: total energy (kinetic + spring + Hamaker potential) of the
     mixed path follows the FP64 path."""
@@ -118,10 +137,14 @@ def test_mixed_runs_of_steps_track_single_steps():
     can give pair terms that differ by an FP32 rounding (1e-7 of a term): after two steps the two
     agree to that; over 20 steps of a bonded aggregate the difference grows with the dynamics'
     sensitivity (about tenfold every ten steps), as any perturbation does. The integrator itself is
-    checked exactly in free flight (next test)."""
+    checked exactly in free flight (next test). The aggregate is compressed by 1 ppm so that every
+    touching pair overlaps definitely: at the bare contact distance single steps let the FP64
+    overlap decide contact (positions current in FP64) while steps inside a run decide it in
+    float-float, and either decision is a rounding accident there."""
     mat = K.Material()
     n = 2500
     x0 = generate_aggregate(31, n, mat.r)
+    x0 = x0.mean(0) + (x0 - x0.mean(0)) * (1.0 - 1e-6)
     v0 = generate_velocities(31, n, 0.1)
     d = _desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, A.LG_PRECISION_MIXED, mat,
               A.LG_FORCE_KERNEL_COMPACT)
