@@ -286,7 +286,7 @@ def accuracy_run(x0, v0, total=None, every=1000):
     return out
 
 
-def time_path(precision, x0, v0, args, l2_flush):
+def time_path(precision, x0, v0, args, l2_flush, tune=False):
     """Device-timed K bench steps (each 20 VV steps, replayed as one CUDA graph) with CUDA events on
     the handle's stream; L2 is flushed before every timed bench step (the flush is outside the
     timed region). The force kernel's own duration is then measured on 2 further bench steps with
@@ -295,6 +295,10 @@ def time_path(precision, x0, v0, args, l2_flush):
     from libgran_gb300.system import System
     mat, d = workload_desc(precision)
     s = System(d, x0, v0)
+    tuning = None
+    if tune:  # the project autotuner picks the kernel family and shape on the live system
+        s.autotune(mat.dt, probe_steps=VV_PER_STEP, rebuild_every=VV_PER_STEP, use_cache=False)
+        tuning = s.tuning()
     for _ in range(args.warmup):
         s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
     l0 = s.launch_count()
@@ -313,7 +317,30 @@ def time_path(precision, x0, v0, args, l2_flush):
     stats = s.pair_stats()
     errs = s.device_errors()
     return s, mat, {"ms": total_ms, "launches": launches, "kernel_ms": kms, "kernel_launches": kcount,
-                    "pair_stats": stats, "device_errors": errs}
+                    "pair_stats": stats, "device_errors": errs, "tuning": tuning}
+
+
+def kernel_name(t):
+    from libgran_gb300 import _abi as A
+    if t and t["force_kernel"] == A.LG_FORCE_KERNEL_PERSISTENT:
+        return "forces_step_mixed (one persistent launch per step)"
+    return "forces_mixed (contacts || hamaker -> finish)"
+
+
+def tuning_desc(t):
+    """The autotuner's pick as names (kernel family and shape)."""
+    from libgran_gb300 import _abi as A
+    if not t:
+        return None
+    names = {A.LG_FORCE_KERNEL_COMPACT: "compact", A.LG_FORCE_KERNEL_ROWGROUP: "rowgroup",
+             A.LG_FORCE_KERNEL_PAIRS: "pairs", A.LG_FORCE_KERNEL_PERSISTENT: "persistent"}
+    out = {"kernel": names.get(t["force_kernel"], str(t["force_kernel"])), "probe_ms_per_step": t["ms_per_step"]}
+    if t["force_kernel"] == A.LG_FORCE_KERNEL_ROWGROUP:
+        out["threads_per_row"] = t["threads_per_row"]
+    if t["force_kernel"] == A.LG_FORCE_KERNEL_PERSISTENT:
+        out.update(min_blocks_per_sm=t["step_min_blocks"], hamaker_slices=t["step_slices"],
+                   items="round robin" if t["step_assign"] else "pulled")
+    return out
 
 
 def batched_section(args, l2_flush):
@@ -340,6 +367,7 @@ def batched_section(args, l2_flush):
     for name, prec in (("mixed", A.LG_PRECISION_MIXED), ("fp64", A.LG_PRECISION_FP64)):
         s = System(desc(int(sizes.sum()), prec), x0, v0, sizes=sizes)
         kern, T = s.autotune(mat.dt, probe_steps=VV_PER_STEP, rebuild_every=VV_PER_STEP)
+        tuned = s.tuning()
         for _ in range(args.warmup):
             s.step(mat.dt, VV_PER_STEP, VV_PER_STEP)
         ms = 0.0
@@ -348,8 +376,7 @@ def batched_section(args, l2_flush):
             l2_flush()
             ms += s.step_timed(mat.dt, VV_PER_STEP, VV_PER_STEP)
         res[name] = {"value": sizes.sum() * VV_PER_STEP * steps / (ms / 1e3), "ms_per_step": ms / steps,
-                     "force_kernel": "compact" if kern == A.LG_FORCE_KERNEL_COMPACT else "rowgroup%d" % T,
-                     "device_errors": s.device_errors()}
+                     "tuning": tuning_desc(tuned), "device_errors": s.device_errors()}
         s.close()
     # one by one: a sample of the aggregates, each its own handle, launched in turn
     sample = min(64, count)
@@ -428,7 +455,7 @@ def run_gb300(args, rank, world):
     torch.cuda.synchronize()
     clocks = ClockSampler(dev)
     clocks.start()
-    sm, mat, tm = time_path(A.LG_PRECISION_MIXED, x0, v0, args, l2_flush)
+    sm, mat, tm = time_path(A.LG_PRECISION_MIXED, x0, v0, args, l2_flush, tune=True)
     clk = clocks.stop()
     torch.cuda.synchronize()
     def amax(v):
@@ -488,8 +515,9 @@ def run_gb300(args, rank, world):
         "accuracy": acc,
         "e2e": e2e,
         "gpu_launches": tm["launches"],
+        "tuning": tuning_desc(tm["tuning"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "forces_mixed (contacts || hamaker -> finish)", "bytes_per_particle": bytes_per_particle,
+                     "traffic": traffic, "kernel": kernel_name(tm["tuning"]), "bytes_per_particle": bytes_per_particle,
                      "per_launch_ms": per_launch_ms, "per_launch_basis": "graph-replayed timed region per VV step",
                      "eager_eval_ms": eager_eval_ms, "peak_source": "measured" if peaks else "fallback"},
         "cpu_baseline": cpu,
@@ -616,6 +644,8 @@ def run_profile(args):
     prec = A.LG_PRECISION_MIXED if args.profile == "mixed" else A.LG_PRECISION_FP64
     x0, v0 = workload_state()
     mat, d = workload_desc(prec)
+    if args.kernel is not None:
+        d.force_kernel = {"compact": A.LG_FORCE_KERNEL_COMPACT, "persistent": A.LG_FORCE_KERNEL_PERSISTENT}[args.kernel]
     s = System(d, x0, v0)
     s.step(mat.dt, VV_PER_STEP * (args.warmup + args.steps), VV_PER_STEP)
     print(json.dumps({"profile": args.profile, "vv_steps": VV_PER_STEP * (args.warmup + args.steps),
@@ -626,6 +656,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile", default=None, choices=[None, "mixed", "fp64"],
                     help="profiling driver: run one path without timing")
+    ap.add_argument("--kernel", default=None, choices=[None, "compact", "persistent"],
+                    help="profiling driver: force kernel of the mixed path")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)

@@ -205,6 +205,11 @@ typedef struct lg_system_desc {
 #define LG_FORCE_KERNEL_COMPACT 2    /* one row per lane, warp-compacted pair queues (see csrc) */
 #define LG_FORCE_KERNEL_PAIRS 3      /* FP64, small systems: one thread per pair slot spread over all SMs,
                                        then an ordered per-row fold (the reference's summation order) */
+#define LG_FORCE_KERNEL_PERSISTENT 4 /* mixed: every step inside a run of steps (no facets, body terms or
+                                       held particles) is one persistent launch whose warps pull contact
+                                       and Hamaker work items of 32-row groups from a device queue and
+                                       complete each group when its last item finishes; the same bits as
+                                       the compacted kernels. Other steps use the compacted kernels. */
 
 /* Fields that lg_get / lg_set move. */
 #define LG_FIELD_X 0       /* positions            get_x()     Granular-system.md:84-120 */
@@ -413,12 +418,33 @@ int lg_batch_get_observables(lg_system *sys, lg_observables *out);
 int lg_snapshot(lg_system *sys);
 int lg_restore(lg_system *sys);
 
-/* Project autotuner: times the force-kernel variants (compacted; row groups of 1..32 lanes) for
+/* Project autotuner (the reference's only tuning knob is the OpenMP thread count): times the
+ * force-kernel variants and shapes -- compacted kernels; row groups of 1..32 lanes; FP64: the
+ * pair-parallel kernel; mixed: the persistent step kernel in every shape of lg_set_step_shape
+ * (register budget 4/5/6 blocks per SM x 1/2/4 Hamaker slices x pulled / round-robin items) -- for
  * probe_steps steps on the live system between a snapshot and its restore (the state afterwards is
- * the state before the call) and keeps the fastest; the choice is cached per
- * (precision, pair mode, functor set, log2 size, batch) when use_cache is 1. */
+ * the state before the call), graph-replayed, best of two timings each, and keeps the fastest. The
+ * choice is cached per (precision, pair mode, functor set, log2 size, batch) when use_cache is 1. */
 int lg_autotune(lg_system *sys, double dt, int64_t probe_steps, int64_t rebuild_every, int32_t *force_kernel,
                 int32_t *threads_per_row, int32_t use_cache);
+
+/* A handle's (or a cache entry's) kernel choice and shape. ms_per_step: the autotuner's timing of
+ * it (0 when not timed). */
+typedef struct {
+    int32_t force_kernel;     /* LG_FORCE_KERNEL_* (resolved, never AUTO) */
+    int32_t threads_per_row;  /* row groups */
+    int32_t step_min_blocks;  /* persistent step kernel: register budget (resident blocks per SM) */
+    int32_t step_slices;      /* persistent step kernel: Hamaker items per 32-row group */
+    int32_t step_assign;      /* persistent step kernel: 0 pulled items, 1 round robin */
+    double ms_per_step;
+} lg_tuning;
+int lg_get_tuning(lg_system *sys, lg_tuning *out);
+/* The autotuner's cache: a lookup for a descriptor, size and batch flag (LG_E_STATE when absent),
+ * and a text file to keep picks across processes (one entry per line; load merges). */
+int lg_autotune_cache_lookup(const lg_system_desc *desc, int64_t n, int32_t batch, lg_tuning *out);
+int lg_autotune_cache_save(const char *path);
+int lg_autotune_cache_load(const char *path);
+int lg_autotune_cache_clear(void);
 
 /* Observables of a particle state held in device memory that the caller owns, computed without
  * allocating any device memory. No counterpart in the reference: it serves callers that cannot
@@ -441,6 +467,14 @@ int lg_autotune(lg_system *sys, double dt, int64_t probe_steps, int64_t rebuild_
 #define LG_NOALLOC_MAX_PARTICLES 1048320
 int lg_observables_noalloc(const double *x, const double *v, const double *omega, int64_t n, double mass,
                            double inertia, double *out, void *stream);
+
+/* Shape of the persistent step kernel (LG_FORCE_KERNEL_PERSISTENT, mixed precision; no
+ * counterpart in the reference): min_blocks = register budget as resident blocks per SM (4, 5 or
+ * 6; 0 = 4), slices = Hamaker items per 32-row group (1, 2 or 4; 0 = the size rule the compacted
+ * kernels use, which gives their bits), assign = 0 (warps pull work items from a device counter)
+ * or 1 (round robin). lg_autotune chooses a shape when it tries the persistent kernel. */
+int lg_set_step_shape(lg_system *sys, int32_t min_blocks, int32_t slices, int32_t assign);
+int lg_get_step_shape(lg_system *sys, int32_t *min_blocks, int32_t *slices, int32_t *assign);
 
 /* Time `nsteps` steps with CUDA events on the handle's stream (no host copies inside); ms_out
  * receives the elapsed device time. Same semantics as lg_step. */

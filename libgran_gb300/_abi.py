@@ -17,6 +17,7 @@ LG_NECK_PER_BOND, LG_NECK_REFERENCE_INDEXING = 0, 1
 LG_PRECISION_FP64, LG_PRECISION_MIXED = 0, 1
 LG_PAIRS_ALL, LG_PAIRS_VERLET = 0, 1
 LG_FORCE_KERNEL_AUTO, LG_FORCE_KERNEL_ROWGROUP, LG_FORCE_KERNEL_COMPACT, LG_FORCE_KERNEL_PAIRS = 0, 1, 2, 3
+LG_FORCE_KERNEL_PERSISTENT = 4
 LG_FIELD_X, LG_FIELD_V, LG_FIELD_THETA, LG_FIELD_OMEGA, LG_FIELD_A, LG_FIELD_ALPHA = range(6)
 LG_DEVERR_LIST_OVERFLOW, LG_DEVERR_NONFINITE, LG_DEVERR_BOND_LOST = 1, 2, 4
 LG_NOALLOC_OBS, LG_NOALLOC_MAX_PARTICLES = 9, 1048320
@@ -86,6 +87,14 @@ class lg_system_desc(C.Structure):
                 ("connector_axes", C.POINTER(C.c_double)), ("n_connector_axes", C.c_int64),
                 ("hold_mask", C.POINTER(C.c_uint8)), ("body", lg_body_force), ("unary_hook", lg_unary_hook),
                 ("unary_hook_user", C.c_void_p)]
+
+
+class lg_tuning(C.Structure):
+    _fields_ = [("force_kernel", C.c_int32), ("threads_per_row", C.c_int32), ("step_min_blocks", C.c_int32),
+                ("step_slices", C.c_int32), ("step_assign", C.c_int32), ("ms_per_step", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class lg_observables(C.Structure):
@@ -171,6 +180,13 @@ def _declare(L):
         "lg_server_get_stats": (C.c_int, [vp, P(lg_server_stats)]),
         "lg_server_inject_alloc_failures": (C.c_int, [vp, i32]),
         "lg_observables_noalloc": (C.c_int, [vp, vp, vp, i64, d, d, vp, vp]),
+        "lg_set_step_shape": (C.c_int, [vp, i32, i32, i32]),
+        "lg_get_tuning": (C.c_int, [vp, P(lg_tuning)]),
+        "lg_autotune_cache_lookup": (C.c_int, [P(lg_system_desc), i64, i32, P(lg_tuning)]),
+        "lg_autotune_cache_save": (C.c_int, [C.c_char_p]),
+        "lg_autotune_cache_load": (C.c_int, [C.c_char_p]),
+        "lg_autotune_cache_clear": (C.c_int, []),
+        "lg_get_step_shape": (C.c_int, [vp, P(i32), P(i32), P(i32)]),
         "lg_restore": (C.c_int, [vp]),
         "lg_get_pair_stats": (C.c_int, [vp, P(lg_pair_stats)]),
         "lg_enable_kernel_timing": (C.c_int, [vp, i32]),

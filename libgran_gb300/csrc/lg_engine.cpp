@@ -371,6 +371,7 @@ constexpr int64_t kPairsAutoSlots = (int64_t)1 << 19;
 
 static int choose_kernel(const lg_system *s, int requested) {
     if (requested == LG_FORCE_KERNEL_ROWGROUP || requested == LG_FORCE_KERNEL_COMPACT) return requested;
+    if (requested == LG_FORCE_KERNEL_PERSISTENT) return s->precision == LG_PRECISION_MIXED ? requested : -1;
     if (requested == LG_FORCE_KERNEL_PAIRS) return s->pres ? requested : -1;
     const int64_t n = s->P.n;
     // mixed precision: the compacted kernels at every size (their float-float completion and fused
@@ -404,6 +405,30 @@ static int rebuild_list(lg_system *s) {
     s->pcur = 1 - s->pcur;
     s->list_built = true;
     LG_CUDA(cudaGetLastError());
+    return LG_OK;
+}
+
+// The current buffers of the double-buffered float-float state (mixed precision).
+static void set_ff_buffers(lg_system *s) {
+    if (!s->x32buf) return;
+    const int64_t n = s->P.n;
+    s->x32 = s->x32buf + 2 * n * s->ffcur;
+    s->v32 = s->v32buf + 3 * n * s->ffcur;
+    s->mx.x32 = s->x32;
+    s->mx.v32 = s->v32;
+}
+
+// Counters and Hamaker partial sums of the persistent step kernel (allocated when it is chosen).
+static int ensure_step_buffers(lg_system *s) {
+    if (s->step_ctr) return LG_OK;
+    const int64_t n = s->P.n;
+    const int64_t groups = (n + 31) / 32;
+    const int sl = mixed_hamaker_slices(n);
+    LG_TRY(s->alloc(&s->step_ctr, (size_t)(2 + groups)));
+    LG_CUDA(cudaMemset(s->step_ctr, 0, sizeof(unsigned) * (size_t)(2 + groups)));
+    LG_TRY(s->alloc(&s->hpart, 2 * (size_t)4 * (size_t)n));
+    s->step_slices = sl;
+    s->fstep = 0;
     return LG_OK;
 }
 
@@ -462,8 +487,40 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
         const int hr = s->hook(&ha, s->hook_user);
         if (hr != 0) return lg_fail(LG_E_STATE, "unary hook returned %d", hr);
     }
-    if (s->precision == LG_PRECISION_MIXED) {
-        if (compact)
+    const bool persistent = s->kernel == LG_FORCE_KERNEL_PERSISTENT;
+    if (s->precision == LG_PRECISION_MIXED && persistent && s->step_ctr && (fuse_kick || prev_fused) &&
+        s->P.n_facets == 0 && !s->P.ext_a && !s->P.hold && s->s32) {
+        // one persistent launch: contacts, Hamaker and the float-float completion of this step
+        const int64_t n = s->P.n;
+        const PairView &pv = s->pv[s->pcur];
+        StepArgs A{};
+        const int nf = 1 - s->ffcur;
+        A.x32n = s->x32buf + 2 * n * nf;
+        A.v32n = s->v32buf + 3 * n * nf;
+        A.hpart = s->hpart;
+        A.ctr = s->step_ctr;
+        A.par = (int)(s->fstep & 1);
+        A.slices = s->step_slices;
+        A.contacts = s->P.binary_model != LG_BINARY_NONE ? 1 : 0;
+        A.hamaker = s->P.hamaker_model != LG_HAMAKER_NONE ? 1 : 0;
+        A.last = fuse_kick ? 0 : 1;
+        A.assign = s->step_assign;
+        A.min_blocks = s->step_min_blocks;
+        A.items = ((n + 31) / 32) * (2 * A.contacts + A.slices * A.hamaker);
+        A.hdt_hi = (float)hdt;
+        A.hdt_lo = (float)(hdt - (double)A.hdt_hi);
+        A.dt_hi = (float)dt;
+        A.dt_lo = (float)(dt - (double)A.dt_hi);
+        MixedExtra MX = s->mx;
+        MX.x64 = prev_fused ? nullptr : s->x;  // FP64 positions are current unless the last step ran in float-float
+        kernels = launch_step_mixed(s->P, S, pv, s->bv, MX, A, s->stream);
+        s->fstep++;
+        if (fuse_kick) {  // the next step reads the buffers this one wrote
+            s->ffcur = nf;
+            set_ff_buffers(s);
+        }
+    } else if (s->precision == LG_PRECISION_MIXED) {
+        if (compact || persistent)
             kernels = launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, fuse_kick,
                                                   prev_fused, s->mx, s->stream, s->side, s->fork_ev, s->join_ev);
         else
@@ -501,7 +558,8 @@ static int step_once(lg_system *s, double dt, int64_t rebuild_every, bool fuse_n
         s->launches += 1;
     }
     const int mv = (s->facet_auto_move && s->P.n_facets > 0) ? 1 : 0;
-    const bool fuse = fuse_next && ((s->precision == LG_PRECISION_MIXED && s->kernel == LG_FORCE_KERNEL_COMPACT) ||
+    const bool fuse = fuse_next && ((s->precision == LG_PRECISION_MIXED && (s->kernel == LG_FORCE_KERNEL_COMPACT ||
+                                                                            s->kernel == LG_FORCE_KERNEL_PERSISTENT)) ||
                                     (s->precision == LG_PRECISION_FP64 && s->kernel == LG_FORCE_KERNEL_PAIRS));
     LG_TRY(launch_forces(s, hdt, dt, mv, fuse, prev_fused));
     s->kick_done = fuse;
@@ -554,7 +612,9 @@ static int check_args(const lg_system_desc *d) {
     if (d->neck_mode != LG_NECK_PER_BOND && d->neck_mode != LG_NECK_REFERENCE_INDEXING) return lg_fail(LG_E_INVALID, "lg_create: unknown neck_mode %d", d->neck_mode);
     if (d->max_neighbors < 0 || d->max_neighbors > 255)
         return lg_fail(LG_E_INVALID, "lg_create: max_neighbors must be in [0, 255]");
-    if (d->force_kernel < 0 || d->force_kernel > 3) return lg_fail(LG_E_INVALID, "lg_create: unknown force_kernel %d", d->force_kernel);
+    if (d->force_kernel < 0 || d->force_kernel > 4) return lg_fail(LG_E_INVALID, "lg_create: unknown force_kernel %d", d->force_kernel);
+    if (d->force_kernel == LG_FORCE_KERNEL_PERSISTENT && d->precision != LG_PRECISION_MIXED)
+        return lg_fail(LG_E_INVALID, "lg_create: the persistent step kernel is mixed precision only");
     LG_TRY(validate_hold(d->hold_mask, d->n_part));
     LG_TRY(validate_unary(&d->body, d->unary_hook));
     if (d->force_kernel == LG_FORCE_KERNEL_PAIRS && d->precision != LG_PRECISION_FP64)
@@ -982,8 +1042,11 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     LG_TRY(s->alloc(&s->obs_out, 32));
 
     if (s->precision == LG_PRECISION_MIXED) {
-        LG_TRY(s->alloc(&s->x32, 2 * (size_t)n));  // float-float: high parts, then low parts
-        LG_TRY(s->alloc(&s->v32, 3 * (size_t)n));  // v high parts, v low parts, spins
+        LG_TRY(s->alloc(&s->x32buf, 4 * (size_t)n));  // two buffers of float-float positions (hi, lo interleaved)
+        LG_TRY(s->alloc(&s->v32buf, 6 * (size_t)n));  // two buffers of v high parts, v low parts, spins
+        s->ffcur = 0;
+        s->x32 = s->x32buf;
+        s->v32 = s->v32buf;
         LG_TRY(s->alloc(&s->s32, 5 * (size_t)n));  // spin low parts, displacement and rotation of a run
         LG_TRY(s->alloc(&s->csum, 3 * (size_t)n));
         LG_TRY(s->alloc(&s->d_flag, 1));
@@ -1053,6 +1116,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     if (s->kernel < 0)
         return lg_fail(LG_E_INVALID, "lg_create: the pair-parallel force kernel takes at most %lld pair slots",
                        (long long)kPairsMaxSlots);
+    if (s->kernel == LG_FORCE_KERNEL_PERSISTENT) LG_TRY(ensure_step_buffers(s));
     if (d->threads_per_row > 0 && d->force_kernel == LG_FORCE_KERNEL_AUTO) s->kernel = LG_FORCE_KERNEL_ROWGROUP;
     LG_TRY(apply_hold(s, d->hold_mask));
     LG_TRY(apply_unary(s, &d->body, d->unary_hook, d->unary_hook_user));
@@ -1097,10 +1161,13 @@ extern "C" int lg_destroy(lg_system *s) {
 // Run `period` steps as one CUDA graph (captured on first use for this pointer parity). The host
 // bookkeeping (buffer parities, step index) advances exactly as step_once advances it.
 static int run_period_graph(lg_system *s, double dt, int64_t period, int64_t rebuild_every) {
-    lg_system::GraphKey key{dt, period, s->kernel, s->T, s->vcur, s->pcur, s->fcur};
+    lg_system::GraphKey key{dt, period, s->kernel, s->T, s->vcur, s->pcur, s->fcur, s->ffcur, (int)(s->fstep & 1)};
     for (auto &g : s->graphs) {
         if (!(g.key == key)) continue;
         LG_CUDA(cudaGraphLaunch(g.exec, s->stream));
+        s->ffcur ^= g.ff_flips;
+        s->fstep += g.f_launches;
+        set_ff_buffers(s);
         // replay the host-side state transitions of `period` steps
         for (int64_t k = 0; k < period; ++k) {
             if (s->P.pairs == LG_PAIRS_VERLET && rebuild_every > 0 && (s->step_index % rebuild_every) == 0) {
@@ -1115,6 +1182,8 @@ static int run_period_graph(lg_system *s, double dt, int64_t period, int64_t reb
         return LG_OK;
     }
     const int64_t l0 = s->launches;
+    const int ff0 = s->ffcur;
+    const int64_t fs0 = s->fstep;
     LG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     int rc = LG_OK;
     for (int64_t k = 0; k < period && rc == LG_OK; ++k) rc = step_once(s, dt, rebuild_every, k + 1 < period);
@@ -1129,7 +1198,7 @@ static int run_period_graph(lg_system *s, double dt, int64_t period, int64_t reb
     ec = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     if (ec != cudaSuccess) return lg_fail(LG_E_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ec));
-    s->graphs.push_back({key, exec, s->launches - l0});
+    s->graphs.push_back({key, exec, s->launches - l0, s->ffcur ^ ff0, s->fstep - fs0});
     LG_CUDA(cudaGraphLaunch(exec, s->stream));
     return LG_OK;
 }
@@ -1321,6 +1390,30 @@ extern "C" int lg_set_state(lg_system *s, const double *x, const double *v, cons
     return state_upload(s, host);
 }
 
+extern "C" int lg_set_step_shape(lg_system *s, int32_t min_blocks, int32_t slices, int32_t assign) {
+    LG_HANDLE(s);
+    if (s->precision != LG_PRECISION_MIXED) return lg_fail(LG_E_INVALID, "lg_set_step_shape: mixed precision only");
+    if (min_blocks != 0 && min_blocks != 4 && min_blocks != 5 && min_blocks != 6)
+        return lg_fail(LG_E_INVALID, "lg_set_step_shape: min_blocks must be 0, 4, 5 or 6");
+    if (slices != 0 && slices != 1 && slices != 2 && slices != 4)
+        return lg_fail(LG_E_INVALID, "lg_set_step_shape: slices must be 0, 1, 2 or 4");
+    if (assign != 0 && assign != 1) return lg_fail(LG_E_INVALID, "lg_set_step_shape: assign must be 0 or 1");
+    LG_TRY(ensure_step_buffers(s));
+    s->step_min_blocks = min_blocks ? min_blocks : 4;
+    s->step_slices = slices ? slices : mixed_hamaker_slices(s->P.n);
+    s->step_assign = assign;
+    s->drop_graphs();  // the graphs hold the previous shape's launches
+    return LG_OK;
+}
+
+extern "C" int lg_get_step_shape(lg_system *s, int32_t *min_blocks, int32_t *slices, int32_t *assign) {
+    LG_HANDLE(s);
+    if (min_blocks) *min_blocks = s->step_min_blocks;
+    if (slices) *slices = s->step_slices ? s->step_slices : mixed_hamaker_slices(s->P.n);
+    if (assign) *assign = s->step_assign;
+    return LG_OK;
+}
+
 extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
     LG_HANDLE(s);
     if (T == 0) {
@@ -1335,11 +1428,14 @@ extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
 
 extern "C" int lg_set_force_kernel(lg_system *s, int32_t variant) {
     LG_HANDLE(s);
-    if (variant < 0 || variant > 3) return lg_fail(LG_E_INVALID, "lg_set_force_kernel: unknown variant %d", variant);
+    if (variant < 0 || variant > 4) return lg_fail(LG_E_INVALID, "lg_set_force_kernel: unknown variant %d", variant);
     const int k = choose_kernel(s, variant);
+    if (k < 0 && variant == LG_FORCE_KERNEL_PERSISTENT)
+        return lg_fail(LG_E_INVALID, "lg_set_force_kernel: the persistent step kernel is mixed precision only");
     if (k < 0)
         return lg_fail(LG_E_INVALID, "lg_set_force_kernel: the pair-parallel kernel is FP64 only and takes at most "
                        "%lld pair slots", (long long)kPairsMaxSlots);
+    if (k == LG_FORCE_KERNEL_PERSISTENT) LG_TRY(ensure_step_buffers(s));
     s->kernel = k;
     return LG_OK;
 }
@@ -1698,8 +1794,110 @@ extern "C" int lg_batch_get_observables(lg_system *s, lg_observables *out) {
 #include <mutex>
 #include <tuple>
 
+// Autotuner cache: (precision, pairs, binary model, Hamaker model, log2 n, batch) -> choice.
+using TuneKey = std::tuple<int, int, int, int, int, int>;
 static std::mutex g_tune_mu;
-static std::map<std::tuple<int, int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
+static std::map<TuneKey, lg_tuning> g_tune_cache;
+
+static TuneKey tune_key(int precision, int pairs, int bm, int hm, int64_t n, int batch) {
+    int lg2 = 0;
+    while (((int64_t)1 << (lg2 + 1)) <= n) ++lg2;
+    return std::make_tuple(precision, pairs, bm, hm, lg2, batch ? 1 : 0);
+}
+
+static lg_tuning tuning_of(const lg_system *s) {
+    lg_tuning t{};
+    t.force_kernel = s->kernel;
+    t.threads_per_row = s->T;
+    t.step_min_blocks = s->step_min_blocks;
+    t.step_slices = s->step_slices ? s->step_slices : mixed_hamaker_slices(s->P.n);
+    t.step_assign = s->step_assign;
+    return t;
+}
+
+static int apply_tuning(lg_system *s, const lg_tuning &t) {
+    if (t.force_kernel == LG_FORCE_KERNEL_PERSISTENT) {
+        if (s->precision != LG_PRECISION_MIXED) return lg_fail(LG_E_INVALID, "tuning: persistent kernel on FP64");
+        LG_TRY(ensure_step_buffers(s));
+        s->step_min_blocks = t.step_min_blocks;
+        s->step_slices = t.step_slices;
+        s->step_assign = t.step_assign;
+    }
+    if (t.force_kernel == LG_FORCE_KERNEL_PAIRS && !s->pres) return lg_fail(LG_E_INVALID, "tuning: no pair-parallel scratch");
+    s->kernel = t.force_kernel;
+    s->T = t.threads_per_row;
+    return LG_OK;
+}
+
+extern "C" int lg_get_tuning(lg_system *s, lg_tuning *out) {
+    LG_HANDLE(s);
+    if (!out) return lg_fail(LG_E_INVALID, "lg_get_tuning: null output");
+    *out = tuning_of(s);
+    return LG_OK;
+}
+
+extern "C" int lg_autotune_cache_lookup(const lg_system_desc *d, int64_t n, int32_t batch, lg_tuning *out) {
+    if (!d || !out || n < 1) return lg_fail(LG_E_INVALID, "lg_autotune_cache_lookup: bad arguments");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(tune_key(d->precision, d->pairs, d->binary_model, d->hamaker_model, n, batch));
+    if (it == g_tune_cache.end()) return lg_fail(LG_E_STATE, "lg_autotune_cache_lookup: no entry");
+    *out = it->second;
+    return LG_OK;
+}
+
+extern "C" int lg_autotune_cache_save(const char *path) {
+    if (!path) return lg_fail(LG_E_INVALID, "lg_autotune_cache_save: null path");
+    FILE *f = std::fopen(path, "w");
+    if (!f) return lg_fail(LG_E_INVALID, "lg_autotune_cache_save: cannot open %s", path);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    std::fprintf(f, "# libgran_gb300 autotune cache: precision pairs binary hamaker log2n batch : kernel T "
+                    "min_blocks slices assign ms_per_step\n");
+    for (auto &e : g_tune_cache) {
+        const TuneKey &k = e.first;
+        const lg_tuning &t = e.second;
+        std::fprintf(f, "%d %d %d %d %d %d : %d %d %d %d %d %.9g\n", std::get<0>(k), std::get<1>(k), std::get<2>(k),
+                     std::get<3>(k), std::get<4>(k), std::get<5>(k), t.force_kernel, t.threads_per_row,
+                     t.step_min_blocks, t.step_slices, t.step_assign, t.ms_per_step);
+    }
+    const bool ok = std::fclose(f) == 0;
+    return ok ? LG_OK : lg_fail(LG_E_INVALID, "lg_autotune_cache_save: write to %s failed", path);
+}
+
+extern "C" int lg_autotune_cache_load(const char *path) {
+    if (!path) return lg_fail(LG_E_INVALID, "lg_autotune_cache_load: null path");
+    FILE *f = std::fopen(path, "r");
+    if (!f) return lg_fail(LG_E_INVALID, "lg_autotune_cache_load: cannot open %s", path);
+    char line[512];
+    int lineno = 0, rc = LG_OK;
+    std::map<TuneKey, lg_tuning> add;
+    while (std::fgets(line, sizeof line, f)) {
+        ++lineno;
+        if (line[0] == '#' || line[0] == '\n') continue;
+        int k[6];
+        lg_tuning t{};
+        if (std::sscanf(line, "%d %d %d %d %d %d : %d %d %d %d %d %lf", &k[0], &k[1], &k[2], &k[3], &k[4], &k[5],
+                        &t.force_kernel, &t.threads_per_row, &t.step_min_blocks, &t.step_slices, &t.step_assign,
+                        &t.ms_per_step) != 12 ||
+            t.force_kernel < 1 || t.force_kernel > 4 || t.threads_per_row < 1 || t.threads_per_row > 32 ||
+            (t.step_min_blocks < 4 || t.step_min_blocks > 6) || (t.step_slices != 1 && t.step_slices != 2 && t.step_slices != 4) ||
+            (t.step_assign != 0 && t.step_assign != 1)) {
+            rc = lg_fail(LG_E_INVALID, "lg_autotune_cache_load: %s line %d is not a cache entry", path, lineno);
+            break;
+        }
+        add[std::make_tuple(k[0], k[1], k[2], k[3], k[4], k[5])] = t;
+    }
+    std::fclose(f);
+    if (rc != LG_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto &e : add) g_tune_cache[e.first] = e.second;
+    return LG_OK;
+}
+
+extern "C" int lg_autotune_cache_clear(void) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache.clear();
+    return LG_OK;
+}
 
 static int snapshot_take(lg_system *s) {
     if (s->snap.empty()) {
@@ -1718,8 +1916,8 @@ static int snapshot_take(lg_system *s) {
         addb(s->fv[0], sizeof(double) * 9 * (size_t)nf);
         addb(s->fv[1], sizeof(double) * 9 * (size_t)nf);
         addb(s->err, sizeof(int32_t));
-        if (s->x32) addb(s->x32, sizeof(float4) * 2 * n);
-        if (s->v32) addb(s->v32, sizeof(float4) * 3 * n);
+        if (s->x32buf) addb(s->x32buf, sizeof(float4) * 4 * n);
+        if (s->v32buf) addb(s->v32buf, sizeof(float4) * 6 * n);
         if (s->s32) addb(s->s32, sizeof(float4) * 5 * n);
         const int npv = s->P.pairs == LG_PAIRS_VERLET ? 2 : 1;
         for (int q = 0; q < npv; ++q) {
@@ -1757,6 +1955,7 @@ static int snapshot_take(lg_system *s) {
     s->snap_vcur = s->vcur;
     s->snap_pcur = s->pcur;
     s->snap_fcur = s->fcur;
+    s->snap_ffcur = s->ffcur;
     s->snap_step = s->step_index;
     s->snap_built = s->list_built;
     return LG_OK;
@@ -1768,6 +1967,8 @@ static int snapshot_restore(lg_system *s) {
     s->vcur = s->snap_vcur;
     s->pcur = s->snap_pcur;
     s->fcur = s->snap_fcur;
+    s->ffcur = s->snap_ffcur;
+    set_ff_buffers(s);
     s->step_index = s->snap_step;
     s->list_built = s->snap_built;
     return LG_OK;
@@ -1787,16 +1988,21 @@ extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t
                            int32_t *T_out, int32_t use_cache) {
     LG_HANDLE(s);
     if (probe_steps < 1) return lg_fail(LG_E_INVALID, "lg_autotune: probe_steps < 1");
-    int lg2 = 0;
-    while (((int64_t)1 << (lg2 + 1)) <= s->P.n) ++lg2;
-    auto key = std::make_tuple(s->precision, s->P.pairs, s->P.binary_model, s->P.hamaker_model, lg2,
-                               s->n_systems > 0 ? 1 : 0);
+    const TuneKey key = tune_key(s->precision, s->P.pairs, s->P.binary_model, s->P.hamaker_model, s->P.n,
+                                 s->n_systems > 0 ? 1 : 0);
     if (use_cache) {
-        std::lock_guard<std::mutex> lk(g_tune_mu);
-        auto it = g_tune_cache.find(key);
-        if (it != g_tune_cache.end()) {
-            s->kernel = it->second.first;
-            s->T = it->second.second;
+        lg_tuning hit{};
+        bool found = false;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end()) {
+                hit = it->second;
+                found = true;
+            }
+        }
+        if (found && apply_tuning(s, hit) == LG_OK) {
+            s->drop_graphs();
             if (kernel_out) *kernel_out = s->kernel;
             if (T_out) *T_out = s->T;
             return LG_OK;
@@ -1804,36 +2010,51 @@ extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t
     }
     // candidates run on the live system between a snapshot and its restore
     LG_TRY(snapshot_take(s));
-    const int keep_kernel = s->kernel, keep_T = s->T;
+    const lg_tuning keep = tuning_of(s);
     const int64_t keep_launch = s->launches;
-    std::vector<std::pair<int, int>> cands;
-    cands.emplace_back(LG_FORCE_KERNEL_COMPACT, 1);
-    if (s->pres) cands.emplace_back(LG_FORCE_KERNEL_PAIRS, 1);
-    for (int T = 1; T <= 32; T *= 2) cands.emplace_back(LG_FORCE_KERNEL_ROWGROUP, T);
+    std::vector<lg_tuning> cands;
+    auto add = [&](int k, int T, int mb, int sl, int asg) {
+        lg_tuning t{};
+        t.force_kernel = k;
+        t.threads_per_row = T;
+        t.step_min_blocks = mb;
+        t.step_slices = sl;
+        t.step_assign = asg;
+        cands.push_back(t);
+    };
+    const int sl0 = mixed_hamaker_slices(s->P.n);
+    add(LG_FORCE_KERNEL_COMPACT, 1, 4, sl0, 0);
+    if (s->pres) add(LG_FORCE_KERNEL_PAIRS, 1, 4, sl0, 0);
+    for (int T = 1; T <= 32; T *= 2) add(LG_FORCE_KERNEL_ROWGROUP, T, 4, sl0, 0);
+    if (s->precision == LG_PRECISION_MIXED)
+        for (int mb = 4; mb <= 6; ++mb)
+            for (int sl = 1; sl <= 4; sl *= 2)
+                for (int asg = 0; asg <= 1; ++asg) add(LG_FORCE_KERNEL_PERSISTENT, 1, mb, sl, asg);
     double best = 1e300;
-    std::pair<int, int> pick(keep_kernel, keep_T);
+    lg_tuning pick = keep;
     for (auto &c : cands) {
-        s->kernel = c.first;
-        s->T = c.second;
-        float ms = 0.f;
-        int rc = lg_step(s, dt, probe_steps, rebuild_every);  // warm-up (and graph capture)
+        int rc = apply_tuning(s, c);
+        float ms = 0.f, ms2 = 0.f;
+        if (rc == LG_OK) rc = lg_step(s, dt, probe_steps, rebuild_every);  // warm-up (and graph capture)
         if (rc == LG_OK) rc = snapshot_restore(s);
         if (rc == LG_OK) rc = lg_step_timed(s, dt, probe_steps, rebuild_every, &ms);
-        int rc2 = snapshot_restore(s);
+        if (rc == LG_OK) rc = snapshot_restore(s);
+        if (rc == LG_OK) rc = lg_step_timed(s, dt, probe_steps, rebuild_every, &ms2);
+        const int rc2 = snapshot_restore(s);
         if (rc != LG_OK || rc2 != LG_OK) {
-            s->kernel = keep_kernel;
-            s->T = keep_T;
+            apply_tuning(s, keep);
             return rc != LG_OK ? rc : rc2;
         }
-        if (ms < best) {
-            best = ms;
+        const double t = std::min(ms, ms2) / (double)probe_steps;
+        if (t < best) {
+            best = t;
             pick = c;
+            pick.ms_per_step = t;
         }
     }
     LG_CUDA(cudaStreamSynchronize(s->stream));
     s->launches = keep_launch;
-    s->kernel = pick.first;
-    s->T = pick.second;
+    LG_TRY(apply_tuning(s, pick));
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune_cache[key] = pick;

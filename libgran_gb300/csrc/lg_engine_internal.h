@@ -44,8 +44,18 @@ struct lg_system {
     double *obs_out = nullptr;
 
     // mixed precision: FP32 position copy for culling
-    float4 *x32 = nullptr;  // mixed: [2n] float-float positions
-    float4 *v32 = nullptr;  // mixed: [3n] float-float velocities, FP32 spins
+    float4 *x32 = nullptr;  // mixed: [2n] float-float positions (the current one of the two buffers)
+    float4 *v32 = nullptr;  // mixed: [3n] float-float velocities, FP32 spins (current buffer)
+    // mixed: both buffers of the double-buffered float-float positions ([2][2n]) and velocities
+    // ([2][3n]); the persistent step kernel reads one and writes the other, ffcur names the current
+    float4 *x32buf = nullptr, *v32buf = nullptr;
+    int ffcur = 0;
+    int64_t fstep = 0;             // persistent step launches so far (their item counters alternate)
+    unsigned *step_ctr = nullptr;  // persistent step: [2 + groups] item and arrival counters
+    float4 *hpart = nullptr;       // persistent step: [4][2n] Hamaker partial sums (up to 4 slices)
+    // persistent step shape: Hamaker slices per group, register budget (resident blocks per SM),
+    // item assignment (0 pulled from a counter, 1 round robin)
+    int step_slices = 0, step_min_blocks = 4, step_assign = 0;
     float4 *s32 = nullptr;  // mixed: [5n] spin low parts, a run's displacement and rotation (float-float)
     float4 *csum = nullptr;    // mixed: [3n] contact sums (float-float)
     float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
@@ -88,16 +98,18 @@ struct lg_system {
     struct GraphKey {
         double dt;
         int64_t period;
-        int kernel, T, vcur, pcur, fcur;
+        int kernel, T, vcur, pcur, fcur, ffcur, fpar;
         bool operator==(const GraphKey &o) const {
             return dt == o.dt && period == o.period && kernel == o.kernel && T == o.T && vcur == o.vcur &&
-                   pcur == o.pcur && fcur == o.fcur;
+                   pcur == o.pcur && fcur == o.fcur && ffcur == o.ffcur && fpar == o.fpar;
         }
     };
     struct GraphEntry {
         GraphKey key;
         cudaGraphExec_t exec;
         int64_t launches;
+        int ff_flips;        // float-float buffer swaps of the period (persistent steps)
+        int64_t f_launches;  // persistent step launches of the period
     };
     std::vector<GraphEntry> graphs;
     bool use_graphs = true;
@@ -110,7 +122,7 @@ struct lg_system {
         size_t bytes;
     };
     std::vector<SnapBuf> snap;
-    int snap_vcur = 0, snap_pcur = 0, snap_fcur = 0;
+    int snap_vcur = 0, snap_pcur = 0, snap_fcur = 0, snap_ffcur = 0;
     int64_t snap_step = 0;
     bool snap_built = false;
 

@@ -122,6 +122,31 @@ void launch_kick_drift_mixed(int64_t n, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, con
                              double hdt, const double *origin, const int32_t *agg, const dbl4 *orig, float4 *x32,
                              float4 *v32, float4 *s32, const uint8_t *hold, cudaStream_t st);
 
+// Slices per 32-row group of the mixed Hamaker work (launch size rule shared by both mixed paths:
+// the same slicing gives the same bits).
+int mixed_hamaker_slices(int64_t n);
+
+// Persistent step of the mixed path (lg_step_mixed.cu): the force evaluation and float-float
+// completion of one step inside a run of steps as one launch whose warps pull work items (per
+// 32-row group: two contact items, `slices` Hamaker items) from a device counter; the warp that
+// finishes a group's last item completes its rows. For plain runs only (no facets, body terms or
+// held particles).
+struct StepArgs {
+    float4 *x32n, *v32n;  // the other buffers of the double-buffered float-float state (written)
+    float4 *hpart;        // [slices][2n] Hamaker partial sums per slice
+    unsigned *ctr;        // [2 + groups]: item counters of alternate launches, then group arrivals
+    int par;              // item counter of this launch (0 / 1, alternating launch by launch)
+    int slices;           // Hamaker items per group
+    int contacts, hamaker;  // which item kinds exist
+    int last;             // the run's last step: write the FP64 state instead of the next step's
+    int assign;           // 0: warps pull items from ctr[par]; 1: warp g takes items g, g + W, ...
+    int min_blocks;       // register budget: resident blocks per SM (4, 5 or 6)
+    int64_t items;        // groups * (2 * contacts + slices * hamaker)
+    float hdt_hi, hdt_lo, dt_hi, dt_lo;  // dt / 2 and dt as float-float values
+};
+int launch_step_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
+                      const MixedExtra &MX, const StepArgs &A, cudaStream_t st);
+
 // Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                 double dt, int move_facets, cudaStream_t st);

@@ -78,7 +78,7 @@ extern "C" int64_t lg_estimate_device_bytes(const lg_system_desc *d, int64_t n) 
     const int64_t cap = d->pairs == LG_PAIRS_VERLET ? (d->max_neighbors > 0 ? d->max_neighbors : 64) : std::max<int64_t>(n - 1, 1);
     const int64_t nbuf = d->pairs == LG_PAIRS_VERLET ? 2 : 1;
     int64_t b = 10 * 32 * n;                                  // x, th, v[2], w[2], a, al (+ slack)
-    b += 240 * n;                                             // float-float state (x32, v32, s32) and partial sums
+    b += 320 * n;                                             // float-float state (two x32, v32; s32) and partial sums
     b += nbuf * cap * n * (4 + 4 + 72 + 5) + nbuf * 8 * n;   // nbr, flags, springs, near lists, row lengths
     b += 8 * n * (1 + 1 + 8 + 72);                            // bonds (up to 8 per particle)
     b += 72 * std::max(d->n_facets, 1) * n;                   // facet springs

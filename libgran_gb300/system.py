@@ -106,6 +106,15 @@ class System:
     def set_threads_per_row(self, T):
         A.check(A.lib().lg_set_threads_per_row(self.h, int(T)), "lg_set_threads_per_row")
 
+    def set_step_shape(self, min_blocks=0, slices=0, assign=0):
+        """Shape of the persistent step kernel (register budget, Hamaker slices, item assignment)."""
+        A.check(A.lib().lg_set_step_shape(self.h, int(min_blocks), int(slices), int(assign)), "lg_set_step_shape")
+
+    def step_shape(self):
+        mb, sl, asg = C.c_int32(), C.c_int32(), C.c_int32()
+        A.check(A.lib().lg_get_step_shape(self.h, C.byref(mb), C.byref(sl), C.byref(asg)), "lg_get_step_shape")
+        return {"min_blocks": mb.value, "slices": sl.value, "assign": asg.value}
+
     def set_force_kernel(self, variant):
         A.check(A.lib().lg_set_force_kernel(self.h, int(variant)), "lg_set_force_kernel")
 
@@ -178,6 +187,12 @@ class System:
         A.check(A.lib().lg_autotune(self.h, float(dt), int(probe_steps), int(rebuild_every), C.byref(k), C.byref(t),
                                     1 if use_cache else 0), "lg_autotune")
         return k.value, t.value
+
+    def tuning(self):
+        """The handle's kernel choice and shape (lg_tuning as a dict)."""
+        t = A.lg_tuning()
+        A.check(A.lib().lg_get_tuning(self.h, C.byref(t)), "lg_get_tuning")
+        return t.as_dict()
 
     def device_errors(self):
         e = C.c_int32()

@@ -56,6 +56,8 @@ def test_create_rejects_bad_descriptors_before_touching_a_gpu():
         K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), n_facets=9),
         K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), precision=A.LG_PRECISION_MIXED,
                     force_kernel=A.LG_FORCE_KERNEL_PAIRS),
+        K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), force_kernel=A.LG_FORCE_KERNEL_PERSISTENT),
+        K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), force_kernel=5),
     ]
     d = K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact())
     K.set_hold(d, np.array([0, 16, 0, 0], dtype=np.uint8))  # unknown bit
@@ -115,3 +117,43 @@ def test_noalloc_refuses_bad_arguments_before_any_cuda_call():
     assert L.lg_observables_noalloc(None, 1, 1, 10, 1.0, 1.0, 1, None) == A.LG_E_INVALID
     assert L.lg_observables_noalloc(1, 1, 1, 10, 1.0, 1.0, None, None) == A.LG_E_INVALID
     assert b"null" in L.lg_last_error()
+
+
+def test_autotune_cache_round_trip(tmp_path):
+    """The autotuner's cache on the host: entries loaded from a file are found for descriptors of
+    the same precision, pair mode, functor set, log2 size and batch flag (and only for those), saved
+    entries read back identically, and a malformed file is refused without changing the cache."""
+    L = A.lib()
+    mat = K.Material()
+    assert L.lg_autotune_cache_clear() == A.LG_OK
+    d = K.make_desc(32768, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, contact=mat.contact(), hamaker=mat.hamaker(),
+                    pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r, precision=A.LG_PRECISION_MIXED)
+    t = A.lg_tuning()
+    assert L.lg_autotune_cache_lookup(C.byref(d), 32768, 0, C.byref(t)) == A.LG_E_STATE
+    f = tmp_path / "tune.txt"
+    # precision pairs binary hamaker log2n batch : kernel T min_blocks slices assign ms_per_step
+    f.write_text("# a comment\n%d %d %d %d 15 0 : 4 1 5 2 0 0.0405\n%d %d %d %d 15 1 : 2 1 4 4 0 0.5\n"
+                 % (A.LG_PRECISION_MIXED, A.LG_PAIRS_VERLET, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED,
+                    A.LG_PRECISION_MIXED, A.LG_PAIRS_VERLET, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED))
+    assert L.lg_autotune_cache_load(str(f).encode()) == A.LG_OK
+    for n in (32768, 40000, 65535):  # same power-of-two bucket
+        assert L.lg_autotune_cache_lookup(C.byref(d), n, 0, C.byref(t)) == A.LG_OK
+        assert t.as_dict() == {"force_kernel": A.LG_FORCE_KERNEL_PERSISTENT, "threads_per_row": 1,
+                               "step_min_blocks": 5, "step_slices": 2, "step_assign": 0, "ms_per_step": 0.0405}
+    assert L.lg_autotune_cache_lookup(C.byref(d), 32768, 1, C.byref(t)) == A.LG_OK
+    assert t.force_kernel == A.LG_FORCE_KERNEL_COMPACT and t.step_slices == 4
+    assert L.lg_autotune_cache_lookup(C.byref(d), 16384, 0, C.byref(t)) == A.LG_E_STATE
+    d64 = K.make_desc(32768, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, contact=mat.contact(), hamaker=mat.hamaker(),
+                      pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r)
+    assert L.lg_autotune_cache_lookup(C.byref(d64), 32768, 0, C.byref(t)) == A.LG_E_STATE
+    g = tmp_path / "saved.txt"
+    assert L.lg_autotune_cache_save(str(g).encode()) == A.LG_OK
+    assert L.lg_autotune_cache_clear() == A.LG_OK
+    assert L.lg_autotune_cache_lookup(C.byref(d), 32768, 0, C.byref(t)) == A.LG_E_STATE
+    assert L.lg_autotune_cache_load(str(g).encode()) == A.LG_OK
+    assert L.lg_autotune_cache_lookup(C.byref(d), 32768, 0, C.byref(t)) == A.LG_OK and t.step_min_blocks == 5
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1 1 1 2 15 0 : 9 1 4 1 0 1.0\n")
+    assert L.lg_autotune_cache_load(str(bad).encode()) == A.LG_E_INVALID
+    assert L.lg_autotune_cache_lookup(C.byref(d), 32768, 0, C.byref(t)) == A.LG_OK and t.step_min_blocks == 5
+    assert L.lg_autotune_cache_clear() == A.LG_OK

@@ -99,12 +99,24 @@ def test_autotuner_picks_a_valid_variant():
                np.concatenate(xs), np.concatenate(vs), sizes=sizes)
     before = [s.get(f) for f in FIELDS]
     k, T = s.autotune(mat.dt, probe_steps=20, rebuild_every=20, use_cache=False)
-    assert k in (A.LG_FORCE_KERNEL_COMPACT, A.LG_FORCE_KERNEL_ROWGROUP)  # the pair-parallel kernel is FP64 only
+    assert k in (A.LG_FORCE_KERNEL_COMPACT, A.LG_FORCE_KERNEL_ROWGROUP, A.LG_FORCE_KERNEL_PERSISTENT)
     assert T in (1, 2, 4, 8, 16, 32)
+    t = s.tuning()
+    assert t["force_kernel"] == k and t["ms_per_step"] > 0
+    assert t["step_min_blocks"] in (4, 5, 6) and t["step_slices"] in (1, 2, 4) and t["step_assign"] in (0, 1)
     for f, b in zip(FIELDS, before):  # tuning leaves the state as it was
         assert np.array_equal(s.get(f), b)
     s.step(mat.dt, 40, 20)
     assert s.device_errors() == 0
+    # a second handle of the same kind takes the cached pick without timing anything
+    s2 = System(_desc(mat, sum(sizes), A.LG_BINARY_SINTER, A.LG_PRECISION_MIXED, kernel=A.LG_FORCE_KERNEL_AUTO),
+                np.concatenate(xs), np.concatenate(vs), sizes=sizes)
+    s2.autotune(mat.dt, probe_steps=20, rebuild_every=20, use_cache=True)
+    t2 = s2.tuning()
+    for key in ("force_kernel", "threads_per_row", "step_min_blocks", "step_slices", "step_assign"):
+        assert t2[key] == t[key], key
+    s2.step(mat.dt, 40, 20)
+    assert s2.device_errors() == 0
 
 
 def test_snapshot_restore_replays_identically():
