@@ -1437,6 +1437,7 @@ extern "C" int lg_set_force_kernel(lg_system *s, int32_t variant) {
                        "%lld pair slots", (long long)kPairsMaxSlots);
     if (k == LG_FORCE_KERNEL_PERSISTENT) LG_TRY(ensure_step_buffers(s));
     s->kernel = k;
+    s->tuned_ms = 0.0;
     return LG_OK;
 }
 
@@ -1812,6 +1813,7 @@ static lg_tuning tuning_of(const lg_system *s) {
     t.step_min_blocks = s->step_min_blocks;
     t.step_slices = s->step_slices ? s->step_slices : mixed_hamaker_slices(s->P.n);
     t.step_assign = s->step_assign;
+    t.ms_per_step = s->tuned_ms;
     return t;
 }
 
@@ -1826,6 +1828,7 @@ static int apply_tuning(lg_system *s, const lg_tuning &t) {
     if (t.force_kernel == LG_FORCE_KERNEL_PAIRS && !s->pres) return lg_fail(LG_E_INVALID, "tuning: no pair-parallel scratch");
     s->kernel = t.force_kernel;
     s->T = t.threads_per_row;
+    s->tuned_ms = t.ms_per_step;
     return LG_OK;
 }
 
@@ -2046,6 +2049,10 @@ extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t
             return rc != LG_OK ? rc : rc2;
         }
         const double t = std::min(ms, ms2) / (double)probe_steps;
+        if (!(t > 0.0)) {  // an event pair that measured nothing cannot rank a candidate
+            apply_tuning(s, keep);
+            return lg_fail(LG_E_CUDA, "lg_autotune: a candidate timed %g ms", t);
+        }
         if (t < best) {
             best = t;
             pick = c;

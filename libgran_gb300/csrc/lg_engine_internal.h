@@ -56,6 +56,7 @@ struct lg_system {
     // persistent step shape: Hamaker slices per group, register budget (resident blocks per SM),
     // item assignment (0 pulled from a counter, 1 round robin)
     int step_slices = 0, step_min_blocks = 4, step_assign = 0;
+    double tuned_ms = 0.0;         // the autotuner's time per step of the handle's current choice
     float4 *s32 = nullptr;  // mixed: [5n] spin low parts, a run's displacement and rotation (float-float)
     float4 *csum = nullptr;    // mixed: [3n] contact sums (float-float)
     float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
