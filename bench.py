@@ -497,9 +497,9 @@ def run_gb300(args, rank, world):
         restruct = restructuring_section(args, l2_flush)
     serving = None
     if os.environ.get("LG_BENCH_SERVING", "1") != "0":
-        lams = [float(v) for v in os.environ.get("LG_SERVE_LAMBDAS", "4,16").split(",")]
-        dur = float(os.environ.get("LG_SERVE_SECONDS", "15"))
-        serving = [serving_section(lam, dur) for lam in lams]
+        lams = [float(v) for v in os.environ.get("LG_SERVE_LAMBDAS", "8,32,64,128").split(",")]
+        dur = float(os.environ.get("LG_SERVE_SECONDS", "8"))
+        serving = {"sweep": [serving_section(lam, dur) for lam in lams], "accuracy": serving_force_error()}
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tm["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -581,16 +581,16 @@ def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):
     """Serving workload: Poisson arrivals at rate lam (requests/s) for duration_s seconds; each
     request an aggregate of log-uniform 64..8192 monomers with its own seed and a step budget drawn
     uniformly from 2e3..2e4 (multiples of 20), mixed precision, sintered bonds + contact + limited
-    Hamaker; a 150 GB device-memory budget. Reports request latency percentiles and the sustained
-    particle-steps/s of the whole run (submission of the first request to retirement of the last)."""
+    Hamaker; a 150 GB device-memory budget. Resident requests occupy slots of one batch (the
+    default size classes) and advance in the same launches. Reports request latency percentiles,
+    the sustained particle-steps/s of the whole run (submission of the first request to retirement
+    of the last), mean slot occupancy and resident particles."""
     from libgran_gb300 import _abi as A
     from libgran_gb300 import configs as K
     from libgran_gb300.serving import Server
     from libgran_gb300.system import generate_aggregate, generate_velocities
     mat = K.Material()
-    d = K.make_desc(1, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(), sinter=mat.sinter(),
-                    hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r,
-                    precision=A.LG_PRECISION_MIXED, max_neighbors=96)
+    d = serving_template(A.LG_PRECISION_MIXED)
     rng = np.random.default_rng(seed)
     t, arrivals = 0.0, []
     while True:
@@ -606,6 +606,7 @@ def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):
     srv = Server(d, budget_bytes=budget_bytes, dt=mat.dt)
     t0 = time.perf_counter()
     nxt = 0
+    busy, resident = [], []
     while True:
         now = time.perf_counter() - t0
         while nxt < len(arrivals) and arrivals[nxt][0] <= now:
@@ -613,6 +614,9 @@ def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):
             srv.submit(inputs[k][0], inputs[k][1], steps)
             nxt += 1
         a, q, _ = srv.tick()
+        st = srv.stats()
+        busy.append(st["slots_busy"])
+        resident.append(st["resident_particles"])
         if nxt >= len(arrivals) and a == 0 and q == 0:
             break
         if a == 0 and q == 0 and nxt < len(arrivals):
@@ -623,7 +627,44 @@ def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):
     return {"lambda_per_s": lam, "requests": len(arrivals), "completed": st["completed"], "failed": st["failed"],
             "p50_latency_ms": st["p50_latency_ms"], "p99_latency_ms": st["p99_latency_ms"],
             "max_latency_ms": st["max_latency_ms"], "particle_steps_per_s": st["particle_steps"] / wall,
-            "wall_s": wall, "peak_bytes": st["peak_bytes"], "budget_bytes": budget_bytes}
+            "offered_particle_steps_per_s": sum(n * steps for (_, n, steps, _) in arrivals) / duration_s,
+            "wall_s": wall, "peak_bytes": st["peak_bytes"], "budget_bytes": budget_bytes, "slots": st["slots"],
+            "slot_particles": st["slot_particles"], "mean_slots_busy": float(np.mean(busy)) if busy else 0.0,
+            "mean_resident_particles": float(np.mean(resident)) if resident else 0.0}
+
+
+def serving_template(precision):
+    from libgran_gb300 import _abi as A
+    from libgran_gb300 import configs as K
+    mat = K.Material()
+    return K.make_desc(1, A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(), sinter=mat.sinter(),
+                       hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r, precision=precision,
+                       max_neighbors=96)
+
+
+def serving_force_error():
+    """Mixed against FP64 forces and torques of serving requests at identical states: requests of
+    64, 1024 and 8192 monomers (the size range) as submitted, both precisions' construction force
+    evaluations (normwise relative error over the request)."""
+    from libgran_gb300 import _abi as A
+    from libgran_gb300 import configs as K
+    from libgran_gb300.system import System, generate_aggregate, generate_velocities
+    mat = K.Material()
+    out = {"force_rel_err_max": 0.0, "torque_rel_err_max": 0.0, "sizes": [64, 1024, 8192]}
+    for k, n in enumerate(out["sizes"]):
+        x0, v0 = generate_aggregate((4 << 32) + 10 ** 6 + k, n, mat.r), generate_velocities((4 << 32) + 10 ** 6 + k, n, 0.1)
+        res = []
+        for prec in (A.LG_PRECISION_FP64, A.LG_PRECISION_MIXED):
+            d = serving_template(prec)
+            d.n_part = n
+            s = System(d, x0, v0)
+            res.append((s.get(A.LG_FIELD_A), s.get(A.LG_FIELD_ALPHA)))
+            s.close()
+        (fa, ta), (fb, tb) = res
+        out["force_rel_err_max"] = max(out["force_rel_err_max"], float(np.abs(fa - fb).max() / np.abs(fa).max()))
+        out["torque_rel_err_max"] = max(out["torque_rel_err_max"],
+                                        float(np.abs(ta - tb).max() / max(np.abs(ta).max(), 1e-300)))
+    return out
 
 
 def combine_ranks(ms, units_per_rank, world, all_reduce_max=None):

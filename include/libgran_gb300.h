@@ -482,13 +482,20 @@ int lg_step_timed(lg_system *sys, double dt, int64_t nsteps, int64_t rebuild_eve
 
 /* ---- serving: continuous batching of aggregate-mechanics requests ---------------------------
  * No counterpart in libgran (its drivers run one system per process). A server holds a system
- * template (functors, pair mode, precision), a device-memory budget and a step size. Requests (an
- * aggregate state and a step budget) may be submitted at any time; each lg_server_tick admits queued
- * requests that fit the budget (first come first served, with backfill), advances every resident
- * request by one rebuild period -- the requests' kernels are enqueued on their own streams before
- * any wait, so they overlap on the device -- and retires finished requests (observables and
- * positions copied back, memory returned to the budget). Each request is simulated exactly as it
- * would be alone. Latency = host time from submission to retirement. */
+ * template (functors, Verlet pairs, precision; no facets, body forces or hold masks), a
+ * device-memory budget and a step size, and keeps one batch of slots of fixed capacities (size
+ * classes; lg_server_set_slots, or by default 8 slots each of 128 .. 8192 monomers, fewer when the
+ * budget is small). Requests (an aggregate state and a step budget) may be submitted at any time;
+ * a request occupies the smallest free slot that holds it, and every resident request advances in
+ * the same launches, one rebuild period at a time. Each lg_server_tick waits for the period in
+ * flight, retires finished requests (observables and positions copied back, slot freed), admits
+ * queued requests into free slots at rebuild boundaries (first come first served, with backfill;
+ * each is first built alone from the template -- bond detection, construction force evaluation --
+ * and then moved into its slot on the device), launches the next period and prepares queued
+ * requests while it runs. A request evolves as it would alone: bit for bit in FP64, and in mixed
+ * precision when the lone run uses the server's Hamaker slicing (lg_server_stats.hamaker_slices,
+ * lg_set_step_shape) and step budgets are multiples of the rebuild period. Latency = host time from
+ * submission to retirement. */
 #define LG_REQ_QUEUED 0
 #define LG_REQ_RUNNING 1
 #define LG_REQ_DONE 2
@@ -501,15 +508,20 @@ typedef struct lg_server_stats {
     int64_t active, queued, completed, rejected, failed, cancelled;
     int64_t particle_steps;
     double p50_latency_ms, p99_latency_ms, max_latency_ms;
+    int64_t slots, slots_busy;              /* slots of the batch, slots holding a request */
+    int64_t slot_particles, resident_particles;  /* capacity of all slots, particles of the residents */
+    int32_t hamaker_slices;                 /* mixed precision: Hamaker slices of the batch's kernels */
 } lg_server_stats;
 
-/* Device bytes a request of n particles is charged against the budget. */
+/* Device bytes a system of n particles (a request alone, or the slots together) is charged. */
 int64_t lg_estimate_device_bytes(const lg_system_desc *tmpl, int64_t n);
 int lg_server_create(const lg_system_desc *tmpl, int64_t budget_bytes, int64_t rebuild_every, double dt, int device,
                      lg_server **out);
 int lg_server_destroy(lg_server *srv);
+/* Slot capacities (before the first admission); LG_E_NOMEM when they do not fit the budget. */
+int lg_server_set_slots(lg_server *srv, const int64_t *capacities, int64_t count);
 /* Queue a request (x0, v0: double[3n]; v0 may be NULL). Malformed requests (n < 1, nsteps < 1,
- * non-finite state) fail with LG_E_INVALID; a request larger than the whole budget with LG_E_NOMEM. */
+ * non-finite state) fail with LG_E_INVALID; a request larger than the largest slot with LG_E_NOMEM. */
 int lg_server_submit(lg_server *srv, int64_t n, const double *x0, const double *v0, int64_t nsteps,
                      int64_t *request_id);
 int lg_server_cancel(lg_server *srv, int64_t request_id);

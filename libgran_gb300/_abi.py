@@ -61,7 +61,9 @@ class lg_pair_stats(C.Structure):
 class lg_server_stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("budget_bytes", "used_bytes", "peak_bytes", "active", "queued", "completed",
                                          "rejected", "failed", "cancelled", "particle_steps")] + \
-               [(n, C.c_double) for n in ("p50_latency_ms", "p99_latency_ms", "max_latency_ms")]
+               [(n, C.c_double) for n in ("p50_latency_ms", "p99_latency_ms", "max_latency_ms")] + \
+               [(n, C.c_int64) for n in ("slots", "slots_busy", "slot_particles", "resident_particles")] + \
+               [("hamaker_slices", C.c_int32)]
 
 
 class lg_body_force(C.Structure):
@@ -179,6 +181,7 @@ def _declare(L):
         "lg_server_release": (C.c_int, [vp, i64]),
         "lg_server_get_stats": (C.c_int, [vp, P(lg_server_stats)]),
         "lg_server_inject_alloc_failures": (C.c_int, [vp, i32]),
+        "lg_server_set_slots": (C.c_int, [vp, P(i64), i64]),
         "lg_observables_noalloc": (C.c_int, [vp, vp, vp, i64, d, d, vp, vp]),
         "lg_set_step_shape": (C.c_int, [vp, i32, i32, i32]),
         "lg_get_tuning": (C.c_int, [vp, P(lg_tuning)]),

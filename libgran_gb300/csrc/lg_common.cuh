@@ -139,6 +139,14 @@ struct Params {
     const dbl4 *ext_al;
 };
 
+// Internal hold bit of a particle that takes no part in the simulation (an unused particle of a
+// serving slot): it is in no cell and no row, and the completion kernels skip it. Callers' hold
+// masks may not carry it (LG_HOLD_* are bits 0..3).
+constexpr uint32_t kHoldInactive = 16u;
+__device__ __forceinline__ bool inactive_of(const uint8_t *hold, int64_t i) {
+    return hold && (hold[i] & kHoldInactive);
+}
+
 // Kick of one half step, v + h * a, unless a step handler holds that increment.
 __device__ __forceinline__ d3 kick_unless(d3 v, double h, d3 a, bool held) { return held ? v : add(v, scl(h, a)); }
 __device__ __forceinline__ uint32_t hold_of(const uint8_t *hold, int64_t i) { return hold ? (uint32_t)hold[i] : 0u; }

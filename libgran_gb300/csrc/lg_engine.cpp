@@ -398,7 +398,7 @@ static int rebuild_list(lg_system *s) {
     PairView &newv = s->pv[1 - s->pcur];
     PairView o = oldv;
     if (!s->list_built) o.row_len = nullptr;
-    BatchView B{s->d_agg, s->d_hoff};
+    BatchView B{s->d_agg, s->d_hoff, s->P.hold};
     launch_list_build(s->P.n, s->x, B, s->P.r_verlet, s->r_near, s->max_cells, s->ls, o, newv, s->bv, s->err,
                       s->stream);
     s->launches += 7;
@@ -522,7 +522,8 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
     } else if (s->precision == LG_PRECISION_MIXED) {
         if (compact || persistent)
             kernels = launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, fuse_kick,
-                                                  prev_fused, s->mx, s->stream, s->side, s->fork_ev, s->join_ev);
+                                                  prev_fused, s->mx, s->stream, s->side, s->fork_ev, s->join_ev,
+                                                  s->ham_slices);
         else
             launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
     } else {
@@ -672,9 +673,17 @@ static int apply_unary(lg_system *s, const lg_body_force *body, lg_unary_hook ho
     return LG_OK;
 }
 
+// A serving arena (lg_arena_create): a batch whose systems are slots that start empty -- every
+// particle inactive, no bonds -- on a lattice of the given spacing, with bond capacity bcap per
+// particle and float-float extents allowed up to ext.
+struct ArenaSpec {
+    int32_t bcap;
+    double lattice, ext;
+};
+
 static int create_impl(const lg_system_desc *d, const double *x0, const double *v0, const double *th0, const double *om0,
                        const lg_facet_desc *facets, const double *neck, int64_t n_neck, int device, lg_system *s,
-                       int64_t n_sys = 0, const int64_t *sizes = nullptr) {
+                       int64_t n_sys = 0, const int64_t *sizes = nullptr, const ArenaSpec *arena = nullptr) {
     LG_TRY(check_args(d));
     if (!x0 || !v0 || !th0 || !om0) return lg_fail(LG_E_INVALID, "lg_create: null state pointer");
     if (d->n_facets > 0 && !facets) return lg_fail(LG_E_INVALID, "lg_create: n_facets > 0 but facets is null");
@@ -743,7 +752,11 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     // bonds
     std::vector<std::pair<int32_t, int32_t>> bonds;
     const bool sinter = d->binary_model == LG_BINARY_SINTER || d->binary_model == LG_BINARY_BREAKING_SINTER;
-    if (sinter) {
+    if (arena) {  // empty slots: bonds arrive with their occupants
+        if (d->binary_model == LG_BINARY_SINTER_CONNECTORS)
+            return lg_fail(LG_E_INVALID, "serving slots do not hold the 5-connector model");
+        s->n_bonds_initial_sys.assign((size_t)s->n_systems, 0);
+    } else if (sinter) {
         if (s->n_systems == 0) {
             LG_TRY(lg_detect_bonds(x0, n, d->sinter.r_part, d->sinter.critical_separation,
                                    d->binary_model == LG_BINARY_SINTER, bonds));
@@ -760,7 +773,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         }
     }
     const bool connectors = d->binary_model == LG_BINARY_SINTER_CONNECTORS;
-    if (connectors) {  // sinter_functor ctor, sinter_bridge.h:146-160: no cycle check, |g| <= dc
+    if (connectors && !arena) {  // sinter_functor ctor, sinter_bridge.h:146-160: no cycle check, |g| <= dc
         const double r = d->contact.r_part, dc = d->connector.critical_separation;
         if (s->n_systems == 0) {
             LG_TRY(lg_detect_bonds(x0, n, r, dc, false, bonds, true));
@@ -786,7 +799,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         deg[b.first]++;
         deg[b.second]++;
     }
-    int32_t bcap = 1;
+    int32_t bcap = arena ? std::max<int32_t>(1, arena->bcap) : 1;
     for (int64_t i = 0; i < n; ++i) bcap = std::max(bcap, deg[i]);
     if (bcap > 255) return lg_fail(LG_E_INVALID, "lg_create: a particle has %d bonds (max 255)", bcap);
     s->bv.bcap = bcap;
@@ -885,6 +898,12 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     LG_TRY(upload4(s->w[0], om0, n, s->stream));
     s->vcur = 0;
 
+    if (arena) {  // every particle of an empty slot takes no part (no cell, no row, no motion)
+        LG_TRY(s->alloc(&s->d_hold, (size_t)n));
+        LG_CUDA(cudaMemset(s->d_hold, (int)kHoldInactive, (size_t)n));
+        P.hold = s->d_hold;
+    }
+
     // batch segmentation: system index per particle, hashing offsets that keep systems apart
     if (s->n_systems > 0) {
         const int64_t ns = s->n_systems;
@@ -907,7 +926,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
             rmax = std::max(rmax, rad[q]);
         }
         // lattice spacing: two system radii, room for growth, and two list radii
-        const double L = 4.0 * rmax + 2.0 * d->r_verlet + 8.0 * d->contact.r_part + 1e-12;
+        const double L = arena ? arena->lattice : 4.0 * rmax + 2.0 * d->r_verlet + 8.0 * d->contact.r_part + 1e-12;
         int64_t m = 1;
         while (m * m * m < ns) ++m;
         std::vector<dbl4> hoff((size_t)ns);
@@ -998,6 +1017,12 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         LG_TRY(alloc_rows(cap));
         s->pcur = 0;
         s->max_cells = std::max<int64_t>(64, (s->n_systems > 0 ? 8 : 4) * n);
+        if (arena) {  // the slot lattice at cells of about r_verlet (capped at 2^25 cells)
+            int64_t m = 1;
+            while (m * m * m < s->n_systems) ++m;
+            const double per = (double)m * arena->lattice / d->r_verlet + 2.0;
+            s->max_cells = std::max<int64_t>(s->max_cells, (int64_t)std::min(per * per * per, 33554432.0));
+        }
         s->ls.nparts = 256;
         LG_TRY(s->alloc(&s->ls.part, 6 * 256));
         LG_TRY(s->alloc(&s->ls.grid, 1));
@@ -1057,6 +1082,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         if (s->n_systems > 0) LG_TRY(s->alloc(&s->d_orig, (size_t)s->n_systems));
         s->r_max = std::max(d->contact.r_part, std::max(d->sinter.r_part, d->hamaker.r_part));
         LG_TRY(set_mixed_origins(s, x0));
+        if (arena) s->ext_max = std::max(s->ext_max, arena->ext);  // room for the widest occupant
         launch_mixed_copies(n, s->x, s->v[s->vcur], s->w[s->vcur], s->th, s->origin, s->d_agg, s->d_orig, s->x32, s->v32, s->s32,
                             s->stream);
         double near = 0.0;
@@ -1118,7 +1144,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
                        (long long)kPairsMaxSlots);
     if (s->kernel == LG_FORCE_KERNEL_PERSISTENT) LG_TRY(ensure_step_buffers(s));
     if (d->threads_per_row > 0 && d->force_kernel == LG_FORCE_KERNEL_AUTO) s->kernel = LG_FORCE_KERNEL_ROWGROUP;
-    LG_TRY(apply_hold(s, d->hold_mask));
+    if (!arena) LG_TRY(apply_hold(s, d->hold_mask));
     LG_TRY(apply_unary(s, &d->body, d->unary_hook, d->unary_hook_user));
     // initial accelerations (the first half kick needs them); velocities are unchanged (hdt = 0)
     LG_TRY(launch_forces(s, 0.0, 0.0, 0));
@@ -1401,6 +1427,7 @@ extern "C" int lg_set_step_shape(lg_system *s, int32_t min_blocks, int32_t slice
     LG_TRY(ensure_step_buffers(s));
     s->step_min_blocks = min_blocks ? min_blocks : 4;
     s->step_slices = slices ? slices : mixed_hamaker_slices(s->P.n);
+    s->ham_slices = slices;  // the two-stream kernels follow an explicit slice count too
     s->step_assign = assign;
     s->drop_graphs();  // the graphs hold the previous shape's launches
     return LG_OK;
@@ -1789,6 +1816,218 @@ extern "C" int lg_batch_get_observables(lg_system *s, lg_observables *out) {
 }
 
 // ------------------------------------------------------------------------------------------------
+// Serving slots: a batch handle whose systems are slots that requests occupy in turn
+// ------------------------------------------------------------------------------------------------
+// Radius bound of a seeded aggregate of `cap` spheres about its centroid, with room to spread: the
+// random-sequential-attachment aggregates measure about 3 r cap^0.3 (8192 spheres: 40 r), and the
+// bound takes 1.5 times that (at least 8 r).
+double lg_arena_radius_bound(int64_t cap, double r_part) {
+    return std::max(8.0 * r_part, 1.5 * 3.0 * r_part * std::pow((double)std::max<int64_t>(cap, 1), 0.3));
+}
+
+int lg_arena_create(const lg_system_desc *tmpl, int64_t n_slots, const int64_t *caps, int device, lg_system **out) {
+    if (!tmpl || !caps || !out || n_slots < 1) return lg_fail(LG_E_INVALID, "lg_arena_create: bad arguments");
+    *out = nullptr;
+    if (tmpl->pairs != LG_PAIRS_VERLET) return lg_fail(LG_E_INVALID, "serving slots need LG_PAIRS_VERLET");
+    if (tmpl->n_facets != 0 || tmpl->hold_mask || tmpl->unary_hook || tmpl->body.model != LG_BODY_NONE)
+        return lg_fail(LG_E_INVALID, "serving slots hold no facets, hold masks or unary terms");
+    int64_t n = 0, cmax = 0;
+    for (int64_t q = 0; q < n_slots; ++q) {
+        if (caps[q] < 1) return lg_fail(LG_E_INVALID, "lg_arena_create: slot %lld has capacity %lld", (long long)q, (long long)caps[q]);
+        n += caps[q];
+        cmax = std::max(cmax, caps[q]);
+    }
+    lg_system_desc d = *tmpl;
+    d.n_part = n;
+    if (d.max_neighbors <= 0) d.max_neighbors = 96;  // imports need the standalone handles' row capacity
+    d.force_kernel = LG_FORCE_KERNEL_COMPACT;
+    d.threads_per_row = 0;
+    const double r = std::max(d.contact.r_part, std::max(d.sinter.r_part, d.hamaker.r_part));
+    const double R = lg_arena_radius_bound(cmax, r);
+    ArenaSpec spec{16, 2.0 * R + 2.0 * d.r_verlet + 8.0 * r, R + 8.0 * r};
+    int64_t m = 1;
+    while (m * m * m < n_slots) ++m;
+    std::vector<double> pos(3 * (size_t)n_slots), x0(3 * (size_t)n), zero(3 * (size_t)n, 0.0);
+    int64_t k = 0;
+    for (int64_t q = 0; q < n_slots; ++q) {
+        pos[3 * q] = (double)(q % m) * spec.lattice;
+        pos[3 * q + 1] = (double)((q / m) % m) * spec.lattice;
+        pos[3 * q + 2] = (double)(q / (m * m)) * spec.lattice;
+        for (int64_t i = 0; i < caps[q]; ++i, ++k)
+            for (int c = 0; c < 3; ++c) x0[3 * k + c] = pos[3 * q + c];
+    }
+    lg_system *s = new (std::nothrow) lg_system();
+    if (!s) return lg_fail(LG_E_NOMEM, "lg_arena_create: host allocation failed");
+    int rc = create_impl(&d, x0.data(), zero.data(), zero.data(), zero.data(), nullptr, nullptr, 0, device, s, n_slots,
+                         caps, &spec);
+    if (rc != LG_OK) {
+        std::string keep = g_last_error;
+        s->release();
+        delete s;
+        g_last_error = keep;
+        return rc;
+    }
+    s->arena = true;
+    s->arena_lattice = spec.lattice;
+    s->slot_pos = std::move(pos);
+    *out = s;
+    return LG_OK;
+}
+
+int lg_arena_import(lg_system *A, int64_t q, lg_system *S, const double *x0) {
+    if (!A || !S || !x0 || !A->arena || q < 0 || q >= A->n_systems)
+        return lg_fail(LG_E_INVALID, "lg_arena_import: bad arguments");
+    const int64_t off = A->sys_off[q], C = A->sys_off[q + 1] - off, n = S->P.n, N = A->P.n;
+    if (S->n_systems != 0 || n > C || S->precision != A->precision || S->P.binary_model != A->P.binary_model ||
+        S->P.hamaker_model != A->P.hamaker_model || S->P.pairs != LG_PAIRS_VERLET || S->pv[0].cap > A->pv[0].cap ||
+        S->bv.bcap > A->bv.bcap || S->bv.aos != A->bv.aos || (S->pv[0].near_len != nullptr) != (A->pv[0].near_len != nullptr) ||
+        S->bv.cn || S->kick_done || A->kick_done)
+        return lg_fail(LG_E_INVALID, "lg_arena_import: the request does not fit slot %lld (n %lld of %lld, %d of %d bond "
+                       "slots, %lld of %lld row slots)", (long long)q, (long long)n, (long long)C, S->bv.bcap, A->bv.bcap,
+                       (long long)S->pv[0].cap, (long long)A->pv[0].cap);
+    double c[3] = {0.0, 0.0, 0.0}, rad = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        for (int64_t i = 0; i < n; ++i) c[k] += x0[3 * i + k];
+        c[k] /= (double)n;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        double r2 = 0.0;
+        for (int k = 0; k < 3; ++k) r2 += (x0[3 * i + k] - c[k]) * (x0[3 * i + k] - c[k]);
+        rad = std::max(rad, std::sqrt(r2));
+    }
+    if (rad > 0.5 * A->arena_lattice - A->P.r_verlet)
+        return lg_fail(LG_E_INVALID, "lg_arena_import: the aggregate (radius %g) is too wide for the slot lattice (%g)", rad,
+                       A->arena_lattice);
+    LG_CUDA(cudaStreamSynchronize(S->stream));
+    const cudaStream_t st = A->stream;
+    const int64_t tail = C - n;
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+    };
+    auto cp2 = [&](void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height) {
+        return height == 0 ? cudaSuccess : cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, cudaMemcpyDeviceToDevice, st);
+    };
+    const size_t d4 = sizeof(dbl4);
+    // state of the occupant; the rest of the slot at its centroid, at rest
+    LG_CUDA(cp(A->x + off, S->x, d4 * n));
+    LG_CUDA(cp(A->th + off, S->th, d4 * n));
+    LG_CUDA(cp(A->a + off, S->a, d4 * n));
+    LG_CUDA(cp(A->al + off, S->al, d4 * n));
+    LG_CUDA(cp(A->v[A->vcur] + off, S->v[S->vcur], d4 * n));
+    LG_CUDA(cp(A->w[A->vcur] + off, S->w[S->vcur], d4 * n));
+    launch_fill_dbl4(A->x + off + n, tail, c[0], c[1], c[2], st);
+    for (dbl4 *p : {A->th, A->a, A->al, A->v[0], A->v[1], A->w[0], A->w[1]})
+        LG_CUDA(cudaMemsetAsync(p + off + n, 0, d4 * tail, st));
+    // hold bits: the occupant's (none in a request template), inactive for the rest
+    std::vector<uint8_t> hold((size_t)C, (uint8_t)kHoldInactive);
+    if (S->P.hold) LG_CUDA(cudaMemcpy(hold.data(), S->P.hold, (size_t)n, cudaMemcpyDeviceToHost));
+    else std::fill(hold.begin(), hold.begin() + n, (uint8_t)0);
+    LG_CUDA(cudaMemcpyAsync(A->d_hold + off, hold.data(), (size_t)C, cudaMemcpyHostToDevice, st));
+    // bonds (bond slot b of particle i at b * N + i), partners moved by the slot offset
+    const int32_t ba = A->bv.bcap, bsz = S->bv.bcap;
+    LG_CUDA(cudaMemset2DAsync(A->bv.j + off, sizeof(int32_t) * N, 0xFF, sizeof(int32_t) * C, ba, st));
+    LG_CUDA(cudaMemset2DAsync(A->bv.intact + off, (size_t)N, 0, (size_t)C, ba, st));
+    LG_CUDA(cp2(A->bv.j + off, sizeof(int32_t) * N, S->bv.j, sizeof(int32_t) * n, sizeof(int32_t) * n, bsz));
+    launch_offset_indices(A->bv.j + off, bsz, N, n, (int32_t)off, st);
+    LG_CUDA(cp2(A->bv.intact + off, (size_t)N, S->bv.intact, (size_t)n, (size_t)n, bsz));
+    LG_CUDA(cp2(A->bv.strength + off, sizeof(double) * N, S->bv.strength, sizeof(double) * n, sizeof(double) * n, bsz));
+    if (A->bv.aos) {  // one 9-component record per bond slot
+        LG_CUDA(cp2(A->bv.xi + 9 * off, 72 * (size_t)N, S->bv.xi, 72 * (size_t)n, 72 * (size_t)n, bsz));
+    } else {
+        for (int k = 0; k < 9; ++k)
+            LG_CUDA(cp2(A->bv.xi + (size_t)k * ba * N + off, sizeof(double) * N, S->bv.xi + (size_t)k * bsz * n,
+                        sizeof(double) * n, sizeof(double) * n, bsz));
+    }
+    for (int64_t b = 0; b < ba; ++b)
+        for (int64_t i = 0; i < C; ++i) {
+            int32_t j = -1;
+            if (b < bsz && i < n && S->host_bond_j[(size_t)(b * n + i)] >= 0) j = S->host_bond_j[(size_t)(b * n + i)] + (int32_t)off;
+            A->host_bond_j[(size_t)(b * N + off + i)] = j;
+        }
+    // pair rows (slot k of row i at k * N + i) with their springs, partners moved by the offset; a
+    // small system's rows hold fewer slots (n - 1), and no row is longer than its capacity
+    PairView &PA = A->pv[A->pcur];
+    const PairView &PS = S->pv[S->pcur];
+    const int64_t cap = PS.cap;
+    LG_CUDA(cp2(PA.nbr + off, sizeof(int32_t) * N, PS.nbr, sizeof(int32_t) * n, sizeof(int32_t) * n, cap));
+    launch_offset_indices(PA.nbr + off, cap, N, n, (int32_t)off, st);
+    LG_CUDA(cp(PA.row_len + off, PS.row_len, sizeof(int32_t) * n));
+    LG_CUDA(cudaMemsetAsync(PA.row_len + off + n, 0, sizeof(int32_t) * tail, st));
+    LG_CUDA(cp2(PA.flags + off, sizeof(uint32_t) * N, PS.flags, sizeof(uint32_t) * n, sizeof(uint32_t) * n, cap));
+    if (PA.aos) {
+        LG_CUDA(cp2(PA.xi + 9 * off, 72 * (size_t)N, PS.xi, 72 * (size_t)n, 72 * (size_t)n, cap));
+    } else {
+        for (int k = 0; k < 9; ++k)
+            LG_CUDA(cp2(PA.xi + (size_t)k * PA.cap * N + off, sizeof(double) * N, PS.xi + (size_t)k * cap * n,
+                        sizeof(double) * n, sizeof(double) * n, cap));
+    }
+    if (PA.near_len) {
+        LG_CUDA(cp2(PA.near_j + off, sizeof(int32_t) * N, PS.near_j, sizeof(int32_t) * n, sizeof(int32_t) * n, cap));
+        launch_offset_indices(PA.near_j + off, cap, N, n, (int32_t)off, st);
+        LG_CUDA(cp2(PA.near_k + off, (size_t)N, PS.near_k, (size_t)n, (size_t)n, cap));
+        LG_CUDA(cp(PA.near_len + off, PS.near_len, sizeof(int32_t) * n));
+        LG_CUDA(cudaMemsetAsync(PA.near_len + off + n, 0, sizeof(int32_t) * tail, st));
+    }
+    // float-float origin (the standalone handle's) and hashing offset to the slot's lattice point
+    dbl4 orig = make_double4_32a(S->origin[0], S->origin[1], S->origin[2], S->origin[3]);
+    const dbl4 hoff = make_double4_32a(A->slot_pos[3 * q] - c[0], A->slot_pos[3 * q + 1] - c[1],
+                                       A->slot_pos[3 * q + 2] - c[2], 0.0);
+    if (A->precision == LG_PRECISION_MIXED) {
+        A->h_orig[(size_t)q] = orig;
+        LG_CUDA(cudaMemcpyAsync(A->d_orig + q, &orig, d4, cudaMemcpyHostToDevice, st));
+    }
+    LG_CUDA(cudaMemcpyAsync(A->d_hoff + q, &hoff, d4, cudaMemcpyHostToDevice, st));
+    A->n_bonds_initial_sys[(size_t)q] = S->n_bonds_initial;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaStreamSynchronize(st));  // host buffers above are released on return
+    return LG_OK;
+}
+
+int lg_arena_clear(lg_system *A, int64_t q) {
+    if (!A || !A->arena || q < 0 || q >= A->n_systems) return lg_fail(LG_E_INVALID, "lg_arena_clear: bad arguments");
+    const int64_t off = A->sys_off[q], C = A->sys_off[q + 1] - off, N = A->P.n;
+    const cudaStream_t st = A->stream;
+    const size_t d4 = sizeof(dbl4);
+    launch_fill_dbl4(A->x + off, C, A->slot_pos[3 * q], A->slot_pos[3 * q + 1], A->slot_pos[3 * q + 2], st);
+    for (dbl4 *p : {A->th, A->a, A->al, A->v[0], A->v[1], A->w[0], A->w[1]})
+        LG_CUDA(cudaMemsetAsync(p + off, 0, d4 * C, st));
+    LG_CUDA(cudaMemsetAsync(A->d_hold + off, (int)kHoldInactive, (size_t)C, st));
+    LG_CUDA(cudaMemset2DAsync(A->bv.j + off, sizeof(int32_t) * N, 0xFF, sizeof(int32_t) * C, A->bv.bcap, st));
+    LG_CUDA(cudaMemset2DAsync(A->bv.intact + off, (size_t)N, 0, (size_t)C, A->bv.bcap, st));
+    for (int64_t b = 0; b < A->bv.bcap; ++b)
+        for (int64_t i = 0; i < C; ++i) A->host_bond_j[(size_t)(b * N + off + i)] = -1;
+    for (int k = 0; k < 2; ++k) {
+        PairView &pv = A->pv[k];
+        LG_CUDA(cudaMemsetAsync(pv.row_len + off, 0, sizeof(int32_t) * C, st));
+        if (pv.near_len) LG_CUDA(cudaMemsetAsync(pv.near_len + off, 0, sizeof(int32_t) * C, st));
+    }
+    const dbl4 zero = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+    LG_CUDA(cudaMemcpyAsync(A->d_hoff + q, &zero, d4, cudaMemcpyHostToDevice, st));
+    A->n_bonds_initial_sys[(size_t)q] = 0;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+int lg_arena_read(lg_system *A, int64_t q, int64_t n, double *x, double *v, double *th, double *w) {
+    if (!A || !A->arena || q < 0 || q >= A->n_systems || n < 1 || n > A->sys_off[q + 1] - A->sys_off[q])
+        return lg_fail(LG_E_INVALID, "lg_arena_read: bad arguments");
+    const int64_t off = A->sys_off[q];
+    double *host[4] = {x, v, th, w};
+    StateIO io{};
+    for (int f = 0; f < 4; ++f) io.out[f] = host[f] ? A->obs_scratch + 3 * n * f : nullptr;
+    launch_state_out(n, io, A->x + off, A->v[A->vcur] + off, A->th + off, A->w[A->vcur] + off, A->stream);
+    A->launches += 1;
+    LG_CUDA(cudaGetLastError());
+    for (int f = 0; f < 4; ++f)
+        if (host[f])
+            LG_CUDA(cudaMemcpyAsync(host[f], A->obs_scratch + 3 * n * f, sizeof(double) * 3 * (size_t)n,
+                                    cudaMemcpyDeviceToHost, A->stream));
+    LG_CUDA(cudaStreamSynchronize(A->stream));
+    return LG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
 // Autotuner: force kernel and lanes per row, measured on a clone of the system
 // ------------------------------------------------------------------------------------------------
 #include <map>
@@ -1821,10 +2060,11 @@ static int apply_tuning(lg_system *s, const lg_tuning &t) {
     if (t.force_kernel == LG_FORCE_KERNEL_PERSISTENT) {
         if (s->precision != LG_PRECISION_MIXED) return lg_fail(LG_E_INVALID, "tuning: persistent kernel on FP64");
         LG_TRY(ensure_step_buffers(s));
-        s->step_min_blocks = t.step_min_blocks;
-        s->step_slices = t.step_slices;
-        s->step_assign = t.step_assign;
     }
+    // the shape fields follow the record whatever the kernel (they only act on the persistent one)
+    s->step_min_blocks = t.step_min_blocks;
+    s->step_slices = t.step_slices;
+    s->step_assign = t.step_assign;
     if (t.force_kernel == LG_FORCE_KERNEL_PAIRS && !s->pres) return lg_fail(LG_E_INVALID, "tuning: no pair-parallel scratch");
     s->kernel = t.force_kernel;
     s->T = t.threads_per_row;

@@ -57,6 +57,11 @@ struct lg_system {
     // item assignment (0 pulled from a counter, 1 round robin)
     int step_slices = 0, step_min_blocks = 4, step_assign = 0;
     double tuned_ms = 0.0;         // the autotuner's time per step of the handle's current choice
+    int ham_slices = 0;            // mixed: Hamaker slices of the two-stream kernels (0: size rule)
+    // serving arena (lg_arena_create): a batch whose systems are slots; lattice point of each slot
+    bool arena = false;
+    double arena_lattice = 0.0;
+    std::vector<double> slot_pos;  // [3 * slots]
     float4 *s32 = nullptr;  // mixed: [5n] spin low parts, a run's displacement and rotation (float-float)
     float4 *csum = nullptr;    // mixed: [3n] contact sums (float-float)
     float4 *hsum = nullptr;    // mixed: [2n] Hamaker sums (float-float)
@@ -145,3 +150,19 @@ struct lg_system {
 };
 
 int lg_fail(int code, const char *fmt, ...);
+
+// Serving slots (lg_engine.cpp), for the serving loop. An arena is a batch handle whose systems
+// are slots of fixed capacities (caps) on a lattice; a slot holds one request (its first n
+// particles) or nothing, and its other particles are inactive (no cell, no row, no motion). All
+// occupants advance in the same launches. lg_arena_import moves a standalone handle built from the
+// same template (the request after its construction force evaluation, at a rebuild boundary) into
+// slot q: state, bonds with their springs, pair rows with their springs (partner indices moved by
+// the slot's offset), float-float origin and hashing offset; the occupant then evolves exactly as
+// the standalone handle would. lg_arena_clear empties a slot; lg_arena_read copies an occupant's
+// state (host arrays of 3n doubles, null: skipped). The caller keeps the arena at a rebuild
+// boundary and idle (synchronised) around imports and clears.
+int lg_arena_create(const lg_system_desc *tmpl, int64_t n_slots, const int64_t *caps, int device, lg_system **out);
+double lg_arena_radius_bound(int64_t cap, double r_part);
+int lg_arena_import(lg_system *arena, int64_t q, lg_system *src, const double *x0);
+int lg_arena_clear(lg_system *arena, int64_t q);
+int lg_arena_read(lg_system *arena, int64_t q, int64_t n, double *x, double *v, double *theta, double *omega);

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(64) forces_finish_mixed(Params P, StateView S,
                                                           MixedExtra MX) {
     if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    if (i >= P.n || inactive_of(P.hold, i)) return;
     finish_fp64_row<FACETS>(P, S, i, hdt, dt, contacts, hamaker, kick, MX);
 }
 
@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(64) forces_finish_ff(Params P, StateView S, in
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t h = hold_of(P.hold, i);
+    if (h & kHoldInactive) return;  // takes no part
     if (h) {  // a held particle keeps its FP64 state current (a held value stays exactly as it was)
         finish_fp64_row<false>(P, S, i, hdt_d, dt_d, contacts, hamaker, LAST ? 0 : 1, MX);
         return;
@@ -257,7 +258,7 @@ int mixed_hamaker_slices(int64_t n) {
 
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                 double dt, int move_facets, bool kick, bool prev_fused, const MixedExtra &MX,
-                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int slices) {
     const bool ver = P.pairs == LG_PAIRS_VERLET;
     const int contacts = P.binary_model != LG_BINARY_NONE ? 1 : 0;
     const int hamaker = P.hamaker_model != LG_HAMAKER_NONE ? 1 : 0;
@@ -275,7 +276,7 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         ++kernels;
     }
     if (hamaker) {
-        switch (mixed_hamaker_slices(P.n)) {
+        switch (slices > 0 ? slices : mixed_hamaker_slices(P.n)) {
             case 8:
                 if (ver) launch_hamaker<true, 8>(P, PV, MX, st);
                 else launch_hamaker<false, 8>(P, PV, MX, st);

@@ -393,6 +393,10 @@ __global__ void cell_count(int64_t n, const dbl4 *__restrict__ x, BatchView B, c
                            int32_t *__restrict__ cell_of, int32_t *__restrict__ count, float4 *__restrict__ x32) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (inactive_of(B.hold, i)) {  // in no cell: never a candidate of any row
+        cell_of[i] = -1;
+        return;
+    }
     dbl4 q = hash_pos(x, B, i);
     int64_t cx = cell_coord(q.x, g->lo[0], g->edge, g->dim[0]);
     int64_t cy = cell_coord(q.y, g->lo[1], g->edge, g->dim[1]);
@@ -433,6 +437,7 @@ __global__ void cell_scatter(int64_t n, const int32_t *__restrict__ cell_of, con
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     int32_t c = cell_of[i];
+    if (c < 0) return;  // inactive
     int32_t p = atomicAdd(&fill[c], 1);
     sorted[start[c] + p] = (int32_t)i;
 }
@@ -485,7 +490,7 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
 
     for (int r = warp; r < kBuildRows; r += kBuildWarps) {
         const int64_t i = row0 + r;
-        if (i >= n) {
+        if (i >= n || inactive_of(B.hold, i)) {  // an inactive particle's row is empty
             if (lane == 0) rlen[r] = rnear[r] = 0;
             continue;
         }

@@ -19,8 +19,9 @@ struct GridDev {
 // Batch segmentation (null pointers for a single system): system index of every particle and the
 // spatial offset of every system used only for cell hashing.
 struct BatchView {
-    const int32_t *agg;  // [n]
-    const dbl4 *hoff;    // [n_systems]
+    const int32_t *agg;    // [n]
+    const dbl4 *hoff;      // [n_systems]
+    const uint8_t *hold;   // [n] hold bits (null: none); inactive particles are left out of the list
 };
 
 struct ListScratch {
@@ -157,9 +158,10 @@ void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairV
 // float-float copies), exactly as launch_kick_drift_mixed would.
 // kick: another step follows (the completion also runs its opening half kick and drift);
 // prev_fused: the step before was such a step (its state may be float-float only).
+// slices: Hamaker slices per 32-row group (0: mixed_hamaker_slices(P.n)).
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                 double dt, int move_facets, bool kick, bool prev_fused, const MixedExtra &MX,
-                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int slices = 0);
 
 // Layout conversion between a caller's [n][3] doubles (already in device memory) and the padded
 // device layout (lg_reduce.cu).
@@ -175,6 +177,11 @@ void launch_state_out(int64_t n, const StateIO &io, const dbl4 *x, const dbl4 *v
                       cudaStream_t st);
 void launch_aos_to_dev4(int64_t n, const double *aos, dbl4 *dst, cudaStream_t st);
 void launch_dev4_to_aos(int64_t n, const dbl4 *src, double *aos, cudaStream_t st);
+
+// Serving slots (lg_reduce.cu): p[r * pitch + c] += off wherever the entry is an index (>= 0), for
+// r < rows, c < width; and count positions set to (x, y, z).
+void launch_offset_indices(int32_t *p, int64_t rows, int64_t pitch, int64_t width, int32_t off, cudaStream_t st);
+void launch_fill_dbl4(dbl4 *p, int64_t count, double x, double y, double z, cudaStream_t st);
 
 // Observables (lg_reduce.cu). scratch: at least obs_scratch_doubles(n) doubles of device memory;
 // out: 20 doubles of device memory (column sums, see lg_reduce.cu).

@@ -406,4 +406,30 @@ void launch_dev4_to_aos(int64_t n, const dbl4 *src, double *aos, cudaStream_t st
     if (n > 0) dev4_to_aos<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, src, aos);
 }
 
+// ---- serving slots: partner indices of a copied block moved by an offset, positions filled ----
+// p[r * pitch + c] += off for r < rows, c < width where the entry is a particle index (>= 0).
+__global__ void offset_indices(int32_t *__restrict__ p, int64_t rows, int64_t pitch, int64_t width, int32_t off) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= rows * width) return;
+    const int64_t e = (t / width) * pitch + t % width;
+    const int32_t v = p[e];
+    if (v >= 0) p[e] = v + off;
+}
+
+__global__ void fill_dbl4(dbl4 *__restrict__ p, int64_t count, double x, double y, double z) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < count) p[i] = make_double4_32a(x, y, z, 0.0);
+}
+
+void launch_offset_indices(int32_t *p, int64_t rows, int64_t pitch, int64_t width, int32_t off, cudaStream_t st) {
+    const int64_t total = rows * width;
+    if (total <= 0) return;
+    offset_indices<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(p, rows, pitch, width, off);
+}
+
+void launch_fill_dbl4(dbl4 *p, int64_t count, double x, double y, double z, cudaStream_t st) {
+    if (count <= 0) return;
+    fill_dbl4<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(p, count, x, y, z);
+}
+
 }  // namespace lg

@@ -1,17 +1,24 @@
 // lg_server.cpp -- continuous-batching serving loop for aggregate-mechanics requests.
 //
-// Requests (an aggregate's state and a step budget) arrive at any time. Each tick the server
-//   1. admits queued requests, first come first served with backfill, while their device
-//      footprint fits the memory budget: a request becomes a resident engine handle (its state,
-//      springs and bonds stay in HBM until it finishes) with its own CUDA stream;
-//   2. keeps every resident request two rebuild periods ahead on its own stream (graph replays;
-//      completion is tracked with events, no global synchronisation), so requests of different
-//      sizes progress at their own pace and their kernels overlap on the device;
-//   3. retires requests whose budget is spent: observables and positions are copied back, the
-//      handle is destroyed and its memory returns to the budget.
-// A request's result does not depend on what else is resident (each is its own handle), so a
-// request gives the same result alone and in the mix. Latency is measured on the host from
-// submission to retirement.
+// Requests (an aggregate's state and a step budget) arrive at any time. The server keeps one batch
+// handle, the arena, whose systems are slots of fixed capacities (size classes); a request occupies
+// one slot from admission to retirement, and its state, bonds and spring history stay in HBM there.
+// Every resident request advances in the same launches: one rebuild period of the arena at a time
+// (graph-replayed), all slots together. Each tick
+//   1. waits for the period in flight and counts its steps for every occupant;
+//   2. retires requests whose step budget is spent: state and observables are copied back and the
+//      slot is emptied;
+//   3. at a rebuild boundary, admits queued requests into free slots (first come first served, with
+//      backfill; the smallest free slot that holds the request): each request is first built as a
+//      standalone handle from the template -- bond detection and its construction force
+//      evaluation, exactly as it would start alone -- and then moved into the slot on the device;
+//   4. launches the next period (up to the next boundary, or to the earliest budget end), and
+//      builds standalone handles for queued requests while the GPU runs.
+// A request therefore evolves as it would alone: bit for bit in FP64; in mixed precision too when
+// the lone run uses the arena's Hamaker slicing (lg_server_stats.hamaker_slices, see
+// lg_set_step_shape) and step budgets are multiples of the rebuild period. Latency is measured on
+// the host from submission to retirement. The arena's device memory is charged against the budget
+// when it is created; standalone handles while they exist.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,19 +45,18 @@ struct Request {
     int64_t n = 0;
     int64_t nsteps = 0, done_steps = 0;
     std::vector<double> x0, v0;
-    int64_t bytes = 0;
     int32_t state = LG_REQ_QUEUED;
-    lg_system *sys = nullptr;
+    int64_t slot = -1;
+    lg_system *stage = nullptr;  // standalone handle built before admission
+    int64_t stage_bytes = 0;
     double t_submit = 0, t_admit = 0, t_done = 0;
     lg_observables obs{};
     std::vector<double> x_final;
     std::string error;
-    int64_t enqueued_steps = 0;
-    std::deque<std::pair<cudaEvent_t, int64_t>> inflight;  // (event after a period, its steps)
-    std::vector<cudaEvent_t> free_events;
 };
 
-constexpr int kPeriodsAhead = 2;
+// Default slots: size classes 128 .. 8192 monomers, 8 slots each.
+const int64_t kClasses[] = {128, 256, 512, 1024, 2048, 4096, 8192};
 
 }  // namespace
 
@@ -69,10 +75,16 @@ struct lg_server {
     int64_t particle_steps = 0;
     int32_t inject_alloc_failures = 0;
     int32_t backfill = 1;
+    // the arena and its slots
+    std::vector<int64_t> caps;      // capacity of every slot
+    std::vector<int64_t> occupant;  // request in every slot, -1: free
+    lg_system *arena = nullptr;
+    int64_t arena_bytes = 0;
+    cudaEvent_t done_ev = nullptr;
+    bool in_flight = false;
+    int64_t flight_steps = 0;
 };
 
-// Device bytes of one request: state and its ping-pong copies, float-float copies, pair slots (two
-// buffers), bonds, facet springs, list scratch, observables scratch, plus a fixed overhead.
 extern "C" int64_t lg_estimate_device_bytes(const lg_system_desc *d, int64_t n) {
     if (!d || n < 1) return -1;
     const int64_t cap = d->pairs == LG_PAIRS_VERLET ? (d->max_neighbors > 0 ? d->max_neighbors : 64) : std::max<int64_t>(n - 1, 1);
@@ -89,6 +101,28 @@ extern "C" int64_t lg_estimate_device_bytes(const lg_system_desc *d, int64_t n) 
     return b + (4 << 20);                                     // fixed overhead
 }
 
+static int64_t slots_bytes(const lg_server *s, const std::vector<int64_t> &caps) {
+    int64_t n = 0;
+    for (int64_t c : caps) n += c;
+    lg_system_desc d = s->tmpl;
+    if (d.max_neighbors <= 0) d.max_neighbors = 96;
+    return lg_estimate_device_bytes(&d, std::max<int64_t>(n, 1));
+}
+
+// Default slots that fit half the budget (the rest for standalone handles): 8 slots per size class,
+// halved while too large, then the largest classes dropped.
+static std::vector<int64_t> default_slots(const lg_server *s) {
+    for (int per = 8; per >= 1; per /= 2)
+        for (int top = 7; top >= 1; --top) {
+            std::vector<int64_t> caps;
+            for (int c = 0; c < top; ++c)
+                for (int k = 0; k < per; ++k) caps.push_back(kClasses[c]);
+            if (slots_bytes(s, caps) <= s->budget / 2) return caps;
+            if (per > 1) break;  // halve the counts before dropping classes
+        }
+    return std::vector<int64_t>(1, kClasses[0]);
+}
+
 extern "C" int lg_server_create(const lg_system_desc *tmpl, int64_t budget_bytes, int64_t rebuild_every, double dt,
                                 int device, lg_server **out) {
     if (!tmpl || !out) return lg_fail(LG_E_INVALID, "lg_server_create: null argument");
@@ -96,34 +130,78 @@ extern "C" int lg_server_create(const lg_system_desc *tmpl, int64_t budget_bytes
     if (rebuild_every < 1) return lg_fail(LG_E_INVALID, "lg_server_create: rebuild_every must be >= 1");
     if (tmpl->hold_mask || tmpl->unary_hook)
         return lg_fail(LG_E_INVALID, "lg_server_create: a request template holds no per-particle mask or unary hook");
+    if (tmpl->pairs != LG_PAIRS_VERLET || tmpl->n_facets != 0 || tmpl->body.model != LG_BODY_NONE ||
+        tmpl->binary_model == LG_BINARY_SINTER_CONNECTORS)
+        return lg_fail(LG_E_INVALID, "lg_server_create: requests need LG_PAIRS_VERLET, no facets, no body force and "
+                                     "no 5-connector model");
     if (!(dt > 0) || !std::isfinite(dt)) return lg_fail(LG_E_INVALID, "lg_server_create: dt must be positive");
     lg_server *s = new (std::nothrow) lg_server();
     if (!s) return lg_fail(LG_E_NOMEM, "lg_server_create: host allocation failed");
     s->tmpl = *tmpl;
+    if (s->tmpl.max_neighbors <= 0) s->tmpl.max_neighbors = 96;  // slots and standalone handles share it
     s->budget = budget_bytes;
     s->rebuild_every = rebuild_every;
     s->dt = dt;
     s->device = device;
+    s->caps = default_slots(s);
+    s->occupant.assign(s->caps.size(), -1);
     *out = s;
     return LG_OK;
 }
 
-static void release_request(lg_server *s, Request &r) {
-    if (r.sys) {
-        cudaStreamSynchronize(r.sys->stream);
-        for (auto &p : r.inflight) cudaEventDestroy(p.first);
-        for (auto e : r.free_events) cudaEventDestroy(e);
-        r.inflight.clear();
-        r.free_events.clear();
-        lg_destroy(r.sys);
-        r.sys = nullptr;
-        s->used -= r.bytes;
+extern "C" int lg_server_set_slots(lg_server *s, const int64_t *caps, int64_t count) {
+    if (!s || !caps || count < 1) return lg_fail(LG_E_INVALID, "lg_server_set_slots: bad arguments");
+    if (s->arena || !s->active.empty()) return lg_fail(LG_E_STATE, "lg_server_set_slots: slots are already in use");
+    std::vector<int64_t> c(caps, caps + count);
+    for (int64_t v : c)
+        if (v < 1) return lg_fail(LG_E_INVALID, "lg_server_set_slots: capacity %lld", (long long)v);
+    const int64_t bytes = slots_bytes(s, c);
+    if (bytes > s->budget)
+        return lg_fail(LG_E_NOMEM, "lg_server_set_slots: the slots need %lld bytes, more than the budget %lld",
+                       (long long)bytes, (long long)s->budget);
+    s->caps = c;
+    s->occupant.assign(c.size(), -1);
+    return LG_OK;
+}
+
+static void drop_stage(lg_server *s, Request &r) {
+    if (r.stage) {
+        lg_destroy(r.stage);
+        r.stage = nullptr;
+        s->used -= r.stage_bytes;
+        r.stage_bytes = 0;
     }
+}
+
+static int wait_flight(lg_server *s) {
+    if (!s->in_flight) return LG_OK;
+    const cudaError_t e = cudaEventSynchronize(s->done_ev);
+    s->in_flight = false;
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return lg_fail(LG_E_CUDA, "serving period failed on the device: %s", cudaGetErrorString(e));
+    }
+    for (int64_t id : s->active) {
+        Request &r = s->reqs[id];
+        r.done_steps += s->flight_steps;
+        s->particle_steps += s->flight_steps * r.n;
+    }
+    return LG_OK;
+}
+
+static void fail_request(lg_server *s, Request &r, const std::string &why) {
+    r.state = LG_REQ_FAILED;
+    r.error = why;
+    r.t_done = now_ms();
+    s->failed++;
 }
 
 extern "C" int lg_server_destroy(lg_server *s) {
     if (!s) return LG_OK;
-    for (auto &kv : s->reqs) release_request(s, kv.second);
+    if (s->in_flight) cudaEventSynchronize(s->done_ev);
+    for (auto &kv : s->reqs) drop_stage(s, kv.second);
+    if (s->arena) lg_destroy(s->arena);
+    if (s->done_ev) cudaEventDestroy(s->done_ev);
     delete s;
     return LG_OK;
 }
@@ -137,11 +215,11 @@ extern "C" int lg_server_submit(lg_server *s, int64_t n, const double *x0, const
     for (int64_t q = 0; q < 3 * n; ++q)
         if (!std::isfinite(x0[q]) || (v0 && !std::isfinite(v0[q])))
             return lg_fail(LG_E_INVALID, "lg_server_submit: malformed request (non-finite state)");
-    const int64_t bytes = lg_estimate_device_bytes(&s->tmpl, n);
-    if (bytes > s->budget) {
+    const int64_t largest = *std::max_element(s->caps.begin(), s->caps.end());
+    if (n > largest) {
         s->rejected++;
-        return lg_fail(LG_E_NOMEM, "lg_server_submit: request needs %lld bytes, more than the whole budget %lld",
-                       (long long)bytes, (long long)s->budget);
+        return lg_fail(LG_E_NOMEM, "lg_server_submit: a request of %lld particles is larger than the largest slot (%lld)",
+                       (long long)n, (long long)largest);
     }
     Request r;
     r.id = s->next_id++;
@@ -150,7 +228,6 @@ extern "C" int lg_server_submit(lg_server *s, int64_t n, const double *x0, const
     r.x0.assign(x0, x0 + 3 * n);
     r.v0.assign(3 * n, 0.0);
     if (v0) std::copy(v0, v0 + 3 * n, r.v0.begin());
-    r.bytes = bytes;
     r.t_submit = now_ms();
     *request_id = r.id;
     s->queue.push_back(r.id);
@@ -165,9 +242,15 @@ extern "C" int lg_server_cancel(lg_server *s, int64_t id) {
     Request &r = it->second;
     if (r.state == LG_REQ_QUEUED) {
         s->queue.erase(std::remove(s->queue.begin(), s->queue.end(), id), s->queue.end());
+        drop_stage(s, r);
     } else if (r.state == LG_REQ_RUNNING) {
-        if (r.sys) cudaStreamSynchronize(r.sys->stream);
-        release_request(s, r);
+        const int rc = wait_flight(s);  // the slot is emptied only while the arena is idle
+        if (rc != LG_OK) return rc;
+        if (r.slot >= 0) {
+            lg_arena_clear(s->arena, r.slot);
+            s->occupant[(size_t)r.slot] = -1;
+            r.slot = -1;
+        }
         s->active.erase(std::remove(s->active.begin(), s->active.end(), id), s->active.end());
     } else {
         return LG_OK;  // already finished
@@ -184,150 +267,185 @@ extern "C" int lg_server_inject_alloc_failures(lg_server *s, int32_t count) {
     return LG_OK;
 }
 
-static int admit(lg_server *s) {
-    // first come first served; with backfill, later requests that fit may pass a head that does not
-    for (auto it = s->queue.begin(); it != s->queue.end();) {
-        Request &r = s->reqs[*it];
-        if (s->used + r.bytes > s->budget) {
-            if (!s->backfill) break;
-            ++it;
-            continue;
-        }
-        lg_system_desc d = s->tmpl;
-        d.n_part = r.n;
-        int rc;
-        if (s->inject_alloc_failures > 0) {  // host-side stand-in for a failing device allocation
-            s->inject_alloc_failures--;
-            rc = lg_fail(LG_E_NOMEM, "cudaMalloc failed: out of memory (injected)");
-        } else {
-            std::vector<double> zeros(3 * r.n, 0.0);
-            rc = lg_create(&d, r.x0.data(), r.v0.data(), zeros.data(), zeros.data(), nullptr, nullptr, 0, s->device,
-                           &r.sys);
-        }
-        if (rc != LG_OK) {
-            r.state = LG_REQ_FAILED;
-            r.error = lg_last_error();
-            r.t_done = now_ms();
-            s->failed++;
-            it = s->queue.erase(it);
-            continue;
-        }
-        s->used += r.bytes;
-        s->peak = std::max(s->peak, s->used);
-        r.state = LG_REQ_RUNNING;
-        r.t_admit = now_ms();
-        r.x0.clear();
-        r.x0.shrink_to_fit();
-        r.v0.clear();
-        r.v0.shrink_to_fit();
-        s->active.push_back(r.id);
-        it = s->queue.erase(it);
+// The standalone handle of a queued request: bond detection and the construction force evaluation,
+// as the request would start alone. A failure (including an injected one) fails the request.
+static bool stage(lg_server *s, Request &r) {
+    if (r.stage) return true;
+    lg_system_desc d = s->tmpl;
+    d.n_part = r.n;
+    const int64_t bytes = lg_estimate_device_bytes(&d, r.n);
+    if (s->used + bytes > s->budget) return false;  // later, when memory is free
+    int rc;
+    if (s->inject_alloc_failures > 0) {  // host-side stand-in for a failing device allocation
+        s->inject_alloc_failures--;
+        rc = lg_fail(LG_E_NOMEM, "cudaMalloc failed: out of memory (injected)");
+    } else {
+        std::vector<double> zeros(3 * r.n, 0.0);
+        rc = lg_create(&d, r.x0.data(), r.v0.data(), zeros.data(), zeros.data(), nullptr, nullptr, 0, s->device, &r.stage);
     }
+    if (rc != LG_OK) {
+        r.stage = nullptr;
+        fail_request(s, r, lg_last_error());
+        return false;
+    }
+    r.stage_bytes = bytes;
+    s->used += bytes;
+    s->peak = std::max(s->peak, s->used);
+    return true;
+}
+
+static int ensure_arena(lg_server *s) {
+    if (s->arena) return LG_OK;
+    const int64_t bytes = slots_bytes(s, s->caps);
+    if (s->used + bytes > s->budget)
+        return lg_fail(LG_E_NOMEM, "serving slots need %lld bytes; %lld of the budget %lld are free", (long long)bytes,
+                       (long long)(s->budget - s->used), (long long)s->budget);
+    int rc = lg_arena_create(&s->tmpl, (int64_t)s->caps.size(), s->caps.data(), s->device, &s->arena);
+    if (rc != LG_OK) return rc;
+    if (cudaEventCreateWithFlags(&s->done_ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return lg_fail(LG_E_CUDA, "cudaEventCreate failed");
+    }
+    s->arena_bytes = bytes;
+    s->used += bytes;
+    s->peak = std::max(s->peak, s->used);
     return LG_OK;
 }
 
-static void retire(lg_server *s, Request &r) {
-    r.x_final.resize(3 * r.n);
-    int rc = lg_get_observables(r.sys, &r.obs);  // synchronises the request's stream
-    if (rc == LG_OK) rc = lg_get(r.sys, LG_FIELD_X, r.x_final.data());
+// The smallest free slot that holds n particles, or -1.
+static int64_t free_slot(const lg_server *s, int64_t n) {
+    int64_t best = -1;
+    for (size_t q = 0; q < s->caps.size(); ++q)
+        if (s->occupant[q] < 0 && s->caps[q] >= n && (best < 0 || s->caps[q] < s->caps[(size_t)best])) best = (int64_t)q;
+    return best;
+}
+
+static void retire(lg_server *s, std::vector<int64_t> &done) {
+    if (done.empty()) return;
+    std::vector<lg_observables> obs(s->caps.size());
+    int rc = lg_batch_get_observables(s->arena, obs.data());
+    std::string why = rc != LG_OK ? std::string(lg_last_error()) : std::string();
     int32_t errs = 0;
-    if (rc == LG_OK) rc = lg_get_device_errors(r.sys, &errs);
-    std::string why = rc != LG_OK ? std::string(lg_last_error()) : std::string("device error word set");
-    release_request(s, r);
-    r.t_done = now_ms();
-    if (rc != LG_OK || errs != 0) {
-        r.state = LG_REQ_FAILED;
-        r.error = why;
-        s->failed++;
-    } else {
-        r.state = LG_REQ_DONE;
-        s->completed++;
-        s->latencies.push_back(r.t_done - r.t_submit);
+    if (rc == LG_OK && lg_get_device_errors(s->arena, &errs) == LG_OK && errs != 0)
+        why = "device error word set (" + std::to_string(errs) + ")";
+    for (int64_t id : done) {
+        Request &r = s->reqs[id];
+        r.x_final.resize(3 * r.n);
+        int rr = why.empty() ? lg_arena_read(s->arena, r.slot, r.n, r.x_final.data(), nullptr, nullptr, nullptr) : LG_E_STATE;
+        if (rr == LG_OK) {
+            // the slot's sums cover its inactive particles (at rest: no kinetic energy, momentum or
+            // contacts); centre of mass and radius of gyration are taken over the occupant alone
+            lg_observables o = obs[(size_t)r.slot];
+            double c[3] = {0.0, 0.0, 0.0}, rg = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                for (int64_t i = 0; i < r.n; ++i) c[k] += r.x_final[3 * i + k];
+                c[k] /= (double)r.n;
+                o.center_of_mass[k] = c[k];
+            }
+            for (int64_t i = 0; i < r.n; ++i)
+                for (int k = 0; k < 3; ++k) rg += (r.x_final[3 * i + k] - c[k]) * (r.x_final[3 * i + k] - c[k]);
+            o.radius_of_gyration = std::sqrt(rg / (double)r.n);
+            r.obs = o;
+        }
+        lg_arena_clear(s->arena, r.slot);
+        s->occupant[(size_t)r.slot] = -1;
+        r.slot = -1;
+        r.t_done = now_ms();
+        if (rr != LG_OK) {
+            fail_request(s, r, why.empty() ? std::string(lg_last_error()) : why);
+        } else {
+            r.state = LG_REQ_DONE;
+            s->completed++;
+            s->latencies.push_back(r.t_done - r.t_submit);
+        }
     }
 }
 
 extern "C" int lg_server_tick(lg_server *s, int32_t *n_active, int32_t *n_queued, int32_t *n_retired) {
     if (!s) return lg_fail(LG_E_INVALID, "lg_server_tick: null server");
-    const size_t queued_before = s->queue.size();
-    int rc = admit(s);
-    if (rc != LG_OK) return rc;
-    bool progress = s->queue.size() != queued_before;
-    const int64_t rb = s->tmpl.pairs == LG_PAIRS_VERLET ? s->rebuild_every : 0;
-    // keep every resident request kPeriodsAhead periods ahead on its stream
-    for (int64_t id : s->active) {
-        Request &r = s->reqs[id];
-        while ((int)r.inflight.size() < kPeriodsAhead && r.enqueued_steps < r.nsteps && r.state == LG_REQ_RUNNING) {
-            const int64_t k = std::min(s->rebuild_every, r.nsteps - r.enqueued_steps);
-            rc = lg_step(r.sys, s->dt, k, rb);
-            cudaEvent_t ev = nullptr;
-            if (rc == LG_OK) {
-                if (!r.free_events.empty()) {
-                    ev = r.free_events.back();
-                    r.free_events.pop_back();
-                } else if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
-                    ev = nullptr;
-                    rc = lg_fail(LG_E_CUDA, "cudaEventCreate failed");
-                }
-            }
-            if (rc == LG_OK && cudaEventRecord(ev, r.sys->stream) != cudaSuccess) rc = lg_fail(LG_E_CUDA, "cudaEventRecord failed");
-            if (rc != LG_OK) {
-                r.state = LG_REQ_FAILED;
-                r.error = lg_last_error();
-                if (ev) r.free_events.push_back(ev);
-                break;
-            }
-            r.inflight.emplace_back(ev, k);
-            r.enqueued_steps += k;
+    int rc = wait_flight(s);
+    if (rc != LG_OK) {  // the period failed: its occupants fail with it
+        const std::string why = lg_last_error();
+        for (int64_t id : s->active) {
+            Request &r = s->reqs[id];
+            if (s->arena && r.slot >= 0) lg_arena_clear(s->arena, r.slot);
+            if (r.slot >= 0) s->occupant[(size_t)r.slot] = -1;
+            r.slot = -1;
+            fail_request(s, r, why);
         }
+        s->active.clear();
     }
-    // collect finished periods; retire finished requests
-    int32_t retired = 0;
-    std::vector<int64_t> still;
-    for (int64_t id : s->active) {
-        Request &r = s->reqs[id];
-        if (r.state == LG_REQ_FAILED) {
-            release_request(s, r);
-            r.t_done = now_ms();
-            s->failed++;
-            ++retired;
-            progress = true;
-            continue;
-        }
-        cudaError_t qe = cudaSuccess;
-        while (!r.inflight.empty() && (qe = cudaEventQuery(r.inflight.front().first)) == cudaSuccess) {
-            r.done_steps += r.inflight.front().second;
-            s->particle_steps += r.inflight.front().second * r.n;
-            r.free_events.push_back(r.inflight.front().first);
-            r.inflight.pop_front();
-            progress = true;
-        }
-        if (qe == cudaErrorNotReady) {
-            cudaGetLastError();  // a pending event is not an error
-        } else if (qe != cudaSuccess) {
-            // the period failed on the device (or the context is lost): the request fails with the
-            // error instead of staying active with an event that never completes
-            cudaGetLastError();
-            r.state = LG_REQ_FAILED;
-            r.error = std::string("device error while running the request: ") + cudaGetErrorString(qe);
-            release_request(s, r);
-            r.t_done = now_ms();
-            s->failed++;
-            ++retired;
-            progress = true;
-            continue;
-        }
-        if (r.done_steps >= r.nsteps) {
-            retire(s, r);
-            ++retired;
-            continue;
-        }
-        still.push_back(id);
-    }
+    // retire requests whose budget is spent
+    std::vector<int64_t> done, still;
+    for (int64_t id : s->active) (s->reqs[id].done_steps >= s->reqs[id].nsteps ? done : still).push_back(id);
+    retire(s, done);
     s->active.swap(still);
-    // nothing moved: wait for the oldest outstanding period instead of spinning
-    if (!progress && !s->active.empty()) {
-        Request &r = s->reqs[s->active.front()];
-        if (!r.inflight.empty()) cudaEventSynchronize(r.inflight.front().first);
+    const int32_t retired = (int32_t)done.size();
+    // admissions at a rebuild boundary: the occupant's rows start with the arena's next build
+    const bool boundary = !s->arena || (s->arena->step_index % s->rebuild_every) == 0;
+    if (boundary) {
+        for (auto it = s->queue.begin(); it != s->queue.end();) {
+            Request &r = s->reqs[*it];
+            const int64_t q = free_slot(s, r.n);
+            if (q < 0) {
+                if (!s->backfill) break;
+                ++it;
+                continue;
+            }
+            if (!stage(s, r)) {
+                if (r.state == LG_REQ_FAILED) {
+                    it = s->queue.erase(it);
+                    continue;
+                }
+                if (!s->backfill) break;
+                ++it;
+                continue;
+            }
+            rc = ensure_arena(s);
+            if (rc == LG_OK) rc = lg_arena_import(s->arena, q, r.stage, r.x0.data());
+            drop_stage(s, r);
+            if (rc != LG_OK) {
+                fail_request(s, r, lg_last_error());
+                it = s->queue.erase(it);
+                continue;
+            }
+            s->occupant[(size_t)q] = r.id;
+            r.slot = q;
+            r.state = LG_REQ_RUNNING;
+            r.t_admit = now_ms();
+            r.x0.clear();
+            r.x0.shrink_to_fit();
+            r.v0.clear();
+            r.v0.shrink_to_fit();
+            s->active.push_back(r.id);
+            it = s->queue.erase(it);
+        }
+    }
+    // the next period of every occupant, in the same launches
+    if (!s->active.empty()) {
+        int64_t k = s->rebuild_every - (s->arena->step_index % s->rebuild_every);
+        for (int64_t id : s->active) k = std::min(k, s->reqs[id].nsteps - s->reqs[id].done_steps);
+        rc = lg_step(s->arena, s->dt, k, s->rebuild_every);
+        if (rc == LG_OK && cudaEventRecord(s->done_ev, s->arena->stream) != cudaSuccess) {
+            cudaGetLastError();
+            rc = lg_fail(LG_E_CUDA, "cudaEventRecord failed");
+        }
+        if (rc != LG_OK) return rc;
+        s->in_flight = true;
+        s->flight_steps = k;
+    }
+    // standalone handles for the head of the queue while the period runs
+    int64_t free_slots = 0;
+    for (int64_t o : s->occupant) free_slots += o < 0 ? 1 : 0;
+    int64_t staged = 0;
+    for (auto it = s->queue.begin(); it != s->queue.end() && staged < free_slots + 2;) {
+        Request &r = s->reqs[*it];
+        if (!stage(s, r) && r.state == LG_REQ_FAILED) {
+            it = s->queue.erase(it);
+            continue;
+        }
+        staged += r.stage ? 1 : 0;
+        ++it;
     }
     if (n_active) *n_active = (int32_t)s->active.size();
     if (n_queued) *n_queued = (int32_t)s->queue.size();
@@ -375,6 +493,15 @@ extern "C" int lg_server_get_stats(lg_server *s, lg_server_stats *o) {
     o->failed = s->failed;
     o->cancelled = s->cancelled;
     o->particle_steps = s->particle_steps;
+    o->slots = (int64_t)s->caps.size();
+    for (size_t q = 0; q < s->caps.size(); ++q) {
+        o->slot_particles += s->caps[q];
+        if (s->occupant[q] >= 0) {
+            o->slots_busy++;
+            o->resident_particles += s->reqs[s->occupant[q]].n;
+        }
+    }
+    o->hamaker_slices = s->tmpl.precision == LG_PRECISION_MIXED ? lg::mixed_hamaker_slices(o->slot_particles) : 0;
     if (!s->latencies.empty()) {
         std::vector<double> l = s->latencies;
         std::sort(l.begin(), l.end());

@@ -11,7 +11,8 @@ def _dp(a):
 
 
 class Server:
-    """Continuous-batching server: submit requests at any time, call tick() to make progress."""
+    """Continuous-batching server: submit requests at any time, call tick() to make progress; resident
+    requests share slots of one batch and advance in the same launches."""
 
     def __init__(self, template_desc, budget_bytes, dt, rebuild_every=20, device=0):
         self.tmpl = template_desc
@@ -31,6 +32,12 @@ class Server:
             self.close()
         except Exception:
             pass
+
+    def set_slots(self, capacities):
+        """Slot capacities of the server's batch (before the first admission)."""
+        c = np.ascontiguousarray(capacities, dtype=np.int64)
+        A.check(A.lib().lg_server_set_slots(self.h, c.ctypes.data_as(C.POINTER(C.c_int64)), len(c)),
+                "lg_server_set_slots")
 
     def estimate_bytes(self, n):
         return A.lib().lg_estimate_device_bytes(C.byref(self.tmpl), int(n))

@@ -1,5 +1,5 @@
-"""Serving loop on the GPU: requests of different sizes arrive while others run, share the device
-within a memory budget, and each result is the same as the request run alone."""
+"""Serving loop on the GPU: requests of different sizes arrive while others run, occupy slots of one
+batch and advance in the same launches, and each result is the same as the request run alone."""
 import numpy as np
 import pytest
 
@@ -32,15 +32,18 @@ def test_results_in_the_mix_equal_results_alone(prec):
     reqs = []
     arrivals = {0: [0, 1], 2: [2, 3], 3: [4], 5: [5]}  # tick -> requests submitted before that tick
     tick = 0
+    busy = 0
     while True:
         for q in arrivals.get(tick, []):
             x0, v0 = _req(500 + q, sizes[q])
             reqs.append((q, s.submit(x0, v0, steps[q])))
         a, qd, _ = s.tick()
+        busy = max(busy, s.stats()["slots_busy"])
         tick += 1
         if tick > 5 and a == 0 and qd == 0:
             break
         assert tick < 1000
+    assert busy >= 4  # requests shared the batch's launches
     for q, rid in reqs:
         p = s.poll(rid, want_x=True)
         assert p["state"] == A.LG_REQ_DONE, p["error"]
@@ -48,6 +51,8 @@ def test_results_in_the_mix_equal_results_alone(prec):
         dd = K.make_desc(sizes[q], d.binary_model, d.hamaker_model, contact=d.contact, sinter=d.sinter,
                          hamaker=d.hamaker, pairs=d.pairs, r_verlet=d.r_verlet, precision=prec, max_neighbors=96)
         alone = System(dd, x0, v0)
+        if prec == A.LG_PRECISION_MIXED:  # the server's Hamaker slicing gives the batch's bits
+            alone.set_step_shape(0, s.stats()["hamaker_slices"], 0)
         alone.step(mat.dt, steps[q], 20)
         assert np.array_equal(p["x"], alone.get(A.LG_FIELD_X)), q
         ao = alone.observables()
@@ -57,30 +62,51 @@ def test_results_in_the_mix_equal_results_alone(prec):
     assert st["p99_latency_ms"] >= st["p50_latency_ms"] > 0
 
 
-def test_budget_bounds_resident_requests():
+def test_slots_bound_resident_requests():
+    """Two slots: six requests of 1500 monomers run two at a time and all complete; the slots and
+    the standalone handles being prepared stay within the budget."""
     mat, d = _tmpl()
-    per = Server(d, budget_bytes=1 << 40, dt=mat.dt).estimate_bytes(1500)
-    s = Server(d, budget_bytes=int(2.5 * per), dt=mat.dt)  # room for two at a time
+    s = Server(d, budget_bytes=16 << 30, dt=mat.dt)
+    s.set_slots([2048, 2048])
     ids = [s.submit(*_req(900 + q, 1500), 100) for q in range(6)]
     peak_active = 0
     while True:
         a, qd, _ = s.tick()
         st = s.stats()
         assert st["used_bytes"] <= st["budget_bytes"]
+        assert st["slots_busy"] <= 2
         peak_active = max(peak_active, a)
         if a == 0 and qd == 0:
             break
     assert peak_active == 2
     assert all(s.poll(r)["state"] == A.LG_REQ_DONE for r in ids)
-    assert s.stats()["peak_bytes"] <= int(2.5 * per)
+    assert s.stats()["completed"] == 6
 
 
-def test_cancel_running_request_returns_its_memory():
+def test_cancel_running_request_frees_its_slot():
     mat, d = _tmpl()
     s = Server(d, budget_bytes=4 << 30, dt=mat.dt)
+    s.set_slots([1024])
     r1 = s.submit(*_req(1, 500), 10000)
     s.tick()
-    assert s.stats()["used_bytes"] > 0
+    assert s.stats()["slots_busy"] == 1
+    r2 = s.submit(*_req(2, 600), 40)
+    s.tick()
+    assert s.poll(r2)["state"] == A.LG_REQ_QUEUED  # the only slot is taken
     s.cancel(r1)
     assert s.poll(r1)["state"] == A.LG_REQ_CANCELLED
-    assert s.stats()["used_bytes"] == 0
+    assert s.stats()["slots_busy"] == 0
+    for _ in range(20):
+        a, qd, _ = s.tick()
+        if a == 0 and qd == 0:
+            break
+    p = s.poll(r2, want_x=True)
+    assert p["state"] == A.LG_REQ_DONE, p["error"]
+    # the slot's previous occupant left nothing behind: the result equals the request alone
+    x0, v0 = _req(2, 600)
+    dd = K.make_desc(600, d.binary_model, d.hamaker_model, contact=d.contact, sinter=d.sinter, hamaker=d.hamaker,
+                     pairs=d.pairs, r_verlet=d.r_verlet, precision=d.precision, max_neighbors=96)
+    alone = System(dd, x0, v0)
+    alone.set_step_shape(0, s.stats()["hamaker_slices"], 0)
+    alone.step(mat.dt, 40, 20)
+    assert np.array_equal(p["x"], alone.get(A.LG_FIELD_X))

@@ -1,5 +1,5 @@
-"""Serving loop host logic without a GPU: request validation, budget admission, injected
-allocation failure, cancellation (no request here ever reaches a device)."""
+"""Serving loop host logic without a GPU: request validation, slot configuration against the budget,
+injected allocation failure, cancellation (no request here ever reaches a device)."""
 import numpy as np
 
 from libgran_gb300 import _abi as A
@@ -54,3 +54,26 @@ def test_cancel_queued_request_and_estimates():
     assert s.stats()["queued"] == 0 and s.stats()["cancelled"] == 1
     e = [s.estimate_bytes(n) for n in (64, 512, 8192)]
     assert e[0] < e[1] < e[2]
+
+
+def test_slot_configuration():
+    """Default slots shrink to fit the budget; explicit slots must fit it; a request larger than the
+    largest slot is refused at submission."""
+    mat, d = _tmpl()
+    big = Server(d, budget_bytes=150 * 10 ** 9, dt=mat.dt).stats()
+    small = Server(d, budget_bytes=256 << 20, dt=mat.dt).stats()
+    assert big["slots"] == 56 and big["slot_particles"] == 8 * (128 + 256 + 512 + 1024 + 2048 + 4096 + 8192)
+    assert 1 <= small["slots"] < big["slots"] and small["slot_particles"] < big["slot_particles"]
+    s = Server(d, budget_bytes=1 << 30, dt=mat.dt)
+    try:
+        s.set_slots([10 ** 7])
+        assert False, "slots beyond the budget were accepted"
+    except A.LgError as e:
+        assert "budget" in str(e)
+    s.set_slots([300, 100])
+    st = s.stats()
+    assert st["slots"] == 2 and st["slot_particles"] == 400 and st["slots_busy"] == 0
+    rid = A.C.c_int64()
+    x = np.zeros((301, 3))
+    rc = A.lib().lg_server_submit(s.h, 301, x.ctypes.data_as(A.C.POINTER(A.C.c_double)), None, 20, A.C.byref(rid))
+    assert rc == A.LG_E_NOMEM and b"largest slot" in A.lib().lg_last_error()
