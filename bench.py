@@ -630,7 +630,9 @@ def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):
             "offered_particle_steps_per_s": sum(n * steps for (_, n, steps, _) in arrivals) / duration_s,
             "wall_s": wall, "peak_bytes": st["peak_bytes"], "budget_bytes": budget_bytes, "slots": st["slots"],
             "slot_particles": st["slot_particles"], "mean_slots_busy": float(np.mean(busy)) if busy else 0.0,
-            "mean_resident_particles": float(np.mean(resident)) if resident else 0.0}
+            "mean_resident_particles": float(np.mean(resident)) if resident else 0.0,
+            "gpu_busy_frac": st["device_ms"] / 1e3 / wall, "periods": st["periods"],
+            "resident_particle_steps_per_device_s": st["particle_steps"] / max(st["device_ms"] / 1e3, 1e-9)}
 
 
 def serving_template(precision):

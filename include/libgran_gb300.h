@@ -511,6 +511,8 @@ typedef struct lg_server_stats {
     int64_t slots, slots_busy;              /* slots of the batch, slots holding a request */
     int64_t slot_particles, resident_particles;  /* capacity of all slots, particles of the residents */
     int32_t hamaker_slices;                 /* mixed precision: Hamaker slices of the batch's kernels */
+    double device_ms;                       /* device time of the periods run (CUDA events) */
+    int64_t periods;                        /* periods run */
 } lg_server_stats;
 
 /* Device bytes a system of n particles (a request alone, or the slots together) is charged. */

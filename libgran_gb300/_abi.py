@@ -63,7 +63,7 @@ class lg_server_stats(C.Structure):
                                          "rejected", "failed", "cancelled", "particle_steps")] + \
                [(n, C.c_double) for n in ("p50_latency_ms", "p99_latency_ms", "max_latency_ms")] + \
                [(n, C.c_int64) for n in ("slots", "slots_busy", "slot_particles", "resident_particles")] + \
-               [("hamaker_slices", C.c_int32)]
+               [("hamaker_slices", C.c_int32), ("device_ms", C.c_double), ("periods", C.c_int64)]
 
 
 class lg_body_force(C.Structure):

@@ -401,7 +401,7 @@ static int rebuild_list(lg_system *s) {
     BatchView B{s->d_agg, s->d_hoff, s->P.hold};
     launch_list_build(s->P.n, s->x, B, s->P.r_verlet, s->r_near, s->max_cells, s->ls, o, newv, s->bv, s->err,
                       s->stream);
-    s->launches += 7;
+    s->launches += 9;
     s->pcur = 1 - s->pcur;
     s->list_built = true;
     LG_CUDA(cudaGetLastError());
@@ -1031,6 +1031,7 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
         LG_TRY(s->alloc(&s->ls.start, (size_t)s->max_cells));
         LG_TRY(s->alloc(&s->ls.fill, (size_t)s->max_cells));
         LG_TRY(s->alloc(&s->ls.sorted, (size_t)n));
+        LG_TRY(s->alloc(&s->ls.tile, (size_t)(s->max_cells / 4096 + 1)));
         LG_TRY(s->alloc(&s->ls.x32, (size_t)n));
         LG_TRY(s->alloc(&s->ls.max_row, 1));
         LG_CUDA(cudaMemset(s->ls.max_row, 0, sizeof(int32_t)));

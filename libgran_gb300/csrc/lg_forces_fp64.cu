@@ -407,28 +407,96 @@ __global__ void cell_count(int64_t n, const dbl4 *__restrict__ x, BatchView B, c
     atomicAdd(&count[c], 1);
 }
 
-// Exclusive scan of cell counts, single block (cells <= a few million).
-__global__ void scan_cells(const GridDev *__restrict__ g, const int32_t *__restrict__ count, int32_t *__restrict__ start) {
-    __shared__ int32_t part[1024];
-    const int64_t nc = g->ncell;
-    const int t = threadIdx.x, T = blockDim.x;
-    const int64_t per = (nc + T - 1) / T;
-    const int64_t b = (int64_t)t * per, e = b + per < nc ? b + per : nc;
-    int32_t s = 0;
-    for (int64_t c = b; c < e; ++c) s += count[c];
-    part[t] = s;
+// Exclusive scan of the cell counts (start of every cell in the sorted list), in three passes over
+// tiles of kScanTile cells: the tiles' totals, an exclusive scan of the totals (one block), and each
+// tile's own scan plus its offset. Loads and stores go through shared memory so that they coalesce.
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = 16;
+constexpr int kScanTile = kScanThreads * kScanPer;  // 4096 cells
+
+__global__ void __launch_bounds__(kScanThreads) scan_tile_sums(const GridDev *__restrict__ g,
+                                                                const int32_t *__restrict__ count,
+                                                                int32_t *__restrict__ tile_sum) {
+    const int64_t nc = g->ncell, base = (int64_t)blockIdx.x * kScanTile;
+    if (base >= nc) return;
+    __shared__ int32_t red[kScanThreads];
+    int32_t v = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        const int64_t c = base + (int64_t)k * kScanThreads + threadIdx.x;
+        if (c < nc) v += count[c];
+    }
+    red[threadIdx.x] = v;
     __syncthreads();
-    // Hillis-Steele inclusive scan of the per-thread sums
-    for (int o = 1; o < T; o <<= 1) {
-        int32_t v = t >= o ? part[t - o] : 0;
+    for (int o = kScanThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = red[0];
+}
+
+// Exclusive scan of the tile totals in place (one block of 1024 threads, any number of tiles).
+__global__ void __launch_bounds__(1024) scan_tile_offsets(const GridDev *__restrict__ g, int32_t *__restrict__ tile_sum) {
+    __shared__ int32_t part[1024];
+    const int64_t tiles = (g->ncell + kScanTile - 1) / kScanTile;
+    const int t = threadIdx.x;
+    const int64_t per = (tiles + 1023) / 1024;
+    const int64_t b = (int64_t)t * per, e = b + per < tiles ? b + per : tiles;
+    int32_t sum = 0;
+    for (int64_t q = b; q < e; ++q) sum += tile_sum[q];
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int32_t v = t >= o ? part[t - o] : 0;
         __syncthreads();
         part[t] += v;
         __syncthreads();
     }
-    int32_t run = part[t] - s;
-    for (int64_t c = b; c < e; ++c) {
-        start[c] = run;
-        run += count[c];
+    int32_t run = part[t] - sum;
+    for (int64_t q = b; q < e; ++q) {
+        const int32_t c = tile_sum[q];
+        tile_sum[q] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_tiles(const GridDev *__restrict__ g, const int32_t *__restrict__ count,
+                                                            const int32_t *__restrict__ tile_off,
+                                                            int32_t *__restrict__ start) {
+    const int64_t nc = g->ncell, base = (int64_t)blockIdx.x * kScanTile;
+    if (base >= nc) return;
+    __shared__ int32_t cell[kScanTile];
+    __shared__ int32_t part[kScanThreads];
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {  // coalesced load of the tile
+        const int64_t c = base + (int64_t)k * kScanThreads + t;
+        cell[k * kScanThreads + t] = c < nc ? count[c] : 0;
+    }
+    __syncthreads();
+    int32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) sum += cell[t * kScanPer + k];
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < kScanThreads; o <<= 1) {
+        const int32_t v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int32_t run = tile_off[blockIdx.x] + part[t] - sum;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {  // exclusive starts of this thread's cells, in place
+        const int32_t c = cell[t * kScanPer + k];
+        cell[t * kScanPer + k] = run;
+        run += c;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {  // coalesced store
+        const int64_t c = base + (int64_t)k * kScanThreads + t;
+        if (c < nc) start[c] = cell[k * kScanThreads + t];
     }
 }
 
@@ -766,7 +834,10 @@ void launch_list_build(int64_t n, const dbl4 *x, BatchView B, double rv, double 
     const int threads = 256;
     unsigned blocks = (unsigned)((n + threads - 1) / threads);
     cell_count<<<blocks, threads, 0, st>>>(n, x, B, ls.grid, ls.cell_of, ls.count, ls.x32);
-    scan_cells<<<1, 1024, 0, st>>>(ls.grid, ls.count, ls.start);
+    const unsigned tiles = (unsigned)((max_cells + kScanTile - 1) / kScanTile);
+    scan_tile_sums<<<tiles, kScanThreads, 0, st>>>(ls.grid, ls.count, ls.tile);
+    scan_tile_offsets<<<1, 1024, 0, st>>>(ls.grid, ls.tile);
+    scan_tiles<<<tiles, kScanThreads, 0, st>>>(ls.grid, ls.count, ls.tile, ls.start);
     cell_scatter<<<blocks, threads, 0, st>>>(n, ls.cell_of, ls.start, ls.fill, ls.sorted);
     const unsigned b2 = (unsigned)((n + kBuildRows - 1) / kBuildRows);
     const size_t smem = build_smem_bytes(newv.cap, BV.bcap);

@@ -33,6 +33,7 @@ struct ListScratch {
     int32_t *start;    // [max_cells]
     int32_t *fill;     // [max_cells]
     int32_t *sorted;   // [n]
+    int32_t *tile;     // [max_cells / 4096 + 1] cell-scan tile totals, then their offsets
     float4 *x32;       // [n] positions relative to the grid origin, FP32 (candidate filter)
     int32_t *max_row;  // [1] longest row found by the last build (before truncation)
 };

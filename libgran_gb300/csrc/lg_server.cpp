@@ -80,9 +80,11 @@ struct lg_server {
     std::vector<int64_t> occupant;  // request in every slot, -1: free
     lg_system *arena = nullptr;
     int64_t arena_bytes = 0;
-    cudaEvent_t done_ev = nullptr;
+    cudaEvent_t start_ev = nullptr, done_ev = nullptr;
     bool in_flight = false;
     int64_t flight_steps = 0;
+    double device_ms = 0.0;  // device time of the periods run so far
+    int64_t periods = 0;
 };
 
 extern "C" int64_t lg_estimate_device_bytes(const lg_system_desc *d, int64_t n) {
@@ -181,6 +183,10 @@ static int wait_flight(lg_server *s) {
         cudaGetLastError();
         return lg_fail(LG_E_CUDA, "serving period failed on the device: %s", cudaGetErrorString(e));
     }
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, s->start_ev, s->done_ev) == cudaSuccess) s->device_ms += ms;
+    cudaGetLastError();
+    s->periods++;
     for (int64_t id : s->active) {
         Request &r = s->reqs[id];
         r.done_steps += s->flight_steps;
@@ -202,6 +208,7 @@ extern "C" int lg_server_destroy(lg_server *s) {
     for (auto &kv : s->reqs) drop_stage(s, kv.second);
     if (s->arena) lg_destroy(s->arena);
     if (s->done_ev) cudaEventDestroy(s->done_ev);
+    if (s->start_ev) cudaEventDestroy(s->start_ev);
     delete s;
     return LG_OK;
 }
@@ -302,7 +309,7 @@ static int ensure_arena(lg_server *s) {
                        (long long)(s->budget - s->used), (long long)s->budget);
     int rc = lg_arena_create(&s->tmpl, (int64_t)s->caps.size(), s->caps.data(), s->device, &s->arena);
     if (rc != LG_OK) return rc;
-    if (cudaEventCreateWithFlags(&s->done_ev, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaEventCreate(&s->done_ev) != cudaSuccess || cudaEventCreate(&s->start_ev) != cudaSuccess) {
         cudaGetLastError();
         return lg_fail(LG_E_CUDA, "cudaEventCreate failed");
     }
@@ -425,7 +432,9 @@ extern "C" int lg_server_tick(lg_server *s, int32_t *n_active, int32_t *n_queued
     if (!s->active.empty()) {
         int64_t k = s->rebuild_every - (s->arena->step_index % s->rebuild_every);
         for (int64_t id : s->active) k = std::min(k, s->reqs[id].nsteps - s->reqs[id].done_steps);
-        rc = lg_step(s->arena, s->dt, k, s->rebuild_every);
+        rc = cudaEventRecord(s->start_ev, s->arena->stream) == cudaSuccess
+                 ? LG_OK : lg_fail(LG_E_CUDA, "cudaEventRecord failed");
+        if (rc == LG_OK) rc = lg_step(s->arena, s->dt, k, s->rebuild_every);
         if (rc == LG_OK && cudaEventRecord(s->done_ev, s->arena->stream) != cudaSuccess) {
             cudaGetLastError();
             rc = lg_fail(LG_E_CUDA, "cudaEventRecord failed");
@@ -502,6 +511,8 @@ extern "C" int lg_server_get_stats(lg_server *s, lg_server_stats *o) {
         }
     }
     o->hamaker_slices = s->tmpl.precision == LG_PRECISION_MIXED ? lg::mixed_hamaker_slices(o->slot_particles) : 0;
+    o->device_ms = s->device_ms;
+    o->periods = s->periods;
     if (!s->latencies.empty()) {
         std::vector<double> l = s->latencies;
         std::sort(l.begin(), l.end());
