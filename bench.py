@@ -499,7 +499,9 @@ def run_gb300(args, rank, world):
     if os.environ.get("LG_BENCH_SERVING", "1") != "0":
         lams = [float(v) for v in os.environ.get("LG_SERVE_LAMBDAS", "8,32,64,128").split(",")]
         dur = float(os.environ.get("LG_SERVE_SECONDS", "8"))
-        serving = {"sweep": [serving_section(lam, dur) for lam in lams], "accuracy": serving_force_error()}
+        per = int(os.environ.get("LG_SERVE_SLOTS_PER_CLASS", "24")) or None
+        serving = {"sweep": [serving_section(lam, dur, slots_per_class=per) for lam in lams],
+                   "accuracy": serving_force_error()}
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tm["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -577,7 +579,10 @@ def restructuring_section(args, l2_flush, steps=None, count=None):
     return out
 
 
-def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):
+SLOT_CLASSES = (128, 256, 512, 1024, 2048, 4096, 8192)
+
+
+def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9, slots_per_class=None):
     """Serving workload: Poisson arrivals at rate lam (requests/s) for duration_s seconds; each
     request an aggregate of log-uniform 64..8192 monomers with its own seed and a step budget drawn
     uniformly from 2e3..2e4 (multiples of 20), mixed precision, sintered bonds + contact + limited
@@ -604,6 +609,8 @@ def serving_section(lam, duration_s, seed=4, budget_bytes=150 * 10 ** 9):
     inputs = [(generate_aggregate((4 << 32) + k, n, mat.r), generate_velocities((4 << 32) + k, n, 0.1))
               for (_, n, _, k) in arrivals]
     srv = Server(d, budget_bytes=budget_bytes, dt=mat.dt)
+    if slots_per_class:
+        srv.set_slots([c for c in SLOT_CLASSES for _ in range(int(slots_per_class))])
     t0 = time.perf_counter()
     nxt = 0
     busy, resident = [], []

@@ -11,7 +11,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <unordered_map>
@@ -337,9 +339,15 @@ void lg_system::drop_graphs() {
 void lg_system::release() {
     if (device >= 0) cudaSetDevice(device);
     drop_graphs();
-    if (h_pin) cudaFreeHost(h_pin);
+    if (h_pin) {
+        if (pooled) std::free(h_pin);
+        else cudaFreeHost(h_pin);
+    }
     h_pin = nullptr;
-    for (void *p : allocations) cudaFree(p);
+    for (void *p : allocations) {
+        if (pooled && stream) cudaFreeAsync(p, stream);  // in stream order, after the handle's work
+        else cudaFree(p);
+    }
     allocations.clear();
     if (stream) cudaStreamDestroy(stream);
     if (side) cudaStreamDestroy(side);
@@ -356,7 +364,17 @@ void lg_system::release() {
 
 template <typename U>
 int lg_system::alloc(U **p, size_t count) {
-    LG_TRY(dalloc(p, count));
+    if (pooled && stream) {
+        *p = nullptr;
+        cudaError_t e = cudaMallocAsync((void **)p, sizeof(U) * std::max<size_t>(count, 1), stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // usable from any stream on return
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return lg_fail(LG_E_NOMEM, "cudaMallocAsync of %zu bytes failed: %s", sizeof(U) * count, cudaGetErrorString(e));
+        }
+    } else {
+        LG_TRY(dalloc(p, count));
+    }
     allocations.push_back((void *)*p);
     return LG_OK;
 }
@@ -1064,7 +1082,12 @@ static int create_impl(const lg_system_desc *d, const double *x0, const double *
     LG_TRY(s->alloc(&s->obs_scratch, (size_t)obs_scratch_doubles(n)));
     LG_TRY(s->alloc(&s->d_ticket, 1));
     LG_CUDA(cudaMemset(s->d_ticket, 0, sizeof(unsigned)));
-    LG_CUDA(cudaMallocHost(&s->h_pin, 64 * sizeof(double)));
+    if (s->pooled) {  // plain host memory: freeing pinned memory can synchronise the device
+        s->h_pin = (double *)std::malloc(64 * sizeof(double));
+        if (!s->h_pin) return lg_fail(LG_E_NOMEM, "lg_create: host allocation failed");
+    } else {
+        LG_CUDA(cudaMallocHost(&s->h_pin, 64 * sizeof(double)));
+    }
     LG_TRY(s->alloc(&s->obs_out, 32));
 
     if (s->precision == LG_PRECISION_MIXED) {
@@ -1875,6 +1898,39 @@ int lg_arena_create(const lg_system_desc *tmpl, int64_t n_slots, const int64_t *
     return LG_OK;
 }
 
+int lg_create_staged(const lg_system_desc *desc, const double *x0, const double *v0, int device, lg_system **out) {
+    if (!desc || !x0 || !v0 || !out) return lg_fail(LG_E_INVALID, "lg_create_staged: bad arguments");
+    *out = nullptr;
+    lg_system *s = new (std::nothrow) lg_system();
+    if (!s) return lg_fail(LG_E_NOMEM, "lg_create_staged: host allocation failed");
+    s->pooled = true;
+    static std::mutex pool_mu;
+    static std::vector<int> pool_set;  // devices whose default pool keeps freed memory for reuse
+    {
+        std::lock_guard<std::mutex> lk(pool_mu);
+        if (std::find(pool_set.begin(), pool_set.end(), device) == pool_set.end()) {
+            cudaMemPool_t pool = nullptr;
+            if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+                uint64_t keep = UINT64_MAX;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+            cudaGetLastError();
+            pool_set.push_back(device);
+        }
+    }
+    const std::vector<double> zeros(3 * (size_t)std::max<int64_t>(desc->n_part, 1), 0.0);
+    int rc = create_impl(desc, x0, v0, zeros.data(), zeros.data(), nullptr, nullptr, 0, device, s);
+    if (rc != LG_OK) {
+        std::string keep = g_last_error;
+        s->release();
+        delete s;
+        g_last_error = keep;
+        return rc;
+    }
+    *out = s;
+    return LG_OK;
+}
+
 int lg_arena_import(lg_system *A, int64_t q, lg_system *S, const double *x0) {
     if (!A || !S || !x0 || !A->arena || q < 0 || q >= A->n_systems)
         return lg_fail(LG_E_INVALID, "lg_arena_import: bad arguments");
@@ -2007,6 +2063,36 @@ int lg_arena_clear(lg_system *A, int64_t q) {
     A->n_bonds_initial_sys[(size_t)q] = 0;
     LG_CUDA(cudaGetLastError());
     LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+int lg_arena_observables(lg_system *A, int64_t q, int64_t n, lg_observables *o) {
+    if (!A || !o || !A->arena || q < 0 || q >= A->n_systems || n < 1 || n > A->sys_off[q + 1] - A->sys_off[q])
+        return lg_fail(LG_E_INVALID, "lg_arena_observables: bad arguments");
+    const Params &P = A->P;
+    const bool sint = P.binary_model == LG_BINARY_SINTER || P.binary_model == LG_BINARY_BREAKING_SINTER;
+    const bool cmass = P.binary_model == LG_BINARY_CONTACT;
+    const double m = sint ? P.sinter.mass : (cmass ? P.contact.mass : P.hamaker.mass);
+    const double I = sint ? P.sinter.inertia : P.contact.inertia;
+    StateView S = state_view(A, false);
+    launch_observables_range(P, S, A->pv[A->pcur], A->bv, m, I, A->sys_off[q], n, A->obs_scratch, A->obs_out, A->stream);
+    A->launches += 2;
+    LG_CUDA(cudaGetLastError());
+    double h[20];
+    LG_CUDA(cudaMemcpyAsync(h, A->obs_out, sizeof(double) * 18, cudaMemcpyDeviceToHost, A->stream));
+    LG_CUDA(cudaStreamSynchronize(A->stream));
+    memset(o, 0, sizeof(*o));
+    o->ke_total = h[0];
+    o->ke_translational = h[1] / 2.0;
+    o->ke_rotational = h[2] / 2.0;
+    o->linear_momentum = m * std::sqrt((h[3] * h[3] + h[4] * h[4]) + h[5] * h[5]);
+    const double L[3] = {h[6] + h[9], h[7] + h[10], h[8] + h[11]};
+    o->angular_momentum = std::sqrt((L[0] * L[0] + L[1] * L[1]) + L[2] * L[2]);
+    for (int k = 0; k < 3; ++k) o->center_of_mass[k] = h[12 + k] / (double)n;
+    o->potential_energy = h[15];
+    o->n_contacts = (int64_t)h[16];
+    o->n_bonds = (int64_t)h[17];
+    o->n_bonds_initial = A->n_bonds_initial_sys[(size_t)q];
     return LG_OK;
 }
 

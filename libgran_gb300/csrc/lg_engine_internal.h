@@ -142,6 +142,9 @@ struct lg_system {
     int64_t step_index = 0;
     int64_t launches = 0;
     std::vector<void *> allocations;
+    // device memory from the stream-ordered pool (cudaMallocAsync / cudaFreeAsync on the handle's
+    // stream): releasing such a handle does not synchronise the device (serving's staging handles)
+    bool pooled = false;
 
     template <typename U>
     int alloc(U **p, size_t count);
@@ -162,7 +165,11 @@ int lg_fail(int code, const char *fmt, ...);
 // state (host arrays of 3n doubles, null: skipped). The caller keeps the arena at a rebuild
 // boundary and idle (synchronised) around imports and clears.
 int lg_arena_create(const lg_system_desc *tmpl, int64_t n_slots, const int64_t *caps, int device, lg_system **out);
+// A standalone handle whose device memory comes from the stream-ordered pool (lg_create otherwise).
+int lg_create_staged(const lg_system_desc *desc, const double *x0, const double *v0, int device, lg_system **out);
 double lg_arena_radius_bound(int64_t cap, double r_part);
 int lg_arena_import(lg_system *arena, int64_t q, lg_system *src, const double *x0);
 int lg_arena_clear(lg_system *arena, int64_t q);
 int lg_arena_read(lg_system *arena, int64_t q, int64_t n, double *x, double *v, double *theta, double *omega);
+// Observables of slot q's occupant (its first n particles; the radius of gyration is left at 0).
+int lg_arena_observables(lg_system *arena, int64_t q, int64_t n, lg_observables *out);

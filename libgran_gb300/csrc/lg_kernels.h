@@ -189,6 +189,10 @@ void launch_fill_dbl4(dbl4 *p, int64_t count, double x, double y, double z, cuda
 int64_t obs_scratch_doubles(int64_t n);
 void launch_observables(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double mass,
                         double inertia, double *scratch, double *out, cudaStream_t st, bool pairs = true);
+// Column sums 0..17 over the particles row0 .. row0 + count - 1 only (one system of a batch).
+void launch_observables_range(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
+                              double mass, double inertia, int64_t row0, int64_t count, double *scratch, double *out,
+                              cudaStream_t st);
 // Handle observables: out[0..14] and out[18] from the particles (launch_observables_state), out[15..17]
 // from the pair slots (launch_observables_pairs); scratch as above.
 void launch_observables_state(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, double mass, double inertia,

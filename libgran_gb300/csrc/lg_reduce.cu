@@ -44,13 +44,15 @@ __device__ __forceinline__ double hamaker_energy(int mode, const lg_hamaker_para
 // Per-particle terms. Column layout of a scratch row:
 //  0 e_tot  1 m|v|^2  2 I|w|^2  3-5 v  6-8 I w  9-11 x cross m v  12-14 x  15 potential energy
 //  16 contacts  17 intact bonds
+// Rows of particles row0 .. row0 + count - 1 into out rows 0 .. count - 1.
 __global__ void obs_rows(Params P, StateView S, PairView PV, BondView BV, double m, double I, int pairs,
-                         double *__restrict__ out) {
+                         double *__restrict__ out, int64_t row0, int64_t count) {
     const int64_t n = P.n;
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t i = row0 + t;
     const d3 v = ld4(S.v, i), w = ld4(S.w, i), x = ld4(S.x, i);
-    double *o = out + i * kObs;
+    double *o = out + t * kObs;
     o[0] = m * dot(v, v) / 2.0 + I * dot(w, w) / 2.0;
     o[1] = m * dot(v, v);
     o[2] = I * dot(w, w);
@@ -248,7 +250,7 @@ void launch_observables_pairs(const Params &P, const StateView &S, const PairVie
                               double inertia, double *scratch, double *out, cudaStream_t st) {
     const int64_t n = P.n;
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    obs_rows<<<blocks, 256, 0, st>>>(P, S, PV, BV, mass, inertia, 1, scratch);
+    obs_rows<<<blocks, 256, 0, st>>>(P, S, PV, BV, mass, inertia, 1, scratch, 0, P.n);
     obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 15, 18, out);
 }
 
@@ -258,8 +260,16 @@ void launch_observables(const Params &P, const StateView &S, const PairView &PV,
                         double inertia, double *scratch, double *out, cudaStream_t st, bool pairs) {
     const int64_t n = P.n;
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    obs_rows<<<blocks, 256, 0, st>>>(P, S, PV, BV, mass, inertia, pairs ? 1 : 0, scratch);
+    obs_rows<<<blocks, 256, 0, st>>>(P, S, PV, BV, mass, inertia, pairs ? 1 : 0, scratch, 0, n);
     obs_reduce<<<1, 1024, 0, st>>>(n, scratch, 0, 18, out);
+}
+
+void launch_observables_range(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
+                              double mass, double inertia, int64_t row0, int64_t count, double *scratch, double *out,
+                              cudaStream_t st) {
+    if (count <= 0) return;
+    obs_rows<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(P, S, PV, BV, mass, inertia, 1, scratch, row0, count);
+    obs_reduce<<<1, 1024, 0, st>>>(count, scratch, 0, 18, out);
 }
 
 

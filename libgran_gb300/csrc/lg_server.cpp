@@ -55,6 +55,9 @@ struct Request {
     std::string error;
 };
 
+// Most rebuild periods one tick runs without returning to the host.
+constexpr int64_t kChunkPeriods = 8;
+
 // Default slots: size classes 128 .. 8192 monomers, 8 slots each.
 const int64_t kClasses[] = {128, 256, 512, 1024, 2048, 4096, 8192};
 
@@ -287,8 +290,7 @@ static bool stage(lg_server *s, Request &r) {
         s->inject_alloc_failures--;
         rc = lg_fail(LG_E_NOMEM, "cudaMalloc failed: out of memory (injected)");
     } else {
-        std::vector<double> zeros(3 * r.n, 0.0);
-        rc = lg_create(&d, r.x0.data(), r.v0.data(), zeros.data(), zeros.data(), nullptr, nullptr, 0, s->device, &r.stage);
+        rc = lg_create_staged(&d, r.x0.data(), r.v0.data(), s->device, &r.stage);
     }
     if (rc != LG_OK) {
         r.stage = nullptr;
@@ -329,30 +331,22 @@ static int64_t free_slot(const lg_server *s, int64_t n) {
 
 static void retire(lg_server *s, std::vector<int64_t> &done) {
     if (done.empty()) return;
-    std::vector<lg_observables> obs(s->caps.size());
-    int rc = lg_batch_get_observables(s->arena, obs.data());
-    std::string why = rc != LG_OK ? std::string(lg_last_error()) : std::string();
+    std::string why;
     int32_t errs = 0;
-    if (rc == LG_OK && lg_get_device_errors(s->arena, &errs) == LG_OK && errs != 0)
-        why = "device error word set (" + std::to_string(errs) + ")";
+    if (lg_get_device_errors(s->arena, &errs) != LG_OK) why = lg_last_error();
+    else if (errs != 0) why = "device error word set (" + std::to_string(errs) + ")";
     for (int64_t id : done) {
         Request &r = s->reqs[id];
         r.x_final.resize(3 * r.n);
-        int rr = why.empty() ? lg_arena_read(s->arena, r.slot, r.n, r.x_final.data(), nullptr, nullptr, nullptr) : LG_E_STATE;
+        // observables over the occupant's own particles; the radius of gyration from its positions
+        int rr = why.empty() ? lg_arena_observables(s->arena, r.slot, r.n, &r.obs) : LG_E_STATE;
+        if (rr == LG_OK) rr = lg_arena_read(s->arena, r.slot, r.n, r.x_final.data(), nullptr, nullptr, nullptr);
         if (rr == LG_OK) {
-            // the slot's sums cover its inactive particles (at rest: no kinetic energy, momentum or
-            // contacts); centre of mass and radius of gyration are taken over the occupant alone
-            lg_observables o = obs[(size_t)r.slot];
-            double c[3] = {0.0, 0.0, 0.0}, rg = 0.0;
-            for (int k = 0; k < 3; ++k) {
-                for (int64_t i = 0; i < r.n; ++i) c[k] += r.x_final[3 * i + k];
-                c[k] /= (double)r.n;
-                o.center_of_mass[k] = c[k];
-            }
+            const double *c = r.obs.center_of_mass;
+            double rg = 0.0;
             for (int64_t i = 0; i < r.n; ++i)
                 for (int k = 0; k < 3; ++k) rg += (r.x_final[3 * i + k] - c[k]) * (r.x_final[3 * i + k] - c[k]);
-            o.radius_of_gyration = std::sqrt(rg / (double)r.n);
-            r.obs = o;
+            r.obs.radius_of_gyration = std::sqrt(rg / (double)r.n);
         }
         lg_arena_clear(s->arena, r.slot);
         s->occupant[(size_t)r.slot] = -1;
@@ -428,9 +422,19 @@ extern "C" int lg_server_tick(lg_server *s, int32_t *n_active, int32_t *n_queued
             it = s->queue.erase(it);
         }
     }
-    // the next period of every occupant, in the same launches
+    // the next periods of every occupant, in the same launches: up to the earliest budget end (the
+    // budgets are known), to the next boundary when a queued request could take a free slot there,
+    // and at most kChunkPeriods periods, so that the host returns between them only when it has
+    // something to do
     if (!s->active.empty()) {
-        int64_t k = s->rebuild_every - (s->arena->step_index % s->rebuild_every);
+        const int64_t to_boundary = s->rebuild_every - (s->arena->step_index % s->rebuild_every);
+        bool admit_next = false;
+        for (int64_t id : s->queue)
+            if (free_slot(s, s->reqs[id].n) >= 0) {
+                admit_next = true;
+                break;
+            }
+        int64_t k = admit_next ? to_boundary : to_boundary + (kChunkPeriods - 1) * s->rebuild_every;
         for (int64_t id : s->active) k = std::min(k, s->reqs[id].nsteps - s->reqs[id].done_steps);
         rc = cudaEventRecord(s->start_ev, s->arena->stream) == cudaSuccess
                  ? LG_OK : lg_fail(LG_E_CUDA, "cudaEventRecord failed");
@@ -443,11 +447,14 @@ extern "C" int lg_server_tick(lg_server *s, int32_t *n_active, int32_t *n_queued
         s->in_flight = true;
         s->flight_steps = k;
     }
-    // standalone handles for the head of the queue while the period runs
+    // standalone handles for the head of the queue while the periods run: as many as there will be
+    // free slots at the next return (free now, or freed by budgets ending), and a few more
     int64_t free_slots = 0;
     for (int64_t o : s->occupant) free_slots += o < 0 ? 1 : 0;
+    for (int64_t id : s->active)
+        if (s->reqs[id].done_steps + (s->in_flight ? s->flight_steps : 0) >= s->reqs[id].nsteps) ++free_slots;
     int64_t staged = 0;
-    for (auto it = s->queue.begin(); it != s->queue.end() && staged < free_slots + 2;) {
+    for (auto it = s->queue.begin(); it != s->queue.end() && staged < free_slots + 4;) {
         Request &r = s->reqs[*it];
         if (!stage(s, r) && r.state == LG_REQ_FAILED) {
             it = s->queue.erase(it);

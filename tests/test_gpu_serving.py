@@ -30,7 +30,7 @@ def test_results_in_the_mix_equal_results_alone(prec):
     steps = [200, 60, 140, 100, 40, 80]
     s = Server(d, budget_bytes=8 << 30, dt=mat.dt)
     reqs = []
-    arrivals = {0: [0, 1], 2: [2, 3], 3: [4], 5: [5]}  # tick -> requests submitted before that tick
+    arrivals = {0: [0, 1, 2, 3], 1: [4], 2: [5]}  # tick -> requests submitted before that tick
     tick = 0
     busy = 0
     while True:
