@@ -286,7 +286,7 @@ def accuracy_run(x0, v0, total=None, every=1000):
     return out
 
 
-def time_path(precision, x0, v0, args, l2_flush, tune=False):
+def time_path(precision, x0, v0, args, l2_flush, tune=False, kernel=None):
     """Device-timed K bench steps (each 20 VV steps, replayed as one CUDA graph) with CUDA events on
     the handle's stream; L2 is flushed before every timed bench step (the flush is outside the
     timed region). The force kernel's own duration is then measured on 2 further bench steps with
@@ -294,6 +294,8 @@ def time_path(precision, x0, v0, args, l2_flush, tune=False):
     from libgran_gb300 import _abi as A
     from libgran_gb300.system import System
     mat, d = workload_desc(precision)
+    if kernel is not None:
+        d.force_kernel = kernel
     s = System(d, x0, v0)
     tuning = None
     if tune:  # the project autotuner picks the kernel family and shape on the live system
@@ -450,6 +452,9 @@ def run_gb300(args, rank, world):
     # plain FP64 first (its number is reported beside the headline)
     s64, mat, t64 = time_path(A.LG_PRECISION_FP64, x0, v0, args, l2_flush)
     s64.close()
+    # the FP64 kernel with reciprocals instead of repeated divisions (within 1e-12, opt-in)
+    s64f, _, t64f = time_path(A.LG_PRECISION_FP64, x0, v0, args, l2_flush, kernel=A.LG_FORCE_KERNEL_FP64_FAST)
+    s64f.close()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -467,6 +472,7 @@ def run_gb300(args, rank, world):
     units = N_PART * VV_PER_STEP * args.steps
     value, tm["ms"] = combine_ranks(tm["ms"], units, world, amax if dist else None)
     value64, t64["ms"] = combine_ranks(t64["ms"], units, world, amax if dist else None)
+    value64f, t64f["ms"] = combine_ranks(t64f["ms"], units, world, amax if dist else None)
     e2e, obs = e2e_path(sm, mat, args, x0, v0)
     e2e["value"] *= world
     sm.close()
@@ -513,7 +519,11 @@ def run_gb300(args, rank, world):
                    else "single GPU"},
         "plain_fp64": {"value": value64, "unit": "particle-steps/s", "ms_per_step": t64["ms"] / args.steps,
                        "force_kernel_ms_per_launch": t64["kernel_ms"] / max(t64["kernel_launches"], 1)},
+        "plain_fp64_fast": {"value": value64f, "unit": "particle-steps/s", "ms_per_step": t64f["ms"] / args.steps,
+                            "force_kernel_ms_per_launch": t64f["kernel_ms"] / max(t64f["kernel_launches"], 1),
+                            "kernel": "LG_FORCE_KERNEL_FP64_FAST (per-step forces within 1e-12 of the reference's)"},
         "mixed_over_fp64": value / value64,
+        "mixed_over_fp64_fast": value / value64f,
         "accuracy": acc,
         "e2e": e2e,
         "gpu_launches": tm["launches"],

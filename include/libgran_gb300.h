@@ -210,6 +210,12 @@ typedef struct lg_system_desc {
                                        and Hamaker work items of 32-row groups from a device queue and
                                        complete each group when its last item finishes; the same bits as
                                        the compacted kernels. Other steps use the compacted kernels. */
+#define LG_FORCE_KERNEL_FP64_FAST 5  /* FP64: the compacted kernel with one reciprocal where libgran divides a
+                                       vector by a scalar, and the Hamaker bracket over one common
+                                       denominator (2 divisions per Hamaker pair instead of 12); contact is
+                                       decided by the reference's exact overlap. Per-step forces within
+                                       1e-12 of the reference's, not bit-identical; chosen explicitly only
+                                       (never by AUTO or the autotuner). */
 
 /* Fields that lg_get / lg_set move. */
 #define LG_FIELD_X 0       /* positions            get_x()     Granular-system.md:84-120 */

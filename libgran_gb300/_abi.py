@@ -18,6 +18,7 @@ LG_PRECISION_FP64, LG_PRECISION_MIXED = 0, 1
 LG_PAIRS_ALL, LG_PAIRS_VERLET = 0, 1
 LG_FORCE_KERNEL_AUTO, LG_FORCE_KERNEL_ROWGROUP, LG_FORCE_KERNEL_COMPACT, LG_FORCE_KERNEL_PAIRS = 0, 1, 2, 3
 LG_FORCE_KERNEL_PERSISTENT = 4
+LG_FORCE_KERNEL_FP64_FAST = 5
 LG_FIELD_X, LG_FIELD_V, LG_FIELD_THETA, LG_FIELD_OMEGA, LG_FIELD_A, LG_FIELD_ALPHA = range(6)
 LG_DEVERR_LIST_OVERFLOW, LG_DEVERR_NONFINITE, LG_DEVERR_BOND_LOST = 1, 2, 4
 LG_NOALLOC_OBS, LG_NOALLOC_MAX_PARTICLES = 9, 1048320

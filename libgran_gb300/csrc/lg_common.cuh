@@ -211,15 +211,34 @@ struct StateView {
 // ------------------------------------------------------------------------------------------------
 // FP64 functors
 // ------------------------------------------------------------------------------------------------
+// FAST = true: where libgran divides a vector by a scalar (normalisation, division by a mass or an
+// inertia) the vector is multiplied by one reciprocal, and the Hamaker bracket is evaluated over one
+// common denominator; every value stays within a few ulp of the reference's (per-step forces within
+// 1e-12 of it), but not bit-identical. FAST = false is the reference's arithmetic, operation for
+// operation.
+template <bool FAST>
+__device__ __forceinline__ d3 dvs_t(d3 a, double s) {
+    if (FAST) {
+        const double r = 1.0 / s;
+        return mk3(a.x * r, a.y * r, a.z * r);
+    }
+    return dvs(a, s);
+}
+template <bool FAST>
+__device__ __forceinline__ d3 nrmz_t(d3 a) {
+    const double z = sqn(a);
+    return z > 0.0 ? dvs_t<FAST>(a, sqrt(z)) : a;
+}
 
 // contact_force.h:105-147
+template <bool FAST = false>
 __device__ __forceinline__ d3 shear_coulomb(d3 &xi, d3 n, double stiffness, double damping, double normal_force,
                                             double mu_static, double phi_dynamic, d3 rel, double dt) {
     double mu_dynamic = mu_static * phi_dynamic;
     d3 xi_new = sub(xi, scl(dot(xi, n), n));
     if (nrm(xi_new) > 0.0) {
         double z = sqn(xi_new);
-        if (z > 0.0) xi_new = dvs(xi_new, sqrt(z));
+        if (z > 0.0) xi_new = dvs_t<FAST>(xi_new, sqrt(z));
         double old = nrm(xi);
         xi_new = scl(old, xi_new);
     }
@@ -228,7 +247,7 @@ __device__ __forceinline__ d3 shear_coulomb(d3 &xi, d3 n, double stiffness, doub
     double static_friction = mu_static * normal_force;
     double dynamic_friction = mu_dynamic * normal_force;
     double f0n = nrm(f0);
-    d3 t = (f0n > 0.0) ? nrmz(f0) : zero3();
+    d3 t = (f0n > 0.0) ? (FAST ? dvs_t<true>(f0, f0n) : nrmz(f0)) : zero3();
     double f_selected;
     if (f0n <= static_friction) {
         xi = add(xi, scl(dt, rel));
@@ -242,11 +261,12 @@ __device__ __forceinline__ d3 shear_coulomb(d3 &xi, d3 n, double stiffness, doub
 }
 
 // alt_sinter_bridge.h:137-156
+template <bool FAST = false>
 __device__ __forceinline__ d3 shear_bond(d3 &xi, d3 n, double stiffness, double damping, d3 rel, double dt) {
     d3 xi_new = sub(xi, scl(dot(xi, n), n));
     if (nrm(xi_new) > 0.0) {
         double z = sqn(xi_new);
-        if (z > 0.0) xi_new = dvs(xi_new, sqrt(z));
+        if (z > 0.0) xi_new = dvs_t<FAST>(xi_new, sqrt(z));
         double old = nrm(xi);
         xi_new = scl(old, xi_new);
     }
@@ -271,6 +291,7 @@ __device__ __forceinline__ double overlap_fp64(const dbl4 *x, int64_t i, int64_t
 
 // contact_force.h:57-96 -- the in-contact branch (caller has established overlap > 0 with the
 // reference's own arithmetic, n and overlap are passed in).
+template <bool FAST = false>
 __device__ __forceinline__ void contact_touching(const lg_contact_params &p, d3 n, double overlap, d3 vi, d3 vj,
                                                  d3 wi, d3 wj, d3 *s, d3 &oa, d3 &oal) {
     double rp = p.r_part - overlap / 2.0;
@@ -281,21 +302,22 @@ __device__ __forceinline__ void contact_touching(const lg_contact_params &p, d3 
     d3 v_t = sub(v_ij, scl(dot(v_ij, n), n));
     d3 v_r = scl(-rp, sub(nwi, nwj));
     d3 v_o = scl(p.r_part * (dot(n, wi) - dot(n, wj)), n);
-    d3 f_t = shear_coulomb(s[0], n, p.k_t, p.gamma_t, f_n, p.mu_s, p.phi_d, v_t, p.dt);
-    d3 f_r = shear_coulomb(s[1], n, p.k_r, p.gamma_r, f_n, p.mu_r, p.phi_r, v_r, p.dt);
-    d3 f_o = shear_coulomb(s[2], n, p.k_o, p.gamma_o, f_n, p.mu_o, p.phi_o, v_o, p.dt);
+    d3 f_t = shear_coulomb<FAST>(s[0], n, p.k_t, p.gamma_t, f_n, p.mu_s, p.phi_d, v_t, p.dt);
+    d3 f_r = shear_coulomb<FAST>(s[1], n, p.k_r, p.gamma_r, f_n, p.mu_r, p.phi_r, v_r, p.dt);
+    d3 f_o = shear_coulomb<FAST>(s[2], n, p.k_o, p.gamma_o, f_n, p.mu_o, p.phi_o, v_o, p.dt);
     d3 tau_t = scl(rp, crs(n, f_t));
     d3 tau_r = scl(p.r_part, crs(n, f_r));
     d3 tau_o = scl(p.r_part, f_o);
-    oa = dvs(add(scl(f_n, n), f_t), p.mass);
-    oal = dvs(add(add(neg(tau_t), tau_r), tau_o), p.inertia);
+    oa = dvs_t<FAST>(add(scl(f_n, n), f_t), p.mass);
+    oal = dvs_t<FAST>(add(add(neg(tau_t), tau_r), tau_o), p.inertia);
 }
 
 // alt_sinter_bridge.h:103-128 / alt_breaking_sinter_bridge.h:89-121. Returns true when the
 // breaking variant breaks the (i, j) bond (|f_tot| > strength, alt_breaking_sinter_bridge.h:118).
+template <bool FAST = false>
 __device__ __forceinline__ bool bond_force(const lg_sinter_params &p, d3 dx, d3 vi, d3 vj, d3 wi, d3 wj, d3 *s,
                                            bool breaking, double strength, d3 &oa, d3 &oal) {
-    d3 n = nrmz(dx);
+    d3 n = nrmz_t<FAST>(dx);
     double overlap = 2.0 * p.r_part - dot(dx, n);
     double rp = p.r_part - overlap / 2.0;
     double v_n = -dot(sub(vi, vj), n);
@@ -305,17 +327,17 @@ __device__ __forceinline__ bool bond_force(const lg_sinter_params &p, d3 dx, d3 
     d3 v_t = sub(v_ij, scl(dot(v_ij, n), n));
     d3 v_r = scl(-rp, sub(nwi, nwj));
     d3 v_o = scl(p.r_part * (dot(n, wi) - dot(n, wj)), n);
-    d3 f_t = shear_bond(s[0], n, p.k_t, p.gamma_t, v_t, p.dt);
-    d3 f_r = shear_bond(s[1], n, p.k_r, p.gamma_r, v_r, p.dt);
-    d3 f_o = shear_bond(s[2], n, p.k_o, p.gamma_o, v_o, p.dt);
+    d3 f_t = shear_bond<FAST>(s[0], n, p.k_t, p.gamma_t, v_t, p.dt);
+    d3 f_r = shear_bond<FAST>(s[1], n, p.k_r, p.gamma_r, v_r, p.dt);
+    d3 f_o = shear_bond<FAST>(s[2], n, p.k_o, p.gamma_o, v_o, p.dt);
     d3 tau_t = scl(rp, crs(n, f_t));
     d3 tau_r = scl(p.r_part, crs(n, f_r));
     d3 tau_o = scl(p.r_part, f_o);
     d3 f_tot = add(scl(f_n, n), f_t);
     d3 tau_tot = add(add(neg(tau_t), tau_r), tau_o);
     bool brk = breaking && (nrm(f_tot) > strength);
-    oa = dvs(f_tot, p.mass);
-    oal = dvs(tau_tot, p.inertia);
+    oa = dvs_t<FAST>(f_tot, p.mass);
+    oal = dvs_t<FAST>(tau_tot, p.inertia);
     return brk;
 }
 
@@ -365,11 +387,29 @@ __device__ __forceinline__ d3 hamaker_accel(int mode, const lg_hamaker_params &p
 }
 
 // As hamaker_accel, with rn = nrm(r) already computed (the same value nrm() and nrmz() would compute).
+// FAST: the bracket over one common denominator, D = (4r + h) h (2r + h), with u = 1 / ((4r + h) h)
+// = (2r + h) / D and w = 1 / (2r + h) = (4r + h) h / D:
+//   (4r+2h) u - 2 w - 4 r^2 w^3 - 2 r^2 (4r+2h) u^2,
+// and the scaling by 1 / (|r| m) as one factor: two divisions per pair instead of twelve.
+template <bool FAST = false>
 __device__ __forceinline__ d3 hamaker_accel_n(int mode, const lg_hamaker_params &p, d3 r, double rn) {
     double h = rn - 2.0 * p.r_part;
     if (h < p.h0) h = p.h0;
     double rp = p.r_part;
     double s;
+    if (FAST) {
+        if (mode == LG_HAMAKER_SIMPLIFIED) {
+            s = 2.0 * p.A * rp / sq_(h);
+        } else {
+            const double q = 4.0 * rp + h, w0 = 2.0 * rp + h, a = 4.0 * rp + 2.0 * h;
+            const double inv = 1.0 / (q * h * w0);
+            const double u = w0 * inv, w = q * h * inv;
+            const double br = a * u - 2.0 * w - 4.0 * sq_(rp) * (w * w * w) - 2.0 * sq_(rp) * a * (u * u);
+            s = -p.A / 6.0 * br;
+        }
+        if (!(rn > 0.0)) return dvs_t<true>(scl(s, r), p.mass);
+        return scl(s / (rn * p.mass), r);
+    }
     if (mode == LG_HAMAKER_SIMPLIFIED) {
         s = 2.0 * p.A * rp / sq_(h);
     } else {

@@ -390,6 +390,7 @@ constexpr int64_t kPairsAutoSlots = (int64_t)1 << 19;
 static int choose_kernel(const lg_system *s, int requested) {
     if (requested == LG_FORCE_KERNEL_ROWGROUP || requested == LG_FORCE_KERNEL_COMPACT) return requested;
     if (requested == LG_FORCE_KERNEL_PERSISTENT) return s->precision == LG_PRECISION_MIXED ? requested : -1;
+    if (requested == LG_FORCE_KERNEL_FP64_FAST) return s->precision == LG_PRECISION_FP64 ? requested : -1;
     if (requested == LG_FORCE_KERNEL_PAIRS) return s->pres ? requested : -1;
     const int64_t n = s->P.n;
     // mixed precision: the compacted kernels at every size (their float-float completion and fused
@@ -548,8 +549,9 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
         if (s->kernel == LG_FORCE_KERNEL_PAIRS)
             kernels = launch_forces_pairs_fp64(s->P, S, s->pv[s->pcur], s->bv, s->pres, hdt, dt, move_facets,
                                                fuse_kick, s->stream);
-        else if (compact)
-            launch_forces_compact_fp64(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
+        else if (compact || s->kernel == LG_FORCE_KERNEL_FP64_FAST)
+            launch_forces_compact_fp64(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream,
+                                       s->kernel == LG_FORCE_KERNEL_FP64_FAST);
         else
             launch_forces_fp64(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->stream);
     }
@@ -631,7 +633,9 @@ static int check_args(const lg_system_desc *d) {
     if (d->neck_mode != LG_NECK_PER_BOND && d->neck_mode != LG_NECK_REFERENCE_INDEXING) return lg_fail(LG_E_INVALID, "lg_create: unknown neck_mode %d", d->neck_mode);
     if (d->max_neighbors < 0 || d->max_neighbors > 255)
         return lg_fail(LG_E_INVALID, "lg_create: max_neighbors must be in [0, 255]");
-    if (d->force_kernel < 0 || d->force_kernel > 4) return lg_fail(LG_E_INVALID, "lg_create: unknown force_kernel %d", d->force_kernel);
+    if (d->force_kernel < 0 || d->force_kernel > 5) return lg_fail(LG_E_INVALID, "lg_create: unknown force_kernel %d", d->force_kernel);
+    if (d->force_kernel == LG_FORCE_KERNEL_FP64_FAST && d->precision != LG_PRECISION_FP64)
+        return lg_fail(LG_E_INVALID, "lg_create: the fast FP64 kernel is FP64 precision only");
     if (d->force_kernel == LG_FORCE_KERNEL_PERSISTENT && d->precision != LG_PRECISION_MIXED)
         return lg_fail(LG_E_INVALID, "lg_create: the persistent step kernel is mixed precision only");
     LG_TRY(validate_hold(d->hold_mask, d->n_part));
@@ -1479,10 +1483,12 @@ extern "C" int lg_set_threads_per_row(lg_system *s, int32_t T) {
 
 extern "C" int lg_set_force_kernel(lg_system *s, int32_t variant) {
     LG_HANDLE(s);
-    if (variant < 0 || variant > 4) return lg_fail(LG_E_INVALID, "lg_set_force_kernel: unknown variant %d", variant);
+    if (variant < 0 || variant > 5) return lg_fail(LG_E_INVALID, "lg_set_force_kernel: unknown variant %d", variant);
     const int k = choose_kernel(s, variant);
     if (k < 0 && variant == LG_FORCE_KERNEL_PERSISTENT)
         return lg_fail(LG_E_INVALID, "lg_set_force_kernel: the persistent step kernel is mixed precision only");
+    if (k < 0 && variant == LG_FORCE_KERNEL_FP64_FAST)
+        return lg_fail(LG_E_INVALID, "lg_set_force_kernel: the fast FP64 kernel is FP64 precision only");
     if (k < 0)
         return lg_fail(LG_E_INVALID, "lg_set_force_kernel: the pair-parallel kernel is FP64 only and takes at most "
                        "%lld pair slots", (long long)kPairsMaxSlots);
@@ -2208,7 +2214,7 @@ extern "C" int lg_autotune_cache_load(const char *path) {
         if (std::sscanf(line, "%d %d %d %d %d %d : %d %d %d %d %d %lf", &k[0], &k[1], &k[2], &k[3], &k[4], &k[5],
                         &t.force_kernel, &t.threads_per_row, &t.step_min_blocks, &t.step_slices, &t.step_assign,
                         &t.ms_per_step) != 12 ||
-            t.force_kernel < 1 || t.force_kernel > 4 || t.threads_per_row < 1 || t.threads_per_row > 32 ||
+            t.force_kernel < 1 || t.force_kernel > 5 || t.threads_per_row < 1 || t.threads_per_row > 32 ||
             (t.step_min_blocks < 4 || t.step_min_blocks > 6) || (t.step_slices != 1 && t.step_slices != 2 && t.step_slices != 4) ||
             (t.step_assign != 0 && t.step_assign != 1)) {
             rc = lg_fail(LG_E_INVALID, "lg_autotune_cache_load: %s line %d is not a cache entry", path, lineno);

@@ -1,4 +1,9 @@
 // lg_forces_compact.cu -- warp-compacted force kernel (sm_103a), FP64; compiled with --fmad=false.
+// Two instances: the reference's arithmetic operation for operation (bit-identical to the sequential
+// evaluation), and FAST (LG_FORCE_KERNEL_FP64_FAST), which multiplies by one reciprocal where libgran
+// divides a vector by a scalar and evaluates the Hamaker bracket over one common denominator
+// (per-step forces within 1e-12 of the reference's); both decide contact with the reference's exact
+// overlap.
 //
 // On GB300 a warp instruction on the FP64 pipe costs the same issue time whether 1 or 32 lanes are
 // active, so a kernel whose lanes each walk their own row and branch on "is this pair in Hamaker
@@ -55,7 +60,7 @@ struct WarpSmem {
 };
 
 // One queued contact / bond pair: owner row io (lane own of the warp), slot e, partner j.
-template <int SL>
+template <int SL, bool FAST>
 __device__ __forceinline__ void contact_item(const Params &P, const StateView &S, const PairView &PV,
                                              const BondView &BV, WarpSmem<SL> &W, int q, int64_t row0, int64_t kstart,
                                              int sl, int64_t n, int64_t xs, int64_t bs) {
@@ -80,7 +85,8 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
         for (int c = 0; c < 3; ++c)
             s[c] = mk3(BV.xi[(3 * c) * bs + be], BV.xi[(3 * c + 1) * bs + be], BV.xi[(3 * c + 2) * bs + be]);
         const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
-        const bool brk = bond_force(P.sinter, dx, vo, vj, wo, wj, s, breaking, breaking ? BV.strength[be] : 0.0, pa, pal);
+        const bool brk =
+            bond_force<FAST>(P.sinter, dx, vo, vj, wo, wj, s, breaking, breaking ? BV.strength[be] : 0.0, pa, pal);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             BV.xi[(3 * c) * bs + be] = s[c].x;
@@ -101,7 +107,7 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
                 for (int c = 0; c < 3; ++c)
                     s[c] = mk3(PV.xi[(3 * c) * xs + e], PV.xi[(3 * c + 1) * xs + e], PV.xi[(3 * c + 2) * xs + e]);
             const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
-            contact_touching(P.contact, nn, overlap, vo, vj, wo, wj, s, pa, pal);
+            contact_touching<FAST>(P.contact, nn, overlap, vo, vj, wo, wj, s, pa, pal);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 PV.xi[(3 * c) * xs + e] = s[c].x;
@@ -123,7 +129,7 @@ __device__ __forceinline__ void contact_item(const Params &P, const StateView &S
     W.cres[q][5] = pal.z;
 }
 
-template <int SL>
+template <int SL, bool FAST>
 __device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S, WarpSmem<SL> &W, int q) {
     const int own = W.hown[q] >> 8;
     const d3 xo = W.xo[own];
@@ -135,7 +141,7 @@ __device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S
     const double rn = nrm(r);
     bool on = true;
     if (P.hamaker_model == LG_HAMAKER_LIMITED) on = !(rn > P.hamaker.r_cutoff);
-    if (on) ha = hamaker_accel_n(P.hamaker_model, P.hamaker, r, rn);
+    if (on) ha = hamaker_accel_n<FAST>(P.hamaker_model, P.hamaker, r, rn);
     W.hres[q][0] = ha.x;
     W.hres[q][1] = ha.y;
     W.hres[q][2] = ha.z;
@@ -143,7 +149,7 @@ __device__ __forceinline__ void hamaker_item(const Params &P, const StateView &S
 
 }  // namespace
 
-template <bool VERLET, int SL>
+template <bool VERLET, int SL, bool FAST>
 __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
     forces_compact_fp64(Params P, StateView S, PairView PV, BondView BV, double hdt, double dt, int move_facets)
 {
@@ -250,7 +256,7 @@ __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
             }
             __syncwarp();
             while (ccount - cdone >= 32) {
-                contact_item<SL>(P, S, PV, BV, W, cdone + lane, row0, kstart, sl, n, xs, bs);
+                contact_item<SL, FAST>(P, S, PV, BV, W, cdone + lane, row0, kstart, sl, n, xs, bs);
                 cdone += 32;
                 __syncwarp();
             }
@@ -258,7 +264,7 @@ __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
         const int64_t kend = k;
         if (cdone < ccount) {
             if (cdone + lane < ccount)
-                contact_item<SL>(P, S, PV, BV, W, cdone + lane, row0, kstart, sl, n, xs, bs);
+                contact_item<SL, FAST>(P, S, PV, BV, W, cdone + lane, row0, kstart, sl, n, xs, bs);
             cdone = ccount;
         }
         __syncwarp();
@@ -284,7 +290,7 @@ __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
             }
             __syncwarp();
             for (int q = lane; q < hcount; q += 32)
-                hamaker_item<SL>(P, S, W, q);
+                hamaker_item<SL, FAST>(P, S, W, q);
             __syncwarp();
 #pragma unroll
             for (int t = 0; t < kWin; ++t) {
@@ -333,7 +339,7 @@ __global__ void __launch_bounds__(Shape<SL>::kWarps * 32)
     compact::finish_row(P, S, i, n, acc, accw, vi, wi, hdt);
 }
 
-template <bool VERLET, int SL>
+template <bool VERLET, int SL, bool FAST>
 static void launch_compact(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                            double dt, int move_facets, cudaStream_t st) {
     using Sh = Shape<SL>;
@@ -343,7 +349,7 @@ static void launch_compact(const Params &P, const StateView &S, const PairView &
     static thread_local int attr_device = -1;  // the attribute is per device; set once per thread and device
     int dev = 0;
     cudaGetDevice(&dev);
-    auto kern = forces_compact_fp64<VERLET, SL>;
+    auto kern = forces_compact_fp64<VERLET, SL, FAST>;
     if (attr_device != dev) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr_device = dev;
@@ -352,11 +358,15 @@ static void launch_compact(const Params &P, const StateView &S, const PairView &
 }
 
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
-                                double dt, int move_facets, cudaStream_t st) {
-    if (P.pairs == LG_PAIRS_VERLET)
-        launch_compact<true, 1>(P, S, PV, BV, hdt, dt, move_facets, st);
-    else
-        launch_compact<false, 1>(P, S, PV, BV, hdt, dt, move_facets, st);
+                                double dt, int move_facets, cudaStream_t st, bool fast) {
+    const bool ver = P.pairs == LG_PAIRS_VERLET;
+    if (fast) {
+        if (ver) launch_compact<true, 1, true>(P, S, PV, BV, hdt, dt, move_facets, st);
+        else launch_compact<false, 1, true>(P, S, PV, BV, hdt, dt, move_facets, st);
+    } else {
+        if (ver) launch_compact<true, 1, false>(P, S, PV, BV, hdt, dt, move_facets, st);
+        else launch_compact<false, 1, false>(P, S, PV, BV, hdt, dt, move_facets, st);
+    }
 }
 
 }  // namespace lg

@@ -150,8 +150,9 @@ int launch_step_mixed(const Params &P, const StateView &S, const PairView &PV, c
                       const MixedExtra &MX, const StepArgs &A, cudaStream_t st);
 
 // Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
+// fast: LG_FORCE_KERNEL_FP64_FAST (reciprocals instead of repeated divisions; within 1e-12).
 void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
-                                double dt, int move_facets, cudaStream_t st);
+                                double dt, int move_facets, cudaStream_t st, bool fast = false);
 // Mixed precision: the contact/bond kernel (if the system has a binary model) on `side`, beside the
 // Hamaker kernel on `st` (fork / join through the two events), then the completion kernel on `st`;
 // returns the number of kernels launched.

@@ -57,7 +57,9 @@ def test_create_rejects_bad_descriptors_before_touching_a_gpu():
         K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), precision=A.LG_PRECISION_MIXED,
                     force_kernel=A.LG_FORCE_KERNEL_PAIRS),
         K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), force_kernel=A.LG_FORCE_KERNEL_PERSISTENT),
-        K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), force_kernel=5),
+        K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), precision=A.LG_PRECISION_MIXED,
+                    force_kernel=A.LG_FORCE_KERNEL_FP64_FAST),
+        K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact(), force_kernel=6),
     ]
     d = K.make_desc(4, A.LG_BINARY_CONTACT, contact=mat.contact())
     K.set_hold(d, np.array([0, 16, 0, 0], dtype=np.uint8))  # unknown bit

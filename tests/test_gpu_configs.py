@@ -42,17 +42,17 @@ def _bit_equal(s, o, where):
         assert np.array_equal(a, b), "%s: %s differs (rel %g)" % (where, H.FIELD_NAMES[f], H.rel_err(a, b))
 
 
-def _rowgroup_forces_at_identical_state(s, o, dt, rebuild, lanes):
+def _rowgroup_forces_at_identical_state(s, o, dt, rebuild, lanes, kernel=A.LG_FORCE_KERNEL_ROWGROUP):
     """s and o hold bit-identical states (positions, velocities, springs). For each lane count, one
-    step of s with the T-lane row-group kernel is compared with one step of o; s is then restored
-    and stepped with its own kernel, which brings it level with o again."""
+    step of s with the T-lane row-group kernel (or another kernel) is compared with one step of o; s
+    is then restored and stepped with its own kernel, which brings it level with o again."""
     kernel0 = s.desc.force_kernel
     T0 = max(int(s.desc.threads_per_row), 1)
     o_next = None
     worst = 0.0
     for T in lanes:
         s.snapshot()
-        s.set_force_kernel(A.LG_FORCE_KERNEL_ROWGROUP)
+        s.set_force_kernel(kernel)
         s.set_threads_per_row(T)
         s.step(dt, 1, rebuild)
         if o_next is None:
@@ -104,6 +104,9 @@ def test_c0_exact_configuration_ten_thousand_steps():
     for cp in (10000, 10001):  # identical states at the end of the run (the helper steps both by one)
         _rowgroup_forces_at_identical_state(s, o, mat.dt, 0, (4, 32))
         _bit_equal(s, o, "after the row-group check at step %d" % (cp + 1))
+    # the fast FP64 kernel (reciprocals, one Hamaker denominator) at the same identical states
+    assert _rowgroup_forces_at_identical_state(s, o, mat.dt, 0, (1,), kernel=A.LG_FORCE_KERNEL_FP64_FAST) <= FORCE_TOL
+    _bit_equal(s, o, "after the fast-kernel check")
     for s in systems.values():
         assert np.array_equal(s.bonds(), o.bonds())
         assert s.device_errors() == 0
@@ -133,6 +136,9 @@ def test_c1_fp64_32768_against_oracle():
     assert o.observables()["n_contacts"] > 1000  # contacts formed and are carried
     worst = _rowgroup_forces_at_identical_state(s, o, mat.dt, 20, (4, 32))
     _bit_equal(s, o, "after the row-group check")
+    assert worst <= FORCE_TOL
+    worst = _rowgroup_forces_at_identical_state(s, o, mat.dt, 20, (1,), kernel=A.LG_FORCE_KERNEL_FP64_FAST)
+    _bit_equal(s, o, "after the fast-kernel check")
     assert worst <= FORCE_TOL
     # springs of contacting pairs agree after the rebuilds
     checked = 0
@@ -204,3 +210,31 @@ def test_c3_batch_at_the_clip_sizes_matches_oracle():
                            precision=prec, n_facets=1, facet_auto_move=1, force_kernel=A.LG_FORCE_KERNEL_COMPACT)
     _batch_against_oracle([4096, 128, 1000, 4096, 130], 3, desc_of, 200, facets=[wall],
                           neck_of=lambda nb: np.full(nb, 1e-8), prep=K.rest_on_wall)
+
+
+@pytest.mark.parametrize("case", ["c0", "c1"])
+def test_fast_fp64_kernel_follows_the_oracle(case):
+    """LG_FORCE_KERNEL_FP64_FAST on its own for 100 steps: forces within 1e-12 of the oracle's at the
+    start (identical state), positions within 1e-9 after 100 steps (2 and 5 list rebuilds)."""
+    mat = K.Material()
+    if case == "c0":
+        n, seed = 256, 0
+        d = K.make_desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_FULL, contact=mat.contact(), sinter=mat.sinter(),
+                        hamaker=mat.hamaker(), pairs=A.LG_PAIRS_ALL, force_kernel=A.LG_FORCE_KERNEL_FP64_FAST)
+        rb = 0
+    else:
+        n, seed = 32768, 1 << 32
+        d = K.make_desc(n, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, contact=mat.contact(), hamaker=mat.hamaker(),
+                        pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r, max_neighbors=96,
+                        force_kernel=A.LG_FORCE_KERNEL_FP64_FAST)
+        rb = 20
+    x0, v0 = generate_aggregate(seed, n, mat.r), generate_velocities(seed, n, 0.1)
+    s = System(d, x0, v0)
+    o = O.OracleSystem(d, x0, v0, threads=THREADS)
+    for f in (A.LG_FIELD_A, A.LG_FIELD_ALPHA):
+        assert H.rel_err(s.get(f), o.get(f)) <= FORCE_TOL, H.FIELD_NAMES[f]
+    s.step(mat.dt, 100, rb)
+    o.step(mat.dt, 100, rb)
+    assert H.rel_err(s.get(A.LG_FIELD_X), o.get(A.LG_FIELD_X)) <= POS_TOL
+    assert H.rel_err(s.get(A.LG_FIELD_X) - x0, o.get(A.LG_FIELD_X) - x0) <= POS_TOL
+    assert s.device_errors() == 0
