@@ -212,8 +212,9 @@ typedef struct lg_system_desc {
                                        the compacted kernels. Other steps use the compacted kernels. */
 #define LG_FORCE_KERNEL_FP64_FAST 5  /* FP64: the compacted kernel with one reciprocal where libgran divides a
                                        vector by a scalar, and the Hamaker bracket over one common
-                                       denominator (2 divisions per Hamaker pair instead of 12); contact is
-                                       decided by the reference's exact overlap. Per-step forces within
+                                       denominator (2 divisions per Hamaker pair instead of 12, 2 per
+                                       contact scaling instead of 6); contact is decided by the reference's
+                                       exact overlap. Per-step forces within
                                        1e-12 of the reference's, not bit-identical; chosen explicitly only
                                        (never by AUTO or the autotuner). */
 

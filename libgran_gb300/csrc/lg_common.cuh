@@ -212,10 +212,12 @@ struct StateView {
 // FP64 functors
 // ------------------------------------------------------------------------------------------------
 // FAST = true: where libgran divides a vector by a scalar (normalisation, division by a mass or an
-// inertia) the vector is multiplied by one reciprocal, and the Hamaker bracket is evaluated over one
-// common denominator; every value stays within a few ulp of the reference's (per-step forces within
+// inertia) the vector is multiplied by one reciprocal; every value stays within a few ulp of the
+// reference's (per-step forces within
 // 1e-12 of it), but not bit-identical. FAST = false is the reference's arithmetic, operation for
-// operation.
+// operation. Normals whose overlap 2r - dx.n is a small difference of large numbers (contact, bond)
+// keep the reference's division in both forms: with a reciprocal there, a bonded aggregate's forces
+// moved by 2.2e-12 of their largest value.
 template <bool FAST>
 __device__ __forceinline__ d3 dvs_t(d3 a, double s) {
     if (FAST) {
@@ -317,7 +319,9 @@ __device__ __forceinline__ void contact_touching(const lg_contact_params &p, d3 
 template <bool FAST = false>
 __device__ __forceinline__ bool bond_force(const lg_sinter_params &p, d3 dx, d3 vi, d3 vj, d3 wi, d3 wj, d3 *s,
                                            bool breaking, double strength, d3 &oa, d3 &oal) {
-    d3 n = nrmz_t<FAST>(dx);
+    // the normal keeps the reference's division even in FAST: the overlap 2r - dx.n of a bonded pair
+    // is a small difference of large numbers, so an ulp of n is a large part of it
+    d3 n = nrmz(dx);
     double overlap = 2.0 * p.r_part - dot(dx, n);
     double rp = p.r_part - overlap / 2.0;
     double v_n = -dot(sub(vi, vj), n);
@@ -397,18 +401,13 @@ __device__ __forceinline__ d3 hamaker_accel_n(int mode, const lg_hamaker_params 
     if (h < p.h0) h = p.h0;
     double rp = p.r_part;
     double s;
-    if (FAST) {
-        if (mode == LG_HAMAKER_SIMPLIFIED) {
-            s = 2.0 * p.A * rp / sq_(h);
-        } else {
-            const double q = 4.0 * rp + h, w0 = 2.0 * rp + h, a = 4.0 * rp + 2.0 * h;
-            const double inv = 1.0 / (q * h * w0);
-            const double u = w0 * inv, w = q * h * inv;
-            const double br = a * u - 2.0 * w - 4.0 * sq_(rp) * (w * w * w) - 2.0 * sq_(rp) * a * (u * u);
-            s = -p.A / 6.0 * br;
-        }
-        if (!(rn > 0.0)) return dvs_t<true>(scl(s, r), p.mass);
-        return scl(s / (rn * p.mass), r);
+    if (FAST && mode != LG_HAMAKER_SIMPLIFIED) {
+        const double q = 4.0 * rp + h, w0 = 2.0 * rp + h, a = 4.0 * rp + 2.0 * h;
+        const double inv = 1.0 / (q * h * w0);
+        const double u = w0 * inv, w = q * h * inv;
+        const double br = a * u - 2.0 * w - 4.0 * sq_(rp) * (w * w * w) - 2.0 * sq_(rp) * a * (u * u);
+        s = -p.A / 6.0 * br;
+        return rn > 0.0 ? scl(s / (rn * p.mass), r) : dvs_t<true>(scl(s, r), p.mass);
     }
     if (mode == LG_HAMAKER_SIMPLIFIED) {
         s = 2.0 * p.A * rp / sq_(h);
@@ -417,6 +416,7 @@ __device__ __forceinline__ d3 hamaker_accel_n(int mode, const lg_hamaker_params 
                     2.0 * sq_(rp) * (4.0 * rp + 2.0 * h) / sq_(4.0 * rp + h) / sq_(h);
         s = -p.A / 6.0 * br;
     }
+    if (FAST) return rn > 0.0 ? scl(s / (rn * p.mass), r) : dvs_t<true>(scl(s, r), p.mass);
     d3 u = (rn > 0.0) ? dvs(r, rn) : r;  // nrmz(r)
     return dvs(scl(s, u), p.mass);
 }

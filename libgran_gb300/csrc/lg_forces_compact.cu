@@ -2,8 +2,8 @@
 // Two instances: the reference's arithmetic operation for operation (bit-identical to the sequential
 // evaluation), and FAST (LG_FORCE_KERNEL_FP64_FAST), which multiplies by one reciprocal where libgran
 // divides a vector by a scalar and evaluates the Hamaker bracket over one common denominator
-// (per-step forces within 1e-12 of the reference's); both decide contact with the reference's exact
-// overlap.
+// (per-step forces within 1e-12 of the reference's); both decide
+// contact with the reference's exact overlap.
 //
 // On GB300 a warp instruction on the FP64 pipe costs the same issue time whether 1 or 32 lanes are
 // active, so a kernel whose lanes each walk their own row and branch on "is this pair in Hamaker
