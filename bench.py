@@ -322,6 +322,46 @@ def time_path(precision, x0, v0, args, l2_flush, tune=False, kernel=None):
                     "pair_stats": stats, "device_errors": errs, "tuning": tuning}
 
 
+def c0_section(steps=10000):
+    """Config 0 as configured: 256 monomers (seed 0), sintered bonds + contact + full Hamaker, all
+    pairs, velocities +-0.1 m/s, 10^4 velocity-Verlet steps -- on the GPU in FP64 (the automatic
+    choice: pair-parallel kernel, bit-identical to the oracle) and in mixed precision, and on the
+    host cores with the oracle (the full run). Reports particle-steps/s of each and whether the FP64
+    end state equals the oracle's bit for bit."""
+    from libgran_gb300 import _abi as A
+    from libgran_gb300 import configs as K
+    from libgran_gb300.system import System
+    from oracle import oracle as O
+    mat = K.Material()
+    n = 256
+    x0, v0 = O.generate_aggregate(0, n, mat.r), O.generate_velocities(0, n, 0.1)
+    out = {"n_part": n, "vv_steps": steps}
+    xs = {}
+    for name, prec in (("fp64", A.LG_PRECISION_FP64), ("mixed", A.LG_PRECISION_MIXED)):
+        d = K.make_desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_FULL, contact=mat.contact(), sinter=mat.sinter(),
+                        hamaker=mat.hamaker(), precision=prec)
+        s = System(d, x0, v0)
+        s.step(mat.dt, 100)  # graphs captured
+        s2 = System(d, x0, v0)
+        ms = s2.step_timed(mat.dt, steps)
+        xs[name] = s2.get(A.LG_FIELD_X)
+        out[name] = {"particle_steps_per_s": n * steps / (ms / 1e3), "us_per_step": 1e3 * ms / steps}
+        s.close()
+        s2.close()
+    d = K.make_desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_FULL, contact=mat.contact(), sinter=mat.sinter(),
+                    hamaker=mat.hamaker())
+    threads = os.cpu_count() or 1
+    o = O.OracleSystem(d, x0, v0, threads=threads)
+    t = time.perf_counter()
+    o.step(mat.dt, steps)
+    el = time.perf_counter() - t
+    out["cpu_oracle"] = {"particle_steps_per_s": n * steps / el, "cores": threads, "s": el}
+    out["fp64_end_state_equals_oracle"] = bool(np.array_equal(xs["fp64"], o.get(A.LG_FIELD_X)))
+    xo = o.get(A.LG_FIELD_X)
+    out["mixed_end_position_rel_diff"] = float(np.abs(xs["mixed"] - xo).max() / np.abs(xo - x0).max())
+    return out
+
+
 def kernel_name(t):
     from libgran_gb300 import _abi as A
     if t and t["force_kernel"] == A.LG_FORCE_KERNEL_PERSISTENT:
@@ -495,6 +535,7 @@ def run_gb300(args, rank, world):
     peak = peaks.get("hbm_gbs", 6800.0)
     traffic = read_profile_traffic("forces_mixed_c1")
     cpu = cpu_reference_rate(x0, v0, target_s=float(os.environ.get("LG_CPU_SAMPLE_S", "12")))
+    c0 = c0_section() if os.environ.get("LG_BENCH_C0", "1") != "0" else None
     batched = None
     if os.environ.get("LG_BENCH_BATCHED", "1") != "0":
         batched = batched_section(args, l2_flush)
@@ -535,6 +576,7 @@ def run_gb300(args, rank, world):
         "cpu_baseline": cpu,
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
         "device_errors": tm["device_errors"],
+        "c0": c0,
         "batched": batched,
         "restructuring": restruct,
         "serving": serving,
@@ -705,8 +747,11 @@ def run_profile(args):
     x0, v0 = workload_state()
     mat, d = workload_desc(prec)
     if args.kernel is not None:
-        d.force_kernel = {"compact": A.LG_FORCE_KERNEL_COMPACT, "persistent": A.LG_FORCE_KERNEL_PERSISTENT}[args.kernel]
+        d.force_kernel = {"compact": A.LG_FORCE_KERNEL_COMPACT, "persistent": A.LG_FORCE_KERNEL_PERSISTENT,
+                          "fp64fast": A.LG_FORCE_KERNEL_FP64_FAST}[args.kernel]
     s = System(d, x0, v0)
+    if args.shape:
+        s.set_step_shape(*[int(v) for v in args.shape.split(",")])
     s.step(mat.dt, VV_PER_STEP * (args.warmup + args.steps), VV_PER_STEP)
     print(json.dumps({"profile": args.profile, "vv_steps": VV_PER_STEP * (args.warmup + args.steps),
                       "device_errors": s.device_errors(), "launches": s.launch_count()}))
@@ -716,8 +761,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile", default=None, choices=[None, "mixed", "fp64"],
                     help="profiling driver: run one path without timing")
-    ap.add_argument("--kernel", default=None, choices=[None, "compact", "persistent"],
-                    help="profiling driver: force kernel of the mixed path")
+    ap.add_argument("--kernel", default=None, choices=[None, "compact", "persistent", "fp64fast"],
+                    help="profiling driver: force kernel (compact / persistent: mixed; fp64fast: FP64)")
+    ap.add_argument("--shape", default=None,
+                    help="profiling driver, persistent kernel: min_blocks,slices,assign")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
