@@ -155,8 +155,10 @@ def _declare(L):
         "lg_reset_acceleration_buffers": (C.c_int, [vp]),
         "lg_get_observables": (C.c_int, [vp, P(lg_observables)]),
         "lg_get_observables_select": (C.c_int, [vp, C.c_int32, P(lg_observables)]),
-        "lg_get_state": (C.c_int, [vp, P(d), P(d), P(d), P(d)]),
-        "lg_set_state": (C.c_int, [vp, P(d), P(d), P(d), P(d)]),
+        # plain addresses: the state calls sit on the per-exchange path, where building four
+        # ctypes pointer objects costs more than the transfer's own host work
+        "lg_get_state": (C.c_int, [vp, vp, vp, vp, vp]),
+        "lg_set_state": (C.c_int, [vp, vp, vp, vp, vp]),
         "lg_get_device_errors": (C.c_int, [vp, P(i32)]),
         "lg_get_bonds": (C.c_int, [vp, P(i64), P(i64), i64]),
         "lg_get_pair_springs": (C.c_int, [vp, i64, i64, P(d)]),

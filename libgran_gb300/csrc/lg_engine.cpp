@@ -1368,6 +1368,14 @@ static const void *mapped_host(const void *p) {
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+// 16-byte accesses for a transfer whose buffers all start on a 16-byte boundary.
+static int32_t io_wide(const StateIO &io) {
+    for (int f = 0; f < 4; ++f) {
+        if ((reinterpret_cast<uintptr_t>(io.in[f]) | reinterpret_cast<uintptr_t>(io.out[f])) & 15u) return 0;
+    }
+    return 1;
+}
+
 // State upload of any of x, v, theta, omega (host [n][3] arrays, null: unchanged) in one kernel,
 // which also refreshes the mixed path's float-float copies. The origins (and the CUDA graphs that
 // hold them) are kept while every position stays within four times its system's extent from its
@@ -1387,16 +1395,29 @@ static int state_upload(lg_system *s, const double *const host[4]) {
             io.in[f] = s->obs_scratch + 3 * n * f;
         }
     }
+    io.wide = io_wide(io);
     const bool refresh = s->x32 && (host[0] || host[1] || host[3]);
-    int32_t *flag = refresh && host[0] ? s->d_flag : nullptr;
-    if (flag) LG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int32_t), s->stream));
+    // the coverage flag: written by the kernel straight into the handle's pinned word when that word
+    // is mapped, else a device word copied back
+    volatile int32_t *hflag = reinterpret_cast<volatile int32_t *>(s->h_pin + 63);
+    int32_t *flag = nullptr;
+    const bool want_flag = refresh && host[0];
+    if (want_flag) {
+        *hflag = 0;
+        flag = s->pooled ? nullptr : (int32_t *)mapped_host((const void *)hflag);
+        if (!flag) {
+            flag = s->d_flag;
+            LG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int32_t), s->stream));
+        }
+    }
     launch_state_in(n, io, s->x, s->v[s->vcur], s->th, s->w[s->vcur], refresh ? s->x32 : nullptr, s->v32, s->s32,
                     s->origin, s->d_agg, s->d_orig, flag, s->stream);
     s->launches += 1;
     LG_CUDA(cudaGetLastError());
-    if (flag) LG_CUDA(cudaMemcpyAsync(s->h_pin, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+    if (flag && flag == s->d_flag)
+        LG_CUDA(cudaMemcpyAsync((void *)hflag, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
     LG_CUDA(cudaStreamSynchronize(s->stream));  // the caller may reuse its buffers on return
-    if (flag && *reinterpret_cast<int32_t *>(s->h_pin)) {
+    if (want_flag && *hflag) {
         LG_TRY(set_mixed_origins(s, host[0]));  // positions moved far: new origins and culling radii
         set_cull_radii(s);
         s->drop_graphs();
@@ -1422,6 +1443,7 @@ static int state_download(lg_system *s, double *const host[4]) {
         staged[f] = m == nullptr;
         io.out[f] = staged[f] ? s->obs_scratch + 3 * n * f : (double *)m;
     }
+    io.wide = io_wide(io);
     launch_state_out(n, io, s->x, s->v[s->vcur], s->th, s->w[s->vcur], s->stream);
     s->launches += 1;
     LG_CUDA(cudaGetLastError());
@@ -2109,6 +2131,7 @@ int lg_arena_read(lg_system *A, int64_t q, int64_t n, double *x, double *v, doub
     double *host[4] = {x, v, th, w};
     StateIO io{};
     for (int f = 0; f < 4; ++f) io.out[f] = host[f] ? A->obs_scratch + 3 * n * f : nullptr;
+    io.wide = io_wide(io);
     launch_state_out(n, io, A->x + off, A->v[A->vcur] + off, A->th + off, A->w[A->vcur] + off, A->stream);
     A->launches += 1;
     LG_CUDA(cudaGetLastError());

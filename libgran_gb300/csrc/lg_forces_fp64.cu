@@ -511,14 +511,17 @@ __global__ void cell_scatter(int64_t n, const int32_t *__restrict__ cell_of, con
 }
 
 constexpr int kBuildRows = 32;   // rows per block
-constexpr int kBuildWarps = 8;   // warps per block; warp w builds rows w, w + 8, ...
+constexpr int kBuildWarps = 16;  // warps per block; warp w builds rows w, w + 16
+constexpr int kBuildBatches = 3; // candidate batches of 32 whose loads are in flight together
 
 // Shared-memory layout of build_rows for row capacity cap and bond capacity bcap: four 32-row
 // tiles (partner, flags, old slot, near partner) with an odd row stride, then per warp the unsorted
-// candidates, the old row and the row's bond partners, then the near-slot tile (bytes).
+// candidates, the old row, the old row's flags and the row's bond partners, then the near-slot tile
+// (bytes).
 __host__ __device__ inline int64_t build_tile_stride(int64_t cap) { return cap | 1; }
+__host__ __device__ inline int64_t build_warp_ints(int64_t cap, int64_t bcap) { return 3 * cap + bcap; }
 __host__ __device__ inline size_t build_smem_bytes(int64_t cap, int64_t bcap) {
-    return sizeof(int32_t) * (size_t)(4 * kBuildRows * build_tile_stride(cap) + kBuildWarps * (2 * cap + bcap)) +
+    return sizeof(int32_t) * (size_t)(4 * kBuildRows * build_tile_stride(cap) + kBuildWarps * build_warp_ints(cap, bcap)) +
            (size_t)(kBuildRows * build_tile_stride(cap));
 }
 
@@ -526,11 +529,14 @@ __host__ __device__ inline size_t build_smem_bytes(int64_t cap, int64_t bcap) {
 // test; an FP32 filter accepts or rejects the clear cases), ascending j, carrying the springs (and
 // live flag) of pairs that were already listed, and marking intact bonds.
 // One warp per row: the 27 neighbour cells are 9 runs of consecutive cells (x fastest), i.e. 9
-// contiguous ranges of the cell-sorted particle list, walked as one list; the lanes test 32
-// candidates at a time and append the accepted ones in scan order (ballot + popc). The row is ordered by a rank sort (j is
-// unique), the old row is searched by bisection for spring carry-over, and the finished rows of the
-// block are written slot-major so that the 32 rows' slot k go out as one coalesced store.
-__global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
+// contiguous ranges of the cell-sorted particle list, walked as one list; the lanes take
+// kBuildBatches x 32 candidates at a time (all their index and position loads issued before the
+// first test, so that one round trip serves them all) and append the accepted ones (ballot + popc). The old row (partners and flags) and the row's bonds are requested before the candidate
+// loop, so their round trip overlaps it. The row is ordered by a rank sort (j is unique), so the
+// append order does not matter; the old row is searched by bisection for spring carry-over, and the
+// finished rows of the block are written slot-major so that the 32 rows' slot k go out as one
+// coalesced store.
+__global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
     int64_t n, const dbl4 *__restrict__ x, BatchView B, const float4 *__restrict__ x32, const GridDev *__restrict__ g,
     const int32_t *__restrict__ cstart, const int32_t *__restrict__ ccount, const int32_t *__restrict__ sorted,
     const int32_t *__restrict__ cell_of, double rv2, PairView oldv, PairView newv, BondView BV, int32_t *err,
@@ -545,10 +551,11 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
     uint32_t *tf = reinterpret_cast<uint32_t *>(tj + kBuildRows * ts);
     int32_t *tp = reinterpret_cast<int32_t *>(tf + kBuildRows * ts);
     int32_t *tnj = tp + kBuildRows * ts;
-    int32_t *wraw = tnj + kBuildRows * ts + (int64_t)warp * (2 * cap + bcap);
+    int32_t *wraw = tnj + kBuildRows * ts + (int64_t)warp * build_warp_ints(cap, bcap);
     int32_t *wold = wraw + cap;
-    int32_t *wbond = wold + cap;
-    uint8_t *tnk = reinterpret_cast<uint8_t *>(tnj + kBuildRows * ts + kBuildWarps * (2 * cap + bcap));
+    uint32_t *wofl = reinterpret_cast<uint32_t *>(wold + cap);
+    int32_t *wbond = reinterpret_cast<int32_t *>(wofl + cap);
+    uint8_t *tnk = reinterpret_cast<uint8_t *>(tnj + kBuildRows * ts + kBuildWarps * build_warp_ints(cap, bcap));
     __shared__ int32_t rnear[kBuildRows];
     const bool near_lists = newv.near_len != nullptr;
     const float rn2 = g->rn2_hi;
@@ -561,6 +568,22 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
         if (i >= n || inactive_of(B.hold, i)) {  // an inactive particle's row is empty
             if (lane == 0) rlen[r] = rnear[r] = 0;
             continue;
+        }
+        // requested now, used after the candidate loop: the first 32 slots of the old row (partner
+        // and flags; every slot below the capacity is allocated, so the loads need not wait for the
+        // old length) and the first 32 bond slots
+        const bool have_old = oldv.row_len != nullptr;
+        const int32_t olen_raw = have_old ? oldv.row_len[i] : 0;
+        int32_t onb0 = -1, bj0 = -1;
+        uint32_t ofl0 = 0;
+        uint8_t bok0 = 0;
+        if (have_old && lane < oldv.cap) {
+            onb0 = oldv.nbr[(int64_t)lane * n + i];
+            ofl0 = oldv.flags[(int64_t)lane * n + i];
+        }
+        if (lane < bcap) {
+            bj0 = BV.j[(int64_t)lane * n + i];
+            bok0 = BV.intact[(int64_t)lane * n + i];
         }
         const float4 fi = x32[i];
         const dbl4 xd = x[i];
@@ -605,40 +628,68 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
             return sorted[q];
         };
         int32_t cnt = 0;
-        int32_t jnext = lane < total ? fetch(lane) : -1;
-        for (int32_t t0 = 0; t0 < total; t0 += 32) {
-            const int32_t j = jnext;
-            jnext = t0 + 32 + lane < total ? fetch(t0 + 32 + lane) : -1;
-            bool in = false;
-            if (j >= 0 && j != (int32_t)i && (!B.agg || B.agg[j] == ai)) {  // pairs never cross systems
-                const float4 fj = x32[j];
-                const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
-                const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                if (d2f < rlo)
-                    in = true;
-                else if (!(d2f > rhi))
-                    in = sqn(sub(xi_, ld4(x, j))) < rv2;
+        for (int32_t t0 = 0; t0 < total; t0 += 32 * kBuildBatches) {
+            int32_t jb[kBuildBatches];
+            float4 fb[kBuildBatches];
+            bool same[kBuildBatches];
+#pragma unroll
+            for (int u = 0; u < kBuildBatches; ++u) {
+                const int32_t t = t0 + 32 * u + lane;
+                jb[u] = t < total ? fetch(t) : -1;
             }
-            const uint32_t bal = __ballot_sync(0xffffffffu, in);
-            if (in) {
-                const int32_t pos = cnt + __popc(bal & lt);
-                if (pos < cap) wraw[pos] = j;
+#pragma unroll
+            for (int u = 0; u < kBuildBatches; ++u) {
+                fb[u] = fi;
+                same[u] = true;
+                if (jb[u] >= 0) {
+                    fb[u] = x32[jb[u]];
+                    if (B.agg) same[u] = B.agg[jb[u]] == ai;  // pairs never cross systems
+                }
             }
-            cnt += __popc(bal);
+#pragma unroll
+            for (int u = 0; u < kBuildBatches; ++u) {
+                const int32_t j = jb[u];
+                bool in = false;
+                if (j >= 0 && j != (int32_t)i && same[u]) {
+                    const float ex = fi.x - fb[u].x, ey = fi.y - fb[u].y, ez = fi.z - fb[u].z;
+                    const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                    if (d2f < rlo)
+                        in = true;
+                    else if (!(d2f > rhi))
+                        in = sqn(sub(xi_, ld4(x, j))) < rv2;
+                }
+                const uint32_t bal = __ballot_sync(0xffffffffu, in);
+                if (in) {
+                    const int32_t pos = cnt + __popc(bal & lt);
+                    if (pos < cap) wraw[pos] = j;
+                }
+                cnt += __popc(bal);
+            }
         }
         if (lane == 0) atomicMax(max_row, cnt);
         if (cnt > cap) {
             if (lane == 0) set_error(err, LG_DEVERR_LIST_OVERFLOW);
             cnt = (int32_t)cap;
         }
-        int32_t olen = oldv.row_len ? oldv.row_len[i] : 0;
+        int32_t olen = olen_raw;
         if (olen > oldv.cap) olen = (int32_t)oldv.cap;  // both buffers share one capacity
-        for (int32_t p = lane; p < olen; p += 32) wold[p] = oldv.nbr[(int64_t)p * n + i];
+        if (lane < olen) {
+            wold[lane] = onb0;
+            wofl[lane] = ofl0;
+        }
+        for (int32_t p = lane + 32; p < olen; p += 32) {
+            wold[p] = oldv.nbr[(int64_t)p * n + i];
+            wofl[p] = oldv.flags[(int64_t)p * n + i];
+        }
         int32_t intact = 0;
         for (int b = lane; b < bcap; b += 32) {
-            const int64_t be = (int64_t)b * n + i;
-            const int32_t bj = BV.j[be];
-            const bool ok = bj >= 0 && BV.intact[be];
+            int32_t bj = bj0;
+            bool ok = bj0 >= 0 && bok0;
+            if (b >= 32) {
+                const int64_t be = (int64_t)b * n + i;
+                bj = BV.j[be];
+                ok = bj >= 0 && BV.intact[be];
+            }
             wbond[b] = ok ? bj : -1;
             intact += ok ? 1 : 0;
         }
@@ -666,7 +717,7 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps) build_rows(
             }
             uint32_t fl = 0;
             int32_t po = -1;
-            if (slot_ok && lo < olen && wold[lo] == j && (oldv.flags[(int64_t)lo * n + i] & kXiLive)) {
+            if (slot_ok && lo < olen && wold[lo] == j && (wofl[lo] & kXiLive)) {
                 fl |= kXiLive;
                 po = lo;
             }

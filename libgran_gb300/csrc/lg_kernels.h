@@ -171,6 +171,7 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
 struct StateIO {
     const double *in[4];
     double *out[4];
+    int32_t wide;  // every non-null in / out pointer is 16-byte aligned: 16-byte accesses
 };
 void launch_state_in(int64_t n, const StateIO &io, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, float4 *x32, float4 *v32,
                      float4 *s32, const double *origin, const int32_t *agg, const dbl4 *orig, int32_t *uncovered,

@@ -145,18 +145,38 @@ int64_t obs_scratch_doubles(int64_t n) { return n * kObs; }
 constexpr int kObsBlock = 256;
 constexpr int kObsCols = 16;  // 15 terms + |x - c|^2
 
-// Block sums of C columns in a fixed order: a butterfly over the warp's lanes, then the kObsBlock /
-// 32 warp sums in warp order by thread c < C; the result row goes to part[blockIdx.x].
+// Block sums of C columns in a fixed order; the result row goes to part[blockIdx.x]. FP64 issues
+// slowly on this GPU (a warp instruction occupies the SM's FP64 pipe for many cycles), so the warp
+// level counts instructions: for C > 2 the warp's C x 32 terms are transposed through shared memory
+// and lanes c and 16 + c add the halves of column c in lane order (16 instructions per warp instead of
+// a 5-step butterfly per column); for C <= 2, a butterfly. Then thread c < C adds the kObsBlock / 32
+// warp sums in warp order.
 template <int C>
 __device__ __forceinline__ void obs_block_row(double (&t)[C], double *__restrict__ part) {
     __shared__ double ws[kObsBlock / 32][C];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if constexpr (C <= 2) {
 #pragma unroll
-    for (int c = 0; c < C; ++c) {
-        double v = t[c];
+        for (int c = 0; c < C; ++c) {
+            double v = t[c];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) ws[warp][c] = v;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) ws[warp][c] = v;
+        }
+    } else {
+        static_assert(C <= 16, "two lanes per column");
+        __shared__ double tr[kObsBlock / 32][C][33];
+#pragma unroll
+        for (int c = 0; c < C; ++c) tr[warp][c][lane] = t[c];
+        __syncwarp();
+        const int c = lane & 15, h = lane >> 4;
+        double r = 0.0;
+        if (c < C) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) r += tr[warp][c][16 * h + q];
+        }
+        const double r2 = __shfl_down_sync(0xffffffffu, r, 16);
+        if (lane < C) ws[warp][lane] = r + r2;
     }
     __syncthreads();
     if ((int)threadIdx.x < C) {
@@ -173,7 +193,8 @@ __device__ __forceinline__ void obs_block_row(double (&t)[C], double *__restrict
 // dependent FP64 add takes tens of cycles on this GPU). Returns without waiting on any block.
 template <int C>
 __device__ __forceinline__ void obs_last_block_combine(int nb, const double *__restrict__ part, int c0, int out0,
-                                                       double *__restrict__ out, unsigned *ticket) {
+                                                       double *__restrict__ out, unsigned *ticket,
+                                                       int64_t centre_n = 0) {
     static_assert(16 * C <= kObsBlock, "one thread per (column, group)");
     __shared__ bool last;
     __shared__ double pg[16][C];
@@ -195,6 +216,9 @@ __device__ __forceinline__ void obs_last_block_combine(int nb, const double *__r
 #pragma unroll
         for (int q = 0; q < 16; ++q) acc += pg[q][threadIdx.x];
         out[out0 + threadIdx.x] = acc;
+        // with centre_n: the centre of mass (columns 12..14 over n) once, to out[20..22]
+        const int col = out0 + (int)threadIdx.x;
+        if (centre_n > 0 && col >= 12 && col < 15) out[20 + col - 12] = acc / (double)centre_n;
     }
     if (threadIdx.x == 0) *ticket = 0u;
 }
@@ -220,7 +244,7 @@ __global__ void __launch_bounds__(kObsBlock) obs_state_terms(int64_t n, const db
         t[12] = xi.x; t[13] = xi.y; t[14] = xi.z;
     }
     obs_block_row<15>(t, part);
-    obs_last_block_combine<15>((int)gridDim.x, part, 0, 0, out, ticket);
+    obs_last_block_combine<15>((int)gridDim.x, part, 0, 0, out, ticket, n);
 }
 
 __global__ void __launch_bounds__(kObsBlock) obs_state_rg(int64_t n, const dbl4 *__restrict__ x,
@@ -229,16 +253,16 @@ __global__ void __launch_bounds__(kObsBlock) obs_state_rg(int64_t n, const dbl4 
     const int64_t i = blockIdx.x * (int64_t)kObsBlock + threadIdx.x;
     double t[1] = {0.0};
     if (i < n) {
-        const double nn = (double)n;
-        const d3 q = sub(ld4(x, i), mk3(sums[12] / nn, sums[13] / nn, sums[14] / nn));
+        const d3 q = sub(ld4(x, i), mk3(sums[20], sums[21], sums[22]));  // the centre, sums[12..14] / n
         t[0] = dot(q, q);
     }
     obs_block_row<1>(t, part);
     obs_last_block_combine<1>((int)gridDim.x, part, 0, 18, out, ticket);
 }
 
-// Two kernels: the terms (with their sums, by the last block to finish), then |x - c|^2 about the
-// centre those sums give (out[18]). ticket: a zeroed device counter owned by the caller.
+// Two kernels: the terms (with their sums and the centre of mass, by the last block to finish), then
+// |x - c|^2 about that centre (out[18]). out holds at least 23 doubles; ticket: a zeroed device
+// counter owned by the caller.
 void launch_observables_state(int64_t n, const dbl4 *x, const dbl4 *v, const dbl4 *w, double mass, double inertia,
                               double *scratch, double *out, unsigned *ticket, cudaStream_t st) {
     const int nb = (int)((n + kObsBlock - 1) / kObsBlock);
@@ -342,21 +366,80 @@ __global__ void dev4_to_aos(int64_t n, const dbl4 *__restrict__ src, double *__r
 
 // The four state fields in one pass. in[f] / out[f]: [n][3] doubles in device memory or in pinned
 // host memory the GPU reads and writes directly (x, v, theta, omega; null: field not moved).
+// A block moves the 3 x kIoBlock consecutive doubles of its particles of every field through a
+// shared-memory tile, so that the accesses to the caller's buffers are consecutive 16-byte words
+// (io.wide) all issued before the first one is used: over the host link the transfer is bound by
+// the number of requests in flight, not by the per-particle work.
 // state_in also refreshes the mixed path's float-float copies (x32 non-null) from the new values,
-// and with `uncovered` flags a position further than four times its system's extent from its origin.
-__global__ void state_in(int64_t n, StateIO io, dbl4 *__restrict__ x, dbl4 *__restrict__ v, dbl4 *__restrict__ th,
-                         dbl4 *__restrict__ w, float4 *__restrict__ x32, float4 *__restrict__ v32,
-                         float4 *__restrict__ s32, double ox, double oy, double oz, double oext,
-                         const int32_t *__restrict__ agg, const dbl4 *__restrict__ orig, int32_t *uncovered) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// and with `uncovered` flags a position further than four times its system's extent from its origin
+// (a plain store of 1: the flag may live in mapped host memory, zeroed by the caller).
+constexpr int kIoBlock = 128;
+constexpr int kIoChunks = (3 * kIoBlock / 2 + kIoBlock - 1) / kIoBlock;  // 16-byte words per thread and field
+
+__device__ __forceinline__ void io_tile_load(const double *__restrict__ src, int64_t d0, int nd, bool wide,
+                                             double *__restrict__ tile) {
+    if (wide) {
+        const double2 *s2 = reinterpret_cast<const double2 *>(src + d0);
+        const int nw = nd / 2;
+        double2 r[kIoChunks];
+#pragma unroll
+        for (int u = 0; u < kIoChunks; ++u) {
+            const int c = (int)threadIdx.x + u * kIoBlock;
+            if (c < nw) r[u] = s2[c];
+        }
+#pragma unroll
+        for (int u = 0; u < kIoChunks; ++u) {
+            const int c = (int)threadIdx.x + u * kIoBlock;
+            if (c < nw) {
+                tile[2 * c] = r[u].x;
+                tile[2 * c + 1] = r[u].y;
+            }
+        }
+        if ((nd & 1) && threadIdx.x == 0) tile[nd - 1] = src[d0 + nd - 1];
+    } else {
+        for (int c = threadIdx.x; c < nd; c += kIoBlock) tile[c] = src[d0 + c];
+    }
+}
+
+__device__ __forceinline__ void io_tile_store(const double *__restrict__ tile, int64_t d0, int nd, bool wide,
+                                              double *__restrict__ dst) {
+    if (wide) {
+        double2 *d2 = reinterpret_cast<double2 *>(dst + d0);
+        const int nw = nd / 2;
+#pragma unroll
+        for (int u = 0; u < kIoChunks; ++u) {
+            const int c = (int)threadIdx.x + u * kIoBlock;
+            if (c < nw) d2[c] = make_double2(tile[2 * c], tile[2 * c + 1]);
+        }
+        if ((nd & 1) && threadIdx.x == 0) dst[d0 + nd - 1] = tile[nd - 1];
+    } else {
+        for (int c = threadIdx.x; c < nd; c += kIoBlock) dst[d0 + c] = tile[c];
+    }
+}
+
+__global__ void __launch_bounds__(kIoBlock) state_in(int64_t n, StateIO io, dbl4 *__restrict__ x, dbl4 *__restrict__ v,
+                                                     dbl4 *__restrict__ th, dbl4 *__restrict__ w,
+                                                     float4 *__restrict__ x32, float4 *__restrict__ v32,
+                                                     float4 *__restrict__ s32, double ox, double oy, double oz,
+                                                     double oext, const int32_t *__restrict__ agg,
+                                                     const dbl4 *__restrict__ orig, int32_t *uncovered) {
+    __shared__ double tile[4][3 * kIoBlock];
+    const int64_t p0 = (int64_t)blockIdx.x * kIoBlock;
+    const int cnt = (int)(n - p0 < kIoBlock ? n - p0 : kIoBlock);
+    const int64_t d0 = 3 * p0;
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+        if (io.in[f]) io_tile_load(io.in[f], d0, 3 * cnt, io.wide != 0, tile[f]);
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t >= cnt) return;
+    const int64_t i = p0 + t;
     dbl4 *dst[4] = {x, v, th, w};
     d3 val[4];
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
         if (io.in[f]) {
-            const double *p = io.in[f] + 3 * i;
-            val[f] = mk3(p[0], p[1], p[2]);
+            val[f] = mk3(tile[f][3 * t], tile[f][3 * t + 1], tile[f][3 * t + 2]);
             st4(dst[f], i, val[f]);
         } else {
             val[f] = ld4(dst[f], i);
@@ -375,37 +458,45 @@ __global__ void state_in(int64_t n, StateIO io, dbl4 *__restrict__ x, dbl4 *__re
         }
         const double lim = 4.0 * oext;
         const d3 q = val[0];
-        if (!(fabs(q.x - ox) <= lim && fabs(q.y - oy) <= lim && fabs(q.z - oz) <= lim)) atomicOr(uncovered, 1);
+        if (!(fabs(q.x - ox) <= lim && fabs(q.y - oy) <= lim && fabs(q.z - oz) <= lim)) *(volatile int32_t *)uncovered = 1;
     }
 }
 
-__global__ void state_out(int64_t n, StateIO io, const dbl4 *__restrict__ x, const dbl4 *__restrict__ v,
-                          const dbl4 *__restrict__ th, const dbl4 *__restrict__ w) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__global__ void __launch_bounds__(kIoBlock) state_out(int64_t n, StateIO io, const dbl4 *__restrict__ x,
+                                                      const dbl4 *__restrict__ v, const dbl4 *__restrict__ th,
+                                                      const dbl4 *__restrict__ w) {
+    __shared__ double tile[4][3 * kIoBlock];
+    const int64_t p0 = (int64_t)blockIdx.x * kIoBlock;
+    const int cnt = (int)(n - p0 < kIoBlock ? n - p0 : kIoBlock);
+    const int t = threadIdx.x;
     const dbl4 *src[4] = {x, v, th, w};
+    if (t < cnt) {
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+            if (io.out[f]) {
+                const d3 q = ld4(src[f], p0 + t);
+                tile[f][3 * t] = q.x;
+                tile[f][3 * t + 1] = q.y;
+                tile[f][3 * t + 2] = q.z;
+            }
+    }
+    __syncthreads();
 #pragma unroll
     for (int f = 0; f < 4; ++f)
-        if (io.out[f]) {
-            const d3 q = ld4(src[f], i);
-            double *p = io.out[f] + 3 * i;
-            p[0] = q.x;
-            p[1] = q.y;
-            p[2] = q.z;
-        }
+        if (io.out[f]) io_tile_store(tile[f], 3 * p0, 3 * cnt, io.wide != 0, io.out[f]);
 }
 
 void launch_state_in(int64_t n, const StateIO &io, dbl4 *x, dbl4 *v, dbl4 *th, dbl4 *w, float4 *x32, float4 *v32,
                      float4 *s32, const double *origin, const int32_t *agg, const dbl4 *orig, int32_t *uncovered,
                      cudaStream_t st) {
     if (n > 0)
-        state_in<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, io, x, v, th, w, x32, v32, s32, origin[0], origin[1],
-                                                             origin[2], origin[3], agg, orig, uncovered);
+        state_in<<<(unsigned)((n + kIoBlock - 1) / kIoBlock), kIoBlock, 0, st>>>(
+            n, io, x, v, th, w, x32, v32, s32, origin[0], origin[1], origin[2], origin[3], agg, orig, uncovered);
 }
 
 void launch_state_out(int64_t n, const StateIO &io, const dbl4 *x, const dbl4 *v, const dbl4 *th, const dbl4 *w,
                       cudaStream_t st) {
-    if (n > 0) state_out<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, io, x, v, th, w);
+    if (n > 0) state_out<<<(unsigned)((n + kIoBlock - 1) / kIoBlock), kIoBlock, 0, st>>>(n, io, x, v, th, w);
 }
 
 void launch_aos_to_dev4(int64_t n, const double *aos, dbl4 *dst, cudaStream_t st) {

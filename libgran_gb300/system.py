@@ -17,6 +17,8 @@ def _dp(a):
 def _vec(a, n):
     if a is None:
         return np.zeros((n, 3))
+    if type(a) is np.ndarray and a.dtype == np.float64 and a.shape == (n, 3) and a.flags.c_contiguous:
+        return a  # the common case, without conversions
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(n, 3))
 
 
@@ -91,17 +93,19 @@ class System:
         float64 arrays of `out` (e.g. views of pinned memory)."""
         if out is None:
             out = tuple(np.empty((self.n, 3)) for _ in range(4))
+        addrs = []
         for a in out:
-            if a.dtype != np.float64 or a.shape != (self.n, 3) or not a.flags["C_CONTIGUOUS"]:
+            if a.dtype != np.float64 or a.shape != (self.n, 3) or not a.flags.c_contiguous:
                 raise ValueError("state arrays must be C-contiguous (n, 3) float64")
-        A.check(A.lib().lg_get_state(self.h, *[_dp(a) for a in out]), "lg_get_state")
+            addrs.append(a.__array_interface__["data"][0])
+        A.check(A.lib().lg_get_state(self.h, *addrs), "lg_get_state")
         return out
 
     def set_state(self, x=None, v=None, theta=None, omega=None):
         """Upload any of (x, v, theta, omega) in one call (None leaves a field unchanged)."""
         arrs = [None if a is None else _vec(a, self.n) for a in (x, v, theta, omega)]
-        ptrs = [None if a is None else _dp(a) for a in arrs]
-        A.check(A.lib().lg_set_state(self.h, *ptrs), "lg_set_state")
+        addrs = [None if a is None else a.__array_interface__["data"][0] for a in arrs]
+        A.check(A.lib().lg_set_state(self.h, *addrs), "lg_set_state")  # arrs stay alive until it returns
 
     def set_threads_per_row(self, T):
         A.check(A.lib().lg_set_threads_per_row(self.h, int(T)), "lg_set_threads_per_row")
