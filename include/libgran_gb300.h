@@ -478,8 +478,11 @@ int lg_observables_noalloc(const double *x, const double *v, const double *omega
 /* Shape of the persistent step kernel (LG_FORCE_KERNEL_PERSISTENT, mixed precision; no
  * counterpart in the reference): min_blocks = register budget as resident blocks per SM (4, 5 or
  * 6; 0 = 4), slices = Hamaker items per 32-row group (1, 2 or 4; 0 = the size rule the compacted
- * kernels use, which gives their bits), assign = 0 (warps pull work items from a device counter)
- * or 1 (round robin). lg_autotune chooses a shape when it tries the persistent kernel. */
+ * kernels use, which gives their bits), assign = 0 (warps pull work items from a device counter),
+ * 1 (round robin) or 2 (contact and Hamaker items as two launches side by side, each compiled for its
+ * own items, each pulling from its own counter; the last of a group's items completes it, so no
+ * completion kernel follows). Every shape gives the same bits for the same slices. lg_autotune
+ * chooses a shape when it tries the persistent kernel. */
 int lg_set_step_shape(lg_system *sys, int32_t min_blocks, int32_t slices, int32_t assign);
 int lg_get_step_shape(lg_system *sys, int32_t *min_blocks, int32_t *slices, int32_t *assign);
 

@@ -443,8 +443,8 @@ static int ensure_step_buffers(lg_system *s) {
     const int64_t n = s->P.n;
     const int64_t groups = (n + 31) / 32;
     const int sl = mixed_hamaker_slices(n);
-    LG_TRY(s->alloc(&s->step_ctr, (size_t)(2 + groups)));
-    LG_CUDA(cudaMemset(s->step_ctr, 0, sizeof(unsigned) * (size_t)(2 + groups)));
+    LG_TRY(s->alloc(&s->step_ctr, (size_t)(6 + groups)));
+    LG_CUDA(cudaMemset(s->step_ctr, 0, sizeof(unsigned) * (size_t)(6 + groups)));
     LG_TRY(s->alloc(&s->hpart, 2 * (size_t)4 * (size_t)n));
     s->step_slices = sl;
     s->fstep = 0;
@@ -532,7 +532,7 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
         A.dt_lo = (float)(dt - (double)A.dt_hi);
         MixedExtra MX = s->mx;
         MX.x64 = prev_fused ? nullptr : s->x;  // FP64 positions are current unless the last step ran in float-float
-        kernels = launch_step_mixed(s->P, S, pv, s->bv, MX, A, s->stream);
+        kernels = launch_step_mixed(s->P, S, pv, s->bv, MX, A, s->stream, s->side, s->fork_ev, s->join_ev);
         s->fstep++;
         if (fuse_kick) {  // the next step reads the buffers this one wrote
             s->ffcur = nf;
@@ -1473,7 +1473,7 @@ extern "C" int lg_set_step_shape(lg_system *s, int32_t min_blocks, int32_t slice
         return lg_fail(LG_E_INVALID, "lg_set_step_shape: min_blocks must be 0, 4, 5 or 6");
     if (slices != 0 && slices != 1 && slices != 2 && slices != 4)
         return lg_fail(LG_E_INVALID, "lg_set_step_shape: slices must be 0, 1, 2 or 4");
-    if (assign != 0 && assign != 1) return lg_fail(LG_E_INVALID, "lg_set_step_shape: assign must be 0 or 1");
+    if (assign < 0 || assign > 2) return lg_fail(LG_E_INVALID, "lg_set_step_shape: assign must be 0, 1 or 2");
     LG_TRY(ensure_step_buffers(s));
     s->step_min_blocks = min_blocks ? min_blocks : 4;
     s->step_slices = slices ? slices : mixed_hamaker_slices(s->P.n);
@@ -2388,7 +2388,7 @@ extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t
     if (s->precision == LG_PRECISION_MIXED)
         for (int mb = 4; mb <= 6; ++mb)
             for (int sl = 1; sl <= 4; sl *= 2)
-                for (int asg = 0; asg <= 1; ++asg) add(LG_FORCE_KERNEL_PERSISTENT, 1, mb, sl, asg);
+                for (int asg = 0; asg <= 2; ++asg) add(LG_FORCE_KERNEL_PERSISTENT, 1, mb, sl, asg);
     double best = 1e300;
     lg_tuning pick = keep;
     for (auto &c : cands) {

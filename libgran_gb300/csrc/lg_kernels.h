@@ -136,18 +136,23 @@ int mixed_hamaker_slices(int64_t n);
 struct StepArgs {
     float4 *x32n, *v32n;  // the other buffers of the double-buffered float-float state (written)
     float4 *hpart;        // [slices][2n] Hamaker partial sums per slice
-    unsigned *ctr;        // [2 + groups]: item counters of alternate launches, then group arrivals
-    int par;              // item counter of this launch (0 / 1, alternating launch by launch)
+    unsigned *ctr;        // [6 + groups]: item counters (two pairs), then group arrivals (ctr + 6)
+    int par;              // item counter of this launch within its pair (0 / 1, alternating by step)
     int slices;           // Hamaker items per group
     int contacts, hamaker;  // which item kinds exist
     int last;             // the run's last step: write the FP64 state instead of the next step's
-    int assign;           // 0: warps pull items from ctr[par]; 1: warp g takes items g, g + W, ...
+    int assign;           // 0: warps pull items from a counter; 1: warp g takes items g, g + W, ...;
+                          // 2: two launches side by side (contact items on the side stream, Hamaker
+                          // items on the main stream), each pulling from its own counter
     int min_blocks;       // register budget: resident blocks per SM (4, 5 or 6)
     int64_t items;        // groups * (2 * contacts + slices * hamaker)
     float hdt_hi, hdt_lo, dt_hi, dt_lo;  // dt / 2 and dt as float-float values
 };
+// One step as one launch on st, or (A.assign == 2) as two launches on side and st joined through the
+// two events; returns the number of kernels launched.
 int launch_step_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV,
-                      const MixedExtra &MX, const StepArgs &A, cudaStream_t st);
+                      const MixedExtra &MX, const StepArgs &A, cudaStream_t st, cudaStream_t side = nullptr,
+                      cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 
 // Warp-compacted force kernels (lg_forces_compact.cu, compiled once per precision)
 // fast: LG_FORCE_KERNEL_FP64_FAST (reciprocals instead of repeated divisions; within 1e-12).

@@ -94,3 +94,44 @@ def test_persistent_falls_back_where_it_does_not_apply():
         s.step(mat.dt, 40, 20)
         outs.append([s.get(f) for f in FIELDS])
     _same(outs[1], outs[0])
+
+
+def _run_shape(desc, x0, v0, kernel, shape, schedule, sizes=None):
+    desc.force_kernel = kernel
+    s = System(desc, x0, v0, sizes=sizes)
+    s.set_step_shape(*shape)
+    for nst, rb in schedule:
+        s.step(K.Material().dt, nst, rb)
+    out = [s.get(f) for f in FIELDS]
+    assert s.device_errors() == 0
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("assign", [0, 1, 2])
+@pytest.mark.parametrize("mb,sl", [(4, 1), (4, 4), (5, 2), (6, 4)])
+def test_persistent_shapes_give_the_compact_bits(mb, sl, assign):
+    """Every shape (register budget, Hamaker slices, one launch pulling or round-robin, or the two
+    launches side by side) gives the bits of the compacted kernels with the same slices."""
+    mat = K.Material()
+    n = 6000
+    x0 = generate_aggregate(77, n, mat.r)
+    v0 = generate_velocities(77, n, 0.1) - 1e7 * (x0 - x0.mean(0))
+    d = K.make_desc(n, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, contact=mat.contact(), hamaker=mat.hamaker(),
+                    pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r, precision=A.LG_PRECISION_MIXED)
+    sched = [(40, 20), (13, 20)]
+    ref = _run_shape(d, x0, v0, A.LG_FORCE_KERNEL_COMPACT, (0, sl, 0), sched)
+    _same(_run_shape(d, x0, v0, A.LG_FORCE_KERNEL_PERSISTENT, (mb, sl, assign), sched), ref)
+
+
+def test_split_launches_in_a_batch_with_bonds():
+    """The two side-by-side launches on a batch of sintered aggregates of uneven sizes."""
+    mat = K.Material()
+    sizes = np.array([1500, 40, 333, 2048, 7])
+    x0, v0 = K.seeded_aggregates(sizes, 4, mat.r)
+    d = K.make_desc(int(sizes.sum()), A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(),
+                    sinter=mat.sinter(), hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r,
+                    precision=A.LG_PRECISION_MIXED)
+    sched = [(60, 20), (5, 20)]
+    ref = _run_shape(d, x0, v0, A.LG_FORCE_KERNEL_COMPACT, (0, 2, 0), sched, sizes=sizes)
+    _same(_run_shape(d, x0, v0, A.LG_FORCE_KERNEL_PERSISTENT, (4, 2, 2), sched, sizes=sizes), ref)
