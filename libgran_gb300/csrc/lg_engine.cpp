@@ -507,8 +507,9 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
         if (hr != 0) return lg_fail(LG_E_STATE, "unary hook returned %d", hr);
     }
     const bool persistent = s->kernel == LG_FORCE_KERNEL_PERSISTENT;
+    // (all pairs take the compacted kernels: their contact rows use a warp per row there)
     if (s->precision == LG_PRECISION_MIXED && persistent && s->step_ctr && (fuse_kick || prev_fused) &&
-        s->P.n_facets == 0 && !s->P.ext_a && !s->P.hold && s->s32) {
+        s->P.n_facets == 0 && !s->P.ext_a && !s->P.hold && s->s32 && s->P.pairs == LG_PAIRS_VERLET) {
         // one persistent launch: contacts, Hamaker and the float-float completion of this step
         const int64_t n = s->P.n;
         const PairView &pv = s->pv[s->pcur];

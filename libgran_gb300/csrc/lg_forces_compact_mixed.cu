@@ -211,10 +211,13 @@ __global__ void __launch_bounds__(64) forces_finish_ff(Params P, StateView S, in
 
 namespace {
 
+// Lanes per row of the contact kernel: kContactLanes for candidate lists (a few entries per row);
+// a whole warp per row for all pairs (n - 1 candidates per row: the lanes share them, and the row
+// count no longer bounds the warps a small system can use).
 template <bool NEAR>
 void launch_contacts(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, const MixedExtra &MX,
                      cudaStream_t st, bool beside_hamaker) {
-    constexpr int T = kContactLanes;
+    constexpr int T = NEAR ? kContactLanes : 32;
     const size_t smem = sizeof(ContactSmem) * kCWarps;
     const int64_t rows_per_block = (32 / T) * kCWarps;
     const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
@@ -256,6 +259,16 @@ int mixed_hamaker_slices(int64_t n) {
     return 1;
 }
 
+// All pairs: every row holds n - 1 partners, so small systems slice their rows further (up to 16
+// warps per 32-row group) under the same two-wave bound.
+static int mixed_hamaker_slices_all_pairs(int64_t n) {
+    const int64_t two_waves = 2 * 152 * 20;
+    const int64_t groups = (n + 31) / 32;
+    for (int sl = 16; sl > 1; sl /= 2)
+        if (groups * sl <= two_waves && (n - 1) >= 4 * kWin * sl) return sl;
+    return 1;
+}
+
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                 double dt, int move_facets, bool kick, bool prev_fused, const MixedExtra &MX,
                                 cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int slices) {
@@ -276,7 +289,11 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         ++kernels;
     }
     if (hamaker) {
-        switch (slices > 0 ? slices : mixed_hamaker_slices(P.n)) {
+        switch (slices > 0 ? slices : ver ? mixed_hamaker_slices(P.n) : mixed_hamaker_slices_all_pairs(P.n)) {
+            case 16:
+                if (ver) launch_hamaker<true, 16>(P, PV, MX, st);
+                else launch_hamaker<false, 16>(P, PV, MX, st);
+                break;
             case 8:
                 if (ver) launch_hamaker<true, 8>(P, PV, MX, st);
                 else launch_hamaker<false, 8>(P, PV, MX, st);

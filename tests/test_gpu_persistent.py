@@ -51,6 +51,7 @@ def test_persistent_matches_compact_verlet(n, bm, hm):
 
 
 def test_persistent_matches_compact_all_pairs():
+    """All pairs: the persistent kernel defers to the compacted kernels (a warp per contact row)."""
     mat = K.Material()
     n = 300
     x0 = generate_aggregate(5, n, mat.r)
