@@ -232,6 +232,8 @@ __global__ void __launch_bounds__(256) forces_fp64(Params P, StateView S, PairVi
 // and the closing half kick and, when another step follows, the next step's kick and drift.
 constexpr int kPairBlock = 32;
 constexpr int kFoldBlock = 32;
+constexpr int kFoldRows = 5;    // rows per warp of the fold (six lanes each)
+constexpr int kFoldAhead = 8;   // slots whose pair terms a lane of the fold loads at once
 
 template <bool VERLET>
 __global__ void __launch_bounds__(kPairBlock) forces_pairs_fp64(Params P, StateView S, PairView PV, BondView BV,
@@ -258,15 +260,35 @@ __global__ void __launch_bounds__(kFoldBlock) fold_pairs_fp64(Params P, StateVie
                                                               double dt, int move_facets, int kick) {
     const int64_t n = P.n;
     if (move_facets && blockIdx.x == 0 && threadIdx.x == 0) compact::move_facets(P, S, dt);
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int64_t len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
-    d3 acc = zero3(), accw = zero3();
-    for (int64_t k = 0; k < len; ++k) {
-        const int64_t e = k * n + i;
-        acc = add(acc, mk3(pres[e], pres[ps + e], pres[2 * ps + e]));
-        accw = add(accw, mk3(pres[3 * ps + e], pres[4 * ps + e], pres[5 * ps + e]));
+    // lane 6 r + c of a warp sums component c (force x, y, z, torque x, y, z) of the warp's row r:
+    // each component's terms in slot order, as one dependent chain per lane, so that a warp's FP64
+    // instructions each advance six chains of a row instead of one (FP64 issues slowly on this GPU).
+    // The loads of kFoldAhead slots are issued before their additions.
+    const int lane = threadIdx.x & 31;
+    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int r = lane / 6, c = lane % 6;
+    const int64_t i = wg * kFoldRows + r;
+    const bool mine = r < kFoldRows && i < n;
+    double sum = 0.0;
+    if (mine) {
+        const int64_t len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
+        const double *col = pres + (int64_t)c * ps + i;
+        int64_t k = 0;
+        for (; k + kFoldAhead <= len; k += kFoldAhead) {
+            double t[kFoldAhead];
+#pragma unroll
+            for (int u = 0; u < kFoldAhead; ++u) t[u] = col[(k + u) * n];
+#pragma unroll
+            for (int u = 0; u < kFoldAhead; ++u) sum += t[u];
+        }
+        for (; k < len; ++k) sum += col[k * n];
     }
+    double f[6];
+    const int src = r < kFoldRows ? 6 * r : 0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) f[q] = __shfl_sync(0xffffffffu, sum, src + q);
+    if (!mine || c != 0) return;
+    d3 acc = mk3(f[0], f[1], f[2]), accw = mk3(f[3], f[4], f[5]);
     const d3 vi = ld4(S.v, i), wi = ld4(S.w, i);
     compact::finish_row<FACETS>(P, S, i, n, acc, accw, vi, wi, hdt);
     if (kick) {  // the next step's opening half kick and drift, as kick_drift_fp64
@@ -841,7 +863,7 @@ int launch_forces_pairs_fp64(const Params &P, const StateView &S, const PairView
         else
             forces_pairs_fp64<false><<<(unsigned)blocks, kPairBlock, 0, st>>>(P, S, PV, BV, pres, ps, total);
     }
-    const unsigned fb = (unsigned)((n + kFoldBlock - 1) / kFoldBlock);
+    const unsigned fb = (unsigned)((n + kFoldRows - 1) / kFoldRows);  // one warp per kFoldRows rows
     const int kk = kick ? 1 : 0;
     const bool unary = P.n_facets > 0 || P.ext_a;
     if (verlet) {
