@@ -332,9 +332,12 @@ def c0_section(steps=10000):
     from libgran_gb300 import configs as K
     from libgran_gb300.system import System
     from oracle import oracle as O
+    from libgran_gb300.system import generate_aggregate, generate_velocities
     mat = K.Material()
     n = 256
-    x0, v0 = O.generate_aggregate(0, n, mat.r), O.generate_velocities(0, n, 0.1)
+    # the GPU runs take the library's generator; the oracle run takes the oracle's own, which gives
+    # the same bits
+    x0, v0 = generate_aggregate(0, n, mat.r), generate_velocities(0, n, 0.1)
     out = {"n_part": n, "vv_steps": steps}
     xs = {}
     for name, prec in (("fp64", A.LG_PRECISION_FP64), ("mixed", A.LG_PRECISION_MIXED)):
@@ -351,7 +354,7 @@ def c0_section(steps=10000):
     d = K.make_desc(n, A.LG_BINARY_SINTER, A.LG_HAMAKER_FULL, contact=mat.contact(), sinter=mat.sinter(),
                     hamaker=mat.hamaker())
     threads = os.cpu_count() or 1
-    o = O.OracleSystem(d, x0, v0, threads=threads)
+    o = O.OracleSystem(d, O.generate_aggregate(0, n, mat.r), O.generate_velocities(0, n, 0.1), threads=threads)
     t = time.perf_counter()
     o.step(mat.dt, steps)
     el = time.perf_counter() - t
@@ -744,7 +747,21 @@ def run_profile(args):
     from libgran_gb300 import _abi as A
     from libgran_gb300.system import System
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    prec = A.LG_PRECISION_MIXED if args.profile == "mixed" else A.LG_PRECISION_FP64
+    prec = A.LG_PRECISION_MIXED if args.profile in ("mixed", "c0-mixed") else A.LG_PRECISION_FP64
+    if args.profile.startswith("c0"):
+        # the 256-monomer all-pairs aggregate (sintered bonds + contact + full Hamaker), 100 steps a
+        # bench step, no list
+        from libgran_gb300 import configs as K
+        from libgran_gb300.system import generate_aggregate, generate_velocities
+        mat = K.Material()
+        x0, v0 = generate_aggregate(0, 256, mat.r), generate_velocities(0, 256, 0.1)
+        d = K.make_desc(256, A.LG_BINARY_SINTER, A.LG_HAMAKER_FULL, contact=mat.contact(), sinter=mat.sinter(),
+                        hamaker=mat.hamaker(), precision=prec)
+        s = System(d, x0, v0)
+        s.step(mat.dt, 100 * (args.warmup + args.steps))
+        print(json.dumps({"profile": args.profile, "vv_steps": 100 * (args.warmup + args.steps),
+                          "device_errors": s.device_errors(), "launches": s.launch_count()}))
+        return
     x0, v0 = workload_state()
     mat, d = workload_desc(prec)
     if args.kernel is not None:
@@ -760,8 +777,8 @@ def run_profile(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--profile", default=None, choices=[None, "mixed", "fp64"],
-                    help="profiling driver: run one path without timing")
+    ap.add_argument("--profile", default=None, choices=[None, "mixed", "fp64", "c0-fp64", "c0-mixed"],
+                    help="profiling driver: run one path without timing (c0-*: the 256-monomer all-pairs case)")
     ap.add_argument("--kernel", default=None, choices=[None, "compact", "persistent", "fp64fast"],
                     help="profiling driver: force kernel (compact / persistent: mixed; fp64fast: FP64)")
     ap.add_argument("--shape", default=None,

@@ -273,15 +273,14 @@ __global__ void __launch_bounds__(kFoldBlock) fold_pairs_fp64(Params P, StateVie
     if (mine) {
         const int64_t len = VERLET ? (int64_t)PV.row_len[i] : n - 1;
         const double *col = pres + (int64_t)c * ps + i;
-        int64_t k = 0;
-        for (; k + kFoldAhead <= len; k += kFoldAhead) {
+        for (int64_t k = 0; k < len; k += kFoldAhead) {
             double t[kFoldAhead];
 #pragma unroll
-            for (int u = 0; u < kFoldAhead; ++u) t[u] = col[(k + u) * n];
+            for (int u = 0; u < kFoldAhead; ++u) t[u] = k + u < len ? col[(k + u) * n] : 0.0;
 #pragma unroll
-            for (int u = 0; u < kFoldAhead; ++u) sum += t[u];
+            for (int u = 0; u < kFoldAhead; ++u)
+                if (k + u < len) sum += t[u];  // (adding a padding zero could turn -0 into +0)
         }
-        for (; k < len; ++k) sum += col[k * n];
     }
     double f[6];
     const int src = r < kFoldRows ? 6 * r : 0;
