@@ -762,6 +762,21 @@ def run_profile(args):
         print(json.dumps({"profile": args.profile, "vv_steps": 100 * (args.warmup + args.steps),
                           "device_errors": s.device_errors(), "launches": s.launch_count()}))
         return
+    if args.profile == "batched-mixed":
+        # the batched workload: 4096 aggregates (median 256 monomers), sintered bonds + limited
+        # Hamaker + contact, mixed precision, the compacted kernels
+        from libgran_gb300 import configs as K
+        mat = K.Material()
+        sizes = K.lognormal_sizes(4096, 256, 32, 2048, seed=2)
+        x0, v0 = K.seeded_aggregates(sizes, 2, mat.r)
+        d = K.make_desc(int(sizes.sum()), A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(),
+                        sinter=mat.sinter(), hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r,
+                        precision=A.LG_PRECISION_MIXED)
+        s = System(d, x0, v0, sizes=sizes)
+        s.step(mat.dt, VV_PER_STEP * (args.warmup + args.steps), VV_PER_STEP)
+        print(json.dumps({"profile": args.profile, "vv_steps": VV_PER_STEP * (args.warmup + args.steps),
+                          "device_errors": s.device_errors(), "launches": s.launch_count()}))
+        return
     x0, v0 = workload_state()
     mat, d = workload_desc(prec)
     if args.kernel is not None:
@@ -777,7 +792,7 @@ def run_profile(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--profile", default=None, choices=[None, "mixed", "fp64", "c0-fp64", "c0-mixed"],
+    ap.add_argument("--profile", default=None, choices=[None, "mixed", "fp64", "c0-fp64", "c0-mixed", "batched-mixed"],
                     help="profiling driver: run one path without timing (c0-*: the 256-monomer all-pairs case)")
     ap.add_argument("--kernel", default=None, choices=[None, "compact", "persistent", "fp64fast"],
                     help="profiling driver: force kernel (compact / persistent: mixed; fp64fast: FP64)")

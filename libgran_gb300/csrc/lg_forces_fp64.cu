@@ -534,6 +534,7 @@ __global__ void cell_scatter(int64_t n, const int32_t *__restrict__ cell_of, con
 constexpr int kBuildRows = 32;   // rows per block
 constexpr int kBuildWarps = 16;  // warps per block; warp w builds rows w, w + 16
 constexpr int kBuildBatches = 3; // candidate batches of 32 whose loads are in flight together
+constexpr uint32_t kNearBit = 0x80000000u;  // a listed partner within the contact-candidate radius
 
 // Shared-memory layout of build_rows for row capacity cap and bond capacity bcap: four 32-row
 // tiles (partner, flags, old slot, near partner) with an odd row stride, then per warp the unsorted
@@ -618,7 +619,7 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
         const int64_t x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < dim0 ? cx + 1 : dim0 - 1;
         // the 9 runs of cells (z, y fixed; x0..x1) are 9 contiguous ranges of the sorted list; lane
         // r < 9 looks up range r, and the ranges are walked as one virtual list of `total`
-        // candidates, 32 per iteration, with the next iteration's indices loaded ahead
+        // candidates, kBuildBatches x 32 per iteration
         int32_t rb = 0, rl = 0;
         if (lane < 9) {
             const int64_t z = cz - 1 + lane / 3, y = cy - 1 + lane % 3;
@@ -635,18 +636,28 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
             if (lane >= o) incl += v;
         }
         const int32_t total = __shfl_sync(0xffffffffu, incl, 8);
-        int32_t rbeg[9], rx[9];  // range begin in the sorted list, exclusive prefix (virtual begin)
+        // the non-empty ranges, compacted: lane c < m holds the c-th one's begin in the sorted list
+        // (rbc) and its first virtual index (exc), which increase strictly with c
+        const uint32_t nem = __ballot_sync(0xffffffffu, lane < 9 && rl > 0);
+        const int m = __popc(nem);
+        int src = 0;  // the range whose rank among the non-empty ones is this lane
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            rbeg[q] = __shfl_sync(0xffffffffu, rb, q);
-            rx[q] = __shfl_sync(0xffffffffu, incl - rl, q);
-        }
-        auto fetch = [&](int32_t t) -> int32_t {  // candidate at virtual index t (t < total)
-            int32_t q = 0;
-#pragma unroll
-            for (int r = 0; r < 9; ++r)
-                if (t >= rx[r]) q = rbeg[r] + (t - rx[r]);
-            return sorted[q];
+        for (int r = 0; r < 9; ++r)
+            if (((nem >> r) & 1u) && __popc(nem & ((1u << r) - 1u)) == lane) src = r;
+        const int32_t rbc = __shfl_sync(0xffffffffu, rb, src), exc = __shfl_sync(0xffffffffu, incl - rl, src);
+        const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+        // candidate of virtual index tb + lane (-1 past the end): the lane's range is the last one
+        // starting at or before its index; ranges starting inside the batch are found with one OR
+        // over the lanes that hold them
+        auto fetch_batch = [&](int32_t tb) -> int32_t {
+            const int32_t L = exc - tb;  // lane of the batch at which range `lane` starts
+            const uint32_t starts = __reduce_or_sync(0xffffffffu, (lane < m && L > 0 && L < 32) ? (1u << L) : 0u);
+            const int before = __popc(__ballot_sync(0xffffffffu, lane < m && L <= 0));
+            const int q = before - 1 + __popc(starts & upto);
+            const int qs = q < 0 ? 0 : q;
+            const int32_t rbq = __shfl_sync(0xffffffffu, rbc, qs), exq = __shfl_sync(0xffffffffu, exc, qs);
+            const int32_t t = tb + lane;
+            return t < total ? sorted[rbq + (t - exq)] : -1;
         };
         int32_t cnt = 0;
         for (int32_t t0 = 0; t0 < total; t0 += 32 * kBuildBatches) {
@@ -654,10 +665,7 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
             float4 fb[kBuildBatches];
             bool same[kBuildBatches];
 #pragma unroll
-            for (int u = 0; u < kBuildBatches; ++u) {
-                const int32_t t = t0 + 32 * u + lane;
-                jb[u] = t < total ? fetch(t) : -1;
-            }
+            for (int u = 0; u < kBuildBatches; ++u) jb[u] = fetch_batch(t0 + 32 * u);
 #pragma unroll
             for (int u = 0; u < kBuildBatches; ++u) {
                 fb[u] = fi;
@@ -670,19 +678,20 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
 #pragma unroll
             for (int u = 0; u < kBuildBatches; ++u) {
                 const int32_t j = jb[u];
-                bool in = false;
+                bool in = false, near_c = false;
                 if (j >= 0 && j != (int32_t)i && same[u]) {
                     const float ex = fi.x - fb[u].x, ey = fi.y - fb[u].y, ez = fi.z - fb[u].z;
                     const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                    near_c = d2f <= rn2;
                     if (d2f < rlo)
                         in = true;
                     else if (!(d2f > rhi))
                         in = sqn(sub(xi_, ld4(x, j))) < rv2;
                 }
                 const uint32_t bal = __ballot_sync(0xffffffffu, in);
-                if (in) {
+                if (in) {  // the partner, with its contact-candidate test in bit 31
                     const int32_t pos = cnt + __popc(bal & lt);
-                    if (pos < cap) wraw[pos] = j;
+                    if (pos < cap) wraw[pos] = (int32_t)((uint32_t)j | (near_c ? kNearBit : 0u));
                 }
                 cnt += __popc(bal);
             }
@@ -715,12 +724,15 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
             intact += ok ? 1 : 0;
         }
         __syncwarp();
-        // rank sort: the partners are distinct, so each one's rank is its slot
+        // rank sort: the partners are distinct, so each one's rank is its slot (compared without the
+        // candidate bit, which travels to tf until the slot's flags replace it)
         for (int32_t a = lane; a < cnt; a += 32) {
-            const int32_t v = wraw[a];
+            const uint32_t w = (uint32_t)wraw[a];
+            const int32_t v = (int32_t)(w & ~kNearBit);
             int32_t rank = 0;
-            for (int32_t t = 0; t < cnt; ++t) rank += wraw[t] < v ? 1 : 0;
+            for (int32_t t = 0; t < cnt; ++t) rank += (wraw[t] & (int32_t)~kNearBit) < v ? 1 : 0;
             tj[r * ts + rank] = v;
+            tf[r * ts + rank] = w & kNearBit;
         }
         __syncwarp();
         int32_t found = 0, nnear = 0;
@@ -728,6 +740,7 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
             const int32_t k = kb + lane;
             const bool slot_ok = k < cnt;
             const int32_t j = slot_ok ? tj[r * ts + k] : 0;
+            const bool near_c = slot_ok && tf[r * ts + k] != 0u;
             int32_t lo = 0, hi = olen;
             while (lo < hi) {
                 const int32_t mid = (lo + hi) >> 1;
@@ -751,9 +764,7 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
                     }
             bool is_near = false;
             if (near_lists && slot_ok) {
-                const float4 fj = x32[j];
-                const float ex = fi.x - fj.x, ey = fi.y - fj.y, ez = fi.z - fj.z;
-                is_near = (fl & kBonded) || fmaf(ez, ez, fmaf(ey, ey, ex * ex)) <= rn2;
+                is_near = (fl & kBonded) || near_c;
                 if (!is_near) {  // apart: its springs reset, so they are not carried
                     fl &= ~kXiLive;
                     po = -1;
