@@ -763,11 +763,11 @@ def run_profile(args):
                           "device_errors": s.device_errors(), "launches": s.launch_count()}))
         return
     if args.profile == "batched-mixed":
-        # the batched workload: 4096 aggregates (median 256 monomers), sintered bonds + limited
-        # Hamaker + contact, mixed precision, the compacted kernels
+        # the batched workload: 4096 aggregates (LG_BATCH_COUNT; median 256 monomers), sintered bonds
+        # + limited Hamaker + contact, mixed precision, the compacted kernels
         from libgran_gb300 import configs as K
         mat = K.Material()
-        sizes = K.lognormal_sizes(4096, 256, 32, 2048, seed=2)
+        sizes = K.lognormal_sizes(int(os.environ.get("LG_BATCH_COUNT", "4096")), 256, 32, 2048, seed=2)
         x0, v0 = K.seeded_aggregates(sizes, 2, mat.r)
         d = K.make_desc(int(sizes.sum()), A.LG_BINARY_SINTER, A.LG_HAMAKER_LIMITED, contact=mat.contact(),
                         sinter=mat.sinter(), hamaker=mat.hamaker(), pairs=A.LG_PAIRS_VERLET, r_verlet=4.5 * mat.r,
