@@ -180,22 +180,23 @@ void launch_role(const Params &P, const StateView &S, const PairView &PV, const 
 template <bool NEAR, bool VERLET, int MINB>
 int launch_step(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, const MixedExtra &MX,
                 const StepArgs &A, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
-    const int64_t groups = (P.n + 31) / 32;
-    if constexpr (NEAR && VERLET)
-    if (A.assign == 2 && A.contacts && A.hamaker && side) {
-        // contact items on the side stream beside the Hamaker items on st
-        StepArgs C = A, H = A;
-        C.items = groups * 2;
-        H.items = groups * A.slices;
-        cudaEventRecord(fork, st);
-        cudaStreamWaitEvent(side, fork, 0);
-        launch_role<NEAR, VERLET, MINB, 1>(P, S, PV, BV, MX, C, side);
-        // the Hamaker items need fewer registers: they always run with the smallest budget, which
-        // they fit without spills (80 registers, 6 resident blocks per SM)
-        launch_role<NEAR, VERLET, 6, 2>(P, S, PV, BV, MX, H, st);
-        cudaEventRecord(join, side);
-        cudaStreamWaitEvent(st, join, 0);
-        return 2;
+    if constexpr (NEAR && VERLET) {  // the two-launch form exists for Verlet rows with contact candidates
+        if (A.assign == 2 && A.contacts && A.hamaker && side) {
+            // contact items on the side stream beside the Hamaker items on st
+            const int64_t groups = (P.n + 31) / 32;
+            StepArgs C = A, H = A;
+            C.items = groups * 2;
+            H.items = groups * A.slices;
+            cudaEventRecord(fork, st);
+            cudaStreamWaitEvent(side, fork, 0);
+            launch_role<NEAR, VERLET, MINB, 1>(P, S, PV, BV, MX, C, side);
+            // the Hamaker items need fewer registers: they always run with the smallest budget, which
+            // they fit without spills (80 registers, 6 resident blocks per SM)
+            launch_role<NEAR, VERLET, 6, 2>(P, S, PV, BV, MX, H, st);
+            cudaEventRecord(join, side);
+            cudaStreamWaitEvent(st, join, 0);
+            return 2;
+        }
     }
     launch_role<NEAR, VERLET, MINB, 0>(P, S, PV, BV, MX, A, st);
     return 1;
