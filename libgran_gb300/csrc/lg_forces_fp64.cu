@@ -87,21 +87,19 @@ __device__ __forceinline__ double group_sum(double v) {
     return v;
 }
 
-// One slot of row i: the binary functor's pair value plus the Hamaker term, in that order (the
-// reference's container returns binary + hamaker for each pair, operator_overloads.h:16-20); pair
-// state (springs, bond state, flags) of slot e is read and written here and nowhere else.
-__device__ __forceinline__ void slot_pair_fp64(const Params &P, const StateView &S, const PairView &PV,
-                                               const BondView &BV, int64_t n, int64_t i, int64_t e, int64_t j,
-                                               const d3 xi_, const d3 vi, const d3 wi, d3 &pa_out, d3 &pal_out) {
-    const int bm = P.binary_model, hm = P.hamaker_model;
+// The binary functor's value for slot e of row i (P.binary_model != LG_BINARY_NONE); pair state
+// (springs, bond state, flags) of slot e is read and written here and nowhere else.
+__device__ __forceinline__ void slot_binary_fp64(const Params &P, const StateView &S, const PairView &PV,
+                                                 const BondView &BV, int64_t n, int64_t i, int64_t e, int64_t j,
+                                                 const d3 xi_, const d3 vi, const d3 wi, d3 &pa, d3 &pal) {
+    const int bm = P.binary_model;
     const bool breaking = bm == LG_BINARY_BREAKING_SINTER;
     const uint32_t fl = PV.flags[e];
     const d3 xj = ld4(S.x, j);
     const d3 dx = sub(xi_, xj);
-    d3 pa = zero3(), pal = zero3();
-    bool have = false;
-    if (bm != LG_BINARY_NONE) {
-        have = true;
+    pa = zero3();
+    pal = zero3();
+    {
         if ((fl & kBonded) && BV.cn) {  // 5-connector model
             const int64_t be = (int64_t)bond_slot_of(fl) * n + i;
             const d3 vj = ld4(S.v, j), wj = ld4(S.w, j);
@@ -160,12 +158,27 @@ __device__ __forceinline__ void slot_pair_fp64(const Params &P, const StateView 
             }
         }
     }
-    if (hm != LG_HAMAKER_NONE) {
-        d3 ha = zero3();
-        bool on = true;
-        if (hm == LG_HAMAKER_LIMITED) on = !(sqn(dx) > P.hamaker_skip_d2) && !(nrm(dx) > P.hamaker.r_cutoff);
-        if (on) ha = hamaker_accel(hm, P.hamaker, sub(xj, xi_));
-        if (have) {
+}
+
+// The Hamaker term of the pair (i, j) (P.hamaker_model != LG_HAMAKER_NONE).
+__device__ __forceinline__ d3 slot_hamaker_fp64(const Params &P, const StateView &S, int64_t j, const d3 xi_) {
+    const int hm = P.hamaker_model;
+    const d3 xj = ld4(S.x, j);
+    const d3 dx = sub(xi_, xj);
+    d3 ha = zero3();
+    bool on = true;
+    if (hm == LG_HAMAKER_LIMITED) on = !(sqn(dx) > P.hamaker_skip_d2) && !(nrm(dx) > P.hamaker.r_cutoff);
+    if (on) ha = hamaker_accel(hm, P.hamaker, sub(xj, xi_));
+    return ha;
+}
+
+// The pair value of a slot: binary + Hamaker as the reference's container adds them.
+__device__ __forceinline__ void combine_pair_fp64(bool have_binary, bool have_hamaker, const d3 &pb, const d3 &pbl,
+                                                  const d3 &ha, d3 &pa, d3 &pal) {
+    pa = pb;
+    pal = pbl;
+    if (have_hamaker) {
+        if (have_binary) {
             pa = add(pa, ha);
             pal = add(pal, zero3());
         } else {
@@ -173,8 +186,18 @@ __device__ __forceinline__ void slot_pair_fp64(const Params &P, const StateView 
             pal = zero3();
         }
     }
-    pa_out = pa;
-    pal_out = pal;
+}
+
+// One slot of row i: the binary functor's pair value plus the Hamaker term, in that order (the
+// reference's container returns binary + hamaker for each pair, operator_overloads.h:16-20).
+__device__ __forceinline__ void slot_pair_fp64(const Params &P, const StateView &S, const PairView &PV,
+                                               const BondView &BV, int64_t n, int64_t i, int64_t e, int64_t j,
+                                               const d3 xi_, const d3 vi, const d3 wi, d3 &pa_out, d3 &pal_out) {
+    const bool hb = P.binary_model != LG_BINARY_NONE, hh = P.hamaker_model != LG_HAMAKER_NONE;
+    d3 pb = zero3(), pbl = zero3(), ha = zero3();
+    if (hb) slot_binary_fp64(P, S, PV, BV, n, i, e, j, xi_, vi, wi, pb, pbl);
+    if (hh) ha = slot_hamaker_fp64(P, S, j, xi_);
+    combine_pair_fp64(hb, hh, pb, pbl, ha, pa_out, pal_out);
 }
 
 template <int T, bool VERLET>
@@ -246,6 +269,47 @@ __global__ void __launch_bounds__(kPairBlock) forces_pairs_fp64(Params P, StateV
     const int64_t j = VERLET ? (int64_t)PV.nbr[t] : (k < i ? k : k + 1);
     d3 pa, pal;
     slot_pair_fp64(P, S, PV, BV, n, i, t, j, ld4(S.x, i), ld4(S.v, i), ld4(S.w, i), pa, pal);
+    pres[t] = pa.x;
+    pres[ps + t] = pa.y;
+    pres[2 * ps + t] = pa.z;
+    pres[3 * ps + t] = pal.x;
+    pres[4 * ps + t] = pal.y;
+    pres[5 * ps + t] = pal.z;
+}
+
+// The same slots with the binary functor and the Hamaker term in two warps of one block (warp 0:
+// binary, warp 1: Hamaker, 32 slots each): each warp issues only its own part's FP64 instructions,
+// which halves the longest instruction sequence a small system waits for. Warp 1 then adds the two
+// parts exactly as slot_pair_fp64 does.
+template <bool VERLET>
+__global__ void __launch_bounds__(2 * kPairBlock) forces_pairs_split_fp64(Params P, StateView S, PairView PV,
+                                                                          BondView BV, double *__restrict__ pres,
+                                                                          int64_t ps, int64_t total) {
+    __shared__ double part[6][kPairBlock];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t t = blockIdx.x * (int64_t)kPairBlock + lane;
+    const int64_t n = P.n;
+    const int64_t k = t / n, i = t - k * n;  // slot t = k * n + i
+    const bool live = t < total && (!VERLET || k < (int64_t)PV.row_len[i]);
+    const int64_t j = !live ? 0 : VERLET ? (int64_t)PV.nbr[t] : (k < i ? k : k + 1);
+    d3 pb = zero3(), pbl = zero3();
+    if (warp == 0) {
+        if (live) slot_binary_fp64(P, S, PV, BV, n, i, t, j, ld4(S.x, i), ld4(S.v, i), ld4(S.w, i), pb, pbl);
+        part[0][lane] = pb.x;
+        part[1][lane] = pb.y;
+        part[2][lane] = pb.z;
+        part[3][lane] = pbl.x;
+        part[4][lane] = pbl.y;
+        part[5][lane] = pbl.z;
+    }
+    d3 ha = zero3();
+    if (warp == 1 && live) ha = slot_hamaker_fp64(P, S, j, ld4(S.x, i));
+    __syncthreads();
+    if (warp != 1 || !live) return;
+    pb = mk3(part[0][lane], part[1][lane], part[2][lane]);
+    pbl = mk3(part[3][lane], part[4][lane], part[5][lane]);
+    d3 pa, pal;
+    combine_pair_fp64(true, true, pb, pbl, ha, pa, pal);
     pres[t] = pa.x;
     pres[ps + t] = pa.y;
     pres[2 * ps + t] = pa.z;
@@ -868,7 +932,12 @@ int launch_forces_pairs_fp64(const Params &P, const StateView &S, const PairView
     const int64_t total = (verlet ? (int64_t)PV.cap : n - 1) * n;
     if (total > 0) {
         const int64_t blocks = (total + kPairBlock - 1) / kPairBlock;
-        if (verlet)
+        const bool split = P.binary_model != LG_BINARY_NONE && P.hamaker_model != LG_HAMAKER_NONE;
+        if (split && verlet)
+            forces_pairs_split_fp64<true><<<(unsigned)blocks, 2 * kPairBlock, 0, st>>>(P, S, PV, BV, pres, ps, total);
+        else if (split)
+            forces_pairs_split_fp64<false><<<(unsigned)blocks, 2 * kPairBlock, 0, st>>>(P, S, PV, BV, pres, ps, total);
+        else if (verlet)
             forces_pairs_fp64<true><<<(unsigned)blocks, kPairBlock, 0, st>>>(P, S, PV, BV, pres, ps, total);
         else
             forces_pairs_fp64<false><<<(unsigned)blocks, kPairBlock, 0, st>>>(P, S, PV, BV, pres, ps, total);
