@@ -788,15 +788,34 @@ __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
             intact += ok ? 1 : 0;
         }
         __syncwarp();
-        // rank sort: the partners are distinct, so each one's rank is its slot (compared without the
-        // candidate bit, which travels to tf until the slot's flags replace it)
-        for (int32_t a = lane; a < cnt; a += 32) {
-            const uint32_t w = (uint32_t)wraw[a];
-            const int32_t v = (int32_t)(w & ~kNearBit);
-            int32_t rank = 0;
-            for (int32_t t = 0; t < cnt; ++t) rank += (wraw[t] & (int32_t)~kNearBit) < v ? 1 : 0;
-            tj[r * ts + rank] = v;
-            tf[r * ts + rank] = w & kNearBit;
+        // order the row by partner (compared without the candidate bit, which travels to tf until
+        // the slot's flags replace it): up to 32 partners by a bitonic network across the lanes (15
+        // compare-exchange steps, padding sorts last), more by a rank sort (the partners are distinct,
+        // so each one's rank is its slot)
+        if (cnt <= 32) {
+            uint32_t w = lane < cnt ? (uint32_t)wraw[lane] : 0xffffffffu;
+#pragma unroll
+            for (int kk = 2; kk <= 32; kk <<= 1)
+#pragma unroll
+                for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                    const uint32_t o = __shfl_xor_sync(0xffffffffu, w, jj);
+                    const bool keep_min = ((lane & jj) == 0) == ((lane & kk) == 0);
+                    const bool w_less = (w & ~kNearBit) < (o & ~kNearBit);
+                    w = keep_min == w_less ? w : o;
+                }
+            if (lane < cnt) {
+                tj[r * ts + lane] = (int32_t)(w & ~kNearBit);
+                tf[r * ts + lane] = w & kNearBit;
+            }
+        } else {
+            for (int32_t a = lane; a < cnt; a += 32) {
+                const uint32_t w = (uint32_t)wraw[a];
+                const int32_t v = (int32_t)(w & ~kNearBit);
+                int32_t rank = 0;
+                for (int32_t t = 0; t < cnt; ++t) rank += (wraw[t] & (int32_t)~kNearBit) < v ? 1 : 0;
+                tj[r * ts + rank] = v;
+                tf[r * ts + rank] = w & kNearBit;
+            }
         }
         __syncwarp();
         int32_t found = 0, nnear = 0;

@@ -274,3 +274,48 @@ def test_state_calls_pinned_and_pageable_agree(precision):
     b.step(mat.dt, 25, 20)
     for f in STATE_FIELDS + (A.LG_FIELD_A, A.LG_FIELD_ALPHA):
         assert np.array_equal(a.get(f), b.get(f)), f
+
+
+@pytest.mark.parametrize("n", [1, 45, 129, 1001])
+def test_state_transfer_tails_and_alignment(n):
+    """lg_set_state / lg_get_state with particle counts that leave a partial block and an odd number
+    of doubles in the last tile, and with caller buffers that start 8 bytes past a 16-byte boundary
+    (the 8-byte path), pinned and pageable: the same numbers as the per-field calls."""
+    import torch
+    mat = K.Material()
+    x0 = generate_aggregate(5 + n, n, mat.r)
+    v0 = generate_velocities(5 + n, n, 0.1)
+    d = _desc(n, A.LG_BINARY_CONTACT, A.LG_HAMAKER_LIMITED, A.LG_PAIRS_VERLET, A.LG_PRECISION_MIXED, mat)
+    s = System(d, x0, v0)
+    s.step(mat.dt, 7, 20)
+    ref = [s.get(f) for f in STATE_FIELDS]
+    rng = np.random.default_rng(n)
+    new = [r + rng.normal(scale=1e-12, size=r.shape) for r in ref]
+
+    def buffers(kind, shift):
+        out = []
+        for _ in range(4):
+            if kind == "pinned":
+                flat = torch.empty(3 * n + 1, dtype=torch.float64).pin_memory().numpy()
+            else:
+                flat = np.empty(3 * n + 1)
+            base = flat.__array_interface__["data"][0]
+            off = (shift - base % 16) % 16 // 8  # doubles to skip so that the start is base + shift mod 16
+            out.append(flat[off:off + 3 * n].reshape(n, 3))
+        return out
+
+    for kind in ("pinned", "pageable"):
+        for shift in (0, 8):
+            bufs = buffers(kind, shift)
+            assert all(b.__array_interface__["data"][0] % 16 == shift for b in bufs)
+            s.get_state(out=tuple(bufs))
+            for b, r in zip(bufs, ref):
+                assert np.array_equal(b, r)
+            for b, v in zip(bufs, new):
+                b[...] = v
+            s.set_state(*bufs)
+            for f, v in zip(STATE_FIELDS, new):
+                assert np.array_equal(s.get(f), v)
+            for f, r in zip(STATE_FIELDS, ref):  # back to the reference state for the next round
+                s.set(f, r)
+    assert s.device_errors() == 0
