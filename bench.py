@@ -382,9 +382,11 @@ def tuning_desc(t):
     out = {"kernel": names.get(t["force_kernel"], str(t["force_kernel"])), "probe_ms_per_step": t["ms_per_step"]}
     if t["force_kernel"] == A.LG_FORCE_KERNEL_ROWGROUP:
         out["threads_per_row"] = t["threads_per_row"]
+    if t["force_kernel"] == A.LG_FORCE_KERNEL_COMPACT:
+        out["contact_lanes_per_row"] = t["threads_per_row"]
     if t["force_kernel"] == A.LG_FORCE_KERNEL_PERSISTENT:
         out.update(min_blocks_per_sm=t["step_min_blocks"], hamaker_slices=t["step_slices"],
-                   items="round robin" if t["step_assign"] else "pulled")
+                   items={0: "pulled", 1: "round robin", 2: "two launches side by side"}.get(t["step_assign"]))
     return out
 
 

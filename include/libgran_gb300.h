@@ -439,7 +439,7 @@ int lg_autotune(lg_system *sys, double dt, int64_t probe_steps, int64_t rebuild_
  * it (0 when not timed). */
 typedef struct {
     int32_t force_kernel;     /* LG_FORCE_KERNEL_* (resolved, never AUTO) */
-    int32_t threads_per_row;  /* row groups */
+    int32_t threads_per_row;  /* row groups: lanes per row; mixed compacted kernels: contact lanes per row (1 or 2) */
     int32_t step_min_blocks;  /* persistent step kernel: register budget (resident blocks per SM) */
     int32_t step_slices;      /* persistent step kernel: Hamaker items per 32-row group */
     int32_t step_assign;      /* persistent step kernel: 0 pulled items, 1 round robin */

@@ -543,7 +543,7 @@ static int launch_forces(lg_system *s, double hdt, double dt, int move_facets, b
         if (compact || persistent)
             kernels = launch_forces_compact_mixed(s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, fuse_kick,
                                                   prev_fused, s->mx, s->stream, s->side, s->fork_ev, s->join_ev,
-                                                  s->ham_slices);
+                                                  s->ham_slices, s->contact_lanes);
         else
             launch_forces_mixed(s->T, s->P, S, s->pv[s->pcur], s->bv, hdt, dt, move_facets, s->mx, s->stream);
     } else {
@@ -1216,7 +1216,8 @@ extern "C" int lg_destroy(lg_system *s) {
 // Run `period` steps as one CUDA graph (captured on first use for this pointer parity). The host
 // bookkeeping (buffer parities, step index) advances exactly as step_once advances it.
 static int run_period_graph(lg_system *s, double dt, int64_t period, int64_t rebuild_every) {
-    lg_system::GraphKey key{dt, period, s->kernel, s->T, s->vcur, s->pcur, s->fcur, s->ffcur, (int)(s->fstep & 1)};
+    lg_system::GraphKey key{dt,      period,  s->kernel, s->T, s->vcur, s->pcur, s->fcur, s->ffcur, (int)(s->fstep & 1),
+                            s->contact_lanes};
     for (auto &g : s->graphs) {
         if (!(g.key == key)) continue;
         LG_CUDA(cudaGraphLaunch(g.exec, s->stream));
@@ -2162,10 +2163,16 @@ static TuneKey tune_key(int precision, int pairs, int bm, int hm, int64_t n, int
     return std::make_tuple(precision, pairs, bm, hm, lg2, batch ? 1 : 0);
 }
 
+// threads_per_row of a record: row-group lanes, or for the mixed compacted kernels the contact
+// kernel's lanes per row
+static bool compact_mixed(const lg_system *s, int kernel) {
+    return kernel == LG_FORCE_KERNEL_COMPACT && s->precision == LG_PRECISION_MIXED;
+}
+
 static lg_tuning tuning_of(const lg_system *s) {
     lg_tuning t{};
     t.force_kernel = s->kernel;
-    t.threads_per_row = s->T;
+    t.threads_per_row = compact_mixed(s, s->kernel) ? s->contact_lanes : s->T;
     t.step_min_blocks = s->step_min_blocks;
     t.step_slices = s->step_slices ? s->step_slices : mixed_hamaker_slices(s->P.n);
     t.step_assign = s->step_assign;
@@ -2184,7 +2191,10 @@ static int apply_tuning(lg_system *s, const lg_tuning &t) {
     s->step_assign = t.step_assign;
     if (t.force_kernel == LG_FORCE_KERNEL_PAIRS && !s->pres) return lg_fail(LG_E_INVALID, "tuning: no pair-parallel scratch");
     s->kernel = t.force_kernel;
-    s->T = t.threads_per_row;
+    if (compact_mixed(s, t.force_kernel))
+        s->contact_lanes = t.threads_per_row == 1 ? 1 : 2;
+    else
+        s->T = t.threads_per_row;
     s->tuned_ms = t.ms_per_step;
     return LG_OK;
 }
@@ -2364,7 +2374,7 @@ extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t
         if (found && apply_tuning(s, hit) == LG_OK) {
             s->drop_graphs();
             if (kernel_out) *kernel_out = s->kernel;
-            if (T_out) *T_out = s->T;
+            if (T_out) *T_out = tuning_of(s).threads_per_row;
             return LG_OK;
         }
     }
@@ -2383,7 +2393,8 @@ extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t
         cands.push_back(t);
     };
     const int sl0 = mixed_hamaker_slices(s->P.n);
-    add(LG_FORCE_KERNEL_COMPACT, 1, 4, sl0, 0);
+    add(LG_FORCE_KERNEL_COMPACT, s->precision == LG_PRECISION_MIXED ? 2 : 1, 4, sl0, 0);
+    if (s->precision == LG_PRECISION_MIXED) add(LG_FORCE_KERNEL_COMPACT, 1, 4, sl0, 0);  // one contact lane per row
     if (s->pres) add(LG_FORCE_KERNEL_PAIRS, 1, 4, sl0, 0);
     for (int T = 1; T <= 32; T *= 2) add(LG_FORCE_KERNEL_ROWGROUP, T, 4, sl0, 0);
     if (s->precision == LG_PRECISION_MIXED)
@@ -2424,6 +2435,6 @@ extern "C" int lg_autotune(lg_system *s, double dt, int64_t probe_steps, int64_t
         g_tune_cache[key] = pick;
     }
     if (kernel_out) *kernel_out = s->kernel;
-    if (T_out) *T_out = s->T;
+    if (T_out) *T_out = tuning_of(s).threads_per_row;
     return LG_OK;
 }

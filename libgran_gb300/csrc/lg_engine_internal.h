@@ -58,6 +58,7 @@ struct lg_system {
     int step_slices = 0, step_min_blocks = 4, step_assign = 0;
     double tuned_ms = 0.0;         // the autotuner's time per step of the handle's current choice
     int ham_slices = 0;            // mixed: Hamaker slices of the two-stream kernels (0: size rule)
+    int contact_lanes = 2;         // mixed: lanes per row of the two-stream contact kernel (1 or 2)
     // serving arena (lg_arena_create): a batch whose systems are slots; lattice point of each slot
     bool arena = false;
     double arena_lattice = 0.0;
@@ -104,10 +105,10 @@ struct lg_system {
     struct GraphKey {
         double dt;
         int64_t period;
-        int kernel, T, vcur, pcur, fcur, ffcur, fpar;
+        int kernel, T, vcur, pcur, fcur, ffcur, fpar, lanes;
         bool operator==(const GraphKey &o) const {
             return dt == o.dt && period == o.period && kernel == o.kernel && T == o.T && vcur == o.vcur &&
-                   pcur == o.pcur && fcur == o.fcur && ffcur == o.ffcur && fpar == o.fpar;
+                   pcur == o.pcur && fcur == o.fcur && ffcur == o.ffcur && fpar == o.fpar && lanes == o.lanes;
         }
     };
     struct GraphEntry {

@@ -211,13 +211,12 @@ __global__ void __launch_bounds__(64) forces_finish_ff(Params P, StateView S, in
 
 namespace {
 
-// Lanes per row of the contact kernel: kContactLanes for candidate lists (a few entries per row);
-// a whole warp per row for all pairs (n - 1 candidates per row: the lanes share them, and the row
-// count no longer bounds the warps a small system can use).
-template <bool NEAR>
+// Lanes per row of the contact kernel: T = 2 (or 1, a tuning choice that suits large batches) for
+// candidate lists (a few entries per row); a whole warp per row for all pairs (n - 1 candidates per
+// row: the lanes share them, and the row count no longer bounds the warps a small system can use).
+template <bool NEAR, int T>
 void launch_contacts(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, const MixedExtra &MX,
                      cudaStream_t st, bool beside_hamaker) {
-    constexpr int T = NEAR ? kContactLanes : 32;
     const size_t smem = sizeof(ContactSmem) * kCWarps;
     const int64_t rows_per_block = (32 / T) * kCWarps;
     const unsigned blocks = (unsigned)((P.n + rows_per_block - 1) / rows_per_block);
@@ -271,7 +270,8 @@ static int mixed_hamaker_slices_all_pairs(int64_t n) {
 
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                 double dt, int move_facets, bool kick, bool prev_fused, const MixedExtra &MX,
-                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int slices) {
+                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int slices,
+                                int contact_lanes) {
     const bool ver = P.pairs == LG_PAIRS_VERLET;
     const int contacts = P.binary_model != LG_BINARY_NONE ? 1 : 0;
     const int hamaker = P.hamaker_model != LG_HAMAKER_NONE ? 1 : 0;
@@ -282,10 +282,12 @@ int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairV
         // the FP64 positions are current unless the step before integrated in float-float
         MixedExtra MC = MX;
         MC.x64 = prev_fused ? nullptr : S.x;
-        if (ver && PV.near_len)
-            launch_contacts<true>(P, S, PV, BV, MC, side, hamaker != 0);
+        if (ver && PV.near_len && contact_lanes == 1)
+            launch_contacts<true, 1>(P, S, PV, BV, MC, side, hamaker != 0);
+        else if (ver && PV.near_len)
+            launch_contacts<true, kContactLanes>(P, S, PV, BV, MC, side, hamaker != 0);
         else
-            launch_contacts<false>(P, S, PV, BV, MC, side, hamaker != 0);
+            launch_contacts<false, 32>(P, S, PV, BV, MC, side, hamaker != 0);
         ++kernels;
     }
     if (hamaker) {

@@ -165,10 +165,12 @@ void launch_forces_compact_fp64(const Params &P, const StateView &S, const PairV
 // float-float copies), exactly as launch_kick_drift_mixed would.
 // kick: another step follows (the completion also runs its opening half kick and drift);
 // prev_fused: the step before was such a step (its state may be float-float only).
-// slices: Hamaker slices per 32-row group (0: mixed_hamaker_slices(P.n)).
+// slices: Hamaker slices per 32-row group (0: mixed_hamaker_slices(P.n)); contact_lanes: lanes per
+// row of the contact kernel over candidate lists (1 or 2; all pairs take a warp per row).
 int launch_forces_compact_mixed(const Params &P, const StateView &S, const PairView &PV, const BondView &BV, double hdt,
                                 double dt, int move_facets, bool kick, bool prev_fused, const MixedExtra &MX,
-                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int slices = 0);
+                                cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int slices = 0,
+                                int contact_lanes = 2);
 
 // Layout conversion between a caller's [n][3] doubles (already in device memory) and the padded
 // device layout (lg_reduce.cu).

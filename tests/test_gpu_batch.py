@@ -190,3 +190,41 @@ def test_pair_parallel_kernel_limits():
                np.concatenate(vs), sizes=sizes)
     with pytest.raises(RuntimeError, match="FP64 only"):
         s.set_force_kernel(A.LG_FORCE_KERNEL_PAIRS)
+
+
+def test_one_contact_lane_per_row_from_a_tuning_record(tmp_path):
+    """The mixed compacted kernels with one contact lane per row (a tuning choice for large batches,
+    applied here from a cache record): eager and graph-replayed give the same bits, and the result
+    stays within the mixed path's tolerance of the default two lanes."""
+    L = A.lib()
+    sizes = [300] * 40
+    n = sum(sizes)
+    mat, xs, vs = _systems(sizes, seed0=17)
+    x0, v0 = np.concatenate(xs), np.concatenate(vs)
+    lg2 = int(np.floor(np.log2(n)))
+    f = tmp_path / "tune.txt"
+    f.write_text("%d %d %d %d %d 1 : %d 1 4 4 0 1.0\n" % (A.LG_PRECISION_MIXED, A.LG_PAIRS_VERLET, A.LG_BINARY_SINTER,
+                                                        A.LG_HAMAKER_LIMITED, lg2, A.LG_FORCE_KERNEL_COMPACT))
+    assert L.lg_autotune_cache_clear() == A.LG_OK
+    assert L.lg_autotune_cache_load(str(f).encode()) == A.LG_OK
+    try:
+        runs = []
+        for graphs in (True, False):
+            s = System(_desc(mat, n, A.LG_BINARY_SINTER, A.LG_PRECISION_MIXED, kernel=A.LG_FORCE_KERNEL_AUTO), x0, v0,
+                       sizes=sizes)
+            k, T = s.autotune(mat.dt, probe_steps=20, rebuild_every=20, use_cache=True)
+            assert k == A.LG_FORCE_KERNEL_COMPACT and T == 1 and s.tuning()["threads_per_row"] == 1
+            s.set_graphs(graphs)
+            s.step(mat.dt, 60, 20)
+            assert s.device_errors() == 0
+            runs.append([s.get(f_) for f_ in FIELDS])
+        for a, b in zip(*runs):
+            assert np.array_equal(a, b)
+        two = System(_desc(mat, n, A.LG_BINARY_SINTER, A.LG_PRECISION_MIXED, kernel=A.LG_FORCE_KERNEL_COMPACT), x0, v0,
+                     sizes=sizes)
+        assert two.tuning()["threads_per_row"] == 2
+        two.step(mat.dt, 60, 20)
+        x1, x2 = runs[0][0], two.get(A.LG_FIELD_X)
+        assert np.abs(x1 - x2).max() <= 1e-5 * np.abs(x2 - x0).max()
+    finally:
+        L.lg_autotune_cache_clear()
