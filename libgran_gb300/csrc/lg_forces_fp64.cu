@@ -617,11 +617,12 @@ __host__ __device__ inline size_t build_smem_bytes(int64_t cap, int64_t bcap) {
 // One warp per row: the 27 neighbour cells are 9 runs of consecutive cells (x fastest), i.e. 9
 // contiguous ranges of the cell-sorted particle list, walked as one list; the lanes take
 // kBuildBatches x 32 candidates at a time (all their index and position loads issued before the
-// first test, so that one round trip serves them all) and append the accepted ones (ballot + popc). The old row (partners and flags) and the row's bonds are requested before the candidate
-// loop, so their round trip overlaps it. The row is ordered by a rank sort (j is unique), so the
-// append order does not matter; the old row is searched by bisection for spring carry-over, and the
-// finished rows of the block are written slot-major so that the 32 rows' slot k go out as one
-// coalesced store.
+// first test, so that one round trip serves them all) and append the accepted ones (ballot +
+// popc), each with its contact-candidate test in bit 31. The old row (partners and flags) and the
+// row's bonds are requested before the candidate loop, so their round trip overlaps it. The row is
+// then ordered by partner (j is unique, so the append order does not matter), the old row is
+// searched by bisection for spring carry-over, and the finished rows of the block are written
+// slot-major so that the 32 rows' slot k go out as one coalesced store.
 __global__ void __launch_bounds__(kBuildRows * kBuildWarps, 2) build_rows(
     int64_t n, const dbl4 *__restrict__ x, BatchView B, const float4 *__restrict__ x32, const GridDev *__restrict__ g,
     const int32_t *__restrict__ cstart, const int32_t *__restrict__ ccount, const int32_t *__restrict__ sorted,
