@@ -426,12 +426,14 @@ int lg_snapshot(lg_system *sys);
 int lg_restore(lg_system *sys);
 
 /* Project autotuner (the reference's only tuning knob is the OpenMP thread count): times the
- * force-kernel variants and shapes -- compacted kernels; row groups of 1..32 lanes; FP64: the
- * pair-parallel kernel; mixed: the persistent step kernel in every shape of lg_set_step_shape
- * (register budget 4/5/6 blocks per SM x 1/2/4 Hamaker slices x pulled / round-robin items) -- for
- * probe_steps steps on the live system between a snapshot and its restore (the state afterwards is
- * the state before the call), graph-replayed, best of two timings each, and keeps the fastest. The
- * choice is cached per (precision, pair mode, functor set, log2 size, batch) when use_cache is 1. */
+ * force-kernel variants and shapes -- compacted kernels (mixed: with two or one contact lanes per
+ * row); row groups of 1..32 lanes; FP64: the pair-parallel kernel; mixed: the persistent step kernel
+ * in every shape of lg_set_step_shape (register budget 4/5/6 blocks per SM x 1/2/4 Hamaker slices x
+ * pulled / round-robin items / two launches side by side) -- for probe_steps steps on the live
+ * system between a snapshot and its restore (the state afterwards is the state before the call),
+ * graph-replayed, best of two timings each, and keeps the fastest. The choice is cached per
+ * (precision, pair mode, functor set, log2 size, batch) when use_cache is 1. *threads_per_row
+ * receives the pick's threads_per_row (lg_tuning). */
 int lg_autotune(lg_system *sys, double dt, int64_t probe_steps, int64_t rebuild_every, int32_t *force_kernel,
                 int32_t *threads_per_row, int32_t use_cache);
 

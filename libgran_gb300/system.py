@@ -187,6 +187,9 @@ class System:
         A.check(A.lib().lg_set_graphs(self.h, 1 if on else 0), "lg_set_graphs")
 
     def autotune(self, dt, probe_steps=20, rebuild_every=20, use_cache=True):
+        """Time the kernel variants and shapes on this system and keep the fastest; returns
+        (force kernel, threads_per_row of the pick: row-group lanes, or contact lanes per row for the
+        mixed compacted kernels)."""
         k, t = C.c_int32(), C.c_int32()
         A.check(A.lib().lg_autotune(self.h, float(dt), int(probe_steps), int(rebuild_every), C.byref(k), C.byref(t),
                                     1 if use_cache else 0), "lg_autotune")
